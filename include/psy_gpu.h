@@ -1,0 +1,284 @@
+/*
+ * psy_gpu.h -- C ABI of the GB300 tracing path for the Psychopath renderer.
+ *
+ * This library replaces two things in Psychopath's Rust renderer:
+ *
+ *   1. `Tracer::trace` (src/tracer.rs:34-37): trace a batch of rays against
+ *      the scene and return one surface intersection per ray.  Here:
+ *      psy_trace().
+ *   2. The body of `Renderer::render_job` for one bucket
+ *      (src/renderer.rs:239-310): per-sample camera rays, the light-path
+ *      state machine (LightPath::next, src/renderer.rs:449-691) and the XYZ
+ *      accumulation.  Here: psy_render_bucket() / psy_render_image().
+ *
+ * The Rust host keeps the .psy parser, the scene/assembly builders and the
+ * bucket scheduler.  It flattens its `Scene` into a PsySceneDesc (plain
+ * pointers and sizes, no Rust or torch types) and calls psy_scene_create()
+ * once; the library builds the same BVH4 trees the reference builds
+ * (src/accel/bvh_base.rs, src/accel/bvh4.rs), uploads everything to HBM and
+ * keeps it resident until psy_scene_destroy().
+ *
+ * Conventions:
+ *   - Every call returns PSY_OK (0) or a negative PSY_E_* code; no call
+ *     aborts the process.  psy_last_error() returns a short message for the
+ *     calling thread's last failure.
+ *   - Handles are opaque and owned by the caller (create/destroy pairs).
+ *   - Calls on different handles may run on different host threads; calls
+ *     on one handle must be serialised by the caller.
+ *   - `stream` arguments are cudaStream_t passed as void* (NULL = the
+ *     library's own stream for that handle).  Calls that take host buffers
+ *     synchronise with that stream before returning.
+ *   - Transforms are 3x4 row-major affine matrices [a b c d; e f g h;
+ *     i j k l] (the reference's Transform::new_from_values order); a point p
+ *     maps to (a*px + b*py + c*pz + d, ...).
+ */
+#ifndef PSY_GPU_H
+#define PSY_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- errors */
+#define PSY_OK 0
+#define PSY_E_INVALID (-1)     /* bad argument or malformed scene description */
+#define PSY_E_CUDA (-2)        /* a CUDA call failed (message in psy_last_error) */
+#define PSY_E_NOMEM (-3)       /* device or host allocation failed */
+#define PSY_E_UNSUPPORTED (-4) /* feature outside what this build implements */
+#define PSY_E_TIMEOUT (-5)     /* a bounded device wait ran out */
+#define PSY_E_BUSY (-6)        /* admission refused: over the memory budget */
+#define PSY_E_NOTFOUND (-7)    /* unknown request id */
+#define PSY_E_CANCELLED (-8)   /* request was cancelled */
+#define PSY_E_OVERFLOW (-9)    /* traversal stack overflow (scene deeper than supported) */
+
+/* ---------------------------------------------------------------- scene */
+
+/* Colour, as the reference's `Color` enum (src/color.rs:47-60).  XYZ values
+ * are already converted from the scene's RGB by the host
+ * (rec709_e_to_xyz, as parse_color does in src/parse/psy.rs:582-615). */
+#define PSY_COLOR_XYZ 0
+#define PSY_COLOR_BLACKBODY 1   /* v = (temperature K, factor, unused) */
+#define PSY_COLOR_TEMPERATURE 2 /* v = (temperature K, factor, unused) */
+typedef struct PsyColor {
+    uint32_t kind;
+    float v[3];
+} PsyColor;
+
+/* Surface shader, as `SimpleSurfaceShader` (src/shading/mod.rs:27-40). */
+#define PSY_SHADER_EMIT 0
+#define PSY_SHADER_LAMBERT 1
+#define PSY_SHADER_GGX 2
+typedef struct PsyShaderDesc {
+    uint32_t kind;
+    PsyColor color;
+    float roughness; /* GGX only */
+    float fresnel;   /* GGX only */
+} PsyShaderDesc;
+
+/* Objects of an assembly (src/scene/assembly.rs:398-402). */
+#define PSY_OBJ_MESH 0         /* TriangleMesh (src/surface/triangle_mesh.rs) */
+#define PSY_OBJ_RECT_LIGHT 1   /* RectangleLight (src/light/rectangle_light.rs) */
+#define PSY_OBJ_SPHERE_LIGHT 2 /* SphereLight (src/light/sphere_light.rs) */
+typedef struct PsyObjectDesc {
+    uint32_t kind;
+    uint32_t time_samples; /* motion keys: vertex keys (mesh) or light keys */
+    /* PSY_OBJ_MESH */
+    uint32_t num_verts;
+    uint32_t num_tris;
+    const float *verts;       /* [time_samples][num_verts][3] */
+    const float *normals;     /* [time_samples][num_verts][3] or NULL */
+    const uint32_t *indices;  /* [num_tris][3], as written in the scene */
+    /* PSY_OBJ_RECT_LIGHT: dims = [time_samples][2] (width, height)
+     * PSY_OBJ_SPHERE_LIGHT: dims = [time_samples] (radius) */
+    const float *dims;
+    const PsyColor *colors;   /* [time_samples] */
+} PsyObjectDesc;
+
+/* An instance in the root assembly (src/scene/assembly.rs:404-411).
+ * xform_count motion keys of world-to-object transforms start at
+ * xforms[xform_start]; xform_count == 0 means no transform. */
+typedef struct PsyInstanceDesc {
+    uint32_t object;
+    int32_t shader; /* index into shaders, or -1 (unassigned: magenta Emit) */
+    uint32_t xform_start;
+    uint32_t xform_count;
+} PsyInstanceDesc;
+
+typedef struct PsyTransform {
+    float m[12];
+} PsyTransform;
+
+/* Camera (src/camera.rs:12-72): camera-to-world transforms, field of view
+ * in radians, aperture radius and focus distance, each with its own keys. */
+typedef struct PsyCameraDesc {
+    uint32_t num_transforms;
+    const PsyTransform *transforms;
+    uint32_t num_fovs;
+    const float *fovs;
+    uint32_t num_aperture_radii; /* 0: pinhole */
+    const float *aperture_radii;
+    uint32_t num_focus_distances;
+    const float *focus_distances;
+} PsyCameraDesc;
+
+/* DistantDiskLight (src/light/distant_disk_light.rs:17-35): angular radius
+ * (radians), direction the light travels, colour; num_keys keys each. */
+typedef struct PsyDistantLightDesc {
+    uint32_t num_keys;
+    const float *radii;       /* [num_keys] */
+    const float *directions;  /* [num_keys][3] */
+    const PsyColor *colors;   /* [num_keys] */
+} PsyDistantLightDesc;
+
+typedef struct PsySceneDesc {
+    uint32_t num_objects;
+    const PsyObjectDesc *objects;
+    uint32_t num_shaders;
+    const PsyShaderDesc *shaders;
+    uint32_t num_instances;
+    const PsyInstanceDesc *instances;
+    uint32_t num_xforms;
+    const PsyTransform *xforms;
+    PsyCameraDesc camera;
+    PsyColor background; /* World background colour (src/scene/world.rs) */
+    uint32_t num_distant_lights;
+    const PsyDistantLightDesc *distant_lights;
+    /* RenderSettings (src/parse/psy.rs:260-351) */
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;
+    uint32_t seed;
+    /* Bounce limit of LightPath::next; the reference hard-codes 2
+     * (src/renderer.rs:599). */
+    uint32_t max_bounces;
+} PsySceneDesc;
+
+/* Options of a scene build. */
+#define PSY_BOUNDS_FP32 0 /* BVH4 child bounds as f32, bit-identical to the reference */
+#define PSY_BOUNDS_FP16 1 /* child bounds as f16 rounded outward (conservative) */
+typedef struct PsySceneOptions {
+    uint32_t bounds_precision; /* PSY_BOUNDS_* */
+    uint32_t reserved[7];
+} PsySceneOptions;
+
+typedef struct PsyScene PsyScene; /* opaque */
+
+/* Build a scene.  Replaces the reference's scene/accel construction:
+ * TriangleMesh::from_verts_and_indices (src/surface/triangle_mesh.rs:29-115),
+ * AssemblyBuilder::build (src/scene/assembly.rs:288-350) and
+ * Camera::new (src/camera.rs:22-72).  opts may be NULL (FP32 bounds). */
+int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts,
+                     PsyScene **out);
+/* Free everything psy_scene_create allocated. */
+int psy_scene_destroy(PsyScene *scene);
+/* Device bytes the scene holds resident (BVHs, geometry, lights). */
+int psy_scene_device_bytes(const PsyScene *scene, uint64_t *bytes);
+
+/* ---------------------------------------------------------------- trace */
+
+/* One ray of a batch; the fields of the reference's `Ray` (src/ray.rs:15-21)
+ * plus the occlusion flag of RayBatch::push (src/ray.rs:65-78). */
+#define PSY_RAY_OCCLUSION 1u
+typedef struct PsyRay {
+    float orig[3];
+    float dir[3];
+    float max_t;
+    float time;
+    float wavelength;
+    uint32_t flags; /* PSY_RAY_OCCLUSION */
+} PsyRay;
+
+/* Result for one ray: the discriminant and intersection data of the
+ * reference's `SurfaceIntersection` (src/surface/mod.rs:72-92). */
+#define PSY_HIT_MISS 0
+#define PSY_HIT_OCCLUDE 1
+#define PSY_HIT_SURFACE 2 /* triangle of a mesh */
+#define PSY_HIT_LIGHT 3   /* surface of a rectangle or sphere light (Emit closure) */
+typedef struct PsyHit {
+    uint32_t kind;
+    uint32_t prim; /* original triangle index in the mesh (rect light: 0/1) */
+    uint32_t inst; /* instance index in PsySceneDesc.instances */
+    float t;
+    float b0, b1, b2; /* barycentrics (triangles) */
+    float pad;
+} PsyHit;
+
+/* Full intersection data (SurfaceIntersectionData, src/surface/mod.rs:76-88)
+ * for callers that keep shading on the host. */
+typedef struct PsySurfaceHit {
+    PsyHit hit;
+    float pos[3];
+    float pos_err;
+    float nor[3];     /* shading normal */
+    float sample_pdf; /* lights only */
+    float nor_g[3];   /* geometric normal */
+    int32_t shader;   /* instance's shader index, -1 if none */
+} PsySurfaceHit;
+
+/* Trace n rays (host buffers) and write one PsyHit per ray.  Replaces
+ * Tracer::trace (src/tracer.rs:34-37).  Like the reference, a hit shrinks
+ * the ray's max_t; this call does not write the rays back.
+ * full_out may be NULL; when given, it receives PsySurfaceHit records. */
+int psy_trace(PsyScene *scene, const PsyRay *rays, uint32_t n, PsyHit *hits,
+              PsySurfaceHit *full_out, void *stream);
+
+/* Device-resident form: rays/hits are device pointers (PsyRay / PsyHit
+ * arrays).  Asynchronous on `stream`. */
+int psy_trace_device(PsyScene *scene, const PsyRay *d_rays, uint32_t n,
+                     PsyHit *d_hits, void *stream);
+
+/* Total rays traced through this scene handle (Tracer::rays_traced,
+ * src/tracer.rs:39-41). */
+int psy_rays_traced(const PsyScene *scene, uint64_t *count);
+
+/* ---------------------------------------------------------------- render */
+
+typedef struct PsyBucket {
+    uint32_t x, y, w, h; /* BucketJob (src/renderer.rs:739-745) */
+} PsyBucket;
+
+/* Stage timers of RenderStats (src/renderer.rs:40-73), in seconds of device
+ * time, plus counters. */
+typedef struct PsyRenderStats {
+    double trace_time;
+    double initial_ray_generation_time;
+    double ray_generation_time;
+    double sample_writing_time;
+    double total_time;
+    uint64_t ray_count;
+    uint64_t accel_node_visits;
+    uint64_t samples;
+} PsyRenderStats;
+
+/* Render one bucket: spp samples per pixel with the scene's seed.
+ * xyz_out (host) receives bucket.w*bucket.h*3 floats, row-major, the XYZ
+ * value each pixel would hold after the reference's accumulation
+ * (src/renderer.rs:299-310).  stats may be NULL. */
+int psy_render_bucket(PsyScene *scene, const PsyBucket *bucket, uint32_t spp,
+                      uint32_t seed, float *xyz_out, PsyRenderStats *stats);
+
+/* Render the whole image (or the crop x0,y0,x1,y1 inclusive when crop is not
+ * NULL) into d_xyz, a DEVICE buffer of width*height*3 floats.  Asynchronous
+ * on `stream`; stats (if not NULL) are filled after an internal sync. */
+int psy_render_image_device(PsyScene *scene, const uint32_t *crop,
+                            float *d_xyz, void *stream, PsyRenderStats *stats);
+
+/* Same, into a HOST buffer (synchronous). */
+int psy_render_image(PsyScene *scene, const uint32_t *crop, float *xyz_out,
+                     PsyRenderStats *stats);
+
+/* ---------------------------------------------------------------- misc */
+
+/* Short description of the calling thread's last error. */
+const char *psy_last_error(void);
+/* Library version string. */
+const char *psy_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PSY_GPU_H */

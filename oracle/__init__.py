@@ -1,0 +1,84 @@
+"""Oracle (test infrastructure only): a CPU restatement of Psychopath's
+tracing path, used by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline as the checker.  The product package never imports this."""
+import ctypes as C
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libpsy_oracle.so")
+SOURCES = ["psy_oracle.cpp", "oracle_sobol.cpp"]
+HEADERS = ["psy_oracle.h", "oracle_math.h", "oracle_shading.h"]
+
+
+def build(force=False):
+    """Compile the oracle with g++ (strict IEEE: no contraction, no fast-math)."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
+    deps = srcs + [os.path.join(HERE, h) for h in HEADERS] + [
+        os.path.join(HERE, "..", "include", "psy_gpu.h"),
+        os.path.join(HERE, "..", "psychopath_gb300", "csrc", "spectra_tables.inc")]
+    if not force and os.path.exists(LIB_PATH):
+        t = os.path.getmtime(LIB_PATH)
+        if all(os.path.getmtime(d) <= t for d in deps):
+            return LIB_PATH
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+           "-Wall", "-Wno-unused-function", "-o", LIB_PATH + ".tmp"] + srcs + ["-lpthread"]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB_PATH + ".tmp", LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        vp, u32, f32, fp, up = C.c_void_p, C.c_uint32, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_uint32)
+        L.psyo_scene_create.restype = vp
+        L.psyo_scene_create.argtypes = [vp]
+        L.psyo_scene_destroy.argtypes = [vp]
+        L.psyo_trace.argtypes = [vp, vp, u32, vp, vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), u32]
+        L.psyo_render.argtypes = [vp, u32, u32, vp, u32, vp, vp]
+        L.psyo_render_paths.argtypes = [vp, vp, vp, vp, vp]
+        L.psyo_hash_u32.restype = u32
+        L.psyo_hash_u32.argtypes = [u32, u32]
+        L.psyo_hash_u64.restype = C.c_uint64
+        L.psyo_hash_u64.argtypes = [C.c_uint64, C.c_uint64]
+        L.psyo_hash_u32_to_f32.restype = f32
+        L.psyo_hash_u32_to_f32.argtypes = [u32, u32]
+        L.psyo_get_sample_4d.argtypes = [u32, u32, u32, u32, u32, fp]
+        L.psyo_golden_ratio_sample.restype = f32
+        L.psyo_golden_ratio_sample.argtypes = [u32, u32]
+        L.psyo_probit.restype = f32
+        L.psyo_probit.argtypes = [f32, f32]
+        L.psyo_fast_exp.restype = f32
+        L.psyo_fast_exp.argtypes = [f32]
+        L.psyo_hilbert_d2xy.argtypes = [u32, up, up]
+        L.psyo_hilbert_xy2d.restype = u32
+        L.psyo_hilbert_xy2d.argtypes = [u32, u32]
+        L.psyo_traversal_table.argtypes = [vp]
+        for n in ("psyo_xf_mul",):
+            getattr(L, n).argtypes = [fp, fp, fp]
+        L.psyo_xf_inverse.argtypes = [fp, fp]
+        L.psyo_xf_lerp.argtypes = [fp, fp, f32, fp]
+        L.psyo_xf_point.argtypes = [fp, fp, fp]
+        L.psyo_xf_normal.argtypes = [fp, fp, fp]
+        L.psyo_lerp_slice.restype = f32
+        L.psyo_lerp_slice.argtypes = [fp, u32, f32]
+        L.psyo_xyz_to_spectrum.argtypes = [fp, f32, fp]
+        L.psyo_spectrum_to_xyz.argtypes = [fp, f32, fp]
+        L.psyo_rec709_e_to_xyz.argtypes = [fp, fp]
+        L.psyo_rec709_to_xyz.argtypes = [fp, fp]
+        L.psyo_intersect_triangle.restype = C.c_int
+        L.psyo_intersect_triangle.argtypes = [fp, fp, f32, fp, fp, fp, fp]
+        L.psyo_quick_select_ints.restype = u32
+        L.psyo_quick_select_ints.argtypes = [C.POINTER(C.c_int32), u32, u32]
+        L.psyo_increment_ulp_check.restype = C.c_int
+        L.psyo_mesh_bvh_info.argtypes = [vp, u32, vp, up]
+        _lib = L
+    return _lib

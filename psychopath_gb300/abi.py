@@ -1,0 +1,126 @@
+"""ctypes mirror of include/psy_gpu.h (the C ABI of the tracing path)."""
+import ctypes as C
+
+PSY_OK = 0
+PSY_E_INVALID = -1
+PSY_E_CUDA = -2
+PSY_E_NOMEM = -3
+PSY_E_UNSUPPORTED = -4
+PSY_E_TIMEOUT = -5
+PSY_E_BUSY = -6
+PSY_E_NOTFOUND = -7
+PSY_E_CANCELLED = -8
+PSY_E_OVERFLOW = -9
+
+PSY_COLOR_XYZ, PSY_COLOR_BLACKBODY, PSY_COLOR_TEMPERATURE = 0, 1, 2
+PSY_SHADER_EMIT, PSY_SHADER_LAMBERT, PSY_SHADER_GGX = 0, 1, 2
+PSY_OBJ_MESH, PSY_OBJ_RECT_LIGHT, PSY_OBJ_SPHERE_LIGHT = 0, 1, 2
+PSY_BOUNDS_FP32, PSY_BOUNDS_FP16 = 0, 1
+PSY_RAY_OCCLUSION = 1
+PSY_HIT_MISS, PSY_HIT_OCCLUDE, PSY_HIT_SURFACE, PSY_HIT_LIGHT = 0, 1, 2, 3
+
+_fp = C.POINTER(C.c_float)
+_up = C.POINTER(C.c_uint32)
+
+
+class PsyColor(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("v", C.c_float * 3)]
+
+
+class PsyShaderDesc(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("color", PsyColor), ("roughness", C.c_float), ("fresnel", C.c_float)]
+
+
+class PsyObjectDesc(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("time_samples", C.c_uint32), ("num_verts", C.c_uint32),
+                ("num_tris", C.c_uint32), ("verts", _fp), ("normals", _fp), ("indices", _up),
+                ("dims", _fp), ("colors", C.POINTER(PsyColor))]
+
+
+class PsyInstanceDesc(C.Structure):
+    _fields_ = [("object", C.c_uint32), ("shader", C.c_int32), ("xform_start", C.c_uint32),
+                ("xform_count", C.c_uint32)]
+
+
+class PsyTransform(C.Structure):
+    _fields_ = [("m", C.c_float * 12)]
+
+
+class PsyCameraDesc(C.Structure):
+    _fields_ = [("num_transforms", C.c_uint32), ("transforms", C.POINTER(PsyTransform)),
+                ("num_fovs", C.c_uint32), ("fovs", _fp),
+                ("num_aperture_radii", C.c_uint32), ("aperture_radii", _fp),
+                ("num_focus_distances", C.c_uint32), ("focus_distances", _fp)]
+
+
+class PsyDistantLightDesc(C.Structure):
+    _fields_ = [("num_keys", C.c_uint32), ("radii", _fp), ("directions", _fp),
+                ("colors", C.POINTER(PsyColor))]
+
+
+class PsySceneDesc(C.Structure):
+    _fields_ = [("num_objects", C.c_uint32), ("objects", C.POINTER(PsyObjectDesc)),
+                ("num_shaders", C.c_uint32), ("shaders", C.POINTER(PsyShaderDesc)),
+                ("num_instances", C.c_uint32), ("instances", C.POINTER(PsyInstanceDesc)),
+                ("num_xforms", C.c_uint32), ("xforms", C.POINTER(PsyTransform)),
+                ("camera", PsyCameraDesc), ("background", PsyColor),
+                ("num_distant_lights", C.c_uint32), ("distant_lights", C.POINTER(PsyDistantLightDesc)),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32),
+                ("seed", C.c_uint32), ("max_bounces", C.c_uint32)]
+
+
+class PsySceneOptions(C.Structure):
+    _fields_ = [("bounds_precision", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+
+
+class PsyRay(C.Structure):
+    _fields_ = [("orig", C.c_float * 3), ("dir", C.c_float * 3), ("max_t", C.c_float),
+                ("time", C.c_float), ("wavelength", C.c_float), ("flags", C.c_uint32)]
+
+
+class PsyHit(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("prim", C.c_uint32), ("inst", C.c_uint32), ("t", C.c_float),
+                ("b0", C.c_float), ("b1", C.c_float), ("b2", C.c_float), ("pad", C.c_float)]
+
+
+class PsySurfaceHit(C.Structure):
+    _fields_ = [("hit", PsyHit), ("pos", C.c_float * 3), ("pos_err", C.c_float), ("nor", C.c_float * 3),
+                ("sample_pdf", C.c_float), ("nor_g", C.c_float * 3), ("shader", C.c_int32)]
+
+
+class PsyBucket(C.Structure):
+    _fields_ = [("x", C.c_uint32), ("y", C.c_uint32), ("w", C.c_uint32), ("h", C.c_uint32)]
+
+
+class PsyRenderStats(C.Structure):
+    _fields_ = [("trace_time", C.c_double), ("initial_ray_generation_time", C.c_double),
+                ("ray_generation_time", C.c_double), ("sample_writing_time", C.c_double),
+                ("total_time", C.c_double), ("ray_count", C.c_uint64), ("accel_node_visits", C.c_uint64),
+                ("samples", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# numpy structured dtypes with the same layout (for bulk ray / hit buffers)
+def ray_dtype():
+    import numpy as np
+    return np.dtype([("orig", "<f4", 3), ("dir", "<f4", 3), ("max_t", "<f4"), ("time", "<f4"),
+                     ("wavelength", "<f4"), ("flags", "<u4")])
+
+
+def hit_dtype():
+    import numpy as np
+    return np.dtype([("kind", "<u4"), ("prim", "<u4"), ("inst", "<u4"), ("t", "<f4"), ("b0", "<f4"),
+                     ("b1", "<f4"), ("b2", "<f4"), ("pad", "<f4")])
+
+
+def surface_hit_dtype():
+    import numpy as np
+    return np.dtype([("hit", hit_dtype()), ("pos", "<f4", 3), ("pos_err", "<f4"), ("nor", "<f4", 3),
+                     ("sample_pdf", "<f4"), ("nor_g", "<f4", 3), ("shader", "<i4")])
+
+
+assert C.sizeof(PsyRay) == 40
+assert C.sizeof(PsyHit) == 32
+assert C.sizeof(PsySurfaceHit) == 80
