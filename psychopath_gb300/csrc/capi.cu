@@ -1,0 +1,454 @@
+// C ABI of the GB300 tracing path (include/psy_gpu.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "scene_build.h"
+
+void psy_set_magenta(const float xyz[3]);
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+int cuda_fail(cudaError_t e, const char *what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? PSY_E_NOMEM : PSY_E_CUDA;
+}
+#define CK(call, what)                                \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+std::once_flag g_const_once;
+int g_device_init = 0;
+
+}  // namespace
+
+struct PsyScene {
+    GScene g{};
+    std::vector<void *> allocs;
+    uint64_t device_bytes = 0;
+    cudaStream_t stream = nullptr;
+    int *d_err = nullptr;
+    uint64_t rays_traced = 0;
+    int stack = 64;
+    // per-scene facts kept for debugging / tree checks
+    std::vector<std::vector<uint32_t>> mesh_tri_order;
+    std::vector<uint32_t> mesh_node_count;
+    std::vector<int32_t> object_to_mesh;
+    uint32_t max_stack = 0;
+    uint32_t node_count = 0;
+    // trace scratch (host-buffer calls)
+    PsyRay *d_rays = nullptr;
+    PsyHit *d_hits = nullptr;
+    PsySurfaceHit *d_full = nullptr;
+    size_t cap_rays = 0;
+    // render scratch
+    uint32_t cap_paths = 0;
+    PathState P{};
+    RayBuf R{};
+    HitBuf H{};
+    uint32_t *queue[2] = {nullptr, nullptr};
+    uint32_t *counts = nullptr;          // [2]
+    unsigned long long *d_raycount = nullptr;
+    float *d_xyz = nullptr;
+    size_t cap_xyz = 0;
+    uint32_t wave_paths = 1u << 24;      // paths per wave
+    int grid = 0;                        // persistent grid for queue kernels (0: size by queue)
+    std::mutex mu;
+};
+
+template <class T>
+static int upload(PsyScene *s, const std::vector<T> &v, const T **out) {
+    size_t bytes = std::max<size_t>(v.size() * sizeof(T), 16);
+    void *p = nullptr;
+    CK(cudaMalloc(&p, bytes), "cudaMalloc scene");
+    s->allocs.push_back(p);
+    s->device_bytes += bytes;
+    if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s->stream), "upload");
+    *out = reinterpret_cast<const T *>(p);
+    return PSY_OK;
+}
+
+static void free_render(PsyScene *s) {
+    void *ptrs[] = {s->P.color, s->P.latt, s->P.pending, s->P.nafac, s->P.nb_o, s->P.nb_d, s->P.tw, s->P.seed, s->P.flags,
+                    s->R.o, s->R.d, s->R.occl, s->H.ki, s->H.tb, s->queue[0], s->queue[1], s->counts, s->d_raycount};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    s->P = PathState{};
+    s->R = RayBuf{};
+    s->H = HitBuf{};
+    s->queue[0] = s->queue[1] = nullptr;
+    s->counts = nullptr;
+    s->d_raycount = nullptr;
+    s->cap_paths = 0;
+}
+
+static int ensure_render(PsyScene *s, uint32_t n) {
+    if (n <= s->cap_paths) return PSY_OK;
+    free_render(s);
+    size_t N = n;
+#define AL(ptr, bytes) CK(cudaMalloc((void **)&(ptr), (bytes)), "cudaMalloc render state")
+    AL(s->P.color, N * 16); AL(s->P.latt, N * 16); AL(s->P.pending, N * 16); AL(s->P.nafac, N * 16);
+    AL(s->P.nb_o, N * 16); AL(s->P.nb_d, N * 16); AL(s->P.tw, N * 8); AL(s->P.seed, N * 4); AL(s->P.flags, N * 4);
+    AL(s->R.o, N * 16); AL(s->R.d, N * 16); AL(s->R.occl, N);
+    AL(s->H.ki, N * 16); AL(s->H.tb, N * 16);
+    AL(s->queue[0], N * 4); AL(s->queue[1], N * 4);
+    AL(s->counts, 16);
+    AL(s->d_raycount, 8);
+#undef AL
+    s->cap_paths = n;
+    return PSY_OK;
+}
+
+static int ensure_trace(PsyScene *s, size_t n, bool full) {
+    if (n <= s->cap_rays && (!full || s->d_full)) return PSY_OK;
+    if (s->d_rays) cudaFree(s->d_rays);
+    if (s->d_hits) cudaFree(s->d_hits);
+    if (s->d_full) cudaFree(s->d_full);
+    s->d_rays = nullptr; s->d_hits = nullptr; s->d_full = nullptr;
+    size_t cap = std::max(n, s->cap_rays);
+    CK(cudaMalloc((void **)&s->d_rays, cap * sizeof(PsyRay)), "cudaMalloc rays");
+    CK(cudaMalloc((void **)&s->d_hits, cap * sizeof(PsyHit)), "cudaMalloc hits");
+    if (full) CK(cudaMalloc((void **)&s->d_full, cap * sizeof(PsySurfaceHit)), "cudaMalloc full hits");
+    s->cap_rays = cap;
+    return PSY_OK;
+}
+
+static int check_err(PsyScene *s) {
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "read error word");
+    CK(cudaStreamSynchronize(s->stream), "stream sync");
+    if (h != 0) {
+        int z = 0;
+        cudaMemcpy(s->d_err, &z, sizeof(int), cudaMemcpyHostToDevice);
+        return fail(h, "device reported error (traversal stack overflow)");
+    }
+    return PSY_OK;
+}
+
+extern "C" {
+
+const char *psy_last_error(void) { return g_last_error.c_str(); }
+const char *psy_version(void) { return "psychopath_gb300 0.1 (sm_103a)"; }
+
+int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyScene **out) {
+    if (!out) return fail(PSY_E_INVALID, "out is null");
+    *out = nullptr;
+    HostScene hs;
+    std::string err;
+    int rc = build_host_scene(desc, opts, hs, err);
+    if (rc != PSY_OK) return fail(rc, err);
+    int ndev = 0;
+    cudaError_t ce = cudaGetDeviceCount(&ndev);
+    if (ce != cudaSuccess || ndev == 0) return fail(PSY_E_CUDA, "no CUDA device available");
+    std::call_once(g_const_once, []() {
+        psy_upload_constants();
+        float m[3];
+        unassigned_magenta_xyz(m);
+        psy_set_magenta(m);
+        g_device_init = 1;
+    });
+    PsyScene *s = new PsyScene();
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete s;
+        return fail(PSY_E_CUDA, "cudaStreamCreate failed");
+    }
+    GScene &g = s->g;
+    int r = PSY_OK;
+#define UP(field, vec) if (r == PSY_OK) r = upload(s, hs.vec, &g.field)
+    UP(nodes, nodes); UP(bounds_ext, bounds_ext);
+    if (!hs.nodes_h.empty()) { UP(nodes_h, nodes_h); }
+    UP(tri_idx, tri_idx); UP(tris, tris); UP(verts, verts); UP(normals, normals); UP(meshes, meshes);
+    UP(instances, instances); UP(xforms, xforms); UP(xforms_inv, xforms_inv); UP(shaders, shaders);
+    UP(lights, lights); UP(light_dims, light_dims); UP(light_colors, light_colors);
+    UP(lt_nodes, lt_nodes); UP(lt_bounds, lt_bounds); UP(light_instances, light_instances);
+    UP(distant, distant); UP(distant_radii, distant_radii); UP(distant_dirs, distant_dirs);
+    UP(distant_colors, distant_colors); UP(cam_xf, cam_xf); UP(cam_tfov, cam_tfov); UP(cam_ap, cam_ap);
+    UP(cam_fd, cam_fd);
+#undef UP
+    if (r == PSY_OK) {
+        cudaError_t e = cudaMalloc((void **)&s->d_err, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) r = cuda_fail(e, "scene upload");
+    }
+    if (r != PSY_OK) {
+        psy_scene_destroy(s);
+        return r;
+    }
+    g.top_root = hs.top_root;
+    g.n_instances = (uint32_t)hs.instances.size();
+    g.n_light_instances = (uint32_t)hs.light_instances.size();
+    g.n_distant = desc->num_distant_lights;
+    g.lt_empty = hs.lt_empty ? 1u : 0u;
+    g.n_cam_xf = (uint32_t)hs.cam_xf.size() / 3;
+    g.n_cam_tfov = (uint32_t)hs.cam_tfov.size();
+    g.n_cam_ap = (uint32_t)hs.cam_ap.size();
+    g.n_cam_fd = (uint32_t)hs.cam_fd.size();
+    g.background = hs.background;
+    g.width = hs.width; g.height = hs.height; g.spp = hs.spp; g.seed = hs.seed; g.max_bounces = hs.max_bounces;
+    g.use_fp16 = hs.nodes_h.empty() ? 0u : 1u;
+    g.distant_energy_total = hs.distant_energy_total;
+    g.lt_root_energy = hs.lt_root_energy;
+    s->max_stack = hs.max_stack;
+    s->stack = hs.max_stack <= 32 ? 32 : (hs.max_stack <= 64 ? 64 : 192);
+    if (hs.max_stack > 192) {
+        psy_scene_destroy(s);
+        return fail(PSY_E_OVERFLOW, "scene needs a traversal stack deeper than 192 entries");
+    }
+    s->mesh_tri_order = std::move(hs.mesh_tri_order);
+    s->mesh_node_count = std::move(hs.mesh_node_count);
+    s->object_to_mesh = std::move(hs.object_to_mesh);
+    s->node_count = (uint32_t)hs.nodes.size();
+    if (const char *wp = std::getenv("PSY_WAVE_PATHS")) {
+        long v = std::atol(wp);
+        if (v > 1024) s->wave_paths = (uint32_t)v;
+    }
+    *out = s;
+    return PSY_OK;
+}
+
+int psy_scene_destroy(PsyScene *s) {
+    if (!s) return PSY_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (void *p : s->allocs) cudaFree(p);
+    free_render(s);
+    if (s->d_rays) cudaFree(s->d_rays);
+    if (s->d_hits) cudaFree(s->d_hits);
+    if (s->d_full) cudaFree(s->d_full);
+    if (s->d_xyz) cudaFree(s->d_xyz);
+    if (s->d_err) cudaFree(s->d_err);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return PSY_OK;
+}
+
+int psy_scene_device_bytes(const PsyScene *s, uint64_t *bytes) {
+    if (!s || !bytes) return fail(PSY_E_INVALID, "null argument");
+    *bytes = s->device_bytes;
+    return PSY_OK;
+}
+
+int psy_trace_device(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyHit *d_hits, void *stream) {
+    if (!s || (n && (!d_rays || !d_hits))) return fail(PSY_E_INVALID, "null argument");
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    cudaError_t e = launch_trace_rays(s->g, d_rays, n, d_hits, nullptr, s->stack, 128, s->d_err, st);
+    if (e != cudaSuccess) return cuda_fail(e, "trace launch");
+    s->rays_traced += n;
+    return PSY_OK;
+}
+
+int psy_trace(PsyScene *s, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurfaceHit *full_out, void *stream) {
+    if (!s || (n && (!rays || !hits))) return fail(PSY_E_INVALID, "null argument");
+    if (n == 0) return PSY_OK;
+    std::lock_guard<std::mutex> lk(s->mu);
+    int r = ensure_trace(s, n, full_out != nullptr);
+    if (r != PSY_OK) return r;
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    CK(cudaMemcpyAsync(s->d_rays, rays, (size_t)n * sizeof(PsyRay), cudaMemcpyHostToDevice, st), "copy rays");
+    CK(launch_trace_rays(s->g, s->d_rays, n, s->d_hits, full_out ? s->d_full : nullptr, s->stack, 128, s->d_err, st),
+       "trace launch");
+    CK(cudaMemcpyAsync(hits, s->d_hits, (size_t)n * sizeof(PsyHit), cudaMemcpyDeviceToHost, st), "copy hits");
+    if (full_out)
+        CK(cudaMemcpyAsync(full_out, s->d_full, (size_t)n * sizeof(PsySurfaceHit), cudaMemcpyDeviceToHost, st),
+           "copy full hits");
+    CK(cudaStreamSynchronize(st), "trace sync");
+    s->rays_traced += n;
+    return check_err(s);
+}
+
+int psy_rays_traced(const PsyScene *s, uint64_t *count) {
+    if (!s || !count) return fail(PSY_E_INVALID, "null argument");
+    *count = s->rays_traced;
+    return PSY_OK;
+}
+
+}  // extern "C"
+
+// Render the pixels of region (x0, y0, w, h) into d_xyz (image-sized, row
+// stride img_w) as a sequence of waves of whole pixel rows.
+static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h, uint32_t spp, uint32_t seed,
+                         float *d_xyz, uint32_t img_w, cudaStream_t st, PsyRenderStats *stats) {
+    if (spp == 0 || w == 0 || h == 0) return PSY_OK;
+    uint64_t row_paths = (uint64_t)w * spp;
+    uint32_t rows = (uint32_t)std::max<uint64_t>(1, s->wave_paths / row_paths);
+    rows = std::min(rows, h);
+    uint64_t max_paths = (uint64_t)rows * row_paths;
+    if (max_paths > 0xFFFFFFFFull) return fail(PSY_E_UNSUPPORTED, "wave too large");
+    int r = ensure_render(s, (uint32_t)max_paths);
+    if (r != PSY_OK) return r;
+    uint32_t iters = 2 * s->g.max_bounces + 3;
+    cudaEvent_t ev[4];
+    bool timing = stats != nullptr;
+    if (timing) {
+        for (auto &e : ev) cudaEventCreate(&e);
+        CK(cudaMemsetAsync(s->d_raycount, 0, 8, st), "memset");
+    }
+    double t_gen = 0, t_loop = 0, t_acc = 0;
+    auto t0 = std::chrono::steady_clock::now();
+    for (uint32_t y = y0; y < y0 + h; y += rows) {
+        Wave wv;
+        wv.x0 = x0; wv.y0 = y; wv.w = w; wv.h = std::min(rows, y0 + h - y);
+        wv.spp = spp; wv.seed = seed;
+        uint32_t n = wv.w * wv.h * spp;
+        if (timing) cudaEventRecord(ev[0], st);
+        CK(launch_camera(s->g, wv, s->P, s->R, s->queue[0], s->counts, st), "camera launch");
+        if (timing) cudaEventRecord(ev[1], st);
+        int cur = 0;
+        for (uint32_t it = 0; it < iters; it++) {
+            CK(launch_trace_queue(s->g, s->R, s->H, s->queue[cur], s->counts + cur, n, s->stack, 128, s->grid, s->d_err, st),
+               "trace launch");
+            CK(cudaMemsetAsync(s->counts + (cur ^ 1), 0, 4, st), "memset count");
+            CK(launch_shade(s->g, wv, s->P, s->R, s->H, s->queue[cur], s->counts + cur, n, s->queue[cur ^ 1],
+                            s->counts + (cur ^ 1), 128, s->grid, st),
+               "shade launch");
+            cur ^= 1;
+        }
+        if (timing) cudaEventRecord(ev[2], st);
+        CK(launch_accumulate(s->g, wv, s->P, d_xyz, img_w, st), "accumulate launch");
+        if (timing) {
+            cudaEventRecord(ev[3], st);
+            CK(launch_count_rays(s->P, n, s->d_raycount, st), "count launch");
+            CK(cudaEventSynchronize(ev[3]), "event sync");
+            float a, b, c;
+            cudaEventElapsedTime(&a, ev[0], ev[1]);
+            cudaEventElapsedTime(&b, ev[1], ev[2]);
+            cudaEventElapsedTime(&c, ev[2], ev[3]);
+            t_gen += a * 1e-3; t_loop += b * 1e-3; t_acc += c * 1e-3;
+            stats->samples += n;
+        }
+    }
+    if (timing) {
+        unsigned long long rc = 0;
+        CK(cudaMemcpyAsync(&rc, s->d_raycount, 8, cudaMemcpyDeviceToHost, st), "copy ray count");
+        CK(cudaStreamSynchronize(st), "sync");
+        stats->ray_count += rc;
+        stats->initial_ray_generation_time += t_gen;
+        stats->trace_time += t_loop;  // trace + shade kernels of the wavefront loop
+        stats->sample_writing_time += t_acc;
+        stats->total_time += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        for (auto &e : ev) cudaEventDestroy(e);
+        s->rays_traced += rc;
+    }
+    return PSY_OK;
+}
+
+extern "C" {
+
+int psy_render_image_device(PsyScene *s, const uint32_t *crop, float *d_xyz, void *stream, PsyRenderStats *stats) {
+    if (!s || !d_xyz) return fail(PSY_E_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    uint32_t W = s->g.width, H = s->g.height;
+    uint32_t x0 = 0, y0 = 0, w = W, h = H;
+    if (crop) {
+        uint32_t x1 = std::min(crop[0], W - 1), y1 = std::min(crop[1], H - 1);
+        uint32_t x2 = std::min(crop[2], W - 1), y2 = std::min(crop[3], H - 1);
+        if (x2 < x1 || y2 < y1) return fail(PSY_E_INVALID, "empty crop");
+        x0 = x1; y0 = y1; w = x2 - x1 + 1; h = y2 - y1 + 1;
+    }
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    int r = render_region(s, x0, y0, w, h, s->g.spp, s->g.seed, d_xyz, W, st, stats);
+    if (r != PSY_OK) return r;
+    if (stats) return check_err(s);
+    return PSY_OK;
+}
+
+int psy_render_image(PsyScene *s, const uint32_t *crop, float *xyz_out, PsyRenderStats *stats) {
+    if (!s || !xyz_out) return fail(PSY_E_INVALID, "null argument");
+    size_t bytes = (size_t)s->g.width * s->g.height * 3 * sizeof(float);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->cap_xyz < bytes) {
+            if (s->d_xyz) cudaFree(s->d_xyz);
+            s->d_xyz = nullptr;
+            CK(cudaMalloc((void **)&s->d_xyz, bytes), "cudaMalloc image");
+            s->cap_xyz = bytes;
+        }
+        CK(cudaMemsetAsync(s->d_xyz, 0, bytes, s->stream), "memset image");
+    }
+    int r = psy_render_image_device(s, crop, s->d_xyz, s->stream, stats);
+    if (r != PSY_OK) return r;
+    CK(cudaMemcpyAsync(xyz_out, s->d_xyz, bytes, cudaMemcpyDeviceToHost, s->stream), "copy image");
+    CK(cudaStreamSynchronize(s->stream), "sync");
+    return check_err(s);
+}
+
+int psy_render_bucket(PsyScene *s, const PsyBucket *b, uint32_t spp, uint32_t seed, float *xyz_out,
+                      PsyRenderStats *stats) {
+    if (!s || !b || !xyz_out) return fail(PSY_E_INVALID, "null argument");
+    if (b->w == 0 || b->h == 0 || b->x + b->w > s->g.width || b->y + b->h > s->g.height)
+        return fail(PSY_E_INVALID, "bucket outside the image");
+    std::lock_guard<std::mutex> lk(s->mu);
+    size_t bytes = (size_t)b->w * b->h * 3 * sizeof(float);
+    if (s->cap_xyz < bytes) {
+        if (s->d_xyz) cudaFree(s->d_xyz);
+        s->d_xyz = nullptr;
+        CK(cudaMalloc((void **)&s->d_xyz, bytes), "cudaMalloc bucket");
+        s->cap_xyz = bytes;
+    }
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    // the bucket's pixels land at (x - b.x, y - b.y) of a bucket-sized buffer:
+    // offset the base pointer so the accumulate kernel's image indexing works
+    // with row stride b->w.
+    float *base = s->d_xyz - ((size_t)b->y * b->w + b->x) * 3;
+    int r = render_region(s, b->x, b->y, b->w, b->h, spp, seed, base, b->w, s->stream, stats);
+    if (r != PSY_OK) return r;
+    CK(cudaMemcpyAsync(xyz_out, s->d_xyz, bytes, cudaMemcpyDeviceToHost, s->stream), "copy bucket");
+    CK(cudaStreamSynchronize(s->stream), "sync");
+    return check_err(s);
+}
+
+// ---------------------------------------------------------------- inspection
+// Not part of the reference-facing interface: facts of the build for tests.
+int psy_debug_mesh_bvh_info(PsyScene *s, uint32_t object, uint32_t *tri_order, uint32_t *node_count) {
+    if (!s || object >= s->object_to_mesh.size() || s->object_to_mesh[object] < 0) return fail(PSY_E_INVALID, "not a mesh");
+    int m = s->object_to_mesh[object];
+    if (tri_order) std::memcpy(tri_order, s->mesh_tri_order[m].data(), s->mesh_tri_order[m].size() * 4);
+    if (node_count) *node_count = s->mesh_node_count[m];
+    return PSY_OK;
+}
+// Host-side build only (no device): BVH facts of a mesh object.
+int psy_debug_host_build(const PsySceneDesc *desc, const PsySceneOptions *opts, uint32_t object, uint32_t *tri_order,
+                         uint32_t *node_count, uint32_t *max_stack) {
+    HostScene hs;
+    std::string err;
+    int rc = build_host_scene(desc, opts, hs, err);
+    if (rc != PSY_OK) return fail(rc, err);
+    if (max_stack) *max_stack = hs.max_stack;
+    if (object >= hs.object_to_mesh.size() || hs.object_to_mesh[object] < 0) return PSY_OK;
+    int m = hs.object_to_mesh[object];
+    if (tri_order) std::memcpy(tri_order, hs.mesh_tri_order[m].data(), hs.mesh_tri_order[m].size() * 4);
+    if (node_count) *node_count = hs.mesh_node_count[m];
+    return PSY_OK;
+}
+int psy_debug_scene_info(PsyScene *s, uint32_t *max_stack, uint32_t *nodes, uint32_t *stack_variant) {
+    if (!s) return fail(PSY_E_INVALID, "null");
+    if (max_stack) *max_stack = s->max_stack;
+    if (nodes) *nodes = s->node_count;
+    if (stack_variant) *stack_variant = (uint32_t)s->stack;
+    return PSY_OK;
+}
+int psy_debug_set_launch(PsyScene *s, int grid, uint32_t wave_paths) {
+    if (!s) return fail(PSY_E_INVALID, "null");
+    s->grid = grid;
+    if (wave_paths >= 1024) s->wave_paths = wave_paths;
+    return PSY_OK;
+}
+
+}  // extern "C"

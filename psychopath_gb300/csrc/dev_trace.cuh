@@ -1,0 +1,307 @@
+// Per-ray BVH4 traversal of the two-level scene (instance BVH -> mesh BVH),
+// replacing Tracer::trace (src/tracer.rs:51-190), BVH4::traverse
+// (src/accel/bvh4.rs:101-184), TriangleMesh::intersect_rays
+// (src/surface/triangle_mesh.rs:124-322) and the light surfaces'
+// intersect_rays (src/light/{rectangle,sphere}_light.rs).
+//
+// The reference traverses packets: a task of ray indices walks the tree and
+// each node's BBox4 test fans the task out into the children's lanes.  Here
+// every thread walks its own ray through the same tree with a private stack
+// and visits the hit children in the reference's front-to-back table order
+// (TRAVERSAL_TABLE row of the ray's own direction octant).  Each ray meets
+// the same nodes and triangles with the same arithmetic, so closest hits and
+// their t are identical to the reference except for exact t ties between
+// triangles (where the visit order decides).
+#pragma once
+
+#include "dev_lights.cuh"
+
+namespace psyd {
+
+// Child visit order per direction octant and node topology (filled by the host).
+__constant__ uint8_t c_traversal_table[8][48];
+
+struct HitRec {
+    uint32_t kind;  // PSY_HIT_*
+    uint32_t prim;  // BVH-order global triangle index (mesh) or 0/1 (rect light)
+    uint32_t slot;  // instance slot (instance-BVH order)
+    float t, b0, b1, b2;
+};
+
+#define PSY_HIT_MISS_K 0u
+#define PSY_HIT_OCCLUDE_K 1u
+#define PSY_HIT_SURFACE_K 2u
+#define PSY_HIT_LIGHT_K 3u
+
+// Child bounds of one node at the ray's time.  Static nodes use the inline
+// key; motion nodes lerp between keys like lerp_slice(bounds, time).
+struct NodeBounds {
+    float4 xlo, xhi, ylo, yhi, zlo, zhi;
+};
+DI void load_key(const GScene &S, const GNode *n, uint32_t ext, uint32_t k, NodeBounds &b) {
+    if (k == 0) {
+        b.xlo = __ldg(&n->xlo); b.xhi = __ldg(&n->xhi); b.ylo = __ldg(&n->ylo);
+        b.yhi = __ldg(&n->yhi); b.zlo = __ldg(&n->zlo); b.zhi = __ldg(&n->zhi);
+    } else {
+        const GBounds4 *e = S.bounds_ext + ext + (k - 1);
+        b.xlo = __ldg(&e->xlo); b.xhi = __ldg(&e->xhi); b.ylo = __ldg(&e->ylo);
+        b.yhi = __ldg(&e->yhi); b.zlo = __ldg(&e->zlo); b.zhi = __ldg(&e->zhi);
+    }
+}
+DI float4 lerp4(float4 a, float4 b, float al) {
+    float ia = 1.0f - al;
+    return make_float4((a.x * ia) + (b.x * al), (a.y * ia) + (b.y * al), (a.z * ia) + (b.z * al), (a.w * ia) + (b.w * al));
+}
+
+// Test the (up to 4) children of a node; returns the hit mask.
+DI uint32_t node_hits(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, float time, uint32_t &code,
+                      uint32_t &count, uint4 &child) {
+    const GNode *n = S.nodes + ni;
+    uint4 meta = __ldg(&n->meta);
+    child = __ldg(&n->child);
+    code = meta.z & 0xFFu;
+    count = meta.z >> 8;
+    NodeBounds b;
+    if (meta.y <= 1) {
+        load_key(S, n, meta.x, 0, b);
+    } else {
+        uint32_t i; float a2;
+        if (lerp_index(meta.y, time, &i, &a2)) {
+            load_key(S, n, meta.x, i, b);
+        } else {
+            NodeBounds b0, b1;
+            load_key(S, n, meta.x, i, b0);
+            load_key(S, n, meta.x, i + 1, b1);
+            b.xlo = lerp4(b0.xlo, b1.xlo, a2); b.xhi = lerp4(b0.xhi, b1.xhi, a2);
+            b.ylo = lerp4(b0.ylo, b1.ylo, a2); b.yhi = lerp4(b0.yhi, b1.yhi, a2);
+            b.zlo = lerp4(b0.zlo, b1.zlo, a2); b.zhi = lerp4(b0.zhi, b1.zhi, a2);
+        }
+    }
+    uint32_t m = 0;
+    m |= slab_hit(b.xlo.x, b.xhi.x, b.ylo.x, b.yhi.x, b.zlo.x, b.zhi.x, o, di, tmax) ? 1u : 0u;
+    m |= slab_hit(b.xlo.y, b.xhi.y, b.ylo.y, b.yhi.y, b.zlo.y, b.zhi.y, o, di, tmax) ? 2u : 0u;
+    m |= slab_hit(b.xlo.z, b.xhi.z, b.ylo.z, b.yhi.z, b.zlo.z, b.zhi.z, o, di, tmax) ? 4u : 0u;
+    m |= slab_hit(b.xlo.w, b.xhi.w, b.ylo.w, b.yhi.w, b.zlo.w, b.zhi.w, o, di, tmax) ? 8u : 0u;
+    return m & ((1u << count) - 1u);
+}
+
+// FP16 node variant: decode the outward-rounded half offsets to f32 bounds
+// (anchor + offset, rounded outward again by one ulp so the f32 box
+// contains the f16 box), then the same slab test.
+DI float h2f_lo(uint32_t bits16, float anchor) {
+    float v = __half2float(__ushort_as_half((unsigned short)bits16));
+    float r = anchor + v;
+    return decrement_ulp(r);
+}
+DI float h2f_hi(uint32_t bits16, float anchor) {
+    float v = __half2float(__ushort_as_half((unsigned short)bits16));
+    float r = anchor + v;
+    return increment_ulp(r);
+}
+DI uint32_t node_hits_h(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, float time, uint32_t &code,
+                        uint32_t &count, uint4 &child) {
+    const GNodeH *n = S.nodes_h + ni;
+    float4 a = __ldg(&n->anchor);
+    if ((__float_as_uint(a.w) >> 16) & 1u)  // motion node: keys only in f32
+        return node_hits(S, ni, o, di, tmax, time, code, count, child);
+    uint2 xl = __ldg(&n->xlo), xh = __ldg(&n->xhi), yl = __ldg(&n->ylo), yh = __ldg(&n->yhi), zl = __ldg(&n->zlo),
+          zh = __ldg(&n->zhi);
+    child = __ldg(&n->child);
+    uint32_t meta = __float_as_uint(a.w);
+    code = meta & 0xFFu;
+    count = (meta >> 8) & 0xFFu;
+    uint32_t m = 0;
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+        uint32_t sh = (l & 1) * 16;
+        uint32_t xlo = (l < 2 ? xl.x : xl.y) >> sh, xhi = (l < 2 ? xh.x : xh.y) >> sh;
+        uint32_t ylo = (l < 2 ? yl.x : yl.y) >> sh, yhi = (l < 2 ? yh.x : yh.y) >> sh;
+        uint32_t zlo = (l < 2 ? zl.x : zl.y) >> sh, zhi = (l < 2 ? zh.x : zh.y) >> sh;
+        bool h = slab_hit(h2f_lo(xlo & 0xFFFF, a.x), h2f_hi(xhi & 0xFFFF, a.x), h2f_lo(ylo & 0xFFFF, a.y),
+                          h2f_hi(yhi & 0xFFFF, a.y), h2f_lo(zlo & 0xFFFF, a.z), h2f_hi(zhi & 0xFFFF, a.z), o, di, tmax);
+        m |= h ? (1u << l) : 0u;
+    }
+    return m & ((1u << count) - 1u);
+}
+
+// World-space vertices of triangle `tri` (global index) of mesh `M` at
+// `time`, transformed into world space by `mat` when the instance has a
+// transform (the reference tests triangles in world space).
+DI void fetch_tri(const GScene &S, const GMesh &M, uint32_t tri, float time, bool xf, const Xf &mat, V3 &p0, V3 &p1,
+                  V3 &p2) {
+    if (M.ts == 1) {
+        const float4 *t = S.tris + 3 * (size_t)tri;
+        p0 = v3(__ldg(t)); p1 = v3(__ldg(t + 1)); p2 = v3(__ldg(t + 2));
+    } else {
+        uint4 ix = __ldg(S.tri_idx + tri);
+        const float4 *vb = S.verts + M.vert_base;
+        p0 = lerp_slice_v3(vb + (size_t)ix.x * M.ts, M.ts, time);
+        p1 = lerp_slice_v3(vb + (size_t)ix.y * M.ts, M.ts, time);
+        p2 = lerp_slice_v3(vb + (size_t)ix.z * M.ts, M.ts, time);
+    }
+    if (xf) {
+        p0 = xf_point(p0, mat);
+        p1 = xf_point(p1, mat);
+        p2 = xf_point(p2, mat);
+    }
+}
+
+// Object->world matrix used for an instance's triangles at `time`.
+DI Xf instance_mat(const GScene &S, const GInstance &in, float time) {
+    if (in.xc == 1) return xf_load(S.xforms_inv + 3 * in.xinv);
+    return xf_inverse(lerp_slice_xf(S.xforms + 3 * in.xs, in.xc, time));
+}
+
+// Rectangle light test (RectangleLight::intersect_rays).
+DI bool rect_hit(const GScene &S, const GInstance &in, V3 o, V3 d, float tmax, float time, float &t, float &b0,
+                 float &b1, float &b2, uint32_t &which) {
+    const GLight L = S.lights[in.obj];
+    float w = light_dim(S, L, 0, time), h = light_dim(S, L, 1, time);
+    Xf xf = instance_xf_at(S, in, time);
+    Xf si = xf_inverse(xf);
+    V3 p1, p2, p3, p4;
+    rect_corners(w, h, si, &p1, &p2, &p3, &p4);
+    TriPre pre = tri_precompute(d);
+    if (tri_intersect(o, pre, tmax, p1, p2, p3, t, b0, b1, b2) && t < tmax) { which = 0; return true; }
+    if (tri_intersect(o, pre, tmax, p3, p4, p1, t, b0, b1, b2) && t < tmax) { which = 1; return true; }
+    return false;
+}
+// Sphere light test (SphereLight::intersect_rays).  `ol` is the ray origin
+// in the light's local space.
+DI bool sphere_hit(const GScene &S, const GInstance &in, V3 ol, V3 d, float tmax, float time, float &t_out) {
+    const GLight L = S.lights[in.obj];
+    Xf xf = instance_xf_at(S, in, time);
+    float radius = light_dim(S, L, 0, time);
+    V3 dir = xf_vector(d, xf);
+    float a = length2(dir);
+    float b = 2.0f * dot(dir, ol);
+    float c = length2(ol) - (radius * radius);
+    float disc = (b * b) - (4.0f * a * c);
+    if (disc < 0.0f) return false;
+    disc = sqrtf(disc);
+    float q = (b < 0.0f) ? -0.5f * (b - disc) : -0.5f * (b + disc);
+    float t0 = q / a;
+    float t1 = (q != 0.0f) ? c / q : tmax;
+    if (t0 > t1) { float tt = t0; t0 = t1; t1 = tt; }
+    if (t0 > tmax || t1 <= 0.0f) return false;
+    if (t0 > 0.0f) t_out = t0;
+    else if (t1 <= tmax) t_out = t1;
+    else return false;
+    return true;
+}
+
+// Trace one ray.  `occl`: any-hit (shadow ray).  Returns false on stack
+// overflow (the scene needs a deeper stack than STACK).
+template <int STACK>
+DI bool trace_ray(const GScene &S, V3 o, V3 d, float tmax, float time, bool occl, HitRec &hit) {
+    hit.kind = PSY_HIT_MISS_K;
+    if (S.top_root == PSY_REF_NONE) return true;
+    Xf ident = xf_identity();
+    // world level: update_local(identity)
+    V3 wo = xf_point(o, ident);
+    V3 wdi = recip(xf_vector(d, ident));
+    V3 lo = wo, ldi = wdi;
+    const uint8_t *row = c_traversal_table[ray_code(wdi)];
+    uint32_t stack[STACK];
+    int sp = 0;
+    uint32_t cur = S.top_root;
+    bool in_inst = false;
+    uint32_t slot = 0;
+    GMesh mesh;
+    Xf mat;
+    bool has_xf = false;
+    TriPre pre = tri_precompute(d);
+    while (true) {
+        // descend internal nodes
+        while (!psy_is_leaf(cur)) {
+            uint32_t code, count;
+            uint4 ch;
+            uint32_t m = S.use_fp16 ? node_hits_h(S, cur, lo, ldi, tmax, time, code, count, ch)
+                                    : node_hits(S, cur, lo, ldi, tmax, time, code, count, ch);
+            if (m == 0) goto pop;
+            uint32_t order = row[code];
+            uint32_t next = PSY_REF_NONE;
+            for (int i = (int)count - 1; i >= 0; i--) {
+                uint32_t ci = (order >> (i * 2)) & 3u;
+                if (m & (1u << ci)) {
+                    if (next != PSY_REF_NONE) {
+                        if (sp >= STACK) return false;
+                        stack[sp++] = next;
+                    }
+                    uint32_t c = ci == 0 ? ch.x : (ci == 1 ? ch.y : (ci == 2 ? ch.z : ch.w));
+                    next = c;
+                }
+            }
+            cur = next;
+        }
+        // leaf
+        if (!in_inst) {
+            slot = psy_leaf_first(cur);
+            GInstance in = S.instances[slot];
+            if (in.kind == PSY_INST_MESH) {
+                mesh = S.meshes[in.obj];
+                has_xf = in.xc != 0;
+                if (has_xf) {
+                    Xf x = lerp_slice_xf(S.xforms + 3 * in.xs, in.xc, time);
+                    lo = xf_point(o, x);
+                    ldi = recip(xf_vector(d, x));
+                    mat = instance_mat(S, in, time);
+                } else {
+                    mat = ident;
+                }
+                if (sp >= STACK) return false;
+                stack[sp++] = PSY_REF_NONE;  // leave-instance marker
+                in_inst = true;
+                row = c_traversal_table[ray_code(ldi)];
+                cur = mesh.root;
+                continue;
+            } else if (in.kind == PSY_INST_RECT) {
+                float t, b0, b1, b2;
+                uint32_t which;
+                if (rect_hit(S, in, o, d, tmax, time, t, b0, b1, b2, which)) {
+                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
+                    hit.kind = PSY_HIT_LIGHT_K; hit.prim = which; hit.slot = slot;
+                    hit.t = t; hit.b0 = b0; hit.b1 = b1; hit.b2 = b2;
+                    tmax = t;
+                }
+            } else {
+                Xf x = instance_xf_at(S, in, time);
+                V3 ol = in.xc ? xf_point(o, x) : wo;
+                float t;
+                if (sphere_hit(S, in, ol, d, tmax, time, t)) {
+                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
+                    hit.kind = PSY_HIT_LIGHT_K; hit.prim = 0; hit.slot = slot;
+                    hit.t = t; hit.b0 = hit.b1 = hit.b2 = 0.0f;
+                    tmax = t;
+                }
+            }
+        } else {
+            uint32_t first = psy_leaf_first(cur), cnt = psy_leaf_count(cur);
+            for (uint32_t k = 0; k < cnt; k++) {
+                uint32_t tri = first + k;
+                V3 p0, p1, p2;
+                fetch_tri(S, mesh, tri, time, has_xf, mat, p0, p1, p2);
+                float t, b0, b1, b2;
+                if (tri_intersect(o, pre, tmax, p0, p1, p2, t, b0, b1, b2)) {
+                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
+                    hit.kind = PSY_HIT_SURFACE_K; hit.prim = tri; hit.slot = slot;
+                    hit.t = t; hit.b0 = b0; hit.b1 = b1; hit.b2 = b2;
+                    tmax = t;
+                }
+            }
+        }
+    pop:
+        while (true) {
+            if (sp == 0) return true;
+            cur = stack[--sp];
+            if (cur != PSY_REF_NONE) break;
+            // leaving the instance: back to world space
+            in_inst = false;
+            lo = wo;
+            ldi = wdi;
+            row = c_traversal_table[ray_code(wdi)];
+        }
+    }
+}
+
+}  // namespace psyd

@@ -1,0 +1,528 @@
+// Kernels of the GB300 tracing path: ray tracing (closest / any hit),
+// camera ray generation, the light-path state machine and accumulation.
+#include <cuda_fp16.h>
+
+#include "dev_trace.cuh"
+#include "kernels.cuh"
+
+using namespace psyd;
+
+// ------------------------------------------------------------------ constants
+// Sobol direction numbers: dimension 1 is van der Corput, dimensions 2..8
+// follow Joe & Kuo's primitive polynomials and initial direction numbers.
+static void sobol_dirs_host(uint32_t d[8][32]) {
+    static const uint32_t s_[7] = {1, 2, 3, 3, 4, 4, 5};
+    static const uint32_t a_[7] = {0, 1, 1, 2, 1, 4, 2};
+    static const uint32_t m_[7][5] = {{1}, {1, 3}, {1, 3, 1}, {1, 1, 1}, {1, 1, 3, 3}, {1, 3, 5, 13}, {1, 1, 5, 5, 17}};
+    for (int k = 0; k < 32; k++) d[0][k] = 1u << (31 - k);
+    for (int j = 1; j < 8; j++) {
+        uint32_t s = s_[j - 1], a = a_[j - 1];
+        for (uint32_t k = 0; k < 32; k++) {
+            if (k < s) {
+                d[j][k] = m_[j - 1][k] << (31 - k);
+            } else {
+                uint32_t x = d[j][k - s] ^ (d[j][k - s] >> s);
+                for (uint32_t i = 1; i < s; i++)
+                    if ((a >> (s - 1 - i)) & 1u) x ^= d[j][k - i];
+                d[j][k] = x;
+            }
+        }
+    }
+}
+// Child visit order per ray octant and node topology (sub_crates/bvh_order).
+static void traversal_table_host(uint8_t t[8][48]) {
+    for (int rd = 0; rd < 8; rd++) {
+        int ray[3] = {rd & 1, (rd >> 1) & 1, (rd >> 2) & 1};
+        int k = 0;
+        auto sw = [](int &a, int &b) { int x = a; a = b; b = x; };
+        for (int s2 = 0; s2 < 3; s2++)
+            for (int s1 = 0; s1 < 3; s1++)
+                for (int s0 = 0; s0 < 3; s0++) {
+                    int p[4] = {0, 1, 2, 3};
+                    if (ray[s1]) sw(p[0], p[1]);
+                    if (ray[s2]) sw(p[2], p[3]);
+                    if (ray[s0]) { sw(p[0], p[2]); sw(p[1], p[3]); }
+                    t[rd][k++] = (uint8_t)(p[0] | (p[1] << 2) | (p[2] << 4) | (p[3] << 6));
+                }
+        for (int s1 = 0; s1 < 3; s1++)
+            for (int s0 = 0; s0 < 3; s0++) {
+                int p[3] = {0, 1, 2};
+                if (ray[s1]) sw(p[0], p[1]);
+                if (ray[s0]) { sw(p[0], p[1]); sw(p[0], p[2]); }
+                t[rd][k++] = (uint8_t)(p[0] | (p[1] << 2) | (p[2] << 4));
+            }
+        for (int s1 = 0; s1 < 3; s1++)
+            for (int s0 = 0; s0 < 3; s0++) {
+                int p[3] = {0, 1, 2};
+                if (ray[s1]) sw(p[1], p[2]);
+                if (ray[s0]) { sw(p[0], p[2]); sw(p[0], p[1]); }
+                t[rd][k++] = (uint8_t)(p[0] | (p[1] << 2) | (p[2] << 4));
+            }
+        for (int s0 = 0; s0 < 3; s0++) {
+            int p[2] = {0, 1};
+            if (ray[s0]) sw(p[0], p[1]);
+            t[rd][k++] = (uint8_t)(p[0] | (p[1] << 2));
+        }
+    }
+}
+void psy_upload_constants() {
+    uint32_t d[8][32];
+    uint8_t t[8][48];
+    sobol_dirs_host(d);
+    traversal_table_host(t);
+    cudaMemcpyToSymbol(c_sobol_dirs, d, sizeof(d));
+    cudaMemcpyToSymbol(c_traversal_table, t, sizeof(t));
+}
+
+// ------------------------------------------------------------------ surface data
+// SurfaceIntersectionData of a hit, recomputed from the hit record with the
+// traversal's own arithmetic (src/surface/triangle_mesh.rs:264-318,
+// src/light/*_light.rs intersect_rays).
+struct SurfData {
+    V3 pos, nor, nor_g;
+    float pos_err, sample_pdf;
+    Closure closure;
+    int32_t shader;
+};
+// Colour of the tracer's shader for instances without one (src/tracer.rs:161-163),
+// rec709_to_xyz((1, 0, 1)) computed on the host.
+__constant__ GColor c_magenta;
+
+__device__ void resolve_hit(const GScene &S, const HitRec &h, V3 o, V3 d, float time, SurfData &sd) {
+    GInstance in = S.instances[h.slot];
+    if (h.kind == PSY_HIT_SURFACE_K) {
+        GMesh M = S.meshes[in.obj];
+        bool has_xf = in.xc != 0;
+        Xf mat = has_xf ? instance_mat(S, in, time) : xf_identity();
+        V3 p0, p1, p2;
+        fetch_tri(S, M, h.prim, time, has_xf, mat, p0, p1, p2);
+        surface_point(p0, p1, p2, h.b0, h.b1, h.b2, &sd.pos, &sd.pos_err);
+        V3 geo = cross(p0 - p1, p0 - p2);
+        V3 sn = geo;
+        if (M.has_normals) {
+            uint4 ix = __ldg(S.tri_idx + h.prim);
+            const float4 *nb = S.normals + M.vert_base;
+            V3 n0 = normalized(lerp_slice_v3(nb + (size_t)ix.x * M.ts, M.ts, time));
+            V3 n1 = normalized(lerp_slice_v3(nb + (size_t)ix.y * M.ts, M.ts, time));
+            V3 n2 = normalized(lerp_slice_v3(nb + (size_t)ix.z * M.ts, M.ts, time));
+            V3 snn = xf_normal((n0 * h.b0) + (n1 * h.b1) + (n2 * h.b2), mat);
+            sn = (dot(snn, geo) >= 0.0f) ? snn : neg(snn);
+        }
+        sd.nor = sn;
+        sd.nor_g = geo;
+        sd.sample_pdf = 0.0f;
+        sd.shader = in.shader;
+        if (in.shader >= 0) {
+            sd.closure = closure_from_shader(S.shaders[in.shader]);
+        } else {
+            sd.closure.kind = PSY_CL_EMIT;
+            sd.closure.color = c_magenta;
+            sd.closure.roughness = 0.0f;
+            sd.closure.fresnel = 0.0f;
+        }
+        return;
+    }
+    // light surfaces
+    const GLight L = S.lights[in.obj];
+    Xf xf = instance_xf_at(S, in, time);
+    sd.shader = -1;
+    sd.closure.kind = PSY_CL_EMIT;
+    sd.closure.roughness = 0.0f;
+    sd.closure.fresnel = 0.0f;
+    GColor col = lerp_slice_color(S.light_colors + L.key_base, L.nkeys, time);
+    if (in.kind == PSY_INST_RECT) {
+        float w = light_dim(S, L, 0, time), hh = light_dim(S, L, 1, time);
+        Xf si = xf_inverse(xf);
+        V3 p1, p2, p3, p4;
+        rect_corners(w, hh, si, &p1, &p2, &p3, &p4);
+        V3 a = h.prim == 0 ? p1 : p3, b = h.prim == 0 ? p2 : p4, c = h.prim == 0 ? p3 : p1;
+        surface_point(a, b, c, h.b0, h.b1, h.b2, &sd.pos, &sd.pos_err);
+        V3 nn = cross(a - b, a - c);
+        sd.nor = nn;
+        sd.nor_g = nn;
+        sd.sample_pdf = rect_sample_pdf(S, L, xf, o, d, sd.pos, time);
+        float isa = (float)(1.0 / ((double)w * (double)hh));
+        sd.closure.color = color_mul(col, isa);
+    } else {
+        float radius = light_dim(S, L, 0, time);
+        Xf ixf = xf_inverse(xf);
+        V3 ol = in.xc ? xf_point(o, xf) : xf_point(o, xf_identity());
+        V3 dir = xf_vector(d, xf);
+        V3 unit = normalized(ol + (dir * h.t));
+        sd.pos = xf_vector(unit * radius, ixf);  // as the reference: a vector transform
+        sd.pos_err = 0.001f;
+        V3 nrm = xf_normal(unit, ixf);
+        sd.nor = nrm;
+        sd.nor_g = nrm;
+        sd.sample_pdf = sphere_sample_pdf(S, L, xf, o, time);
+        float isa = (float)(1.0 / (4.0 * PSY_PI_64 * (double)radius * (double)radius));
+        sd.closure.color = color_mul(col, isa);
+    }
+}
+
+// ------------------------------------------------------------------ ray tracing
+template <int STACK>
+__global__ void __launch_bounds__(128) k_trace_rays(GScene S, const PsyRay *__restrict__ rays, uint32_t n,
+                                                    PsyHit *__restrict__ hits, PsySurfaceHit *__restrict__ full,
+                                                    int *err) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *r = reinterpret_cast<const float *>(rays + i);
+    V3 o = v3(r[0], r[1], r[2]), d = v3(r[3], r[4], r[5]);
+    float tmax = r[6], time = r[7];
+    uint32_t flags = reinterpret_cast<const uint32_t *>(r)[9];
+    HitRec h;
+    if (!trace_ray<STACK>(S, o, d, tmax, time, (flags & PSY_RAY_OCCLUSION) != 0, h)) {
+        atomicExch(err, PSY_E_OVERFLOW);
+        h.kind = PSY_HIT_MISS_K;
+    }
+    PsyHit out;
+    out.kind = h.kind;
+    out.prim = 0; out.inst = 0; out.t = 0.0f; out.b0 = 0.0f; out.b1 = 0.0f; out.b2 = 0.0f; out.pad = 0.0f;
+    if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
+        GInstance in = S.instances[h.slot];
+        out.prim = h.kind == PSY_HIT_SURFACE_K ? __ldg(S.tri_idx + h.prim).w : h.prim;
+        out.inst = in.id;
+        out.t = h.t; out.b0 = h.b0; out.b1 = h.b1; out.b2 = h.b2;
+    }
+    hits[i] = out;
+    if (full) {
+        PsySurfaceHit f;
+        f.hit = out;
+        f.shader = -1;
+        f.pos[0] = f.pos[1] = f.pos[2] = 0.0f;
+        f.nor[0] = f.nor[1] = f.nor[2] = 0.0f;
+        f.nor_g[0] = f.nor_g[1] = f.nor_g[2] = 0.0f;
+        f.pos_err = 0.0f;
+        f.sample_pdf = 0.0f;
+        if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
+            SurfData sd;
+            resolve_hit(S, h, o, d, time, sd);
+            f.pos[0] = sd.pos.x; f.pos[1] = sd.pos.y; f.pos[2] = sd.pos.z;
+            f.nor[0] = sd.nor.x; f.nor[1] = sd.nor.y; f.nor[2] = sd.nor.z;
+            f.nor_g[0] = sd.nor_g.x; f.nor_g[1] = sd.nor_g.y; f.nor_g[2] = sd.nor_g.z;
+            f.pos_err = sd.pos_err;
+            f.sample_pdf = sd.sample_pdf;
+            f.shader = sd.shader;
+        }
+        full[i] = f;
+    }
+}
+
+cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurfaceHit *full,
+                              int stack, int block, int *d_err, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    (void)block;
+    dim3 b(128), g((n + 127) / 128);
+    if (stack <= 32) k_trace_rays<32><<<g, b, 0, st>>>(S, rays, n, hits, full, d_err);
+    else if (stack <= 64) k_trace_rays<64><<<g, b, 0, st>>>(S, rays, n, hits, full, d_err);
+    else k_trace_rays<192><<<g, b, 0, st>>>(S, rays, n, hits, full, d_err);
+    return cudaGetLastError();
+}
+
+// Queue-driven trace for the render wavefront: a grid-stride loop over the
+// live paths listed in queue[0 .. *count).
+template <int STACK>
+__global__ void __launch_bounds__(128) k_trace_queue(GScene S, RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
+                                                     const uint32_t *__restrict__ count, int *err) {
+    uint32_t n = *count;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        uint32_t p = queue[q];
+        float4 ro = R.o[p], rd = R.d[p];
+        HitRec h;
+        if (!trace_ray<STACK>(S, v3(ro), v3(rd), ro.w, rd.w, R.occl[p] != 0, h)) {
+            atomicExch(err, PSY_E_OVERFLOW);
+            h.kind = PSY_HIT_MISS_K;
+        }
+        H.ki[p] = make_uint4(h.kind, h.prim, h.slot, 0u);
+        H.tb[p] = make_float4(h.t, h.b0, h.b1, h.b2);
+    }
+}
+
+cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
+                               uint32_t max_count, int stack, int block, int grid, int *d_err, cudaStream_t st) {
+    (void)block;
+    if (grid <= 0) grid = (int)((max_count + 127) / 128);
+    if (grid == 0) return cudaSuccess;
+    if (stack <= 32) k_trace_queue<32><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err);
+    else if (stack <= 64) k_trace_queue<64><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err);
+    else k_trace_queue<192><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ camera
+// Ray generation of Renderer::render_job (src/renderer.rs:241-275) and
+// LightPath::new (src/renderer.rs:392-431) / Camera::generate_ray
+// (src/camera.rs:74-102).
+__global__ void k_camera(GScene S, Wave w, PathState P, RayBuf R, uint32_t *queue, uint32_t *count) {
+    uint32_t n = w.w * w.h * w.spp;
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) *count = n;
+    if (p >= n) return;
+    uint32_t lp = p / w.spp, si = p - lp * w.spp;
+    uint32_t x = w.x0 + lp % w.w, y = w.y0 + lp / w.w;
+    float cmpx = 1.0f / (float)S.width, cmpy = 1.0f / (float)S.height;
+    float min_x = -1.0f, max_x = 1.0f;
+    float min_y = -((float)S.height / (float)S.width), max_y = (float)S.height / (float)S.width;
+    float xe = max_x - min_x, ye = max_y - min_y;
+    float d[4], d4[4];
+    get_sample_4d(si, 0, x, y, w.seed, d);
+    get_sample_4d(si, 1, x, y, w.seed, d4);
+    float fx = probit(d[3], 2.0f / 6.0f) + 0.5f;
+    float fy = probit(d4[0], 2.0f / 6.0f) + 0.5f;
+    float sx = (fx + (float)x) * cmpx;
+    float sy = (fy + (float)y) * cmpy;
+    float ix = (sx - 0.5f) * xe, iy = (0.5f - sy) * ye;
+    float wl = map_0_1_to_wavelength(golden_ratio_sample(si, hash_u32((x << 16) ^ y, w.seed)));
+    float time = d[0];
+    // Camera::generate_ray
+    Xf xf = lerp_slice_xf(S.cam_xf, S.n_cam_xf, time);
+    float tfov = lerp_slice_f(S.cam_tfov, S.n_cam_tfov, time);
+    float ar = lerp_slice_f(S.cam_ap, S.n_cam_ap, time);
+    float fd = lerp_slice_f(S.cam_fd, S.n_cam_fd, time);
+    float cu, cv;
+    square_to_circle((d[1] * 2.0f) - 1.0f, (d[2] * 2.0f) - 1.0f, &cu, &cv);
+    V3 orig = v3(ar * cu, ar * cv, 0.0f);
+    V3 dir = normalized(v3((ix * tfov) - (orig.x / fd), (iy * tfov) - (orig.y / fd), 1.0f));
+    V3 wo = xf_point(orig, xf), wd = xf_vector(dir, xf);
+    P.color[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    P.latt[p] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    P.pending[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    P.nafac[p] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    P.nb_o[p] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);  // w: closure_sample_pdf = 1
+    P.nb_d[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    P.tw[p] = make_float2(time, wl);
+    P.seed[p] = w.seed ^ 0x40d4682bu;
+    P.flags[p] = 0u;  // EV_CAMERA, bounce 0, no next bounce, 0 rays
+    R.o[p] = make_float4(wo.x, wo.y, wo.z, CUDART_INF_F);
+    R.d[p] = make_float4(wd.x, wd.y, wd.z, time);
+    R.occl[p] = 0;
+    queue[p] = p;
+}
+
+cudaError_t launch_camera(const GScene &S, const Wave &w, PathState P, RayBuf R, uint32_t *queue, uint32_t *count,
+                          cudaStream_t st) {
+    uint32_t n = w.w * w.h * w.spp;
+    if (n == 0) return cudaSuccess;
+    k_camera<<<(n + 255) / 256, 256, 0, st>>>(S, w, P, R, queue, count);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ shade
+#define EV_CAMERA 0u
+#define EV_BOUNCE 1u
+#define EV_SHADOW 2u
+
+__device__ __forceinline__ void push_live(bool alive, uint32_t p, uint32_t *next_queue, uint32_t *next_count) {
+    unsigned mask = __ballot_sync(__activemask(), alive);
+    if (mask == 0) return;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(next_count, (uint32_t)__popc(mask));
+    base = __shfl_sync(__activemask(), base, leader);
+    if (alive) next_queue[base + __popc(mask & ((1u << lane) - 1u))] = p;
+}
+
+// LightPath::next (src/renderer.rs:449-691).
+__global__ void __launch_bounds__(128) k_shade(GScene S, Wave w, PathState P, RayBuf R, HitBuf H,
+                                               const uint32_t *__restrict__ queue, const uint32_t *__restrict__ count,
+                                               uint32_t *next_queue, uint32_t *next_count) {
+    uint32_t n = *count;
+    uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t nloop = (n + stride - 1) / stride * stride;  // keep whole warps in the loop for the ballot
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nloop; q += stride) {
+        bool alive = false;
+        uint32_t p = 0;
+        if (q < n) {
+            p = queue[q];
+            uint32_t fl = P.flags[p];
+            uint32_t ev = fl & 3u, bounce = (fl >> 2) & 0xFFu, has_nb = (fl >> 10) & 1u, nrays = fl >> 16;
+            nrays += 1;
+            float2 tw = P.tw[p];
+            float time = tw.x, wl = tw.y;
+            uint4 ki = H.ki[p];
+            float4 tb = H.tb[p];
+            float4 ro = R.o[p], rd = R.d[p];
+            V3 o = v3(ro), d = v3(rd);
+            V4 color = v4(P.color[p]);
+            V4 latt = v4(P.latt[p]);
+            float4 nbo = P.nb_o[p];
+            float csp = nbo.w;  // closure_sample_pdf
+            uint32_t seed = P.seed[p];
+            uint32_t pix = p / w.spp;
+            uint32_t si = p - pix * w.spp;
+            uint32_t px = w.x0 + pix % w.w, py = w.y0 + pix / w.w;
+            if (ev == EV_CAMERA || ev == EV_BOUNCE) {
+                if (ki.x == PSY_HIT_SURFACE_K || ki.x == PSY_HIT_LIGHT_K) {
+                    HitRec h;
+                    h.kind = ki.x; h.prim = ki.y; h.slot = ki.z;
+                    h.t = tb.x; h.b0 = tb.y; h.b1 = tb.z; h.b2 = tb.w;
+                    SurfData sd;
+                    resolve_hit(S, h, o, d, time, sd);
+                    const Closure &cl = sd.closure;
+                    if (cl.kind == PSY_CL_EMIT) {
+                        V4 c = color_to_spectral(cl.color, wl);
+                        if (ev == EV_CAMERA) {
+                            color = color + c;
+                        } else {
+                            float mis = power_heuristic(csp, sd.sample_pdf);
+                            color = color + c * latt / splat4(mis);
+                        }
+                        P.color[p] = f4(color);
+                    } else {
+                        latt = latt / splat4(csp);
+                        seed += 1;
+                        float smp[4];
+                        get_sample_4d(si, 0, px, py, seed, smp);
+                        LightSample li = scene_sample_lights(S, smp[0], smp[1], smp[2], wl, time, d, sd.pos, sd.nor,
+                                                             sd.nor_g, cl);
+                        bool found = false;
+                        if (li.kind != 0 && !(li.pdf <= 0.0f) && !(li.sel_pdf <= 0.0f)) {
+                            V4 att;
+                            float cpdf;
+                            V3 so, sdir;
+                            float smax;
+                            if (li.kind == 1) {
+                                att = closure_evaluate(cl, d, li.dir, sd.nor, sd.nor_g, wl, &cpdf);
+                                so = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), li.dir);
+                                sdir = li.dir;
+                                smax = CUDART_INF_F;
+                            } else {
+                                V3 dir = li.sp - sd.pos;
+                                att = closure_evaluate(cl, d, dir, sd.nor, sd.nor_g, wl, &cpdf);
+                                so = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
+                                V3 oe = robust_ray_origin(li.sp, li.serr, normalized(li.sn), neg(dir));
+                                sdir = oe - so;
+                                smax = 1.0f;
+                            }
+                            if (!(max_elem4(att) <= 0.0f)) {
+                                float lmis = power_heuristic(li.pdf, cpdf);
+                                V4 pend = li.color * att * latt / splat4(lmis * li.sel_pdf);
+                                P.pending[p] = f4(pend);
+                                R.o[p] = make_float4(so.x, so.y, so.z, smax);
+                                R.d[p] = make_float4(sdir.x, sdir.y, sdir.z, time);
+                                R.occl[p] = 1;
+                                found = true;
+                            }
+                        }
+                        bool do_bounce = false;
+                        V4 nafac = v4(P.nafac[p]);
+                        if (bounce < S.max_bounces) {
+                            bounce += 1;
+                            seed += 1;
+                            float b4[4];
+                            get_sample_4d(si, 0, px, py, seed, b4);
+                            V3 dir;
+                            float pdf;
+                            V4 filt = closure_sample(cl, d, sd.nor, sd.nor_g, b4[0], b4[1], wl, &dir, &pdf);
+                            if ((pdf > 0.0f) && (max_elem4(filt) > 0.0f)) {
+                                nafac = filt;
+                                csp = pdf;
+                                V3 nb = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
+                                P.nafac[p] = f4(nafac);
+                                P.nb_o[p] = make_float4(nb.x, nb.y, nb.z, csp);
+                                P.nb_d[p] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                                has_nb = 1;
+                                do_bounce = true;
+                            }
+                        } else {
+                            has_nb = 0;
+                        }
+                        if (found) {
+                            ev = EV_SHADOW;
+                            alive = true;
+                        } else if (do_bounce) {
+                            float4 nb = P.nb_o[p], nd = P.nb_d[p];
+                            R.o[p] = make_float4(nb.x, nb.y, nb.z, CUDART_INF_F);
+                            R.d[p] = make_float4(nd.x, nd.y, nd.z, time);
+                            R.occl[p] = 0;
+                            ev = EV_BOUNCE;
+                            latt = latt * nafac;
+                            alive = true;
+                        }
+                        P.latt[p] = f4(latt);
+                        P.seed[p] = seed;
+                    }
+                } else {
+                    V4 bg = color_to_spectral(S.background, wl);
+                    color = color + bg * latt / splat4(csp);
+                    P.color[p] = f4(color);
+                }
+            } else {
+                // shadow ray result
+                if (ki.x == PSY_HIT_MISS_K) {
+                    color = color + v4(P.pending[p]);
+                    P.color[p] = f4(color);
+                }
+                if (has_nb) {
+                    float4 nb = P.nb_o[p], nd = P.nb_d[p];
+                    R.o[p] = make_float4(nb.x, nb.y, nb.z, CUDART_INF_F);
+                    R.d[p] = make_float4(nd.x, nd.y, nd.z, time);
+                    R.occl[p] = 0;
+                    latt = latt * v4(P.nafac[p]);
+                    P.latt[p] = f4(latt);
+                    ev = EV_BOUNCE;
+                    alive = true;
+                }
+            }
+            P.flags[p] = ev | (bounce << 2) | (has_nb << 10) | (nrays << 16);
+        }
+        push_live(alive, p, next_queue, next_count);
+    }
+}
+
+cudaError_t launch_shade(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
+                         const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
+                         int block, int grid, cudaStream_t st) {
+    (void)block;
+    if (grid <= 0) grid = (int)((max_count + 127) / 128);
+    if (grid == 0) return cudaSuccess;
+    k_shade<<<grid, 128, 0, st>>>(S, w, P, R, H, queue, count, next_queue, next_count);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ accumulate
+// XYZ::from_spectral_sample / spp added per pixel (src/renderer.rs:299-310),
+// summing the pixel's samples in sample order.
+__global__ void k_accumulate(GScene S, Wave w, PathState P, float *xyz, uint32_t img_w) {
+    uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= w.w * w.h) return;
+    uint32_t x = w.x0 + pix % w.w, y = w.y0 + pix / w.w;
+    float inv = (float)w.spp;
+    V3 acc = v3(0.0f, 0.0f, 0.0f);
+    for (uint32_t s = 0; s < w.spp; s++) {
+        uint32_t p = pix * w.spp + s;
+        V3 c = xyz_from_spectral(v4(P.color[p]), P.tw[p].y);
+        acc = acc + (c / inv);
+    }
+    float *o = xyz + ((size_t)y * img_w + x) * 3;
+    o[0] = acc.x; o[1] = acc.y; o[2] = acc.z;
+}
+
+cudaError_t launch_accumulate(const GScene &S, const Wave &w, PathState P, float *xyz, uint32_t img_w,
+                              cudaStream_t st) {
+    uint32_t n = w.w * w.h;
+    if (n == 0) return cudaSuccess;
+    k_accumulate<<<(n + 127) / 128, 128, 0, st>>>(S, w, P, xyz, img_w);
+    return cudaGetLastError();
+}
+
+__global__ void k_count_rays(PathState P, uint32_t n, unsigned long long *out) {
+    unsigned long long local = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) local += P.flags[i] >> 16;
+    for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, local);
+}
+cudaError_t launch_count_rays(PathState P, uint32_t n, unsigned long long *out, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_count_rays<<<152 * 4, 256, 0, st>>>(P, n, out);
+    return cudaGetLastError();
+}
+
+// Host helper: set the magenta constant (rec709_to_xyz((1,0,1))) computed by
+// the host with the reference's f32 arithmetic.
+void psy_set_magenta(const float xyz[3]) {
+    GColor c{PSY_COLOR_XYZ_K, xyz[0], xyz[1], xyz[2]};
+    cudaMemcpyToSymbol(c_magenta, &c, sizeof(c));
+}

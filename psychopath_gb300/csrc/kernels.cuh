@@ -1,0 +1,57 @@
+// Kernel interfaces of the tracing path (host-visible launch helpers).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/psy_gpu.h"
+#include "psy_layout.h"
+
+// Wavefront path state, structure of arrays (one entry per path = one
+// (pixel, sample) of the wave).  Mirrors LightPath (src/renderer.rs:370-388).
+struct PathState {
+    float4 *color;    // accumulated path colour (4 hero wavelengths)
+    float4 *latt;     // light_attenuation
+    float4 *pending;  // pending_color_addition
+    float4 *nafac;    // next_attenuation_fac
+    float4 *nb_o;     // next bounce ray origin, w = closure_sample_pdf
+    float4 *nb_d;     // next bounce ray direction, w unused
+    float2 *tw;       // (time, wavelength)
+    uint32_t *seed;   // sampling_seed
+    uint32_t *flags;  // event (bits 0-1) | bounce_count << 2 (8 bits) | has_next_bounce << 10 | rays << 16
+};
+struct RayBuf {
+    float4 *o;        // origin xyz, max_t
+    float4 *d;        // direction xyz, time
+    uint8_t *occl;    // occlusion flag
+};
+struct HitBuf {
+    uint4 *ki;        // kind, prim, slot, 0
+    float4 *tb;       // t, b0, b1, b2
+};
+// A rectangular region of pixels rendered as one wave, all spp samples each.
+struct Wave {
+    uint32_t x0, y0, w, h;
+    uint32_t spp, seed;
+};
+
+void psy_upload_constants();  // Sobol directions + traversal table -> __constant__
+
+// Trace n PsyRay records (device) into PsyHit records (device).
+cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurfaceHit *full,
+                              int stack, int block, int *d_err, cudaStream_t st);
+// Camera rays for a wave; fills queue with 0..n-1 and *count = n.
+cudaError_t launch_camera(const GScene &S, const Wave &w, PathState P, RayBuf R, uint32_t *queue, uint32_t *count,
+                          cudaStream_t st);
+// Trace the queued rays of a wave.
+cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
+                               uint32_t max_count, int stack, int block, int grid, int *d_err, cudaStream_t st);
+// LightPath::next for the queued paths; live paths go to next_queue.
+cudaError_t launch_shade(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
+                         const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
+                         int block, int grid, cudaStream_t st);
+// Per-pixel XYZ (sum over samples in sample order / spp) into xyz[(y*W + x)*3].
+cudaError_t launch_accumulate(const GScene &S, const Wave &w, PathState P, float *xyz, uint32_t img_w,
+                              cudaStream_t st);
+// Sum of per-path ray counts of a wave into *out (u64).
+cudaError_t launch_count_rays(PathState P, uint32_t n, unsigned long long *out, cudaStream_t st);

@@ -1,0 +1,179 @@
+"""Python binding of the C ABI (include/psy_gpu.h), mirroring the
+reference's Tracer / Renderer interface for this path:
+
+    scene = Scene(scene_data)                  # AssemblyBuilder::build + Camera::new
+    tracer = Tracer(scene)                     # Tracer::from_assembly
+    hits = tracer.trace(rays)                  # Tracer::trace
+    tracer.rays_traced()                       # Tracer::rays_traced
+    img, stats = Renderer(scene).render()      # Renderer::render
+
+The CUDA library is required: loading fails loudly when it is missing or no
+GPU is present; there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libpsy_gpu.so")
+_lib = None
+
+EXPORTED = [
+    "psy_scene_create", "psy_scene_destroy", "psy_scene_device_bytes", "psy_trace", "psy_trace_device",
+    "psy_rays_traced", "psy_render_bucket", "psy_render_image_device", "psy_render_image", "psy_last_error",
+    "psy_version",
+]
+
+
+class PsyError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("psy error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib(path=None):
+    """Load libpsy_gpu.so (built by psychopath_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or _LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("libpsy_gpu.so not built (run psychopath_gb300.build.build()): %s" % p)
+    L = C.CDLL(p)
+    vp, u32 = C.c_void_p, C.c_uint32
+    L.psy_scene_create.argtypes = [vp, vp, C.POINTER(vp)]
+    L.psy_scene_destroy.argtypes = [vp]
+    L.psy_scene_device_bytes.argtypes = [vp, C.POINTER(C.c_uint64)]
+    L.psy_trace.argtypes = [vp, vp, u32, vp, vp, vp]
+    L.psy_trace_device.argtypes = [vp, vp, u32, vp, vp]
+    L.psy_rays_traced.argtypes = [vp, C.POINTER(C.c_uint64)]
+    L.psy_render_bucket.argtypes = [vp, vp, u32, u32, vp, vp]
+    L.psy_render_image_device.argtypes = [vp, vp, vp, vp, vp]
+    L.psy_render_image.argtypes = [vp, vp, vp, vp]
+    L.psy_last_error.restype = C.c_char_p
+    L.psy_version.restype = C.c_char_p
+    L.psy_debug_mesh_bvh_info.argtypes = [vp, u32, vp, C.POINTER(u32)]
+    L.psy_debug_scene_info.argtypes = [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]
+    L.psy_debug_set_launch.argtypes = [vp, C.c_int, u32]
+    L.psy_debug_host_build.argtypes = [vp, vp, u32, vp, C.POINTER(u32), C.POINTER(u32)]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise PsyError(rc, lib().psy_last_error().decode())
+
+
+def host_build_info(scene_data, obj, bounds="fp32"):
+    """Run only the host-side scene build (no GPU needed): the mesh object's
+    triangle order after the BVH build, its BVH4 node count and the scene's
+    worst-case traversal stack depth."""
+    desc = scene_data.desc()
+    opts = abi.PsySceneOptions()
+    opts.bounds_precision = abi.PSY_BOUNDS_FP16 if bounds == "fp16" else abi.PSY_BOUNDS_FP32
+    n = scene_data.objects[obj]["indices"].shape[0] if scene_data.objects[obj]["kind"] == abi.PSY_OBJ_MESH else 0
+    order = np.zeros(max(1, n), dtype=np.uint32)
+    nc, ms = C.c_uint32(), C.c_uint32()
+    _check(lib().psy_debug_host_build(C.byref(desc), C.byref(opts), obj, order.ctypes.data, C.byref(nc), C.byref(ms)))
+    return order[:n], nc.value, ms.value
+
+
+class Scene:
+    """A scene resident on the GPU (psy_scene_create)."""
+
+    def __init__(self, scene_data, bounds="fp32"):
+        self.data = scene_data
+        self._desc = scene_data.desc()
+        opts = abi.PsySceneOptions()
+        opts.bounds_precision = abi.PSY_BOUNDS_FP16 if bounds == "fp16" else abi.PSY_BOUNDS_FP32
+        h = C.c_void_p()
+        _check(lib().psy_scene_create(C.byref(self._desc), C.byref(opts), C.byref(h)))
+        self.h = h
+        self.width, self.height, self.spp = scene_data.width, scene_data.height, scene_data.spp
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().psy_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def device_bytes(self):
+        v = C.c_uint64()
+        _check(lib().psy_scene_device_bytes(self.h, C.byref(v)))
+        return v.value
+
+    def info(self):
+        a, b, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        _check(lib().psy_debug_scene_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"max_stack": a.value, "nodes": b.value, "stack_variant": c.value}
+
+    def mesh_bvh_info(self, obj):
+        n = self.data.objects[obj]["indices"].shape[0]
+        order = np.zeros(n, dtype=np.uint32)
+        nc = C.c_uint32()
+        _check(lib().psy_debug_mesh_bvh_info(self.h, obj, order.ctypes.data, C.byref(nc)))
+        return order, nc.value
+
+    def set_launch(self, grid=0, wave_paths=0):
+        _check(lib().psy_debug_set_launch(self.h, grid, wave_paths))
+
+
+class Tracer:
+    """Tracer::from_assembly / trace / rays_traced over the GPU scene."""
+
+    def __init__(self, scene):
+        self.scene = scene
+
+    def trace(self, rays, full=False):
+        rays = np.ascontiguousarray(rays, dtype=abi.ray_dtype())
+        n = len(rays)
+        hits = np.zeros(n, dtype=abi.hit_dtype())
+        fh = np.zeros(n, dtype=abi.surface_hit_dtype()) if full else None
+        _check(lib().psy_trace(self.scene.h, rays.ctypes.data, n, hits.ctypes.data,
+                               fh.ctypes.data if full else None, None))
+        return (hits, fh) if full else hits
+
+    def trace_device(self, d_rays_ptr, n, d_hits_ptr, stream=None):
+        _check(lib().psy_trace_device(self.scene.h, d_rays_ptr, n, d_hits_ptr, stream))
+
+    def rays_traced(self):
+        v = C.c_uint64()
+        _check(lib().psy_rays_traced(self.scene.h, C.byref(v)))
+        return v.value
+
+
+class Renderer:
+    """Renderer::render over the GPU scene: XYZ image (height, width, 3)."""
+
+    def __init__(self, scene):
+        self.scene = scene
+
+    def render(self, crop=None):
+        img = np.zeros((self.scene.height, self.scene.width, 3), dtype=np.float32)
+        st = abi.PsyRenderStats()
+        cr = (C.c_uint32 * 4)(*crop) if crop is not None else None
+        _check(lib().psy_render_image(self.scene.h, cr, img.ctypes.data, C.byref(st)))
+        return img, st.as_dict()
+
+    def render_device(self, d_xyz_ptr, stream=None, crop=None, stats=False):
+        st = abi.PsyRenderStats() if stats else None
+        cr = (C.c_uint32 * 4)(*crop) if crop is not None else None
+        _check(lib().psy_render_image_device(self.scene.h, cr, d_xyz_ptr, stream, C.byref(st) if stats else None))
+        return st.as_dict() if stats else None
+
+    def render_bucket(self, x, y, w, h, spp=None, seed=None):
+        out = np.zeros((h, w, 3), dtype=np.float32)
+        b = abi.PsyBucket(x, y, w, h)
+        st = abi.PsyRenderStats()
+        _check(lib().psy_render_bucket(self.scene.h, C.byref(b), spp if spp is not None else self.scene.spp,
+                                       seed if seed is not None else self.scene.data.seed, out.ctypes.data,
+                                       C.byref(st)))
+        return out, st.as_dict()

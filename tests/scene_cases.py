@@ -1,0 +1,77 @@
+"""Small seeded scenes and ray sets shared by the parity tests (sizes the CPU
+oracle finishes in seconds)."""
+import math
+
+import numpy as np
+
+from psychopath_gb300 import abi, scenes
+
+
+def cornell(w=32, h=32, spp=4, bounces=2):
+    return scenes.cornell_box(w, h, spp, max_bounces=bounces)
+
+
+def sphere_small(w=32, h=18, spp=4, bounces=6, level=4):
+    return scenes.mesh_stress(w, h, spp, max_bounces=bounces, level=level)
+
+
+def motion_small(w=32, h=18, spp=4, bounces=2, n=40, level=3, lights=8):
+    return scenes.motion_instances(w, h, spp, max_bounces=bounces, n_instances=n, level=level, n_lights=lights)
+
+
+def grid_small(nx=64, ny=32):
+    return scenes.grid_mesh(nx, ny)
+
+
+def random_rays(n, lo, hi, seed, time_random=False, occl_frac=0.0, max_t=None):
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    r = scenes.rays_array(o, d)
+    if time_random:
+        r["time"] = rng.random(n).astype(np.float32)
+        r["time"][:8] = np.array([0.0, 1.0, 0.5, 0.25, 0.75, 1.0, 0.0, 0.999], dtype=np.float32)
+    if occl_frac > 0:
+        r["flags"] = (rng.random(n) < occl_frac).astype(np.uint32) * abi.PSY_RAY_OCCLUSION
+    if max_t is not None:
+        r["max_t"] = rng.uniform(0.0, max_t, n).astype(np.float32)
+    return r
+
+
+def targeted_rays(n, targets_lo, targets_hi, origins_lo, origins_hi, seed, time_random=False):
+    """Rays from random origins toward random targets (most of them hit)."""
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(origins_lo, origins_hi, (n, 3))
+    t = rng.uniform(targets_lo, targets_hi, (n, 3))
+    d = (t - o)
+    r = scenes.rays_array(o.astype(np.float32), d.astype(np.float32))
+    if time_random:
+        r["time"] = rng.random(n).astype(np.float32)
+    return r
+
+
+def compare_hits(hg, ho, near_edge_eps=1e-4):
+    """Returns a dict of agreement statistics between GPU (hg) and oracle (ho)
+    PsyHit arrays.  Mismatched primitive ids are allowed only at near-edge
+    hits (a barycentric below near_edge_eps) or exact t ties."""
+    kind_ok = hg["kind"] == ho["kind"]
+    surf = (ho["kind"] >= abi.PSY_HIT_SURFACE) & kind_ok
+    same_prim = (hg["prim"] == ho["prim"]) & (hg["inst"] == ho["inst"])
+    t_o = ho["t"].astype(np.float64)
+    t_g = hg["t"].astype(np.float64)
+    rel = np.abs(t_g - t_o) / np.maximum(np.abs(t_o), 1e-30)
+    bmin_o = np.minimum(np.minimum(ho["b0"], ho["b1"]), ho["b2"])
+    bmin_g = np.minimum(np.minimum(hg["b0"], hg["b1"]), hg["b2"])
+    near_edge = (np.abs(bmin_o) < near_edge_eps) | (np.abs(bmin_g) < near_edge_eps)
+    tie = rel <= 1e-6
+    unexplained = surf & ~same_prim & ~(near_edge | tie)
+    return {
+        "n": len(ho),
+        "kind_mismatch": int((~kind_ok).sum()),
+        "surface": int(surf.sum()),
+        "prim_mismatch": int((surf & ~same_prim).sum()),
+        "unexplained": int(unexplained.sum()),
+        "t_max_rel": float(rel[surf & same_prim].max()) if (surf & same_prim).any() else 0.0,
+        "t_bit_exact": float(np.mean(hg["t"][surf & same_prim] == ho["t"][surf & same_prim])) if (surf & same_prim).any() else 1.0,
+        "occluded": int((ho["kind"] == abi.PSY_HIT_OCCLUDE).sum()),
+    }

@@ -1,0 +1,131 @@
+"""Tracer::trace parity: the GPU closest-hit / any-hit results against the
+oracle's packet traversal on the same rays, hit by hit.  Primitive and
+instance ids must agree except at near-edge hits and exact t ties, and t must
+agree to 1e-5 relative (it is bit-exact in practice: same arithmetic)."""
+import numpy as np
+import pytest
+
+from oracle.runner import OracleScene
+from psychopath_gb300 import abi, gpu
+
+from . import scene_cases as sc
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(scene_data, rays, bounds="fp32", full=False):
+    g = gpu.Scene(scene_data, bounds=bounds)
+    o = OracleScene(scene_data)
+    tr = gpu.Tracer(g)
+    if full:
+        hg, fg = tr.trace(rays, full=True)
+    else:
+        hg, fg = tr.trace(rays), None
+    ho, fo, _, _ = o.trace(rays, threads=8, full=full)
+    assert tr.rays_traced() == len(rays)
+    g.close()
+    return hg, ho, fg, fo
+
+
+def _assert_parity(st, min_surface=1):
+    assert st["kind_mismatch"] == 0, st
+    assert st["unexplained"] == 0, st
+    assert st["surface"] >= min_surface, st
+    assert st["t_max_rel"] <= 1e-5, st
+
+
+def test_cornell_random_rays(gpu_lib):
+    rays = sc.random_rays(20000, [-0.95, 0.05, -0.95], [0.95, 1.95, 0.95], seed=1)
+    hg, ho, _, _ = _run(sc.cornell(), rays)
+    st = sc.compare_hits(hg, ho)
+    _assert_parity(st, 15000)
+    assert st["t_bit_exact"] == 1.0, st
+
+
+def test_cornell_occlusion_and_max_t(gpu_lib):
+    rays = sc.random_rays(20000, [-0.95, 0.05, -0.95], [0.95, 1.95, 0.95], seed=2, occl_frac=0.5, max_t=3.0)
+    hg, ho, _, _ = _run(sc.cornell(), rays)
+    st = sc.compare_hits(hg, ho)
+    _assert_parity(st, 100)
+    assert st["occluded"] > 1000
+
+
+def test_displaced_sphere(gpu_lib):
+    s = sc.sphere_small(level=5)
+    rays = sc.targeted_rays(30000, [-1.1, -0.1, -1.1], [1.1, 2.1, 1.1], [-4, 0.05, -4], [4, 4, 4], seed=3)
+    hg, ho, _, _ = _run(s, rays)
+    st = sc.compare_hits(hg, ho)
+    _assert_parity(st, 20000)
+    assert st["prim_mismatch"] <= 5, st
+
+
+def test_motion_instances(gpu_lib):
+    s = sc.motion_small()
+    rays = sc.targeted_rays(30000, [-50, -50, -50], [50, 50, 50], [-60, -60, 60], [60, 60, 95], seed=4,
+                            time_random=True)
+    hg, ho, _, _ = _run(s, rays)
+    st = sc.compare_hits(hg, ho)
+    _assert_parity(st, 200)
+
+
+def test_grid_incoherent(gpu_lib):
+    s, P, F = sc.grid_small()
+    from psychopath_gb300 import scenes
+    rays = scenes.incoherent_rays(P, F, 30000, seed=7)
+    hg, ho, _, _ = _run(s, rays)
+    st = sc.compare_hits(hg, ho)
+    _assert_parity(st, 1000)
+
+
+def test_grid_coherent(gpu_lib):
+    s, P, F = sc.grid_small()
+    from psychopath_gb300 import scenes
+    rays = scenes.coherent_rays(128)
+    hg, ho, _, _ = _run(s, rays)
+    st = sc.compare_hits(hg, ho)
+    _assert_parity(st, 5000)
+
+
+def test_full_surface_data(gpu_lib):
+    rays = sc.random_rays(5000, [-0.95, 0.05, -0.95], [0.95, 1.95, 0.95], seed=5)
+    hg, ho, fg, fo = _run(sc.cornell(), rays, full=True)
+    same = (hg["kind"] >= abi.PSY_HIT_SURFACE) & (hg["kind"] == ho["kind"]) & (hg["prim"] == ho["prim"]) & (
+        hg["inst"] == ho["inst"])
+    assert same.sum() > 3000
+    for f in ("pos", "nor", "nor_g"):
+        np.testing.assert_allclose(fg[f][same], fo[f][same], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(fg["pos_err"][same], fo["pos_err"][same], rtol=1e-6)
+    np.testing.assert_allclose(fg["sample_pdf"][same], fo["sample_pdf"][same], rtol=1e-4, atol=1e-7)
+    assert np.array_equal(fg["shader"][same], fo["shader"][same])
+
+
+@pytest.mark.parametrize("case", ["sphere", "motion"])
+def test_fp16_bounds_conservative(gpu_lib, case):
+    """FP16 outward-rounded child bounds lose no hit: results equal FP32's."""
+    if case == "sphere":
+        s = sc.sphere_small(level=5)
+        rays = sc.targeted_rays(20000, [-1.1, -0.1, -1.1], [1.1, 2.1, 1.1], [-4, 0.05, -4], [4, 4, 4], seed=6)
+    else:
+        s = sc.motion_small()
+        rays = sc.targeted_rays(20000, [-50, -50, -50], [50, 50, 50], [-60, -60, 60], [60, 60, 95], seed=8,
+                                time_random=True)
+    g32 = gpu.Scene(s)
+    g16 = gpu.Scene(s, bounds="fp16")
+    h32 = gpu.Tracer(g32).trace(rays)
+    h16 = gpu.Tracer(g16).trace(rays)
+    st = sc.compare_hits(h16, h32)
+    _assert_parity(st, 100)
+
+
+def test_empty_batch_and_misses(gpu_lib):
+    s = sc.cornell()
+    g = gpu.Scene(s)
+    tr = gpu.Tracer(g)
+    h = tr.trace(np.zeros(0, dtype=abi.ray_dtype()))
+    assert len(h) == 0
+    # rays leaving through the open front face miss everything
+    from psychopath_gb300 import scenes
+    rays = scenes.rays_array(np.array([[0, 1, 0.5]] * 4, dtype=np.float32),
+                             np.array([[0, 0, 1], [0.01, 0, 1], [0, 0.01, 1], [0.1, 0.1, 1]], dtype=np.float32))
+    h = tr.trace(rays)
+    assert (h["kind"] == abi.PSY_HIT_MISS).all()

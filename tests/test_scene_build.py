@@ -1,0 +1,43 @@
+"""The GPU library's host-side BVH build produces the reference's trees: the
+same triangle order after the SAH build and the same BVH4 node count as the
+oracle's restatement of src/accel/bvh_base.rs + src/accel/bvh4.rs (runs on
+CPU: only the host build)."""
+import numpy as np
+import pytest
+
+from oracle.runner import OracleScene
+from psychopath_gb300 import gpu
+
+from . import scene_cases as sc
+
+
+@pytest.mark.parametrize("case", ["cornell", "sphere", "motion", "grid"])
+def test_bvh_identical_to_oracle(gpu_lib, case):
+    if case == "cornell":
+        s = sc.cornell()
+    elif case == "sphere":
+        s = sc.sphere_small(level=4)
+    elif case == "motion":
+        s = sc.motion_small()
+    else:
+        s, _, _ = sc.grid_small()
+    o = OracleScene(s)
+    for obj, od in enumerate(s.objects):
+        if od["kind"] != 0:
+            continue
+        order_g, nodes_g, max_stack = gpu.host_build_info(s, obj)
+        order_o, nodes_o = o.mesh_bvh_info(obj)
+        assert np.array_equal(order_g, order_o), (case, obj)
+        assert nodes_g == nodes_o, (case, obj, nodes_g, nodes_o)
+        assert 0 < max_stack <= 192
+
+
+def test_invalid_descriptions_rejected(gpu_lib):
+    import ctypes as C
+    from psychopath_gb300 import abi
+    s = sc.cornell()
+    s.objects[0]["indices"] = s.objects[0]["indices"].copy()
+    s.objects[0]["indices"][0, 0] = 10 ** 6  # index out of range
+    with pytest.raises(gpu.PsyError) as e:
+        gpu.host_build_info(s, 0)
+    assert e.value.code == abi.PSY_E_INVALID
