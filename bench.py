@@ -1,0 +1,417 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 tracing path on the mesh-stress workload.
+
+One step = one full frame of the hot path: camera rays for every (pixel,
+sample), the wavefront light-path loop (trace + LightPath::next) and the XYZ
+accumulation, for a 1920x1080, 64 spp, max-6-bounce render of a seeded
+noise-displaced level-8 icosphere (1,310,720 tris) on a 2-tri ground plane
+lit by a sphere light and a 0.5-degree sun (GGX, roughness U(0.1, 0.8)).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--bounds fp32|fp16] [--workload mesh_stress|cornell|motion]
+
+Prints one JSON line on rank 0.  --impl reference times the CPU oracle (a
+restatement of the reference's CPU renderer; the Rust binary cannot be built
+here) on all host threads, each step a bounded sample of the same frame.
+Multi-GPU: every rank renders its own full frame (weak scaling, no
+collective on the data path); value = all ranks' samples / max time.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--bounds", default="fp32", choices=["fp32", "fp16"])
+    ap.add_argument("--workload", default="mesh_stress", choices=["mesh_stress", "cornell", "motion", "traversal"])
+    ap.add_argument("--rays", type=int, default=1 << 24, help="rays per set of the traversal microbenchmark")
+    ap.add_argument("--level", type=int, default=8, help="icosphere subdivision level of mesh_stress")
+    ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (profiling on smaller cases)")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_scene(args):
+    from psychopath_gb300 import scenes
+    if args.workload == "mesh_stress":
+        sd = scenes.mesh_stress(level=args.level)
+        desc = ("mesh_stress: level-%d noise-displaced icosphere (%d tris) + 2-tri ground, sphere light r=0.1 + "
+                "0.5 deg sun disc, GGX roughness U(0.1,0.8); 1920x1080, 64 spp, max 6 bounces, seed 0"
+                % (args.level, sd.num_tris))
+    elif args.workload == "cornell":
+        sd = scenes.cornell_box()
+        desc = "cornell: 5 wall quads + 2 rotated boxes (34 tris), 0.25x0.25 rect light; 512x512, 16 spp, max 4 bounces"
+    else:
+        sd = scenes.motion_instances()
+        desc = ("motion: 2000 motion-blurred instances of a 20480-tri displaced sphere + deforming mesh, 64 sphere "
+                "lights; 1280x720, 32 spp")
+    return sd, desc
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_render_sample(sd, target_seconds, threads):
+    """Time the CPU oracle on a bounded sample of the frame: every k-th bucket
+    of the reference's Hilbert bucket order, k chosen so the run takes about
+    target_seconds on `threads` host threads."""
+    from oracle.runner import OracleScene
+    o = OracleScene(sd)
+    stride = 4096
+    t0 = time.perf_counter()
+    _, st = o.render_sampled(stride, threads=threads)
+    dt = time.perf_counter() - t0
+    while dt < 0.5 and stride > 1:
+        stride = max(1, stride // 4)
+        t0 = time.perf_counter()
+        _, st = o.render_sampled(stride, threads=threads)
+        dt = time.perf_counter() - t0
+    stride = max(1, int(round(stride * dt / target_seconds)))
+    t0 = time.perf_counter()
+    _, st = o.render_sampled(stride, threads=threads)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"samples": st["samples"], "rays": st["ray_count"], "seconds": dt, "stride": stride}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sd, desc = make_scene(args)
+    if args.spp:
+        sd.spp = args.spp
+    threads = os.cpu_count() or 1
+    from oracle.runner import OracleScene
+    o = OracleScene(sd)
+    # calibrate the per-step sample: every stride-th bucket, ~target seconds
+    stride = 4096
+    t0 = time.perf_counter()
+    o.render_sampled(stride, threads=threads)
+    dt = time.perf_counter() - t0
+    while dt < 0.3 and stride > 1:
+        stride = max(1, stride // 4)
+        t0 = time.perf_counter()
+        o.render_sampled(stride, threads=threads)
+        dt = time.perf_counter() - t0
+    per_step_target = max(2.0, min(12.0, 100.0 / max(1, args.steps + args.warmup)))
+    stride = max(1, int(round(stride * dt / per_step_target)))
+    for _ in range(args.warmup):
+        o.render_sampled(stride, threads=threads)
+    samples, rays, secs = 0, 0, 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, st = o.render_sampled(stride, threads=threads)
+        secs += time.perf_counter() - t0
+        samples += st["samples"]
+        rays += st["ray_count"]
+    value = samples / secs
+    sample_desc = "every %d-th bucket (Hilbert order, 8x8 px x 64 spp) of the frame per step" % stride
+    line = {
+        "impl": "reference",
+        "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": desc, "bounds": "f32 (CPU)"},
+        "mrays_per_s": rays / secs / 1e6,
+        "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
+                         "sample": sample_desc},
+        "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU oracle (C++ restatement of the reference's CPU renderer); the Rust reference cannot be built here",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU
+def run_ours(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from psychopath_gb300 import build, gpu
+    build.build()
+    sd, desc = make_scene(args)
+    sd.seed = sd.seed + rank  # independent sample sets per replica
+    if args.spp:
+        sd.spp = args.spp
+    t0 = time.perf_counter()
+    scene = gpu.Scene(sd, bounds=args.bounds)
+    build_s = time.perf_counter() - t0
+    W, H, spp = sd.width, sd.height, sd.spp
+    rend = gpu.Renderer(scene)
+    xyz = torch.zeros(H * W * 3, dtype=torch.float32, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    for _ in range(args.warmup):
+        rend.render_device(xyz.data_ptr(), stream=sp)
+    torch.cuda.synchronize()
+
+    # traversal work counters for the roofline (one extra, untimed frame)
+    scene.counters(True)
+    rend.render_device(xyz.data_ptr(), stream=sp)
+    torch.cuda.synchronize()
+    n_nodes, n_tris, n_rays_c = scene.counters(False)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    trace_s = 0.0
+    rays = 0
+    samples = 0
+    ev0.record(stream)
+    for _ in range(args.steps):
+        flush.zero_()
+        st = rend.render_device(xyz.data_ptr(), stream=sp, stats=True)
+        trace_s += st["trace_time"]
+        rays += st["ray_count"]
+        samples += st["samples"]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    t = torch.tensor([elapsed], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    elapsed = float(t.item())
+    total_samples = samples * world
+    value = total_samples / elapsed
+
+    # end to end through the public C ABI with a host image buffer
+    img = np.zeros((H, W, 3), dtype=np.float32)
+    barrier()
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        img, _ = rend.render()
+    e_el = time.perf_counter() - e0
+    te = torch.tensor([e_el], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = (W * H * spp * args.steps * world) / float(te.item())
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # roofline: algorithmic bytes of the traversal kernel (per ray: ray in
+    # 32 B + hit out 16 B + 128 B per BVH4 node test + 36 B per triangle
+    # test), over the measured traversal-kernel time of the timed frames
+    node_bytes = 64 if args.bounds == "fp16" else 128
+    frames = args.steps
+    alg_bytes_frame = 48.0 * n_rays_c + node_bytes * n_nodes + 36.0 * n_tris
+    achieved = alg_bytes_frame * frames / max(trace_s, 1e-12) / 1e9
+    peaks_path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        try:
+            peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    traffic = None
+    tr_path = os.path.join(HERE, "profiles", "trace_traffic.json")
+    if os.path.exists(tr_path):
+        try:
+            tj = json.load(open(tr_path))
+            if tj.get("workload") == args.workload and tj.get("bounds") == args.bounds:
+                traffic = tj.get("dram_bytes_per_ray") and tj["dram_bytes_per_ray"] * n_rays_c
+        except Exception:
+            traffic = None
+    rows = max(1, (1 << 24) // (W * spp))
+    waves = math.ceil(H / rows)
+    iters = 2 * sd.max_bounces + 3
+    launches_per_frame = waves * (1 + 2 * iters + 1 + 1)
+    line = {
+        "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": desc, "bounds": args.bounds, "l2": "256 MiB written between steps; path state per "
+                   "wave ~3 GB > L2", "scene_build_s": round(build_s, 3), "scene_device_bytes": scene.device_bytes()},
+        "mrays_per_s": rays * world / elapsed / 1e6,
+        "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": W * H * 3 * 4,
+                "note": "psy_render_image (host XYZ buffer, D2H inside the timed loop); the scene is resident (uploaded "
+                        "once at psy_scene_create), so a step has no input upload"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_src, "kernel": "k_trace_queue",
+                     "per_frame": {"rays": n_rays_c, "node_tests": n_nodes, "tri_tests": n_tris,
+                                   "trace_kernel_s": trace_s / frames}},
+        "clocks": clk,
+        "gpu_launches": launches_per_frame * args.steps,
+    }
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cb = cpu_render_sample(sd, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": cb["samples"] / cb["seconds"], "unit": "samples/s", "cores": threads,
+                                "kind": "port", "sample": "every %d-th bucket (Hilbert order) of the frame: %d samples, "
+                                "%.1f s" % (cb["stride"], cb["samples"], cb["seconds"])}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ---------------------------------------------------------------- traversal microbenchmark
+def run_traversal(args):
+    """16M coherent (pinhole) and 16M incoherent (cosine-hemisphere from random
+    surface points, seed 7) rays against the 2048x1024-quad displaced grid
+    (4,194,304 tris): Mrays/s, algorithmic GB/s, closest-hit agreement with the
+    CPU oracle on a sample of each set."""
+    import numpy as np
+    import torch
+    from psychopath_gb300 import abi, gpu, scenes
+    from oracle.runner import OracleScene
+    torch.cuda.set_device(0)
+    sd, P, F = scenes.grid_mesh(2048, 1024)
+    n_side = int(round(math.sqrt(args.rays)))
+    sets = {"coherent": scenes.coherent_rays(n_side), "incoherent": scenes.incoherent_rays(P, F, n_side * n_side, seed=7)}
+    g = gpu.Scene(sd, bounds=args.bounds)
+    tr = gpu.Tracer(g)
+    o = OracleScene(sd)
+    peaks_path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    peak = float(json.load(open(peaks_path))["hbm_gbs"]) if os.path.exists(peaks_path) else 6800.0
+    node_bytes = 64 if args.bounds == "fp16" else 128
+    stream = torch.cuda.current_stream()
+    out = {}
+    for name, rays in sets.items():
+        n = len(rays)
+        d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+        d_hits = torch.zeros(n * 32, dtype=torch.uint8, device="cuda")
+        for _ in range(args.warmup):
+            tr.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+        g.counters(True)
+        tr.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+        gn, gt, gr = g.counters(False)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            tr.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3 / args.steps
+        hits = d_hits.cpu().numpy().view(abi.hit_dtype())
+        # oracle on a sample: agreement and per-ray node / triangle tests
+        idx = np.random.default_rng(11).choice(n, size=min(n, 200000), replace=False)
+        ho, _, on, ot = o.trace(rays[idx], threads=os.cpu_count() or 1)
+        hg = hits[idx]
+        surf = ho["kind"] >= abi.PSY_HIT_SURFACE
+        same = (hg["kind"] == ho["kind"]) & (~surf | ((hg["prim"] == ho["prim"]) & (hg["inst"] == ho["inst"])))
+        bmin = np.minimum(np.minimum(ho["b0"], ho["b1"]), ho["b2"])
+        near = surf & (np.abs(bmin) < 1e-4)
+        n_node = on / len(idx)
+        n_tri = ot / len(idx)
+        alg = 32 + 16 + n_node * node_bytes + n_tri * 36
+        gbs = alg * n / sec / 1e9
+        out[name] = {"mrays_per_s": n / sec / 1e6, "ms_per_launch": sec * 1e3, "rays": n,
+                     "alg_bytes_per_ray": alg, "achieved_gbs": gbs, "frac": gbs / peak,
+                     "oracle_node_tests_per_ray": n_node, "oracle_tri_tests_per_ray": n_tri,
+                     "gpu_node_tests_per_ray": gn / max(1, gr), "gpu_tri_tests_per_ray": gt / max(1, gr),
+                     "hit_agreement": float(same.mean()), "disagree_not_near_edge": int((~same & ~near).sum()),
+                     "sample": len(idx), "hit_fraction": float(surf.mean())}
+        del d_rays, d_hits
+    inc = out["incoherent"]
+    line = {"metric": "Mrays/s (incoherent)", "value": inc["mrays_per_s"], "unit": "Mrays/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": inc["ms_per_launch"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded grid mesh and rays)",
+            "config": {"workload": "traversal: 2048x1024-quad displaced grid (4,194,304 tris), %d rays per set" % len(sets["incoherent"]),
+                       "bounds": args.bounds},
+            "roofline": {"bound": "hbm", "achieved": inc["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": inc["frac"], "traffic": None, "kernel": "k_trace_rays"},
+            "sets": out}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.workload == "traversal":
+        return run_traversal(args)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

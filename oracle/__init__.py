@@ -44,6 +44,7 @@ def lib():
         L.psyo_scene_destroy.argtypes = [vp]
         L.psyo_trace.argtypes = [vp, vp, u32, vp, vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), u32]
         L.psyo_render.argtypes = [vp, u32, u32, vp, u32, vp, vp]
+        L.psyo_render_sampled.argtypes = [vp, u32, u32, vp, u32, u32, vp, vp]
         L.psyo_render_paths.argtypes = [vp, vp, vp, vp, vp]
         L.psyo_hash_u32.restype = u32
         L.psyo_hash_u32.argtypes = [u32, u32]

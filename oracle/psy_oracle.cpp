@@ -1840,6 +1840,11 @@ extern "C" uint32_t psyo_hilbert_xy2d(uint32_t x, uint32_t y) {
 // Renderer::render (src/renderer.rs:76-191)
 extern "C" int psyo_render(PsyoScene *s, uint32_t spb, uint32_t nthreads, const uint32_t *crop, uint32_t max_buckets,
                            float *xyz, PsyRenderStats *stats) {
+    return psyo_render_sampled(s, spb, nthreads, crop, 1, max_buckets, xyz, stats);
+}
+
+extern "C" int psyo_render_sampled(PsyoScene *s, uint32_t spb, uint32_t nthreads, const uint32_t *crop,
+                                   uint32_t bucket_stride, uint32_t max_buckets, float *xyz, PsyRenderStats *stats) {
     if (!s || !xyz) return PSY_E_INVALID;
     if (nthreads == 0) nthreads = 1;
     if (spb == 0) spb = 4096;
@@ -1866,6 +1871,11 @@ extern "C" int psyo_render(PsyoScene *s, uint32_t spb, uint32_t nthreads, const 
         size_t h = (height >= y) ? std::min(bd, height - y) : bd;
         if (x < width && y < height && w > 0 && h > 0)
             jobs.push_back(BucketJob{(uint32_t)(sx + x), (uint32_t)(sy + y), (uint32_t)w, (uint32_t)h});
+    }
+    if (bucket_stride > 1) {
+        std::vector<BucketJob> kept;
+        for (size_t j = 0; j < jobs.size(); j += bucket_stride) kept.push_back(jobs[j]);
+        jobs.swap(kept);
     }
     if (max_buckets && jobs.size() > max_buckets) jobs.resize(max_buckets);
     std::memset(xyz, 0, sizeof(float) * W * H * 3);

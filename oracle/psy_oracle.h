@@ -36,6 +36,11 @@ int psyo_trace(PsyoScene *s, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySu
 int psyo_render(PsyoScene *s, uint32_t spb, uint32_t nthreads, const uint32_t *crop,
                 uint32_t max_buckets, float *xyz, PsyRenderStats *stats);
 
+/* As psyo_render, keeping only every bucket_stride-th bucket of the Hilbert
+ * order (a sample spread over the whole image). */
+int psyo_render_sampled(PsyoScene *s, uint32_t spb, uint32_t nthreads, const uint32_t *crop, uint32_t bucket_stride,
+                        uint32_t max_buckets, float *xyz, PsyRenderStats *stats);
+
 /* Render one bucket and return every sample's final path colour (4 floats)
  * and hero wavelength, indexed ((y - b.y) * b.w + (x - b.x)) * spp + si,
  * plus the number of rays each sample traced. */

@@ -52,6 +52,17 @@ class OracleScene:
             raise RuntimeError("psyo_render failed: %d" % rc)
         return img, st.as_dict()
 
+    def render_sampled(self, stride, max_buckets=0, spb=4096, threads=1):
+        """Render every stride-th bucket of the Hilbert order (a bounded sample
+        of the frame spread over the image)."""
+        from psychopath_gb300 import abi
+        img = np.zeros((self.height, self.width, 3), dtype=np.float32)
+        st = abi.PsyRenderStats()
+        rc = _lib().psyo_render_sampled(self.h, spb, threads, None, stride, max_buckets, img.ctypes.data, C.byref(st))
+        if rc != 0:
+            raise RuntimeError("psyo_render_sampled failed: %d" % rc)
+        return img, st.as_dict()
+
     def render_paths(self, x, y, w, h):
         from psychopath_gb300 import abi
         n = w * h * self.spp

@@ -69,6 +69,8 @@ struct PsyScene {
     size_t cap_xyz = 0;
     uint32_t wave_paths = 1u << 24;      // paths per wave
     int grid = 0;                        // persistent grid for queue kernels (0: size by queue)
+    bool counting = false;               // accumulate traversal counters during renders
+    unsigned long long *d_counters = nullptr;  // node visits, triangle tests, rays
     std::mutex mu;
 };
 
@@ -126,6 +128,13 @@ static int ensure_trace(PsyScene *s, size_t n, bool full) {
     CK(cudaMalloc((void **)&s->d_hits, cap * sizeof(PsyHit)), "cudaMalloc hits");
     if (full) CK(cudaMalloc((void **)&s->d_full, cap * sizeof(PsySurfaceHit)), "cudaMalloc full hits");
     s->cap_rays = cap;
+    return PSY_OK;
+}
+
+static int ensure_counters(PsyScene *s) {
+    if (s->d_counters) return PSY_OK;
+    CK(cudaMalloc((void **)&s->d_counters, 3 * sizeof(unsigned long long)), "cudaMalloc counters");
+    CK(cudaMemsetAsync(s->d_counters, 0, 3 * sizeof(unsigned long long), s->stream), "memset counters");
     return PSY_OK;
 }
 
@@ -233,6 +242,7 @@ int psy_scene_destroy(PsyScene *s) {
     if (s->d_full) cudaFree(s->d_full);
     if (s->d_xyz) cudaFree(s->d_xyz);
     if (s->d_err) cudaFree(s->d_err);
+    if (s->d_counters) cudaFree(s->d_counters);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return PSY_OK;
@@ -247,7 +257,13 @@ int psy_scene_device_bytes(const PsyScene *s, uint64_t *bytes) {
 int psy_trace_device(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyHit *d_hits, void *stream) {
     if (!s || (n && (!d_rays || !d_hits))) return fail(PSY_E_INVALID, "null argument");
     cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
-    cudaError_t e = launch_trace_rays(s->g, d_rays, n, d_hits, nullptr, s->stack, 128, s->d_err, st);
+    unsigned long long *ctr = nullptr;
+    if (s->counting) {
+        int r = ensure_counters(s);
+        if (r != PSY_OK) return r;
+        ctr = s->d_counters;
+    }
+    cudaError_t e = launch_trace_rays(s->g, d_rays, n, d_hits, nullptr, s->stack, 128, s->d_err, ctr, st);
     if (e != cudaSuccess) return cuda_fail(e, "trace launch");
     s->rays_traced += n;
     return PSY_OK;
@@ -261,7 +277,14 @@ int psy_trace(PsyScene *s, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurf
     if (r != PSY_OK) return r;
     cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
     CK(cudaMemcpyAsync(s->d_rays, rays, (size_t)n * sizeof(PsyRay), cudaMemcpyHostToDevice, st), "copy rays");
-    CK(launch_trace_rays(s->g, s->d_rays, n, s->d_hits, full_out ? s->d_full : nullptr, s->stack, 128, s->d_err, st),
+    unsigned long long *ctr = nullptr;
+    if (s->counting) {
+        r = ensure_counters(s);
+        if (r != PSY_OK) return r;
+        ctr = s->d_counters;
+    }
+    CK(launch_trace_rays(s->g, s->d_rays, n, s->d_hits, full_out ? s->d_full : nullptr, s->stack, 128, s->d_err, ctr,
+                         st),
        "trace launch");
     CK(cudaMemcpyAsync(hits, s->d_hits, (size_t)n * sizeof(PsyHit), cudaMemcpyDeviceToHost, st), "copy hits");
     if (full_out)
@@ -293,13 +316,20 @@ static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint
     int r = ensure_render(s, (uint32_t)max_paths);
     if (r != PSY_OK) return r;
     uint32_t iters = 2 * s->g.max_bounces + 3;
-    cudaEvent_t ev[4];
     bool timing = stats != nullptr;
+    // events: camera start/end, per iteration trace start/end + shade end, accumulate end
+    std::vector<cudaEvent_t> ev;
     if (timing) {
+        ev.resize(3 + 3 * iters);
         for (auto &e : ev) cudaEventCreate(&e);
         CK(cudaMemsetAsync(s->d_raycount, 0, 8, st), "memset");
     }
-    double t_gen = 0, t_loop = 0, t_acc = 0;
+    if (s->counting) {
+        int rr = ensure_counters(s);
+        if (rr != PSY_OK) return rr;
+    }
+    unsigned long long *ctr = s->counting ? s->d_counters : nullptr;
+    double t_gen = 0, t_trace = 0, t_shade = 0, t_acc = 0;
     auto t0 = std::chrono::steady_clock::now();
     for (uint32_t y = y0; y < y0 + h; y += rows) {
         Wave wv;
@@ -311,25 +341,34 @@ static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint
         if (timing) cudaEventRecord(ev[1], st);
         int cur = 0;
         for (uint32_t it = 0; it < iters; it++) {
-            CK(launch_trace_queue(s->g, s->R, s->H, s->queue[cur], s->counts + cur, n, s->stack, 128, s->grid, s->d_err, st),
+            if (timing) cudaEventRecord(ev[2 + 3 * it], st);
+            CK(launch_trace_queue(s->g, s->R, s->H, s->queue[cur], s->counts + cur, n, s->stack, 128, s->grid, s->d_err,
+                                  ctr, st),
                "trace launch");
+            if (timing) cudaEventRecord(ev[3 + 3 * it], st);
             CK(cudaMemsetAsync(s->counts + (cur ^ 1), 0, 4, st), "memset count");
             CK(launch_shade(s->g, wv, s->P, s->R, s->H, s->queue[cur], s->counts + cur, n, s->queue[cur ^ 1],
                             s->counts + (cur ^ 1), 128, s->grid, st),
                "shade launch");
+            if (timing) cudaEventRecord(ev[4 + 3 * it], st);
             cur ^= 1;
         }
-        if (timing) cudaEventRecord(ev[2], st);
         CK(launch_accumulate(s->g, wv, s->P, d_xyz, img_w, st), "accumulate launch");
         if (timing) {
-            cudaEventRecord(ev[3], st);
+            cudaEventRecord(ev[2 + 3 * iters], st);
             CK(launch_count_rays(s->P, n, s->d_raycount, st), "count launch");
-            CK(cudaEventSynchronize(ev[3]), "event sync");
-            float a, b, c;
-            cudaEventElapsedTime(&a, ev[0], ev[1]);
-            cudaEventElapsedTime(&b, ev[1], ev[2]);
-            cudaEventElapsedTime(&c, ev[2], ev[3]);
-            t_gen += a * 1e-3; t_loop += b * 1e-3; t_acc += c * 1e-3;
+            CK(cudaEventSynchronize(ev[2 + 3 * iters]), "event sync");
+            float ms;
+            cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            t_gen += ms * 1e-3;
+            for (uint32_t it = 0; it < iters; it++) {
+                cudaEventElapsedTime(&ms, ev[2 + 3 * it], ev[3 + 3 * it]);
+                t_trace += ms * 1e-3;
+                cudaEventElapsedTime(&ms, ev[3 + 3 * it], ev[4 + 3 * it]);
+                t_shade += ms * 1e-3;
+            }
+            cudaEventElapsedTime(&ms, ev[1 + 3 * iters], ev[2 + 3 * iters]);
+            t_acc += ms * 1e-3;
             stats->samples += n;
         }
     }
@@ -339,7 +378,8 @@ static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint
         CK(cudaStreamSynchronize(st), "sync");
         stats->ray_count += rc;
         stats->initial_ray_generation_time += t_gen;
-        stats->trace_time += t_loop;  // trace + shade kernels of the wavefront loop
+        stats->trace_time += t_trace;
+        stats->ray_generation_time += t_shade;
         stats->sample_writing_time += t_acc;
         stats->total_time += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         for (auto &e : ev) cudaEventDestroy(e);
@@ -442,6 +482,26 @@ int psy_debug_scene_info(PsyScene *s, uint32_t *max_stack, uint32_t *nodes, uint
     if (max_stack) *max_stack = s->max_stack;
     if (nodes) *nodes = s->node_count;
     if (stack_variant) *stack_variant = (uint32_t)s->stack;
+    return PSY_OK;
+}
+// Traversal counters of renders: enable (and zero) or read them.
+int psy_debug_counters(PsyScene *s, int enable, uint64_t *nodes, uint64_t *tris, uint64_t *rays) {
+    if (!s) return fail(PSY_E_INVALID, "null");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->d_counters) {
+        unsigned long long h[3] = {0, 0, 0};
+        CK(cudaMemcpyAsync(h, s->d_counters, sizeof(h), cudaMemcpyDeviceToHost, s->stream), "copy counters");
+        CK(cudaStreamSynchronize(s->stream), "sync");
+        if (nodes) *nodes = h[0];
+        if (tris) *tris = h[1];
+        if (rays) *rays = h[2];
+        CK(cudaMemsetAsync(s->d_counters, 0, sizeof(h), s->stream), "memset counters");
+    } else {
+        if (nodes) *nodes = 0;
+        if (tris) *tris = 0;
+        if (rays) *rays = 0;
+    }
+    s->counting = enable != 0;
     return PSY_OK;
 }
 int psy_debug_set_launch(PsyScene *s, int grid, uint32_t wave_paths) {

@@ -192,8 +192,14 @@ DI bool sphere_hit(const GScene &S, const GInstance &in, V3 ol, V3 d, float tmax
 
 // Trace one ray.  `occl`: any-hit (shadow ray).  Returns false on stack
 // overflow (the scene needs a deeper stack than STACK).
-template <int STACK>
-DI bool trace_ray(const GScene &S, V3 o, V3 d, float tmax, float time, bool occl, HitRec &hit) {
+// Traversal work counters (ray x node tests and ray x triangle tests).
+struct TraceCount {
+    uint32_t nodes, tris;
+};
+
+template <int STACK, bool COUNT = false>
+DI bool trace_ray(const GScene &S, V3 o, V3 d, float tmax, float time, bool occl, HitRec &hit,
+                  TraceCount *cnt = nullptr) {
     hit.kind = PSY_HIT_MISS_K;
     if (S.top_root == PSY_REF_NONE) return true;
     Xf ident = xf_identity();
@@ -218,6 +224,7 @@ DI bool trace_ray(const GScene &S, V3 o, V3 d, float tmax, float time, bool occl
             uint4 ch;
             uint32_t m = S.use_fp16 ? node_hits_h(S, cur, lo, ldi, tmax, time, code, count, ch)
                                     : node_hits(S, cur, lo, ldi, tmax, time, code, count, ch);
+            if (COUNT) cnt->nodes++;
             if (m == 0) goto pop;
             uint32_t order = row[code];
             uint32_t next = PSY_REF_NONE;
@@ -276,12 +283,13 @@ DI bool trace_ray(const GScene &S, V3 o, V3 d, float tmax, float time, bool occl
                 }
             }
         } else {
-            uint32_t first = psy_leaf_first(cur), cnt = psy_leaf_count(cur);
-            for (uint32_t k = 0; k < cnt; k++) {
+            uint32_t first = psy_leaf_first(cur), ntri = psy_leaf_count(cur);
+            for (uint32_t k = 0; k < ntri; k++) {
                 uint32_t tri = first + k;
                 V3 p0, p1, p2;
                 fetch_tri(S, mesh, tri, time, has_xf, mat, p0, p1, p2);
                 float t, b0, b1, b2;
+                if (COUNT) cnt->tris++;
                 if (tri_intersect(o, pre, tmax, p0, p1, p2, t, b0, b1, b2)) {
                     if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
                     hit.kind = PSY_HIT_SURFACE_K; hit.prim = tri; hit.slot = slot;

@@ -161,92 +161,136 @@ __device__ void resolve_hit(const GScene &S, const HitRec &h, V3 o, V3 d, float 
 }
 
 // ------------------------------------------------------------------ ray tracing
-template <int STACK>
+template <int STACK, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_rays(GScene S, const PsyRay *__restrict__ rays, uint32_t n,
                                                     PsyHit *__restrict__ hits, PsySurfaceHit *__restrict__ full,
-                                                    int *err) {
+                                                    int *err, unsigned long long *counters) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float *r = reinterpret_cast<const float *>(rays + i);
-    V3 o = v3(r[0], r[1], r[2]), d = v3(r[3], r[4], r[5]);
-    float tmax = r[6], time = r[7];
-    uint32_t flags = reinterpret_cast<const uint32_t *>(r)[9];
-    HitRec h;
-    if (!trace_ray<STACK>(S, o, d, tmax, time, (flags & PSY_RAY_OCCLUSION) != 0, h)) {
-        atomicExch(err, PSY_E_OVERFLOW);
-        h.kind = PSY_HIT_MISS_K;
-    }
-    PsyHit out;
-    out.kind = h.kind;
-    out.prim = 0; out.inst = 0; out.t = 0.0f; out.b0 = 0.0f; out.b1 = 0.0f; out.b2 = 0.0f; out.pad = 0.0f;
-    if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
-        GInstance in = S.instances[h.slot];
-        out.prim = h.kind == PSY_HIT_SURFACE_K ? __ldg(S.tri_idx + h.prim).w : h.prim;
-        out.inst = in.id;
-        out.t = h.t; out.b0 = h.b0; out.b1 = h.b1; out.b2 = h.b2;
-    }
-    hits[i] = out;
-    if (full) {
-        PsySurfaceHit f;
-        f.hit = out;
-        f.shader = -1;
-        f.pos[0] = f.pos[1] = f.pos[2] = 0.0f;
-        f.nor[0] = f.nor[1] = f.nor[2] = 0.0f;
-        f.nor_g[0] = f.nor_g[1] = f.nor_g[2] = 0.0f;
-        f.pos_err = 0.0f;
-        f.sample_pdf = 0.0f;
-        if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
-            SurfData sd;
-            resolve_hit(S, h, o, d, time, sd);
-            f.pos[0] = sd.pos.x; f.pos[1] = sd.pos.y; f.pos[2] = sd.pos.z;
-            f.nor[0] = sd.nor.x; f.nor[1] = sd.nor.y; f.nor[2] = sd.nor.z;
-            f.nor_g[0] = sd.nor_g.x; f.nor_g[1] = sd.nor_g.y; f.nor_g[2] = sd.nor_g.z;
-            f.pos_err = sd.pos_err;
-            f.sample_pdf = sd.sample_pdf;
-            f.shader = sd.shader;
+    TraceCount tc{0, 0};
+    if (i < n) {
+        const float *r = reinterpret_cast<const float *>(rays + i);
+        V3 o = v3(r[0], r[1], r[2]), d = v3(r[3], r[4], r[5]);
+        float tmax = r[6], time = r[7];
+        uint32_t flags = reinterpret_cast<const uint32_t *>(r)[9];
+        HitRec h;
+        if (!trace_ray<STACK, COUNT>(S, o, d, tmax, time, (flags & PSY_RAY_OCCLUSION) != 0, h, &tc)) {
+            atomicExch(err, PSY_E_OVERFLOW);
+            h.kind = PSY_HIT_MISS_K;
         }
-        full[i] = f;
+        PsyHit out;
+        out.kind = h.kind;
+        out.prim = 0; out.inst = 0; out.t = 0.0f; out.b0 = 0.0f; out.b1 = 0.0f; out.b2 = 0.0f; out.pad = 0.0f;
+        if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
+            GInstance in = S.instances[h.slot];
+            out.prim = h.kind == PSY_HIT_SURFACE_K ? __ldg(S.tri_idx + h.prim).w : h.prim;
+            out.inst = in.id;
+            out.t = h.t; out.b0 = h.b0; out.b1 = h.b1; out.b2 = h.b2;
+        }
+        hits[i] = out;
+        if (full) {
+            PsySurfaceHit f;
+            f.hit = out;
+            f.shader = -1;
+            f.pos[0] = f.pos[1] = f.pos[2] = 0.0f;
+            f.nor[0] = f.nor[1] = f.nor[2] = 0.0f;
+            f.nor_g[0] = f.nor_g[1] = f.nor_g[2] = 0.0f;
+            f.pos_err = 0.0f;
+            f.sample_pdf = 0.0f;
+            if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
+                SurfData sd;
+                resolve_hit(S, h, o, d, time, sd);
+                f.pos[0] = sd.pos.x; f.pos[1] = sd.pos.y; f.pos[2] = sd.pos.z;
+                f.nor[0] = sd.nor.x; f.nor[1] = sd.nor.y; f.nor[2] = sd.nor.z;
+                f.nor_g[0] = sd.nor_g.x; f.nor_g[1] = sd.nor_g.y; f.nor_g[2] = sd.nor_g.z;
+                f.pos_err = sd.pos_err;
+                f.sample_pdf = sd.sample_pdf;
+                f.shader = sd.shader;
+            }
+            full[i] = f;
+        }
+    }
+    if (COUNT) {
+        unsigned long long a = tc.nodes, b = tc.tris, c = (i < n) ? 1ull : 0ull;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, off);
+            b += __shfl_down_sync(0xffffffffu, b, off);
+            c += __shfl_down_sync(0xffffffffu, c, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(counters, a);
+            atomicAdd(counters + 1, b);
+            atomicAdd(counters + 2, c);
+        }
     }
 }
 
 cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurfaceHit *full,
-                              int stack, int block, int *d_err, cudaStream_t st) {
+                              int stack, int block, int *d_err, unsigned long long *counters, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     (void)block;
     dim3 b(128), g((n + 127) / 128);
-    if (stack <= 32) k_trace_rays<32><<<g, b, 0, st>>>(S, rays, n, hits, full, d_err);
-    else if (stack <= 64) k_trace_rays<64><<<g, b, 0, st>>>(S, rays, n, hits, full, d_err);
-    else k_trace_rays<192><<<g, b, 0, st>>>(S, rays, n, hits, full, d_err);
+    bool c = counters != nullptr;
+#define TR(SZ)                                                                                        \
+    if (c) k_trace_rays<SZ, true><<<g, b, 0, st>>>(S, rays, n, hits, full, d_err, counters);         \
+    else k_trace_rays<SZ, false><<<g, b, 0, st>>>(S, rays, n, hits, full, d_err, counters)
+    if (stack <= 32) { TR(32); }
+    else if (stack <= 64) { TR(64); }
+    else { TR(192); }
+#undef TR
     return cudaGetLastError();
 }
 
 // Queue-driven trace for the render wavefront: a grid-stride loop over the
-// live paths listed in queue[0 .. *count).
-template <int STACK>
+// live paths listed in queue[0 .. *count).  COUNT adds the work counters
+// (node visits, triangle tests, rays) into counters[0..2].
+template <int STACK, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_queue(GScene S, RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
-                                                     const uint32_t *__restrict__ count, int *err) {
+                                                     const uint32_t *__restrict__ count, int *err,
+                                                     unsigned long long *counters) {
     uint32_t n = *count;
+    TraceCount tc{0, 0};
+    uint32_t nr = 0;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         uint32_t p = queue[q];
         float4 ro = R.o[p], rd = R.d[p];
         HitRec h;
-        if (!trace_ray<STACK>(S, v3(ro), v3(rd), ro.w, rd.w, R.occl[p] != 0, h)) {
+        if (!trace_ray<STACK, COUNT>(S, v3(ro), v3(rd), ro.w, rd.w, R.occl[p] != 0, h, &tc)) {
             atomicExch(err, PSY_E_OVERFLOW);
             h.kind = PSY_HIT_MISS_K;
         }
+        nr++;
         H.ki[p] = make_uint4(h.kind, h.prim, h.slot, 0u);
         H.tb[p] = make_float4(h.t, h.b0, h.b1, h.b2);
+    }
+    if (COUNT) {
+        unsigned long long a = tc.nodes, b = tc.tris, c = nr;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, off);
+            b += __shfl_down_sync(0xffffffffu, b, off);
+            c += __shfl_down_sync(0xffffffffu, c, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(counters, a);
+            atomicAdd(counters + 1, b);
+            atomicAdd(counters + 2, c);
+        }
     }
 }
 
 cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
-                               uint32_t max_count, int stack, int block, int grid, int *d_err, cudaStream_t st) {
+                               uint32_t max_count, int stack, int block, int grid, int *d_err,
+                               unsigned long long *counters, cudaStream_t st) {
     (void)block;
     if (grid <= 0) grid = (int)((max_count + 127) / 128);
     if (grid == 0) return cudaSuccess;
-    if (stack <= 32) k_trace_queue<32><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err);
-    else if (stack <= 64) k_trace_queue<64><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err);
-    else k_trace_queue<192><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err);
+    bool c = counters != nullptr;
+#define TQ(SZ)                                                                                            \
+    if (c) k_trace_queue<SZ, true><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, counters);        \
+    else k_trace_queue<SZ, false><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, counters)
+    if (stack <= 32) { TQ(32); }
+    else if (stack <= 64) { TQ(64); }
+    else { TQ(192); }
+#undef TQ
     return cudaGetLastError();
 }
 

@@ -39,13 +39,14 @@ void psy_upload_constants();  // Sobol directions + traversal table -> __constan
 
 // Trace n PsyRay records (device) into PsyHit records (device).
 cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurfaceHit *full,
-                              int stack, int block, int *d_err, cudaStream_t st);
+                              int stack, int block, int *d_err, unsigned long long *counters, cudaStream_t st);
 // Camera rays for a wave; fills queue with 0..n-1 and *count = n.
 cudaError_t launch_camera(const GScene &S, const Wave &w, PathState P, RayBuf R, uint32_t *queue, uint32_t *count,
                           cudaStream_t st);
 // Trace the queued rays of a wave.
 cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
-                               uint32_t max_count, int stack, int block, int grid, int *d_err, cudaStream_t st);
+                               uint32_t max_count, int stack, int block, int grid, int *d_err,
+                               unsigned long long *counters, cudaStream_t st);
 // LightPath::next for the queued paths; live paths go to next_queue.
 cudaError_t launch_shade(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                          const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,

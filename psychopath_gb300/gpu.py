@@ -57,6 +57,7 @@ def lib(path=None):
     L.psy_debug_mesh_bvh_info.argtypes = [vp, u32, vp, C.POINTER(u32)]
     L.psy_debug_scene_info.argtypes = [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]
     L.psy_debug_set_launch.argtypes = [vp, C.c_int, u32]
+    L.psy_debug_counters.argtypes = [vp, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     L.psy_debug_host_build.argtypes = [vp, vp, u32, vp, C.POINTER(u32), C.POINTER(u32)]
     _lib = L
     return L
@@ -121,6 +122,14 @@ class Scene:
         nc = C.c_uint32()
         _check(lib().psy_debug_mesh_bvh_info(self.h, obj, order.ctypes.data, C.byref(nc)))
         return order, nc.value
+
+    def counters(self, enable):
+        """Read (and zero) the render traversal counters, then enable or
+        disable counting for later renders: (node visits, triangle tests,
+        rays)."""
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(lib().psy_debug_counters(self.h, 1 if enable else 0, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
 
     def set_launch(self, grid=0, wave_paths=0):
         _check(lib().psy_debug_set_launch(self.h, grid, wave_paths))
