@@ -159,9 +159,14 @@ typedef struct PsySceneDesc {
 /* Options of a scene build. */
 #define PSY_BOUNDS_FP32 0 /* BVH4 child bounds as f32, bit-identical to the reference */
 #define PSY_BOUNDS_FP16 1 /* child bounds as f16 rounded outward (conservative) */
+/* Arithmetic of the light / cone / spherical-triangle sampling and the pixel
+ * filter, which the reference evaluates in f64. */
+#define PSY_SHADING_F64 0 /* as the reference (f64 where it uses f64) */
+#define PSY_SHADING_F32 1 /* f32 throughout: no FP64 outside the watertight triangle retest */
 typedef struct PsySceneOptions {
-    uint32_t bounds_precision; /* PSY_BOUNDS_* */
-    uint32_t reserved[7];
+    uint32_t bounds_precision;  /* PSY_BOUNDS_* */
+    uint32_t shading_precision; /* PSY_SHADING_* */
+    uint32_t reserved[6];
 } PsySceneOptions;
 
 typedef struct PsyScene PsyScene; /* opaque */

@@ -16,6 +16,7 @@ PSY_COLOR_XYZ, PSY_COLOR_BLACKBODY, PSY_COLOR_TEMPERATURE = 0, 1, 2
 PSY_SHADER_EMIT, PSY_SHADER_LAMBERT, PSY_SHADER_GGX = 0, 1, 2
 PSY_OBJ_MESH, PSY_OBJ_RECT_LIGHT, PSY_OBJ_SPHERE_LIGHT = 0, 1, 2
 PSY_BOUNDS_FP32, PSY_BOUNDS_FP16 = 0, 1
+PSY_SHADING_F64, PSY_SHADING_F32 = 0, 1
 PSY_RAY_OCCLUSION = 1
 PSY_HIT_MISS, PSY_HIT_OCCLUDE, PSY_HIT_SURFACE, PSY_HIT_LIGHT = 0, 1, 2, 3
 
@@ -70,7 +71,7 @@ class PsySceneDesc(C.Structure):
 
 
 class PsySceneOptions(C.Structure):
-    _fields_ = [("bounds_precision", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+    _fields_ = [("bounds_precision", C.c_uint32), ("shading_precision", C.c_uint32), ("reserved", C.c_uint32 * 6)]
 
 
 class PsyRay(C.Structure):

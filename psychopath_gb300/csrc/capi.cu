@@ -70,6 +70,14 @@ struct PsyScene {
     uint32_t wave_paths = 1u << 24;      // paths per wave
     int grid = 0;                        // persistent grid for queue kernels (0: size by queue)
     bool counting = false;               // accumulate traversal counters during renders
+    int trace_mode = 0;                  // 0: one thread per ray, 1: persistent with lane refill
+    int prec = 0;                        // shading arithmetic: 0 f64 (reference), 1 f32
+    int sort_bits = 0;                   // ray binning key width between iterations (0: off)
+    uint32_t *d_stage = nullptr;         // binning staging queue
+    uint16_t *d_stage_key = nullptr;
+    uint32_t *d_bins = nullptr;
+    int minb = 4;                        // persistent kernel register budget (4 or 8 blocks/SM)
+    uint32_t *d_work = nullptr;          // work counter of the persistent kernels
     unsigned long long *d_counters = nullptr;  // node visits, triangle tests, rays
     std::mutex mu;
 };
@@ -88,7 +96,8 @@ static int upload(PsyScene *s, const std::vector<T> &v, const T **out) {
 
 static void free_render(PsyScene *s) {
     void *ptrs[] = {s->P.color, s->P.latt, s->P.pending, s->P.nafac, s->P.nb_o, s->P.nb_d, s->P.tw, s->P.seed, s->P.flags,
-                    s->R.o, s->R.d, s->R.occl, s->H.ki, s->H.tb, s->queue[0], s->queue[1], s->counts, s->d_raycount};
+                    s->R.o, s->R.d, s->R.occl, s->H.ki, s->H.tb, s->queue[0], s->queue[1], s->counts, s->d_raycount,
+                    s->d_stage, s->d_stage_key, s->d_bins};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     s->P = PathState{};
@@ -97,6 +106,9 @@ static void free_render(PsyScene *s) {
     s->queue[0] = s->queue[1] = nullptr;
     s->counts = nullptr;
     s->d_raycount = nullptr;
+    s->d_stage = nullptr;
+    s->d_stage_key = nullptr;
+    s->d_bins = nullptr;
     s->cap_paths = 0;
 }
 
@@ -112,6 +124,7 @@ static int ensure_render(PsyScene *s, uint32_t n) {
     AL(s->queue[0], N * 4); AL(s->queue[1], N * 4);
     AL(s->counts, 16);
     AL(s->d_raycount, 8);
+    AL(s->d_stage, N * 4); AL(s->d_stage_key, N * 2); AL(s->d_bins, 2 * 1024 * 4);
 #undef AL
     s->cap_paths = n;
     return PSY_OK;
@@ -192,6 +205,7 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
 #undef UP
     if (r == PSY_OK) {
         cudaError_t e = cudaMalloc((void **)&s->d_err, sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_work, 64 * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         if (e != cudaSuccess) r = cuda_fail(e, "scene upload");
@@ -214,7 +228,13 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
     g.use_fp16 = hs.nodes_h.empty() ? 0u : 1u;
     g.distant_energy_total = hs.distant_energy_total;
     g.lt_root_energy = hs.lt_root_energy;
+    for (int a = 0; a < 3; a++) {
+        float ext = hs.scene_max[a] - hs.scene_min[a];
+        (&g.bounds_min.x)[a] = hs.scene_min[a];
+        (&g.bounds_inv_extent.x)[a] = ext > 0.0f ? 1.0f / ext : 0.0f;
+    }
     s->max_stack = hs.max_stack;
+    s->prec = (opts && opts->shading_precision == PSY_SHADING_F32) ? 1 : 0;
     s->stack = hs.max_stack <= 32 ? 32 : (hs.max_stack <= 64 ? 64 : 192);
     if (hs.max_stack > 192) {
         psy_scene_destroy(s);
@@ -243,6 +263,7 @@ int psy_scene_destroy(PsyScene *s) {
     if (s->d_xyz) cudaFree(s->d_xyz);
     if (s->d_err) cudaFree(s->d_err);
     if (s->d_counters) cudaFree(s->d_counters);
+    if (s->d_work) cudaFree(s->d_work);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return PSY_OK;
@@ -263,7 +284,9 @@ int psy_trace_device(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyHit *d_hi
         if (r != PSY_OK) return r;
         ctr = s->d_counters;
     }
-    cudaError_t e = launch_trace_rays(s->g, d_rays, n, d_hits, nullptr, s->stack, 128, s->d_err, ctr, st);
+    cudaError_t e = s->trace_mode == 1
+                        ? launch_trace_persist_rays(s->g, d_rays, n, d_hits, s->stack, s->minb, s->d_work, s->d_err, ctr, st)
+                        : launch_trace_rays(s->g, d_rays, n, d_hits, nullptr, s->stack, 128, s->d_err, ctr, st);
     if (e != cudaSuccess) return cuda_fail(e, "trace launch");
     s->rays_traced += n;
     return PSY_OK;
@@ -283,9 +306,13 @@ int psy_trace(PsyScene *s, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurf
         if (r != PSY_OK) return r;
         ctr = s->d_counters;
     }
-    CK(launch_trace_rays(s->g, s->d_rays, n, s->d_hits, full_out ? s->d_full : nullptr, s->stack, 128, s->d_err, ctr,
-                         st),
-       "trace launch");
+    if (full_out || s->trace_mode == 0)
+        CK(launch_trace_rays(s->g, s->d_rays, n, s->d_hits, full_out ? s->d_full : nullptr, s->stack, 128, s->d_err, ctr,
+                             st),
+           "trace launch");
+    else
+        CK(launch_trace_persist_rays(s->g, s->d_rays, n, s->d_hits, s->stack, s->minb, s->d_work, s->d_err, ctr, st),
+           "trace launch");
     CK(cudaMemcpyAsync(hits, s->d_hits, (size_t)n * sizeof(PsyHit), cudaMemcpyDeviceToHost, st), "copy hits");
     if (full_out)
         CK(cudaMemcpyAsync(full_out, s->d_full, (size_t)n * sizeof(PsySurfaceHit), cudaMemcpyDeviceToHost, st),
@@ -337,19 +364,31 @@ static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint
         wv.spp = spp; wv.seed = seed;
         uint32_t n = wv.w * wv.h * spp;
         if (timing) cudaEventRecord(ev[0], st);
-        CK(launch_camera(s->g, wv, s->P, s->R, s->queue[0], s->counts, st), "camera launch");
+        CK(launch_camera(s->g, wv, s->P, s->R, s->queue[0], s->counts, s->prec, st), "camera launch");
         if (timing) cudaEventRecord(ev[1], st);
         int cur = 0;
         for (uint32_t it = 0; it < iters; it++) {
             if (timing) cudaEventRecord(ev[2 + 3 * it], st);
-            CK(launch_trace_queue(s->g, s->R, s->H, s->queue[cur], s->counts + cur, n, s->stack, 128, s->grid, s->d_err,
-                                  ctr, st),
-               "trace launch");
+            if (s->trace_mode == 1)
+                CK(launch_trace_persist_queue(s->g, s->R, s->H, s->queue[cur], s->counts + cur, n, s->stack, s->minb,
+                                              s->d_work, s->d_err, ctr, st),
+                   "trace launch");
+            else
+                CK(launch_trace_queue(s->g, s->R, s->H, s->queue[cur], s->counts + cur, n, s->stack, 128, s->grid,
+                                      s->d_err, ctr, st),
+                   "trace launch");
             if (timing) cudaEventRecord(ev[3 + 3 * it], st);
             CK(cudaMemsetAsync(s->counts + (cur ^ 1), 0, 4, st), "memset count");
-            CK(launch_shade(s->g, wv, s->P, s->R, s->H, s->queue[cur], s->counts + cur, n, s->queue[cur ^ 1],
-                            s->counts + (cur ^ 1), 128, s->grid, st),
-               "shade launch");
+            if (s->sort_bits > 0) {
+                SortBuf sb{s->d_stage, s->d_stage_key, s->d_bins, s->sort_bits};
+                CK(launch_shade_sorted(s->g, wv, s->P, s->R, s->H, s->queue[cur], s->counts + cur, n, sb,
+                                       s->counts + (cur ^ 1), s->queue[cur ^ 1], s->grid, s->prec, st),
+                   "shade launch");
+            } else {
+                CK(launch_shade(s->g, wv, s->P, s->R, s->H, s->queue[cur], s->counts + cur, n, s->queue[cur ^ 1],
+                                s->counts + (cur ^ 1), 128, s->grid, s->prec, st),
+                   "shade launch");
+            }
             if (timing) cudaEventRecord(ev[4 + 3 * it], st);
             cur ^= 1;
         }
@@ -502,6 +541,20 @@ int psy_debug_counters(PsyScene *s, int enable, uint64_t *nodes, uint64_t *tris,
         if (rays) *rays = 0;
     }
     s->counting = enable != 0;
+    return PSY_OK;
+}
+// Traversal kernel choice: mode 0 = one thread per ray, 1 = persistent with
+// lane refill; minb = resident blocks per SM the register budget targets.
+int psy_debug_set_trace(PsyScene *s, int mode, int minb) {
+    if (!s || mode < 0 || mode > 1) return fail(PSY_E_INVALID, "bad trace mode");
+    s->trace_mode = mode;
+    s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : 4);
+    return PSY_OK;
+}
+// Ray binning key width between wavefront iterations: 0 (off), 1, 4, 7, 10.
+int psy_debug_set_sort(PsyScene *s, int bits) {
+    if (!s || !(bits == 0 || bits == 1 || bits == 4 || bits == 7 || bits == 10)) return fail(PSY_E_INVALID, "bad sort bits");
+    s->sort_bits = bits;
     return PSY_OK;
 }
 int psy_debug_set_launch(PsyScene *s, int grid, uint32_t wave_paths) {

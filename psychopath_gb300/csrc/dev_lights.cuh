@@ -26,14 +26,15 @@ DI void rect_corners(float w, float h, const Xf &si, V3 *p1, V3 *p2, V3 *p3, V3 
     *p4 = xf_point(v3(w * 0.5f, h * -0.5f, 0.0f), si);
 }
 // RectangleLight::sample_pdf
+template <class R>
 DI float rect_sample_pdf(const GScene &S, const GLight &L, const Xf &space, V3 arr, V3 sample_dir, V3 hit, float time) {
     float w = light_dim(S, L, 0, time), h = light_dim(S, L, 1, time);
     Xf si = xf_inverse(space);
     V3 p1, p2, p3, p4;
     rect_corners(w, h, si, &p1, &p2, &p3, &p4);
     V3 sp1 = normalized(p1 - arr), sp2 = normalized(p2 - arr), sp3 = normalized(p3 - arr), sp4 = normalized(p4 - arr);
-    float a1 = spherical_triangle_solid_angle(sp2, sp1, sp3);
-    float a2 = spherical_triangle_solid_angle(sp4, sp1, sp3);
+    float a1 = spherical_triangle_solid_angle<R>(sp2, sp1, sp3);
+    float a2 = spherical_triangle_solid_angle<R>(sp4, sp1, sp3);
     V3 normal = xf_normal(v3(0.0f, 0.0f, 1.0f), si);
     if ((a1 + a2) < 0.01f) {
         float area = triangle_surface_area(p2, p1, p3) + triangle_surface_area(p4, p1, p3);
@@ -42,16 +43,17 @@ DI float rect_sample_pdf(const GScene &S, const GLight &L, const Xf &space, V3 a
     return 1.0f / (a1 + a2);
 }
 // SphereLight::sample_pdf
+template <class R>
 DI float sphere_sample_pdf(const GScene &S, const GLight &L, const Xf &space, V3 arr_w, float time) {
     V3 arr = xf_point(arr_w, space);
-    double radius = (double)light_dim(S, L, 0, time);
-    double d2 = (double)length2(v3(0.0f, 0.0f, 0.0f) - arr);
-    double d = sqrt(d2);
+    R radius = (R)light_dim(S, L, 0, time);
+    R d2 = (R)length2(v3(0.0f, 0.0f, 0.0f) - arr);
+    R d = msqrt(d2);
     if (d > radius) {
-        double st2 = fmin((radius * radius) / d2, 1.0);
-        return (float)uniform_sample_cone_pdf(sqrt(1.0 - st2));
+        R st2 = mfmin((radius * radius) / d2, (R)1);
+        return (float)uniform_sample_cone_pdf<R>(msqrt((R)1 - st2));
     }
-    return (float)(1.0 / (4.0 * PSY_PI_64));
+    return (float)((R)1 / ((R)4 * pi_r<R>()));
 }
 
 struct LightSample {
@@ -61,17 +63,18 @@ struct LightSample {
     float serr, pdf, sel_pdf;
 };
 
+template <class R>
 DI V4 rect_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr, float u, float v, float wl, float time,
                   LightSample &o) {
     float w = light_dim(S, L, 0, time), h = light_dim(S, L, 1, time);
     GColor col = lerp_slice_color(S.light_colors + L.key_base, L.nkeys, time);
-    double sai = 1.0 / ((double)w * (double)h);
+    R sai = (R)1 / ((R)w * (R)h);
     Xf si = xf_inverse(space);
     V3 p1, p2, p3, p4;
     rect_corners(w, h, si, &p1, &p2, &p3, &p4);
     V3 sp1 = normalized(p1 - arr), sp2 = normalized(p2 - arr), sp3 = normalized(p3 - arr), sp4 = normalized(p4 - arr);
-    float a1 = spherical_triangle_solid_angle(sp2, sp1, sp3);
-    float a2 = spherical_triangle_solid_angle(sp4, sp1, sp3);
+    float a1 = spherical_triangle_solid_angle<R>(sp2, sp1, sp3);
+    float a2 = spherical_triangle_solid_angle<R>(sp4, sp1, sp3);
     V3 normal = xf_normal(v3(0.0f, 0.0f, 1.0f), si);
     if ((a1 + a2) < 0.01f) {
         float sa1 = triangle_surface_area(p2, p1, p3);
@@ -86,8 +89,8 @@ DI V4 rect_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr, flo
     }
     float prob_1 = isinf(a1) ? 1.0f : (isinf(a2) ? 0.0f : a1 / (a1 + a2));
     float prob_2 = 1.0f - prob_1;
-    V3 shadow_vec = (u < prob_1) ? uniform_sample_spherical_triangle(sp2, sp1, sp3, v, u / prob_1)
-                                 : uniform_sample_spherical_triangle(sp4, sp1, sp3, v, 1.0f - ((u - prob_1) / prob_2));
+    V3 shadow_vec = (u < prob_1) ? uniform_sample_spherical_triangle<R>(sp2, sp1, sp3, v, u / prob_1)
+                                 : uniform_sample_spherical_triangle<R>(sp4, sp1, sp3, v, 1.0f - ((u - prob_1) / prob_2));
     V3 arr_local = xf_point(arr, space);
     V3 svl = xf_vector(shadow_vec, space);
     svl = svl * (-arr_local.z / svl.z);
@@ -102,48 +105,54 @@ DI V4 rect_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr, flo
     return color_to_spectral(col, wl) * (float)sai * 0.5f;
 }
 
+template <class R>
 DI V4 sphere_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr_w, float u, float v, float wl, float time,
                     LightSample &o) {
     V3 arr = xf_point(arr_w, space);
     Xf inv = xf_inverse(space);
-    double radius = (double)light_dim(S, L, 0, time);
+    R radius = (R)light_dim(S, L, 0, time);
     GColor col = lerp_slice_color(S.light_colors + L.key_base, L.nkeys, time);
-    double sai = 1.0 / (4.0 * PSY_PI_64 * radius * radius);
+    R sai = (R)1 / ((R)4 * pi_r<R>() * radius * radius);
     V3 zv = v3(0.0f, 0.0f, 0.0f) - arr;
-    double d2 = (double)length2(zv);
-    double d = sqrt(d2);
+    R d2 = (R)length2(zv);
+    R d = msqrt(d2);
     V3 z, x, y;
     coordinate_system_from_vector(zv, &z, &x, &y);
     x = normalized(x); y = normalized(y); z = normalized(z);
     float rf = (float)radius;
     o.serr = length(xf_vector(v3(rf, rf, rf), inv)) * 0.001f;
+    // phi = v * 2 pi is shared by the cone sample and the point placement
+    R sp, cp;
+    msincos_2pi((R)v, &sp, &cp);
     if (d > radius) {
-        double st2 = fmin((radius * radius) / d2, 1.0);
-        double ct2 = 1.0 - st2;
-        double st = sqrt(st2);
-        double ct = sqrt(ct2);
-        V3 smp = normalized(uniform_sample_cone(u, v, ct));
-        double cos_theta = (double)smp.z;
-        double cos_theta2 = cos_theta * cos_theta;
-        double sin_theta2 = fmax(1.0 - cos_theta2, 0.0);
-        double sin_theta = sqrt(sin_theta2);
-        double dd = 1.0 - (d2 * sin_theta * sin_theta / (radius * radius));
-        double cos_a = (dd <= 0.0) ? st : ((d / radius) * sin_theta2) + (cos_theta * sqrt(dd));
-        double sin_a = sqrt(fmax(1.0 - (cos_a * cos_a), 0.0));
-        double phi = (double)v * 2.0 * PSY_PI_64;
-        V3 s2 = v3((float)(cos(phi) * sin_a * radius), (float)(sin(phi) * sin_a * radius), (float)(d - (cos_a * radius)));
+        R st2 = mfmin((radius * radius) / d2, (R)1);
+        R ct2 = (R)1 - st2;
+        R st = msqrt(st2);
+        R ct = msqrt(ct2);
+        // uniform_sample_cone(u, v, ct), normalized
+        R cone_c = ((R)1 - (R)u) + ((R)u * ct);
+        R cone_s = msqrt((R)1 - (cone_c * cone_c));
+        V3 smp = normalized(v3((float)(cp * cone_s), (float)(sp * cone_s), (float)cone_c));
+        R cos_theta = (R)smp.z;
+        R cos_theta2 = cos_theta * cos_theta;
+        R sin_theta2 = mfmax((R)1 - cos_theta2, (R)0);
+        R sin_theta = msqrt(sin_theta2);
+        R dd = (R)1 - (d2 * sin_theta * sin_theta / (radius * radius));
+        R cos_a = (dd <= (R)0) ? st : ((d / radius) * sin_theta2) + (cos_theta * msqrt(dd));
+        R sin_a = msqrt(mfmax((R)1 - (cos_a * cos_a), (R)0));
+        V3 s2 = v3((float)(cp * sin_a * radius), (float)(sp * sin_a * radius), (float)(d - (cos_a * radius)));
         V3 svec = (x * s2.x) + (y * s2.y) + (z * s2.z);
         V3 normal = normalized(arr + svec);
         o.sp = xf_point(normal * rf, inv);
         o.sn = xf_normal(normal, inv);
-        o.pdf = (float)uniform_sample_cone_pdf(ct);
+        o.pdf = (float)uniform_sample_cone_pdf<R>(ct);
         return color_to_spectral(col, wl) * (float)sai;
     }
     V3 svec = uniform_sample_sphere(u, v);
     V3 normal = normalized(arr + svec);
     o.sp = xf_point(normal * rf, inv);
     o.sn = xf_normal(normal, inv);
-    o.pdf = (float)(1.0 / (4.0 * PSY_PI_64));
+    o.pdf = (float)((R)1 / ((R)4 * pi_r<R>()));
     return color_to_spectral(col, wl) * (float)sai;
 }
 
@@ -208,6 +217,7 @@ DI bool lt_select(const GScene &S, V3 inc, V3 pos, V3 nor, V3 nor_g, const Closu
 
 // Scene::sample_lights for the root assembly.  `pos, nor, nor_g, inc` are
 // the hit's world-space intersection data.
+template <class R>
 DI LightSample scene_sample_lights(const GScene &S, float n, float u, float v, float wl, float time, V3 inc, V3 pos,
                                    V3 nor, V3 nor_g, const Closure &cl) {
     LightSample out;
@@ -231,18 +241,29 @@ DI LightSample scene_sample_lights(const GScene &S, float n, float u, float v, f
             if (i == S.n_distant - 1) p = wgt / total;
         }
         const GDistant &L = S.distant[pick];
-        double radius = (double)lerp_slice_f(S.distant_radii + L.key_base, L.nkeys, time);
         V3 direction = lerp_slice_v3(S.distant_dirs + L.key_base, L.nkeys, time);
         GColor col = lerp_slice_color(S.distant_colors + L.key_base, L.nkeys, time);
-        double sai = 1.0 / (2.0 * PSY_PI_64 * (1.0 - cos(radius)));
+        R ctm;
+        float sai_f, pdf_f;
+        if (L.is_static) {
+            // cos(radius) and the cone's solid-angle inverse, evaluated by the host
+            ctm = (R)L.ctm;
+            sai_f = L.sai;
+            pdf_f = L.sai;
+        } else {
+            R radius = (R)lerp_slice_f(S.distant_radii + L.key_base, L.nkeys, time);
+            ctm = mcos(radius);
+            R sai = (R)1 / ((R)2 * pi_r<R>() * ((R)1 - ctm));
+            sai_f = (float)sai;
+            pdf_f = (float)uniform_sample_cone_pdf<R>(ctm);
+        }
         V3 z, x3, y3;
         coordinate_system_from_vector(neg(normalized(direction)), &z, &x3, &y3);
-        double ctm = cos(radius);
-        V3 smp = normalized(uniform_sample_cone(u, v, ctm));
+        V3 smp = normalized(uniform_sample_cone<R>(u, v, ctm));
         out.kind = 1;
-        out.color = color_to_spectral(col, wl) * (float)sai;
+        out.color = color_to_spectral(col, wl) * sai_f;
         out.dir = (x3 * smp.x) + (y3 * smp.y) + (z * smp.z);
-        out.pdf = (float)uniform_sample_cone_pdf(ctm);
+        out.pdf = pdf_f;
         out.sel_pdf = p * wl_prob;
         return out;
     }
@@ -256,8 +277,8 @@ DI LightSample scene_sample_lights(const GScene &S, float n, float u, float v, f
     GInstance inst = S.light_instances[li];
     Xf xf = instance_xf_at(S, inst, time);
     const GLight &L = S.lights[inst.obj];
-    V4 col = (inst.kind == PSY_INST_RECT) ? rect_sample(S, L, xf, pos, u, v, wl, time, out)
-                                          : sphere_sample(S, L, xf, pos, u, v, wl, time, out);
+    V4 col = (inst.kind == PSY_INST_RECT) ? rect_sample<R>(S, L, xf, pos, u, v, wl, time, out)
+                                          : sphere_sample<R>(S, L, xf, pos, u, v, wl, time, out);
     out.kind = 2;
     out.color = col;
     out.sel_pdf = sel_pdf * (1.0f - wl_prob);

@@ -236,36 +236,42 @@ DI void get_sample_4d(uint32_t i, uint32_t set, uint32_t px, uint32_t py, uint32
         for (uint32_t k = 0; k < 4; k++) out[k] = hash_u32_to_f32((set * 4 + k) ^ (i << 16), s);
     }
 }
-// Acklam's probit approximation in f64 (src/math.rs:67-132)
+// Acklam's probit approximation (src/math.rs:67-132); the reference
+// evaluates it in f64 (R = double), the precision variant in f32.
+DI double plog(double x) { return log(x); }
+DI float plog(float x) { return logf(x); }
+DI double psqrt(double x) { return sqrt(x); }
+DI float psqrt(float x) { return sqrtf(x); }
+template <class R>
 DI float probit(float nf, float width) {
-    double n = (double)nf;
-    const double A1 = -3.969683028665376e+01, A2 = 2.209460984245205e+02, A3 = -2.759285104469687e+02,
-                 A4 = 1.383577518672690e+02, A5 = -3.066479806614716e+01, A6 = 2.506628277459239e+00;
-    const double B1 = -5.447609879822406e+01, B2 = 1.615858368580409e+02, B3 = -1.556989798598866e+02,
-                 B4 = 6.680131188771972e+01, B5 = -1.328068155288572e+01;
-    const double C1 = -7.784894002430293e-03, C2 = -3.223964580411365e-01, C3 = -2.400758277161838e+00,
-                 C4 = -2.549732539343734e+00, C5 = 4.374664141464968e+00, C6 = 2.938163982698783e+00;
-    const double D1 = 7.784695709041462e-03, D2 = 3.224671290700398e-01, D3 = 2.445134137142996e+00,
-                 D4 = 3.754408661907416e+00;
-    const double N_LOW = 0.02425, N_HIGH = 1.0 - N_LOW;
-    double x;
-    if (0.0 < n && n < N_LOW) {
-        double q = sqrt(-2.0 * log(n));
-        x = (((((C1 * q + C2) * q + C3) * q + C4) * q + C5) * q + C6) / ((((D1 * q + D2) * q + D3) * q + D4) * q + 1.0);
+    R n = (R)nf;
+    const R A1 = (R)-3.969683028665376e+01, A2 = (R)2.209460984245205e+02, A3 = (R)-2.759285104469687e+02,
+            A4 = (R)1.383577518672690e+02, A5 = (R)-3.066479806614716e+01, A6 = (R)2.506628277459239e+00;
+    const R B1 = (R)-5.447609879822406e+01, B2 = (R)1.615858368580409e+02, B3 = (R)-1.556989798598866e+02,
+            B4 = (R)6.680131188771972e+01, B5 = (R)-1.328068155288572e+01;
+    const R C1 = (R)-7.784894002430293e-03, C2 = (R)-3.223964580411365e-01, C3 = (R)-2.400758277161838e+00,
+            C4 = (R)-2.549732539343734e+00, C5 = (R)4.374664141464968e+00, C6 = (R)2.938163982698783e+00;
+    const R D1 = (R)7.784695709041462e-03, D2 = (R)3.224671290700398e-01, D3 = (R)2.445134137142996e+00,
+            D4 = (R)3.754408661907416e+00;
+    const R N_LOW = (R)0.02425, N_HIGH = (R)1 - N_LOW;
+    R x;
+    if ((R)0 < n && n < N_LOW) {
+        R q = psqrt((R)-2 * plog(n));
+        x = (((((C1 * q + C2) * q + C3) * q + C4) * q + C5) * q + C6) / ((((D1 * q + D2) * q + D3) * q + D4) * q + (R)1);
     } else if (n <= N_HIGH) {
-        double q = n - 0.5;
-        double r = q * q;
+        R q = n - (R)0.5;
+        R r = q * q;
         x = (((((A1 * r + A2) * r + A3) * r + A4) * r + A5) * r + A6) * q /
-            (((((B1 * r + B2) * r + B3) * r + B4) * r + B5) * r + 1.0);
-    } else if (n < 1.0) {
-        double q = sqrt(-2.0 * log(1.0 - n));
-        x = -(((((C1 * q + C2) * q + C3) * q + C4) * q + C5) * q + C6) / ((((D1 * q + D2) * q + D3) * q + D4) * q + 1.0);
-    } else if (n == 0.0) {
-        x = -CUDART_INF;
-    } else if (n == 1.0) {
-        x = CUDART_INF;
+            (((((B1 * r + B2) * r + B3) * r + B4) * r + B5) * r + (R)1);
+    } else if (n < (R)1) {
+        R q = psqrt((R)-2 * plog((R)1 - n));
+        x = -(((((C1 * q + C2) * q + C3) * q + C4) * q + C5) * q + C6) / ((((D1 * q + D2) * q + D3) * q + D4) * q + (R)1);
+    } else if (n == (R)0) {
+        x = (R)-CUDART_INF;
+    } else if (n == (R)1) {
+        x = (R)CUDART_INF;
     } else {
-        x = CUDART_NAN;
+        x = (R)CUDART_NAN;
     }
     return (float)x * width;
 }
@@ -327,6 +333,25 @@ DI bool slab_hit(float xlo, float xhi, float ylo, float yhi, float zlo, float zh
     float far_t = vmin(vmin(fx, vmin(fy, fz)) * PSY_BBOX_MAXT_ADJUST, max_t);
     float near_t = vmax(vmax(nx, ny), vmax(nz, 0.0f));
     return near_t < far_t;
+}
+// Same test when the ray's inverse direction has no infinite or NaN
+// component: then no slab distance is NaN, so IEEE minNum/maxNum (one
+// instruction each) give the same hit decision as the SSE select order (the
+// only difference, the sign of a zero, does not change the comparisons).
+DI bool slab_hit_finite(float xlo, float xhi, float ylo, float yhi, float zlo, float zhi, V3 o, V3 di, float max_t) {
+    float t1x = (xlo - o.x) * di.x, t1y = (ylo - o.y) * di.y, t1z = (zlo - o.z) * di.z;
+    float t2x = (xhi - o.x) * di.x, t2y = (yhi - o.y) * di.y, t2z = (zhi - o.z) * di.z;
+    float fx = fmaxf(t1x, t2x), fy = fmaxf(t1y, t2y), fz = fmaxf(t1z, t2z);
+    float nx = fminf(t1x, t2x), ny = fminf(t1y, t2y), nz = fminf(t1z, t2z);
+    float far_t = fminf(fminf(fx, fminf(fy, fz)) * PSY_BBOX_MAXT_ADJUST, max_t);
+    float near_t = fmaxf(fmaxf(nx, ny), fmaxf(nz, 0.0f));
+    return near_t < far_t;
+}
+DI bool finite3(V3 v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }
+// Inverse direction finite and nonzero in every component (so the slab
+// distances (bound - o) * di are never 0 * inf).
+DI bool slab_safe(V3 o, V3 di, float tmax) {
+    return finite3(o) && finite3(di) && di.x != 0.0f && di.y != 0.0f && di.z != 0.0f && !isnan(tmax);
 }
 DI uint32_t ray_code(V3 d) {
     return (uint32_t)(d.x < 0.0f) + ((uint32_t)(d.y < 0.0f) << 1) + ((uint32_t)(d.z < 0.0f) << 2);

@@ -167,6 +167,33 @@ DI V3 xyz_from_spectral(V4 e, float hero) {
     return acc * 0.75f;
 }
 
+// ------------------------------------------------------------------ precision helpers
+// The reference evaluates light / cone / spherical-triangle sampling and the
+// pixel filter in f64.  Those routines are templated on the real type R:
+// R = double is the reference's arithmetic (the plain form); R = float is
+// the precision variant (no FP64 outside the watertight triangle retest),
+// whose image error against the f64 oracle is measured, not assumed.
+DI double msqrt(double x) { return sqrt(x); }
+DI float msqrt(float x) { return sqrtf(x); }
+DI double macos(double x) { return acos(x); }
+DI float macos(float x) { return acosf(x); }
+DI double msin(double x) { return sin(x); }
+DI float msin(float x) { return sinf(x); }
+DI double mcos(double x) { return cos(x); }
+DI float mcos(float x) { return cosf(x); }
+DI double mlog(double x) { return log(x); }
+DI float mlog(float x) { return logf(x); }
+DI double mfmin(double a, double b) { return fmin(a, b); }
+DI float mfmin(float a, float b) { return fminf(a, b); }
+DI double mfmax(double a, double b) { return fmax(a, b); }
+DI float mfmax(float a, float b) { return fmaxf(a, b); }
+// sin / cos of (v * 2 pi): sincospi of 2v (exact argument), equal to the
+// reference's cos(v * 2.0 * PI) up to the rounding of the product.
+DI void msincos_2pi(double v, double *s, double *c) { sincospi(v * 2.0, s, c); }
+DI void msincos_2pi(float v, float *s, float *c) { sincospif(v * 2.0f, s, c); }
+template <class R>
+DI R pi_r() { return (R)PSY_PI_64; }
+
 // ------------------------------------------------------------------ sampling
 DI void square_to_circle(float x, float y, float *ox, float *oy) {
     if (x == 0.0f && y == 0.0f) { *ox = 0.0f; *oy = 0.0f; return; }
@@ -190,13 +217,16 @@ DI V3 uniform_sample_sphere(float u, float v) {
     float phi = 2.0f * PSY_PI_32 * v;
     return v3(r * cosf(phi), r * sinf(phi), z);
 }
-DI V3 uniform_sample_cone(float u, float v, double cos_theta_max) {
-    double cos_theta = (1.0 - (double)u) + ((double)u * cos_theta_max);
-    double sin_theta = sqrt(1.0 - (cos_theta * cos_theta));
-    double phi = (double)v * 2.0 * PSY_PI_64;
-    return v3((float)(cos(phi) * sin_theta), (float)(sin(phi) * sin_theta), (float)cos_theta);
+template <class R>
+DI V3 uniform_sample_cone(float u, float v, R cos_theta_max) {
+    R cos_theta = ((R)1 - (R)u) + ((R)u * cos_theta_max);
+    R sin_theta = msqrt((R)1 - (cos_theta * cos_theta));
+    R sp, cp;
+    msincos_2pi((R)v, &sp, &cp);
+    return v3((float)(cp * sin_theta), (float)(sp * sin_theta), (float)cos_theta);
 }
-DI double uniform_sample_cone_pdf(double ctm) { return 1.0 / (2.0 * PSY_PI_64 * (1.0 - ctm)); }
+template <class R>
+DI R uniform_sample_cone_pdf(R ctm) { return (R)1 / ((R)2 * pi_r<R>() * ((R)1 - ctm)); }
 DI V3 uniform_sample_triangle(V3 va, V3 vb, V3 vc, float i, float j) {
     float isqrt = sqrtf(i);
     float a = 1.0f - isqrt;
@@ -205,43 +235,46 @@ DI V3 uniform_sample_triangle(V3 va, V3 vb, V3 vc, float i, float j) {
     return (va * a) + (vb * b) + (vc * c);
 }
 DI float triangle_surface_area(V3 p0, V3 p1, V3 p2) { return 0.5f * length(cross(p1 - p0, p2 - p0)); }
-DI double clampd(double x) { return fmin(fmax(x, -1.0), 1.0); }
+template <class R>
+DI R clamp1(R x) { return mfmin(mfmax(x, (R)-1), (R)1); }
+template <class R>
 DI float spherical_triangle_solid_angle(V3 va, V3 vb, V3 vc) {
-    double cos_a = (double)rmin(rmax(dot(vb, vc), -1.0f), 1.0f);
-    double cos_b = (double)rmin(rmax(dot(vc, va), -1.0f), 1.0f);
-    double cos_c = (double)rmin(rmax(dot(va, vb), -1.0f), 1.0f);
-    double sin_a = sqrt(1.0 - (cos_a * cos_a));
-    double sin_b = sqrt(1.0 - (cos_b * cos_b));
-    double sin_c = sqrt(1.0 - (cos_c * cos_c));
-    if (cos_a == 1.0 || cos_b == 1.0 || cos_c == 1.0) return 0.0f;
-    double cos_va = clampd((cos_a - (cos_b * cos_c)) / (sin_b * sin_c));
-    double cos_vb = clampd((cos_b - (cos_c * cos_a)) / (sin_c * sin_a));
-    double cos_vc = clampd((cos_c - (cos_a * cos_b)) / (sin_a * sin_b));
-    return (float)(acos(cos_va) + acos(cos_vb) + acos(cos_vc) - PSY_PI_64);
+    R cos_a = (R)rmin(rmax(dot(vb, vc), -1.0f), 1.0f);
+    R cos_b = (R)rmin(rmax(dot(vc, va), -1.0f), 1.0f);
+    R cos_c = (R)rmin(rmax(dot(va, vb), -1.0f), 1.0f);
+    R sin_a = msqrt((R)1 - (cos_a * cos_a));
+    R sin_b = msqrt((R)1 - (cos_b * cos_b));
+    R sin_c = msqrt((R)1 - (cos_c * cos_c));
+    if (cos_a == (R)1 || cos_b == (R)1 || cos_c == (R)1) return 0.0f;
+    R cos_va = clamp1((cos_a - (cos_b * cos_c)) / (sin_b * sin_c));
+    R cos_vb = clamp1((cos_b - (cos_c * cos_a)) / (sin_c * sin_a));
+    R cos_vc = clamp1((cos_c - (cos_a * cos_b)) / (sin_a * sin_b));
+    return (float)(macos(cos_va) + macos(cos_vb) + macos(cos_vc) - pi_r<R>());
 }
+template <class R>
 DI V3 uniform_sample_spherical_triangle(V3 va, V3 vb, V3 vc, float i, float j) {
-    double cos_a = (double)rmin(rmax(dot(vb, vc), -1.0f), 1.0f);
-    double cos_b = (double)rmin(rmax(dot(vc, va), -1.0f), 1.0f);
-    double cos_c = (double)rmin(rmax(dot(va, vb), -1.0f), 1.0f);
-    double sin_a = sqrt(1.0 - (cos_a * cos_a));
-    double sin_b = sqrt(1.0 - (cos_b * cos_b));
-    double sin_c = sqrt(1.0 - (cos_c * cos_c));
-    if (cos_a == 1.0 || cos_b == 1.0 || cos_c == 1.0) return va;
-    double cos_va = clampd((cos_a - (cos_b * cos_c)) / (sin_b * sin_c));
-    double cos_vb = clampd((cos_b - (cos_c * cos_a)) / (sin_c * sin_a));
-    double cos_vc = clampd((cos_c - (cos_a * cos_b)) / (sin_a * sin_b));
-    double sin_va = sqrt(1.0 - (cos_va * cos_va));
-    double ang_va = acos(cos_va), ang_vb = acos(cos_vb), ang_vc = acos(cos_vc);
-    double area = ang_va + ang_vb + ang_vc - PSY_PI_64;
-    double area_2 = area * (double)i;
-    double s = sin(area_2 - ang_va);
-    double t = cos(area_2 - ang_va);
-    double u = t - cos_va;
-    double v = s + (sin_va * cos_c);
-    double q_top = (((v * t) - (u * s)) * cos_va) - v;
-    double q_bottom = ((v * s) + (u * t)) * sin_va;
-    double q = q_top / q_bottom;
-    V3 vc_2 = (va * (float)q) + (normalized(vc - (va * dot(vc, va))) * (float)sqrt(1.0 - (q * q)));
+    R cos_a = (R)rmin(rmax(dot(vb, vc), -1.0f), 1.0f);
+    R cos_b = (R)rmin(rmax(dot(vc, va), -1.0f), 1.0f);
+    R cos_c = (R)rmin(rmax(dot(va, vb), -1.0f), 1.0f);
+    R sin_a = msqrt((R)1 - (cos_a * cos_a));
+    R sin_b = msqrt((R)1 - (cos_b * cos_b));
+    R sin_c = msqrt((R)1 - (cos_c * cos_c));
+    if (cos_a == (R)1 || cos_b == (R)1 || cos_c == (R)1) return va;
+    R cos_va = clamp1((cos_a - (cos_b * cos_c)) / (sin_b * sin_c));
+    R cos_vb = clamp1((cos_b - (cos_c * cos_a)) / (sin_c * sin_a));
+    R cos_vc = clamp1((cos_c - (cos_a * cos_b)) / (sin_a * sin_b));
+    R sin_va = msqrt((R)1 - (cos_va * cos_va));
+    R ang_va = macos(cos_va), ang_vb = macos(cos_vb), ang_vc = macos(cos_vc);
+    R area = ang_va + ang_vb + ang_vc - pi_r<R>();
+    R area_2 = area * (R)i;
+    R s = msin(area_2 - ang_va);
+    R t = mcos(area_2 - ang_va);
+    R u = t - cos_va;
+    R v = s + (sin_va * cos_c);
+    R q_top = (((v * t) - (u * s)) * cos_va) - v;
+    R q_bottom = ((v * s) + (u * t)) * sin_va;
+    R q = q_top / q_bottom;
+    V3 vc_2 = (va * (float)q) + (normalized(vc - (va * dot(vc, va))) * (float)msqrt((R)1 - (q * q)));
     float z = 1.0f - (j * (1.0f - dot(vc_2, vb)));
     return (vb * z) + (normalized(vc_2 - (vb * dot(vc_2, vb))) * sqrtf(1.0f - (z * z)));
 }

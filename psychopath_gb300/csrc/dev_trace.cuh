@@ -78,10 +78,17 @@ DI uint32_t node_hits(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, flo
         }
     }
     uint32_t m = 0;
-    m |= slab_hit(b.xlo.x, b.xhi.x, b.ylo.x, b.yhi.x, b.zlo.x, b.zhi.x, o, di, tmax) ? 1u : 0u;
-    m |= slab_hit(b.xlo.y, b.xhi.y, b.ylo.y, b.yhi.y, b.zlo.y, b.zhi.y, o, di, tmax) ? 2u : 0u;
-    m |= slab_hit(b.xlo.z, b.xhi.z, b.ylo.z, b.yhi.z, b.zlo.z, b.zhi.z, o, di, tmax) ? 4u : 0u;
-    m |= slab_hit(b.xlo.w, b.xhi.w, b.ylo.w, b.yhi.w, b.zlo.w, b.zhi.w, o, di, tmax) ? 8u : 0u;
+    if (slab_safe(o, di, tmax)) {
+        m |= slab_hit_finite(b.xlo.x, b.xhi.x, b.ylo.x, b.yhi.x, b.zlo.x, b.zhi.x, o, di, tmax) ? 1u : 0u;
+        m |= slab_hit_finite(b.xlo.y, b.xhi.y, b.ylo.y, b.yhi.y, b.zlo.y, b.zhi.y, o, di, tmax) ? 2u : 0u;
+        m |= slab_hit_finite(b.xlo.z, b.xhi.z, b.ylo.z, b.yhi.z, b.zlo.z, b.zhi.z, o, di, tmax) ? 4u : 0u;
+        m |= slab_hit_finite(b.xlo.w, b.xhi.w, b.ylo.w, b.yhi.w, b.zlo.w, b.zhi.w, o, di, tmax) ? 8u : 0u;
+    } else {
+        m |= slab_hit(b.xlo.x, b.xhi.x, b.ylo.x, b.yhi.x, b.zlo.x, b.zhi.x, o, di, tmax) ? 1u : 0u;
+        m |= slab_hit(b.xlo.y, b.xhi.y, b.ylo.y, b.yhi.y, b.zlo.y, b.zhi.y, o, di, tmax) ? 2u : 0u;
+        m |= slab_hit(b.xlo.z, b.xhi.z, b.ylo.z, b.yhi.z, b.zlo.z, b.zhi.z, o, di, tmax) ? 4u : 0u;
+        m |= slab_hit(b.xlo.w, b.xhi.w, b.ylo.w, b.yhi.w, b.zlo.w, b.zhi.w, o, di, tmax) ? 8u : 0u;
+    }
     return m & ((1u << count) - 1u);
 }
 
@@ -197,8 +204,15 @@ struct TraceCount {
     uint32_t nodes, tris;
 };
 
+// Copies the traversal table into shared memory (per-lane indexed reads of
+// __constant__ memory would serialize across the warp).
+DI void load_traversal_table(uint8_t *smem) {
+    for (int i = threadIdx.x; i < 8 * 48; i += blockDim.x) smem[i] = (&c_traversal_table[0][0])[i];
+    __syncthreads();
+}
+
 template <int STACK, bool COUNT = false>
-DI bool trace_ray(const GScene &S, V3 o, V3 d, float tmax, float time, bool occl, HitRec &hit,
+DI bool trace_ray(const GScene &S, const uint8_t *table, V3 o, V3 d, float tmax, float time, bool occl, HitRec &hit,
                   TraceCount *cnt = nullptr) {
     hit.kind = PSY_HIT_MISS_K;
     if (S.top_root == PSY_REF_NONE) return true;
@@ -207,7 +221,7 @@ DI bool trace_ray(const GScene &S, V3 o, V3 d, float tmax, float time, bool occl
     V3 wo = xf_point(o, ident);
     V3 wdi = recip(xf_vector(d, ident));
     V3 lo = wo, ldi = wdi;
-    const uint8_t *row = c_traversal_table[ray_code(wdi)];
+    const uint8_t *row = table + 48 * ray_code(wdi);
     uint32_t stack[STACK];
     int sp = 0;
     uint32_t cur = S.top_root;
@@ -259,7 +273,7 @@ DI bool trace_ray(const GScene &S, V3 o, V3 d, float tmax, float time, bool occl
                 if (sp >= STACK) return false;
                 stack[sp++] = PSY_REF_NONE;  // leave-instance marker
                 in_inst = true;
-                row = c_traversal_table[ray_code(ldi)];
+                row = table + 48 * ray_code(ldi);
                 cur = mesh.root;
                 continue;
             } else if (in.kind == PSY_INST_RECT) {
@@ -307,9 +321,173 @@ DI bool trace_ray(const GScene &S, V3 o, V3 d, float tmax, float time, bool occl
             in_inst = false;
             lo = wo;
             ldi = wdi;
-            row = c_traversal_table[ray_code(wdi)];
+            row = table + 48 * ray_code(wdi);
         }
     }
+}
+
+}  // namespace psyd
+
+namespace psyd {
+
+// ------------------------------------------------------------------ persistent traversal
+// Per-lane traversal state, kept in registers across the loop of the
+// persistent kernel; the stack lives in local memory and persists too.
+struct Lane {
+    V3 o, d;            // world ray
+    V3 lo, ldi;         // ray in the current space (world or instance local)
+    float tmax, time;
+    TriPre pre;
+    Xf mat;             // object->world of the current instance (has_xf)
+    uint32_t cur;       // node or leaf reference to process next
+    uint32_t slot;      // current instance slot
+    uint32_t mts, mvb;  // current mesh: vertex time samples and vertex base
+    int sp;
+    uint8_t occl, in_inst, has_xf, octant;
+    HitRec hit;
+};
+
+DI void lane_init(const GScene &S, Lane &L, V3 o, V3 d, float tmax, float time, bool occl) {
+    Xf ident = xf_identity();
+    L.o = o;
+    L.d = d;
+    L.lo = xf_point(o, ident);
+    L.ldi = recip(xf_vector(d, ident));
+    L.tmax = tmax;
+    L.time = time;
+    L.pre = tri_precompute(d);
+    L.cur = S.top_root;
+    L.slot = 0;
+    L.mts = 1;
+    L.mvb = 0;
+    L.sp = 0;
+    L.occl = occl ? 1 : 0;
+    L.in_inst = 0;
+    L.has_xf = 0;
+    L.octant = (uint8_t)ray_code(L.ldi);
+    L.hit.kind = PSY_HIT_MISS_K;
+    L.hit.prim = 0;
+    L.hit.slot = 0;
+    L.hit.t = 0.0f;
+    L.hit.b0 = L.hit.b1 = L.hit.b2 = 0.0f;
+}
+
+// Pops the next reference; returns false when the ray is finished.
+template <int STACK>
+DI bool lane_pop(Lane &L, const uint32_t *stack) {
+    while (true) {
+        if (L.sp == 0) return false;
+        L.cur = stack[--L.sp];
+        if (L.cur != PSY_REF_NONE) return true;
+        // leaving the instance: back to world space
+        Xf ident = xf_identity();
+        L.in_inst = 0;
+        L.lo = xf_point(L.o, ident);
+        L.ldi = recip(xf_vector(L.d, ident));
+        L.octant = (uint8_t)ray_code(L.ldi);
+    }
+}
+
+// One while-while iteration: descend to a leaf, process it, pop.  Returns
+// 0 = continue, 1 = finished, -1 = stack overflow.
+template <int STACK>
+DI int lane_step(const GScene &S, const uint8_t *table, Lane &L, uint32_t *stack, TraceCount &tc, bool count) {
+    if (L.cur == PSY_REF_NONE) return 1;  // empty scene
+    while (!psy_is_leaf(L.cur)) {
+        uint32_t code, cnt;
+        uint4 ch;
+        uint32_t m = S.use_fp16 ? node_hits_h(S, L.cur, L.lo, L.ldi, L.tmax, L.time, code, cnt, ch)
+                                : node_hits(S, L.cur, L.lo, L.ldi, L.tmax, L.time, code, cnt, ch);
+        if (count) tc.nodes++;
+        if (m == 0) {
+            if (!lane_pop<STACK>(L, stack)) return 1;
+            continue;
+        }
+        uint32_t order = table[48 * L.octant + code];
+        uint32_t next = PSY_REF_NONE;
+        for (int i = (int)cnt - 1; i >= 0; i--) {
+            uint32_t ci = (order >> (i * 2)) & 3u;
+            if (m & (1u << ci)) {
+                if (next != PSY_REF_NONE) {
+                    if (L.sp >= STACK) return -1;
+                    stack[L.sp++] = next;
+                }
+                next = ci == 0 ? ch.x : (ci == 1 ? ch.y : (ci == 2 ? ch.z : ch.w));
+            }
+        }
+        L.cur = next;
+    }
+    if (!L.in_inst) {
+        L.slot = psy_leaf_first(L.cur);
+        const GInstance in = S.instances[L.slot];
+        if (in.kind == PSY_INST_MESH) {
+            const GMesh M = S.meshes[in.obj];
+            L.mts = M.ts;
+            L.mvb = M.vert_base;
+            L.has_xf = in.xc != 0;
+            if (L.has_xf) {
+                Xf x = lerp_slice_xf(S.xforms + 3 * in.xs, in.xc, L.time);
+                L.lo = xf_point(L.o, x);
+                L.ldi = recip(xf_vector(L.d, x));
+                L.mat = instance_mat(S, in, L.time);
+                L.octant = (uint8_t)ray_code(L.ldi);
+            }
+            if (L.sp >= STACK) return -1;
+            stack[L.sp++] = PSY_REF_NONE;  // leave-instance marker
+            L.in_inst = 1;
+            L.cur = M.root;
+            return 0;
+        } else if (in.kind == PSY_INST_RECT) {
+            float t, b0, b1, b2;
+            uint32_t which;
+            if (rect_hit(S, in, L.o, L.d, L.tmax, L.time, t, b0, b1, b2, which)) {
+                if (L.occl) { L.hit.kind = PSY_HIT_OCCLUDE_K; return 1; }
+                L.hit.kind = PSY_HIT_LIGHT_K; L.hit.prim = which; L.hit.slot = L.slot;
+                L.hit.t = t; L.hit.b0 = b0; L.hit.b1 = b1; L.hit.b2 = b2;
+                L.tmax = t;
+            }
+        } else {
+            Xf x = instance_xf_at(S, in, L.time);
+            V3 ol = in.xc ? xf_point(L.o, x) : L.lo;
+            float t;
+            if (sphere_hit(S, in, ol, L.d, L.tmax, L.time, t)) {
+                if (L.occl) { L.hit.kind = PSY_HIT_OCCLUDE_K; return 1; }
+                L.hit.kind = PSY_HIT_LIGHT_K; L.hit.prim = 0; L.hit.slot = L.slot;
+                L.hit.t = t; L.hit.b0 = L.hit.b1 = L.hit.b2 = 0.0f;
+                L.tmax = t;
+            }
+        }
+    } else {
+        uint32_t first = psy_leaf_first(L.cur), ntri = psy_leaf_count(L.cur);
+        for (uint32_t k = 0; k < ntri; k++) {
+            uint32_t tri = first + k;
+            V3 p0, p1, p2;
+            if (L.mts == 1) {
+                const float4 *t = S.tris + 3 * (size_t)tri;
+                p0 = v3(__ldg(t)); p1 = v3(__ldg(t + 1)); p2 = v3(__ldg(t + 2));
+            } else {
+                uint4 ix = __ldg(S.tri_idx + tri);
+                const float4 *vb = S.verts + L.mvb;
+                p0 = lerp_slice_v3(vb + (size_t)ix.x * L.mts, L.mts, L.time);
+                p1 = lerp_slice_v3(vb + (size_t)ix.y * L.mts, L.mts, L.time);
+                p2 = lerp_slice_v3(vb + (size_t)ix.z * L.mts, L.mts, L.time);
+            }
+            if (L.has_xf) {
+                p0 = xf_point(p0, L.mat);
+                p1 = xf_point(p1, L.mat);
+                p2 = xf_point(p2, L.mat);
+            }
+            if (count) tc.tris++;
+            float t, b0, b1, b2;
+            if (tri_intersect(L.o, L.pre, L.tmax, p0, p1, p2, t, b0, b1, b2)) {
+                if (L.occl) { L.hit.kind = PSY_HIT_OCCLUDE_K; return 1; }
+                L.hit.kind = PSY_HIT_SURFACE_K; L.hit.prim = tri; L.hit.slot = L.slot;
+                L.hit.t = t; L.hit.b0 = b0; L.hit.b1 = b1; L.hit.b2 = b2;
+                L.tmax = t;
+            }
+        }
+    }
+    return lane_pop<STACK>(L, stack) ? 0 : 1;
 }
 
 }  // namespace psyd

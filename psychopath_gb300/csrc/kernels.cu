@@ -2,6 +2,8 @@
 // camera ray generation, the light-path state machine and accumulation.
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "dev_trace.cuh"
 #include "kernels.cuh"
 
@@ -88,6 +90,7 @@ struct SurfData {
 // rec709_to_xyz((1, 0, 1)) computed on the host.
 __constant__ GColor c_magenta;
 
+template <class R>
 __device__ void resolve_hit(const GScene &S, const HitRec &h, V3 o, V3 d, float time, SurfData &sd) {
     GInstance in = S.instances[h.slot];
     if (h.kind == PSY_HIT_SURFACE_K) {
@@ -140,7 +143,7 @@ __device__ void resolve_hit(const GScene &S, const HitRec &h, V3 o, V3 d, float 
         V3 nn = cross(a - b, a - c);
         sd.nor = nn;
         sd.nor_g = nn;
-        sd.sample_pdf = rect_sample_pdf(S, L, xf, o, d, sd.pos, time);
+        sd.sample_pdf = rect_sample_pdf<R>(S, L, xf, o, d, sd.pos, time);
         float isa = (float)(1.0 / ((double)w * (double)hh));
         sd.closure.color = color_mul(col, isa);
     } else {
@@ -154,7 +157,7 @@ __device__ void resolve_hit(const GScene &S, const HitRec &h, V3 o, V3 d, float 
         V3 nrm = xf_normal(unit, ixf);
         sd.nor = nrm;
         sd.nor_g = nrm;
-        sd.sample_pdf = sphere_sample_pdf(S, L, xf, o, time);
+        sd.sample_pdf = sphere_sample_pdf<R>(S, L, xf, o, time);
         float isa = (float)(1.0 / (4.0 * PSY_PI_64 * (double)radius * (double)radius));
         sd.closure.color = color_mul(col, isa);
     }
@@ -165,6 +168,8 @@ template <int STACK, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_rays(GScene S, const PsyRay *__restrict__ rays, uint32_t n,
                                                     PsyHit *__restrict__ hits, PsySurfaceHit *__restrict__ full,
                                                     int *err, unsigned long long *counters) {
+    __shared__ uint8_t table[8 * 48];
+    load_traversal_table(table);
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     TraceCount tc{0, 0};
     if (i < n) {
@@ -173,7 +178,7 @@ __global__ void __launch_bounds__(128) k_trace_rays(GScene S, const PsyRay *__re
         float tmax = r[6], time = r[7];
         uint32_t flags = reinterpret_cast<const uint32_t *>(r)[9];
         HitRec h;
-        if (!trace_ray<STACK, COUNT>(S, o, d, tmax, time, (flags & PSY_RAY_OCCLUSION) != 0, h, &tc)) {
+        if (!trace_ray<STACK, COUNT>(S, table, o, d, tmax, time, (flags & PSY_RAY_OCCLUSION) != 0, h, &tc)) {
             atomicExch(err, PSY_E_OVERFLOW);
             h.kind = PSY_HIT_MISS_K;
         }
@@ -198,7 +203,7 @@ __global__ void __launch_bounds__(128) k_trace_rays(GScene S, const PsyRay *__re
             f.sample_pdf = 0.0f;
             if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
                 SurfData sd;
-                resolve_hit(S, h, o, d, time, sd);
+                resolve_hit<double>(S, h, o, d, time, sd);
                 f.pos[0] = sd.pos.x; f.pos[1] = sd.pos.y; f.pos[2] = sd.pos.z;
                 f.nor[0] = sd.nor.x; f.nor[1] = sd.nor.y; f.nor[2] = sd.nor.z;
                 f.nor_g[0] = sd.nor_g.x; f.nor_g[1] = sd.nor_g.y; f.nor_g[2] = sd.nor_g.z;
@@ -240,6 +245,169 @@ cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, P
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ persistent traversal
+// Ray sources / sinks of the persistent traversal kernel.
+struct IOQueue {  // wavefront: rays of the paths listed in queue[0 .. *count)
+    const uint32_t *queue;
+    const uint32_t *count;
+    const float4 *ro, *rd;
+    const uint8_t *occl;
+    uint4 *ki;
+    float4 *tb;
+    __device__ __forceinline__ uint32_t n() const { return *count; }
+    __device__ __forceinline__ uint32_t load(uint32_t q, V3 &o, V3 &d, float &tmax, float &time, bool &oc) const {
+        uint32_t p = queue[q];
+        float4 a = ro[p], b = rd[p];
+        o = v3(a); d = v3(b); tmax = a.w; time = b.w; oc = occl[p] != 0;
+        return p;
+    }
+    __device__ __forceinline__ void store(const GScene &, uint32_t p, const HitRec &h) const {
+        ki[p] = make_uint4(h.kind, h.prim, h.slot, 0u);
+        tb[p] = make_float4(h.t, h.b0, h.b1, h.b2);
+    }
+};
+struct IORays {  // PsyRay records in, PsyHit records out
+    const PsyRay *rays;
+    uint32_t count;
+    PsyHit *hits;
+    __device__ __forceinline__ uint32_t n() const { return count; }
+    __device__ __forceinline__ uint32_t load(uint32_t q, V3 &o, V3 &d, float &tmax, float &time, bool &oc) const {
+        const float *r = reinterpret_cast<const float *>(rays + q);
+        o = v3(r[0], r[1], r[2]); d = v3(r[3], r[4], r[5]); tmax = r[6]; time = r[7];
+        oc = (reinterpret_cast<const uint32_t *>(r)[9] & PSY_RAY_OCCLUSION) != 0;
+        return q;
+    }
+    __device__ __forceinline__ void store(const GScene &S, uint32_t q, const HitRec &h) const {
+        PsyHit out;
+        out.kind = h.kind;
+        out.prim = 0; out.inst = 0; out.t = 0.0f; out.b0 = 0.0f; out.b1 = 0.0f; out.b2 = 0.0f; out.pad = 0.0f;
+        if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
+            out.prim = h.kind == PSY_HIT_SURFACE_K ? __ldg(S.tri_idx + h.prim).w : h.prim;
+            out.inst = S.instances[h.slot].id;
+            out.t = h.t; out.b0 = h.b0; out.b1 = h.b1; out.b2 = h.b2;
+        }
+        hits[q] = out;
+    }
+};
+
+// Persistent traversal: each warp keeps its lanes busy by refilling lanes
+// whose ray finished with the next rays of a global work counter (one
+// aggregated atomic per warp), so long and short rays no longer idle the
+// rest of the warp (Aila & Laine, "Understanding the Efficiency of Ray
+// Traversal on GPUs", 2009).
+template <int STACK, int MINB, class IO>
+__global__ void __launch_bounds__(128, MINB) k_trace_persist(GScene S, IO io, uint32_t *work, int *err,
+                                                            unsigned long long *counters) {
+    __shared__ uint8_t table[8 * 48];
+    load_traversal_table(table);
+    const uint32_t n = io.n();
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint32_t stack[STACK];
+    Lane L;
+    bool active = false, exhausted = false;
+    uint32_t id = 0, nr = 0;
+    TraceCount tc{0, 0};
+    const bool count = counters != nullptr;
+    while (true) {
+        unsigned idle = __ballot_sync(FULL, !active);
+        if (idle && !exhausted) {
+            int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(work, (uint32_t)__popc(idle));
+            base = __shfl_sync(FULL, base, leader);
+            if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+            if (!active) {
+                uint32_t my = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (my < n) {
+                    V3 o, d;
+                    float tmax, time;
+                    bool oc;
+                    id = io.load(my, o, d, tmax, time, oc);
+                    lane_init(S, L, o, d, tmax, time, oc);
+                    active = true;
+                    nr++;
+                }
+            }
+        }
+        if (!__any_sync(FULL, active)) break;
+        if (active) {
+            int r = lane_step<STACK>(S, table, L, stack, tc, count);
+            if (r != 0) {
+                if (r < 0) {
+                    atomicExch(err, PSY_E_OVERFLOW);
+                    L.hit.kind = PSY_HIT_MISS_K;
+                }
+                io.store(S, id, L.hit);
+                active = false;
+            }
+        }
+    }
+    if (count) {
+        unsigned long long a = tc.nodes, b = tc.tris, c = nr;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_down_sync(FULL, a, off);
+            b += __shfl_down_sync(FULL, b, off);
+            c += __shfl_down_sync(FULL, c, off);
+        }
+        if (lane == 0) {
+            atomicAdd(counters, a);
+            atomicAdd(counters + 1, b);
+            atomicAdd(counters + 2, c);
+        }
+    }
+}
+
+template <class IO, int STACK, int MINB>
+static int persist_grid() {
+    static int g = 0;
+    if (g == 0) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trace_persist<STACK, MINB, IO>, 128, 0);
+        g = sms * (per > 0 ? per : 1);
+    }
+    return g;
+}
+
+template <class IO>
+static cudaError_t launch_persist(const GScene &S, const IO &io, uint32_t max_count, int stack, int minb,
+                                  uint32_t *work, int *d_err, unsigned long long *counters, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+#define TP(SZ, MB)                                                                          \
+    {                                                                                       \
+        int g = persist_grid<IO, SZ, MB>();                                                 \
+        uint32_t need = (max_count + 127) / 128;                                            \
+        if ((uint32_t)g > need) g = (int)need;                                              \
+        if (g > 0) k_trace_persist<SZ, MB, IO><<<g, 128, 0, st>>>(S, io, work, d_err, counters); \
+    }
+    if (minb >= 8) {
+        if (stack <= 32) TP(32, 8) else if (stack <= 64) TP(64, 8) else TP(192, 8)
+    } else if (minb >= 6) {
+        if (stack <= 32) TP(32, 6) else if (stack <= 64) TP(64, 6) else TP(192, 6)
+    } else {
+        if (stack <= 32) TP(32, 4) else if (stack <= 64) TP(64, 4) else TP(192, 4)
+    }
+#undef TP
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_persist_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue,
+                                       const uint32_t *count, uint32_t max_count, int stack, int minb, uint32_t *work,
+                                       int *d_err, unsigned long long *counters, cudaStream_t st) {
+    IOQueue io{queue, count, R.o, R.d, R.occl, H.ki, H.tb};
+    return launch_persist(S, io, max_count, stack, minb, work, d_err, counters, st);
+}
+cudaError_t launch_trace_persist_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, int stack,
+                                      int minb, uint32_t *work, int *d_err, unsigned long long *counters,
+                                      cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    IORays io{rays, n, hits};
+    return launch_persist(S, io, n, stack, minb, work, d_err, counters, st);
+}
+
 // Queue-driven trace for the render wavefront: a grid-stride loop over the
 // live paths listed in queue[0 .. *count).  COUNT adds the work counters
 // (node visits, triangle tests, rays) into counters[0..2].
@@ -247,6 +415,8 @@ template <int STACK, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_queue(GScene S, RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
                                                      const uint32_t *__restrict__ count, int *err,
                                                      unsigned long long *counters) {
+    __shared__ uint8_t table[8 * 48];
+    load_traversal_table(table);
     uint32_t n = *count;
     TraceCount tc{0, 0};
     uint32_t nr = 0;
@@ -254,7 +424,7 @@ __global__ void __launch_bounds__(128) k_trace_queue(GScene S, RayBuf R, HitBuf 
         uint32_t p = queue[q];
         float4 ro = R.o[p], rd = R.d[p];
         HitRec h;
-        if (!trace_ray<STACK, COUNT>(S, v3(ro), v3(rd), ro.w, rd.w, R.occl[p] != 0, h, &tc)) {
+        if (!trace_ray<STACK, COUNT>(S, table, v3(ro), v3(rd), ro.w, rd.w, R.occl[p] != 0, h, &tc)) {
             atomicExch(err, PSY_E_OVERFLOW);
             h.kind = PSY_HIT_MISS_K;
         }
@@ -298,6 +468,7 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
 // Ray generation of Renderer::render_job (src/renderer.rs:241-275) and
 // LightPath::new (src/renderer.rs:392-431) / Camera::generate_ray
 // (src/camera.rs:74-102).
+template <class RT>
 __global__ void k_camera(GScene S, Wave w, PathState P, RayBuf R, uint32_t *queue, uint32_t *count) {
     uint32_t n = w.w * w.h * w.spp;
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -312,8 +483,8 @@ __global__ void k_camera(GScene S, Wave w, PathState P, RayBuf R, uint32_t *queu
     float d[4], d4[4];
     get_sample_4d(si, 0, x, y, w.seed, d);
     get_sample_4d(si, 1, x, y, w.seed, d4);
-    float fx = probit(d[3], 2.0f / 6.0f) + 0.5f;
-    float fy = probit(d4[0], 2.0f / 6.0f) + 0.5f;
+    float fx = probit<RT>(d[3], 2.0f / 6.0f) + 0.5f;
+    float fy = probit<RT>(d4[0], 2.0f / 6.0f) + 0.5f;
     float sx = (fx + (float)x) * cmpx;
     float sy = (fy + (float)y) * cmpy;
     float ix = (sx - 0.5f) * xe, iy = (0.5f - sy) * ye;
@@ -345,10 +516,11 @@ __global__ void k_camera(GScene S, Wave w, PathState P, RayBuf R, uint32_t *queu
 }
 
 cudaError_t launch_camera(const GScene &S, const Wave &w, PathState P, RayBuf R, uint32_t *queue, uint32_t *count,
-                          cudaStream_t st) {
+                          int prec, cudaStream_t st) {
     uint32_t n = w.w * w.h * w.spp;
     if (n == 0) return cudaSuccess;
-    k_camera<<<(n + 255) / 256, 256, 0, st>>>(S, w, P, R, queue, count);
+    if (prec == 1) k_camera<float><<<(n + 255) / 256, 256, 0, st>>>(S, w, P, R, queue, count);
+    else k_camera<double><<<(n + 255) / 256, 256, 0, st>>>(S, w, P, R, queue, count);
     return cudaGetLastError();
 }
 
@@ -369,9 +541,26 @@ __device__ __forceinline__ void push_live(bool alive, uint32_t p, uint32_t *next
 }
 
 // LightPath::next (src/renderer.rs:449-691).
+// Sort key of a path's next ray: occlusion flag, direction octant, origin
+// cell (bits/3 - 1 bits per axis of the scene box), packed into `bits` bits.
+__device__ __forceinline__ uint32_t ray_sort_key(const GScene &S, float4 o, float4 d, bool occl, int bits) {
+    uint32_t key = occl ? 1u : 0u;
+    if (bits >= 4) key |= ray_code(v3(d)) << 1;
+    if (bits >= 7) {
+        int per = (bits - 4) / 3;  // 1 or 2 bits per axis
+        float cells = (float)(1 << per);
+        uint32_t cx = (uint32_t)fminf(fmaxf((o.x - S.bounds_min.x) * S.bounds_inv_extent.x * cells, 0.0f), cells - 1.0f);
+        uint32_t cy = (uint32_t)fminf(fmaxf((o.y - S.bounds_min.y) * S.bounds_inv_extent.y * cells, 0.0f), cells - 1.0f);
+        uint32_t cz = (uint32_t)fminf(fmaxf((o.z - S.bounds_min.z) * S.bounds_inv_extent.z * cells, 0.0f), cells - 1.0f);
+        key |= ((cx << (2 * per)) | (cy << per) | cz) << 4;
+    }
+    return key;
+}
+
+template <class RT, bool SORT>
 __global__ void __launch_bounds__(128) k_shade(GScene S, Wave w, PathState P, RayBuf R, HitBuf H,
                                                const uint32_t *__restrict__ queue, const uint32_t *__restrict__ count,
-                                               uint32_t *next_queue, uint32_t *next_count) {
+                                               uint32_t *next_queue, uint32_t *next_count, SortBuf sb) {
     uint32_t n = *count;
     uint32_t stride = gridDim.x * blockDim.x;
     uint32_t nloop = (n + stride - 1) / stride * stride;  // keep whole warps in the loop for the ballot
@@ -403,7 +592,7 @@ __global__ void __launch_bounds__(128) k_shade(GScene S, Wave w, PathState P, Ra
                     h.kind = ki.x; h.prim = ki.y; h.slot = ki.z;
                     h.t = tb.x; h.b0 = tb.y; h.b1 = tb.z; h.b2 = tb.w;
                     SurfData sd;
-                    resolve_hit(S, h, o, d, time, sd);
+                    resolve_hit<RT>(S, h, o, d, time, sd);
                     const Closure &cl = sd.closure;
                     if (cl.kind == PSY_CL_EMIT) {
                         V4 c = color_to_spectral(cl.color, wl);
@@ -419,8 +608,8 @@ __global__ void __launch_bounds__(128) k_shade(GScene S, Wave w, PathState P, Ra
                         seed += 1;
                         float smp[4];
                         get_sample_4d(si, 0, px, py, seed, smp);
-                        LightSample li = scene_sample_lights(S, smp[0], smp[1], smp[2], wl, time, d, sd.pos, sd.nor,
-                                                             sd.nor_g, cl);
+                        LightSample li = scene_sample_lights<RT>(S, smp[0], smp[1], smp[2], wl, time, d, sd.pos,
+                                                                 sd.nor, sd.nor_g, cl);
                         bool found = false;
                         if (li.kind != 0 && !(li.pdf <= 0.0f) && !(li.sel_pdf <= 0.0f)) {
                             V4 att;
@@ -512,17 +701,76 @@ __global__ void __launch_bounds__(128) k_shade(GScene S, Wave w, PathState P, Ra
             }
             P.flags[p] = ev | (bounce << 2) | (has_nb << 10) | (nrays << 16);
         }
-        push_live(alive, p, next_queue, next_count);
+        if (SORT) {
+            uint32_t key = 0;
+            if (alive) key = ray_sort_key(S, R.o[p], R.d[p], R.occl[p] != 0, sb.bits);
+            unsigned mask = __ballot_sync(__activemask(), alive);
+            if (mask != 0) {
+                int lane = threadIdx.x & 31;
+                int leader = __ffs(mask) - 1;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(next_count, (uint32_t)__popc(mask));
+                base = __shfl_sync(__activemask(), base, leader);
+                if (alive) {
+                    uint32_t pos = base + __popc(mask & ((1u << lane) - 1u));
+                    sb.stage[pos] = p;
+                    sb.stage_key[pos] = (uint16_t)key;
+                    // one atomic per distinct key in the warp
+                    unsigned same = __match_any_sync(mask, key);
+                    if (lane == __ffs(same) - 1) atomicAdd(sb.bins + key, (uint32_t)__popc(same));
+                }
+            }
+        } else {
+            push_live(alive, p, next_queue, next_count);
+        }
+    }
+}
+
+// Scatter staged paths into the next queue grouped by sort key.
+__global__ void k_bin_scatter(const uint32_t *__restrict__ stage, const uint16_t *__restrict__ stage_key,
+                              const uint32_t *__restrict__ count, uint32_t *bins, int nbins, uint32_t *out) {
+    __shared__ uint32_t offs[1024];
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int k = 0; k < nbins; k++) {
+            offs[k] = acc;
+            acc += bins[k];
+        }
+    }
+    __syncthreads();
+    uint32_t n = *count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t k = stage_key[i];
+        uint32_t pos = offs[k] + atomicAdd(bins + nbins + k, 1u);
+        out[pos] = stage[i];
     }
 }
 
 cudaError_t launch_shade(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                          const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
-                         int block, int grid, cudaStream_t st) {
+                         int block, int grid, int prec, cudaStream_t st) {
     (void)block;
     if (grid <= 0) grid = (int)((max_count + 127) / 128);
     if (grid == 0) return cudaSuccess;
-    k_shade<<<grid, 128, 0, st>>>(S, w, P, R, H, queue, count, next_queue, next_count);
+    SortBuf none{nullptr, nullptr, nullptr, 0};
+    if (prec == 1) k_shade<float, false><<<grid, 128, 0, st>>>(S, w, P, R, H, queue, count, next_queue, next_count, none);
+    else k_shade<double, false><<<grid, 128, 0, st>>>(S, w, P, R, H, queue, count, next_queue, next_count, none);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade_sorted(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
+                                const uint32_t *count, uint32_t max_count, SortBuf sb, uint32_t *stage_count,
+                                uint32_t *next_queue, int grid, int prec, cudaStream_t st) {
+    if (grid <= 0) grid = (int)((max_count + 127) / 128);
+    if (grid == 0) return cudaSuccess;
+    int nbins = 1 << sb.bits;
+    cudaError_t e = cudaMemsetAsync(sb.bins, 0, 2 * nbins * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    if (prec == 1) k_shade<float, true><<<grid, 128, 0, st>>>(S, w, P, R, H, queue, count, nullptr, stage_count, sb);
+    else k_shade<double, true><<<grid, 128, 0, st>>>(S, w, P, R, H, queue, count, nullptr, stage_count, sb);
+    int sg = (int)std::min<uint32_t>((max_count + 255) / 256, 152u * 8u);
+    if (sg < 1) sg = 1;
+    k_bin_scatter<<<sg, 256, 0, st>>>(sb.stage, sb.stage_key, stage_count, sb.bins, nbins, next_queue);
     return cudaGetLastError();
 }
 

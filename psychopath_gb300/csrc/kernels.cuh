@@ -40,9 +40,19 @@ void psy_upload_constants();  // Sobol directions + traversal table -> __constan
 // Trace n PsyRay records (device) into PsyHit records (device).
 cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurfaceHit *full,
                               int stack, int block, int *d_err, unsigned long long *counters, cudaStream_t st);
+// Persistent traversal kernels with per-lane ray refill.  `minb` selects the
+// register budget (4 or 8 resident blocks of 128 threads per SM); `work` is a
+// device counter the launch zeroes first.
+cudaError_t launch_trace_persist_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue,
+                                       const uint32_t *count, uint32_t max_count, int stack, int minb, uint32_t *work,
+                                       int *d_err, unsigned long long *counters, cudaStream_t st);
+cudaError_t launch_trace_persist_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, int stack,
+                                      int minb, uint32_t *work, int *d_err, unsigned long long *counters,
+                                      cudaStream_t st);
 // Camera rays for a wave; fills queue with 0..n-1 and *count = n.
+// prec: 0 = f64 sampling arithmetic as the reference, 1 = f32.
 cudaError_t launch_camera(const GScene &S, const Wave &w, PathState P, RayBuf R, uint32_t *queue, uint32_t *count,
-                          cudaStream_t st);
+                          int prec, cudaStream_t st);
 // Trace the queued rays of a wave.
 cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
                                uint32_t max_count, int stack, int block, int grid, int *d_err,
@@ -50,7 +60,20 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
 // LightPath::next for the queued paths; live paths go to next_queue.
 cudaError_t launch_shade(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                          const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
-                         int block, int grid, cudaStream_t st);
+                         int block, int grid, int prec, cudaStream_t st);
+// Ray binning between wavefront iterations: with sort_bits > 0 the shade
+// kernel appends live paths to `stage` with a key (occlusion flag, direction
+// octant, origin cell) and counts keys in `bins`; k_bin_scatter then writes
+// them grouped by key into the next queue.
+struct SortBuf {
+    uint32_t *stage;      // staged path ids
+    uint16_t *stage_key;  // their keys
+    uint32_t *bins;       // [2 * nbins]: key counts, then fill cursors
+    int bits;             // key width: 0 (no sort), 1, 4, 7 or 10
+};
+cudaError_t launch_shade_sorted(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
+                                const uint32_t *count, uint32_t max_count, SortBuf sb, uint32_t *stage_count,
+                                uint32_t *next_queue, int grid, int prec, cudaStream_t st);
 // Per-pixel XYZ (sum over samples in sample order / spp) into xyz[(y*W + x)*3].
 cudaError_t launch_accumulate(const GScene &S, const Wave &w, PathState P, float *xyz, uint32_t img_w,
                               cudaStream_t st);

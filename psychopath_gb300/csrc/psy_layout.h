@@ -100,7 +100,10 @@ struct __align__(16) GLightTreeNode {
 struct __align__(16) GDistant {
     uint32_t key_base, nkeys;
     float energy;
-    uint32_t pad;
+    uint32_t is_static;  // one key: the cone constants below are valid
+    double ctm;          // cos(radius), evaluated by the host in f64
+    float sai;           // (float)(1 / (2 pi (1 - cos(radius)))) = solid-angle inverse = cone pdf
+    float pad;
 };
 
 // Everything the kernels need, passed by value as a kernel argument.
@@ -138,4 +141,5 @@ struct GScene {
     uint32_t use_fp16;
     float distant_energy_total;  // sum of distant light energies
     float lt_root_energy;
+    float4 bounds_min, bounds_inv_extent;  // scene box, for the ray sort key's origin cell
 };

@@ -611,6 +611,15 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
         ibounds[i] = transform_bounds(objs[in.object].bounds, in.xform_count ? &xforms[in.xform_start] : nullptr, in.xform_count);
     }
     for (auto &x : xforms) push_xf(hs.xforms, x);
+    {
+        BB u = bb_empty();
+        for (auto &v : ibounds)
+            for (auto &b : v) u = bb_or(u, b);
+        for (int a = 0; a < 3; a++) {
+            hs.scene_min[a] = std::isfinite(u.mn[a]) ? u.mn[a] : 0.0f;
+            hs.scene_max[a] = std::isfinite(u.mx[a]) ? u.mx[a] : 0.0f;
+        }
+    }
     std::vector<uint32_t> iorder(ni);
     for (uint32_t i = 0; i < ni; i++) iorder[i] = i;
     uint32_t top_push = 0;
@@ -777,6 +786,14 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
         }
         g.energy = e / (float)dl.num_keys;
         total = total + g.energy;
+        if (dl.num_keys == 1) {
+            // DistantDiskLight::sample_from_point constants (src/light/distant_disk_light.rs:67-83)
+            double radius = (double)dl.radii[0];
+            double ctm = std::cos(radius);
+            g.is_static = 1;
+            g.ctm = ctm;
+            g.sai = (float)(1.0 / (2.0 * 3.14159265358979323846 * (1.0 - ctm)));
+        }
         hs.distant.push_back(g);
     }
     hs.distant_energy_total = total;

@@ -37,6 +37,7 @@ struct HostScene {
     float distant_energy_total = 0.0f;
     float lt_root_energy = 0.0f;
     bool lt_empty = true;
+    float scene_min[3] = {0, 0, 0}, scene_max[3] = {0, 0, 0};  // union of instance bounds
     GColor background{};
     uint32_t width = 0, height = 0, spp = 0, seed = 0, max_bounces = 2;
     // per mesh object (desc order): BVH-order original triangle indices and BVH4 node count

@@ -58,6 +58,8 @@ def lib(path=None):
     L.psy_debug_scene_info.argtypes = [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]
     L.psy_debug_set_launch.argtypes = [vp, C.c_int, u32]
     L.psy_debug_counters.argtypes = [vp, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    L.psy_debug_set_trace.argtypes = [vp, C.c_int, C.c_int]
+    L.psy_debug_set_sort.argtypes = [vp, C.c_int]
     L.psy_debug_host_build.argtypes = [vp, vp, u32, vp, C.POINTER(u32), C.POINTER(u32)]
     _lib = L
     return L
@@ -85,11 +87,12 @@ def host_build_info(scene_data, obj, bounds="fp32"):
 class Scene:
     """A scene resident on the GPU (psy_scene_create)."""
 
-    def __init__(self, scene_data, bounds="fp32"):
+    def __init__(self, scene_data, bounds="fp32", shading="f64"):
         self.data = scene_data
         self._desc = scene_data.desc()
         opts = abi.PsySceneOptions()
         opts.bounds_precision = abi.PSY_BOUNDS_FP16 if bounds == "fp16" else abi.PSY_BOUNDS_FP32
+        opts.shading_precision = abi.PSY_SHADING_F32 if shading == "f32" else abi.PSY_SHADING_F64
         h = C.c_void_p()
         _check(lib().psy_scene_create(C.byref(self._desc), C.byref(opts), C.byref(h)))
         self.h = h
@@ -130,6 +133,15 @@ class Scene:
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
         _check(lib().psy_debug_counters(self.h, 1 if enable else 0, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
+
+    def set_trace(self, mode=1, minb=4):
+        """Traversal kernel: mode 0 = one thread per ray, 1 = persistent with
+        lane refill; minb = target resident blocks per SM (4 or 8)."""
+        _check(lib().psy_debug_set_trace(self.h, mode, minb))
+
+    def set_sort(self, bits):
+        """Ray binning key width between wavefront iterations (0 = off)."""
+        _check(lib().psy_debug_set_sort(self.h, bits))
 
     def set_launch(self, grid=0, wave_paths=0):
         _check(lib().psy_debug_set_launch(self.h, grid, wave_paths))

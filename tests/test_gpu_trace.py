@@ -129,3 +129,19 @@ def test_empty_batch_and_misses(gpu_lib):
                              np.array([[0, 0, 1], [0.01, 0, 1], [0, 0.01, 1], [0.1, 0.1, 1]], dtype=np.float32))
     h = tr.trace(rays)
     assert (h["kind"] == abi.PSY_HIT_MISS).all()
+
+
+@pytest.mark.parametrize("mode,minb", [(0, 4), (1, 4), (1, 6), (1, 8)])
+def test_trace_kernel_variants_identical(gpu_lib, mode, minb):
+    """Every traversal kernel variant (one thread per ray, persistent with lane
+    refill at each register budget) returns identical hits."""
+    s = sc.motion_small()
+    rays = sc.targeted_rays(20000, [-50, -50, -50], [50, 50, 50], [-60, -60, 60], [60, 60, 95], seed=9,
+                            time_random=True)
+    g = gpu.Scene(s)
+    tr = gpu.Tracer(g)
+    g.set_trace(0, 4)
+    ref = tr.trace(rays)
+    g.set_trace(mode, minb)
+    h = tr.trace(rays)
+    assert np.array_equal(h, ref)
