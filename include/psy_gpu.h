@@ -275,6 +275,30 @@ int psy_render_image_device(PsyScene *scene, const uint32_t *crop,
 int psy_render_image(PsyScene *scene, const uint32_t *crop, float *xyz_out,
                      PsyRenderStats *stats);
 
+/* Render one bucket without allocating device memory.  This call has no
+ * counterpart in the reference: it exists for hosts that cannot call
+ * cudaMalloc once they are running -- for example a process whose device
+ * memory is reserved up front by another framework's allocator, or a render
+ * worker that must keep a fixed memory footprint after start-up.  The caller
+ * passes d_xyz_out, a DEVICE buffer of bucket->w * bucket->h * 3 floats
+ * (row-major within the bucket), and receives the same values
+ * psy_render_bucket writes.  All scratch lives in one static device array of
+ * the library (46.25 MiB, held on every GPU that loads the library until the
+ * process exits), so a bucket may hold at most PSY_NOALLOC_MAX_SAMPLES
+ * samples (w * h * spp); larger buckets are rejected with PSY_E_INVALID.
+ * Nothing has to start at zero: every value of d_xyz_out is overwritten, and
+ * the call clears its own queue counters and error word inside the array at
+ * the start of each call.  The scene itself must have been created (its
+ * geometry upload is the one allocation, made at psy_scene_create).
+ * The first call on a device looks up that array's device address, so make
+ * the first call before any stream capture.  Every call shares the array:
+ * calls that overlap on the GPU (other threads, other streams) race and must
+ * be serialised by the caller.  The call runs on `stream` (NULL: the scene's
+ * stream) and returns after that stream has finished the bucket. */
+#define PSY_NOALLOC_MAX_SAMPLES 262144u
+int psy_render_bucket_noalloc(PsyScene *scene, const PsyBucket *bucket, uint32_t spp, uint32_t seed,
+                              float *d_xyz_out, void *stream);
+
 /* ---------------------------------------------------------------- misc */
 
 /* Short description of the calling thread's last error. */

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "kernels.cuh"
@@ -332,16 +333,10 @@ int psy_rays_traced(const PsyScene *s, uint64_t *count) {
 
 // Render the pixels of region (x0, y0, w, h) into d_xyz (image-sized, row
 // stride img_w) as a sequence of waves of whole pixel rows.
-static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h, uint32_t spp, uint32_t seed,
-                         float *d_xyz, uint32_t img_w, cudaStream_t st, PsyRenderStats *stats) {
+int render_region_core(PsyScene *s, const WaveBufs &B, uint32_t rows, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
+                       uint32_t spp, uint32_t seed, float *d_xyz, uint32_t img_w, cudaStream_t st,
+                       PsyRenderStats *stats) {
     if (spp == 0 || w == 0 || h == 0) return PSY_OK;
-    uint64_t row_paths = (uint64_t)w * spp;
-    uint32_t rows = (uint32_t)std::max<uint64_t>(1, s->wave_paths / row_paths);
-    rows = std::min(rows, h);
-    uint64_t max_paths = (uint64_t)rows * row_paths;
-    if (max_paths > 0xFFFFFFFFull) return fail(PSY_E_UNSUPPORTED, "wave too large");
-    int r = ensure_render(s, (uint32_t)max_paths);
-    if (r != PSY_OK) return r;
     uint32_t iters = 2 * s->g.max_bounces + 3;
     bool timing = stats != nullptr;
     // events: camera start/end, per iteration trace start/end + shade end, accumulate end
@@ -351,11 +346,7 @@ static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint
         for (auto &e : ev) cudaEventCreate(&e);
         CK(cudaMemsetAsync(s->d_raycount, 0, 8, st), "memset");
     }
-    if (s->counting) {
-        int rr = ensure_counters(s);
-        if (rr != PSY_OK) return rr;
-    }
-    unsigned long long *ctr = s->counting ? s->d_counters : nullptr;
+    unsigned long long *ctr = (s->counting && stats) ? s->d_counters : nullptr;
     double t_gen = 0, t_trace = 0, t_shade = 0, t_acc = 0;
     auto t0 = std::chrono::steady_clock::now();
     for (uint32_t y = y0; y < y0 + h; y += rows) {
@@ -364,38 +355,38 @@ static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint
         wv.spp = spp; wv.seed = seed;
         uint32_t n = wv.w * wv.h * spp;
         if (timing) cudaEventRecord(ev[0], st);
-        CK(launch_camera(s->g, wv, s->P, s->R, s->queue[0], s->counts, s->prec, st), "camera launch");
+        CK(launch_camera(s->g, wv, B.P, B.R, B.queue[0], B.counts, s->prec, st), "camera launch");
         if (timing) cudaEventRecord(ev[1], st);
         int cur = 0;
         for (uint32_t it = 0; it < iters; it++) {
             if (timing) cudaEventRecord(ev[2 + 3 * it], st);
             if (s->trace_mode == 1)
-                CK(launch_trace_persist_queue(s->g, s->R, s->H, s->queue[cur], s->counts + cur, n, s->stack, s->minb,
-                                              s->d_work, s->d_err, ctr, st),
+                CK(launch_trace_persist_queue(s->g, B.R, B.H, B.queue[cur], B.counts + cur, n, s->stack, s->minb,
+                                              B.work, B.err, ctr, st),
                    "trace launch");
             else
-                CK(launch_trace_queue(s->g, s->R, s->H, s->queue[cur], s->counts + cur, n, s->stack, 128, s->grid,
-                                      s->d_err, ctr, st),
+                CK(launch_trace_queue(s->g, B.R, B.H, B.queue[cur], B.counts + cur, n, s->stack, 128, s->grid,
+                                      B.err, ctr, st),
                    "trace launch");
             if (timing) cudaEventRecord(ev[3 + 3 * it], st);
-            CK(cudaMemsetAsync(s->counts + (cur ^ 1), 0, 4, st), "memset count");
-            if (s->sort_bits > 0) {
-                SortBuf sb{s->d_stage, s->d_stage_key, s->d_bins, s->sort_bits};
-                CK(launch_shade_sorted(s->g, wv, s->P, s->R, s->H, s->queue[cur], s->counts + cur, n, sb,
-                                       s->counts + (cur ^ 1), s->queue[cur ^ 1], s->grid, s->prec, st),
+            CK(cudaMemsetAsync(B.counts + (cur ^ 1), 0, 4, st), "memset count");
+            if (s->sort_bits > 0 && B.stage) {
+                SortBuf sb{B.stage, B.stage_key, B.bins, s->sort_bits};
+                CK(launch_shade_sorted(s->g, wv, B.P, B.R, B.H, B.queue[cur], B.counts + cur, n, sb,
+                                       B.counts + (cur ^ 1), B.queue[cur ^ 1], s->grid, s->prec, st),
                    "shade launch");
             } else {
-                CK(launch_shade(s->g, wv, s->P, s->R, s->H, s->queue[cur], s->counts + cur, n, s->queue[cur ^ 1],
-                                s->counts + (cur ^ 1), 128, s->grid, s->prec, st),
+                CK(launch_shade(s->g, wv, B.P, B.R, B.H, B.queue[cur], B.counts + cur, n, B.queue[cur ^ 1],
+                                B.counts + (cur ^ 1), 128, s->grid, s->prec, st),
                    "shade launch");
             }
             if (timing) cudaEventRecord(ev[4 + 3 * it], st);
             cur ^= 1;
         }
-        CK(launch_accumulate(s->g, wv, s->P, d_xyz, img_w, st), "accumulate launch");
+        CK(launch_accumulate(s->g, wv, B.P, d_xyz, img_w, st), "accumulate launch");
         if (timing) {
             cudaEventRecord(ev[2 + 3 * iters], st);
-            CK(launch_count_rays(s->P, n, s->d_raycount, st), "count launch");
+            CK(launch_count_rays(B.P, n, s->d_raycount, st), "count launch");
             CK(cudaEventSynchronize(ev[2 + 3 * iters]), "event sync");
             float ms;
             cudaEventElapsedTime(&ms, ev[0], ev[1]);
@@ -424,6 +415,128 @@ static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint
         for (auto &e : ev) cudaEventDestroy(e);
         s->rays_traced += rc;
     }
+    return PSY_OK;
+}
+
+
+// Render with the scene's own wavefront buffers (allocated on first use,
+// sized for waves of whole pixel rows up to wave_paths paths).
+static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h, uint32_t spp, uint32_t seed,
+                         float *d_xyz, uint32_t img_w, cudaStream_t st, PsyRenderStats *stats) {
+    if (spp == 0 || w == 0 || h == 0) return PSY_OK;
+    uint64_t row_paths = (uint64_t)w * spp;
+    uint32_t rows = (uint32_t)std::max<uint64_t>(1, s->wave_paths / row_paths);
+    rows = std::min(rows, h);
+    uint64_t max_paths = (uint64_t)rows * row_paths;
+    if (max_paths > 0xFFFFFFFFull) return fail(PSY_E_UNSUPPORTED, "wave too large");
+    int r = ensure_render(s, (uint32_t)max_paths);
+    if (r != PSY_OK) return r;
+    if (s->counting && stats) {
+        r = ensure_counters(s);
+        if (r != PSY_OK) return r;
+    }
+    WaveBufs B;
+    B.P = s->P; B.R = s->R; B.H = s->H;
+    B.queue[0] = s->queue[0]; B.queue[1] = s->queue[1];
+    B.counts = s->counts;
+    B.work = s->d_work;
+    B.err = s->d_err;
+    B.stage = s->d_stage; B.stage_key = s->d_stage_key; B.bins = s->d_bins;
+    B.cap = s->cap_paths;
+    return render_region_core(s, B, rows, x0, y0, w, h, spp, seed, d_xyz, img_w, st, stats);
+}
+
+
+// ---------------------------------------------------------------- no-allocation bucket render
+// Scratch of psy_render_bucket_noalloc: one file-scope device array, resident
+// on every GPU that loads this library until the process exits.  Host code
+// must not pass the symbol itself to a kernel (on the host it is only a
+// stand-in); its device address comes from cudaGetSymbolAddress, taken once
+// per device with that device current.
+namespace {
+constexpr size_t kNoallocAlign = 256;
+constexpr size_t na_round(size_t b) { return (b + kNoallocAlign - 1) / kNoallocAlign * kNoallocAlign; }
+constexpr size_t kNoallocPaths = PSY_NOALLOC_MAX_SAMPLES;
+// path state (9 arrays), ray (3), hit (2), two queues, control block
+constexpr size_t kNoallocBytes = 6 * na_round(kNoallocPaths * 16) + na_round(kNoallocPaths * 8) +
+                                 2 * na_round(kNoallocPaths * 4) + 2 * na_round(kNoallocPaths * 16) +
+                                 na_round(kNoallocPaths) + 2 * na_round(kNoallocPaths * 16) +
+                                 2 * na_round(kNoallocPaths * 4) + na_round(1024);
+}  // namespace
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {nullptr};
+
+// Device address of the scratch array on the current device (set up on the
+// first call per device).
+int noalloc_base(unsigned char **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= 64) return fail(PSY_E_UNSUPPORTED, "device index beyond 63");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+    return PSY_OK;
+}
+}  // namespace
+
+extern "C" int psy_render_bucket_noalloc(PsyScene *s, const PsyBucket *b, uint32_t spp, uint32_t seed,
+                                         float *d_xyz_out, void *stream) {
+    if (!s || !b || !d_xyz_out) return fail(PSY_E_INVALID, "null argument");
+    if (b->w == 0 || b->h == 0 || spp == 0) return fail(PSY_E_INVALID, "empty bucket or zero spp");
+    if ((uint64_t)b->x + b->w > s->g.width || (uint64_t)b->y + b->h > s->g.height)
+        return fail(PSY_E_INVALID, "bucket outside the image");
+    uint64_t n = (uint64_t)b->w * b->h * spp;
+    if (n > PSY_NOALLOC_MAX_SAMPLES)
+        return fail(PSY_E_INVALID, "bucket too large for the no-allocation scratch: w*h*spp must be <= " +
+                                       std::to_string(PSY_NOALLOC_MAX_SAMPLES));
+    unsigned char *base = nullptr;
+    int r = noalloc_base(&base);
+    if (r != PSY_OK) return r;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        unsigned char *p = base + off;
+        off += na_round(bytes);
+        return p;
+    };
+    const size_t C = kNoallocPaths;
+    WaveBufs B;
+    B.P.color = (float4 *)take(C * 16); B.P.latt = (float4 *)take(C * 16); B.P.pending = (float4 *)take(C * 16);
+    B.P.nafac = (float4 *)take(C * 16); B.P.nb_o = (float4 *)take(C * 16); B.P.nb_d = (float4 *)take(C * 16);
+    B.P.tw = (float2 *)take(C * 8); B.P.seed = (uint32_t *)take(C * 4); B.P.flags = (uint32_t *)take(C * 4);
+    B.R.o = (float4 *)take(C * 16); B.R.d = (float4 *)take(C * 16); B.R.occl = (uint8_t *)take(C);
+    B.H.ki = (uint4 *)take(C * 16); B.H.tb = (float4 *)take(C * 16);
+    B.queue[0] = (uint32_t *)take(C * 4); B.queue[1] = (uint32_t *)take(C * 4);
+    unsigned char *ctrl = take(1024);
+    B.counts = (uint32_t *)ctrl;            // [2]
+    B.work = (uint32_t *)(ctrl + 256);      // persistent-kernel work counter
+    B.err = (int *)(ctrl + 512);            // device error word
+    B.stage = nullptr; B.stage_key = nullptr; B.bins = nullptr;
+    B.cap = (uint32_t)C;
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    std::lock_guard<std::mutex> lk(s->mu);
+    // every call shares the scratch: clear the control block (queue lengths,
+    // work counter, error word); the camera kernel writes all path state
+    CK(cudaMemsetAsync(ctrl, 0, 1024, st), "clear scratch control block");
+    // the bucket's pixels land at (x - b.x, y - b.y) of a bucket-sized image
+    float *img = d_xyz_out - ((size_t)b->y * b->w + b->x) * 3;
+    int sort = s->sort_bits;
+    s->sort_bits = 0;
+    r = render_region_core(s, B, b->h, b->x, b->y, b->w, b->h, spp, seed, img, b->w, st, nullptr);
+    s->sort_bits = sort;
+    if (r != PSY_OK) return r;
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, B.err, sizeof(int), cudaMemcpyDeviceToHost, st), "read error word");
+    CK(cudaStreamSynchronize(st), "stream sync");
+    if (h != 0) return fail(h, "device reported error (traversal stack overflow)");
     return PSY_OK;
 }
 

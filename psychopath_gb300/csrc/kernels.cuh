@@ -74,6 +74,21 @@ struct SortBuf {
 cudaError_t launch_shade_sorted(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                                 const uint32_t *count, uint32_t max_count, SortBuf sb, uint32_t *stage_count,
                                 uint32_t *next_queue, int grid, int prec, cudaStream_t st);
+// All device buffers one render wave needs (owned by a scene, or carved from
+// a static scratch array by the no-allocation entry point).
+struct WaveBufs {
+    PathState P;
+    RayBuf R;
+    HitBuf H;
+    uint32_t *queue[2];
+    uint32_t *counts;      // [2] queue lengths
+    uint32_t *work;        // persistent-kernel work counter
+    int *err;              // device error word
+    uint32_t *stage;       // ray binning (may be null: no binning)
+    uint16_t *stage_key;
+    uint32_t *bins;
+    uint32_t cap;          // paths per wave
+};
 // Per-pixel XYZ (sum over samples in sample order / spp) into xyz[(y*W + x)*3].
 cudaError_t launch_accumulate(const GScene &S, const Wave &w, PathState P, float *xyz, uint32_t img_w,
                               cudaStream_t st);

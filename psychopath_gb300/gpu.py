@@ -23,7 +23,7 @@ _lib = None
 EXPORTED = [
     "psy_scene_create", "psy_scene_destroy", "psy_scene_device_bytes", "psy_trace", "psy_trace_device",
     "psy_rays_traced", "psy_render_bucket", "psy_render_image_device", "psy_render_image", "psy_last_error",
-    "psy_version",
+    "psy_version", "psy_render_bucket_noalloc",
 ]
 
 
@@ -52,6 +52,7 @@ def lib(path=None):
     L.psy_render_bucket.argtypes = [vp, vp, u32, u32, vp, vp]
     L.psy_render_image_device.argtypes = [vp, vp, vp, vp, vp]
     L.psy_render_image.argtypes = [vp, vp, vp, vp]
+    L.psy_render_bucket_noalloc.argtypes = [vp, vp, u32, u32, vp, vp]
     L.psy_last_error.restype = C.c_char_p
     L.psy_version.restype = C.c_char_p
     L.psy_debug_mesh_bvh_info.argtypes = [vp, u32, vp, C.POINTER(u32)]
@@ -189,6 +190,14 @@ class Renderer:
         cr = (C.c_uint32 * 4)(*crop) if crop is not None else None
         _check(lib().psy_render_image_device(self.scene.h, cr, d_xyz_ptr, stream, C.byref(st) if stats else None))
         return st.as_dict() if stats else None
+
+    def render_bucket_noalloc(self, x, y, w, h, d_xyz_ptr, spp=None, seed=None, stream=None):
+        """psy_render_bucket_noalloc: render into a caller-owned DEVICE buffer
+        of w*h*3 floats; the library allocates no device memory for it."""
+        b = abi.PsyBucket(x, y, w, h)
+        _check(lib().psy_render_bucket_noalloc(self.scene.h, C.byref(b),
+                                               spp if spp is not None else self.scene.spp,
+                                               seed if seed is not None else self.scene.data.seed, d_xyz_ptr, stream))
 
     def render_bucket(self, x, y, w, h, spp=None, seed=None):
         out = np.zeros((h, w, 3), dtype=np.float32)
