@@ -38,7 +38,13 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--bounds", default="fp32", choices=["fp32", "fp16"])
-    ap.add_argument("--workload", default="mesh_stress", choices=["mesh_stress", "cornell", "motion", "traversal"])
+    ap.add_argument("--workload", default="mesh_stress",
+                    choices=["mesh_stress", "cornell", "motion", "traversal", "serving"])
+    ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of Poisson arrivals")
+    ap.add_argument("--rate", type=float, default=40.0, help="serving: mean arrivals per second")
+    ap.add_argument("--wave-paths", type=int, default=1 << 23, help="serving: paths per wave of each scene lane")
+    ap.add_argument("--plain-seconds", type=float, default=20.0,
+                    help="serving: bound on the one-at-a-time plain-path baseline run")
     ap.add_argument("--rays", type=int, default=1 << 24, help="rays per set of the traversal microbenchmark")
     ap.add_argument("--level", type=int, default=8, help="icosphere subdivision level of mesh_stress")
     ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (profiling on smaller cases)")
@@ -213,7 +219,12 @@ def run_ours(args):
     rend = gpu.Renderer(scene)
     xyz = torch.zeros(H * W * 3, dtype=torch.float32, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library runs on the stream it is given, and the
+    # L2 flush and the timing events must be ordered with its kernels (the
+    # legacy default stream's handle is 0, which the ABI reads as "the
+    # scene's own stream")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
 
     for _ in range(args.warmup):
@@ -351,7 +362,8 @@ def run_traversal(args):
     peaks_path = os.path.join(HERE, "MEASURED_PEAKS.json")
     peak = float(json.load(open(peaks_path))["hbm_gbs"]) if os.path.exists(peaks_path) else 6800.0
     node_bytes = 64 if args.bounds == "fp16" else 128
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # non-null handle: kernels and events on one stream
+    torch.cuda.set_stream(stream)
     out = {}
     for name, rays in sets.items():
         n = len(rays)
@@ -403,10 +415,138 @@ def run_traversal(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- serving
+def serving_requests(duration, rate, seed=2024):
+    """Poisson arrivals: (t, scene, resolution, spp, seed) with the scene
+    uniform over the three resident scenes, the resolution uniform over
+    {256, 512, 1024} squared and spp uniform over {1, 4, 16, 64}."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t >= duration:
+            return out
+        out.append((t, int(rng.integers(0, 3)), (256, 512, 1024)[int(rng.integers(0, 3))],
+                    (1, 4, 16, 64)[int(rng.integers(0, 4))], int(rng.integers(0, 1 << 30))))
+
+
+def run_serving(args):
+    """Three resident scenes (cornell, mesh_stress, motion); requests arrive
+    as a Poisson process and are served by psy_submit with host result
+    buffers (so every latency includes the result's device-to-host copy).
+    Reports p50/p99 latency, aggregate samples/s, and the same requests'
+    samples/s when run one at a time on the plain render path."""
+    import threading
+    import numpy as np
+    import torch
+    from psychopath_gb300 import build, gpu, scenes
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    build.build()
+    sds = [scenes.cornell_box(), scenes.mesh_stress(level=args.level), scenes.motion_instances()]
+    names = ["cornell", "mesh_stress", "motion"]
+    t0 = time.perf_counter()
+    gs = [gpu.Scene(sd, bounds=args.bounds) for sd in sds]
+    build_s = time.perf_counter() - t0
+    reqs = serving_requests(args.duration, args.rate)
+    offered = sum(r * r * spp for (_, _, r, spp, _) in reqs) / args.duration
+    srv = gpu.Server(hbm_budget_bytes=120 * 10**9, wave_paths=args.wave_paths, use_graphs=True)
+    lanes = [srv.add_scene(g) for g in gs]
+    # warm-up: capture each lane's graphs, touch the image pool
+    for _ in range(max(1, args.warmup)):
+        ids = [srv.submit(lanes[k], 256, 256, 4, 1) for k in range(3)]
+        for i in ids:
+            srv.wait(i)
+    base = srv.stats()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ids = [None] * len(reqs)
+    start = time.perf_counter()
+
+    def submitter():
+        for i, (t, k, res, spp, seed) in enumerate(reqs):
+            delay = start + t - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            ids[i] = srv.submit(lanes[k], res, res, spp, seed)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    lat, qd, shared, waves = [], [], 0, 0
+    for i in range(len(reqs)):
+        while ids[i] is None:
+            time.sleep(0.0005)
+        st = srv.wait(ids[i], timeout=3600.0)
+        if st["state"] != 2:
+            raise RuntimeError("request %d ended in state %d (error %d)" % (i, st["state"], st["error"]))
+        lat.append(st["latency_s"])
+        qd.append(st["queued_s"])
+        shared += st["shared_waves"] > 0
+        waves += st["waves"]
+        srv._bufs.pop(ids[i], None)  # release the host result
+    end = time.perf_counter()
+    th.join()
+    clk = clocks.stop()
+    stats = srv.stats()
+    srv.close()
+    samples = sum(r * r * spp for (_, _, r, spp, _) in reqs)
+    served = samples / (end - start)
+    lat = np.array(lat) * 1e3
+    # the same requests one at a time on the plain path (device image, then
+    # the result copied to the host), over a bounded prefix of the list
+    dev = torch.empty(1024 * 1024 * 3, dtype=torch.float32, device="cuda")
+    host = torch.empty(1024 * 1024 * 3, dtype=torch.float32, pin_memory=False)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    p_samples, p_secs, p_n = 0, 0.0, 0
+    for (_, k, res, spp, seed) in reqs:
+        if p_secs >= args.plain_seconds:
+            break
+        t1 = time.perf_counter()
+        gs[k].render_sized(res, res, spp, seed, dev.data_ptr(), stream=stream.cuda_stream)
+        host[: res * res * 3].copy_(dev[: res * res * 3])
+        p_secs += time.perf_counter() - t1
+        p_samples += res * res * spp
+        p_n += 1
+    plain = p_samples / p_secs
+    line = {
+        "metric": "samples/s (served)", "value": served, "unit": "samples/s", "n_gpus": 1, "steps": len(reqs),
+        "warmup": args.warmup, "ms_per_step": (end - start) / max(1, len(reqs)) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes and arrivals)",
+        "config": {"workload": "serving: 3 resident scenes (%s), Poisson %.0f req/s for %.0f s (%d requests), "
+                               "resolution {256,512,1024}^2, spp {1,4,16,64}, HBM budget 120 GB" %
+                               (", ".join(names), args.rate, args.duration, len(reqs)),
+                   "bounds": args.bounds, "wave_paths": args.wave_paths, "graphs": True,
+                   "scene_build_s": round(build_s, 2)},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "mean": float(lat.mean()), "max": float(lat.max()),
+                       "queued_p50": float(np.percentile(np.array(qd) * 1e3, 50))},
+        "offered_samples_per_s": offered,
+        "overloaded": offered > served * 1.02,
+        "requests_sharing_a_wave": int(shared),
+        "plain_one_at_a_time": {"value": plain, "unit": "samples/s", "requests": p_n,
+                                "note": "psy render of each request alone (render_sized + D2H), same request list prefix"},
+        "served_over_plain": served / plain,
+        "e2e": {"value": served, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(sum(r * r * 12 for (_, _, r, _, _) in reqs) / max(1, len(reqs))),
+                "note": "psy_submit with host result buffers; latency ends when the image is in host memory"},
+        "hbm_peak_bytes": stats["hbm_peak_bytes"],
+        "waves": stats["waves"] - base["waves"],
+        "gpu_launches": stats["kernel_launches"] - base["kernel_launches"],
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.workload == "traversal":
         return run_traversal(args)
+    if args.workload == "serving":
+        return run_serving(args)
     if args.impl == "reference":
         run_reference(args)
     else:

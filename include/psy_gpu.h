@@ -299,6 +299,86 @@ int psy_render_image(PsyScene *scene, const uint32_t *crop, float *xyz_out,
 int psy_render_bucket_noalloc(PsyScene *scene, const PsyBucket *bucket, uint32_t spp, uint32_t seed,
                               float *d_xyz_out, void *stream);
 
+/* ---------------------------------------------------------------- serving */
+
+/* A render server: a persistent request loop over resident scenes.  The
+ * reference renders one scene per process invocation (src/main.rs:150-330,
+ * Renderer::render src/renderer.rs:76-191) and has no request API; these
+ * calls are the serving surface of the GPU path.  Each added scene gets a
+ * lane (its own stream and wavefront buffers).  Requests of a scene -- each
+ * with its own resolution, spp and seed -- are admitted while the HBM budget
+ * and the active-request limit allow, split into rows of pixels, and packed
+ * together into the lane's waves, so the paths of several requests share
+ * one set of wavefront queues.  Requests that arrive while waves are on the
+ * GPU join the next wave (continuous batching).  A request's image is the
+ * same whether it ran alone or among others: every path depends only on
+ * (scene, resolution, pixel, sample index, seed). */
+typedef struct PsyServer PsyServer;
+
+typedef struct PsyServerOptions {
+    uint64_t hbm_budget_bytes; /* resident scenes + lane buffers + request images (0: 120 GB) */
+    uint32_t wave_paths;       /* paths per wave of each lane (0: 4,194,304) */
+    uint32_t max_active;       /* requests admitted at once (0: 64) */
+    uint32_t use_graphs;       /* 1: replay each wave's launch sequence from a CUDA graph */
+    uint32_t waves_in_flight;  /* queued waves per lane, 1..4 (0: 2) */
+    uint32_t reserved[4];
+} PsyServerOptions;
+
+typedef struct PsyRequest {
+    uint32_t scene;            /* lane index from psy_server_add_scene */
+    uint32_t width, height;    /* resolution, through the scene's camera */
+    uint32_t spp, seed;
+    uint32_t reserved;
+    float *xyz_out;            /* HOST result, width*height*3 floats (row-major XYZ), or NULL */
+    float *d_xyz_out;          /* DEVICE result buffer instead (no image allocation, no copy), or NULL */
+} PsyRequest;
+
+#define PSY_REQ_QUEUED 0u
+#define PSY_REQ_RUNNING 1u
+#define PSY_REQ_DONE 2u
+#define PSY_REQ_CANCELLED 3u
+#define PSY_REQ_FAILED 4u
+
+typedef struct PsyRequestStatus {
+    uint32_t state;            /* PSY_REQ_* */
+    int32_t error;             /* PSY_E_* of a failed request */
+    uint64_t samples;          /* width * height * spp */
+    double queued_s;           /* submit -> admission */
+    double latency_s;          /* submit -> result in place (DONE / CANCELLED / FAILED) */
+    uint32_t waves;            /* waves that carried some of its paths */
+    uint32_t shared_waves;     /* of those, waves that also carried other requests */
+} PsyRequestStatus;
+
+typedef struct PsyServerStats {
+    uint64_t requests_done, samples_done, waves;
+    uint64_t kernel_launches;  /* kernels launched for those waves */
+    uint64_t hbm_used_bytes, hbm_peak_bytes, hbm_budget_bytes;
+    uint32_t queued, active;
+} PsyServerStats;
+
+/* Creates the server (its scheduling thread starts at once) on the current
+ * CUDA device. */
+int psy_server_create(const PsyServerOptions *opts, PsyServer **out);
+/* Makes `scene` resident for serving and returns its lane index.  The scene
+ * is borrowed: it must outlive the server.  PSY_E_NOMEM when the scene's
+ * bytes plus the lane's buffers exceed the budget. */
+int psy_server_add_scene(PsyServer *srv, PsyScene *scene, uint32_t *lane);
+/* Queues a request; returns at once with its id.  The result buffer must
+ * stay valid until the request is finished.  PSY_E_INVALID when one row of
+ * the request (width * spp paths) does not fit a wave or no output is given. */
+int psy_submit(PsyServer *srv, const PsyRequest *req, uint64_t *id);
+/* Current status of a request (PSY_E_NOTFOUND for an unknown id). */
+int psy_poll(PsyServer *srv, uint64_t id, PsyRequestStatus *status);
+/* Waits until the request is finished or timeout_s passes (PSY_E_TIMEOUT). */
+int psy_wait(PsyServer *srv, uint64_t id, double timeout_s, PsyRequestStatus *status);
+/* Cancels a queued or running request: it schedules no further rows and
+ * ends CANCELLED once its waves in flight are done (its result buffer is
+ * then partly written).  PSY_E_INVALID if it has already finished. */
+int psy_cancel(PsyServer *srv, uint64_t id);
+int psy_server_stats(PsyServer *srv, PsyServerStats *stats);
+/* Cancels what is queued or running, waits for the GPU, frees the lanes. */
+int psy_server_destroy(PsyServer *srv);
+
 /* ---------------------------------------------------------------- misc */
 
 /* Short description of the calling thread's last error. */

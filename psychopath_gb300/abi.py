@@ -20,6 +20,7 @@ PSY_SHADING_F64, PSY_SHADING_F32 = 0, 1
 PSY_RAY_OCCLUSION = 1
 PSY_NOALLOC_MAX_SAMPLES = 262144
 PSY_HIT_MISS, PSY_HIT_OCCLUDE, PSY_HIT_SURFACE, PSY_HIT_LIGHT = 0, 1, 2, 3
+PSY_REQ_QUEUED, PSY_REQ_RUNNING, PSY_REQ_DONE, PSY_REQ_CANCELLED, PSY_REQ_FAILED = 0, 1, 2, 3, 4
 
 _fp = C.POINTER(C.c_float)
 _up = C.POINTER(C.c_uint32)
@@ -104,6 +105,33 @@ class PsyRenderStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class PsyServerOptions(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("wave_paths", C.c_uint32), ("max_active", C.c_uint32),
+                ("use_graphs", C.c_uint32), ("waves_in_flight", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+
+
+class PsyRequest(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32),
+                ("seed", C.c_uint32), ("reserved", C.c_uint32), ("xyz_out", C.c_void_p), ("d_xyz_out", C.c_void_p)]
+
+
+class PsyRequestStatus(C.Structure):
+    _fields_ = [("state", C.c_uint32), ("error", C.c_int32), ("samples", C.c_uint64), ("queued_s", C.c_double),
+                ("latency_s", C.c_double), ("waves", C.c_uint32), ("shared_waves", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PsyServerStats(C.Structure):
+    _fields_ = [("requests_done", C.c_uint64), ("samples_done", C.c_uint64), ("waves", C.c_uint64),
+                ("kernel_launches", C.c_uint64), ("hbm_used_bytes", C.c_uint64), ("hbm_peak_bytes", C.c_uint64), ("hbm_budget_bytes", C.c_uint64),
+                ("queued", C.c_uint32), ("active", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # numpy structured dtypes with the same layout (for bulk ray / hit buffers)
 def ray_dtype():
     import numpy as np
@@ -126,3 +154,6 @@ def surface_hit_dtype():
 assert C.sizeof(PsyRay) == 40
 assert C.sizeof(PsyHit) == 32
 assert C.sizeof(PsySurfaceHit) == 80
+assert C.sizeof(PsyServerOptions) == 40
+assert C.sizeof(PsyRequest) == 40
+assert C.sizeof(PsyRequestStatus) == 40

@@ -13,6 +13,7 @@
 
 #include "kernels.cuh"
 #include "scene_build.h"
+#include "scene_handle.h"
 
 void psy_set_magenta(const float xyz[3]);
 
@@ -39,49 +40,9 @@ int g_device_init = 0;
 
 }  // namespace
 
-struct PsyScene {
-    GScene g{};
-    std::vector<void *> allocs;
-    uint64_t device_bytes = 0;
-    cudaStream_t stream = nullptr;
-    int *d_err = nullptr;
-    uint64_t rays_traced = 0;
-    int stack = 64;
-    // per-scene facts kept for debugging / tree checks
-    std::vector<std::vector<uint32_t>> mesh_tri_order;
-    std::vector<uint32_t> mesh_node_count;
-    std::vector<int32_t> object_to_mesh;
-    uint32_t max_stack = 0;
-    uint32_t node_count = 0;
-    // trace scratch (host-buffer calls)
-    PsyRay *d_rays = nullptr;
-    PsyHit *d_hits = nullptr;
-    PsySurfaceHit *d_full = nullptr;
-    size_t cap_rays = 0;
-    // render scratch
-    uint32_t cap_paths = 0;
-    PathState P{};
-    RayBuf R{};
-    HitBuf H{};
-    uint32_t *queue[2] = {nullptr, nullptr};
-    uint32_t *counts = nullptr;          // [2]
-    unsigned long long *d_raycount = nullptr;
-    float *d_xyz = nullptr;
-    size_t cap_xyz = 0;
-    uint32_t wave_paths = 1u << 24;      // paths per wave
-    int grid = 0;                        // persistent grid for queue kernels (0: size by queue)
-    bool counting = false;               // accumulate traversal counters during renders
-    int trace_mode = 0;                  // 0: one thread per ray, 1: persistent with lane refill
-    int prec = 0;                        // shading arithmetic: 0 f64 (reference), 1 f32
-    int sort_bits = 0;                   // ray binning key width between iterations (0: off)
-    uint32_t *d_stage = nullptr;         // binning staging queue
-    uint16_t *d_stage_key = nullptr;
-    uint32_t *d_bins = nullptr;
-    int minb = 4;                        // persistent kernel register budget (4 or 8 blocks/SM)
-    uint32_t *d_work = nullptr;          // work counter of the persistent kernels
-    unsigned long long *d_counters = nullptr;  // node visits, triangle tests, rays
-    std::mutex mu;
-};
+int psy_fail(int code, const std::string &msg) { return fail(code, msg); }
+int psy_cuda_fail(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+
 
 template <class T>
 static int upload(PsyScene *s, const std::vector<T> &v, const T **out) {
@@ -96,9 +57,10 @@ static int upload(PsyScene *s, const std::vector<T> &v, const T **out) {
 }
 
 static void free_render(PsyScene *s) {
+    s->graph.reset();
     void *ptrs[] = {s->P.color, s->P.latt, s->P.pending, s->P.nafac, s->P.nb_o, s->P.nb_d, s->P.tw, s->P.seed, s->P.flags,
                     s->R.o, s->R.d, s->R.occl, s->H.ki, s->H.tb, s->queue[0], s->queue[1], s->counts, s->d_raycount,
-                    s->d_stage, s->d_stage_key, s->d_bins};
+                    s->d_stage, s->d_stage_key, s->d_bins, s->d_waves};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     s->P = PathState{};
@@ -110,6 +72,8 @@ static void free_render(PsyScene *s) {
     s->d_stage = nullptr;
     s->d_stage_key = nullptr;
     s->d_bins = nullptr;
+    s->d_waves = nullptr;
+    s->cap_waves = 0;
     s->cap_paths = 0;
 }
 
@@ -256,6 +220,7 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
 int psy_scene_destroy(PsyScene *s) {
     if (!s) return PSY_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    s->graph.reset();
     for (void *p : s->allocs) cudaFree(p);
     free_render(s);
     if (s->d_rays) cudaFree(s->d_rays);
@@ -331,14 +296,148 @@ int psy_rays_traced(const PsyScene *s, uint64_t *count) {
 
 }  // extern "C"
 
-// Render the pixels of region (x0, y0, w, h) into d_xyz (image-sized, row
-// stride img_w) as a sequence of waves of whole pixel rows.
+// The launch sequence of one wave on stream st: camera rays, then the fixed
+// 2 * max_bounces + 3 trace/shade iterations over the live-path queues, then
+// accumulation.  Grids cover max_paths / max_pix (the wave's capacity); the
+// kernels read the actual sizes from the descriptor, so the sequence does not
+// depend on the wave's contents.  ev (optional) receives 3 + 3 * iters
+// timing events.
+int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t max_paths, uint32_t max_pix,
+                       cudaStream_t st, unsigned long long *ctr, const cudaEvent_t *ev) {
+    uint32_t iters = 2 * s->g.max_bounces + 3;
+    uint32_t n = max_paths;
+    if (ev) cudaEventRecord(ev[0], st);
+    CK(launch_camera(s->g, d_wave, n, B.P, B.R, B.queue[0], B.counts, s->prec, st), "camera launch");
+    if (ev) cudaEventRecord(ev[1], st);
+    int cur = 0;
+    for (uint32_t it = 0; it < iters; it++) {
+        if (ev) cudaEventRecord(ev[2 + 3 * it], st);
+        if (s->trace_mode == 1)
+            CK(launch_trace_persist_queue(s->g, B.R, B.H, B.queue[cur], B.counts + cur, n, s->stack, s->minb, B.work,
+                                          B.err, ctr, st),
+               "trace launch");
+        else
+            CK(launch_trace_queue(s->g, B.R, B.H, B.queue[cur], B.counts + cur, n, s->stack, 128, s->grid, B.err, ctr,
+                                  st),
+               "trace launch");
+        if (ev) cudaEventRecord(ev[3 + 3 * it], st);
+        CK(cudaMemsetAsync(B.counts + (cur ^ 1), 0, 4, st), "memset count");
+        if (s->sort_bits > 0 && B.stage) {
+            SortBuf sb{B.stage, B.stage_key, B.bins, s->sort_bits};
+            CK(launch_shade_sorted(s->g, d_wave, B.P, B.R, B.H, B.queue[cur], B.counts + cur, n, sb,
+                                   B.counts + (cur ^ 1), B.queue[cur ^ 1], s->grid, s->prec, st),
+               "shade launch");
+        } else {
+            CK(launch_shade(s->g, d_wave, B.P, B.R, B.H, B.queue[cur], B.counts + cur, n, B.queue[cur ^ 1],
+                            B.counts + (cur ^ 1), 128, s->grid, s->prec, st),
+               "shade launch");
+        }
+        if (ev) cudaEventRecord(ev[4 + 3 * it], st);
+        cur ^= 1;
+    }
+    CK(launch_accumulate(s->g, d_wave, max_pix, B.P, st), "accumulate launch");
+    if (ev) cudaEventRecord(ev[2 + 3 * iters], st);
+    return PSY_OK;
+}
+
+// Captures launch_wave on a private stream (thread-local capture mode, so
+// other threads' CUDA calls are unaffected) and replays it on st.  The graph
+// is re-captured when the launch configuration or the buffers change.
+int launch_wave_graph(PsyScene *s, const WaveBufs &B, WaveGraph &G, const WaveDesc *d_wave, uint32_t max_paths,
+                      uint32_t max_pix, cudaStream_t st) {
+    WaveLaunchKey k{s->trace_mode, s->minb, s->sort_bits, s->prec, s->stack, s->grid,
+                    max_paths, max_pix, d_wave, B.P.color};
+    if (!G.valid || !(G.key == k)) {
+        G.reset();
+        cudaStream_t cs = nullptr;
+        CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaStreamDestroy(cs);
+            return cuda_fail(e, "begin wave capture");
+        }
+        int r = launch_wave(s, B, d_wave, max_paths, max_pix, cs, nullptr, nullptr);
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(cs, &graph);
+        cudaStreamDestroy(cs);
+        if (r != PSY_OK || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return r != PSY_OK ? r : cuda_fail(e, "end wave capture");
+        }
+        e = cudaGraphInstantiate(&G.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            G.exec = nullptr;
+            return cuda_fail(e, "instantiate wave graph");
+        }
+        G.key = k;
+        G.valid = true;
+    }
+    CK(cudaGraphLaunch(G.exec, st), "wave graph launch");
+    return PSY_OK;
+}
+
+int alloc_wave_bufs(WaveBufs &B, uint32_t cap, uint32_t cap_waves, bool sorting, std::vector<void *> &allocs,
+                    uint64_t &bytes) {
+    B = WaveBufs{};
+    size_t N = cap;
+    cudaError_t e = cudaSuccess;
+    auto al = [&](auto **p, size_t b) {
+        if (e != cudaSuccess) return;
+        void *q = nullptr;
+        e = cudaMalloc(&q, b);
+        if (e == cudaSuccess) {
+            allocs.push_back(q);
+            bytes += b;
+            *p = reinterpret_cast<std::remove_pointer_t<decltype(p)>>(q);
+        }
+    };
+    al(&B.P.color, N * 16); al(&B.P.latt, N * 16); al(&B.P.pending, N * 16); al(&B.P.nafac, N * 16);
+    al(&B.P.nb_o, N * 16); al(&B.P.nb_d, N * 16); al(&B.P.tw, N * 8); al(&B.P.seed, N * 4); al(&B.P.flags, N * 4);
+    al(&B.R.o, N * 16); al(&B.R.d, N * 16); al(&B.R.occl, N);
+    al(&B.H.ki, N * 16); al(&B.H.tb, N * 16);
+    al(&B.queue[0], N * 4); al(&B.queue[1], N * 4);
+    unsigned char *ctrl = nullptr;
+    al(&ctrl, 1024);
+    if (sorting) {
+        al(&B.stage, N * 4); al(&B.stage_key, N * 2); al(&B.bins, 2 * 1024 * 4);
+    }
+    al(&B.waves, (size_t)cap_waves * sizeof(WaveDesc));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc wave buffers");
+    B.counts = reinterpret_cast<uint32_t *>(ctrl);
+    B.work = reinterpret_cast<uint32_t *>(ctrl + 256);
+    B.err = reinterpret_cast<int *>(ctrl + 512);
+    CK(cudaMemset(ctrl, 0, 1024), "clear wave control block");
+    B.cap = cap;
+    B.cap_waves = cap_waves;
+    return PSY_OK;
+}
+
+// Render the pixels of region (x0, y0, w, h) of a cam_w x cam_h image into
+// d_xyz (row stride img_w) as a sequence of waves of whole pixel rows.
 int render_region_core(PsyScene *s, const WaveBufs &B, uint32_t rows, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
-                       uint32_t spp, uint32_t seed, float *d_xyz, uint32_t img_w, cudaStream_t st,
-                       PsyRenderStats *stats) {
+                       uint32_t spp, uint32_t seed, float *d_xyz, uint32_t img_w, uint32_t cam_w, uint32_t cam_h,
+                       cudaStream_t st, PsyRenderStats *stats) {
     if (spp == 0 || w == 0 || h == 0) return PSY_OK;
     uint32_t iters = 2 * s->g.max_bounces + 3;
     bool timing = stats != nullptr;
+    // one single-segment descriptor per wave, uploaded with one copy
+    std::vector<WaveDesc> waves;
+    for (uint32_t y = y0; y < y0 + h; y += rows) {
+        WaveDesc d{};
+        WaveSeg &g = d.seg[0];
+        g.x0 = x0; g.y0 = y; g.w = w; g.h = std::min(rows, y0 + h - y);
+        g.spp = spp; g.seed = seed;
+        g.img_w = cam_w; g.img_h = cam_h;
+        g.out = d_xyz; g.out_stride = img_w;
+        d.nseg = 1; d.npix = g.w * g.h; d.npaths = d.npix * spp;
+        waves.push_back(d);
+    }
+    if (waves.size() > B.cap_waves) return fail(PSY_E_OVERFLOW, "too many waves for the descriptor buffer");
+    CK(cudaMemcpyAsync(B.waves, waves.data(), waves.size() * sizeof(WaveDesc), cudaMemcpyHostToDevice, st),
+       "upload wave descriptors");
+    uint32_t max_paths = std::min<uint32_t>(rows, h) * w * spp;
+    uint32_t max_pix = std::min<uint32_t>(rows, h) * w;
     // events: camera start/end, per iteration trace start/end + shade end, accumulate end
     std::vector<cudaEvent_t> ev;
     if (timing) {
@@ -349,44 +448,22 @@ int render_region_core(PsyScene *s, const WaveBufs &B, uint32_t rows, uint32_t x
     unsigned long long *ctr = (s->counting && stats) ? s->d_counters : nullptr;
     double t_gen = 0, t_trace = 0, t_shade = 0, t_acc = 0;
     auto t0 = std::chrono::steady_clock::now();
-    for (uint32_t y = y0; y < y0 + h; y += rows) {
-        Wave wv;
-        wv.x0 = x0; wv.y0 = y; wv.w = w; wv.h = std::min(rows, y0 + h - y);
-        wv.spp = spp; wv.seed = seed;
-        uint32_t n = wv.w * wv.h * spp;
-        if (timing) cudaEventRecord(ev[0], st);
-        CK(launch_camera(s->g, wv, B.P, B.R, B.queue[0], B.counts, s->prec, st), "camera launch");
-        if (timing) cudaEventRecord(ev[1], st);
-        int cur = 0;
-        for (uint32_t it = 0; it < iters; it++) {
-            if (timing) cudaEventRecord(ev[2 + 3 * it], st);
-            if (s->trace_mode == 1)
-                CK(launch_trace_persist_queue(s->g, B.R, B.H, B.queue[cur], B.counts + cur, n, s->stack, s->minb,
-                                              B.work, B.err, ctr, st),
-                   "trace launch");
-            else
-                CK(launch_trace_queue(s->g, B.R, B.H, B.queue[cur], B.counts + cur, n, s->stack, 128, s->grid,
-                                      B.err, ctr, st),
-                   "trace launch");
-            if (timing) cudaEventRecord(ev[3 + 3 * it], st);
-            CK(cudaMemsetAsync(B.counts + (cur ^ 1), 0, 4, st), "memset count");
-            if (s->sort_bits > 0 && B.stage) {
-                SortBuf sb{B.stage, B.stage_key, B.bins, s->sort_bits};
-                CK(launch_shade_sorted(s->g, wv, B.P, B.R, B.H, B.queue[cur], B.counts + cur, n, sb,
-                                       B.counts + (cur ^ 1), B.queue[cur ^ 1], s->grid, s->prec, st),
-                   "shade launch");
-            } else {
-                CK(launch_shade(s->g, wv, B.P, B.R, B.H, B.queue[cur], B.counts + cur, n, B.queue[cur ^ 1],
-                                B.counts + (cur ^ 1), 128, s->grid, s->prec, st),
-                   "shade launch");
-            }
-            if (timing) cudaEventRecord(ev[4 + 3 * it], st);
-            cur ^= 1;
+    // CUDA graph replay needs a spare descriptor slot (the graph reads a fixed
+    // address; each wave's descriptor is copied there first).  The
+    // no-allocation entry point has none, so it never instantiates a graph.
+    bool graph = s->use_graph && !timing && B.cap_waves > waves.size();
+    WaveDesc *slot = B.waves + (B.cap_waves - 1);
+    for (size_t i = 0; i < waves.size(); i++) {
+        int r;
+        if (graph) {
+            CK(cudaMemcpyAsync(slot, B.waves + i, sizeof(WaveDesc), cudaMemcpyDeviceToDevice, st), "wave slot copy");
+            r = launch_wave_graph(s, B, s->graph, slot, max_paths, max_pix, st);
+        } else {
+            r = launch_wave(s, B, B.waves + i, max_paths, max_pix, st, ctr, timing ? ev.data() : nullptr);
         }
-        CK(launch_accumulate(s->g, wv, B.P, d_xyz, img_w, st), "accumulate launch");
+        if (r != PSY_OK) return r;
         if (timing) {
-            cudaEventRecord(ev[2 + 3 * iters], st);
-            CK(launch_count_rays(B.P, n, s->d_raycount, st), "count launch");
+            CK(launch_count_rays(B.P, waves[i].npaths, s->d_raycount, st), "count launch");
             CK(cudaEventSynchronize(ev[2 + 3 * iters]), "event sync");
             float ms;
             cudaEventElapsedTime(&ms, ev[0], ev[1]);
@@ -399,7 +476,7 @@ int render_region_core(PsyScene *s, const WaveBufs &B, uint32_t rows, uint32_t x
             }
             cudaEventElapsedTime(&ms, ev[1 + 3 * iters], ev[2 + 3 * iters]);
             t_acc += ms * 1e-3;
-            stats->samples += n;
+            stats->samples += waves[i].npaths;
         }
     }
     if (timing) {
@@ -422,7 +499,9 @@ int render_region_core(PsyScene *s, const WaveBufs &B, uint32_t rows, uint32_t x
 // Render with the scene's own wavefront buffers (allocated on first use,
 // sized for waves of whole pixel rows up to wave_paths paths).
 static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h, uint32_t spp, uint32_t seed,
-                         float *d_xyz, uint32_t img_w, cudaStream_t st, PsyRenderStats *stats) {
+                         float *d_xyz, uint32_t img_w, cudaStream_t st, PsyRenderStats *stats, uint32_t cam_w = 0,
+                         uint32_t cam_h = 0) {
+    if (cam_w == 0) { cam_w = s->g.width; cam_h = s->g.height; }
     if (spp == 0 || w == 0 || h == 0) return PSY_OK;
     uint64_t row_paths = (uint64_t)w * spp;
     uint32_t rows = (uint32_t)std::max<uint64_t>(1, s->wave_paths / row_paths);
@@ -443,7 +522,18 @@ static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint
     B.err = s->d_err;
     B.stage = s->d_stage; B.stage_key = s->d_stage_key; B.bins = s->d_bins;
     B.cap = s->cap_paths;
-    return render_region_core(s, B, rows, x0, y0, w, h, spp, seed, d_xyz, img_w, st, stats);
+    uint32_t nwaves = (h + rows - 1) / rows + 1;  // + the graph's descriptor slot
+    if (nwaves > s->cap_waves) {
+        s->graph.reset();
+        if (s->d_waves) cudaFree(s->d_waves);
+        s->d_waves = nullptr;
+        s->cap_waves = 0;
+        CK(cudaMalloc((void **)&s->d_waves, (size_t)nwaves * sizeof(WaveDesc)), "cudaMalloc wave descriptors");
+        s->cap_waves = nwaves;
+    }
+    B.waves = s->d_waves;
+    B.cap_waves = s->cap_waves;
+    return render_region_core(s, B, rows, x0, y0, w, h, spp, seed, d_xyz, img_w, cam_w, cam_h, st, stats);
 }
 
 
@@ -457,11 +547,11 @@ namespace {
 constexpr size_t kNoallocAlign = 256;
 constexpr size_t na_round(size_t b) { return (b + kNoallocAlign - 1) / kNoallocAlign * kNoallocAlign; }
 constexpr size_t kNoallocPaths = PSY_NOALLOC_MAX_SAMPLES;
-// path state (9 arrays), ray (3), hit (2), two queues, control block
+// path state (9 arrays), ray (3), hit (2), two queues, control block, wave descriptor
 constexpr size_t kNoallocBytes = 6 * na_round(kNoallocPaths * 16) + na_round(kNoallocPaths * 8) +
                                  2 * na_round(kNoallocPaths * 4) + 2 * na_round(kNoallocPaths * 16) +
                                  na_round(kNoallocPaths) + 2 * na_round(kNoallocPaths * 16) +
-                                 2 * na_round(kNoallocPaths * 4) + na_round(1024);
+                                 2 * na_round(kNoallocPaths * 4) + na_round(1024) + na_round(sizeof(WaveDesc));
 }  // namespace
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
@@ -521,6 +611,8 @@ extern "C" int psy_render_bucket_noalloc(PsyScene *s, const PsyBucket *b, uint32
     B.err = (int *)(ctrl + 512);            // device error word
     B.stage = nullptr; B.stage_key = nullptr; B.bins = nullptr;
     B.cap = (uint32_t)C;
+    B.waves = (WaveDesc *)take(sizeof(WaveDesc));  // the bucket is one wave
+    B.cap_waves = 1;
     cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
     std::lock_guard<std::mutex> lk(s->mu);
     // every call shares the scratch: clear the control block (queue lengths,
@@ -530,7 +622,8 @@ extern "C" int psy_render_bucket_noalloc(PsyScene *s, const PsyBucket *b, uint32
     float *img = d_xyz_out - ((size_t)b->y * b->w + b->x) * 3;
     int sort = s->sort_bits;
     s->sort_bits = 0;
-    r = render_region_core(s, B, b->h, b->x, b->y, b->w, b->h, spp, seed, img, b->w, st, nullptr);
+    r = render_region_core(s, B, b->h, b->x, b->y, b->w, b->h, spp, seed, img, b->w, s->g.width, s->g.height, st,
+                           nullptr);
     s->sort_bits = sort;
     if (r != PSY_OK) return r;
     int h = 0;
@@ -674,6 +767,28 @@ int psy_debug_set_launch(PsyScene *s, int grid, uint32_t wave_paths) {
     if (!s) return fail(PSY_E_INVALID, "null");
     s->grid = grid;
     if (wave_paths >= 1024) s->wave_paths = wave_paths;
+    return PSY_OK;
+}
+// Render a whole width x height image with spp samples and seed through the
+// scene's camera (a resolution other than the scene's own) into the device
+// buffer d_xyz; returns when done.  The one-request-at-a-time form of what
+// the render server does.
+int psy_debug_render_sized(PsyScene *s, uint32_t width, uint32_t height, uint32_t spp, uint32_t seed, float *d_xyz,
+                           void *stream) {
+    if (!s || !d_xyz || width == 0 || height == 0 || spp == 0) return fail(PSY_E_INVALID, "invalid argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    int r = render_region(s, 0, 0, width, height, spp, seed, d_xyz, width, st, nullptr, width, height);
+    if (r != PSY_OK) return r;
+    CK(cudaStreamSynchronize(st), "sync");
+    return check_err(s);
+}
+// Replay each wave from a CUDA graph (1) or launch it kernel by kernel (0).
+int psy_debug_set_graph(PsyScene *s, int on) {
+    if (!s) return fail(PSY_E_INVALID, "null");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->use_graph = on != 0;
+    if (!s->use_graph) s->graph.reset();
     return PSY_OK;
 }
 

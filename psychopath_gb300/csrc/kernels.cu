@@ -464,21 +464,44 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ wave segments
+// Copies the wave descriptor into shared memory (one read per block).
+__device__ __forceinline__ void load_wave(const WaveDesc *__restrict__ g, WaveDesc &sm) {
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(g);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(&sm);
+    for (int i = threadIdx.x; i < (int)(sizeof(WaveDesc) / 4); i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+}
+__device__ __forceinline__ int seg_of_path(const WaveDesc &wd, uint32_t p) {
+    int i = 0;
+    while (i + 1 < (int)wd.nseg && p >= wd.seg[i + 1].path_begin) i++;
+    return i;
+}
+__device__ __forceinline__ int seg_of_pixel(const WaveDesc &wd, uint32_t q) {
+    int i = 0;
+    while (i + 1 < (int)wd.nseg && q >= wd.seg[i + 1].pix_begin) i++;
+    return i;
+}
+
 // ------------------------------------------------------------------ camera
 // Ray generation of Renderer::render_job (src/renderer.rs:241-275) and
 // LightPath::new (src/renderer.rs:392-431) / Camera::generate_ray
 // (src/camera.rs:74-102).
 template <class RT>
-__global__ void k_camera(GScene S, Wave w, PathState P, RayBuf R, uint32_t *queue, uint32_t *count) {
-    uint32_t n = w.w * w.h * w.spp;
+__global__ void k_camera(GScene S, const WaveDesc *__restrict__ gwave, PathState P, RayBuf R, uint32_t *queue,
+                         uint32_t *count) {
+    __shared__ WaveDesc wdesc;
+    load_wave(gwave, wdesc);
+    uint32_t n = wdesc.npaths;
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p == 0) *count = n;
     if (p >= n) return;
-    uint32_t lp = p / w.spp, si = p - lp * w.spp;
+    const WaveSeg &w = wdesc.seg[seg_of_path(wdesc, p)];
+    uint32_t lp = (p - w.path_begin) / w.spp, si = (p - w.path_begin) - lp * w.spp;
     uint32_t x = w.x0 + lp % w.w, y = w.y0 + lp / w.w;
-    float cmpx = 1.0f / (float)S.width, cmpy = 1.0f / (float)S.height;
+    float cmpx = 1.0f / (float)w.img_w, cmpy = 1.0f / (float)w.img_h;
     float min_x = -1.0f, max_x = 1.0f;
-    float min_y = -((float)S.height / (float)S.width), max_y = (float)S.height / (float)S.width;
+    float min_y = -((float)w.img_h / (float)w.img_w), max_y = (float)w.img_h / (float)w.img_w;
     float xe = max_x - min_x, ye = max_y - min_y;
     float d[4], d4[4];
     get_sample_4d(si, 0, x, y, w.seed, d);
@@ -515,12 +538,12 @@ __global__ void k_camera(GScene S, Wave w, PathState P, RayBuf R, uint32_t *queu
     queue[p] = p;
 }
 
-cudaError_t launch_camera(const GScene &S, const Wave &w, PathState P, RayBuf R, uint32_t *queue, uint32_t *count,
-                          int prec, cudaStream_t st) {
-    uint32_t n = w.w * w.h * w.spp;
+cudaError_t launch_camera(const GScene &S, const WaveDesc *d_wave, uint32_t max_paths, PathState P, RayBuf R,
+                          uint32_t *queue, uint32_t *count, int prec, cudaStream_t st) {
+    uint32_t n = max_paths;
     if (n == 0) return cudaSuccess;
-    if (prec == 1) k_camera<float><<<(n + 255) / 256, 256, 0, st>>>(S, w, P, R, queue, count);
-    else k_camera<double><<<(n + 255) / 256, 256, 0, st>>>(S, w, P, R, queue, count);
+    if (prec == 1) k_camera<float><<<(n + 255) / 256, 256, 0, st>>>(S, d_wave, P, R, queue, count);
+    else k_camera<double><<<(n + 255) / 256, 256, 0, st>>>(S, d_wave, P, R, queue, count);
     return cudaGetLastError();
 }
 
@@ -558,9 +581,12 @@ __device__ __forceinline__ uint32_t ray_sort_key(const GScene &S, float4 o, floa
 }
 
 template <class RT, bool SORT>
-__global__ void __launch_bounds__(128) k_shade(GScene S, Wave w, PathState P, RayBuf R, HitBuf H,
-                                               const uint32_t *__restrict__ queue, const uint32_t *__restrict__ count,
-                                               uint32_t *next_queue, uint32_t *next_count, SortBuf sb) {
+__global__ void __launch_bounds__(128) k_shade(GScene S, const WaveDesc *__restrict__ gwave, PathState P, RayBuf R,
+                                               HitBuf H, const uint32_t *__restrict__ queue,
+                                               const uint32_t *__restrict__ count, uint32_t *next_queue,
+                                               uint32_t *next_count, SortBuf sb) {
+    __shared__ WaveDesc wdesc;
+    load_wave(gwave, wdesc);
     uint32_t n = *count;
     uint32_t stride = gridDim.x * blockDim.x;
     uint32_t nloop = (n + stride - 1) / stride * stride;  // keep whole warps in the loop for the ballot
@@ -583,8 +609,10 @@ __global__ void __launch_bounds__(128) k_shade(GScene S, Wave w, PathState P, Ra
             float4 nbo = P.nb_o[p];
             float csp = nbo.w;  // closure_sample_pdf
             uint32_t seed = P.seed[p];
-            uint32_t pix = p / w.spp;
-            uint32_t si = p - pix * w.spp;
+            const WaveSeg &w = wdesc.seg[seg_of_path(wdesc, p)];
+            uint32_t lp = p - w.path_begin;
+            uint32_t pix = lp / w.spp;
+            uint32_t si = lp - pix * w.spp;
             uint32_t px = w.x0 + pix % w.w, py = w.y0 + pix / w.w;
             if (ev == EV_CAMERA || ev == EV_BOUNCE) {
                 if (ki.x == PSY_HIT_SURFACE_K || ki.x == PSY_HIT_LIGHT_K) {
@@ -746,19 +774,19 @@ __global__ void k_bin_scatter(const uint32_t *__restrict__ stage, const uint16_t
     }
 }
 
-cudaError_t launch_shade(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
+cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                          const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
                          int block, int grid, int prec, cudaStream_t st) {
     (void)block;
     if (grid <= 0) grid = (int)((max_count + 127) / 128);
     if (grid == 0) return cudaSuccess;
     SortBuf none{nullptr, nullptr, nullptr, 0};
-    if (prec == 1) k_shade<float, false><<<grid, 128, 0, st>>>(S, w, P, R, H, queue, count, next_queue, next_count, none);
-    else k_shade<double, false><<<grid, 128, 0, st>>>(S, w, P, R, H, queue, count, next_queue, next_count, none);
+    if (prec == 1) k_shade<float, false><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count, none);
+    else k_shade<double, false><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count, none);
     return cudaGetLastError();
 }
 
-cudaError_t launch_shade_sorted(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
+cudaError_t launch_shade_sorted(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                                 const uint32_t *count, uint32_t max_count, SortBuf sb, uint32_t *stage_count,
                                 uint32_t *next_queue, int grid, int prec, cudaStream_t st) {
     if (grid <= 0) grid = (int)((max_count + 127) / 128);
@@ -766,8 +794,8 @@ cudaError_t launch_shade_sorted(const GScene &S, const Wave &w, PathState P, Ray
     int nbins = 1 << sb.bits;
     cudaError_t e = cudaMemsetAsync(sb.bins, 0, 2 * nbins * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    if (prec == 1) k_shade<float, true><<<grid, 128, 0, st>>>(S, w, P, R, H, queue, count, nullptr, stage_count, sb);
-    else k_shade<double, true><<<grid, 128, 0, st>>>(S, w, P, R, H, queue, count, nullptr, stage_count, sb);
+    if (prec == 1) k_shade<float, true><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, nullptr, stage_count, sb);
+    else k_shade<double, true><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, nullptr, stage_count, sb);
     int sg = (int)std::min<uint32_t>((max_count + 255) / 256, 152u * 8u);
     if (sg < 1) sg = 1;
     k_bin_scatter<<<sg, 256, 0, st>>>(sb.stage, sb.stage_key, stage_count, sb.bins, nbins, next_queue);
@@ -777,26 +805,28 @@ cudaError_t launch_shade_sorted(const GScene &S, const Wave &w, PathState P, Ray
 // ------------------------------------------------------------------ accumulate
 // XYZ::from_spectral_sample / spp added per pixel (src/renderer.rs:299-310),
 // summing the pixel's samples in sample order.
-__global__ void k_accumulate(GScene S, Wave w, PathState P, float *xyz, uint32_t img_w) {
-    uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= w.w * w.h) return;
-    uint32_t x = w.x0 + pix % w.w, y = w.y0 + pix / w.w;
+__global__ void k_accumulate(GScene S, const WaveDesc *__restrict__ gwave, PathState P) {
+    __shared__ WaveDesc wdesc;
+    load_wave(gwave, wdesc);
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= wdesc.npix) return;
+    const WaveSeg &w = wdesc.seg[seg_of_pixel(wdesc, q)];
+    uint32_t lq = q - w.pix_begin;
+    uint32_t x = w.x0 + lq % w.w, y = w.y0 + lq / w.w;
     float inv = (float)w.spp;
     V3 acc = v3(0.0f, 0.0f, 0.0f);
     for (uint32_t s = 0; s < w.spp; s++) {
-        uint32_t p = pix * w.spp + s;
+        uint32_t p = w.path_begin + lq * w.spp + s;
         V3 c = xyz_from_spectral(v4(P.color[p]), P.tw[p].y);
         acc = acc + (c / inv);
     }
-    float *o = xyz + ((size_t)y * img_w + x) * 3;
+    float *o = w.out + ((size_t)y * w.out_stride + x) * 3;
     o[0] = acc.x; o[1] = acc.y; o[2] = acc.z;
 }
 
-cudaError_t launch_accumulate(const GScene &S, const Wave &w, PathState P, float *xyz, uint32_t img_w,
-                              cudaStream_t st) {
-    uint32_t n = w.w * w.h;
-    if (n == 0) return cudaSuccess;
-    k_accumulate<<<(n + 127) / 128, 128, 0, st>>>(S, w, P, xyz, img_w);
+cudaError_t launch_accumulate(const GScene &S, const WaveDesc *d_wave, uint32_t max_pix, PathState P, cudaStream_t st) {
+    if (max_pix == 0) return cudaSuccess;
+    k_accumulate<<<(max_pix + 127) / 128, 128, 0, st>>>(S, d_wave, P);
     return cudaGetLastError();
 }
 

@@ -29,10 +29,25 @@ struct HitBuf {
     uint4 *ki;        // kind, prim, slot, 0
     float4 *tb;       // t, b0, b1, b2
 };
-// A rectangular region of pixels rendered as one wave, all spp samples each.
-struct Wave {
-    uint32_t x0, y0, w, h;
+// One wave of the wavefront renderer: up to PSY_WAVE_MAX_SEGS segments, each
+// a rectangle of pixels of some image rendered with all its spp samples.
+// Segments may belong to different requests (different resolution, spp and
+// seed) that share the wave's queues.  Paths of a segment are numbered
+// pixel-major (all samples of a pixel are consecutive).
+#define PSY_WAVE_MAX_SEGS 16
+struct WaveSeg {
+    uint32_t x0, y0, w, h;  // pixel rectangle in the segment's image
     uint32_t spp, seed;
+    uint32_t img_w, img_h;  // resolution the camera maps (the request's image)
+    float *out;             // XYZ image base of the segment's image
+    uint32_t out_stride;    // row stride of `out` in pixels
+    uint32_t path_begin;    // first path of the segment in the wave
+    uint32_t pix_begin;     // first pixel of the segment in the wave
+    uint32_t pad;
+};
+struct WaveDesc {
+    uint32_t nseg, npaths, npix, pad;
+    WaveSeg seg[PSY_WAVE_MAX_SEGS];
 };
 
 void psy_upload_constants();  // Sobol directions + traversal table -> __constant__
@@ -49,16 +64,17 @@ cudaError_t launch_trace_persist_queue(const GScene &S, RayBuf R, HitBuf H, cons
 cudaError_t launch_trace_persist_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, int stack,
                                       int minb, uint32_t *work, int *d_err, unsigned long long *counters,
                                       cudaStream_t st);
-// Camera rays for a wave; fills queue with 0..n-1 and *count = n.
+// Camera rays for the wave described by d_wave (device memory; the grid
+// covers max_paths); fills queue with 0..n-1 and *count = n.
 // prec: 0 = f64 sampling arithmetic as the reference, 1 = f32.
-cudaError_t launch_camera(const GScene &S, const Wave &w, PathState P, RayBuf R, uint32_t *queue, uint32_t *count,
-                          int prec, cudaStream_t st);
+cudaError_t launch_camera(const GScene &S, const WaveDesc *d_wave, uint32_t max_paths, PathState P, RayBuf R,
+                          uint32_t *queue, uint32_t *count, int prec, cudaStream_t st);
 // Trace the queued rays of a wave.
 cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
                                uint32_t max_count, int stack, int block, int grid, int *d_err,
                                unsigned long long *counters, cudaStream_t st);
 // LightPath::next for the queued paths; live paths go to next_queue.
-cudaError_t launch_shade(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
+cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                          const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
                          int block, int grid, int prec, cudaStream_t st);
 // Ray binning between wavefront iterations: with sort_bits > 0 the shade
@@ -71,7 +87,7 @@ struct SortBuf {
     uint32_t *bins;       // [2 * nbins]: key counts, then fill cursors
     int bits;             // key width: 0 (no sort), 1, 4, 7 or 10
 };
-cudaError_t launch_shade_sorted(const GScene &S, const Wave &w, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
+cudaError_t launch_shade_sorted(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                                 const uint32_t *count, uint32_t max_count, SortBuf sb, uint32_t *stage_count,
                                 uint32_t *next_queue, int grid, int prec, cudaStream_t st);
 // All device buffers one render wave needs (owned by a scene, or carved from
@@ -88,9 +104,11 @@ struct WaveBufs {
     uint16_t *stage_key;
     uint32_t *bins;
     uint32_t cap;          // paths per wave
+    WaveDesc *waves;       // wave descriptors (device)
+    uint32_t cap_waves;
 };
-// Per-pixel XYZ (sum over samples in sample order / spp) into xyz[(y*W + x)*3].
-cudaError_t launch_accumulate(const GScene &S, const Wave &w, PathState P, float *xyz, uint32_t img_w,
-                              cudaStream_t st);
+// Per-pixel XYZ (sum over samples in sample order / spp) into each segment's
+// image, out[(y * out_stride + x) * 3].  The grid covers max_pix pixels.
+cudaError_t launch_accumulate(const GScene &S, const WaveDesc *d_wave, uint32_t max_pix, PathState P, cudaStream_t st);
 // Sum of per-path ray counts of a wave into *out (u64).
 cudaError_t launch_count_rays(PathState P, uint32_t n, unsigned long long *out, cudaStream_t st);

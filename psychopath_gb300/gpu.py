@@ -23,7 +23,8 @@ _lib = None
 EXPORTED = [
     "psy_scene_create", "psy_scene_destroy", "psy_scene_device_bytes", "psy_trace", "psy_trace_device",
     "psy_rays_traced", "psy_render_bucket", "psy_render_image_device", "psy_render_image", "psy_last_error",
-    "psy_version", "psy_render_bucket_noalloc",
+    "psy_version", "psy_render_bucket_noalloc", "psy_server_create", "psy_server_add_scene", "psy_submit",
+    "psy_poll", "psy_wait", "psy_cancel", "psy_server_stats", "psy_server_destroy",
 ]
 
 
@@ -62,6 +63,16 @@ def lib(path=None):
     L.psy_debug_set_trace.argtypes = [vp, C.c_int, C.c_int]
     L.psy_debug_set_sort.argtypes = [vp, C.c_int]
     L.psy_debug_host_build.argtypes = [vp, vp, u32, vp, C.POINTER(u32), C.POINTER(u32)]
+    L.psy_debug_set_graph.argtypes = [vp, C.c_int]
+    L.psy_debug_render_sized.argtypes = [vp, u32, u32, u32, u32, vp, vp]
+    L.psy_server_create.argtypes = [vp, C.POINTER(vp)]
+    L.psy_server_add_scene.argtypes = [vp, vp, C.POINTER(u32)]
+    L.psy_submit.argtypes = [vp, vp, C.POINTER(C.c_uint64)]
+    L.psy_poll.argtypes = [vp, C.c_uint64, vp]
+    L.psy_wait.argtypes = [vp, C.c_uint64, C.c_double, vp]
+    L.psy_cancel.argtypes = [vp, C.c_uint64]
+    L.psy_server_stats.argtypes = [vp, vp]
+    L.psy_server_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -147,6 +158,15 @@ class Scene:
     def set_launch(self, grid=0, wave_paths=0):
         _check(lib().psy_debug_set_launch(self.h, grid, wave_paths))
 
+    def set_graph(self, on=True):
+        """Replay each render wave from a captured CUDA graph."""
+        _check(lib().psy_debug_set_graph(self.h, 1 if on else 0))
+
+    def render_sized(self, width, height, spp, seed, d_xyz_ptr, stream=None):
+        """Whole image at another resolution through the scene's camera into a
+        device buffer (blocking): one request on the plain render path."""
+        _check(lib().psy_debug_render_sized(self.h, width, height, spp, seed, d_xyz_ptr, stream))
+
 
 class Tracer:
     """Tracer::from_assembly / trace / rays_traced over the GPU scene."""
@@ -207,3 +227,74 @@ class Renderer:
                                        seed if seed is not None else self.scene.data.seed, out.ctypes.data,
                                        C.byref(st)))
         return out, st.as_dict()
+
+
+class Server:
+    """Render server over resident scenes (psy_server_*, psy_submit,
+    psy_poll, psy_wait, psy_cancel)."""
+
+    def __init__(self, hbm_budget_bytes=0, wave_paths=0, max_active=0, use_graphs=False, waves_in_flight=0):
+        o = abi.PsyServerOptions()
+        o.hbm_budget_bytes = hbm_budget_bytes
+        o.wave_paths = wave_paths
+        o.max_active = max_active
+        o.use_graphs = 1 if use_graphs else 0
+        o.waves_in_flight = waves_in_flight
+        h = C.c_void_p()
+        _check(lib().psy_server_create(C.byref(o), C.byref(h)))
+        self.h = h
+        self._scenes = []
+        self._bufs = {}
+
+    def add_scene(self, scene):
+        v = C.c_uint32()
+        _check(lib().psy_server_add_scene(self.h, scene.h, C.byref(v)))
+        self._scenes.append(scene)  # the server borrows it
+        return v.value
+
+    def submit(self, lane, width, height, spp, seed, out=None, d_out=None):
+        """Queue a request.  out: a float32 host array of height*width*3
+        (allocated when neither out nor d_out is given); d_out: a device
+        pointer instead.  Returns the request id."""
+        if out is None and d_out is None:
+            out = np.zeros((height, width, 3), dtype=np.float32)
+        r = abi.PsyRequest()
+        r.scene, r.width, r.height, r.spp, r.seed = lane, width, height, spp, seed
+        r.xyz_out = out.ctypes.data if out is not None else None
+        r.d_xyz_out = d_out
+        v = C.c_uint64()
+        _check(lib().psy_submit(self.h, C.byref(r), C.byref(v)))
+        self._bufs[v.value] = out
+        return v.value
+
+    def result(self, rid):
+        return self._bufs.get(rid)
+
+    def poll(self, rid):
+        st = abi.PsyRequestStatus()
+        _check(lib().psy_poll(self.h, rid, C.byref(st)))
+        return st.as_dict()
+
+    def wait(self, rid, timeout=120.0):
+        st = abi.PsyRequestStatus()
+        _check(lib().psy_wait(self.h, rid, timeout, C.byref(st)))
+        return st.as_dict()
+
+    def cancel(self, rid):
+        _check(lib().psy_cancel(self.h, rid))
+
+    def stats(self):
+        st = abi.PsyServerStats()
+        _check(lib().psy_server_stats(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().psy_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

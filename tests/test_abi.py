@@ -47,3 +47,35 @@ def test_abi_struct_sizes():
     assert abi.ray_dtype().itemsize == 40
     assert abi.hit_dtype().itemsize == 32
     assert abi.surface_hit_dtype().itemsize == 80
+
+
+def test_ctypes_layout_matches_header(tmp_path):
+    """Every ctypes mirror in abi.py has the size and field offsets the C
+    compiler gives the header's struct (compiled with gcc, no GPU)."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    import pytest
+    from psychopath_gb300 import abi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = [n for n in dir(abi) if n.startswith("Psy") and isinstance(getattr(abi, n), type)
+               and issubclass(getattr(abi, n), C.Structure)]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "psy_gpu.h"', "int main(void) {"]
+    for n in structs:
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (n, n))
+        for f in getattr(abi, n)._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (n, f[0], n, f[0]))
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = dict(l.rsplit(" ", 1) for l in out if l.strip())
+    for n in structs:
+        T = getattr(abi, n)
+        assert int(got[n]) == C.sizeof(T), n
+        for f in T._fields_:
+            assert int(got["%s.%s" % (n, f[0])]) == getattr(T, f[0]).offset, (n, f[0])
