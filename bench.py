@@ -50,6 +50,11 @@ def parse_args():
     ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (profiling on smaller cases)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--form", default="both", choices=["both", "plain", "optimized"],
+                    help="frame workloads: which forms to time (the headline is the optimized one)")
+    ap.add_argument("--launch", default="",
+                    help="optimized form: fixed launch configuration 'mode,minb' instead of psy_autotune "
+                         "(profiling a known configuration)")
     return ap.parse_args()
 
 
@@ -198,7 +203,38 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- GPU
+def time_frames(rend, xyz, flush, stream, steps, warmup, barrier):
+    """W untimed frames, then K frames bracketed by CUDA events on the
+    render stream (L2 flushed before each).  Returns (elapsed s, summed
+    traversal-kernel s, rays, samples)."""
+    import torch
+    sp = stream.cuda_stream
+    for _ in range(warmup):
+        rend.render_device(xyz.data_ptr(), stream=sp)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    trace_s, rays, samples = 0.0, 0, 0
+    ev0.record(stream)
+    for _ in range(steps):
+        flush.zero_()
+        st = rend.render_device(xyz.data_ptr(), stream=sp, stats=True)
+        trace_s += st["trace_time"]
+        rays += st["ray_count"]
+        samples += st["samples"]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    return ev0.elapsed_time(ev1) / 1e3, trace_s, rays, samples
+
+
 def run_ours(args):
+    """Headline: the optimized form (f32 shading arithmetic, launch
+    configuration picked by psy_autotune, CUDA-graph wave replay when the
+    tuner keeps it).  Beside it: the plain form (f64 shading arithmetic as
+    the reference, default launch configuration) on the same frame, and the
+    relative RMSE between the two images."""
     import numpy as np
     import torch
     rank, world, local = dist_env()
@@ -212,61 +248,71 @@ def run_ours(args):
     sd.seed = sd.seed + rank  # independent sample sets per replica
     if args.spp:
         sd.spp = args.spp
-    t0 = time.perf_counter()
-    scene = gpu.Scene(sd, bounds=args.bounds)
-    build_s = time.perf_counter() - t0
     W, H, spp = sd.width, sd.height, sd.spp
-    rend = gpu.Renderer(scene)
-    xyz = torch.zeros(H * W * 3, dtype=torch.float32, device="cuda")
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
     # a dedicated stream: the library runs on the stream it is given, and the
     # L2 flush and the timing events must be ordered with its kernels (the
     # legacy default stream's handle is 0, which the ABI reads as "the
     # scene's own stream")
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    sp = stream.cuda_stream
+    xyz = torch.zeros(H * W * 3, dtype=torch.float32, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
-    for _ in range(args.warmup):
-        rend.render_device(xyz.data_ptr(), stream=sp)
-    torch.cuda.synchronize()
-
+    # plain form
+    t0 = time.perf_counter()
+    plain = gpu.Scene(sd, bounds=args.bounds)
+    build_s = time.perf_counter() - t0
+    plain_img = None
+    p_el, p_trace, p_rays, p_samples = 1.0, 0.0, 0, 0
+    if args.form == "both":
+        p_el, p_trace, p_rays, p_samples = time_frames(gpu.Renderer(plain), xyz, flush, stream, args.steps,
+                                                       args.warmup, barrier)
+        plain_img = xyz.cpu().numpy().copy()
+    if args.form == "plain":
+        scene = plain  # report the plain form as the line's value
+        tune = {"trace_mode": 0, "minb": 4, "wave_paths": 1 << 24, "sort_bits": 0, "use_graph": 0}
+        tune_s = 0.0
+    else:
+        plain.close()
+        # optimized form
+        scene = gpu.Scene(sd, bounds=args.bounds, shading="f32")
+        t0 = time.perf_counter()
+        if args.launch:
+            mode, minb = (int(x) for x in args.launch.split(","))
+            scene.set_trace(mode, minb)
+            tune = {"trace_mode": mode, "minb": minb, "wave_paths": 1 << 24, "sort_bits": 0, "use_graph": 0,
+                    "fixed": True}
+        else:
+            tune = scene.autotune()
+        tune_s = time.perf_counter() - t0
+    rend = gpu.Renderer(scene)
     # traversal work counters for the roofline (one extra, untimed frame)
     scene.counters(True)
-    rend.render_device(xyz.data_ptr(), stream=sp)
+    rend.render_device(xyz.data_ptr(), stream=stream.cuda_stream, stats=True)  # counters run in stats mode
     torch.cuda.synchronize()
     n_nodes, n_tris, n_rays_c = scene.counters(False)
-
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-
     clocks = ClockSampler(local)
-    barrier()
-    torch.cuda.synchronize()
     clocks.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    trace_s = 0.0
-    rays = 0
-    samples = 0
-    ev0.record(stream)
-    for _ in range(args.steps):
-        flush.zero_()
-        st = rend.render_device(xyz.data_ptr(), stream=sp, stats=True)
-        trace_s += st["trace_time"]
-        rays += st["ray_count"]
-        samples += st["samples"]
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
+    elapsed, trace_s, rays, samples = time_frames(rend, xyz, flush, stream, args.steps, args.warmup, barrier)
     clk = clocks.stop()
-    elapsed = ev0.elapsed_time(ev1) / 1e3
-    t = torch.tensor([elapsed], device="cuda")
+    opt_img = xyz.cpu().numpy()
+    rmse = None
+    if plain_img is not None:
+        rmse = float(np.sqrt(np.mean((opt_img.astype(np.float64) - plain_img) ** 2)) /
+                     max(1e-30, np.sqrt(np.mean(plain_img.astype(np.float64) ** 2))))
+    if args.form == "plain":
+        p_el, p_samples = elapsed, samples
+    t = torch.tensor([elapsed, p_el], device="cuda")
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    elapsed = float(t.item())
-    total_samples = samples * world
-    value = total_samples / elapsed
+    elapsed, p_el = float(t[0].item()), float(t[1].item())
+    value = samples * world / elapsed
+    plain_value = p_samples * world / p_el
 
     # end to end through the public C ABI with a host image buffer
     img = np.zeros((H, W, 3), dtype=np.float32)
@@ -309,17 +355,29 @@ def run_ours(args):
                 traffic = tj.get("dram_bytes_per_ray") and tj["dram_bytes_per_ray"] * n_rays_c
         except Exception:
             traffic = None
-    rows = max(1, (1 << 24) // (W * spp))
+    rows = max(1, tune["wave_paths"] // (W * spp))
     waves = math.ceil(H / rows)
     iters = 2 * sd.max_bounces + 3
-    launches_per_frame = waves * (1 + 2 * iters + 1 + 1)
+    per_iter = 3 if tune["sort_bits"] else 2
+    launches_per_frame = waves * (1 + per_iter * iters + 1) + waves  # + the ray-count kernel of stats frames
     line = {
         "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": {"workload": desc, "bounds": args.bounds, "l2": "256 MiB written between steps; path state per "
-                   "wave ~3 GB > L2", "scene_build_s": round(build_s, 3), "scene_device_bytes": scene.device_bytes()},
+        "config": {"workload": desc, "bounds": args.bounds,
+                   "form": ("plain: f64 shading, default launch" if args.form == "plain" else
+                            "optimized: f32 shading, %s launch" % ("fixed" if args.launch else "autotuned")),
+                   "graphs": "timed frames record per-stage events, so waves launch kernel by kernel even when the "
+                             "tuner keeps graph replay (which saves launch gaps only)",
+                   "l2": "256 MiB written between steps; path state per wave ~1.5-3 GB > L2",
+                   "scene_build_s": round(build_s, 3), "scene_device_bytes": scene.device_bytes(),
+                   "autotune": tune, "autotune_s": round(tune_s, 2)},
         "mrays_per_s": rays * world / elapsed / 1e6,
+        "plain": {"value": plain_value, "unit": "samples/s", "ms_per_step": p_el / args.steps * 1e3,
+                  "mrays_per_s": p_rays * world / p_el / 1e6, "trace_kernel_s_per_frame": p_trace / frames,
+                  "form": "f64 shading arithmetic (reference precision), default launch configuration"},
+        "speedup_vs_plain": value / plain_value,
+        "rel_rmse_vs_plain": rmse,
         "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": W * H * 3 * 4,
                 "note": "psy_render_image (host XYZ buffer, D2H inside the timed loop); the scene is resident (uploaded "
@@ -347,12 +405,17 @@ def run_traversal(args):
     """16M coherent (pinhole) and 16M incoherent (cosine-hemisphere from random
     surface points, seed 7) rays against the 2048x1024-quad displaced grid
     (4,194,304 tris): Mrays/s, algorithmic GB/s, closest-hit agreement with the
-    CPU oracle on a sample of each set."""
+    CPU oracle on a sample of each set.  Each set is traced under a few launch
+    configurations (the plain one first: one thread per ray, default register
+    budget, rays in the given order); every configuration returns identical
+    hits (checked), and the line's value is the fastest on the incoherent set."""
     import numpy as np
     import torch
     from psychopath_gb300 import abi, gpu, scenes
     from oracle.runner import OracleScene
     torch.cuda.set_device(0)
+    build_mod = __import__("psychopath_gb300.build", fromlist=["build"])
+    build_mod.build()
     sd, P, F = scenes.grid_mesh(2048, 1024)
     n_side = int(round(math.sqrt(args.rays)))
     sets = {"coherent": scenes.coherent_rays(n_side), "incoherent": scenes.incoherent_rays(P, F, n_side * n_side, seed=7)}
@@ -364,30 +427,24 @@ def run_traversal(args):
     node_bytes = 64 if args.bounds == "fp16" else 128
     stream = torch.cuda.Stream()  # non-null handle: kernels and events on one stream
     torch.cuda.set_stream(stream)
+    configs = [("plain", 0, 4, False), ("minb8", 0, 8, False), ("minb8+binned", 0, 8, True),
+               ("persistent8+binned", 1, 8, True)]
     out = {}
     for name, rays in sets.items():
         n = len(rays)
         d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
         d_hits = torch.zeros(n * 32, dtype=torch.uint8, device="cuda")
-        for _ in range(args.warmup):
-            tr.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream.cuda_stream)
-        torch.cuda.synchronize()
+        g.set_trace(0, 4)
+        g.set_ray_order(False)
         g.counters(True)
         tr.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream.cuda_stream)
         torch.cuda.synchronize()
         gn, gt, gr = g.counters(False)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            tr.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream.cuda_stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        sec = e0.elapsed_time(e1) / 1e3 / args.steps
-        hits = d_hits.cpu().numpy().view(abi.hit_dtype())
+        ref_hits = d_hits.cpu().numpy()
         # oracle on a sample: agreement and per-ray node / triangle tests
         idx = np.random.default_rng(11).choice(n, size=min(n, 200000), replace=False)
         ho, _, on, ot = o.trace(rays[idx], threads=os.cpu_count() or 1)
-        hg = hits[idx]
+        hg = ref_hits.view(abi.hit_dtype())[idx]
         surf = ho["kind"] >= abi.PSY_HIT_SURFACE
         same = (hg["kind"] == ho["kind"]) & (~surf | ((hg["prim"] == ho["prim"]) & (hg["inst"] == ho["inst"])))
         bmin = np.minimum(np.minimum(ho["b0"], ho["b1"]), ho["b2"])
@@ -395,22 +452,45 @@ def run_traversal(args):
         n_node = on / len(idx)
         n_tri = ot / len(idx)
         alg = 32 + 16 + n_node * node_bytes + n_tri * 36
-        gbs = alg * n / sec / 1e9
-        out[name] = {"mrays_per_s": n / sec / 1e6, "ms_per_launch": sec * 1e3, "rays": n,
-                     "alg_bytes_per_ray": alg, "achieved_gbs": gbs, "frac": gbs / peak,
-                     "oracle_node_tests_per_ray": n_node, "oracle_tri_tests_per_ray": n_tri,
-                     "gpu_node_tests_per_ray": gn / max(1, gr), "gpu_tri_tests_per_ray": gt / max(1, gr),
-                     "hit_agreement": float(same.mean()), "disagree_not_near_edge": int((~same & ~near).sum()),
-                     "sample": len(idx), "hit_fraction": float(surf.mean())}
+        res = {"rays": n, "alg_bytes_per_ray": alg, "oracle_node_tests_per_ray": n_node,
+               "oracle_tri_tests_per_ray": n_tri, "gpu_node_tests_per_ray": gn / max(1, gr),
+               "gpu_tri_tests_per_ray": gt / max(1, gr), "hit_agreement": float(same.mean()),
+               "disagree_not_near_edge": int((~same & ~near).sum()), "sample": len(idx),
+               "hit_fraction": float(surf.mean()), "configs": {}}
+        for cname, mode, minb, binned in configs:
+            g.set_trace(mode, minb)
+            g.set_ray_order(binned)
+            for _ in range(args.warmup):
+                tr.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream.cuda_stream)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                tr.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            sec = e0.elapsed_time(e1) / 1e3 / args.steps
+            identical = bool(np.array_equal(d_hits.cpu().numpy(), ref_hits))
+            gbs = alg * n / sec / 1e9
+            res["configs"][cname] = {"trace_mode": mode, "minb": minb, "binned": binned, "ms_per_call": sec * 1e3,
+                                     "mrays_per_s": n / sec / 1e6, "achieved_gbs": gbs, "frac": gbs / peak,
+                                     "hits_identical_to_plain": identical}
+        best = max(res["configs"].items(), key=lambda kv: kv[1]["mrays_per_s"])
+        res["best"] = best[0]
+        out[name] = res
         del d_rays, d_hits
     inc = out["incoherent"]
-    line = {"metric": "Mrays/s (incoherent)", "value": inc["mrays_per_s"], "unit": "Mrays/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": inc["ms_per_launch"], "higher_is_better": True,
+    bc = inc["configs"][inc["best"]]
+    line = {"metric": "Mrays/s (incoherent)", "value": bc["mrays_per_s"], "unit": "Mrays/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": bc["ms_per_call"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded grid mesh and rays)",
-            "config": {"workload": "traversal: 2048x1024-quad displaced grid (4,194,304 tris), %d rays per set" % len(sets["incoherent"]),
-                       "bounds": args.bounds},
-            "roofline": {"bound": "hbm", "achieved": inc["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                         "frac": inc["frac"], "traffic": None, "kernel": "k_trace_rays"},
+            "config": {"workload": "traversal: 2048x1024-quad displaced grid (4,194,304 tris), %d rays per set"
+                                   % len(sets["incoherent"]), "bounds": args.bounds, "launch": inc["best"],
+                       "l2": "inputs (671 MB of rays per set) larger than L2"},
+            "plain": inc["configs"]["plain"],
+            "roofline": {"bound": "hbm", "achieved": bc["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": bc["frac"], "traffic": None, "kernel": "k_trace_rays",
+                         "note": "algorithmic bytes from the oracle's node / triangle tests per ray"},
             "sets": out}
     print(json.dumps(line), flush=True)
 
@@ -449,8 +529,10 @@ def run_serving(args):
     sds = [scenes.cornell_box(), scenes.mesh_stress(level=args.level), scenes.motion_instances()]
     names = ["cornell", "mesh_stress", "motion"]
     t0 = time.perf_counter()
-    gs = [gpu.Scene(sd, bounds=args.bounds) for sd in sds]
+    gs = [gpu.Scene(sd, bounds=args.bounds, shading="f32") for sd in sds]
     build_s = time.perf_counter() - t0
+    tunes = [g.autotune() for g in gs]  # per-scene launch configuration, kept by the server's lanes
+    plain_gs = [gpu.Scene(sd, bounds=args.bounds) for sd in sds]  # f64 shading, default launch
     reqs = serving_requests(args.duration, args.rate)
     offered = sum(r * r * spp for (_, _, r, spp, _) in reqs) / args.duration
     srv = gpu.Server(hbm_budget_bytes=120 * 10**9, wave_paths=args.wave_paths, use_graphs=True)
@@ -506,7 +588,7 @@ def run_serving(args):
         if p_secs >= args.plain_seconds:
             break
         t1 = time.perf_counter()
-        gs[k].render_sized(res, res, spp, seed, dev.data_ptr(), stream=stream.cuda_stream)
+        plain_gs[k].render_sized(res, res, spp, seed, dev.data_ptr(), stream=stream.cuda_stream)
         host[: res * res * 3].copy_(dev[: res * res * 3])
         p_secs += time.perf_counter() - t1
         p_samples += res * res * spp
@@ -520,7 +602,8 @@ def run_serving(args):
                                "resolution {256,512,1024}^2, spp {1,4,16,64}, HBM budget 120 GB" %
                                (", ".join(names), args.rate, args.duration, len(reqs)),
                    "bounds": args.bounds, "wave_paths": args.wave_paths, "graphs": True,
-                   "scene_build_s": round(build_s, 2)},
+                   "form": "served scenes: f32 shading, autotuned launch; plain: f64 shading, default launch",
+                   "autotune": tunes, "scene_build_s": round(build_s, 2)},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "mean": float(lat.mean()), "max": float(lat.max()),
                        "queued_p50": float(np.percentile(np.array(qd) * 1e3, 50))},

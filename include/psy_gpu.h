@@ -163,10 +163,15 @@ typedef struct PsySceneDesc {
  * filter, which the reference evaluates in f64. */
 #define PSY_SHADING_F64 0 /* as the reference (f64 where it uses f64) */
 #define PSY_SHADING_F32 1 /* f32 throughout: no FP64 outside the watertight triangle retest */
+/* Order in which psy_trace / psy_trace_device traverse the rays of a call.
+ * Hits always land at each ray's own index, so results do not change. */
+#define PSY_RAY_ORDER_AS_GIVEN 0
+#define PSY_RAY_ORDER_BINNED 1 /* calls of >= 65,536 rays: group by direction octant and origin cell first */
 typedef struct PsySceneOptions {
     uint32_t bounds_precision;  /* PSY_BOUNDS_* */
     uint32_t shading_precision; /* PSY_SHADING_* */
-    uint32_t reserved[6];
+    uint32_t ray_order;         /* PSY_RAY_ORDER_* */
+    uint32_t reserved[5];
 } PsySceneOptions;
 
 typedef struct PsyScene PsyScene; /* opaque */
@@ -298,6 +303,43 @@ int psy_render_image(PsyScene *scene, const uint32_t *crop, float *xyz_out,
 #define PSY_NOALLOC_MAX_SAMPLES 262144u
 int psy_render_bucket_noalloc(PsyScene *scene, const PsyBucket *bucket, uint32_t spp, uint32_t seed,
                               float *d_xyz_out, void *stream);
+
+/* ---------------------------------------------------------------- autotuning */
+
+/* Picks the scene's launch configuration by timing a probe render: a band of
+ * full-width rows in the middle of the scene's image with about probe_paths
+ * paths (all samples of each pixel).  Coordinate descent over, in order: the
+ * trace kernel (one thread per ray with a register budget of 4, 5, 6 or 8
+ * resident blocks per SM, or persistent with lane refill at 4, 6 or 8),
+ * the traversal stack depth (64 or 192 entries, if the scene fits),
+ * the queue tile (grid of the wavefront kernels: sized by the queue, or a
+ * grid-stride grid of 8, 16 or 32 blocks per SM), the ray-sort key width
+ * (0, 4, 7 or 10 bits), the wave size (paths per wave) and CUDA graph replay.
+ * A candidate replaces the current choice only when its probe time is at
+ * least 2% lower.  Every candidate renders the same image bit for bit (only
+ * scheduling changes), so tuning never changes results.  The chosen
+ * configuration stays on the scene.  No counterpart in the reference (its renderer has no GPU
+ * launch parameters). */
+typedef struct PsyTuneOptions {
+    uint32_t probe_paths;  /* 0: 16,777,216 (capped at the whole image) */
+    uint32_t repeats;      /* timed probe renders per candidate, best taken (0: 3) */
+    uint32_t reserved[6];
+} PsyTuneOptions;
+
+typedef struct PsyTuneResult {
+    uint32_t trace_mode;   /* 0: one thread per ray, 1: persistent */
+    uint32_t minb;         /* register budget (resident blocks per SM) */
+    uint32_t stack;        /* traversal stack entries */
+    uint32_t grid;         /* wavefront kernel grid (0: sized by the queue) */
+    uint32_t sort_bits;
+    uint32_t wave_paths;
+    uint32_t use_graph;
+    uint32_t candidates;   /* configurations timed */
+    double default_s;      /* probe time of the configuration before tuning */
+    double best_s;         /* probe time of the chosen configuration */
+} PsyTuneResult;
+
+int psy_autotune(PsyScene *scene, const PsyTuneOptions *opts, PsyTuneResult *result);
 
 /* ---------------------------------------------------------------- serving */
 

@@ -17,6 +17,7 @@ PSY_SHADER_EMIT, PSY_SHADER_LAMBERT, PSY_SHADER_GGX = 0, 1, 2
 PSY_OBJ_MESH, PSY_OBJ_RECT_LIGHT, PSY_OBJ_SPHERE_LIGHT = 0, 1, 2
 PSY_BOUNDS_FP32, PSY_BOUNDS_FP16 = 0, 1
 PSY_SHADING_F64, PSY_SHADING_F32 = 0, 1
+PSY_RAY_ORDER_AS_GIVEN, PSY_RAY_ORDER_BINNED = 0, 1
 PSY_RAY_OCCLUSION = 1
 PSY_NOALLOC_MAX_SAMPLES = 262144
 PSY_HIT_MISS, PSY_HIT_OCCLUDE, PSY_HIT_SURFACE, PSY_HIT_LIGHT = 0, 1, 2, 3
@@ -73,7 +74,8 @@ class PsySceneDesc(C.Structure):
 
 
 class PsySceneOptions(C.Structure):
-    _fields_ = [("bounds_precision", C.c_uint32), ("shading_precision", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+    _fields_ = [("bounds_precision", C.c_uint32), ("shading_precision", C.c_uint32), ("ray_order", C.c_uint32),
+                ("reserved", C.c_uint32 * 5)]
 
 
 class PsyRay(C.Structure):
@@ -127,6 +129,19 @@ class PsyServerStats(C.Structure):
     _fields_ = [("requests_done", C.c_uint64), ("samples_done", C.c_uint64), ("waves", C.c_uint64),
                 ("kernel_launches", C.c_uint64), ("hbm_used_bytes", C.c_uint64), ("hbm_peak_bytes", C.c_uint64), ("hbm_budget_bytes", C.c_uint64),
                 ("queued", C.c_uint32), ("active", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PsyTuneOptions(C.Structure):
+    _fields_ = [("probe_paths", C.c_uint32), ("repeats", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+
+
+class PsyTuneResult(C.Structure):
+    _fields_ = [("trace_mode", C.c_uint32), ("minb", C.c_uint32), ("stack", C.c_uint32), ("grid", C.c_uint32),
+                ("sort_bits", C.c_uint32), ("wave_paths", C.c_uint32), ("use_graph", C.c_uint32),
+                ("candidates", C.c_uint32), ("default_s", C.c_double), ("best_s", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

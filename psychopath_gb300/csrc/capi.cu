@@ -109,6 +109,10 @@ static int ensure_trace(PsyScene *s, size_t n, bool full) {
     return PSY_OK;
 }
 
+// Trace calls below this many rays are not binned (the three binning
+// kernels cost more than they save).
+constexpr uint32_t kBinMinRays = 1u << 16;
+
 static int ensure_counters(PsyScene *s) {
     if (s->d_counters) return PSY_OK;
     CK(cudaMalloc((void **)&s->d_counters, 3 * sizeof(unsigned long long)), "cudaMalloc counters");
@@ -191,6 +195,16 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
     g.background = hs.background;
     g.width = hs.width; g.height = hs.height; g.spp = hs.spp; g.seed = hs.seed; g.max_bounces = hs.max_bounces;
     g.use_fp16 = hs.nodes_h.empty() ? 0u : 1u;
+    // boxes with lo <= hi on every axis let the traversal pick each axis's
+    // near and far plane from the ray direction's sign alone
+    g.ordered_slabs = 1u;
+    for (const GNode &n : hs.nodes) {
+        uint32_t cnt = n.meta.z >> 8;
+        const float *lo[3] = {&n.xlo.x, &n.ylo.x, &n.zlo.x}, *hi[3] = {&n.xhi.x, &n.yhi.x, &n.zhi.x};
+        for (uint32_t c = 0; c < cnt && c < 4; c++)
+            for (int a = 0; a < 3; a++)
+                if (!(lo[a][c] <= hi[a][c])) g.ordered_slabs = 0u;
+    }
     g.distant_energy_total = hs.distant_energy_total;
     g.lt_root_energy = hs.lt_root_energy;
     for (int a = 0; a < 3; a++) {
@@ -200,7 +214,8 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
     }
     s->max_stack = hs.max_stack;
     s->prec = (opts && opts->shading_precision == PSY_SHADING_F32) ? 1 : 0;
-    s->stack = hs.max_stack <= 32 ? 32 : (hs.max_stack <= 64 ? 64 : 192);
+    s->ray_order = (opts && opts->ray_order == PSY_RAY_ORDER_BINNED) ? 1 : 0;
+    s->stack = hs.max_stack <= 64 ? 64 : 192;
     if (hs.max_stack > 192) {
         psy_scene_destroy(s);
         return fail(PSY_E_OVERFLOW, "scene needs a traversal stack deeper than 192 entries");
@@ -230,6 +245,9 @@ int psy_scene_destroy(PsyScene *s) {
     if (s->d_err) cudaFree(s->d_err);
     if (s->d_counters) cudaFree(s->d_counters);
     if (s->d_work) cudaFree(s->d_work);
+    if (s->d_bkeys) cudaFree(s->d_bkeys);
+    if (s->d_border) cudaFree(s->d_border);
+    if (s->d_bhist) cudaFree(s->d_bhist);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return PSY_OK;
@@ -241,21 +259,51 @@ int psy_scene_device_bytes(const PsyScene *s, uint64_t *bytes) {
     return PSY_OK;
 }
 
-int psy_trace_device(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyHit *d_hits, void *stream) {
-    if (!s || (n && (!d_rays || !d_hits))) return fail(PSY_E_INVALID, "null argument");
-    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+// Ray binning scratch for trace calls of n rays (allocated on first use).
+static int ensure_binning(PsyScene *s, size_t n) {
+    if (n <= s->cap_bin) return PSY_OK;
+    if (s->d_bkeys) cudaFree(s->d_bkeys);
+    if (s->d_border) cudaFree(s->d_border);
+    s->d_bkeys = nullptr; s->d_border = nullptr; s->cap_bin = 0;
+    if (!s->d_bhist) CK(cudaMalloc((void **)&s->d_bhist, PSY_RAY_BINS * sizeof(uint32_t)), "cudaMalloc ray bins");
+    CK(cudaMalloc((void **)&s->d_bkeys, n * sizeof(uint32_t)), "cudaMalloc ray keys");
+    CK(cudaMalloc((void **)&s->d_border, n * sizeof(uint32_t)), "cudaMalloc ray order");
+    s->cap_bin = n;
+    return PSY_OK;
+}
+
+// Traces n device-resident rays; with the scene's ray_order option, large
+// batches are first binned by direction octant and origin cell.
+static int trace_device_core(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyHit *d_hits, PsySurfaceHit *d_full,
+                             cudaStream_t st) {
     unsigned long long *ctr = nullptr;
     if (s->counting) {
         int r = ensure_counters(s);
         if (r != PSY_OK) return r;
         ctr = s->d_counters;
     }
-    cudaError_t e = s->trace_mode == 1
-                        ? launch_trace_persist_rays(s->g, d_rays, n, d_hits, s->stack, s->minb, s->d_work, s->d_err, ctr, st)
-                        : launch_trace_rays(s->g, d_rays, n, d_hits, nullptr, s->stack, 128, s->d_err, ctr, st);
-    if (e != cudaSuccess) return cuda_fail(e, "trace launch");
+    const uint32_t *order = nullptr;
+    if (s->ray_order && n >= kBinMinRays) {
+        int r = ensure_binning(s, n);
+        if (r != PSY_OK) return r;
+        CK(launch_ray_binning(s->g, d_rays, n, s->d_bkeys, s->d_bhist, s->d_border, st), "ray binning");
+        order = s->d_border;
+    }
+    if (d_full || s->trace_mode == 0)
+        CK(launch_trace_rays(s->g, d_rays, n, order, d_hits, d_full, s->stack, s->minb, s->d_err, ctr, st),
+           "trace launch");
+    else
+        CK(launch_trace_persist_rays(s->g, d_rays, n, order, d_hits, s->stack, s->minb, s->d_work, s->d_err, ctr, st),
+           "trace launch");
     s->rays_traced += n;
     return PSY_OK;
+}
+
+int psy_trace_device(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyHit *d_hits, void *stream) {
+    if (!s || (n && (!d_rays || !d_hits))) return fail(PSY_E_INVALID, "null argument");
+    if (n == 0) return PSY_OK;
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    return trace_device_core(s, d_rays, n, d_hits, nullptr, st);
 }
 
 int psy_trace(PsyScene *s, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurfaceHit *full_out, void *stream) {
@@ -266,25 +314,13 @@ int psy_trace(PsyScene *s, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurf
     if (r != PSY_OK) return r;
     cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
     CK(cudaMemcpyAsync(s->d_rays, rays, (size_t)n * sizeof(PsyRay), cudaMemcpyHostToDevice, st), "copy rays");
-    unsigned long long *ctr = nullptr;
-    if (s->counting) {
-        r = ensure_counters(s);
-        if (r != PSY_OK) return r;
-        ctr = s->d_counters;
-    }
-    if (full_out || s->trace_mode == 0)
-        CK(launch_trace_rays(s->g, s->d_rays, n, s->d_hits, full_out ? s->d_full : nullptr, s->stack, 128, s->d_err, ctr,
-                             st),
-           "trace launch");
-    else
-        CK(launch_trace_persist_rays(s->g, s->d_rays, n, s->d_hits, s->stack, s->minb, s->d_work, s->d_err, ctr, st),
-           "trace launch");
+    r = trace_device_core(s, s->d_rays, n, s->d_hits, full_out ? s->d_full : nullptr, st);
+    if (r != PSY_OK) return r;
     CK(cudaMemcpyAsync(hits, s->d_hits, (size_t)n * sizeof(PsyHit), cudaMemcpyDeviceToHost, st), "copy hits");
     if (full_out)
         CK(cudaMemcpyAsync(full_out, s->d_full, (size_t)n * sizeof(PsySurfaceHit), cudaMemcpyDeviceToHost, st),
            "copy full hits");
     CK(cudaStreamSynchronize(st), "trace sync");
-    s->rays_traced += n;
     return check_err(s);
 }
 
@@ -317,7 +353,7 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
                                           B.err, ctr, st),
                "trace launch");
         else
-            CK(launch_trace_queue(s->g, B.R, B.H, B.queue[cur], B.counts + cur, n, s->stack, 128, s->grid, B.err, ctr,
+            CK(launch_trace_queue(s->g, B.R, B.H, B.queue[cur], B.counts + cur, n, s->stack, s->minb, s->grid, B.err, ctr,
                                   st),
                "trace launch");
         if (ev) cudaEventRecord(ev[3 + 3 * it], st);
@@ -699,6 +735,147 @@ int psy_render_bucket(PsyScene *s, const PsyBucket *b, uint32_t spp, uint32_t se
     return check_err(s);
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------- autotuning
+namespace {
+struct TuneCfg {
+    int trace_mode, minb, stack, grid, sort_bits;
+    uint32_t wave_paths;
+    bool graph;
+};
+TuneCfg get_cfg(const PsyScene *s) {
+    return {s->trace_mode, s->minb, s->stack, s->grid, s->sort_bits, s->wave_paths, s->use_graph};
+}
+void set_cfg(PsyScene *s, const TuneCfg &c) {
+    s->trace_mode = c.trace_mode; s->minb = c.minb; s->stack = c.stack; s->grid = c.grid;
+    s->sort_bits = c.sort_bits; s->wave_paths = c.wave_paths;
+    if (s->use_graph != c.graph) s->graph.reset();
+    s->use_graph = c.graph;
+}
+}  // namespace
+
+extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResult *res) {
+    if (!s || !res) return fail(PSY_E_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    uint32_t probe = (opts && opts->probe_paths) ? opts->probe_paths : (1u << 24);
+    uint32_t reps = (opts && opts->repeats) ? opts->repeats : 3;
+    uint32_t W = s->g.width, H = s->g.height, spp = s->g.spp;
+    if (W == 0 || H == 0 || spp == 0) return fail(PSY_E_INVALID, "scene has an empty image");
+    uint64_t row = (uint64_t)W * spp;
+    uint32_t rows = (uint32_t)std::min<uint64_t>(H, std::max<uint64_t>(1, probe / row));
+    uint32_t y0 = (H - rows) / 2;
+    float *d_img = nullptr;
+    CK(cudaMalloc((void **)&d_img, (size_t)W * rows * 12), "cudaMalloc probe image");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaStream_t st = s->stream;
+    uint32_t ncand = 0;
+    int err = PSY_OK;
+    // time one configuration: one untimed render, then the best of reps
+    auto measure = [&](const TuneCfg &c, double &out) -> int {
+        set_cfg(s, c);
+        float *base = d_img - (size_t)y0 * W * 3;
+        int r = render_region(s, 0, y0, W, rows, spp, s->g.seed, base, W, st, nullptr);
+        if (r != PSY_OK) return r;
+        double best = 1e30;
+        for (uint32_t k = 0; k < reps; k++) {
+            cudaEventRecord(e0, st);
+            r = render_region(s, 0, y0, W, rows, spp, s->g.seed, base, W, st, nullptr);
+            if (r != PSY_OK) return r;
+            cudaEventRecord(e1, st);
+            CK(cudaEventSynchronize(e1), "probe sync");
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            best = std::min(best, (double)ms * 1e-3);
+        }
+        ncand++;
+        out = best;
+        return check_err(s);
+    };
+    TuneCfg start = get_cfg(s), cur = start;
+    double best = 0, t = 0;
+    err = measure(cur, best);
+    double default_s = best;
+    auto try_set = [&](std::vector<TuneCfg> cands) {
+        for (const TuneCfg &c : cands) {
+            if (err != PSY_OK) return;
+            err = measure(c, t);
+            // a candidate must beat the current choice by 2%: differences
+            // inside the run-to-run noise keep the earlier (simpler) choice
+            if (err == PSY_OK && t < 0.98 * best) {
+                best = t;
+                cur = c;
+            }
+        }
+    };
+    // 1. trace kernel and register budget
+    {
+        std::vector<TuneCfg> v;
+        for (int m : {4, 5, 6, 8}) { TuneCfg c = cur; c.trace_mode = 0; c.minb = m; v.push_back(c); }
+        for (int m : {4, 6, 8}) { TuneCfg c = cur; c.trace_mode = 1; c.minb = m; v.push_back(c); }
+        try_set(v);
+    }
+    // 2. stack depth: the fitting variant and the larger ones
+    {
+        std::vector<TuneCfg> v;
+        for (int k : {64, 192})
+            if ((uint32_t)k >= s->max_stack && k != cur.stack) { TuneCfg c = cur; c.stack = k; v.push_back(c); }
+        try_set(v);
+    }
+    // 3. queue tile: grid of the wavefront kernels
+    {
+        int dev = 0, sms = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        std::vector<TuneCfg> v;
+        for (int k : {0, 8, 16, 32}) { TuneCfg c = cur; c.grid = k * sms; if (c.grid != cur.grid) v.push_back(c); }
+        try_set(v);
+    }
+    // 4. ray-sort key width
+    {
+        std::vector<TuneCfg> v;
+        for (int b : {0, 4, 7, 10}) { TuneCfg c = cur; c.sort_bits = b; if (b != cur.sort_bits) v.push_back(c); }
+        try_set(v);
+    }
+    // 5. wave size
+    {
+        std::vector<TuneCfg> v;
+        for (uint32_t w : {1u << 21, 1u << 22, 1u << 23, 1u << 24}) {
+            TuneCfg c = cur; c.wave_paths = w;
+            if (w != cur.wave_paths) v.push_back(c);
+        }
+        try_set(v);
+    }
+    // 6. CUDA graph replay of each wave
+    {
+        TuneCfg c = cur; c.graph = !cur.graph;
+        try_set({c});
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d_img);
+    if (err != PSY_OK) {
+        set_cfg(s, start);
+        return err;
+    }
+    set_cfg(s, cur);
+    res->trace_mode = (uint32_t)cur.trace_mode;
+    res->minb = (uint32_t)cur.minb;
+    res->stack = (uint32_t)cur.stack;
+    res->grid = (uint32_t)cur.grid;
+    res->sort_bits = (uint32_t)cur.sort_bits;
+    res->wave_paths = cur.wave_paths;
+    res->use_graph = cur.graph ? 1u : 0u;
+    res->candidates = ncand;
+    res->default_s = default_s;
+    res->best_s = best;
+    return PSY_OK;
+}
+
+extern "C" {
+
 // ---------------------------------------------------------------- inspection
 // Not part of the reference-facing interface: facts of the build for tests.
 int psy_debug_mesh_bvh_info(PsyScene *s, uint32_t object, uint32_t *tri_order, uint32_t *node_count) {
@@ -754,7 +931,9 @@ int psy_debug_counters(PsyScene *s, int enable, uint64_t *nodes, uint64_t *tris,
 int psy_debug_set_trace(PsyScene *s, int mode, int minb) {
     if (!s || mode < 0 || mode > 1) return fail(PSY_E_INVALID, "bad trace mode");
     s->trace_mode = mode;
-    s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : 4);
+    // persistent kernel: 4, 6 or 8 blocks per SM; one thread per ray: 4, 5 or 6
+    if (mode == 1) s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : 4);
+    else s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : (minb == 5 ? 5 : 4));
     return PSY_OK;
 }
 // Ray binning key width between wavefront iterations: 0 (off), 1, 4, 7, 10.
@@ -782,6 +961,12 @@ int psy_debug_render_sized(PsyScene *s, uint32_t width, uint32_t height, uint32_
     if (r != PSY_OK) return r;
     CK(cudaStreamSynchronize(st), "sync");
     return check_err(s);
+}
+// Ray order of trace calls: 0 = as given, 1 = binned (PsySceneOptions.ray_order).
+int psy_debug_set_ray_order(PsyScene *s, int order) {
+    if (!s || order < 0 || order > 1) return fail(PSY_E_INVALID, "bad ray order");
+    s->ray_order = order;
+    return PSY_OK;
 }
 // Replay each wave from a CUDA graph (1) or launch it kernel by kernel (0).
 int psy_debug_set_graph(PsyScene *s, int on) {

@@ -198,7 +198,7 @@ DI float golden_ratio_sample(uint32_t i, uint32_t scramble) {
 // Sobol direction numbers for 8 dimensions (van der Corput + Joe & Kuo
 // 2..8), filled by the host at library load.  (Only kernels.cu includes the
 // device headers, so the constant banks are defined here.)
-__constant__ uint32_t c_sobol_dirs[8][32];
+static __constant__ uint32_t c_sobol_dirs[8][32];
 DI uint32_t laine_karras(uint32_t x, uint32_t seed) {
     x += seed;
     x ^= x * 0x6c50b47cu;
@@ -343,6 +343,18 @@ DI bool slab_hit_finite(float xlo, float xhi, float ylo, float yhi, float zlo, f
     float t2x = (xhi - o.x) * di.x, t2y = (yhi - o.y) * di.y, t2z = (zhi - o.z) * di.z;
     float fx = fmaxf(t1x, t2x), fy = fmaxf(t1y, t2y), fz = fmaxf(t1z, t2z);
     float nx = fminf(t1x, t2x), ny = fminf(t1y, t2y), nz = fminf(t1z, t2z);
+    float far_t = fminf(fminf(fx, fminf(fy, fz)) * PSY_BBOX_MAXT_ADJUST, max_t);
+    float near_t = fmaxf(fmaxf(nx, ny), fmaxf(nz, 0.0f));
+    return near_t < far_t;
+}
+// Same test with each axis's near and far plane already chosen from the sign
+// of the inverse direction (finite, nonzero): for lo <= hi,
+// (lo - o) * di <= (hi - o) * di when di > 0 (rounding is monotonic) and the
+// reverse when di < 0, so min / max of the two slab distances are known and
+// need no instructions.  Decisions equal slab_hit_finite's.
+DI bool slab_hit_ordered(float nxp, float fxp, float nyp, float fyp, float nzp, float fzp, V3 o, V3 di, float max_t) {
+    float nx = (nxp - o.x) * di.x, ny = (nyp - o.y) * di.y, nz = (nzp - o.z) * di.z;
+    float fx = (fxp - o.x) * di.x, fy = (fyp - o.y) * di.y, fz = (fzp - o.z) * di.z;
     float far_t = fminf(fminf(fx, fminf(fy, fz)) * PSY_BBOX_MAXT_ADJUST, max_t);
     float near_t = fmaxf(fmaxf(nx, ny), fmaxf(nz, 0.0f));
     return near_t < far_t;

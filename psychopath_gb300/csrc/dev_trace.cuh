@@ -19,7 +19,7 @@
 namespace psyd {
 
 // Child visit order per direction octant and node topology (filled by the host).
-__constant__ uint8_t c_traversal_table[8][48];
+static __constant__ uint8_t c_traversal_table[8][48];
 
 struct HitRec {
     uint32_t kind;  // PSY_HIT_*
@@ -54,13 +54,29 @@ DI float4 lerp4(float4 a, float4 b, float al) {
 }
 
 // Test the (up to 4) children of a node; returns the hit mask.
-DI uint32_t node_hits(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, float time, uint32_t &code,
-                      uint32_t &count, uint4 &child) {
+// Child hit mask of BVH4 node ni.  safe: the ray passes slab_safe and the
+// scene's boxes are ordered (ordered_slabs); oct: ray_code(di).
+DI uint32_t node_hits(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, float time, uint32_t oct, bool safe,
+                      uint32_t &code, uint32_t &count, uint4 &child) {
     const GNode *n = S.nodes + ni;
     uint4 meta = __ldg(&n->meta);
     child = __ldg(&n->child);
     code = meta.z & 0xFFu;
     count = meta.z >> 8;
+    if (safe && meta.y <= 1) {
+        // single time key: near / far planes picked by the direction's signs
+        const float4 *bb = reinterpret_cast<const float4 *>(n);  // xlo, xhi, ylo, yhi, zlo, zhi
+        uint32_t sx = oct & 1u, sy = (oct >> 1) & 1u, sz = (oct >> 2) & 1u;
+        float4 nx = __ldg(bb + sx), fx = __ldg(bb + (sx ^ 1u));
+        float4 ny = __ldg(bb + 2 + sy), fy = __ldg(bb + 2 + (sy ^ 1u));
+        float4 nz = __ldg(bb + 4 + sz), fz = __ldg(bb + 4 + (sz ^ 1u));
+        uint32_t m = 0;
+        m |= slab_hit_ordered(nx.x, fx.x, ny.x, fy.x, nz.x, fz.x, o, di, tmax) ? 1u : 0u;
+        m |= slab_hit_ordered(nx.y, fx.y, ny.y, fy.y, nz.y, fz.y, o, di, tmax) ? 2u : 0u;
+        m |= slab_hit_ordered(nx.z, fx.z, ny.z, fy.z, nz.z, fz.z, o, di, tmax) ? 4u : 0u;
+        m |= slab_hit_ordered(nx.w, fx.w, ny.w, fy.w, nz.w, fz.w, o, di, tmax) ? 8u : 0u;
+        return m & ((1u << count) - 1u);
+    }
     NodeBounds b;
     if (meta.y <= 1) {
         load_key(S, n, meta.x, 0, b);
@@ -78,7 +94,7 @@ DI uint32_t node_hits(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, flo
         }
     }
     uint32_t m = 0;
-    if (slab_safe(o, di, tmax)) {
+    if (slab_safe(o, di, tmax)) {  // finite inverse direction: one-instruction min / max
         m |= slab_hit_finite(b.xlo.x, b.xhi.x, b.ylo.x, b.yhi.x, b.zlo.x, b.zhi.x, o, di, tmax) ? 1u : 0u;
         m |= slab_hit_finite(b.xlo.y, b.xhi.y, b.ylo.y, b.yhi.y, b.zlo.y, b.zhi.y, o, di, tmax) ? 2u : 0u;
         m |= slab_hit_finite(b.xlo.z, b.xhi.z, b.ylo.z, b.yhi.z, b.zlo.z, b.zhi.z, o, di, tmax) ? 4u : 0u;
@@ -105,12 +121,12 @@ DI float h2f_hi(uint32_t bits16, float anchor) {
     float r = anchor + v;
     return increment_ulp(r);
 }
-DI uint32_t node_hits_h(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, float time, uint32_t &code,
-                        uint32_t &count, uint4 &child) {
+DI uint32_t node_hits_h(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, float time, uint32_t oct, bool safe,
+                        uint32_t &code, uint32_t &count, uint4 &child) {
     const GNodeH *n = S.nodes_h + ni;
     float4 a = __ldg(&n->anchor);
     if ((__float_as_uint(a.w) >> 16) & 1u)  // motion node: keys only in f32
-        return node_hits(S, ni, o, di, tmax, time, code, count, child);
+        return node_hits(S, ni, o, di, tmax, time, oct, safe, code, count, child);
     uint2 xl = __ldg(&n->xlo), xh = __ldg(&n->xhi), yl = __ldg(&n->ylo), yh = __ldg(&n->yhi), zl = __ldg(&n->zlo),
           zh = __ldg(&n->zhi);
     child = __ldg(&n->child);
@@ -221,7 +237,10 @@ DI bool trace_ray(const GScene &S, const uint8_t *table, V3 o, V3 d, float tmax,
     V3 wo = xf_point(o, ident);
     V3 wdi = recip(xf_vector(d, ident));
     V3 lo = wo, ldi = wdi;
-    const uint8_t *row = table + 48 * ray_code(wdi);
+    uint32_t oct = ray_code(wdi);
+    const uint8_t *row = table + 48 * oct;
+    // slab_safe holds for the whole ray in a space (tmax only shrinks to a finite t)
+    bool safe = S.ordered_slabs && slab_safe(lo, ldi, tmax);
     uint32_t stack[STACK];
     int sp = 0;
     uint32_t cur = S.top_root;
@@ -236,8 +255,8 @@ DI bool trace_ray(const GScene &S, const uint8_t *table, V3 o, V3 d, float tmax,
         while (!psy_is_leaf(cur)) {
             uint32_t code, count;
             uint4 ch;
-            uint32_t m = S.use_fp16 ? node_hits_h(S, cur, lo, ldi, tmax, time, code, count, ch)
-                                    : node_hits(S, cur, lo, ldi, tmax, time, code, count, ch);
+            uint32_t m = S.use_fp16 ? node_hits_h(S, cur, lo, ldi, tmax, time, oct, safe, code, count, ch)
+                                    : node_hits(S, cur, lo, ldi, tmax, time, oct, safe, code, count, ch);
             if (COUNT) cnt->nodes++;
             if (m == 0) goto pop;
             uint32_t order = row[code];
@@ -273,7 +292,9 @@ DI bool trace_ray(const GScene &S, const uint8_t *table, V3 o, V3 d, float tmax,
                 if (sp >= STACK) return false;
                 stack[sp++] = PSY_REF_NONE;  // leave-instance marker
                 in_inst = true;
-                row = table + 48 * ray_code(ldi);
+                oct = ray_code(ldi);
+                row = table + 48 * oct;
+                safe = S.ordered_slabs && slab_safe(lo, ldi, tmax);
                 cur = mesh.root;
                 continue;
             } else if (in.kind == PSY_INST_RECT) {
@@ -321,7 +342,9 @@ DI bool trace_ray(const GScene &S, const uint8_t *table, V3 o, V3 d, float tmax,
             in_inst = false;
             lo = wo;
             ldi = wdi;
-            row = table + 48 * ray_code(wdi);
+            oct = ray_code(wdi);
+            row = table + 48 * oct;
+            safe = S.ordered_slabs && slab_safe(lo, ldi, tmax);
         }
     }
 }
@@ -343,7 +366,7 @@ struct Lane {
     uint32_t slot;      // current instance slot
     uint32_t mts, mvb;  // current mesh: vertex time samples and vertex base
     int sp;
-    uint8_t occl, in_inst, has_xf, octant;
+    uint8_t occl, in_inst, has_xf, octant, safe, ordered;
     HitRec hit;
 };
 
@@ -365,6 +388,8 @@ DI void lane_init(const GScene &S, Lane &L, V3 o, V3 d, float tmax, float time, 
     L.in_inst = 0;
     L.has_xf = 0;
     L.octant = (uint8_t)ray_code(L.ldi);
+    L.ordered = S.ordered_slabs ? 1 : 0;
+    L.safe = (L.ordered && slab_safe(L.lo, L.ldi, tmax)) ? 1 : 0;
     L.hit.kind = PSY_HIT_MISS_K;
     L.hit.prim = 0;
     L.hit.slot = 0;
@@ -385,6 +410,7 @@ DI bool lane_pop(Lane &L, const uint32_t *stack) {
         L.lo = xf_point(L.o, ident);
         L.ldi = recip(xf_vector(L.d, ident));
         L.octant = (uint8_t)ray_code(L.ldi);
+        L.safe = (L.ordered && slab_safe(L.lo, L.ldi, L.tmax)) ? 1 : 0;
     }
 }
 
@@ -396,8 +422,8 @@ DI int lane_step(const GScene &S, const uint8_t *table, Lane &L, uint32_t *stack
     while (!psy_is_leaf(L.cur)) {
         uint32_t code, cnt;
         uint4 ch;
-        uint32_t m = S.use_fp16 ? node_hits_h(S, L.cur, L.lo, L.ldi, L.tmax, L.time, code, cnt, ch)
-                                : node_hits(S, L.cur, L.lo, L.ldi, L.tmax, L.time, code, cnt, ch);
+        uint32_t m = S.use_fp16 ? node_hits_h(S, L.cur, L.lo, L.ldi, L.tmax, L.time, L.octant, L.safe, code, cnt, ch)
+                                : node_hits(S, L.cur, L.lo, L.ldi, L.tmax, L.time, L.octant, L.safe, code, cnt, ch);
         if (count) tc.nodes++;
         if (m == 0) {
             if (!lane_pop<STACK>(L, stack)) return 1;
@@ -431,6 +457,7 @@ DI int lane_step(const GScene &S, const uint8_t *table, Lane &L, uint32_t *stack
                 L.ldi = recip(xf_vector(L.d, x));
                 L.mat = instance_mat(S, in, L.time);
                 L.octant = (uint8_t)ray_code(L.ldi);
+                L.safe = (L.ordered && slab_safe(L.lo, L.ldi, L.tmax)) ? 1 : 0;
             }
             if (L.sp >= STACK) return -1;
             stack[L.sp++] = PSY_REF_NONE;  // leave-instance marker

@@ -1,10 +1,10 @@
-// Kernels of the GB300 tracing path: ray tracing (closest / any hit),
-// camera ray generation, the light-path state machine and accumulation.
+// Kernels of the GB300 tracing path: camera ray generation, the light-path
+// state machine and accumulation (traversal kernels: trace_kernels.cu).
 #include <cuda_fp16.h>
 
 #include <algorithm>
 
-#include "dev_trace.cuh"
+#include "dev_surface.cuh"
 #include "kernels.cuh"
 
 using namespace psyd;
@@ -74,394 +74,7 @@ void psy_upload_constants() {
     traversal_table_host(t);
     cudaMemcpyToSymbol(c_sobol_dirs, d, sizeof(d));
     cudaMemcpyToSymbol(c_traversal_table, t, sizeof(t));
-}
-
-// ------------------------------------------------------------------ surface data
-// SurfaceIntersectionData of a hit, recomputed from the hit record with the
-// traversal's own arithmetic (src/surface/triangle_mesh.rs:264-318,
-// src/light/*_light.rs intersect_rays).
-struct SurfData {
-    V3 pos, nor, nor_g;
-    float pos_err, sample_pdf;
-    Closure closure;
-    int32_t shader;
-};
-// Colour of the tracer's shader for instances without one (src/tracer.rs:161-163),
-// rec709_to_xyz((1, 0, 1)) computed on the host.
-__constant__ GColor c_magenta;
-
-template <class R>
-__device__ void resolve_hit(const GScene &S, const HitRec &h, V3 o, V3 d, float time, SurfData &sd) {
-    GInstance in = S.instances[h.slot];
-    if (h.kind == PSY_HIT_SURFACE_K) {
-        GMesh M = S.meshes[in.obj];
-        bool has_xf = in.xc != 0;
-        Xf mat = has_xf ? instance_mat(S, in, time) : xf_identity();
-        V3 p0, p1, p2;
-        fetch_tri(S, M, h.prim, time, has_xf, mat, p0, p1, p2);
-        surface_point(p0, p1, p2, h.b0, h.b1, h.b2, &sd.pos, &sd.pos_err);
-        V3 geo = cross(p0 - p1, p0 - p2);
-        V3 sn = geo;
-        if (M.has_normals) {
-            uint4 ix = __ldg(S.tri_idx + h.prim);
-            const float4 *nb = S.normals + M.vert_base;
-            V3 n0 = normalized(lerp_slice_v3(nb + (size_t)ix.x * M.ts, M.ts, time));
-            V3 n1 = normalized(lerp_slice_v3(nb + (size_t)ix.y * M.ts, M.ts, time));
-            V3 n2 = normalized(lerp_slice_v3(nb + (size_t)ix.z * M.ts, M.ts, time));
-            V3 snn = xf_normal((n0 * h.b0) + (n1 * h.b1) + (n2 * h.b2), mat);
-            sn = (dot(snn, geo) >= 0.0f) ? snn : neg(snn);
-        }
-        sd.nor = sn;
-        sd.nor_g = geo;
-        sd.sample_pdf = 0.0f;
-        sd.shader = in.shader;
-        if (in.shader >= 0) {
-            sd.closure = closure_from_shader(S.shaders[in.shader]);
-        } else {
-            sd.closure.kind = PSY_CL_EMIT;
-            sd.closure.color = c_magenta;
-            sd.closure.roughness = 0.0f;
-            sd.closure.fresnel = 0.0f;
-        }
-        return;
-    }
-    // light surfaces
-    const GLight L = S.lights[in.obj];
-    Xf xf = instance_xf_at(S, in, time);
-    sd.shader = -1;
-    sd.closure.kind = PSY_CL_EMIT;
-    sd.closure.roughness = 0.0f;
-    sd.closure.fresnel = 0.0f;
-    GColor col = lerp_slice_color(S.light_colors + L.key_base, L.nkeys, time);
-    if (in.kind == PSY_INST_RECT) {
-        float w = light_dim(S, L, 0, time), hh = light_dim(S, L, 1, time);
-        Xf si = xf_inverse(xf);
-        V3 p1, p2, p3, p4;
-        rect_corners(w, hh, si, &p1, &p2, &p3, &p4);
-        V3 a = h.prim == 0 ? p1 : p3, b = h.prim == 0 ? p2 : p4, c = h.prim == 0 ? p3 : p1;
-        surface_point(a, b, c, h.b0, h.b1, h.b2, &sd.pos, &sd.pos_err);
-        V3 nn = cross(a - b, a - c);
-        sd.nor = nn;
-        sd.nor_g = nn;
-        sd.sample_pdf = rect_sample_pdf<R>(S, L, xf, o, d, sd.pos, time);
-        float isa = (float)(1.0 / ((double)w * (double)hh));
-        sd.closure.color = color_mul(col, isa);
-    } else {
-        float radius = light_dim(S, L, 0, time);
-        Xf ixf = xf_inverse(xf);
-        V3 ol = in.xc ? xf_point(o, xf) : xf_point(o, xf_identity());
-        V3 dir = xf_vector(d, xf);
-        V3 unit = normalized(ol + (dir * h.t));
-        sd.pos = xf_vector(unit * radius, ixf);  // as the reference: a vector transform
-        sd.pos_err = 0.001f;
-        V3 nrm = xf_normal(unit, ixf);
-        sd.nor = nrm;
-        sd.nor_g = nrm;
-        sd.sample_pdf = sphere_sample_pdf<R>(S, L, xf, o, time);
-        float isa = (float)(1.0 / (4.0 * PSY_PI_64 * (double)radius * (double)radius));
-        sd.closure.color = color_mul(col, isa);
-    }
-}
-
-// ------------------------------------------------------------------ ray tracing
-template <int STACK, bool COUNT>
-__global__ void __launch_bounds__(128) k_trace_rays(GScene S, const PsyRay *__restrict__ rays, uint32_t n,
-                                                    PsyHit *__restrict__ hits, PsySurfaceHit *__restrict__ full,
-                                                    int *err, unsigned long long *counters) {
-    __shared__ uint8_t table[8 * 48];
-    load_traversal_table(table);
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    TraceCount tc{0, 0};
-    if (i < n) {
-        const float *r = reinterpret_cast<const float *>(rays + i);
-        V3 o = v3(r[0], r[1], r[2]), d = v3(r[3], r[4], r[5]);
-        float tmax = r[6], time = r[7];
-        uint32_t flags = reinterpret_cast<const uint32_t *>(r)[9];
-        HitRec h;
-        if (!trace_ray<STACK, COUNT>(S, table, o, d, tmax, time, (flags & PSY_RAY_OCCLUSION) != 0, h, &tc)) {
-            atomicExch(err, PSY_E_OVERFLOW);
-            h.kind = PSY_HIT_MISS_K;
-        }
-        PsyHit out;
-        out.kind = h.kind;
-        out.prim = 0; out.inst = 0; out.t = 0.0f; out.b0 = 0.0f; out.b1 = 0.0f; out.b2 = 0.0f; out.pad = 0.0f;
-        if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
-            GInstance in = S.instances[h.slot];
-            out.prim = h.kind == PSY_HIT_SURFACE_K ? __ldg(S.tri_idx + h.prim).w : h.prim;
-            out.inst = in.id;
-            out.t = h.t; out.b0 = h.b0; out.b1 = h.b1; out.b2 = h.b2;
-        }
-        hits[i] = out;
-        if (full) {
-            PsySurfaceHit f;
-            f.hit = out;
-            f.shader = -1;
-            f.pos[0] = f.pos[1] = f.pos[2] = 0.0f;
-            f.nor[0] = f.nor[1] = f.nor[2] = 0.0f;
-            f.nor_g[0] = f.nor_g[1] = f.nor_g[2] = 0.0f;
-            f.pos_err = 0.0f;
-            f.sample_pdf = 0.0f;
-            if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
-                SurfData sd;
-                resolve_hit<double>(S, h, o, d, time, sd);
-                f.pos[0] = sd.pos.x; f.pos[1] = sd.pos.y; f.pos[2] = sd.pos.z;
-                f.nor[0] = sd.nor.x; f.nor[1] = sd.nor.y; f.nor[2] = sd.nor.z;
-                f.nor_g[0] = sd.nor_g.x; f.nor_g[1] = sd.nor_g.y; f.nor_g[2] = sd.nor_g.z;
-                f.pos_err = sd.pos_err;
-                f.sample_pdf = sd.sample_pdf;
-                f.shader = sd.shader;
-            }
-            full[i] = f;
-        }
-    }
-    if (COUNT) {
-        unsigned long long a = tc.nodes, b = tc.tris, c = (i < n) ? 1ull : 0ull;
-        for (int off = 16; off > 0; off >>= 1) {
-            a += __shfl_down_sync(0xffffffffu, a, off);
-            b += __shfl_down_sync(0xffffffffu, b, off);
-            c += __shfl_down_sync(0xffffffffu, c, off);
-        }
-        if ((threadIdx.x & 31) == 0) {
-            atomicAdd(counters, a);
-            atomicAdd(counters + 1, b);
-            atomicAdd(counters + 2, c);
-        }
-    }
-}
-
-cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurfaceHit *full,
-                              int stack, int block, int *d_err, unsigned long long *counters, cudaStream_t st) {
-    if (n == 0) return cudaSuccess;
-    (void)block;
-    dim3 b(128), g((n + 127) / 128);
-    bool c = counters != nullptr;
-#define TR(SZ)                                                                                        \
-    if (c) k_trace_rays<SZ, true><<<g, b, 0, st>>>(S, rays, n, hits, full, d_err, counters);         \
-    else k_trace_rays<SZ, false><<<g, b, 0, st>>>(S, rays, n, hits, full, d_err, counters)
-    if (stack <= 32) { TR(32); }
-    else if (stack <= 64) { TR(64); }
-    else { TR(192); }
-#undef TR
-    return cudaGetLastError();
-}
-
-// ------------------------------------------------------------------ persistent traversal
-// Ray sources / sinks of the persistent traversal kernel.
-struct IOQueue {  // wavefront: rays of the paths listed in queue[0 .. *count)
-    const uint32_t *queue;
-    const uint32_t *count;
-    const float4 *ro, *rd;
-    const uint8_t *occl;
-    uint4 *ki;
-    float4 *tb;
-    __device__ __forceinline__ uint32_t n() const { return *count; }
-    __device__ __forceinline__ uint32_t load(uint32_t q, V3 &o, V3 &d, float &tmax, float &time, bool &oc) const {
-        uint32_t p = queue[q];
-        float4 a = ro[p], b = rd[p];
-        o = v3(a); d = v3(b); tmax = a.w; time = b.w; oc = occl[p] != 0;
-        return p;
-    }
-    __device__ __forceinline__ void store(const GScene &, uint32_t p, const HitRec &h) const {
-        ki[p] = make_uint4(h.kind, h.prim, h.slot, 0u);
-        tb[p] = make_float4(h.t, h.b0, h.b1, h.b2);
-    }
-};
-struct IORays {  // PsyRay records in, PsyHit records out
-    const PsyRay *rays;
-    uint32_t count;
-    PsyHit *hits;
-    __device__ __forceinline__ uint32_t n() const { return count; }
-    __device__ __forceinline__ uint32_t load(uint32_t q, V3 &o, V3 &d, float &tmax, float &time, bool &oc) const {
-        const float *r = reinterpret_cast<const float *>(rays + q);
-        o = v3(r[0], r[1], r[2]); d = v3(r[3], r[4], r[5]); tmax = r[6]; time = r[7];
-        oc = (reinterpret_cast<const uint32_t *>(r)[9] & PSY_RAY_OCCLUSION) != 0;
-        return q;
-    }
-    __device__ __forceinline__ void store(const GScene &S, uint32_t q, const HitRec &h) const {
-        PsyHit out;
-        out.kind = h.kind;
-        out.prim = 0; out.inst = 0; out.t = 0.0f; out.b0 = 0.0f; out.b1 = 0.0f; out.b2 = 0.0f; out.pad = 0.0f;
-        if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
-            out.prim = h.kind == PSY_HIT_SURFACE_K ? __ldg(S.tri_idx + h.prim).w : h.prim;
-            out.inst = S.instances[h.slot].id;
-            out.t = h.t; out.b0 = h.b0; out.b1 = h.b1; out.b2 = h.b2;
-        }
-        hits[q] = out;
-    }
-};
-
-// Persistent traversal: each warp keeps its lanes busy by refilling lanes
-// whose ray finished with the next rays of a global work counter (one
-// aggregated atomic per warp), so long and short rays no longer idle the
-// rest of the warp (Aila & Laine, "Understanding the Efficiency of Ray
-// Traversal on GPUs", 2009).
-template <int STACK, int MINB, class IO>
-__global__ void __launch_bounds__(128, MINB) k_trace_persist(GScene S, IO io, uint32_t *work, int *err,
-                                                            unsigned long long *counters) {
-    __shared__ uint8_t table[8 * 48];
-    load_traversal_table(table);
-    const uint32_t n = io.n();
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    uint32_t stack[STACK];
-    Lane L;
-    bool active = false, exhausted = false;
-    uint32_t id = 0, nr = 0;
-    TraceCount tc{0, 0};
-    const bool count = counters != nullptr;
-    while (true) {
-        unsigned idle = __ballot_sync(FULL, !active);
-        if (idle && !exhausted) {
-            int leader = __ffs(idle) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(work, (uint32_t)__popc(idle));
-            base = __shfl_sync(FULL, base, leader);
-            if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
-            if (!active) {
-                uint32_t my = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
-                if (my < n) {
-                    V3 o, d;
-                    float tmax, time;
-                    bool oc;
-                    id = io.load(my, o, d, tmax, time, oc);
-                    lane_init(S, L, o, d, tmax, time, oc);
-                    active = true;
-                    nr++;
-                }
-            }
-        }
-        if (!__any_sync(FULL, active)) break;
-        if (active) {
-            int r = lane_step<STACK>(S, table, L, stack, tc, count);
-            if (r != 0) {
-                if (r < 0) {
-                    atomicExch(err, PSY_E_OVERFLOW);
-                    L.hit.kind = PSY_HIT_MISS_K;
-                }
-                io.store(S, id, L.hit);
-                active = false;
-            }
-        }
-    }
-    if (count) {
-        unsigned long long a = tc.nodes, b = tc.tris, c = nr;
-        for (int off = 16; off > 0; off >>= 1) {
-            a += __shfl_down_sync(FULL, a, off);
-            b += __shfl_down_sync(FULL, b, off);
-            c += __shfl_down_sync(FULL, c, off);
-        }
-        if (lane == 0) {
-            atomicAdd(counters, a);
-            atomicAdd(counters + 1, b);
-            atomicAdd(counters + 2, c);
-        }
-    }
-}
-
-template <class IO, int STACK, int MINB>
-static int persist_grid() {
-    static int g = 0;
-    if (g == 0) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trace_persist<STACK, MINB, IO>, 128, 0);
-        g = sms * (per > 0 ? per : 1);
-    }
-    return g;
-}
-
-template <class IO>
-static cudaError_t launch_persist(const GScene &S, const IO &io, uint32_t max_count, int stack, int minb,
-                                  uint32_t *work, int *d_err, unsigned long long *counters, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), st);
-    if (e != cudaSuccess) return e;
-#define TP(SZ, MB)                                                                          \
-    {                                                                                       \
-        int g = persist_grid<IO, SZ, MB>();                                                 \
-        uint32_t need = (max_count + 127) / 128;                                            \
-        if ((uint32_t)g > need) g = (int)need;                                              \
-        if (g > 0) k_trace_persist<SZ, MB, IO><<<g, 128, 0, st>>>(S, io, work, d_err, counters); \
-    }
-    if (minb >= 8) {
-        if (stack <= 32) TP(32, 8) else if (stack <= 64) TP(64, 8) else TP(192, 8)
-    } else if (minb >= 6) {
-        if (stack <= 32) TP(32, 6) else if (stack <= 64) TP(64, 6) else TP(192, 6)
-    } else {
-        if (stack <= 32) TP(32, 4) else if (stack <= 64) TP(64, 4) else TP(192, 4)
-    }
-#undef TP
-    return cudaGetLastError();
-}
-
-cudaError_t launch_trace_persist_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue,
-                                       const uint32_t *count, uint32_t max_count, int stack, int minb, uint32_t *work,
-                                       int *d_err, unsigned long long *counters, cudaStream_t st) {
-    IOQueue io{queue, count, R.o, R.d, R.occl, H.ki, H.tb};
-    return launch_persist(S, io, max_count, stack, minb, work, d_err, counters, st);
-}
-cudaError_t launch_trace_persist_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, int stack,
-                                      int minb, uint32_t *work, int *d_err, unsigned long long *counters,
-                                      cudaStream_t st) {
-    if (n == 0) return cudaSuccess;
-    IORays io{rays, n, hits};
-    return launch_persist(S, io, n, stack, minb, work, d_err, counters, st);
-}
-
-// Queue-driven trace for the render wavefront: a grid-stride loop over the
-// live paths listed in queue[0 .. *count).  COUNT adds the work counters
-// (node visits, triangle tests, rays) into counters[0..2].
-template <int STACK, bool COUNT>
-__global__ void __launch_bounds__(128) k_trace_queue(GScene S, RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
-                                                     const uint32_t *__restrict__ count, int *err,
-                                                     unsigned long long *counters) {
-    __shared__ uint8_t table[8 * 48];
-    load_traversal_table(table);
-    uint32_t n = *count;
-    TraceCount tc{0, 0};
-    uint32_t nr = 0;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        uint32_t p = queue[q];
-        float4 ro = R.o[p], rd = R.d[p];
-        HitRec h;
-        if (!trace_ray<STACK, COUNT>(S, table, v3(ro), v3(rd), ro.w, rd.w, R.occl[p] != 0, h, &tc)) {
-            atomicExch(err, PSY_E_OVERFLOW);
-            h.kind = PSY_HIT_MISS_K;
-        }
-        nr++;
-        H.ki[p] = make_uint4(h.kind, h.prim, h.slot, 0u);
-        H.tb[p] = make_float4(h.t, h.b0, h.b1, h.b2);
-    }
-    if (COUNT) {
-        unsigned long long a = tc.nodes, b = tc.tris, c = nr;
-        for (int off = 16; off > 0; off >>= 1) {
-            a += __shfl_down_sync(0xffffffffu, a, off);
-            b += __shfl_down_sync(0xffffffffu, b, off);
-            c += __shfl_down_sync(0xffffffffu, c, off);
-        }
-        if ((threadIdx.x & 31) == 0) {
-            atomicAdd(counters, a);
-            atomicAdd(counters + 1, b);
-            atomicAdd(counters + 2, c);
-        }
-    }
-}
-
-cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
-                               uint32_t max_count, int stack, int block, int grid, int *d_err,
-                               unsigned long long *counters, cudaStream_t st) {
-    (void)block;
-    if (grid <= 0) grid = (int)((max_count + 127) / 128);
-    if (grid == 0) return cudaSuccess;
-    bool c = counters != nullptr;
-#define TQ(SZ)                                                                                            \
-    if (c) k_trace_queue<SZ, true><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, counters);        \
-    else k_trace_queue<SZ, false><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, counters)
-    if (stack <= 32) { TQ(32); }
-    else if (stack <= 64) { TQ(64); }
-    else { TQ(192); }
-#undef TQ
-    return cudaGetLastError();
+    psy_upload_trace_constants(t, nullptr);
 }
 
 // ------------------------------------------------------------------ wave segments
@@ -847,4 +460,5 @@ cudaError_t launch_count_rays(PathState P, uint32_t n, unsigned long long *out, 
 void psy_set_magenta(const float xyz[3]) {
     GColor c{PSY_COLOR_XYZ_K, xyz[0], xyz[1], xyz[2]};
     cudaMemcpyToSymbol(c_magenta, &c, sizeof(c));
+    psy_upload_trace_constants(nullptr, xyz);
 }

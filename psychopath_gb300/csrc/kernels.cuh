@@ -51,19 +51,31 @@ struct WaveDesc {
 };
 
 void psy_upload_constants();  // Sobol directions + traversal table -> __constant__
+// The traversal translation unit's own copies of its constants (null: skip).
+void psy_upload_trace_constants(const uint8_t table[8][48], const float magenta[3]);
 
 // Trace n PsyRay records (device) into PsyHit records (device).
-cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, PsySurfaceHit *full,
-                              int stack, int block, int *d_err, unsigned long long *counters, cudaStream_t st);
+// minb: resident blocks of 128 threads per SM the register budget targets
+// (4 = the compiler's choice, 5 or 6 = fewer registers, some spills).
+// order (optional): thread q traces ray order[q] (hits still land at the
+// ray's own index).
+cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order, PsyHit *hits,
+                              PsySurfaceHit *full, int stack, int minb, int *d_err, unsigned long long *counters,
+                              cudaStream_t st);
+// Ray binning by direction octant and origin cell: keys[n], hist[PSY_RAY_BINS]
+// scratch; order[n] receives a permutation of 0..n-1 grouped by bin.
+#define PSY_RAY_BINS (1u << 18)
+cudaError_t launch_ray_binning(const GScene &S, const PsyRay *rays, uint32_t n, uint32_t *keys, uint32_t *hist,
+                               uint32_t *order, cudaStream_t st);
 // Persistent traversal kernels with per-lane ray refill.  `minb` selects the
 // register budget (4 or 8 resident blocks of 128 threads per SM); `work` is a
 // device counter the launch zeroes first.
 cudaError_t launch_trace_persist_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue,
                                        const uint32_t *count, uint32_t max_count, int stack, int minb, uint32_t *work,
                                        int *d_err, unsigned long long *counters, cudaStream_t st);
-cudaError_t launch_trace_persist_rays(const GScene &S, const PsyRay *rays, uint32_t n, PsyHit *hits, int stack,
-                                      int minb, uint32_t *work, int *d_err, unsigned long long *counters,
-                                      cudaStream_t st);
+cudaError_t launch_trace_persist_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order,
+                                      PsyHit *hits, int stack, int minb, uint32_t *work, int *d_err,
+                                      unsigned long long *counters, cudaStream_t st);
 // Camera rays for the wave described by d_wave (device memory; the grid
 // covers max_paths); fills queue with 0..n-1 and *count = n.
 // prec: 0 = f64 sampling arithmetic as the reference, 1 = f32.
@@ -71,7 +83,7 @@ cudaError_t launch_camera(const GScene &S, const WaveDesc *d_wave, uint32_t max_
                           uint32_t *queue, uint32_t *count, int prec, cudaStream_t st);
 // Trace the queued rays of a wave.
 cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
-                               uint32_t max_count, int stack, int block, int grid, int *d_err,
+                               uint32_t max_count, int stack, int minb, int grid, int *d_err,
                                unsigned long long *counters, cudaStream_t st);
 // LightPath::next for the queued paths; live paths go to next_queue.
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,

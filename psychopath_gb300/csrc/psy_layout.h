@@ -139,6 +139,7 @@ struct GScene {
     GColor background;
     uint32_t width, height, spp, seed, max_bounces;
     uint32_t use_fp16;
+    uint32_t ordered_slabs;      // every child box of every node has lo <= hi on each axis (host-checked)
     float distant_energy_total;  // sum of distant light energies
     float lt_root_energy;
     float4 bounds_min, bounds_inv_extent;  // scene box, for the ray sort key's origin cell

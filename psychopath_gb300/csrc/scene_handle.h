@@ -82,10 +82,13 @@ struct PsyScene {
     uint32_t *d_bins = nullptr;
     WaveDesc *d_waves = nullptr;         // wave descriptors of one render call
     uint32_t cap_waves = 0;
-    int minb = 4;                        // persistent kernel register budget (4 or 8 blocks/SM)
+    int minb = 4;                        // trace kernel register budget (target resident blocks per SM)
     uint32_t *d_work = nullptr;          // work counter of the persistent kernels
     unsigned long long *d_counters = nullptr;  // node visits, triangle tests, rays
     bool use_graph = false;              // replay each wave's launch sequence from a CUDA graph
+    int ray_order = 0;                   // trace calls: 1 = bin rays by octant and origin cell first
+    uint32_t *d_bkeys = nullptr, *d_border = nullptr, *d_bhist = nullptr;  // binning scratch
+    size_t cap_bin = 0;
     WaveGraph graph;                     // graph of the scene's own render buffers
     std::mutex mu;
 };

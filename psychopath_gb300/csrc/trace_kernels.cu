@@ -1,0 +1,417 @@
+// Traversal kernels of the GB300 tracing path: closest / any hit for ray
+// batches (one thread per ray, or persistent with lane refill) and for the
+// render wavefront's queues.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+
+#include "dev_surface.cuh"
+#include "kernels.cuh"
+
+using namespace psyd;
+
+// ------------------------------------------------------------------ ray tracing
+template <int STACK, bool COUNT, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay *__restrict__ rays, uint32_t n,
+                                                    const uint32_t *__restrict__ order, PsyHit *__restrict__ hits,
+                                                    PsySurfaceHit *__restrict__ full, int *err,
+                                                    unsigned long long *counters) {
+    __shared__ uint8_t table[8 * 48];
+    load_traversal_table(table);
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t i = q;
+    TraceCount tc{0, 0};
+    if (q < n) {
+        if (order) i = order[q];  // binned order: thread q traces ray order[q]
+        const float *r = reinterpret_cast<const float *>(rays + i);
+        V3 o = v3(r[0], r[1], r[2]), d = v3(r[3], r[4], r[5]);
+        float tmax = r[6], time = r[7];
+        uint32_t flags = reinterpret_cast<const uint32_t *>(r)[9];
+        HitRec h;
+        if (!trace_ray<STACK, COUNT>(S, table, o, d, tmax, time, (flags & PSY_RAY_OCCLUSION) != 0, h, &tc)) {
+            atomicExch(err, PSY_E_OVERFLOW);
+            h.kind = PSY_HIT_MISS_K;
+        }
+        PsyHit out;
+        out.kind = h.kind;
+        out.prim = 0; out.inst = 0; out.t = 0.0f; out.b0 = 0.0f; out.b1 = 0.0f; out.b2 = 0.0f; out.pad = 0.0f;
+        if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
+            GInstance in = S.instances[h.slot];
+            out.prim = h.kind == PSY_HIT_SURFACE_K ? __ldg(S.tri_idx + h.prim).w : h.prim;
+            out.inst = in.id;
+            out.t = h.t; out.b0 = h.b0; out.b1 = h.b1; out.b2 = h.b2;
+        }
+        hits[i] = out;
+        if (full) {
+            PsySurfaceHit f;
+            f.hit = out;
+            f.shader = -1;
+            f.pos[0] = f.pos[1] = f.pos[2] = 0.0f;
+            f.nor[0] = f.nor[1] = f.nor[2] = 0.0f;
+            f.nor_g[0] = f.nor_g[1] = f.nor_g[2] = 0.0f;
+            f.pos_err = 0.0f;
+            f.sample_pdf = 0.0f;
+            if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
+                SurfData sd;
+                resolve_hit<double>(S, h, o, d, time, sd);
+                f.pos[0] = sd.pos.x; f.pos[1] = sd.pos.y; f.pos[2] = sd.pos.z;
+                f.nor[0] = sd.nor.x; f.nor[1] = sd.nor.y; f.nor[2] = sd.nor.z;
+                f.nor_g[0] = sd.nor_g.x; f.nor_g[1] = sd.nor_g.y; f.nor_g[2] = sd.nor_g.z;
+                f.pos_err = sd.pos_err;
+                f.sample_pdf = sd.sample_pdf;
+                f.shader = sd.shader;
+            }
+            full[i] = f;
+        }
+    }
+    if (COUNT) {
+        unsigned long long a = tc.nodes, b = tc.tris, c = (q < n) ? 1ull : 0ull;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, off);
+            b += __shfl_down_sync(0xffffffffu, b, off);
+            c += __shfl_down_sync(0xffffffffu, c, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(counters, a);
+            atomicAdd(counters + 1, b);
+            atomicAdd(counters + 2, c);
+        }
+    }
+}
+
+// Kernel variants: stack depth 64 or 192 entries (local memory only), and a
+// register budget for 4 (the compiler's choice), 5, 6 or 8 resident blocks
+// per SM.  Counting kernels (traversal statistics) exist for the default
+// budget only: node and triangle counts do not depend on the launch shape.
+cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order, PsyHit *hits,
+                              PsySurfaceHit *full, int stack, int minb, int *d_err, unsigned long long *counters,
+                              cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    dim3 b(128), g((n + 127) / 128);
+#define TR(SZ, C, MB) k_trace_rays<SZ, C, MB><<<g, b, 0, st>>>(S, rays, n, order, hits, full, d_err, counters)
+#define TRS(SZ)                                                   \
+    if (counters) TR(SZ, true, 4);                                \
+    else if (minb >= 8) TR(SZ, false, 8);                         \
+    else if (minb >= 6) TR(SZ, false, 6);                         \
+    else if (minb == 5) TR(SZ, false, 5);                         \
+    else TR(SZ, false, 4)
+    if (stack <= 64) { TRS(64); } else { TRS(192); }
+#undef TRS
+#undef TR
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ persistent traversal
+// Ray sources / sinks of the persistent traversal kernel.
+struct IOQueue {  // wavefront: rays of the paths listed in queue[0 .. *count)
+    const uint32_t *queue;
+    const uint32_t *count;
+    const float4 *ro, *rd;
+    const uint8_t *occl;
+    uint4 *ki;
+    float4 *tb;
+    __device__ __forceinline__ uint32_t n() const { return *count; }
+    __device__ __forceinline__ uint32_t load(uint32_t q, V3 &o, V3 &d, float &tmax, float &time, bool &oc) const {
+        uint32_t p = queue[q];
+        float4 a = ro[p], b = rd[p];
+        o = v3(a); d = v3(b); tmax = a.w; time = b.w; oc = occl[p] != 0;
+        return p;
+    }
+    __device__ __forceinline__ void store(const GScene &, uint32_t p, const HitRec &h) const {
+        ki[p] = make_uint4(h.kind, h.prim, h.slot, 0u);
+        tb[p] = make_float4(h.t, h.b0, h.b1, h.b2);
+    }
+};
+struct IORays {  // PsyRay records in, PsyHit records out
+    const PsyRay *rays;
+    uint32_t count;
+    PsyHit *hits;
+    const uint32_t *order;  // optional: the q-th ray taken is order[q]
+    __device__ __forceinline__ uint32_t n() const { return count; }
+    __device__ __forceinline__ uint32_t load(uint32_t q, V3 &o, V3 &d, float &tmax, float &time, bool &oc) const {
+        if (order) q = order[q];
+        const float *r = reinterpret_cast<const float *>(rays + q);
+        o = v3(r[0], r[1], r[2]); d = v3(r[3], r[4], r[5]); tmax = r[6]; time = r[7];
+        oc = (reinterpret_cast<const uint32_t *>(r)[9] & PSY_RAY_OCCLUSION) != 0;
+        return q;
+    }
+    __device__ __forceinline__ void store(const GScene &S, uint32_t q, const HitRec &h) const {
+        PsyHit out;
+        out.kind = h.kind;
+        out.prim = 0; out.inst = 0; out.t = 0.0f; out.b0 = 0.0f; out.b1 = 0.0f; out.b2 = 0.0f; out.pad = 0.0f;
+        if (h.kind == PSY_HIT_SURFACE_K || h.kind == PSY_HIT_LIGHT_K) {
+            out.prim = h.kind == PSY_HIT_SURFACE_K ? __ldg(S.tri_idx + h.prim).w : h.prim;
+            out.inst = S.instances[h.slot].id;
+            out.t = h.t; out.b0 = h.b0; out.b1 = h.b1; out.b2 = h.b2;
+        }
+        hits[q] = out;
+    }
+};
+
+// Persistent traversal: each warp keeps its lanes busy by refilling lanes
+// whose ray finished with the next rays of a global work counter (one
+// aggregated atomic per warp), so long and short rays no longer idle the
+// rest of the warp (Aila & Laine, "Understanding the Efficiency of Ray
+// Traversal on GPUs", 2009).
+template <int STACK, int MINB, class IO>
+__global__ void __launch_bounds__(128, MINB) k_trace_persist(GScene S, IO io, uint32_t *work, int *err,
+                                                            unsigned long long *counters) {
+    __shared__ uint8_t table[8 * 48];
+    load_traversal_table(table);
+    const uint32_t n = io.n();
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint32_t stack[STACK];
+    Lane L;
+    bool active = false, exhausted = false;
+    uint32_t id = 0, nr = 0;
+    TraceCount tc{0, 0};
+    const bool count = counters != nullptr;
+    while (true) {
+        unsigned idle = __ballot_sync(FULL, !active);
+        if (idle && !exhausted) {
+            int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(work, (uint32_t)__popc(idle));
+            base = __shfl_sync(FULL, base, leader);
+            if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+            if (!active) {
+                uint32_t my = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (my < n) {
+                    V3 o, d;
+                    float tmax, time;
+                    bool oc;
+                    id = io.load(my, o, d, tmax, time, oc);
+                    lane_init(S, L, o, d, tmax, time, oc);
+                    active = true;
+                    nr++;
+                }
+            }
+        }
+        if (!__any_sync(FULL, active)) break;
+        if (active) {
+            int r = lane_step<STACK>(S, table, L, stack, tc, count);
+            if (r != 0) {
+                if (r < 0) {
+                    atomicExch(err, PSY_E_OVERFLOW);
+                    L.hit.kind = PSY_HIT_MISS_K;
+                }
+                io.store(S, id, L.hit);
+                active = false;
+            }
+        }
+    }
+    if (count) {
+        unsigned long long a = tc.nodes, b = tc.tris, c = nr;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_down_sync(FULL, a, off);
+            b += __shfl_down_sync(FULL, b, off);
+            c += __shfl_down_sync(FULL, c, off);
+        }
+        if (lane == 0) {
+            atomicAdd(counters, a);
+            atomicAdd(counters + 1, b);
+            atomicAdd(counters + 2, c);
+        }
+    }
+}
+
+template <class IO, int STACK, int MINB>
+static int persist_grid() {
+    static int g = 0;
+    if (g == 0) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trace_persist<STACK, MINB, IO>, 128, 0);
+        g = sms * (per > 0 ? per : 1);
+    }
+    return g;
+}
+
+template <class IO>
+static cudaError_t launch_persist(const GScene &S, const IO &io, uint32_t max_count, int stack, int minb,
+                                  uint32_t *work, int *d_err, unsigned long long *counters, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+#define TP(SZ, MB)                                                                          \
+    {                                                                                       \
+        int g = persist_grid<IO, SZ, MB>();                                                 \
+        uint32_t need = (max_count + 127) / 128;                                            \
+        if ((uint32_t)g > need) g = (int)need;                                              \
+        if (g > 0) k_trace_persist<SZ, MB, IO><<<g, 128, 0, st>>>(S, io, work, d_err, counters); \
+    }
+    if (minb >= 8) {
+        if (stack <= 64) TP(64, 8) else TP(192, 8)
+    } else if (minb >= 6) {
+        if (stack <= 64) TP(64, 6) else TP(192, 6)
+    } else {
+        if (stack <= 64) TP(64, 4) else TP(192, 4)
+    }
+#undef TP
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_persist_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue,
+                                       const uint32_t *count, uint32_t max_count, int stack, int minb, uint32_t *work,
+                                       int *d_err, unsigned long long *counters, cudaStream_t st) {
+    IOQueue io{queue, count, R.o, R.d, R.occl, H.ki, H.tb};
+    return launch_persist(S, io, max_count, stack, minb, work, d_err, counters, st);
+}
+cudaError_t launch_trace_persist_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order,
+                                      PsyHit *hits, int stack, int minb, uint32_t *work, int *d_err,
+                                      unsigned long long *counters, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    IORays io{rays, n, hits, order};
+    return launch_persist(S, io, n, stack, minb, work, d_err, counters, st);
+}
+
+// Queue-driven trace for the render wavefront: a grid-stride loop over the
+// live paths listed in queue[0 .. *count).  COUNT adds the work counters
+// (node visits, triangle tests, rays) into counters[0..2].
+template <int STACK, bool COUNT, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
+                                                     const uint32_t *__restrict__ count, int *err,
+                                                     unsigned long long *counters) {
+    __shared__ uint8_t table[8 * 48];
+    load_traversal_table(table);
+    uint32_t n = *count;
+    TraceCount tc{0, 0};
+    uint32_t nr = 0;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        uint32_t p = queue[q];
+        float4 ro = R.o[p], rd = R.d[p];
+        HitRec h;
+        if (!trace_ray<STACK, COUNT>(S, table, v3(ro), v3(rd), ro.w, rd.w, R.occl[p] != 0, h, &tc)) {
+            atomicExch(err, PSY_E_OVERFLOW);
+            h.kind = PSY_HIT_MISS_K;
+        }
+        nr++;
+        H.ki[p] = make_uint4(h.kind, h.prim, h.slot, 0u);
+        H.tb[p] = make_float4(h.t, h.b0, h.b1, h.b2);
+    }
+    if (COUNT) {
+        unsigned long long a = tc.nodes, b = tc.tris, c = nr;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, off);
+            b += __shfl_down_sync(0xffffffffu, b, off);
+            c += __shfl_down_sync(0xffffffffu, c, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(counters, a);
+            atomicAdd(counters + 1, b);
+            atomicAdd(counters + 2, c);
+        }
+    }
+}
+
+cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
+                               uint32_t max_count, int stack, int minb, int grid, int *d_err,
+                               unsigned long long *counters, cudaStream_t st) {
+    if (grid <= 0) grid = (int)((max_count + 127) / 128);
+    if (grid == 0) return cudaSuccess;
+#define TQ(SZ, C, MB) k_trace_queue<SZ, C, MB><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, counters)
+#define TQS(SZ)                                                   \
+    if (counters) TQ(SZ, true, 4);                                \
+    else if (minb >= 8) TQ(SZ, false, 8);                         \
+    else if (minb >= 6) TQ(SZ, false, 6);                         \
+    else if (minb == 5) TQ(SZ, false, 5);                         \
+    else TQ(SZ, false, 4)
+    if (stack <= 64) { TQS(64); } else { TQS(192); }
+#undef TQS
+#undef TQ
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ ray binning
+// Before a large trace call, rays can be grouped so that a warp's rays start
+// near each other and point into the same octant: key = direction octant
+// (3 bits) above a 15-bit Morton code of the origin's cell in a 32^3 grid
+// over the scene box.  Binning is a counting sort over the 2^18 keys (order
+// inside a bin is arbitrary); each ray's hit is still written at its own
+// index, so results do not depend on it.
+__device__ __forceinline__ uint32_t morton5(uint32_t x, uint32_t y, uint32_t z) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++)
+        m |= (((x >> b) & 1u) << (3 * b)) | (((y >> b) & 1u) << (3 * b + 1)) | (((z >> b) & 1u) << (3 * b + 2));
+    return m;
+}
+__device__ __forceinline__ uint32_t cell5(float v, float lo, float inv) {
+    float c = (v - lo) * inv * 32.0f;
+    c = fminf(fmaxf(c, 0.0f), 31.0f);  // NaN -> 0
+    return (uint32_t)c;
+}
+// Warp-aggregated increment of counters[key]: one atomic per distinct key
+// in the warp.  Returns this lane's slot (old value + rank among equal keys).
+__device__ __forceinline__ uint32_t warp_add_key(uint32_t *counters, uint32_t key, uint32_t active) {
+    uint32_t same = __match_any_sync(active, key);
+    uint32_t lane = threadIdx.x & 31u;
+    uint32_t leader = __ffs(same) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counters + key, (uint32_t)__popc(same));
+    base = __shfl_sync(same, base, leader);
+    return base + __popc(same & ((1u << lane) - 1u));
+}
+__global__ void k_ray_keys(const PsyRay *__restrict__ rays, uint32_t n, float4 bmin, float4 binv,
+                           uint32_t *__restrict__ keys, uint32_t *__restrict__ hist) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t active = __ballot_sync(0xffffffffu, i < n);
+    if (i >= n) return;
+    const float *r = reinterpret_cast<const float *>(rays + i);
+    uint32_t oct = (uint32_t)(r[3] < 0.0f) | ((uint32_t)(r[4] < 0.0f) << 1) | ((uint32_t)(r[5] < 0.0f) << 2);
+    uint32_t key = (oct << 15) | morton5(cell5(r[0], bmin.x, binv.x), cell5(r[1], bmin.y, binv.y),
+                                         cell5(r[2], bmin.z, binv.z));
+    keys[i] = key;
+    warp_add_key(hist, key, active);
+}
+// Exclusive prefix sum of the 2^18 bin counts in place (one block of 1024).
+__global__ void __launch_bounds__(1024) k_scan_bins(uint32_t *hist, uint32_t nbins) {
+    __shared__ uint32_t part[1024];
+    uint32_t per = nbins / 1024, t = threadIdx.x;
+    uint32_t sum = 0;
+    for (uint32_t k = 0; k < per; k++) sum += hist[t * per + k];
+    part[t] = sum;
+    __syncthreads();
+    for (uint32_t off = 1; off < 1024; off <<= 1) {
+        uint32_t v = t >= off ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[t] - sum;
+    for (uint32_t k = 0; k < per; k++) {
+        uint32_t c = hist[t * per + k];
+        hist[t * per + k] = run;
+        run += c;
+    }
+}
+__global__ void k_ray_scatter(const uint32_t *__restrict__ keys, uint32_t n, uint32_t *__restrict__ cursor,
+                              uint32_t *__restrict__ order) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t active = __ballot_sync(0xffffffffu, i < n);
+    if (i >= n) return;
+    order[warp_add_key(cursor, keys[i], active)] = i;
+}
+
+cudaError_t launch_ray_binning(const GScene &S, const PsyRay *rays, uint32_t n, uint32_t *keys, uint32_t *hist,
+                               uint32_t *order, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(hist, 0, PSY_RAY_BINS * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    uint32_t g = (n + 255) / 256;
+    k_ray_keys<<<g, 256, 0, st>>>(rays, n, S.bounds_min, S.bounds_inv_extent, keys, hist);
+    k_scan_bins<<<1, 1024, 0, st>>>(hist, PSY_RAY_BINS);
+    k_ray_scatter<<<g, 256, 0, st>>>(keys, n, hist, order);
+    return cudaGetLastError();
+}
+
+// Constants of this translation unit: the child-order table and the colour
+// of unshaded instances (kernels.cu keeps its own copies).
+void psy_upload_trace_constants(const uint8_t table[8][48], const float magenta[3]) {
+    if (table) cudaMemcpyToSymbol(c_traversal_table, table, 8 * 48);
+    if (magenta) {
+        GColor c{PSY_COLOR_XYZ_K, magenta[0], magenta[1], magenta[2]};
+        cudaMemcpyToSymbol(c_magenta, &c, sizeof(c));
+    }
+}

@@ -24,7 +24,7 @@ EXPORTED = [
     "psy_scene_create", "psy_scene_destroy", "psy_scene_device_bytes", "psy_trace", "psy_trace_device",
     "psy_rays_traced", "psy_render_bucket", "psy_render_image_device", "psy_render_image", "psy_last_error",
     "psy_version", "psy_render_bucket_noalloc", "psy_server_create", "psy_server_add_scene", "psy_submit",
-    "psy_poll", "psy_wait", "psy_cancel", "psy_server_stats", "psy_server_destroy",
+    "psy_poll", "psy_wait", "psy_cancel", "psy_server_stats", "psy_server_destroy", "psy_autotune",
 ]
 
 
@@ -64,6 +64,7 @@ def lib(path=None):
     L.psy_debug_set_sort.argtypes = [vp, C.c_int]
     L.psy_debug_host_build.argtypes = [vp, vp, u32, vp, C.POINTER(u32), C.POINTER(u32)]
     L.psy_debug_set_graph.argtypes = [vp, C.c_int]
+    L.psy_debug_set_ray_order.argtypes = [vp, C.c_int]
     L.psy_debug_render_sized.argtypes = [vp, u32, u32, u32, u32, vp, vp]
     L.psy_server_create.argtypes = [vp, C.POINTER(vp)]
     L.psy_server_add_scene.argtypes = [vp, vp, C.POINTER(u32)]
@@ -73,6 +74,7 @@ def lib(path=None):
     L.psy_cancel.argtypes = [vp, C.c_uint64]
     L.psy_server_stats.argtypes = [vp, vp]
     L.psy_server_destroy.argtypes = [vp]
+    L.psy_autotune.argtypes = [vp, vp, vp]
     _lib = L
     return L
 
@@ -99,12 +101,13 @@ def host_build_info(scene_data, obj, bounds="fp32"):
 class Scene:
     """A scene resident on the GPU (psy_scene_create)."""
 
-    def __init__(self, scene_data, bounds="fp32", shading="f64"):
+    def __init__(self, scene_data, bounds="fp32", shading="f64", ray_order="as_given"):
         self.data = scene_data
         self._desc = scene_data.desc()
         opts = abi.PsySceneOptions()
         opts.bounds_precision = abi.PSY_BOUNDS_FP16 if bounds == "fp16" else abi.PSY_BOUNDS_FP32
         opts.shading_precision = abi.PSY_SHADING_F32 if shading == "f32" else abi.PSY_SHADING_F64
+        opts.ray_order = abi.PSY_RAY_ORDER_BINNED if ray_order == "binned" else abi.PSY_RAY_ORDER_AS_GIVEN
         h = C.c_void_p()
         _check(lib().psy_scene_create(C.byref(self._desc), C.byref(opts), C.byref(h)))
         self.h = h
@@ -157,6 +160,19 @@ class Scene:
 
     def set_launch(self, grid=0, wave_paths=0):
         _check(lib().psy_debug_set_launch(self.h, grid, wave_paths))
+
+    def autotune(self, probe_paths=0, repeats=0):
+        """psy_autotune: time a probe render under candidate launch
+        configurations and keep the fastest on the scene (images unchanged)."""
+        o = abi.PsyTuneOptions()
+        o.probe_paths, o.repeats = probe_paths, repeats
+        r = abi.PsyTuneResult()
+        _check(lib().psy_autotune(self.h, C.byref(o), C.byref(r)))
+        return r.as_dict()
+
+    def set_ray_order(self, binned=True):
+        """Trace calls: bin rays by direction octant and origin cell first."""
+        _check(lib().psy_debug_set_ray_order(self.h, 1 if binned else 0))
 
     def set_graph(self, on=True):
         """Replay each render wave from a captured CUDA graph."""

@@ -1,0 +1,37 @@
+"""psy_autotune: the tuner times a probe render under candidate launch
+configurations (trace kernel form and register budget, stack depth, queue
+tile, sort-key width, wave size, CUDA graphs) and keeps the fastest.  Every
+candidate must render the same image bit for bit, so the image after tuning
+equals the image before."""
+import numpy as np
+import pytest
+
+from psychopath_gb300 import gpu
+
+from . import scene_cases as sc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("case", ["sphere", "motion"])
+def test_autotune_keeps_image(gpu_lib, case):
+    s = sc.sphere_small(48, 27, 8, 6, level=4) if case == "sphere" else sc.motion_small(48, 27, 8, 2)
+    g = gpu.Scene(s)
+    r = gpu.Renderer(g)
+    before, _ = r.render()
+    res = g.autotune(probe_paths=4096, repeats=1)
+    assert res["trace_mode"] in (0, 1)
+    assert res["minb"] in ((4, 5, 6, 8) if res["trace_mode"] == 0 else (4, 6, 8))
+    assert res["stack"] >= g.info()["max_stack"]
+    assert res["sort_bits"] in (0, 4, 7, 10)
+    assert res["candidates"] >= 15
+    assert 0 < res["best_s"] <= res["default_s"]
+    after, _ = r.render()
+    assert np.array_equal(before, after)
+    # the device path with the chosen configuration (graphs included) agrees too
+    torch = pytest.importorskip("torch")
+    d = torch.zeros(before.size, dtype=torch.float32, device="cuda")
+    r.render_device(d.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(d.cpu().numpy().reshape(before.shape), before)
+    g.close()

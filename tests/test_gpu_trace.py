@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from oracle.runner import OracleScene
-from psychopath_gb300 import abi, gpu
+from psychopath_gb300 import abi, gpu, scenes
 
 from . import scene_cases as sc
 
@@ -131,7 +131,7 @@ def test_empty_batch_and_misses(gpu_lib):
     assert (h["kind"] == abi.PSY_HIT_MISS).all()
 
 
-@pytest.mark.parametrize("mode,minb", [(0, 4), (1, 4), (1, 6), (1, 8)])
+@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 5), (0, 6), (0, 8), (1, 4), (1, 6), (1, 8)])
 def test_trace_kernel_variants_identical(gpu_lib, mode, minb):
     """Every traversal kernel variant (one thread per ray, persistent with lane
     refill at each register budget) returns identical hits."""
@@ -145,3 +145,27 @@ def test_trace_kernel_variants_identical(gpu_lib, mode, minb):
     g.set_trace(mode, minb)
     h = tr.trace(rays)
     assert np.array_equal(h, ref)
+
+
+@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 8), (1, 8)])
+def test_binned_ray_order_identical(gpu_lib, mode, minb):
+    """Binning a large batch by direction octant and origin cell only changes
+    which thread traces which ray: hits are identical to the given order."""
+    sd, P, F = sc.grid_small(256, 128)
+    rays = np.concatenate([scenes.incoherent_rays(P, F, 1 << 16, seed=7), scenes.coherent_rays(128)])
+    g = gpu.Scene(sd)
+    tr = gpu.Tracer(g)
+    g.set_trace(mode, minb)
+    ref = tr.trace(rays)
+    g.set_ray_order(True)
+    h = tr.trace(rays)
+    assert np.array_equal(h, ref)
+    # a motion scene through the full-output kernel
+    s = sc.motion_small()
+    rays = sc.targeted_rays(70000, [-50, -50, -50], [50, 50, 50], [-60, -60, 60], [60, 60, 95], seed=3,
+                            time_random=True)
+    g2 = gpu.Scene(s, ray_order="binned")
+    a, fa = gpu.Tracer(g2).trace(rays, full=True)
+    g2.set_ray_order(False)
+    b, fb = gpu.Tracer(g2).trace(rays, full=True)
+    assert np.array_equal(a, b) and np.array_equal(fa, fb)
