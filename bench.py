@@ -53,8 +53,8 @@ def parse_args():
     ap.add_argument("--form", default="both", choices=["both", "plain", "optimized"],
                     help="frame workloads: which forms to time (the headline is the optimized one)")
     ap.add_argument("--launch", default="",
-                    help="optimized form: fixed launch configuration 'mode,minb' instead of psy_autotune "
-                         "(profiling a known configuration)")
+                    help="optimized form: fixed launch configuration 'mode,minb[,queue binning bits]' instead of "
+                         "psy_autotune (profiling a known configuration)")
     return ap.parse_args()
 
 
@@ -283,9 +283,11 @@ def run_ours(args):
         scene = gpu.Scene(sd, bounds=args.bounds, shading="f32")
         t0 = time.perf_counter()
         if args.launch:
-            mode, minb = (int(x) for x in args.launch.split(","))
+            vals = [int(x) for x in args.launch.split(",")]
+            mode, minb, bits = vals[0], vals[1], (vals[2] if len(vals) > 2 else 0)
             scene.set_trace(mode, minb)
-            tune = {"trace_mode": mode, "minb": minb, "wave_paths": 1 << 24, "sort_bits": 0, "use_graph": 0,
+            scene.set_sort(bits)
+            tune = {"trace_mode": mode, "minb": minb, "wave_paths": 1 << 24, "sort_bits": bits, "use_graph": 0,
                     "fixed": True}
         else:
             tune = scene.autotune()
@@ -312,7 +314,7 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     elapsed, p_el = float(t[0].item()), float(t[1].item())
     value = samples * world / elapsed
-    plain_value = p_samples * world / p_el
+    plain_value = p_samples * world / p_el if p_samples else None
 
     # end to end through the public C ABI with a host image buffer
     img = np.zeros((H, W, 3), dtype=np.float32)
@@ -358,8 +360,8 @@ def run_ours(args):
     rows = max(1, tune["wave_paths"] // (W * spp))
     waves = math.ceil(H / rows)
     iters = 2 * sd.max_bounces + 3
-    per_iter = 3 if tune["sort_bits"] else 2
-    launches_per_frame = waves * (1 + per_iter * iters + 1) + waves  # + the ray-count kernel of stats frames
+    binning = 3 * (iters - 1) if tune["sort_bits"] else 0  # keys, scan, scatter between iterations
+    launches_per_frame = waves * (2 + 2 * iters + binning) + waves  # + the ray-count kernel of stats frames
     line = {
         "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
@@ -373,10 +375,11 @@ def run_ours(args):
                    "scene_build_s": round(build_s, 3), "scene_device_bytes": scene.device_bytes(),
                    "autotune": tune, "autotune_s": round(tune_s, 2)},
         "mrays_per_s": rays * world / elapsed / 1e6,
-        "plain": {"value": plain_value, "unit": "samples/s", "ms_per_step": p_el / args.steps * 1e3,
-                  "mrays_per_s": p_rays * world / p_el / 1e6, "trace_kernel_s_per_frame": p_trace / frames,
-                  "form": "f64 shading arithmetic (reference precision), default launch configuration"},
-        "speedup_vs_plain": value / plain_value,
+        "plain": ({"value": plain_value, "unit": "samples/s", "ms_per_step": p_el / args.steps * 1e3,
+                   "mrays_per_s": p_rays * world / p_el / 1e6, "trace_kernel_s_per_frame": p_trace / frames,
+                   "form": "f64 shading arithmetic (reference precision), default launch configuration"}
+                  if plain_value else None),
+        "speedup_vs_plain": value / plain_value if plain_value else None,
         "rel_rmse_vs_plain": rmse,
         "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": W * H * 3 * 4,

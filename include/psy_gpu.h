@@ -313,8 +313,10 @@ int psy_render_bucket_noalloc(PsyScene *scene, const PsyBucket *bucket, uint32_t
  * resident blocks per SM, or persistent with lane refill at 4, 6 or 8),
  * the traversal stack depth (64 or 192 entries, if the scene fits),
  * the queue tile (grid of the wavefront kernels: sized by the queue, or a
- * grid-stride grid of 8, 16 or 32 blocks per SM), the ray-sort key width
- * (0, 4, 7 or 10 bits), the wave size (paths per wave) and CUDA graph replay.
+ * grid-stride grid of 8, 16 or 32 blocks per SM), the key width of the
+ * queue binning between wavefront iterations (0 = off, 4 = occlusion flag
+ * and direction octant, 10 / 13 / 16 = also 2 / 3 / 4 bits per axis of the
+ * origin's cell), the wave size (paths per wave) and CUDA graph replay.
  * A candidate replaces the current choice only when its probe time is at
  * least 2% lower.  Every candidate renders the same image bit for bit (only
  * scheduling changes), so tuning never changes results.  The chosen

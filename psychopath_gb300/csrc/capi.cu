@@ -89,7 +89,7 @@ static int ensure_render(PsyScene *s, uint32_t n) {
     AL(s->queue[0], N * 4); AL(s->queue[1], N * 4);
     AL(s->counts, 16);
     AL(s->d_raycount, 8);
-    AL(s->d_stage, N * 4); AL(s->d_stage_key, N * 2); AL(s->d_bins, 2 * 1024 * 4);
+    AL(s->d_stage, N * 4); AL(s->d_stage_key, N * 2); AL(s->d_bins, 65536 * 4);
 #undef AL
     s->cap_paths = n;
     return PSY_OK;
@@ -339,37 +339,43 @@ int psy_rays_traced(const PsyScene *s, uint64_t *count) {
 // depend on the wave's contents.  ev (optional) receives 3 + 3 * iters
 // timing events.
 int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t max_paths, uint32_t max_pix,
-                       cudaStream_t st, unsigned long long *ctr, const cudaEvent_t *ev) {
+                cudaStream_t st, unsigned long long *ctr, const cudaEvent_t *ev) {
     uint32_t iters = 2 * s->g.max_bounces + 3;
     uint32_t n = max_paths;
+    bool binning = s->sort_bits > 0 && B.stage;
     if (ev) cudaEventRecord(ev[0], st);
     CK(launch_camera(s->g, d_wave, n, B.P, B.R, B.queue[0], B.counts, s->prec, st), "camera launch");
     if (ev) cudaEventRecord(ev[1], st);
-    int cur = 0;
+    // queue rotation: without binning the live paths alternate between
+    // queue[0] and queue[1]; with binning shade writes queue[1] (after the
+    // first iteration its input is the stage buffer) and the binning pass
+    // writes the grouped queue back into the stage buffer
+    uint32_t *qin = B.queue[0], *cin = B.counts;
     for (uint32_t it = 0; it < iters; it++) {
         if (ev) cudaEventRecord(ev[2 + 3 * it], st);
         if (s->trace_mode == 1)
-            CK(launch_trace_persist_queue(s->g, B.R, B.H, B.queue[cur], B.counts + cur, n, s->stack, s->minb, B.work,
-                                          B.err, ctr, st),
+            CK(launch_trace_persist_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, B.work, B.err, ctr, st),
                "trace launch");
         else
-            CK(launch_trace_queue(s->g, B.R, B.H, B.queue[cur], B.counts + cur, n, s->stack, s->minb, s->grid, B.err, ctr,
-                                  st),
+            CK(launch_trace_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, s->grid, B.err, ctr, st),
                "trace launch");
         if (ev) cudaEventRecord(ev[3 + 3 * it], st);
-        CK(cudaMemsetAsync(B.counts + (cur ^ 1), 0, 4, st), "memset count");
-        if (s->sort_bits > 0 && B.stage) {
-            SortBuf sb{B.stage, B.stage_key, B.bins, s->sort_bits};
-            CK(launch_shade_sorted(s->g, d_wave, B.P, B.R, B.H, B.queue[cur], B.counts + cur, n, sb,
-                                   B.counts + (cur ^ 1), B.queue[cur ^ 1], s->grid, s->prec, st),
-               "shade launch");
+        uint32_t *qout = qin == B.queue[1] ? B.queue[0] : B.queue[1];
+        uint32_t *cout = qin == B.queue[1] ? B.counts : B.counts + 1;
+        CK(cudaMemsetAsync(cout, 0, 4, st), "memset count");
+        CK(launch_shade(s->g, d_wave, B.P, B.R, B.H, qin, cin, n, qout, cout, 128, s->grid, s->prec, st),
+           "shade launch");
+        if (binning && it + 1 < iters) {
+            CK(launch_queue_binning(s->g, B.R, qout, cout, n, s->sort_bits, B.stage_key, B.bins, B.stage,
+                                    B.counts + 2, st),
+               "queue binning");
+            qin = B.stage;
+            cin = B.counts + 2;
         } else {
-            CK(launch_shade(s->g, d_wave, B.P, B.R, B.H, B.queue[cur], B.counts + cur, n, B.queue[cur ^ 1],
-                            B.counts + (cur ^ 1), 128, s->grid, s->prec, st),
-               "shade launch");
+            qin = qout;
+            cin = cout;
         }
         if (ev) cudaEventRecord(ev[4 + 3 * it], st);
-        cur ^= 1;
     }
     CK(launch_accumulate(s->g, d_wave, max_pix, B.P, st), "accumulate launch");
     if (ev) cudaEventRecord(ev[2 + 3 * iters], st);
@@ -436,7 +442,7 @@ int alloc_wave_bufs(WaveBufs &B, uint32_t cap, uint32_t cap_waves, bool sorting,
     unsigned char *ctrl = nullptr;
     al(&ctrl, 1024);
     if (sorting) {
-        al(&B.stage, N * 4); al(&B.stage_key, N * 2); al(&B.bins, 2 * 1024 * 4);
+        al(&B.stage, N * 4); al(&B.stage_key, N * 2); al(&B.bins, 65536 * 4);
     }
     al(&B.waves, (size_t)cap_waves * sizeof(WaveDesc));
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc wave buffers");
@@ -836,7 +842,7 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
     // 4. ray-sort key width
     {
         std::vector<TuneCfg> v;
-        for (int b : {0, 4, 7, 10}) { TuneCfg c = cur; c.sort_bits = b; if (b != cur.sort_bits) v.push_back(c); }
+        for (int b : {0, 4, 10, 13, 16}) { TuneCfg c = cur; c.sort_bits = b; if (b != cur.sort_bits) v.push_back(c); }
         try_set(v);
     }
     // 5. wave size
@@ -936,9 +942,9 @@ int psy_debug_set_trace(PsyScene *s, int mode, int minb) {
     else s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : (minb == 5 ? 5 : 4));
     return PSY_OK;
 }
-// Ray binning key width between wavefront iterations: 0 (off), 1, 4, 7, 10.
+// Queue binning key width between wavefront iterations: 0 (off), 4, 10, 13, 16.
 int psy_debug_set_sort(PsyScene *s, int bits) {
-    if (!s || !(bits == 0 || bits == 1 || bits == 4 || bits == 7 || bits == 10)) return fail(PSY_E_INVALID, "bad sort bits");
+    if (!s || !(bits == 0 || bits == 4 || bits == 10 || bits == 13 || bits == 16)) return fail(PSY_E_INVALID, "bad sort bits");
     s->sort_bits = bits;
     return PSY_OK;
 }

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 
+#include "dev_bins.cuh"
 #include "dev_surface.cuh"
 #include "kernels.cuh"
 
@@ -177,27 +178,11 @@ __device__ __forceinline__ void push_live(bool alive, uint32_t p, uint32_t *next
 }
 
 // LightPath::next (src/renderer.rs:449-691).
-// Sort key of a path's next ray: occlusion flag, direction octant, origin
-// cell (bits/3 - 1 bits per axis of the scene box), packed into `bits` bits.
-__device__ __forceinline__ uint32_t ray_sort_key(const GScene &S, float4 o, float4 d, bool occl, int bits) {
-    uint32_t key = occl ? 1u : 0u;
-    if (bits >= 4) key |= ray_code(v3(d)) << 1;
-    if (bits >= 7) {
-        int per = (bits - 4) / 3;  // 1 or 2 bits per axis
-        float cells = (float)(1 << per);
-        uint32_t cx = (uint32_t)fminf(fmaxf((o.x - S.bounds_min.x) * S.bounds_inv_extent.x * cells, 0.0f), cells - 1.0f);
-        uint32_t cy = (uint32_t)fminf(fmaxf((o.y - S.bounds_min.y) * S.bounds_inv_extent.y * cells, 0.0f), cells - 1.0f);
-        uint32_t cz = (uint32_t)fminf(fmaxf((o.z - S.bounds_min.z) * S.bounds_inv_extent.z * cells, 0.0f), cells - 1.0f);
-        key |= ((cx << (2 * per)) | (cy << per) | cz) << 4;
-    }
-    return key;
-}
-
-template <class RT, bool SORT>
+template <class RT>
 __global__ void __launch_bounds__(128) k_shade(GScene S, const WaveDesc *__restrict__ gwave, PathState P, RayBuf R,
                                                HitBuf H, const uint32_t *__restrict__ queue,
                                                const uint32_t *__restrict__ count, uint32_t *next_queue,
-                                               uint32_t *next_count, SortBuf sb) {
+                                               uint32_t *next_count) {
     __shared__ WaveDesc wdesc;
     load_wave(gwave, wdesc);
     uint32_t n = *count;
@@ -342,48 +327,7 @@ __global__ void __launch_bounds__(128) k_shade(GScene S, const WaveDesc *__restr
             }
             P.flags[p] = ev | (bounce << 2) | (has_nb << 10) | (nrays << 16);
         }
-        if (SORT) {
-            uint32_t key = 0;
-            if (alive) key = ray_sort_key(S, R.o[p], R.d[p], R.occl[p] != 0, sb.bits);
-            unsigned mask = __ballot_sync(__activemask(), alive);
-            if (mask != 0) {
-                int lane = threadIdx.x & 31;
-                int leader = __ffs(mask) - 1;
-                uint32_t base = 0;
-                if (lane == leader) base = atomicAdd(next_count, (uint32_t)__popc(mask));
-                base = __shfl_sync(__activemask(), base, leader);
-                if (alive) {
-                    uint32_t pos = base + __popc(mask & ((1u << lane) - 1u));
-                    sb.stage[pos] = p;
-                    sb.stage_key[pos] = (uint16_t)key;
-                    // one atomic per distinct key in the warp
-                    unsigned same = __match_any_sync(mask, key);
-                    if (lane == __ffs(same) - 1) atomicAdd(sb.bins + key, (uint32_t)__popc(same));
-                }
-            }
-        } else {
-            push_live(alive, p, next_queue, next_count);
-        }
-    }
-}
-
-// Scatter staged paths into the next queue grouped by sort key.
-__global__ void k_bin_scatter(const uint32_t *__restrict__ stage, const uint16_t *__restrict__ stage_key,
-                              const uint32_t *__restrict__ count, uint32_t *bins, int nbins, uint32_t *out) {
-    __shared__ uint32_t offs[1024];
-    if (threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (int k = 0; k < nbins; k++) {
-            offs[k] = acc;
-            acc += bins[k];
-        }
-    }
-    __syncthreads();
-    uint32_t n = *count;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t k = stage_key[i];
-        uint32_t pos = offs[k] + atomicAdd(bins + nbins + k, 1u);
-        out[pos] = stage[i];
+        push_live(alive, p, next_queue, next_count);
     }
 }
 
@@ -393,25 +337,72 @@ cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, R
     (void)block;
     if (grid <= 0) grid = (int)((max_count + 127) / 128);
     if (grid == 0) return cudaSuccess;
-    SortBuf none{nullptr, nullptr, nullptr, 0};
-    if (prec == 1) k_shade<float, false><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count, none);
-    else k_shade<double, false><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count, none);
+    if (prec == 1) k_shade<float><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count);
+    else k_shade<double><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count);
     return cudaGetLastError();
 }
 
-cudaError_t launch_shade_sorted(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
-                                const uint32_t *count, uint32_t max_count, SortBuf sb, uint32_t *stage_count,
-                                uint32_t *next_queue, int grid, int prec, cudaStream_t st) {
-    if (grid <= 0) grid = (int)((max_count + 127) / 128);
-    if (grid == 0) return cudaSuccess;
-    int nbins = 1 << sb.bits;
-    cudaError_t e = cudaMemsetAsync(sb.bins, 0, 2 * nbins * sizeof(uint32_t), st);
+// ------------------------------------------------------------------ queue binning
+// Between wavefront iterations the live paths can be grouped by their next
+// ray so that a warp's rays start near each other and point into the same
+// octant: key = occlusion flag, direction octant, then a Morton code of the
+// origin's cell (k bits per axis of the scene box), `bits` = 4 + 3k bits in
+// all.  A counting sort (order inside a bin arbitrary); paths are
+// independent, so the image does not change.
+__device__ __forceinline__ uint32_t queue_key(const GScene &S, float4 o, float4 d, bool occl, int bits) {
+    uint32_t key = (occl ? 1u : 0u) | (ray_code(v3(d)) << 1);
+    int per = (bits - 4) / 3;
+    if (per > 0) {
+        float cells = (float)(1u << per);
+        uint32_t c[3];
+        float ov[3] = {o.x, o.y, o.z}, lo[3] = {S.bounds_min.x, S.bounds_min.y, S.bounds_min.z},
+              iv[3] = {S.bounds_inv_extent.x, S.bounds_inv_extent.y, S.bounds_inv_extent.z};
+#pragma unroll
+        for (int a = 0; a < 3; a++) c[a] = (uint32_t)fminf(fmaxf((ov[a] - lo[a]) * iv[a] * cells, 0.0f), cells - 1.0f);
+        uint32_t m = 0;
+        for (int b = 0; b < per; b++)
+            m |= (((c[0] >> b) & 1u) << (3 * b)) | (((c[1] >> b) & 1u) << (3 * b + 1)) | (((c[2] >> b) & 1u) << (3 * b + 2));
+        key |= m << 4;
+    }
+    return key;
+}
+__global__ void k_queue_keys(GScene S, RayBuf R, const uint32_t *__restrict__ queue, const uint32_t *__restrict__ count,
+                             int bits, uint16_t *__restrict__ keys, uint32_t *__restrict__ hist) {
+    uint32_t n = *count;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        uint32_t q = base + threadIdx.x;
+        uint32_t active = __ballot_sync(0xffffffffu, q < n);
+        if (q < n) {
+            uint32_t p = queue[q];
+            uint32_t key = queue_key(S, R.o[p], R.d[p], R.occl[p] != 0, bits);
+            keys[q] = (uint16_t)key;
+            warp_add_key(hist, key, active);
+        }
+    }
+}
+__global__ void k_queue_scatter(const uint32_t *__restrict__ queue, const uint32_t *__restrict__ count,
+                                const uint16_t *__restrict__ keys, uint32_t *__restrict__ cursor,
+                                uint32_t *__restrict__ out, uint32_t *__restrict__ out_count) {
+    uint32_t n = *count;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *out_count = n;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        uint32_t q = base + threadIdx.x;
+        uint32_t active = __ballot_sync(0xffffffffu, q < n);
+        if (q < n) out[warp_add_key(cursor, keys[q], active)] = queue[q];
+    }
+}
+
+cudaError_t launch_queue_binning(const GScene &S, RayBuf R, const uint32_t *queue, const uint32_t *count,
+                                 uint32_t max_count, int bits, uint16_t *keys, uint32_t *hist, uint32_t *out,
+                                 uint32_t *out_count, cudaStream_t st) {
+    uint32_t nbins = 1u << bits;
+    cudaError_t e = cudaMemsetAsync(hist, 0, nbins * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    if (prec == 1) k_shade<float, true><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, nullptr, stage_count, sb);
-    else k_shade<double, true><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, nullptr, stage_count, sb);
-    int sg = (int)std::min<uint32_t>((max_count + 255) / 256, 152u * 8u);
-    if (sg < 1) sg = 1;
-    k_bin_scatter<<<sg, 256, 0, st>>>(sb.stage, sb.stage_key, stage_count, sb.bins, nbins, next_queue);
+    int g = (int)std::min<uint32_t>((max_count + 255) / 256, 152u * 16u);
+    if (g < 1) g = 1;
+    k_queue_keys<<<g, 256, 0, st>>>(S, R, queue, count, bits, keys, hist);
+    k_scan_bins<<<1, 1024, 0, st>>>(hist, nbins);
+    k_queue_scatter<<<g, 256, 0, st>>>(queue, count, keys, hist, out, out_count);
     return cudaGetLastError();
 }
 

@@ -89,19 +89,12 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                          const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
                          int block, int grid, int prec, cudaStream_t st);
-// Ray binning between wavefront iterations: with sort_bits > 0 the shade
-// kernel appends live paths to `stage` with a key (occlusion flag, direction
-// octant, origin cell) and counts keys in `bins`; k_bin_scatter then writes
-// them grouped by key into the next queue.
-struct SortBuf {
-    uint32_t *stage;      // staged path ids
-    uint16_t *stage_key;  // their keys
-    uint32_t *bins;       // [2 * nbins]: key counts, then fill cursors
-    int bits;             // key width: 0 (no sort), 1, 4, 7 or 10
-};
-cudaError_t launch_shade_sorted(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
-                                const uint32_t *count, uint32_t max_count, SortBuf sb, uint32_t *stage_count,
-                                uint32_t *next_queue, int grid, int prec, cudaStream_t st);
+// Groups the live paths of queue[0 .. *count) by their next ray (occlusion
+// flag, direction octant, origin cell; `bits` = 4, 10, 13 or 16) into
+// out[0 .. n) and sets *out_count = n.  keys: max_count u16; hist: 2^bits u32.
+cudaError_t launch_queue_binning(const GScene &S, RayBuf R, const uint32_t *queue, const uint32_t *count,
+                                 uint32_t max_count, int bits, uint16_t *keys, uint32_t *hist, uint32_t *out,
+                                 uint32_t *out_count, cudaStream_t st);
 // All device buffers one render wave needs (owned by a scene, or carved from
 // a static scratch array by the no-allocation entry point).
 struct WaveBufs {
@@ -109,12 +102,12 @@ struct WaveBufs {
     RayBuf R;
     HitBuf H;
     uint32_t *queue[2];
-    uint32_t *counts;      // [2] queue lengths
+    uint32_t *counts;      // [3] lengths of queue[0], queue[1] and stage
     uint32_t *work;        // persistent-kernel work counter
     int *err;              // device error word
-    uint32_t *stage;       // ray binning (may be null: no binning)
-    uint16_t *stage_key;
-    uint32_t *bins;
+    uint32_t *stage;       // binned queue (may be null: no binning)
+    uint16_t *stage_key;   // binning keys
+    uint32_t *bins;        // 2^16 bin counters
     uint32_t cap;          // paths per wave
     WaveDesc *waves;       // wave descriptors (device)
     uint32_t cap_waves;

@@ -212,8 +212,10 @@ bool issue_wave(PsyServer *s, Lane &L, std::string &err) {
     L.inflight.push_back(std::move(f));
     L.next_slot = (slot + 1) % kRing;
     s->waves++;
-    // camera + (trace, shade[, bin scatter]) per iteration + accumulate
-    s->launches += 2 + (uint64_t)(2 * sc->g.max_bounces + 3) * (sc->sort_bits > 0 ? 3 : 2);
+    // camera + (trace, shade) per iteration + accumulate, and the three
+    // queue-binning kernels between iterations when binning is on
+    uint64_t iters = 2 * sc->g.max_bounces + 3;
+    s->launches += 2 + iters * 2 + (sc->sort_bits > 0 ? 3 * (iters - 1) : 0);
     return true;
 }
 

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 
+#include "dev_bins.cuh"
 #include "dev_surface.cuh"
 #include "kernels.cuh"
 
@@ -342,17 +343,6 @@ __device__ __forceinline__ uint32_t cell5(float v, float lo, float inv) {
     c = fminf(fmaxf(c, 0.0f), 31.0f);  // NaN -> 0
     return (uint32_t)c;
 }
-// Warp-aggregated increment of counters[key]: one atomic per distinct key
-// in the warp.  Returns this lane's slot (old value + rank among equal keys).
-__device__ __forceinline__ uint32_t warp_add_key(uint32_t *counters, uint32_t key, uint32_t active) {
-    uint32_t same = __match_any_sync(active, key);
-    uint32_t lane = threadIdx.x & 31u;
-    uint32_t leader = __ffs(same) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(counters + key, (uint32_t)__popc(same));
-    base = __shfl_sync(same, base, leader);
-    return base + __popc(same & ((1u << lane) - 1u));
-}
 __global__ void k_ray_keys(const PsyRay *__restrict__ rays, uint32_t n, float4 bmin, float4 binv,
                            uint32_t *__restrict__ keys, uint32_t *__restrict__ hist) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -364,27 +354,6 @@ __global__ void k_ray_keys(const PsyRay *__restrict__ rays, uint32_t n, float4 b
                                          cell5(r[2], bmin.z, binv.z));
     keys[i] = key;
     warp_add_key(hist, key, active);
-}
-// Exclusive prefix sum of the 2^18 bin counts in place (one block of 1024).
-__global__ void __launch_bounds__(1024) k_scan_bins(uint32_t *hist, uint32_t nbins) {
-    __shared__ uint32_t part[1024];
-    uint32_t per = nbins / 1024, t = threadIdx.x;
-    uint32_t sum = 0;
-    for (uint32_t k = 0; k < per; k++) sum += hist[t * per + k];
-    part[t] = sum;
-    __syncthreads();
-    for (uint32_t off = 1; off < 1024; off <<= 1) {
-        uint32_t v = t >= off ? part[t - off] : 0u;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
-    }
-    uint32_t run = part[t] - sum;
-    for (uint32_t k = 0; k < per; k++) {
-        uint32_t c = hist[t * per + k];
-        hist[t * per + k] = run;
-        run += c;
-    }
 }
 __global__ void k_ray_scatter(const uint32_t *__restrict__ keys, uint32_t n, uint32_t *__restrict__ cursor,
                               uint32_t *__restrict__ order) {
