@@ -348,15 +348,7 @@ def run_ours(args):
             peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
         except Exception:
             pass
-    traffic = None
-    tr_path = os.path.join(HERE, "profiles", "trace_traffic.json")
-    if os.path.exists(tr_path):
-        try:
-            tj = json.load(open(tr_path))
-            if tj.get("workload") == args.workload and tj.get("bounds") == args.bounds:
-                traffic = tj.get("dram_bytes_per_ray") and tj["dram_bytes_per_ray"] * n_rays_c
-        except Exception:
-            traffic = None
+    traffic = None  # no ncu capture with a known ray count for the frame's trace launches
     rows = max(1, tune["wave_paths"] // (W * spp))
     waves = math.ceil(H / rows)
     iters = 2 * sd.max_bounces + 3
@@ -404,6 +396,19 @@ def run_ours(args):
 
 
 # ---------------------------------------------------------------- traversal microbenchmark
+def traversal_traffic(launch, rays):
+    """DRAM bytes of one traversal launch of `rays` incoherent rays, scaled
+    from the committed ncu summary (traffic grows with the ray count), or
+    None when the summary is for another launch configuration."""
+    path = os.path.join(HERE, "profiles", "traversal_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    kv = dict(l.split(":", 1) for l in open(path) if ":" in l and not l.startswith("#"))
+    if kv.get("launch", "").strip() != launch:
+        return None
+    return float(kv["dram_bytes_per_ray"]) * rays
+
+
 def run_traversal(args):
     """16M coherent (pinhole) and 16M incoherent (cosine-hemisphere from random
     surface points, seed 7) rays against the 2048x1024-quad displaced grid
@@ -492,7 +497,8 @@ def run_traversal(args):
                        "l2": "inputs (671 MB of rays per set) larger than L2"},
             "plain": inc["configs"]["plain"],
             "roofline": {"bound": "hbm", "achieved": bc["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                         "frac": bc["frac"], "traffic": None, "kernel": "k_trace_rays",
+                         "frac": bc["frac"], "traffic": traversal_traffic(inc["best"], n_side * n_side),
+                         "kernel": "k_trace_rays",
                          "note": "algorithmic bytes from the oracle's node / triangle tests per ray"},
             "sets": out}
     print(json.dumps(line), flush=True)

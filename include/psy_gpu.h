@@ -311,6 +311,7 @@ int psy_render_bucket_noalloc(PsyScene *scene, const PsyBucket *bucket, uint32_t
  * paths (all samples of each pixel).  Coordinate descent over, in order: the
  * trace kernel (one thread per ray with a register budget of 4, 5, 6 or 8
  * resident blocks per SM, or persistent with lane refill at 4, 6 or 8),
+ * the shading kernel's register budget (4, 6 or 8 blocks per SM),
  * the traversal stack depth (64 or 192 entries, if the scene fits),
  * the queue tile (grid of the wavefront kernels: sized by the queue, or a
  * grid-stride grid of 8, 16 or 32 blocks per SM), the key width of the
@@ -336,6 +337,7 @@ typedef struct PsyTuneResult {
     uint32_t sort_bits;
     uint32_t wave_paths;
     uint32_t use_graph;
+    uint32_t shade_minb;   /* shading kernel register budget (resident blocks per SM) */
     uint32_t candidates;   /* configurations timed */
     double default_s;      /* probe time of the configuration before tuning */
     double best_s;         /* probe time of the chosen configuration */

@@ -141,7 +141,7 @@ class PsyTuneOptions(C.Structure):
 class PsyTuneResult(C.Structure):
     _fields_ = [("trace_mode", C.c_uint32), ("minb", C.c_uint32), ("stack", C.c_uint32), ("grid", C.c_uint32),
                 ("sort_bits", C.c_uint32), ("wave_paths", C.c_uint32), ("use_graph", C.c_uint32),
-                ("candidates", C.c_uint32), ("default_s", C.c_double), ("best_s", C.c_double)]
+                ("shade_minb", C.c_uint32), ("candidates", C.c_uint32), ("default_s", C.c_double), ("best_s", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

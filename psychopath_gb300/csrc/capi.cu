@@ -363,7 +363,7 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
         uint32_t *qout = qin == B.queue[1] ? B.queue[0] : B.queue[1];
         uint32_t *cout = qin == B.queue[1] ? B.counts : B.counts + 1;
         CK(cudaMemsetAsync(cout, 0, 4, st), "memset count");
-        CK(launch_shade(s->g, d_wave, B.P, B.R, B.H, qin, cin, n, qout, cout, 128, s->grid, s->prec, st),
+        CK(launch_shade(s->g, d_wave, B.P, B.R, B.H, qin, cin, n, qout, cout, s->shade_minb, s->grid, s->prec, st),
            "shade launch");
         if (binning && it + 1 < iters) {
             CK(launch_queue_binning(s->g, B.R, qout, cout, n, s->sort_bits, B.stage_key, B.bins, B.stage,
@@ -387,7 +387,7 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
 // is re-captured when the launch configuration or the buffers change.
 int launch_wave_graph(PsyScene *s, const WaveBufs &B, WaveGraph &G, const WaveDesc *d_wave, uint32_t max_paths,
                       uint32_t max_pix, cudaStream_t st) {
-    WaveLaunchKey k{s->trace_mode, s->minb, s->sort_bits, s->prec, s->stack, s->grid,
+    WaveLaunchKey k{s->trace_mode, s->minb, s->sort_bits, s->prec, s->stack, s->grid, s->shade_minb,
                     max_paths, max_pix, d_wave, B.P.color};
     if (!G.valid || !(G.key == k)) {
         G.reset();
@@ -749,12 +749,14 @@ struct TuneCfg {
     int trace_mode, minb, stack, grid, sort_bits;
     uint32_t wave_paths;
     bool graph;
+    int shade_minb;
 };
 TuneCfg get_cfg(const PsyScene *s) {
-    return {s->trace_mode, s->minb, s->stack, s->grid, s->sort_bits, s->wave_paths, s->use_graph};
+    return {s->trace_mode, s->minb, s->stack, s->grid, s->sort_bits, s->wave_paths, s->use_graph, s->shade_minb};
 }
 void set_cfg(PsyScene *s, const TuneCfg &c) {
     s->trace_mode = c.trace_mode; s->minb = c.minb; s->stack = c.stack; s->grid = c.grid;
+    s->shade_minb = c.shade_minb;
     s->sort_bits = c.sort_bits; s->wave_paths = c.wave_paths;
     if (s->use_graph != c.graph) s->graph.reset();
     s->use_graph = c.graph;
@@ -823,6 +825,12 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
         for (int m : {4, 6, 8}) { TuneCfg c = cur; c.trace_mode = 1; c.minb = m; v.push_back(c); }
         try_set(v);
     }
+    // 1b. shading kernel register budget
+    {
+        std::vector<TuneCfg> v;
+        for (int m : {6, 8}) { TuneCfg c = cur; c.shade_minb = m; v.push_back(c); }
+        try_set(v);
+    }
     // 2. stack depth: the fitting variant and the larger ones
     {
         std::vector<TuneCfg> v;
@@ -874,6 +882,7 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
     res->sort_bits = (uint32_t)cur.sort_bits;
     res->wave_paths = cur.wave_paths;
     res->use_graph = cur.graph ? 1u : 0u;
+    res->shade_minb = (uint32_t)cur.shade_minb;
     res->candidates = ncand;
     res->default_s = default_s;
     res->best_s = best;
@@ -940,6 +949,12 @@ int psy_debug_set_trace(PsyScene *s, int mode, int minb) {
     // persistent kernel: 4, 6 or 8 blocks per SM; one thread per ray: 4, 5 or 6
     if (mode == 1) s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : 4);
     else s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : (minb == 5 ? 5 : 4));
+    return PSY_OK;
+}
+// Shading kernel register budget: 4 (compiler's choice), 6 or 8 blocks per SM.
+int psy_debug_set_shade(PsyScene *s, int minb) {
+    if (!s || !(minb == 4 || minb == 6 || minb == 8)) return fail(PSY_E_INVALID, "bad shade budget");
+    s->shade_minb = minb;
     return PSY_OK;
 }
 // Queue binning key width between wavefront iterations: 0 (off), 4, 10, 13, 16.

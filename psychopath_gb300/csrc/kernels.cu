@@ -178,8 +178,8 @@ __device__ __forceinline__ void push_live(bool alive, uint32_t p, uint32_t *next
 }
 
 // LightPath::next (src/renderer.rs:449-691).
-template <class RT>
-__global__ void __launch_bounds__(128) k_shade(GScene S, const WaveDesc *__restrict__ gwave, PathState P, RayBuf R,
+template <class RT, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_shade(GScene S, const WaveDesc *__restrict__ gwave, PathState P, RayBuf R,
                                                HitBuf H, const uint32_t *__restrict__ queue,
                                                const uint32_t *__restrict__ count, uint32_t *next_queue,
                                                uint32_t *next_count) {
@@ -333,12 +333,21 @@ __global__ void __launch_bounds__(128) k_shade(GScene S, const WaveDesc *__restr
 
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                          const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
-                         int block, int grid, int prec, cudaStream_t st) {
-    (void)block;
+                         int minb, int grid, int prec, cudaStream_t st) {
     if (grid <= 0) grid = (int)((max_count + 127) / 128);
     if (grid == 0) return cudaSuccess;
-    if (prec == 1) k_shade<float><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count);
-    else k_shade<double><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count);
+#define SH(RT, MB) k_shade<RT, MB><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count)
+    // budget 4 = the compiler's own choice (MINB 0 = unspecified)
+    if (prec == 1) {
+        if (minb >= 8) SH(float, 8);
+        else if (minb >= 6) SH(float, 6);
+        else SH(float, 0);
+    } else {
+        if (minb >= 8) SH(double, 8);
+        else if (minb >= 6) SH(double, 6);
+        else SH(double, 0);
+    }
+#undef SH
     return cudaGetLastError();
 }
 

@@ -86,9 +86,10 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
                                uint32_t max_count, int stack, int minb, int grid, int *d_err,
                                unsigned long long *counters, cudaStream_t st);
 // LightPath::next for the queued paths; live paths go to next_queue.
+// minb: register budget for 4 (compiler's choice), 6 or 8 resident blocks.
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                          const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
-                         int block, int grid, int prec, cudaStream_t st);
+                         int minb, int grid, int prec, cudaStream_t st);
 // Groups the live paths of queue[0 .. *count) by their next ray (occlusion
 // flag, direction octant, origin cell; `bits` = 4, 10, 13 or 16) into
 // out[0 .. n) and sets *out_count = n.  keys: max_count u16; hist: 2^bits u32.

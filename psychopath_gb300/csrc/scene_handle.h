@@ -19,12 +19,13 @@ int psy_cuda_fail(cudaError_t e, const char *what);
 // Launch configuration of the wave sequence; the fields a captured CUDA graph
 // depends on.
 struct WaveLaunchKey {
-    int trace_mode, minb, sort_bits, prec, stack, grid;
+    int trace_mode, minb, sort_bits, prec, stack, grid, shade_minb;
     uint32_t max_paths, max_pix;
     const WaveDesc *d_wave;
     const void *bufs;  // identity of the WaveBufs (its path-state base)
     bool operator==(const WaveLaunchKey &o) const {
         return trace_mode == o.trace_mode && minb == o.minb && sort_bits == o.sort_bits && prec == o.prec &&
+               shade_minb == o.shade_minb &&
                stack == o.stack && grid == o.grid && max_paths == o.max_paths && max_pix == o.max_pix &&
                d_wave == o.d_wave && bufs == o.bufs;
     }
@@ -83,6 +84,7 @@ struct PsyScene {
     WaveDesc *d_waves = nullptr;         // wave descriptors of one render call
     uint32_t cap_waves = 0;
     int minb = 4;                        // trace kernel register budget (target resident blocks per SM)
+    int shade_minb = 4;                  // shading kernel register budget
     uint32_t *d_work = nullptr;          // work counter of the persistent kernels
     unsigned long long *d_counters = nullptr;  // node visits, triangle tests, rays
     bool use_graph = false;              // replay each wave's launch sequence from a CUDA graph

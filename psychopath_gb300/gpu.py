@@ -62,6 +62,7 @@ def lib(path=None):
     L.psy_debug_counters.argtypes = [vp, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     L.psy_debug_set_trace.argtypes = [vp, C.c_int, C.c_int]
     L.psy_debug_set_sort.argtypes = [vp, C.c_int]
+    L.psy_debug_set_shade.argtypes = [vp, C.c_int]
     L.psy_debug_host_build.argtypes = [vp, vp, u32, vp, C.POINTER(u32), C.POINTER(u32)]
     L.psy_debug_set_graph.argtypes = [vp, C.c_int]
     L.psy_debug_set_ray_order.argtypes = [vp, C.c_int]
@@ -153,6 +154,10 @@ class Scene:
         """Traversal kernel: mode 0 = one thread per ray, 1 = persistent with
         lane refill; minb = target resident blocks per SM (4 or 8)."""
         _check(lib().psy_debug_set_trace(self.h, mode, minb))
+
+    def set_shade(self, minb):
+        """Shading kernel register budget: 4, 6 or 8 resident blocks per SM."""
+        _check(lib().psy_debug_set_shade(self.h, minb))
 
     def set_sort(self, bits):
         """Ray binning key width between wavefront iterations (0 = off)."""

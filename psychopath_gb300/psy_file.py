@@ -1,0 +1,512 @@
+"""Reader for Psychopath's .psy scene files: parses a scene into a
+`SceneData` (the flattened `PsySceneDesc` the C ABI consumes), following the
+reference's parser:
+
+  tokenizer / data tree     src/parse/data_tree.rs:22-44, 287-546
+  Scene, RenderSettings,    src/parse/psy.rs:95-377 (parse_scene,
+  Camera, World               parse_render_settings, parse_camera,
+                              parse_world)
+  Transform, Color leaves   src/parse/psy.rs:554-615 (parse_matrix,
+                              parse_color)
+  Assembly, Instance        src/parse/psy_assembly.rs:17-188
+  MeshSurface               src/parse/psy_mesh_surface.rs:27-127
+  Sphere / Rectangle /      src/parse/psy_light.rs
+  DistantDisk lights
+  SurfaceShader             src/parse/psy_surface_shader.rs
+
+Numbers are read as f32 with correct rounding (the reference parses text
+straight to f32), and everything the reference computes at parse time is
+computed here in f32 with the same operation order: degrees to radians for
+the field of view, normal normalisation, rec709 to XYZ.
+
+Layout: the reference's parser reads shaders and objects inside the root
+Assembly and binds shaders on instances.  Its two example scenes use an
+older layout -- `Shaders {}` and `Objects {}` sections at Scene level and
+`SurfaceShaderBind` on the mesh -- which that parser does not read;
+`layout="auto"` accepts them by treating both sections as part of the root
+assembly and applying a mesh's binding to its instances that have none.
+
+Nested assemblies (an Instance of an Assembly) are not flattened: the host
+that owns the scene's assembly hierarchy flattens them before building the
+scene description, and this reader raises PsyFileError for them.
+"""
+import math
+import struct
+from decimal import Decimal
+
+import numpy as np
+
+from . import abi, scenes
+
+
+class PsyFileError(ValueError):
+    """A .psy file the reader cannot turn into a scene (the reference's
+    PsyParseError cases), with the line it refers to."""
+
+
+# ---------------------------------------------------------------- data tree
+class Node:
+    """Internal node (children) or leaf (contents) of the data tree."""
+
+    __slots__ = ("type_name", "ident", "children", "contents", "offset")
+
+    def __init__(self, type_name, ident=None, children=None, contents=None, offset=0):
+        self.type_name, self.ident, self.children, self.contents, self.offset = (
+            type_name, ident, children, contents, offset)
+
+    @property
+    def is_leaf(self):
+        return self.children is None
+
+    def leaves(self, type_name):
+        return [c for c in self.children or [] if c.is_leaf and c.type_name == type_name]
+
+    def internals(self, type_name):
+        return [c for c in self.children or [] if not c.is_leaf and c.type_name == type_name]
+
+    def nodes(self, type_name):
+        return [c for c in self.children or [] if c.type_name == type_name]
+
+
+_WS = " \t\r\n"
+_RESERVED = "{}[]$#\\"
+
+
+def _is_ident_char(c):
+    return c not in _WS and c not in _RESERVED
+
+
+class _Tokens:
+    def __init__(self, text):
+        self.t = text
+        self.i = 0
+
+    def skip(self):
+        t, n = self.t, len(self.t)
+        while True:
+            j = self.i
+            while j < n and t[j] in _WS:
+                j += 1
+            if j < n and t[j] == "#":
+                while j < n and t[j] not in "\r\n":
+                    j += 1
+            if j == self.i:
+                return
+            self.i = j
+
+    def next(self):
+        """(kind, value, offset) with kind in '{', '}', '[', ']', 'type',
+        'ident', 'end', 'unknown'."""
+        self.skip()
+        t, i = self.t, self.i
+        if i >= len(t):
+            return ("end", None, i)
+        c = t[i]
+        if c in "{}[]":
+            self.i = i + 1
+            return (c, c, i)
+        if c == "$":
+            j = i + 1
+            esc = False
+            while j < len(t):
+                ch = t[j]
+                if esc:
+                    esc = False
+                elif ch == "\\":
+                    esc = True
+                elif not _is_ident_char(ch):
+                    break
+                j += 1
+            self.i = j
+            return ("ident", t[i:j], i)
+        if _is_ident_char(c):
+            j = i
+            while j < len(t) and _is_ident_char(t[j]):
+                j += 1
+            self.i = j
+            return ("type", t[i:j], i)
+        return ("unknown", c, i)
+
+    def leaf_contents(self):
+        t, i = self.t, self.i
+        j = i
+        esc = False
+        while j < len(t):
+            ch = t[j]
+            if esc:
+                esc = False
+            elif ch == "\\":
+                esc = True
+            elif ch == "]":
+                break
+            j += 1
+        self.i = j
+        return t[i:j]
+
+
+def _line(text, offset):
+    return text.count("\n", 0, offset) + 1
+
+
+def parse_data_tree(text):
+    """The whole file as a ROOT node (src/parse/data_tree.rs:22-44)."""
+    tk = _Tokens(text)
+
+    def err(msg, off):
+        raise PsyFileError("line %d: %s" % (_line(text, off), msg))
+
+    def node():
+        save = tk.i
+        kind, val, off = tk.next()
+        if kind != "type":
+            tk.i = save
+            return None
+        k2, v2, o2 = tk.next()
+        ident = None
+        if k2 == "ident":
+            ident = v2
+            k2, v2, o2 = tk.next()
+            if k2 != "{":
+                err("missing '{' after %s %s" % (val, ident), o2)
+        if k2 == "{":
+            children = []
+            while True:
+                c = node()
+                if c is None:
+                    break
+                children.append(c)
+            k3, _, o3 = tk.next()
+            if k3 != "}":
+                err("missing '}' closing %s" % val, o3)
+            return Node(val, ident, children, None, off)
+        if k2 == "[":
+            contents = tk.leaf_contents()
+            k3, _, o3 = tk.next()
+            if k3 != "]":
+                err("missing ']' closing %s" % val, o3)
+            return Node(val, None, None, contents, off)
+        err("expected '{' or '[' after %s" % val, o2)
+
+    items = []
+    while True:
+        n = node()
+        if n is None:
+            break
+        items.append(n)
+    tk.skip()
+    if tk.i != len(text):
+        err("failed to parse the entire file", tk.i)
+    return Node("ROOT", None, items, None, 0)
+
+
+# ---------------------------------------------------------------- numbers
+def parse_f32(s):
+    """Decimal text -> nearest f32 (ties to even), as a direct text-to-f32
+    conversion does.  Going through f64 first can round twice; that only
+    happens when the f64 value sits exactly halfway between two f32s, and
+    then the exact decimal value decides."""
+    x = float(s)
+    f = np.float32(x)
+    if not np.isfinite(f) or float(f) == x:
+        return f
+    other = np.nextafter(f, np.float32(np.inf) if x > float(f) else np.float32(-np.inf), dtype=np.float32)
+    mid = (float(f) + float(other)) / 2.0  # exact in f64
+    if x != mid:
+        return f
+    d = Decimal(s.strip())
+    lo, hi = (f, other) if float(f) < float(other) else (other, f)
+    dm = Decimal(float(lo)) + (Decimal(float(hi)) - Decimal(float(lo))) / 2
+    if d < dm:
+        return lo
+    if d > dm:
+        return hi
+    even = lo if (struct.unpack("<I", struct.pack("<f", float(lo)))[0] & 1) == 0 else hi
+    return even
+
+
+def _floats(contents, what, node, text, count=None):
+    toks = contents.split()
+    try:
+        vals = [parse_f32(t) for t in toks]
+    except ValueError:
+        raise PsyFileError("line %d: %s must be decimal numbers" % (_line(text, node.offset), what))
+    if count is not None and len(vals) != count:
+        raise PsyFileError("line %d: %s needs %d numbers, found %d" % (_line(text, node.offset), what, count,
+                                                                        len(vals)))
+    return vals
+
+
+def _uints(contents, what, node, text):
+    try:
+        vals = [int(t) for t in contents.split()]
+    except ValueError:
+        raise PsyFileError("line %d: %s must be integers" % (_line(text, node.offset), what))
+    if any(v < 0 for v in vals):
+        raise PsyFileError("line %d: %s must be non-negative" % (_line(text, node.offset), what))
+    return vals
+
+
+def parse_matrix(contents, node, text):
+    """16 numbers, column-major 4x4; the last row is dropped
+    (src/parse/psy.rs:554-568).  Returns the 4x4 (f64 holding f32 values)
+    in the row layout `SceneData` takes."""
+    n = _floats(contents, "Transform", node, text, 16)
+    m = np.zeros((4, 4), dtype=np.float64)
+    for r in range(3):
+        for c in range(4):
+            m[r, c] = float(n[4 * c + r])
+    m[3, 3] = 1.0
+    return m
+
+
+def parse_color(contents, node, text):
+    """'rec709, r g b' / 'blackbody, K factor' / 'color_temperature, K factor'
+    (src/parse/psy.rs:578-615)."""
+    items = [s.strip() for s in contents.split(",")]
+    if len(items) != 2:
+        raise PsyFileError("line %d: colour must be '<space>, <values>'" % _line(text, node.offset))
+    kind, vals = items
+    if kind == "rec709":
+        v = _floats(vals, "rec709 colour", node, text, 3)
+        return scenes.xyz_color(np.array(v, dtype=np.float32))
+    if kind in ("blackbody", "color_temperature"):
+        v = _floats(vals, kind + " colour", node, text, 2)
+        c = abi.PsyColor()
+        c.kind = abi.PSY_COLOR_BLACKBODY if kind == "blackbody" else abi.PSY_COLOR_TEMPERATURE
+        c.v[0], c.v[1], c.v[2] = float(v[0]), float(v[1]), 0.0
+        return c
+    raise PsyFileError("line %d: unknown colour space '%s'" % (_line(text, node.offset), kind))
+
+
+def _normalized_f32(v):
+    """glam normalize in f32: v * (1 / sqrt((x*x + y*y) + z*z))."""
+    v = np.asarray(v, dtype=np.float32)
+    d = (v[..., 0] * v[..., 0] + v[..., 1] * v[..., 1]) + v[..., 2] * v[..., 2]
+    r = np.float32(1.0) / np.sqrt(d)
+    return v * r[..., None]
+
+
+# ---------------------------------------------------------------- scene
+def _one(node, type_name, text):
+    found = node.nodes(type_name)
+    if len(found) != 1:
+        raise PsyFileError("line %d: %s needs exactly one %s section, found %d" % (
+            _line(text, node.offset), node.type_name, type_name, len(found)))
+    return found[0]
+
+
+def _leaf1(node, type_name, text, required=True):
+    found = node.leaves(type_name)
+    if not found:
+        if required:
+            raise PsyFileError("line %d: %s is missing %s" % (_line(text, node.offset), node.type_name, type_name))
+        return None
+    return found[0]
+
+
+def _render_settings(node, text):
+    res = _leaf1(node, "Resolution", text)
+    spp = _leaf1(node, "SamplesPerPixel", text)
+    r = _uints(res.contents, "Resolution", res, text)
+    s = _uints(spp.contents, "SamplesPerPixel", spp, text)
+    if len(r) != 2 or len(s) != 1:
+        raise PsyFileError("line %d: Resolution is '[width height]', SamplesPerPixel '[n]'" % _line(text, node.offset))
+    seed = 0
+    sd = _leaf1(node, "Seed", text, required=False)
+    if sd is not None:
+        v = _uints(sd.contents, "Seed", sd, text)
+        if len(v) != 1:
+            raise PsyFileError("line %d: Seed is '[n]'" % _line(text, sd.offset))
+        seed = v[0]
+    return r[0], r[1], s[0], seed
+
+
+def _camera(node, text):
+    mats, fovs, fds, ars = [], [], [], []
+    deg = np.float32(np.float32(math.pi) / np.float32(180.0))
+    for c in node.children:
+        if not c.is_leaf:
+            continue
+        if c.type_name == "Fov":
+            fovs.append(np.float32(_floats(c.contents, "Fov", c, text, 1)[0] * deg))
+        elif c.type_name == "FocalDistance":
+            fds.append(_floats(c.contents, "FocalDistance", c, text, 1)[0])
+        elif c.type_name == "ApertureRadius":
+            ars.append(_floats(c.contents, "ApertureRadius", c, text, 1)[0])
+        elif c.type_name == "Transform":
+            mats.append(parse_matrix(c.contents, c, text))
+    if not mats or not fovs:
+        raise PsyFileError("line %d: Camera needs at least a Fov and a Transform" % _line(text, node.offset))
+    return mats, fovs, ars, fds
+
+
+def _shader(node, text):
+    t = _leaf1(node, "Type", text).contents.strip()
+    col = _leaf1(node, "Color", text)
+    color = parse_color(col.contents, col, text)
+    s = abi.PsyShaderDesc()
+    s.color = color
+    if t == "Lambert":
+        s.kind = abi.PSY_SHADER_LAMBERT
+    elif t == "Emit":
+        s.kind = abi.PSY_SHADER_EMIT
+    elif t == "GGX":
+        s.kind = abi.PSY_SHADER_GGX
+        r = _leaf1(node, "Roughness", text)
+        f = _leaf1(node, "Fresnel", text)
+        s.roughness = float(_floats(r.contents, "Roughness", r, text, 1)[0])
+        s.fresnel = float(_floats(f.contents, "Fresnel", f, text, 1)[0])
+    else:
+        raise PsyFileError("line %d: unknown SurfaceShader type '%s'" % (_line(text, node.offset), t))
+    return s
+
+
+def _mesh(node, text):
+    verts = []
+    for lf in node.leaves("Vertices"):
+        v = _floats(lf.contents, "Vertices", lf, text)
+        verts.append(np.array(v[: len(v) // 3 * 3], dtype=np.float32).reshape(-1, 3))
+    if not verts:
+        raise PsyFileError("line %d: MeshSurface has no Vertices" % _line(text, node.offset))
+    nv = verts[0].shape[0]
+    if any(v.shape[0] != nv for v in verts):
+        raise PsyFileError("line %d: every Vertices time sample needs the same count" % _line(text, node.offset))
+    normals = []
+    for lf in node.leaves("Normals"):
+        n = _floats(lf.contents, "Normals", lf, text)
+        normals.append(_normalized_f32(np.array(n[: len(n) // 3 * 3], dtype=np.float32).reshape(-1, 3)))
+    if normals and (len(normals) != len(verts) or any(n.shape[0] != nv for n in normals)):
+        raise PsyFileError("line %d: Normals must match Vertices in time samples and count" % _line(text, node.offset))
+    fvc = node.leaves("FaceVertCounts")
+    fvi = node.leaves("FaceVertIndices")
+    counts = _uints(fvc[0].contents, "FaceVertCounts", fvc[0], text) if fvc else []
+    idx = _uints(fvi[0].contents, "FaceVertIndices", fvi[0], text) if fvi else []
+    tris = []
+    ii = 0
+    for fc in counts:
+        if fc < 3:
+            raise PsyFileError("line %d: polygons need at least three vertices" % _line(text, node.offset))
+        if ii + fc > len(idx):
+            raise PsyFileError("line %d: FaceVertIndices is shorter than FaceVertCounts says" % _line(text, node.offset))
+        for vi in range(fc - 2):  # fan from the polygon's first vertex
+            tris.append((idx[ii], idx[ii + vi + 1], idx[ii + vi + 2]))
+        ii += fc
+    tris = np.array(tris, dtype=np.uint32).reshape(-1, 3)
+    if tris.size and int(tris.max()) >= nv:
+        raise PsyFileError("line %d: face vertex index out of range" % _line(text, node.offset))
+    return np.stack(verts), (np.stack(normals) if normals else None), tris
+
+
+def _light_keys(node, text, leaf, count):
+    out = []
+    for lf in node.leaves(leaf):
+        out.append(_floats(lf.contents, leaf, lf, text, count))
+    return out
+
+
+def _colors(node, text):
+    return [parse_color(lf.contents, lf, text) for lf in node.leaves("Color")]
+
+
+class PsyScene:
+    """A parsed .psy scene: `data` (SceneData) plus the names the file used."""
+
+    def __init__(self, data, name, output_path, object_names, shader_names):
+        self.data, self.name, self.output_path = data, name, output_path
+        self.object_names, self.shader_names = object_names, shader_names
+
+
+def load_psy(text, scene_index=0, layout="auto", max_bounces=2):
+    """Parse .psy text and return the scene_index-th Scene as a PsyScene.
+    max_bounces is the bounce limit of the light paths (the reference
+    renderer hard-codes 2, src/renderer.rs:599)."""
+    root = parse_data_tree(text)
+    sc = root.internals("Scene")
+    if scene_index >= len(sc):
+        raise PsyFileError("file has %d Scene sections" % len(sc))
+    scene = sc[scene_index]
+    out = _one(scene, "Output", text)
+    path_leaf = _leaf1(out, "Path", text)
+    p = path_leaf.contents.strip()
+    if len(p) < 2 or p[0] != '"' or not p.endswith('"'):
+        raise PsyFileError("line %d: file paths must be surrounded by quotes" % _line(text, path_leaf.offset))
+    w, h, spp, seed = _render_settings(_one(scene, "RenderSettings", text), text)
+    mats, fovs, ars, fds = _camera(_one(scene, "Camera", text), text)
+    world = _one(scene, "World", text)
+    asm = _one(scene, "Assembly", text)
+
+    sd = scenes.SceneData(w, h, spp, seed=seed, max_bounces=max_bounces)
+    sd.set_camera(mats, [], ars, fds, fovs_rad=fovs)
+    bgs = _one(world, "BackgroundShader", text)
+    bt = _leaf1(bgs, "Type", text).contents.strip()
+    if bt != "Color":
+        raise PsyFileError("line %d: unknown BackgroundShader type '%s'" % (_line(text, bgs.offset), bt))
+    bc = _leaf1(bgs, "Color", text)
+    sd.background = parse_color(bc.contents, bc, text)
+    for dl in world.internals("DistantDiskLight"):
+        radii = [k[0] for k in _light_keys(dl, text, "Radius", 1)]
+        dirs = _light_keys(dl, text, "Direction", 3)
+        cols = _colors(dl, text)
+        if not radii or not dirs or not cols:
+            raise PsyFileError("line %d: DistantDiskLight needs Radius, Direction and Color" % _line(text, dl.offset))
+        sd.add_distant_light(radii, np.array(dirs, dtype=np.float32), cols)
+
+    # root assembly content, plus the Scene-level Shaders / Objects sections
+    # of the older layout
+    content = list(asm.children)
+    if layout == "auto":
+        for sec in ("Shaders", "Objects"):
+            for s in scene.internals(sec):
+                content = list(s.children) + content
+    elif layout != "current":
+        raise ValueError("layout is 'auto' or 'current'")
+    shader_names, object_names, object_binds = {}, {}, {}
+    instances = []
+    for c in content:
+        t = c.type_name
+        if t == "SurfaceShader":
+            if c.is_leaf or c.ident is None:
+                raise PsyFileError("line %d: a SurfaceShader needs a $name and a body" % _line(text, c.offset))
+            shader_names[c.ident] = sd.add_shader(0)
+            sd.shaders[shader_names[c.ident]] = _shader(c, text)
+        elif t == "MeshSurface":
+            if c.is_leaf or c.ident is None:
+                raise PsyFileError("line %d: a MeshSurface needs a $name and a body" % _line(text, c.offset))
+            v, n, tr = _mesh(c, text)
+            object_names[c.ident] = sd.add_mesh(v, tr, n)
+            if layout == "auto" and c.leaves("SurfaceShaderBind"):
+                # older layout: the shader is bound on the object
+                object_binds[c.ident] = c.leaves("SurfaceShaderBind")[0]
+        elif t == "SphereLight":
+            radii = [k[0] for k in _light_keys(c, text, "Radius", 1)]
+            object_names[c.ident] = sd.add_sphere_light(radii, _colors(c, text))
+        elif t == "RectangleLight":
+            dims = _light_keys(c, text, "Dimensions", 2)
+            object_names[c.ident] = sd.add_rect_light(dims, _colors(c, text))
+        elif t == "Assembly":
+            raise PsyFileError("line %d: nested assemblies are flattened by the host, not read here"
+                               % _line(text, c.offset))
+        elif t == "Instance":
+            instances.append(c)
+    for c in instances:
+        data = c.leaves("Data")
+        if len(data) != 1:
+            raise PsyFileError("line %d: an Instance needs exactly one Data" % _line(text, c.offset))
+        name = data[0].contents.strip()
+        if name not in object_names:
+            raise PsyFileError("line %d: Instance of unknown data '%s'" % (_line(text, data[0].offset), name))
+        bind = c.leaves("SurfaceShaderBind") or ([object_binds[name]] if name in object_binds else [])
+        shader = -1
+        if bind:
+            sname = bind[0].contents.strip()
+            if sname not in shader_names:
+                raise PsyFileError("line %d: unknown shader '%s'" % (_line(text, bind[0].offset), sname))
+            shader = shader_names[sname]
+        keys = [parse_matrix(t.contents, t, text) for t in c.leaves("Transform")]
+        sd.add_instance(object_names[name], shader, keys)
+    return PsyScene(sd, scene.ident, p[1:-1], object_names, shader_names)
+
+
+def load_psy_file(path, **kw):
+    with open(path, "r", encoding="utf-8") as f:
+        return load_psy(f.read(), **kw)

@@ -155,9 +155,11 @@ class SceneData:
         self.instances.append((obj, shader, [np.asarray(k, dtype=np.float64) for k in world_to_object_keys]))
         return len(self.instances) - 1
 
-    def set_camera(self, cam_to_world_keys, fovs_deg, aperture_radii=(), focus_distances=()):
-        self.camera = ([np.asarray(k) for k in cam_to_world_keys], [math.radians(f) for f in fovs_deg],
-                       list(aperture_radii), list(focus_distances))
+    def set_camera(self, cam_to_world_keys, fovs_deg, aperture_radii=(), focus_distances=(), fovs_rad=None):
+        """Camera keys; fields of view in degrees, or already in radians
+        (fovs_rad, as f32 values computed by the caller)."""
+        fovs = list(fovs_rad) if fovs_rad is not None else [math.radians(f) for f in fovs_deg]
+        self.camera = ([np.asarray(k) for k in cam_to_world_keys], fovs, list(aperture_radii), list(focus_distances))
 
     def add_distant_light(self, radii, directions, colors):
         self.distant.append((list(radii), np.asarray(directions, dtype=np.float32).reshape(-1, 3), list(colors)))

@@ -115,3 +115,18 @@ def test_f32_shading_precision_error(gpu_lib):
     o = OracleScene(s)
     ref, _ = o.render(threads=8)
     assert rel_rmse(img, ref) < 0.01, rel_rmse(img, ref)
+
+
+@pytest.mark.parametrize("minb", [6, 8])
+def test_shade_register_budget_does_not_change_image(gpu_lib, minb):
+    """The shading kernel compiled for more resident blocks (fewer registers)
+    computes the same paths: bit-identical image, both precisions."""
+    s = sc.sphere_small(24, 16, 4, 6, level=3)
+    for shading in ("f64", "f32"):
+        g = gpu.Scene(s, shading=shading)
+        r = gpu.Renderer(g)
+        a, _ = r.render()
+        g.set_shade(minb)
+        b, _ = r.render()
+        assert np.array_equal(a, b)
+        g.close()
