@@ -352,11 +352,25 @@ DI bool slab_hit_finite(float xlo, float xhi, float ylo, float yhi, float zlo, f
 // (lo - o) * di <= (hi - o) * di when di > 0 (rounding is monotonic) and the
 // reverse when di < 0, so min / max of the two slab distances are known and
 // need no instructions.  Decisions equal slab_hit_finite's.
+// Three-input minimum / maximum (PTX min.f32 / max.f32 with three
+// operands).  Exact, like two two-input steps, for inputs without NaN.
+DI float fmin3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+DI float fmax3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
 DI bool slab_hit_ordered(float nxp, float fxp, float nyp, float fyp, float nzp, float fzp, V3 o, V3 di, float max_t) {
     float nx = (nxp - o.x) * di.x, ny = (nyp - o.y) * di.y, nz = (nzp - o.z) * di.z;
     float fx = (fxp - o.x) * di.x, fy = (fyp - o.y) * di.y, fz = (fzp - o.z) * di.z;
-    float far_t = fminf(fminf(fx, fminf(fy, fz)) * PSY_BBOX_MAXT_ADJUST, max_t);
-    float near_t = fmaxf(fmaxf(nx, ny), fmaxf(nz, 0.0f));
+    // no NaN here (finite, nonzero inverse direction; finite or infinite
+    // bounds), so the three-input forms give the same values
+    float far_t = fminf(fmin3f(fx, fy, fz) * PSY_BBOX_MAXT_ADJUST, max_t);
+    float near_t = fmax3f(nx, ny, fmaxf(nz, 0.0f));
     return near_t < far_t;
 }
 DI bool finite3(V3 v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }

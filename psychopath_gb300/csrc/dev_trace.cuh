@@ -259,9 +259,14 @@ DI bool trace_ray(const GScene &S, const uint8_t *table, V3 o, V3 d, float tmax,
                                     : node_hits(S, cur, lo, ldi, tmax, time, oct, safe, code, count, ch);
             if (COUNT) cnt->nodes++;
             if (m == 0) goto pop;
+            // children in the table's visit order: push all hit children
+            // but the first, descend into the first.  The device table maps
+            // positions past the node's child count to its empty slots (never
+            // in m), so the loop has a fixed trip count.
             uint32_t order = row[code];
             uint32_t next = PSY_REF_NONE;
-            for (int i = (int)count - 1; i >= 0; i--) {
+#pragma unroll
+            for (int i = 3; i >= 0; i--) {
                 uint32_t ci = (order >> (i * 2)) & 3u;
                 if (m & (1u << ci)) {
                     if (next != PSY_REF_NONE) {
@@ -272,6 +277,7 @@ DI bool trace_ray(const GScene &S, const uint8_t *table, V3 o, V3 d, float tmax,
                     next = c;
                 }
             }
+            (void)count;
             cur = next;
         }
         // leaf

@@ -68,11 +68,22 @@ static void traversal_table_host(uint8_t t[8][48]) {
         }
     }
 }
+// Device copy of the table: positions past a node's child count (entries
+// 27..44 order three children, 45..47 two) point at the node's empty child
+// slots, so traversal can walk all four positions.
+static void extend_traversal_table(uint8_t t[8][48]) {
+    for (int rd = 0; rd < 8; rd++)
+        for (int k = 27; k < 48; k++) {
+            if (k < 45) t[rd][k] = (uint8_t)(t[rd][k] | (3u << 6));
+            else t[rd][k] = (uint8_t)(t[rd][k] | (2u << 4) | (3u << 6));
+        }
+}
 void psy_upload_constants() {
     uint32_t d[8][32];
     uint8_t t[8][48];
     sobol_dirs_host(d);
     traversal_table_host(t);
+    extend_traversal_table(t);
     cudaMemcpyToSymbol(c_sobol_dirs, d, sizeof(d));
     cudaMemcpyToSymbol(c_traversal_table, t, sizeof(t));
     psy_upload_trace_constants(t, nullptr);
