@@ -280,6 +280,15 @@ int psy_render_image_device(PsyScene *scene, const uint32_t *crop,
 int psy_render_image(PsyScene *scene, const uint32_t *crop, float *xyz_out,
                      PsyRenderStats *stats);
 
+/* Image output as the reference writes PNGs (Image::write_png,
+ * src/image.rs:138-164): the XYZ image d_xyz (width*height*3 floats, row 0
+ * first, as the render calls produce) becomes RGBA8 in d_rgba
+ * (width*height*4 bytes): XYZ -> rec709 (equal-energy white), sRGB gamma,
+ * clamp to [0, 1], x 255 truncated; rows flipped (d_rgba row 0 = the
+ * image's last row), alpha 255.  Runs on `stream` (NULL: the legacy default
+ * stream); both buffers are device memory. */
+int psy_xyz_to_srgb8(const float *d_xyz, uint32_t width, uint32_t height, uint8_t *d_rgba, void *stream);
+
 /* Render one bucket without allocating device memory.  This call has no
  * counterpart in the reference: it exists for hosts that cannot call
  * cudaMalloc once they are running -- for example a process whose device

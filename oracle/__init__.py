@@ -75,6 +75,7 @@ def lib():
         L.psyo_spectrum_to_xyz.argtypes = [fp, f32, fp]
         L.psyo_rec709_e_to_xyz.argtypes = [fp, fp]
         L.psyo_rec709_to_xyz.argtypes = [fp, fp]
+        L.psyo_xyz_to_srgb8.argtypes = [fp, C.c_uint32, C.c_uint32, C.c_void_p]
         L.psyo_intersect_triangle.restype = C.c_int
         L.psyo_intersect_triangle.argtypes = [fp, fp, f32, fp, fp, fp, fp]
         L.psyo_quick_select_ints.restype = u32

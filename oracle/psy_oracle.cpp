@@ -2032,6 +2032,63 @@ extern "C" void psyo_rec709_to_xyz(const float *rgb, float *xyz) {
     rgb_to_xyz_matrix(0.640, 0.330, 0.300, 0.600, 0.150, 0.060, 0.3127, 0.3290, m);
     apply3(m, rgb, xyz);
 }
+// Image::write_png's pixel conversion (src/image.rs:138-164, 275-305) with
+// the xyz_to_rec709_e matrix of sub_crates/color/build.rs:162-188 (inverse of
+// the equal-energy rec709 matrix by Gauss-Jordan elimination with partial
+// pivoting, :246-323, in f64, printed with 10 decimals).
+static void xyz_to_rec709_e_m(float out[9]) {
+    const double rx = 0.640, ry = 0.330, gx = 0.300, gy = 0.600, bx = 0.150, by = 0.060;
+    const double wx = 1.0 / 3.0, wy = 1.0 / 3.0, Y = 1.0;
+    double X = wx * Y / wy, Z = (1.0 - wx - wy) * Y / wy;
+    double d = rx * (by - gy) + bx * (gy - ry) + gx * (ry - by);
+    double sr = (X * (by - gy) - gx * (Y * (by - 1.0) + by * (X + Z)) + bx * (Y * (gy - 1.0) + gy * (X + Z))) / d;
+    double sg = (X * (ry - by) + rx * (Y * (by - 1.0) + by * (X + Z)) - bx * (Y * (ry - 1.0) + ry * (X + Z))) / d;
+    double sb = (X * (gy - ry) - rx * (Y * (gy - 1.0) + gy * (X + Z)) + gx * (Y * (ry - 1.0) + ry * (X + Z))) / d;
+    double a[3][3] = {{sr * rx, sg * gx, sb * bx}, {sr * ry, sg * gy, sb * by},
+                      {sr * (1.0 - rx - ry), sg * (1.0 - gx - gy), sb * (1.0 - bx - by)}};
+    double inv[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int i = 0; i < 2; i++) {  // forward elimination, largest pivot
+        int p = i;
+        double best = std::fabs(a[i][i]);
+        for (int j = i + 1; j < 3; j++)
+            if (std::fabs(a[j][i]) > best) { best = std::fabs(a[j][i]); p = j; }
+        if (p != i)
+            for (int k = 0; k < 3; k++) { std::swap(a[i][k], a[p][k]); std::swap(inv[i][k], inv[p][k]); }
+        for (int j = i + 1; j < 3; j++) {
+            double f = a[j][i] / a[i][i];
+            for (int k = 0; k < 3; k++) { a[j][k] -= f * a[i][k]; inv[j][k] -= f * inv[i][k]; }
+        }
+    }
+    for (int i = 2; i >= 0; i--) {  // back substitution
+        double f = a[i][i];
+        for (int k = 0; k < 3; k++) { a[i][k] /= f; inv[i][k] /= f; }
+        for (int j = 0; j < i; j++) {
+            double g = a[j][i];
+            for (int k = 0; k < 3; k++) { a[j][k] -= g * a[i][k]; inv[j][k] -= g * inv[i][k]; }
+        }
+    }
+    for (int i = 0; i < 9; i++) {
+        char buf[64];
+        std::snprintf(buf, sizeof(buf), "%.10f", inv[i / 3][i % 3]);
+        out[i] = std::strtof(buf, nullptr);
+    }
+}
+extern "C" void psyo_xyz_to_srgb8(const float *xyz, uint32_t w, uint32_t h, uint8_t *rgba) {
+    float m[9];
+    xyz_to_rec709_e_m(m);
+    auto gamma = [](float n) { return n < 0.0031308f ? n * 12.92f : (1.055f * std::pow(n, 1.0f / 2.4f)) - 0.055f; };
+    auto q = [](float n) {
+        float v = std::fmin(1.0f, std::fmax(0.0f, n)) * 255.0f;
+        return (uint8_t)v;
+    };
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) {
+            float rgb[3];
+            apply3(m, xyz + ((size_t)(h - 1 - y) * w + x) * 3, rgb);
+            uint8_t *o = rgba + ((size_t)y * w + x) * 4;
+            o[0] = q(gamma(rgb[0])); o[1] = q(gamma(rgb[1])); o[2] = q(gamma(rgb[2])); o[3] = 255;
+        }
+}
 extern "C" int psyo_intersect_triangle(const float *o, const float *d, float max_t, const float *p0, const float *p1,
                                        const float *p2, float *out) {
     TriPre pre = tri_precompute(v3(d[0], d[1], d[2]));

@@ -68,6 +68,7 @@ void psyo_xyz_to_spectrum(const float *xyz, float hero_wavelength, float *out4);
 void psyo_spectrum_to_xyz(const float *e4, float hero_wavelength, float *xyz_out);
 void psyo_rec709_e_to_xyz(const float *rgb, float *xyz);
 void psyo_rec709_to_xyz(const float *rgb, float *xyz);
+void psyo_xyz_to_srgb8(const float *xyz, uint32_t w, uint32_t h, uint8_t *rgba);
 int psyo_intersect_triangle(const float *orig, const float *dir, float max_t, const float *p0, const float *p1,
                             const float *p2, float *out_tb);
 uint32_t psyo_quick_select_ints(int32_t *list, uint32_t n, uint32_t place);

@@ -891,6 +891,20 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
 
 extern "C" {
 
+// ---------------------------------------------------------------- image output
+// XYZ image -> sRGB RGBA8 as Image::write_png converts it (src/image.rs:138-164).
+int psy_xyz_to_srgb8(const float *d_xyz, uint32_t width, uint32_t height, uint8_t *d_rgba, void *stream) {
+    if (!d_xyz || !d_rgba) return fail(PSY_E_INVALID, "null argument");
+    if ((uint64_t)width * height > 0xFFFFFFFFull) return fail(PSY_E_INVALID, "image too large");
+    static Mat3f m = [] {
+        Mat3f r;
+        xyz_to_rec709_e_matrix(r.m);
+        return r;
+    }();
+    CK(launch_xyz_to_srgb8(d_xyz, width, height, m, d_rgba, (cudaStream_t)stream), "srgb conversion");
+    return PSY_OK;
+}
+
 // ---------------------------------------------------------------- inspection
 // Not part of the reference-facing interface: facts of the build for tests.
 int psy_debug_mesh_bvh_info(PsyScene *s, uint32_t object, uint32_t *tri_order, uint32_t *node_count) {

@@ -466,6 +466,38 @@ cudaError_t launch_count_rays(PathState P, uint32_t n, unsigned long long *out, 
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ image output
+// Image::write_png's conversion (src/image.rs:138-164, 293-305): XYZ ->
+// rec709 (m, row-major, the generated xyz_to_rec709_e), sRGB gamma, clamp
+// to [0, 1], x 255 truncated to u8, alpha 255; rows flipped (PNG row 0 is
+// the image's last row).
+__device__ __forceinline__ float srgb_gamma(float n) {
+    return n < 0.0031308f ? n * 12.92f : (1.055f * powf(n, 1.0f / 2.4f)) - 0.055f;
+}
+__device__ __forceinline__ uint8_t quantize_255(float n) {
+    float v = fminf(1.0f, fmaxf(0.0f, n)) * 255.0f;  // NaN -> 0 (Rust's max)
+    return (uint8_t)v;
+}
+__global__ void k_xyz_to_srgb8(const float *__restrict__ xyz, uint32_t w, uint32_t h, Mat3f m,
+                               uchar4 *__restrict__ out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w * h) return;
+    uint32_t x = i % w, y = i / w;
+    const float *p = xyz + ((size_t)(h - 1 - y) * w + x) * 3;
+    float X = p[0], Y = p[1], Z = p[2];
+    float r = ((X * m.m[0]) + (Y * m.m[1])) + (Z * m.m[2]);
+    float g = ((X * m.m[3]) + (Y * m.m[4])) + (Z * m.m[5]);
+    float b = ((X * m.m[6]) + (Y * m.m[7])) + (Z * m.m[8]);
+    out[i] = make_uchar4(quantize_255(srgb_gamma(r)), quantize_255(srgb_gamma(g)), quantize_255(srgb_gamma(b)), 255);
+}
+cudaError_t launch_xyz_to_srgb8(const float *xyz, uint32_t w, uint32_t h, const Mat3f &m, uint8_t *rgba,
+                                cudaStream_t st) {
+    uint32_t n = w * h;
+    if (n == 0) return cudaSuccess;
+    k_xyz_to_srgb8<<<(n + 255) / 256, 256, 0, st>>>(xyz, w, h, m, reinterpret_cast<uchar4 *>(rgba));
+    return cudaGetLastError();
+}
+
 // Host helper: set the magenta constant (rec709_to_xyz((1,0,1))) computed by
 // the host with the reference's f32 arithmetic.
 void psy_set_magenta(const float xyz[3]) {

@@ -116,5 +116,13 @@ struct WaveBufs {
 // Per-pixel XYZ (sum over samples in sample order / spp) into each segment's
 // image, out[(y * out_stride + x) * 3].  The grid covers max_pix pixels.
 cudaError_t launch_accumulate(const GScene &S, const WaveDesc *d_wave, uint32_t max_pix, PathState P, cudaStream_t st);
+// 3x3 matrix passed by value to a kernel.
+struct Mat3f {
+    float m[9];
+};
+// XYZ image (w*h*3 floats, row 0 first) -> RGBA8 sRGB, rows flipped, as the
+// reference writes PNGs; m = the XYZ -> rec709 matrix.
+cudaError_t launch_xyz_to_srgb8(const float *xyz, uint32_t w, uint32_t h, const Mat3f &m, uint8_t *rgba,
+                                cudaStream_t st);
 // Sum of per-path ray counts of a wave into *out (u64).
 cudaError_t launch_count_rays(PathState P, uint32_t n, unsigned long long *out, cudaStream_t st);

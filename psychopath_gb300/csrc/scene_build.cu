@@ -411,7 +411,8 @@ float color_energy(const PsyColor &c) {
 }
 GColor to_gcolor(const PsyColor &c) { return GColor{c.kind, c.v[0], c.v[1], c.v[2]}; }
 
-void rgb_to_xyz_matrix(double rx, double ry, double gx, double gy, double bx, double by, double wx, double wy, float out[9]) {
+static void rgb_to_xyz_matrix_f64(double rx, double ry, double gx, double gy, double bx, double by, double wx,
+                                  double wy, double m[9]) {
     double Y = 1.0;
     double X = wx * Y / wy;
     double Z = (1.0 - wx - wy) * Y / wy;
@@ -419,12 +420,60 @@ void rgb_to_xyz_matrix(double rx, double ry, double gx, double gy, double bx, do
     double sr = (X * (by - gy) - gx * (Y * (by - 1.0) + by * (X + Z)) + bx * (Y * (gy - 1.0) + gy * (X + Z))) / d;
     double sg = (X * (ry - by) + rx * (Y * (by - 1.0) + by * (X + Z)) - bx * (Y * (ry - 1.0) + ry * (X + Z))) / d;
     double sb = (X * (gy - ry) - rx * (Y * (gy - 1.0) + gy * (X + Z)) + gx * (Y * (ry - 1.0) + ry * (X + Z))) / d;
-    double m[9] = {sr * rx, sg * gx, sb * bx, sr * ry, sg * gy, sb * by, sr * (1.0 - rx - ry), sg * (1.0 - gx - gy), sb * (1.0 - bx - by)};
+    double v[9] = {sr * rx, sg * gx, sb * bx, sr * ry, sg * gy, sb * by, sr * (1.0 - rx - ry), sg * (1.0 - gx - gy), sb * (1.0 - bx - by)};
+    for (int i = 0; i < 9; i++) m[i] = v[i];
+}
+// The generated Rust source prints each coefficient with 10 decimals; the
+// f32 constant is that decimal number.
+static void round_10(const double m[9], float out[9]) {
     for (int i = 0; i < 9; i++) {
         char buf[64];
         std::snprintf(buf, sizeof(buf), "%.10f", m[i]);
         out[i] = std::strtof(buf, nullptr);
     }
+}
+void rgb_to_xyz_matrix(double rx, double ry, double gx, double gy, double bx, double by, double wx, double wy, float out[9]) {
+    double m[9];
+    rgb_to_xyz_matrix_f64(rx, ry, gx, gy, bx, by, wx, wy, m);
+    round_10(m, out);
+}
+
+// xyz_to_rec709_e: the inverse of the equal-energy rec709 matrix by
+// Gauss-Jordan elimination with partial pivoting in f64 (the color crate's
+// build script, sub_crates/color/build.rs:162-188, 246-323), then printed
+// with 10 decimals.
+void xyz_to_rec709_e_matrix(float out[9]) {
+    double e[9];
+    rgb_to_xyz_matrix_f64(0.640, 0.330, 0.300, 0.600, 0.150, 0.060, 1.0 / 3.0, 1.0 / 3.0, e);
+    double t[3][3], s[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) t[i][j] = e[i * 3 + j];
+    for (int i = 0; i < 2; i++) {
+        int pivot = i;
+        double psize = t[i][i] < 0.0 ? -t[i][i] : t[i][i];
+        for (int j = i + 1; j < 3; j++) {
+            double tmp = t[j][i] < 0.0 ? -t[j][i] : t[j][i];
+            if (tmp > psize) { pivot = j; psize = tmp; }
+        }
+        if (pivot != i)
+            for (int j = 0; j < 3; j++) { std::swap(t[i][j], t[pivot][j]); std::swap(s[i][j], s[pivot][j]); }
+        for (int j = i + 1; j < 3; j++) {
+            double f = t[j][i] / t[i][i];
+            for (int k = 0; k < 3; k++) { t[j][k] -= f * t[i][k]; s[j][k] -= f * s[i][k]; }
+        }
+    }
+    for (int i = 2; i >= 0; i--) {
+        double f = t[i][i];
+        for (int j = 0; j < 3; j++) { t[i][j] /= f; s[i][j] /= f; }
+        for (int j = 0; j < i; j++) {
+            double g = t[j][i];
+            for (int k = 0; k < 3; k++) { t[j][k] -= g * t[i][k]; s[j][k] -= g * s[i][k]; }
+        }
+    }
+    double inv[9];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) inv[i * 3 + j] = s[i][j];
+    round_10(inv, out);
 }
 
 float4 f4(float a, float b, float c, float d) { return make_float4(a, b, c, d); }

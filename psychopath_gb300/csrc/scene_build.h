@@ -53,3 +53,7 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
 // rec709_to_xyz((1, 0, 1)) in the reference's f32 arithmetic (the colour of
 // the tracer's shader for instances that have none).
 void unassigned_magenta_xyz(float out[3]);
+
+// The XYZ -> rec709 (equal-energy white) matrix of the reference's image
+// output, row-major, as f32 constants.
+void xyz_to_rec709_e_matrix(float out[9]);

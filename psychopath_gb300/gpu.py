@@ -25,6 +25,7 @@ EXPORTED = [
     "psy_rays_traced", "psy_render_bucket", "psy_render_image_device", "psy_render_image", "psy_last_error",
     "psy_version", "psy_render_bucket_noalloc", "psy_server_create", "psy_server_add_scene", "psy_submit",
     "psy_poll", "psy_wait", "psy_cancel", "psy_server_stats", "psy_server_destroy", "psy_autotune",
+    "psy_xyz_to_srgb8",
 ]
 
 
@@ -76,6 +77,7 @@ def lib(path=None):
     L.psy_server_stats.argtypes = [vp, vp]
     L.psy_server_destroy.argtypes = [vp]
     L.psy_autotune.argtypes = [vp, vp, vp]
+    L.psy_xyz_to_srgb8.argtypes = [vp, u32, u32, vp, vp]
     _lib = L
     return L
 
