@@ -438,6 +438,26 @@ void rgb_to_xyz_matrix(double rx, double ry, double gx, double gy, double bx, do
     round_10(m, out);
 }
 
+
+float4 f4(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+void push_xf(std::vector<float4> &v, const M34 &m) {
+    v.push_back(f4(m.m[0], m.m[1], m.m[2], m.m[3]));
+    v.push_back(f4(m.m[4], m.m[5], m.m[6], m.m[7]));
+    v.push_back(f4(m.m[8], m.m[9], m.m[10], m.m[11]));
+}
+
+// Round a float to f16 toward -inf / +inf.
+uint16_t f16_down(float x) {
+    __half h = __float2half_rd(x);
+    return __half_as_ushort(h);
+}
+uint16_t f16_up(float x) {
+    __half h = __float2half_ru(x);
+    return __half_as_ushort(h);
+}
+
+}  // namespace
+
 // xyz_to_rec709_e: the inverse of the equal-energy rec709 matrix by
 // Gauss-Jordan elimination with partial pivoting in f64 (the color crate's
 // build script, sub_crates/color/build.rs:162-188, 246-323), then printed
@@ -475,25 +495,6 @@ void xyz_to_rec709_e_matrix(float out[9]) {
         for (int j = 0; j < 3; j++) inv[i * 3 + j] = s[i][j];
     round_10(inv, out);
 }
-
-float4 f4(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
-void push_xf(std::vector<float4> &v, const M34 &m) {
-    v.push_back(f4(m.m[0], m.m[1], m.m[2], m.m[3]));
-    v.push_back(f4(m.m[4], m.m[5], m.m[6], m.m[7]));
-    v.push_back(f4(m.m[8], m.m[9], m.m[10], m.m[11]));
-}
-
-// Round a float to f16 toward -inf / +inf.
-uint16_t f16_down(float x) {
-    __half h = __float2half_rd(x);
-    return __half_as_ushort(h);
-}
-uint16_t f16_up(float x) {
-    __half h = __float2half_ru(x);
-    return __half_as_ushort(h);
-}
-
-}  // namespace
 
 void unassigned_magenta_xyz(float out[3]) {
     float m[9];
