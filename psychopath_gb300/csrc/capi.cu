@@ -292,6 +292,8 @@ static int trace_device_core(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyH
     if (d_full || s->trace_mode == 0)
         CK(launch_trace_rays(s->g, d_rays, n, order, d_hits, d_full, s->stack, s->minb, s->d_err, ctr, st),
            "trace launch");
+    else if (s->trace_mode == 2)
+        CK(launch_trace_packet_rays(s->g, d_rays, n, order, d_hits, s->stack, s->d_err, ctr, st), "trace launch");
     else
         CK(launch_trace_persist_rays(s->g, d_rays, n, order, d_hits, s->stack, s->minb, s->d_work, s->d_err, ctr, st),
            "trace launch");
@@ -355,6 +357,9 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
         if (ev) cudaEventRecord(ev[2 + 3 * it], st);
         if (s->trace_mode == 1)
             CK(launch_trace_persist_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, B.work, B.err, ctr, st),
+               "trace launch");
+        else if (s->trace_mode == 2)
+            CK(launch_trace_packet_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->grid, B.err, ctr, st),
                "trace launch");
         else
             CK(launch_trace_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, s->grid, B.err, ctr, st),
@@ -823,6 +828,8 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
         std::vector<TuneCfg> v;
         for (int m : {4, 5, 6, 8}) { TuneCfg c = cur; c.trace_mode = 0; c.minb = m; v.push_back(c); }
         for (int m : {4, 6, 8}) { TuneCfg c = cur; c.trace_mode = 1; c.minb = m; v.push_back(c); }
+        // warp packets (trace mode 2) are not tried: 2-7x slower on every
+        // measured workload, as one-thread-per-ray keeps more rays in flight
         try_set(v);
     }
     // 1b. shading kernel register budget
@@ -958,7 +965,7 @@ int psy_debug_counters(PsyScene *s, int enable, uint64_t *nodes, uint64_t *tris,
 // Traversal kernel choice: mode 0 = one thread per ray, 1 = persistent with
 // lane refill; minb = resident blocks per SM the register budget targets.
 int psy_debug_set_trace(PsyScene *s, int mode, int minb) {
-    if (!s || mode < 0 || mode > 1) return fail(PSY_E_INVALID, "bad trace mode");
+    if (!s || mode < 0 || mode > 2) return fail(PSY_E_INVALID, "bad trace mode");
     s->trace_mode = mode;
     // persistent kernel: 4, 6 or 8 blocks per SM; one thread per ray: 4, 5 or 6
     if (mode == 1) s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : 4);

@@ -81,6 +81,13 @@ cudaError_t launch_trace_persist_rays(const GScene &S, const PsyRay *rays, uint3
 // prec: 0 = f64 sampling arithmetic as the reference, 1 = f32.
 cudaError_t launch_camera(const GScene &S, const WaveDesc *d_wave, uint32_t max_paths, PathState P, RayBuf R,
                           uint32_t *queue, uint32_t *count, int prec, cudaStream_t st);
+// Warp-packet traversal (trace mode 2): the same hits as the per-ray kernels.
+cudaError_t launch_trace_packet_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue,
+                                      const uint32_t *count, uint32_t max_count, int stack, int grid, int *d_err,
+                                      unsigned long long *counters, cudaStream_t st);
+cudaError_t launch_trace_packet_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order,
+                                     PsyHit *hits, int stack, int *d_err, unsigned long long *counters,
+                                     cudaStream_t st);
 // Trace the queued rays of a wave.
 cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
                                uint32_t max_count, int stack, int minb, int grid, int *d_err,

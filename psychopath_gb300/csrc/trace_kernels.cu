@@ -6,6 +6,7 @@
 #include <algorithm>
 
 #include "dev_bins.cuh"
+#include "dev_packet.cuh"
 #include "dev_surface.cuh"
 #include "kernels.cuh"
 
@@ -265,6 +266,89 @@ cudaError_t launch_trace_persist_rays(const GScene &S, const PsyRay *rays, uint3
     if (n == 0) return cudaSuccess;
     IORays io{rays, n, hits, order};
     return launch_persist(S, io, n, stack, minb, work, d_err, counters, st);
+}
+
+// ------------------------------------------------------------------ warp-packet traversal
+// One warp traces 32 rays as a packet (dev_packet.cuh); the warp's stack
+// lives in shared memory.  Grid-stride over the rays in warp-sized chunks.
+template <int STACK>
+struct PacketDepth {
+    // every hit child is pushed (not count - 1 as per ray), plus octant
+    // groups at the root and at instance entry
+    static constexpr int value = 2 * STACK + 32;
+};
+template <int STACK, bool COUNT, class IO>
+__global__ void __launch_bounds__(128) k_trace_packet(GScene S, IO io, int *err, unsigned long long *counters) {
+    constexpr int DEPTH = PacketDepth<STACK>::value;
+    __shared__ uint8_t table[8 * 48];
+    __shared__ PacketEntry stk[4][DEPTH];
+    load_traversal_table(table);
+    PacketEntry *st = stk[threadIdx.x >> 5];
+    const uint32_t n = io.n();
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    TraceCount tc{0, 0};
+    uint32_t nr = 0;
+    for (uint32_t base = wid * 32; base < n; base += nw * 32) {
+        uint32_t q = base + lane;
+        bool active = q < n;
+        V3 o = v3(0.0f, 0.0f, 0.0f), d = v3(0.0f, 0.0f, 1.0f);
+        float tmax = 0.0f, time = 0.0f;
+        bool oc = false;
+        uint32_t p = 0;
+        if (active) p = io.load(q, o, d, tmax, time, oc);
+        HitRec h;
+        bool ok = trace_packet<DEPTH, COUNT>(S, table, st, active, o, d, tmax, time, oc, h, &tc);
+        if (active) {
+            if (!ok) {
+                atomicExch(err, PSY_E_OVERFLOW);
+                h.kind = PSY_HIT_MISS_K;
+            }
+            io.store(S, p, h);
+            nr++;
+        }
+    }
+    if (COUNT) {
+        unsigned long long a = tc.nodes, b = tc.tris, c = nr;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, off);
+            b += __shfl_down_sync(0xffffffffu, b, off);
+            c += __shfl_down_sync(0xffffffffu, c, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(counters, a);
+            atomicAdd(counters + 1, b);
+            atomicAdd(counters + 2, c);
+        }
+    }
+}
+
+template <class IO>
+static cudaError_t launch_packet(const GScene &S, const IO &io, uint32_t max_count, int stack, int grid, int *d_err,
+                                 unsigned long long *counters, cudaStream_t st) {
+    if (grid <= 0) grid = (int)((max_count + 127) / 128);
+    if (grid == 0) return cudaSuccess;
+#define TK(SZ, C) k_trace_packet<SZ, C, IO><<<grid, 128, 0, st>>>(S, io, d_err, counters)
+    if (stack <= 64) {
+        if (counters) TK(64, true); else TK(64, false);
+    } else {
+        if (counters) TK(192, true); else TK(192, false);
+    }
+#undef TK
+    return cudaGetLastError();
+}
+cudaError_t launch_trace_packet_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue,
+                                      const uint32_t *count, uint32_t max_count, int stack, int grid, int *d_err,
+                                      unsigned long long *counters, cudaStream_t st) {
+    IOQueue io{queue, count, R.o, R.d, R.occl, H.ki, H.tb};
+    return launch_packet(S, io, max_count, stack, grid, d_err, counters, st);
+}
+cudaError_t launch_trace_packet_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order,
+                                     PsyHit *hits, int stack, int *d_err, unsigned long long *counters,
+                                     cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    IORays io{rays, n, hits, order};
+    return launch_packet(S, io, n, stack, 0, d_err, counters, st);
 }
 
 // Queue-driven trace for the render wavefront: a grid-stride loop over the

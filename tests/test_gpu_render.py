@@ -130,3 +130,17 @@ def test_shade_register_budget_does_not_change_image(gpu_lib, minb):
         b, _ = r.render()
         assert np.array_equal(a, b)
         g.close()
+
+
+@pytest.mark.parametrize("mode,minb", [(1, 8), (2, 4)])
+def test_trace_mode_does_not_change_image(gpu_lib, mode, minb):
+    """The wavefront renders the same image with the persistent and the
+    warp-packet traversal as with one thread per ray."""
+    for s in (sc.sphere_small(24, 16, 4, 6, level=3), sc.motion_small(24, 16, 4, 2)):
+        g = gpu.Scene(s)
+        r = gpu.Renderer(g)
+        a, _ = r.render()
+        g.set_trace(mode, minb)
+        b, _ = r.render()
+        assert np.array_equal(a, b)
+        g.close()

@@ -131,10 +131,10 @@ def test_empty_batch_and_misses(gpu_lib):
     assert (h["kind"] == abi.PSY_HIT_MISS).all()
 
 
-@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 5), (0, 6), (0, 8), (1, 4), (1, 6), (1, 8)])
+@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 5), (0, 6), (0, 8), (1, 4), (1, 6), (1, 8), (2, 4)])
 def test_trace_kernel_variants_identical(gpu_lib, mode, minb):
     """Every traversal kernel variant (one thread per ray, persistent with lane
-    refill at each register budget) returns identical hits."""
+    refill at each register budget, warp packets) returns identical hits."""
     s = sc.motion_small()
     rays = sc.targeted_rays(20000, [-50, -50, -50], [50, 50, 50], [-60, -60, 60], [60, 60, 95], seed=9,
                             time_random=True)
@@ -147,7 +147,7 @@ def test_trace_kernel_variants_identical(gpu_lib, mode, minb):
     assert np.array_equal(h, ref)
 
 
-@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 8), (1, 8)])
+@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 8), (1, 8), (2, 4)])
 def test_binned_ray_order_identical(gpu_lib, mode, minb):
     """Binning a large batch by direction octant and origin cell only changes
     which thread traces which ray: hits are identical to the given order."""
@@ -169,3 +169,36 @@ def test_binned_ray_order_identical(gpu_lib, mode, minb):
     g2.set_ray_order(False)
     b, fb = gpu.Tracer(g2).trace(rays, full=True)
     assert np.array_equal(a, b) and np.array_equal(fa, fb)
+
+
+@pytest.mark.parametrize("case", ["grid", "motion", "cornell"])
+def test_warp_packets_match_per_ray(gpu_lib, case):
+    """Warp-packet traversal (octant groups per warp, split again at
+    instance entry) gives bit-identical hits to one thread per ray, with
+    mixed-octant warps, motion-blurred instances, lights and occlusion rays."""
+    if case == "grid":
+        sd, P, F = sc.grid_small(128, 64)
+        rays = np.concatenate([scenes.incoherent_rays(P, F, 20000, seed=3), scenes.coherent_rays(100)])
+    elif case == "motion":
+        sd = sc.motion_small()
+        rays = sc.targeted_rays(30000, [-50, -50, -50], [50, 50, 50], [-60, -60, 60], [60, 60, 95], seed=4,
+                                time_random=True)
+    else:
+        sd = sc.cornell()
+        rays = sc.random_rays(30000, [-1.0, 0.0, -1.0], [1.0, 2.0, 1.0], seed=5, occl_frac=0.5, max_t=1.5)
+    g = gpu.Scene(sd)
+    tr = gpu.Tracer(g)
+    g.set_trace(0, 4)
+    ref = tr.trace(rays)
+    g.set_trace(2, 4)
+    h = tr.trace(rays)
+    assert np.array_equal(h, ref)
+    g.counters(True)
+    g.set_trace(2, 4)
+    tr.trace(rays)
+    pn, pt, _ = g.counters(False)
+    g.counters(True)
+    g.set_trace(0, 4)
+    tr.trace(rays)
+    rn, rt, _ = g.counters(False)
+    assert (pn, pt) == (rn, rt)  # same node and triangle tests per ray
