@@ -13,8 +13,12 @@ lit by a sphere light and a 0.5-degree sun (GGX, roughness U(0.1, 0.8)).
 Prints one JSON line on rank 0.  --impl reference times the CPU oracle (a
 restatement of the reference's CPU renderer; the Rust binary cannot be built
 here) on all host threads, each step a bounded sample of the same frame.
-Multi-GPU: every rank renders its own full frame (weak scaling, no
-collective on the data path); value = all ranks' samples / max time.
+Multi-GPU (one process per GPU under torchrun): by default every rank
+renders its own full frame with its own seed (weak scaling, no collective on
+the data path); with --split rows the ranks render bands of one frame with
+the frame's seed and all-gather the bands once per frame (strong scaling;
+pixels identical to a 1-GPU render).  value = all ranks' samples / the
+slowest rank's time.
 """
 import argparse
 import json
@@ -50,6 +54,9 @@ def parse_args():
     ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (profiling on smaller cases)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--split", default="replicas", choices=["replicas", "rows"],
+                    help="N>1 frame workloads: 'replicas' = every rank renders its own frame (weak scaling); "
+                         "'rows' = the ranks split one frame's rows and all-gather the bands (strong scaling)")
     ap.add_argument("--form", default="both", choices=["both", "plain", "optimized"],
                     help="frame workloads: which forms to time (the headline is the optimized one)")
     ap.add_argument("--launch", default="",
@@ -203,14 +210,18 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- GPU
-def time_frames(rend, xyz, flush, stream, steps, warmup, barrier):
+def time_frames(rend, xyz, flush, stream, steps, warmup, barrier, crop=None, post=None):
     """W untimed frames, then K frames bracketed by CUDA events on the
-    render stream (L2 flushed before each).  Returns (elapsed s, summed
+    render stream (L2 flushed before each).  crop: the region this rank
+    renders; post: called after each frame inside the timed region (the
+    band all-gather of a row split).  Returns (elapsed s, summed
     traversal-kernel s, rays, samples)."""
     import torch
     sp = stream.cuda_stream
     for _ in range(warmup):
-        rend.render_device(xyz.data_ptr(), stream=sp)
+        rend.render_device(xyz.data_ptr(), stream=sp, crop=crop)
+        if post:
+            post()
     torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
@@ -219,7 +230,9 @@ def time_frames(rend, xyz, flush, stream, steps, warmup, barrier):
     ev0.record(stream)
     for _ in range(steps):
         flush.zero_()
-        st = rend.render_device(xyz.data_ptr(), stream=sp, stats=True)
+        st = rend.render_device(xyz.data_ptr(), stream=sp, stats=True, crop=crop)
+        if post:
+            post()
         trace_s += st["trace_time"]
         rays += st["ray_count"]
         samples += st["samples"]
@@ -245,10 +258,17 @@ def run_ours(args):
     from psychopath_gb300 import build, gpu
     build.build()
     sd, desc = make_scene(args)
-    sd.seed = sd.seed + rank  # independent sample sets per replica
+    rows_split = world > 1 and args.split == "rows"
+    if not rows_split:
+        sd.seed = sd.seed + rank  # independent sample sets per replica
     if args.spp:
         sd.spp = args.spp
     W, H, spp = sd.width, sd.height, sd.spp
+    crop, gather = None, None
+    if rows_split:
+        from psychopath_gb300 import multi
+        bands = multi.row_bands(H, world)
+        crop = multi.band_crop(bands[rank], W)
 
     def barrier():
         if world > 1:
@@ -262,6 +282,9 @@ def run_ours(args):
     torch.cuda.set_stream(stream)
     xyz = torch.zeros(H * W * 3, dtype=torch.float32, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    if rows_split:
+        def gather():  # one all-gather of the bands per frame (NCCL)
+            multi.gather_bands(xyz.view(H, W, 3), bands, rank, world)
 
     # plain form
     t0 = time.perf_counter()
@@ -271,7 +294,7 @@ def run_ours(args):
     p_el, p_trace, p_rays, p_samples = 1.0, 0.0, 0, 0
     if args.form == "both":
         p_el, p_trace, p_rays, p_samples = time_frames(gpu.Renderer(plain), xyz, flush, stream, args.steps,
-                                                       args.warmup, barrier)
+                                                       args.warmup, barrier, crop, gather)
         plain_img = xyz.cpu().numpy().copy()
     if args.form == "plain":
         scene = plain  # report the plain form as the line's value
@@ -300,7 +323,8 @@ def run_ours(args):
     n_nodes, n_tris, n_rays_c = scene.counters(False)
     clocks = ClockSampler(local)
     clocks.start()
-    elapsed, trace_s, rays, samples = time_frames(rend, xyz, flush, stream, args.steps, args.warmup, barrier)
+    elapsed, trace_s, rays, samples = time_frames(rend, xyz, flush, stream, args.steps, args.warmup, barrier, crop,
+                                                  gather)
     clk = clocks.stop()
     opt_img = xyz.cpu().numpy()
     rmse = None
@@ -310,11 +334,14 @@ def run_ours(args):
     if args.form == "plain":
         p_el, p_samples = elapsed, samples
     t = torch.tensor([elapsed, p_el], device="cuda")
+    tot = torch.tensor([samples, p_samples, rays, p_rays], dtype=torch.float64, device="cuda")
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.SUM)
     elapsed, p_el = float(t[0].item()), float(t[1].item())
-    value = samples * world / elapsed
-    plain_value = p_samples * world / p_el if p_samples else None
+    samples_all, p_samples_all, rays_all, p_rays_all = (float(v) for v in tot.tolist())
+    value = samples_all / elapsed
+    plain_value = p_samples_all / p_el if p_samples else None
 
     # end to end through the public C ABI with a host image buffer
     img = np.zeros((H, W, 3), dtype=np.float32)
@@ -322,12 +349,17 @@ def run_ours(args):
     torch.cuda.synchronize()
     e0 = time.perf_counter()
     for _ in range(args.steps):
-        img, _ = rend.render()
+        if rows_split:  # band on the device, all-gather, full image to the host
+            rend.render_device(xyz.data_ptr(), stream=stream.cuda_stream, crop=crop)
+            img = multi.gather_bands(xyz.view(H, W, 3), bands, rank, world).cpu().numpy()
+        else:
+            img, _ = rend.render()
     e_el = time.perf_counter() - e0
     te = torch.tensor([e_el], device="cuda")
     if world > 1:
         torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = (W * H * spp * args.steps * world) / float(te.item())
+    frames_all = args.steps * (1 if rows_split else world)
+    e2e_value = (W * H * spp * frames_all) / float(te.item())
 
     if rank != 0:
         if world > 1:
@@ -357,7 +389,8 @@ def run_ours(args):
     line = {
         "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "scaling": "strong" if rows_split else "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded procedural scene)",
         "config": {"workload": desc, "bounds": args.bounds,
                    "form": ("plain: f64 shading, default launch" if args.form == "plain" else
                             "optimized: f32 shading, %s launch" % ("fixed" if args.launch else "autotuned")),
@@ -366,9 +399,9 @@ def run_ours(args):
                    "l2": "256 MiB written between steps; path state per wave ~1.5-3 GB > L2",
                    "scene_build_s": round(build_s, 3), "scene_device_bytes": scene.device_bytes(),
                    "autotune": tune, "autotune_s": round(tune_s, 2)},
-        "mrays_per_s": rays * world / elapsed / 1e6,
+        "mrays_per_s": rays_all / elapsed / 1e6,
         "plain": ({"value": plain_value, "unit": "samples/s", "ms_per_step": p_el / args.steps * 1e3,
-                   "mrays_per_s": p_rays * world / p_el / 1e6, "trace_kernel_s_per_frame": p_trace / frames,
+                   "mrays_per_s": p_rays_all / p_el / 1e6, "trace_kernel_s_per_frame": p_trace / frames,
                    "form": "f64 shading arithmetic (reference precision), default launch configuration"}
                   if plain_value else None),
         "speedup_vs_plain": value / plain_value if plain_value else None,
