@@ -54,3 +54,39 @@ def test_gpu_conversion_matches_oracle(gpu_lib, oracle_lib):
     d = np.abs(got.astype(int) - ref.astype(int))
     assert d.max() <= 1
     assert (d > 0).mean() <= 1e-3
+
+
+def test_exr_round_trip_and_layout(tmp_path):
+    rng = np.random.default_rng(2)
+    xyz = (rng.random((5, 9, 3)) * 4.0).astype(np.float32)
+    data = image.exr_bytes(xyz)
+    # magic, version 2 (single-part scanline), then the header attributes
+    assert data[:8] == bytes([0x76, 0x2F, 0x31, 0x01, 2, 0, 0, 0])
+    for name in (b"channels\0chlist", b"compression\0compression", b"dataWindow\0box2i", b"displayWindow\0box2i",
+                 b"lineOrder\0lineOrder", b"pixelAspectRatio\0float", b"screenWindowCenter\0v2f",
+                 b"screenWindowWidth\0float"):
+        assert name in data
+    got = image.read_exr_rgb(data)
+    assert np.array_equal(got, image.xyz_to_rec709_e(xyz).astype(np.float16))
+    image.write_exr(str(tmp_path / "x.exr"), xyz)
+
+
+def test_xyz_to_rec709_e_matches_oracle_matrix(oracle_lib):
+    """The host matrix equals the oracle's (both restate the color crate's
+    generator): XYZ (1, 1, 1) maps to its rec709_e white, and the conversion
+    inverts rec709_e_to_xyz to f32 precision."""
+    from psychopath_gb300 import scenes
+    white = image.xyz_to_rec709_e(np.ones(3, dtype=np.float32))
+    assert np.allclose(white, 1.0, atol=1e-6)
+    rgb = np.array([0.2, 0.5, 0.9], dtype=np.float32)
+    back = image.xyz_to_rec709_e(scenes.rec709_e_to_xyz(rgb))
+    assert np.allclose(back, rgb, atol=1e-6)
+    # PNG path on the oracle: same matrix -> the oracle's srgb8 of a pixel
+    # equals the host conversion followed by the same gamma and quantisation
+    xyz = np.array([[[0.3, 0.4, 0.5]]], dtype=np.float32)
+    out = _oracle_srgb8(oracle_lib, xyz)[0, 0, :3]
+    lin = image.xyz_to_rec709_e(xyz)[0, 0]
+    g = np.where(lin < np.float32(0.0031308), lin * np.float32(12.92),
+                 np.float32(1.055) * np.power(lin, np.float32(1.0) / np.float32(2.4)) - np.float32(0.055))
+    q = (np.minimum(np.float32(1), np.maximum(np.float32(0), g)) * np.float32(255)).astype(np.uint8)
+    assert np.abs(q.astype(int) - out.astype(int)).max() <= 1
