@@ -373,6 +373,32 @@ DI bool slab_hit_ordered(float nxp, float fxp, float nyp, float fyp, float nzp, 
     float near_t = fmax3f(nx, ny, fmaxf(nz, 0.0f));
     return near_t < far_t;
 }
+// Packed two-lane f32 arithmetic (PTX sub.rn.f32x2 / mul.rn.f32x2): each
+// lane rounds to nearest like the scalar instruction, so results are the
+// same bits at half the instruction count.
+typedef unsigned long long f32x2;
+DI f32x2 pk2(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+DI void upk2(f32x2 v, float &a, float &b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); }
+DI f32x2 sub2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+DI f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+// (plane - o) * di for the four children of one axis, two children per
+// packed operation.
+DI void slab_axis4(float4 plane, f32x2 o2, f32x2 d2, float t[4]) {
+    upk2(mul2(sub2(pk2(plane.x, plane.y), o2), d2), t[0], t[1]);
+    upk2(mul2(sub2(pk2(plane.z, plane.w), o2), d2), t[2], t[3]);
+}
 DI bool finite3(V3 v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }
 // Inverse direction finite and nonzero in every component (so the slab
 // distances (bound - o) * di are never 0 * inf).

@@ -70,11 +70,21 @@ DI uint32_t node_hits(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, flo
         float4 nx = __ldg(bb + sx), fx = __ldg(bb + (sx ^ 1u));
         float4 ny = __ldg(bb + 2 + sy), fy = __ldg(bb + 2 + (sy ^ 1u));
         float4 nz = __ldg(bb + 4 + sz), fz = __ldg(bb + 4 + (sz ^ 1u));
+        // slab distances of all four children, two per packed operation
+        // (bit-identical to slab_hit_ordered's scalar arithmetic)
+        float tnx[4], tfx[4], tny[4], tfy[4], tnz[4], tfz[4];
+        f32x2 ox = pk2(o.x, o.x), oy = pk2(o.y, o.y), oz = pk2(o.z, o.z);
+        f32x2 dx = pk2(di.x, di.x), dy = pk2(di.y, di.y), dz = pk2(di.z, di.z);
+        slab_axis4(nx, ox, dx, tnx); slab_axis4(fx, ox, dx, tfx);
+        slab_axis4(ny, oy, dy, tny); slab_axis4(fy, oy, dy, tfy);
+        slab_axis4(nz, oz, dz, tnz); slab_axis4(fz, oz, dz, tfz);
         uint32_t m = 0;
-        m |= slab_hit_ordered(nx.x, fx.x, ny.x, fy.x, nz.x, fz.x, o, di, tmax) ? 1u : 0u;
-        m |= slab_hit_ordered(nx.y, fx.y, ny.y, fy.y, nz.y, fz.y, o, di, tmax) ? 2u : 0u;
-        m |= slab_hit_ordered(nx.z, fx.z, ny.z, fy.z, nz.z, fz.z, o, di, tmax) ? 4u : 0u;
-        m |= slab_hit_ordered(nx.w, fx.w, ny.w, fy.w, nz.w, fz.w, o, di, tmax) ? 8u : 0u;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            float far_t = fminf(fmin3f(tfx[c], tfy[c], tfz[c]) * PSY_BBOX_MAXT_ADJUST, tmax);
+            float near_t = fmax3f(tnx[c], tny[c], fmaxf(tnz[c], 0.0f));
+            m |= near_t < far_t ? (1u << c) : 0u;
+        }
         return m & ((1u << count) - 1u);
     }
     NodeBounds b;
