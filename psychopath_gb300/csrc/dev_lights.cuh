@@ -51,7 +51,7 @@ DI float sphere_sample_pdf(const GScene &S, const GLight &L, const Xf &space, V3
     R d = msqrt(d2);
     if (d > radius) {
         R st2 = mfmin((radius * radius) / d2, (R)1);
-        return (float)uniform_sample_cone_pdf<R>(msqrt((R)1 - st2));
+        return (float)cone_pdf_st2<R>(st2, msqrt((R)1 - st2));
     }
     return (float)((R)1 / ((R)4 * pi_r<R>()));
 }
@@ -131,7 +131,11 @@ DI V4 sphere_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr_w,
         R ct = msqrt(ct2);
         // uniform_sample_cone(u, v, ct), normalized
         R cone_c = ((R)1 - (R)u) + ((R)u * ct);
-        R cone_s = msqrt((R)1 - (cone_c * cone_c));
+        // in f64 cone_c <= 1 exactly (1 - u is exact); in f32 1 - u can round
+        // up, so clamp (the reference's form has nothing to clamp)
+        R sc2 = (R)1 - (cone_c * cone_c);
+        if (sizeof(R) == sizeof(float)) sc2 = mfmax(sc2, (R)0);
+        R cone_s = msqrt(sc2);
         V3 smp = normalized(v3((float)(cp * cone_s), (float)(sp * cone_s), (float)cone_c));
         R cos_theta = (R)smp.z;
         R cos_theta2 = cos_theta * cos_theta;
@@ -145,7 +149,7 @@ DI V4 sphere_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr_w,
         V3 normal = normalized(arr + svec);
         o.sp = xf_point(normal * rf, inv);
         o.sn = xf_normal(normal, inv);
-        o.pdf = (float)uniform_sample_cone_pdf<R>(ct);
+        o.pdf = (float)cone_pdf_st2<R>(st2, ct);
         return color_to_spectral(col, wl) * (float)sai;
     }
     V3 svec = uniform_sample_sphere(u, v);

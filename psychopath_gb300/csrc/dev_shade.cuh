@@ -227,6 +227,15 @@ DI V3 uniform_sample_cone(float u, float v, R cos_theta_max) {
 }
 template <class R>
 DI R uniform_sample_cone_pdf(R ctm) { return (R)1 / ((R)2 * pi_r<R>() * ((R)1 - ctm)); }
+// Cone pdf from sin^2 of the cone's half angle (st2) and its cosine (ctm)
+// for the f32 shading variant: 1 - ctm = st2 / (1 + ctm) exactly, which
+// keeps the pdf finite where 1 - st2 rounds to 1 in f32 (a small, distant
+// sphere light).  The f64 form evaluates the reference's expression.
+template <class R>
+DI R cone_pdf_st2(R st2, R ctm) {
+    if (sizeof(R) == sizeof(double)) return uniform_sample_cone_pdf<R>(ctm);
+    return ((R)1 + ctm) / ((R)2 * pi_r<R>() * st2);
+}
 DI V3 uniform_sample_triangle(V3 va, V3 vb, V3 vc, float i, float j) {
     float isqrt = sqrtf(i);
     float a = 1.0f - isqrt;

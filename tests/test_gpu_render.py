@@ -144,3 +144,18 @@ def test_trace_mode_does_not_change_image(gpu_lib, mode, minb):
         b, _ = r.render()
         assert np.array_equal(a, b)
         g.close()
+
+
+def test_f32_shading_sphere_lights(gpu_lib):
+    """The f32 variant on a motion scene lit by sphere lights (cone sampling
+    and its pdf in f32): within 1% relative RMSE of the oracle, and no
+    non-finite pixel the oracle does not also have."""
+    s = sc.motion_small(48, 27, 8, 2)
+    g = gpu.Scene(s, shading="f32")
+    img, _ = gpu.Renderer(g).render()
+    ref, _ = OracleScene(s).render(threads=8)
+    bad_g = ~np.isfinite(img).all(axis=-1)
+    bad_o = ~np.isfinite(ref).all(axis=-1)
+    assert not (bad_g & ~bad_o).any()
+    ok = ~(bad_g | bad_o)
+    assert rel_rmse(img[ok], ref[ok]) < 0.01, rel_rmse(img[ok], ref[ok])
