@@ -467,9 +467,12 @@ def run_traversal(args):
     sd, P, F = scenes.grid_mesh(2048, 1024)
     n_side = int(round(math.sqrt(args.rays)))
     sets = {"coherent": scenes.coherent_rays(n_side), "incoherent": scenes.incoherent_rays(P, F, n_side * n_side, seed=7)}
+    t0 = time.perf_counter()
     g = gpu.Scene(sd, bounds=args.bounds)
+    sah_build_s = time.perf_counter() - t0
     tr = gpu.Tracer(g)
     o = OracleScene(sd)
+    sah_hits = {}
     peaks_path = os.path.join(HERE, "MEASURED_PEAKS.json")
     peak = float(json.load(open(peaks_path))["hbm_gbs"]) if os.path.exists(peaks_path) else 6800.0
     node_bytes = 64 if args.bounds == "fp16" else 128
@@ -489,6 +492,7 @@ def run_traversal(args):
         torch.cuda.synchronize()
         gn, gt, gr = g.counters(False)
         ref_hits = d_hits.cpu().numpy()
+        sah_hits[name] = ref_hits
         # oracle on a sample: agreement and per-ray node / triangle tests
         idx = np.random.default_rng(11).choice(n, size=min(n, 200000), replace=False)
         ho, _, on, ot = o.trace(rays[idx], threads=os.cpu_count() or 1)
@@ -527,6 +531,39 @@ def run_traversal(args):
         res["best"] = best[0]
         out[name] = res
         del d_rays, d_hits
+    # the same rays against a GPU-built tree (PSY_BVH_GPU): creation time,
+    # speed with the best launch configuration, hits against the SAH tree
+    g.close()
+    t0 = time.perf_counter()
+    gb = gpu.Scene(sd, bounds=args.bounds, bvh="gpu")
+    gpu_build_s = time.perf_counter() - t0
+    trb = gpu.Tracer(gb)
+    gpu_bvh = {"create_s": round(gpu_build_s, 3), "sah_create_s": round(sah_build_s, 3), "sets": {}}
+    for name, rays in sets.items():
+        n = len(rays)
+        best = out[name]["configs"][out[name]["best"]]
+        gb.set_trace(best["trace_mode"], best["minb"])
+        gb.set_ray_order(best["binned"])
+        d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+        d_hits = torch.zeros(n * 32, dtype=torch.uint8, device="cuda")
+        for _ in range(args.warmup):
+            trb.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            trb.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3 / args.steps
+        hb = d_hits.cpu().numpy().view(abi.hit_dtype())
+        ref = sah_hits[name].view(abi.hit_dtype())
+        surf = ref["kind"] >= abi.PSY_HIT_SURFACE
+        same = (hb["kind"] == ref["kind"]) & (~surf | (hb["prim"] == ref["prim"]))
+        gpu_bvh["sets"][name] = {"launch": out[name]["best"], "mrays_per_s": n / sec / 1e6,
+                                 "hit_agreement_vs_sah": float(same.mean())}
+        del d_rays, d_hits
+    gb.close()
     inc = out["incoherent"]
     bc = inc["configs"][inc["best"]]
     line = {"metric": "Mrays/s (incoherent)", "value": bc["mrays_per_s"], "unit": "Mrays/s", "n_gpus": 1,
@@ -540,7 +577,7 @@ def run_traversal(args):
                          "frac": bc["frac"], "traffic": traversal_traffic(inc["best"], n_side * n_side),
                          "kernel": "k_trace_rays",
                          "note": "algorithmic bytes from the oracle's node / triangle tests per ray"},
-            "sets": out}
+            "sets": out, "gpu_bvh": gpu_bvh}
     print(json.dumps(line), flush=True)
 
 

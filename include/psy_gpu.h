@@ -167,11 +167,21 @@ typedef struct PsySceneDesc {
  * Hits always land at each ray's own index, so results do not change. */
 #define PSY_RAY_ORDER_AS_GIVEN 0
 #define PSY_RAY_ORDER_BINNED 1 /* calls of >= 65,536 rays: group by direction octant and origin cell first */
+/* How mesh BVHs are built.  PSY_BVH_SAH is the reference's builder
+ * (src/accel/bvh_base.rs, objects_split.rs, bvh4.rs) on the host: the same
+ * tree, so the same hits including exact ties and the same node-visit
+ * counts.  PSY_BVH_GPU builds static meshes' BVHs on the GPU (Morton codes,
+ * radix sort, binary radix tree, BVH4 collapse): a different tree, so hits
+ * agree except where two primitives tie exactly, in a fraction of the scene
+ * creation time.  Motion-blurred meshes always use the SAH build. */
+#define PSY_BVH_SAH 0
+#define PSY_BVH_GPU 1
 typedef struct PsySceneOptions {
     uint32_t bounds_precision;  /* PSY_BOUNDS_* */
     uint32_t shading_precision; /* PSY_SHADING_* */
     uint32_t ray_order;         /* PSY_RAY_ORDER_* */
-    uint32_t reserved[5];
+    uint32_t bvh_build;         /* PSY_BVH_* */
+    uint32_t reserved[4];
 } PsySceneOptions;
 
 typedef struct PsyScene PsyScene; /* opaque */

@@ -18,6 +18,7 @@ PSY_OBJ_MESH, PSY_OBJ_RECT_LIGHT, PSY_OBJ_SPHERE_LIGHT = 0, 1, 2
 PSY_BOUNDS_FP32, PSY_BOUNDS_FP16 = 0, 1
 PSY_SHADING_F64, PSY_SHADING_F32 = 0, 1
 PSY_RAY_ORDER_AS_GIVEN, PSY_RAY_ORDER_BINNED = 0, 1
+PSY_BVH_SAH, PSY_BVH_GPU = 0, 1
 PSY_RAY_OCCLUSION = 1
 PSY_NOALLOC_MAX_SAMPLES = 262144
 PSY_HIT_MISS, PSY_HIT_OCCLUDE, PSY_HIT_SURFACE, PSY_HIT_LIGHT = 0, 1, 2, 3
@@ -75,7 +76,7 @@ class PsySceneDesc(C.Structure):
 
 class PsySceneOptions(C.Structure):
     _fields_ = [("bounds_precision", C.c_uint32), ("shading_precision", C.c_uint32), ("ray_order", C.c_uint32),
-                ("reserved", C.c_uint32 * 5)]
+                ("bvh_build", C.c_uint32), ("reserved", C.c_uint32 * 4)]
 
 
 class PsyRay(C.Structure):

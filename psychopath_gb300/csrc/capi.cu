@@ -142,11 +142,23 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
     *out = nullptr;
     HostScene hs;
     std::string err;
-    int rc = build_host_scene(desc, opts, hs, err);
-    if (rc != PSY_OK) return fail(rc, err);
     int ndev = 0;
     cudaError_t ce = cudaGetDeviceCount(&ndev);
-    if (ce != cudaSuccess || ndev == 0) return fail(PSY_E_CUDA, "no CUDA device available");
+    bool have_gpu = ce == cudaSuccess && ndev > 0;
+    GpuMeshBuild gpu_build = [](const LbvhInput &in, LbvhOutput &out, std::string &e) -> int {
+        cudaStream_t bs = nullptr;
+        cudaError_t c = cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking);
+        if (c == cudaSuccess) c = lbvh_build_mesh(in, out, bs);
+        if (bs) cudaStreamDestroy(bs);
+        if (c != cudaSuccess) {
+            e = std::string("GPU BVH build: ") + cudaGetErrorString(c);
+            return c == cudaErrorMemoryAllocation ? PSY_E_NOMEM : PSY_E_CUDA;
+        }
+        return PSY_OK;
+    };
+    int rc = build_host_scene(desc, opts, hs, err, have_gpu ? &gpu_build : nullptr);
+    if (rc != PSY_OK) return fail(rc, err);
+    if (!have_gpu) return fail(PSY_E_CUDA, "no CUDA device available");
     std::call_once(g_const_once, []() {
         psy_upload_constants();
         float m[3];

@@ -503,7 +503,19 @@ void unassigned_magenta_xyz(float out[3]) {
     for (int r = 0; r < 3; r++) out[r] = ((rgb[0] * m[r * 3]) + (rgb[1] * m[r * 3 + 1])) + (rgb[2] * m[r * 3 + 2]);
 }
 
-int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostScene &hs, std::string &err) {
+// Worst-case traversal stack entries pushed below a GPU-built node (the
+// host collapse returns the same figure for its own trees).
+static uint32_t node_maxpush(const std::vector<GNode> &nodes, uint32_t base, uint32_t ref) {
+    if (psy_is_leaf(ref)) return 0;
+    const GNode &n = nodes[ref - base];
+    uint32_t cc = n.meta.z >> 8, mp = 0;
+    const uint32_t ch[4] = {n.child.x, n.child.y, n.child.z, n.child.w};
+    for (uint32_t i = 0; i < cc; i++) mp = std::max(mp, node_maxpush(nodes, base, ch[i]));
+    return mp + (cc - 1);
+}
+
+int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostScene &hs, std::string &err,
+                     const GpuMeshBuild *gpu_build) {
     if (!d) { err = "null scene description"; return PSY_E_INVALID; }
     if (d->num_objects && !d->objects) { err = "objects pointer is null"; return PSY_E_INVALID; }
     if (d->num_instances && !d->instances) { err = "instances pointer is null"; return PSY_E_INVALID; }
@@ -587,9 +599,19 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
             }
             std::vector<uint32_t> order(nt);
             for (uint32_t t = 0; t < nt; t++) order[t] = t;
+            bool on_gpu = opts && opts->bvh_build == PSY_BVH_GPU && ts == 1;
+            LbvhOutput lb;
             BoundsFn bf = [&](uint32_t t) { return Bounds{&tb[(size_t)t * ts], (size_t)ts}; };
             Base base(bf);
-            base.build(0, 0, 3, order.data(), nt);
+            if (on_gpu) {
+                if (!gpu_build) { err = "GPU BVH build needs a CUDA device"; return PSY_E_UNSUPPORTED; }
+                LbvhInput li{od.verts, nv, od.indices, nt, (uint32_t)hs.nodes.size(), (uint32_t)hs.tri_idx.size()};
+                int rc = (*gpu_build)(li, lb, err);
+                if (rc != PSY_OK) return rc;
+                order = lb.order;
+            } else {
+                base.build(0, 0, 3, order.data(), nt);
+            }
             // triangles in BVH order: (v0, v2, v1, original) as the reference's index tuples
             for (uint32_t i = 0; i < nt; i++) {
                 uint32_t t = order[i];
@@ -609,17 +631,31 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
                 }
             }
             uint32_t tri_base = gm.tri_base;
-            Collapser col{base, hs, [tri_base](uint32_t o0, uint32_t cnt) { return psy_make_leaf(tri_base + o0, cnt); }};
-            uint32_t mp;
-            gm.root = col.emit(0, &mp);
+            uint32_t mp, node_count;
+            if (on_gpu) {
+                uint32_t node_base = (uint32_t)hs.nodes.size();
+                hs.nodes.insert(hs.nodes.end(), lb.nodes.begin(), lb.nodes.end());
+                gm.root = lb.root;
+                mp = node_maxpush(hs.nodes, 0, lb.root);
+                node_count = lb.node_count;
+                // object bounds: the union of the triangle bounds
+                BB u = bb_empty();
+                for (uint32_t t = 0; t < nt; t++) u = bb_or(u, tb[t]);
+                info.bounds.assign(1, u);
+                (void)node_base;
+            } else {
+                Collapser col{base, hs, [tri_base](uint32_t o0, uint32_t cnt) { return psy_make_leaf(tri_base + o0, cnt); }};
+                gm.root = col.emit(0, &mp);
+                node_count = col.node_count;
+                const Base::Node &root = base.nodes[0];
+                info.bounds.assign(base.bounds.begin() + root.b0, base.bounds.begin() + root.b1);
+            }
             max_mesh_push = std::max(max_mesh_push, mp);
-            const Base::Node &root = base.nodes[0];
-            info.bounds.assign(base.bounds.begin() + root.b0, base.bounds.begin() + root.b1);
             info.index = (uint32_t)hs.meshes.size();
             hs.object_to_mesh[oi] = (int32_t)hs.meshes.size();
             hs.meshes.push_back(gm);
             hs.mesh_tri_order.push_back(order);
-            hs.mesh_node_count.push_back(col.node_count);
+            hs.mesh_node_count.push_back(node_count);
         } else if (od.kind == PSY_OBJ_RECT_LIGHT || od.kind == PSY_OBJ_SPHERE_LIGHT) {
             if (!od.dims || !od.colors) { err = "light without dims or colors"; return PSY_E_INVALID; }
             GLight L{};

@@ -46,9 +46,20 @@ struct HostScene {
     std::vector<int32_t> object_to_mesh;
 };
 
+#include <functional>
+
+#include "bvh_build.h"
+
+// Builds one static mesh's BVH4 on the GPU (PSY_BVH_GPU); returns PSY_OK or
+// a PSY_E_* code with a message in `err`.
+using GpuMeshBuild = std::function<int(const LbvhInput &, LbvhOutput &, std::string &)>;
+
 // Validates the description and builds the host scene.  Returns PSY_OK or a
-// PSY_E_* code with a message in `err`.
-int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostScene &hs, std::string &err);
+// PSY_E_* code with a message in `err`.  gpu_build is needed when the
+// options ask for GPU-built mesh BVHs (a host-only build then fails with
+// PSY_E_UNSUPPORTED).
+int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostScene &hs, std::string &err,
+                     const GpuMeshBuild *gpu_build = nullptr);
 
 // rec709_to_xyz((1, 0, 1)) in the reference's f32 arithmetic (the colour of
 // the tracer's shader for instances that have none).

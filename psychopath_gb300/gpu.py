@@ -104,13 +104,14 @@ def host_build_info(scene_data, obj, bounds="fp32"):
 class Scene:
     """A scene resident on the GPU (psy_scene_create)."""
 
-    def __init__(self, scene_data, bounds="fp32", shading="f64", ray_order="as_given"):
+    def __init__(self, scene_data, bounds="fp32", shading="f64", ray_order="as_given", bvh="sah"):
         self.data = scene_data
         self._desc = scene_data.desc()
         opts = abi.PsySceneOptions()
         opts.bounds_precision = abi.PSY_BOUNDS_FP16 if bounds == "fp16" else abi.PSY_BOUNDS_FP32
         opts.shading_precision = abi.PSY_SHADING_F32 if shading == "f32" else abi.PSY_SHADING_F64
         opts.ray_order = abi.PSY_RAY_ORDER_BINNED if ray_order == "binned" else abi.PSY_RAY_ORDER_AS_GIVEN
+        opts.bvh_build = abi.PSY_BVH_GPU if bvh == "gpu" else abi.PSY_BVH_SAH
         h = C.c_void_p()
         _check(lib().psy_scene_create(C.byref(self._desc), C.byref(opts), C.byref(h)))
         self.h = h

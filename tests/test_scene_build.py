@@ -41,3 +41,18 @@ def test_invalid_descriptions_rejected(gpu_lib):
     with pytest.raises(gpu.PsyError) as e:
         gpu.host_build_info(s, 0)
     assert e.value.code == abi.PSY_E_INVALID
+
+
+def test_gpu_bvh_needs_a_device(gpu_lib):
+    """The host-only build entry point rejects GPU-built BVHs cleanly."""
+    import ctypes as C
+    from psychopath_gb300 import abi
+    from . import scene_cases as sc
+    sd = sc.cornell()
+    desc = sd.desc()
+    opts = abi.PsySceneOptions()
+    opts.bvh_build = abi.PSY_BVH_GPU
+    order = np.zeros(64, dtype=np.uint32)
+    nc, ms = C.c_uint32(), C.c_uint32()
+    rc = gpu_lib.psy_debug_host_build(C.byref(desc), C.byref(opts), 0, order.ctypes.data, C.byref(nc), C.byref(ms))
+    assert rc == abi.PSY_E_UNSUPPORTED
