@@ -212,10 +212,13 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
     g.ordered_slabs = 1u;
     for (const GNode &n : hs.nodes) {
         uint32_t cnt = n.meta.z >> 8;
-        const float *lo[3] = {&n.xlo.x, &n.ylo.x, &n.zlo.x}, *hi[3] = {&n.xhi.x, &n.yhi.x, &n.zhi.x};
-        for (uint32_t c = 0; c < cnt && c < 4; c++)
-            for (int a = 0; a < 3; a++)
-                if (!(lo[a][c] <= hi[a][c])) g.ordered_slabs = 0u;
+        for (uint32_t k = 0; k < std::max(1u, n.meta.y); k++) {  // every time key of the node
+            const GBounds4 &b = k == 0 ? *reinterpret_cast<const GBounds4 *>(&n) : hs.bounds_ext[n.meta.x + k - 1];
+            const float *lo[3] = {&b.xlo.x, &b.ylo.x, &b.zlo.x}, *hi[3] = {&b.xhi.x, &b.yhi.x, &b.zhi.x};
+            for (uint32_t c = 0; c < cnt && c < 4; c++)
+                for (int a = 0; a < 3; a++)
+                    if (!(lo[a][c] <= hi[a][c])) g.ordered_slabs = 0u;
+        }
     }
     g.distant_energy_total = hs.distant_energy_total;
     g.lt_root_energy = hs.lt_root_energy;
@@ -316,6 +319,7 @@ static int trace_device_core(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyH
 int psy_trace_device(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyHit *d_hits, void *stream) {
     if (!s || (n && (!d_rays || !d_hits))) return fail(PSY_E_INVALID, "null argument");
     if (n == 0) return PSY_OK;
+    std::lock_guard<std::mutex> lk(s->mu);  // binning scratch and counters belong to the scene
     cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
     return trace_device_core(s, d_rays, n, d_hits, nullptr, st);
 }

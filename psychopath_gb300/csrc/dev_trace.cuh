@@ -63,13 +63,36 @@ DI uint32_t node_hits(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, flo
     child = __ldg(&n->child);
     code = meta.z & 0xFFu;
     count = meta.z >> 8;
-    if (safe && meta.y <= 1) {
-        // single time key: near / far planes picked by the direction's signs
-        const float4 *bb = reinterpret_cast<const float4 *>(n);  // xlo, xhi, ylo, yhi, zlo, zhi
+    if (safe) {
+        // near / far planes picked by the direction's signs; with motion
+        // keys, each plane is lerped between the two keys (a lerp of ordered
+        // boxes stays ordered: both products and the sum round monotonically)
         uint32_t sx = oct & 1u, sy = (oct >> 1) & 1u, sz = (oct >> 2) & 1u;
-        float4 nx = __ldg(bb + sx), fx = __ldg(bb + (sx ^ 1u));
-        float4 ny = __ldg(bb + 2 + sy), fy = __ldg(bb + 2 + (sy ^ 1u));
-        float4 nz = __ldg(bb + 4 + sz), fz = __ldg(bb + 4 + (sz ^ 1u));
+        float4 nx, fx, ny, fy, nz, fz;
+        auto planes = [&](const float4 *bb, float4 &px, float4 &qx, float4 &py, float4 &qy, float4 &pz, float4 &qz) {
+            px = __ldg(bb + sx); qx = __ldg(bb + (sx ^ 1u));
+            py = __ldg(bb + 2 + sy); qy = __ldg(bb + 2 + (sy ^ 1u));
+            pz = __ldg(bb + 4 + sz); qz = __ldg(bb + 4 + (sz ^ 1u));
+        };
+        auto key_ptr = [&](uint32_t k) -> const float4 * {  // xlo, xhi, ylo, yhi, zlo, zhi of key k
+            return k == 0 ? reinterpret_cast<const float4 *>(n)
+                          : reinterpret_cast<const float4 *>(S.bounds_ext + meta.x + (k - 1));
+        };
+        if (meta.y <= 1) {
+            planes(key_ptr(0), nx, fx, ny, fy, nz, fz);
+        } else {
+            uint32_t i; float a2;
+            if (lerp_index(meta.y, time, &i, &a2)) {
+                planes(key_ptr(i), nx, fx, ny, fy, nz, fz);
+            } else {
+                float4 ax, bx, ay, by, az, bz, cx, dx, cy, dy, cz, dz;
+                planes(key_ptr(i), ax, bx, ay, by, az, bz);
+                planes(key_ptr(i + 1), cx, dx, cy, dy, cz, dz);
+                nx = lerp4(ax, cx, a2); fx = lerp4(bx, dx, a2);
+                ny = lerp4(ay, cy, a2); fy = lerp4(by, dy, a2);
+                nz = lerp4(az, cz, a2); fz = lerp4(bz, dz, a2);
+            }
+        }
         // slab distances of all four children, two per packed operation
         // (bit-identical to slab_hit_ordered's scalar arithmetic)
         float tnx[4], tfx[4], tny[4], tfy[4], tnz[4], tfz[4];
