@@ -166,7 +166,7 @@ typedef struct PsySceneDesc {
 /* Order in which psy_trace / psy_trace_device traverse the rays of a call.
  * Hits always land at each ray's own index, so results do not change. */
 #define PSY_RAY_ORDER_AS_GIVEN 0
-#define PSY_RAY_ORDER_BINNED 1 /* calls of >= 65,536 rays: group by direction octant and origin cell first */
+#define PSY_RAY_ORDER_BINNED 1 /* calls of >= 65,536 rays: sort by origin and a point along the ray first */
 /* How mesh BVHs are built.  PSY_BVH_SAH is the reference's builder
  * (src/accel/bvh_base.rs, objects_split.rs, bvh4.rs) on the host: the same
  * tree, so the same hits including exact ties and the same node-visit

@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(OUT_DIR, "libpsy_gpu.so")
-SOURCES = ["kernels.cu", "trace_kernels.cu", "scene_build.cu", "capi.cu", "server.cu", "bvh_build.cu"]
+SOURCES = ["kernels.cu", "trace_kernels.cu", "scene_build.cu", "capi.cu", "server.cu", "bvh_build.cu",
+           "radix_sort.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

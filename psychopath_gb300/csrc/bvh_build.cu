@@ -17,13 +17,11 @@
 #include <vector>
 
 #include "bvh_build.h"
+#include "radix_sort.h"
 
 namespace {
 
 constexpr uint32_t kLeafBit = 0x80000000u;  // binary child reference: sorted primitive index
-constexpr int kSortThreads = 256;
-constexpr int kSortItems = 4;
-constexpr int kSortTile = kSortThreads * kSortItems;
 
 __device__ __forceinline__ uint32_t ordered_bits(float f) {
     uint32_t b = __float_as_uint(f);
@@ -86,92 +84,6 @@ __global__ void k_morton(const float4 *__restrict__ cent, uint32_t n, const uint
     }
     keys[t] = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
     vals[t] = t;
-}
-
-// ---------------------------------------------------------------- stable LSD radix sort, 8-bit digits
-// Per block: digit histogram of its tile -> hist[digit * nblocks + block].
-__global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint32_t *__restrict__ keys, uint32_t n, int shift,
-                                                            uint32_t *hist, uint32_t nblocks) {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
-    __syncthreads();
-    uint32_t base = blockIdx.x * kSortTile;
-    for (int k = 0; k < kSortItems; k++) {
-        uint32_t i = base + k * kSortThreads + threadIdx.x;
-        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
-    }
-    __syncthreads();
-    hist[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
-}
-// Exclusive prefix sum of n words in place (one block of 1024 threads).
-__global__ void __launch_bounds__(1024) k_sort_scan(uint32_t *a, uint32_t n) {
-    __shared__ uint32_t part[1024];
-    uint32_t per = (n + 1023) / 1024, t = threadIdx.x;
-    uint32_t sum = 0;
-    for (uint32_t k = 0; k < per; k++)
-        if (t * per + k < n) sum += a[t * per + k];
-    part[t] = sum;
-    __syncthreads();
-    for (uint32_t off = 1; off < 1024; off <<= 1) {
-        uint32_t v = t >= off ? part[t - off] : 0u;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
-    }
-    uint32_t run = part[t] - sum;
-    for (uint32_t k = 0; k < per; k++) {
-        if (t * per + k >= n) break;
-        uint32_t c = a[t * per + k];
-        a[t * per + k] = run;
-        run += c;
-    }
-}
-// Scatter the tile's keys to their sorted positions.  Ranks within the
-// block follow the keys' original order (rounds of 256 keys, warps in order,
-// lanes in order), so the sort is stable.
-__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t *__restrict__ keys,
-                                                               const uint32_t *__restrict__ vals, uint32_t n, int shift,
-                                                               const uint32_t *__restrict__ hist, uint32_t nblocks,
-                                                               uint32_t *__restrict__ okeys, uint32_t *__restrict__ ovals) {
-    constexpr int W = kSortThreads / 32;
-    __shared__ uint32_t cnt[W][256];
-    __shared__ uint32_t run[256];
-    __shared__ uint32_t goff[256];
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    goff[threadIdx.x] = hist[threadIdx.x * nblocks + blockIdx.x];
-    run[threadIdx.x] = 0;
-    uint32_t base = blockIdx.x * kSortTile;
-    for (int k = 0; k < kSortItems; k++) {
-        for (int w = 0; w < W; w++) cnt[w][threadIdx.x] = 0;
-        __syncthreads();
-        uint32_t i = base + k * kSortThreads + threadIdx.x;
-        bool valid = i < n;
-        uint32_t key = valid ? keys[i] : 0u, d = (key >> shift) & 255u;
-        uint32_t active = __ballot_sync(0xffffffffu, valid);
-        uint32_t peers = 0, rank = 0;
-        if (valid) {
-            peers = __match_any_sync(active, d);
-            rank = __popc(peers & ((1u << lane) - 1u));
-            if (rank == 0) cnt[warp][d] = __popc(peers);
-        }
-        __syncthreads();
-        {  // per digit: exclusive offsets over the warps of this round
-            uint32_t dg = threadIdx.x, r = run[dg];
-            for (int w = 0; w < W; w++) {
-                uint32_t c = cnt[w][dg];
-                cnt[w][dg] = r;
-                r += c;
-            }
-            run[dg] = r;
-        }
-        __syncthreads();
-        if (valid) {
-            uint32_t pos = goff[d] + cnt[warp][d] + rank;
-            okeys[pos] = key;
-            ovals[pos] = vals[i];
-        }
-        __syncthreads();
-    }
 }
 
 // ---------------------------------------------------------------- radix tree
@@ -365,8 +277,7 @@ cudaError_t lbvh_build_mesh(const LbvhInput &in, LbvhOutput &out, cudaStream_t s
     float4 *tmin = B.get<float4>(n), *tmax = B.get<float4>(n), *cent = B.get<float4>(n);
     uint32_t *gbox = B.get<uint32_t>(8), *keys = B.get<uint32_t>(n), *vals = B.get<uint32_t>(n);
     uint32_t *keys2 = B.get<uint32_t>(n), *vals2 = B.get<uint32_t>(n);
-    uint32_t nblocks = (n + kSortTile - 1) / kSortTile;
-    uint32_t *hist = B.get<uint32_t>(256 * (size_t)nblocks);
+    uint32_t *sort_scratch = B.get<uint32_t>(radix_sort_scratch_words(n));
     size_t ni = n > 1 ? n - 1 : 1;
     uint32_t *left = B.get<uint32_t>(ni), *right = B.get<uint32_t>(ni), *first = B.get<uint32_t>(ni);
     uint32_t *last = B.get<uint32_t>(ni), *parent = B.get<uint32_t>(ni), *lparent = B.get<uint32_t>(n);
@@ -388,15 +299,8 @@ cudaError_t lbvh_build_mesh(const LbvhInput &in, LbvhOutput &out, cudaStream_t s
     uint32_t g = (n + 255) / 256;
     k_prep<<<g, 256, 0, st>>>(verts, 0, idx, n, tmin, tmax, cent, gbox);
     k_morton<<<g, 256, 0, st>>>(cent, n, gbox, keys, vals);
-    uint32_t *ka = keys, *va = vals, *kb = keys2, *vb = vals2;
-    for (int shift = 0; shift < 32; shift += 8) {
-        k_sort_hist<<<nblocks, kSortThreads, 0, st>>>(ka, n, shift, hist, nblocks);
-        k_sort_scan<<<1, 1024, 0, st>>>(hist, 256 * nblocks);
-        k_sort_scatter<<<nblocks, kSortThreads, 0, st>>>(ka, va, n, shift, hist, nblocks, kb, vb);
-        std::swap(ka, kb);
-        std::swap(va, vb);
-    }
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    uint32_t *ka = nullptr, *va = nullptr;  // 30-bit Morton codes
+    if ((e = radix_sort_pairs(keys, vals, keys2, vals2, sort_scratch, n, 30, &ka, &va, st)) != cudaSuccess) return e;
     out.order.resize(n);
     if ((e = cudaMemcpyAsync(out.order.data(), va, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return e;

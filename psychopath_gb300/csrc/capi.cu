@@ -13,6 +13,7 @@
 
 #include "kernels.cuh"
 #include "scene_build.h"
+#include "radix_sort.h"
 #include "scene_handle.h"
 
 void psy_set_magenta(const float xyz[3]);
@@ -260,9 +261,7 @@ int psy_scene_destroy(PsyScene *s) {
     if (s->d_err) cudaFree(s->d_err);
     if (s->d_counters) cudaFree(s->d_counters);
     if (s->d_work) cudaFree(s->d_work);
-    if (s->d_bkeys) cudaFree(s->d_bkeys);
     if (s->d_border) cudaFree(s->d_border);
-    if (s->d_bhist) cudaFree(s->d_bhist);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return PSY_OK;
@@ -274,15 +273,14 @@ int psy_scene_device_bytes(const PsyScene *s, uint64_t *bytes) {
     return PSY_OK;
 }
 
-// Ray binning scratch for trace calls of n rays (allocated on first use).
+// Ray order scratch for trace calls of n rays (allocated on first use):
+// 4n words of keys / values plus the radix sort's scratch.
 static int ensure_binning(PsyScene *s, size_t n) {
     if (n <= s->cap_bin) return PSY_OK;
-    if (s->d_bkeys) cudaFree(s->d_bkeys);
     if (s->d_border) cudaFree(s->d_border);
-    s->d_bkeys = nullptr; s->d_border = nullptr; s->cap_bin = 0;
-    if (!s->d_bhist) CK(cudaMalloc((void **)&s->d_bhist, PSY_RAY_BINS * sizeof(uint32_t)), "cudaMalloc ray bins");
-    CK(cudaMalloc((void **)&s->d_bkeys, n * sizeof(uint32_t)), "cudaMalloc ray keys");
-    CK(cudaMalloc((void **)&s->d_border, n * sizeof(uint32_t)), "cudaMalloc ray order");
+    s->d_border = nullptr; s->cap_bin = 0;
+    size_t words = 4 * n + radix_sort_scratch_words((uint32_t)n);
+    CK(cudaMalloc((void **)&s->d_border, words * sizeof(uint32_t)), "cudaMalloc ray order");
     s->cap_bin = n;
     return PSY_OK;
 }
@@ -301,8 +299,9 @@ static int trace_device_core(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyH
     if (s->ray_order && n >= kBinMinRays) {
         int r = ensure_binning(s, n);
         if (r != PSY_OK) return r;
-        CK(launch_ray_binning(s->g, d_rays, n, s->d_bkeys, s->d_bhist, s->d_border, st), "ray binning");
-        order = s->d_border;
+        uint32_t *b = s->d_border;
+        RayOrderBufs rb{b, b + n, b + 2 * (size_t)n, b + 3 * (size_t)n, b + 4 * (size_t)n};
+        CK(launch_ray_order(s->g, d_rays, n, rb, &order, st), "ray order");
     }
     if (d_full || s->trace_mode == 0)
         CK(launch_trace_rays(s->g, d_rays, n, order, d_hits, d_full, s->stack, s->minb, s->d_err, ctr, st),
@@ -1024,6 +1023,26 @@ int psy_debug_render_sized(PsyScene *s, uint32_t width, uint32_t height, uint32_
 int psy_debug_set_ray_order(PsyScene *s, int order) {
     if (!s || order < 0 || order > 1) return fail(PSY_E_INVALID, "bad ray order");
     s->ray_order = order;
+    return PSY_OK;
+}
+// The ray order of a trace call of n device rays: d_keys receives the
+// sorted two-point keys, d_order the ray index at each position.
+int psy_debug_ray_order(PsyScene *s, const PsyRay *d_rays, uint32_t n, uint32_t *d_keys, uint32_t *d_order,
+                        void *stream) {
+    if (!s || (n && (!d_rays || !d_keys || !d_order))) return fail(PSY_E_INVALID, "null argument");
+    if (n == 0) return PSY_OK;
+    std::lock_guard<std::mutex> lk(s->mu);
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    int r = ensure_binning(s, n);
+    if (r != PSY_OK) return r;
+    uint32_t *b = s->d_border;
+    RayOrderBufs rb{b, b + n, b + 2 * (size_t)n, b + 3 * (size_t)n, b + 4 * (size_t)n};
+    const uint32_t *order = nullptr;
+    CK(launch_ray_order(s->g, d_rays, n, rb, &order, st), "ray order");
+    const uint32_t *keys = order == rb.vals ? rb.keys : rb.keys2;
+    CK(cudaMemcpyAsync(d_keys, keys, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st), "copy keys");
+    CK(cudaMemcpyAsync(d_order, order, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st), "copy order");
+    CK(cudaStreamSynchronize(st), "ray order");
     return PSY_OK;
 }
 // Replay each wave from a CUDA graph (1) or launch it kernel by kernel (0).

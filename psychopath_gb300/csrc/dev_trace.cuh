@@ -274,7 +274,8 @@ DI bool trace_ray(const GScene &S, const uint8_t *table, V3 o, V3 d, float tmax,
     const uint8_t *row = table + 48 * oct;
     // slab_safe holds for the whole ray in a space (tmax only shrinks to a finite t)
     bool safe = S.ordered_slabs && slab_safe(lo, ldi, tmax);
-    uint32_t stack[STACK];
+    // 4 spare entries take the unconditional stores of the child push
+    uint32_t stack[STACK + 4];
     int sp = 0;
     uint32_t cur = S.top_root;
     bool in_inst = false;
@@ -293,22 +294,22 @@ DI bool trace_ray(const GScene &S, const uint8_t *table, V3 o, V3 d, float tmax,
             if (COUNT) cnt->nodes++;
             if (m == 0) goto pop;
             // children in the table's visit order: push all hit children
-            // but the first, descend into the first.  The device table maps
-            // positions past the node's child count to its empty slots (never
-            // in m), so the loop has a fixed trip count.
+            // but the first, descend into the first.  Every lane stores at
+            // each of the four positions and advances the stack pointer only
+            // for hit children, so lanes with different hit masks run the
+            // same instructions.  The device table maps positions past the
+            // node's child count to its empty slots (never in m).
             uint32_t order = row[code];
             uint32_t next = PSY_REF_NONE;
+            if (sp + __popc(m) - 1 > STACK) return false;
 #pragma unroll
             for (int i = 3; i >= 0; i--) {
                 uint32_t ci = (order >> (i * 2)) & 3u;
-                if (m & (1u << ci)) {
-                    if (next != PSY_REF_NONE) {
-                        if (sp >= STACK) return false;
-                        stack[sp++] = next;
-                    }
-                    uint32_t c = ci == 0 ? ch.x : (ci == 1 ? ch.y : (ci == 2 ? ch.z : ch.w));
-                    next = c;
-                }
+                bool h = (m >> ci) & 1u;
+                uint32_t c = ci == 0 ? ch.x : (ci == 1 ? ch.y : (ci == 2 ? ch.z : ch.w));
+                stack[sp] = next;  // kept only if this child is hit and a candidate exists
+                sp += (h && next != PSY_REF_NONE) ? 1 : 0;
+                next = h ? c : next;
             }
             (void)count;
             cur = next;

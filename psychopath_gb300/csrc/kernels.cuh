@@ -62,11 +62,13 @@ void psy_upload_trace_constants(const uint8_t table[8][48], const float magenta[
 cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order, PsyHit *hits,
                               PsySurfaceHit *full, int stack, int minb, int *d_err, unsigned long long *counters,
                               cudaStream_t st);
-// Ray binning by direction octant and origin cell: keys[n], hist[PSY_RAY_BINS]
-// scratch; order[n] receives a permutation of 0..n-1 grouped by bin.
-#define PSY_RAY_BINS (1u << 18)
-cudaError_t launch_ray_binning(const GScene &S, const PsyRay *rays, uint32_t n, uint32_t *keys, uint32_t *hist,
-                               uint32_t *order, cudaStream_t st);
+// Ray order of trace calls (two-point keys, stable radix sort): n words each.
+struct RayOrderBufs {
+    uint32_t *keys, *vals, *keys2, *vals2;
+    uint32_t *scratch;  // radix_sort_scratch_words(n)
+};
+cudaError_t launch_ray_order(const GScene &S, const PsyRay *rays, uint32_t n, const RayOrderBufs &B,
+                             const uint32_t **order, cudaStream_t st);
 // Persistent traversal kernels with per-lane ray refill.  `minb` selects the
 // register budget (4 or 8 resident blocks of 128 threads per SM); `work` is a
 // device counter the launch zeroes first.

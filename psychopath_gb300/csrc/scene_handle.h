@@ -75,7 +75,7 @@ struct PsyScene {
     uint32_t wave_paths = 1u << 24;      // paths per wave
     int grid = 0;                        // persistent grid for queue kernels (0: size by queue)
     bool counting = false;               // accumulate traversal counters during renders
-    int trace_mode = 0;                  // 0: one thread per ray, 1: persistent with lane refill
+    int trace_mode = 0;                  // 0: one thread per ray, 1: persistent with lane refill, 2: warp packets
     int prec = 0;                        // shading arithmetic: 0 f64 (reference), 1 f32
     int sort_bits = 0;                   // ray binning key width between iterations (0: off)
     uint32_t *d_stage = nullptr;         // binning staging queue
@@ -89,7 +89,7 @@ struct PsyScene {
     unsigned long long *d_counters = nullptr;  // node visits, triangle tests, rays
     bool use_graph = false;              // replay each wave's launch sequence from a CUDA graph
     int ray_order = 0;                   // trace calls: 1 = bin rays by octant and origin cell first
-    uint32_t *d_bkeys = nullptr, *d_border = nullptr, *d_bhist = nullptr;  // binning scratch
+    uint32_t *d_border = nullptr;  // ray order scratch of trace calls: keys, order, second buffers, sort scratch
     size_t cap_bin = 0;
     WaveGraph graph;                     // graph of the scene's own render buffers
     std::mutex mu;

@@ -9,6 +9,7 @@
 #include "dev_packet.cuh"
 #include "dev_surface.cuh"
 #include "kernels.cuh"
+#include "radix_sort.h"
 
 using namespace psyd;
 
@@ -408,55 +409,63 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
     return cudaGetLastError();
 }
 
-// ------------------------------------------------------------------ ray binning
-// Before a large trace call, rays can be grouped so that a warp's rays start
-// near each other and point into the same octant: key = direction octant
-// (3 bits) above a 15-bit Morton code of the origin's cell in a 32^3 grid
-// over the scene box.  Binning is a counting sort over the 2^18 keys (order
-// inside a bin is arbitrary); each ray's hit is still written at its own
-// index, so results do not depend on it.
-__device__ __forceinline__ uint32_t morton5(uint32_t x, uint32_t y, uint32_t z) {
-    uint32_t m = 0;
+// ------------------------------------------------------------------ ray order
+// Before a large trace call, rays can be put in an order where a warp's rays
+// start near each other and run in similar directions.  Key: 30-bit 6-D
+// Morton code of the ray's origin and of the point at distance L along its
+// unit direction, 5 bits per coordinate over the scene box grown by L on
+// every side, L = 1/20 of the box diagonal (the "two-point" key of Meister,
+// Boksansky, Guthe and Bittner, "On Ray Reordering Techniques for Faster GPU
+// Ray Tracing", I3D 2020); then a stable radix sort of (key, ray index).
+// Each ray's hit is still written at its own index, so results do not
+// depend on the order.
+__device__ __forceinline__ uint32_t spread5_6(uint32_t v) {  // bit b -> bit 6b
+    uint32_t r = 0;
 #pragma unroll
-    for (int b = 0; b < 5; b++)
-        m |= (((x >> b) & 1u) << (3 * b)) | (((y >> b) & 1u) << (3 * b + 1)) | (((z >> b) & 1u) << (3 * b + 2));
-    return m;
+    for (int b = 0; b < 5; b++) r |= ((v >> b) & 1u) << (6 * b);
+    return r;
 }
 __device__ __forceinline__ uint32_t cell5(float v, float lo, float inv) {
     float c = (v - lo) * inv * 32.0f;
     c = fminf(fmaxf(c, 0.0f), 31.0f);  // NaN -> 0
     return (uint32_t)c;
 }
-__global__ void k_ray_keys(const PsyRay *__restrict__ rays, uint32_t n, float4 bmin, float4 binv,
-                           uint32_t *__restrict__ keys, uint32_t *__restrict__ hist) {
+__global__ void k_ray_keys(const PsyRay *__restrict__ rays, uint32_t n, float4 lo, float4 inv, float len,
+                           uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t active = __ballot_sync(0xffffffffu, i < n);
     if (i >= n) return;
     const float *r = reinterpret_cast<const float *>(rays + i);
-    uint32_t oct = (uint32_t)(r[3] < 0.0f) | ((uint32_t)(r[4] < 0.0f) << 1) | ((uint32_t)(r[5] < 0.0f) << 2);
-    uint32_t key = (oct << 15) | morton5(cell5(r[0], bmin.x, binv.x), cell5(r[1], bmin.y, binv.y),
-                                         cell5(r[2], bmin.z, binv.z));
+    float ox = r[0], oy = r[1], oz = r[2], dx = r[3], dy = r[4], dz = r[5];
+    float l2 = dx * dx + dy * dy + dz * dz;
+    float s = l2 > 0.0f ? len / sqrtf(l2) : 0.0f;
+    uint32_t c[6] = {cell5(ox, lo.x, inv.x), cell5(oy, lo.y, inv.y), cell5(oz, lo.z, inv.z),
+                     cell5(ox + dx * s, lo.x, inv.x), cell5(oy + dy * s, lo.y, inv.y), cell5(oz + dz * s, lo.z, inv.z)};
+    uint32_t key = 0;
+#pragma unroll
+    for (int k = 0; k < 6; k++) key |= spread5_6(c[k]) << k;
     keys[i] = key;
-    warp_add_key(hist, key, active);
-}
-__global__ void k_ray_scatter(const uint32_t *__restrict__ keys, uint32_t n, uint32_t *__restrict__ cursor,
-                              uint32_t *__restrict__ order) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t active = __ballot_sync(0xffffffffu, i < n);
-    if (i >= n) return;
-    order[warp_add_key(cursor, keys[i], active)] = i;
+    vals[i] = i;
 }
 
-cudaError_t launch_ray_binning(const GScene &S, const PsyRay *rays, uint32_t n, uint32_t *keys, uint32_t *hist,
-                               uint32_t *order, cudaStream_t st) {
+cudaError_t launch_ray_order(const GScene &S, const PsyRay *rays, uint32_t n, const RayOrderBufs &B,
+                             const uint32_t **order, cudaStream_t st) {
+    *order = nullptr;
     if (n == 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(hist, 0, PSY_RAY_BINS * sizeof(uint32_t), st);
-    if (e != cudaSuccess) return e;
-    uint32_t g = (n + 255) / 256;
-    k_ray_keys<<<g, 256, 0, st>>>(rays, n, S.bounds_min, S.bounds_inv_extent, keys, hist);
-    k_scan_bins<<<1, 1024, 0, st>>>(hist, PSY_RAY_BINS);
-    k_ray_scatter<<<g, 256, 0, st>>>(keys, n, hist, order);
-    return cudaGetLastError();
+    float ext[3], lo[3], d2 = 0.0f;
+    for (int a = 0; a < 3; a++) {
+        float iv = (&S.bounds_inv_extent.x)[a];
+        ext[a] = iv > 0.0f ? 1.0f / iv : 0.0f;
+        lo[a] = (&S.bounds_min.x)[a];
+        d2 += ext[a] * ext[a];
+    }
+    float len = d2 > 0.0f ? sqrtf(d2) / 20.0f : 1.0f;
+    float4 glo = make_float4(lo[0] - len, lo[1] - len, lo[2] - len, 0.0f);
+    float4 ginv = make_float4(1.0f / (ext[0] + 2.0f * len), 1.0f / (ext[1] + 2.0f * len), 1.0f / (ext[2] + 2.0f * len), 0.0f);
+    k_ray_keys<<<(n + 255) / 256, 256, 0, st>>>(rays, n, glo, ginv, len, B.keys, B.vals);
+    uint32_t *ok = nullptr, *ov = nullptr;
+    cudaError_t e = radix_sort_pairs(B.keys, B.vals, B.keys2, B.vals2, B.scratch, n, 30, &ok, &ov, st);
+    *order = ov;
+    return e;
 }
 
 // Constants of this translation unit: the child-order table and the colour

@@ -67,6 +67,7 @@ def lib(path=None):
     L.psy_debug_host_build.argtypes = [vp, vp, u32, vp, C.POINTER(u32), C.POINTER(u32)]
     L.psy_debug_set_graph.argtypes = [vp, C.c_int]
     L.psy_debug_set_ray_order.argtypes = [vp, C.c_int]
+    L.psy_debug_ray_order.argtypes = [vp, vp, u32, vp, vp, vp]
     L.psy_debug_render_sized.argtypes = [vp, u32, u32, u32, u32, vp, vp]
     L.psy_server_create.argtypes = [vp, C.POINTER(vp)]
     L.psy_server_add_scene.argtypes = [vp, vp, C.POINTER(u32)]
@@ -179,8 +180,20 @@ class Scene:
         return r.as_dict()
 
     def set_ray_order(self, binned=True):
-        """Trace calls: bin rays by direction octant and origin cell first."""
+        """Trace calls of >= 65,536 rays: sort the rays by their two-point
+        key (origin and a point along the ray) first."""
         _check(lib().psy_debug_set_ray_order(self.h, 1 if binned else 0))
+
+    def ray_order(self, rays):
+        """The order a binned trace call gives a host batch of PsyRay
+        records: (sorted keys, ray index at each position) as numpy arrays."""
+        import torch
+        n = len(rays)
+        d_rays = torch.from_numpy(np.ascontiguousarray(rays).view(np.uint8).reshape(-1)).cuda()
+        d_keys = torch.empty(n, dtype=torch.int32, device="cuda")
+        d_order = torch.empty(n, dtype=torch.int32, device="cuda")
+        _check(lib().psy_debug_ray_order(self.h, d_rays.data_ptr(), n, d_keys.data_ptr(), d_order.data_ptr(), None))
+        return d_keys.cpu().numpy().view(np.uint32), d_order.cpu().numpy().view(np.uint32)
 
     def set_graph(self, on=True):
         """Replay each render wave from a captured CUDA graph."""

@@ -149,8 +149,8 @@ def test_trace_kernel_variants_identical(gpu_lib, mode, minb):
 
 @pytest.mark.parametrize("mode,minb", [(0, 4), (0, 8), (1, 8), (2, 4)])
 def test_binned_ray_order_identical(gpu_lib, mode, minb):
-    """Binning a large batch by direction octant and origin cell only changes
-    which thread traces which ray: hits are identical to the given order."""
+    """Sorting a large batch by two-point key only changes which thread
+    traces which ray: hits are identical to the given order."""
     sd, P, F = sc.grid_small(256, 128)
     rays = np.concatenate([scenes.incoherent_rays(P, F, 1 << 16, seed=7), scenes.coherent_rays(128)])
     g = gpu.Scene(sd)
@@ -169,6 +169,29 @@ def test_binned_ray_order_identical(gpu_lib, mode, minb):
     g2.set_ray_order(False)
     b, fb = gpu.Tracer(g2).trace(rays, full=True)
     assert np.array_equal(a, b) and np.array_equal(fa, fb)
+
+
+@pytest.mark.parametrize("n", [1, 4095, 4097, 70000, 300001])
+def test_ray_order_is_a_stable_sort(gpu_lib, n):
+    """The ray order of binned trace calls: a permutation of the rays whose
+    keys are non-decreasing, equal keys in their original order (the radix
+    sort is stable); ragged sizes around the 4096-key tile."""
+    sd, P, F = sc.grid_small(64, 32)
+    rays = np.concatenate([scenes.incoherent_rays(P, F, n // 2, seed=5), scenes.coherent_rays(256)])[:n]
+    if len(rays) < n:
+        rays = np.concatenate([rays, scenes.incoherent_rays(P, F, n - len(rays), seed=6)])
+    g = gpu.Scene(sd)
+    keys, order = g.ray_order(rays)
+    assert len(order) == n
+    assert np.array_equal(np.sort(order), np.arange(n, dtype=np.uint32))
+    assert (keys < (1 << 30)).all() and (np.diff(keys.astype(np.int64)) >= 0).all()
+    tie = np.diff(keys.astype(np.int64)) == 0
+    assert (np.diff(order.astype(np.int64))[tie] > 0).all()
+    # a batch whose rays all share one key keeps the given order
+    same = np.repeat(rays[:1], min(n, 5000))
+    k2, o2 = g.ray_order(same)
+    assert (k2 == k2[0]).all() and np.array_equal(o2, np.arange(len(same), dtype=np.uint32))
+    g.close()
 
 
 @pytest.mark.parametrize("case", ["grid", "motion", "cornell"])
