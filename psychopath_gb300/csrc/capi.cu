@@ -61,7 +61,7 @@ static void free_render(PsyScene *s) {
     s->graph.reset();
     void *ptrs[] = {s->P.color, s->P.latt, s->P.pending, s->P.nafac, s->P.nb_o, s->P.nb_d, s->P.tw, s->P.seed, s->P.flags,
                     s->R.o, s->R.d, s->R.occl, s->H.ki, s->H.tb, s->queue[0], s->queue[1], s->counts, s->d_raycount,
-                    s->d_stage, s->d_stage_key, s->d_bins, s->d_waves};
+                    s->d_stage, s->d_stage_key, s->d_bins, s->d_qradix, s->d_waves};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     s->P = PathState{};
@@ -73,6 +73,7 @@ static void free_render(PsyScene *s) {
     s->d_stage = nullptr;
     s->d_stage_key = nullptr;
     s->d_bins = nullptr;
+    s->d_qradix = nullptr;
     s->d_waves = nullptr;
     s->cap_waves = 0;
     s->cap_paths = 0;
@@ -91,6 +92,7 @@ static int ensure_render(PsyScene *s, uint32_t n) {
     AL(s->counts, 16);
     AL(s->d_raycount, 8);
     AL(s->d_stage, N * 4); AL(s->d_stage_key, N * 2); AL(s->d_bins, 65536 * 4);
+    AL(s->d_qradix, queue_radix_words(n) * 4);
 #undef AL
     s->cap_paths = n;
     return PSY_OK;
@@ -359,7 +361,7 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
                 cudaStream_t st, unsigned long long *ctr, const cudaEvent_t *ev) {
     uint32_t iters = 2 * s->g.max_bounces + 3;
     uint32_t n = max_paths;
-    bool binning = s->sort_bits > 0 && B.stage;
+    bool binning = s->sort_bits > 0 && B.stage && (s->sort_bits <= 16 || B.qradix);
     if (ev) cudaEventRecord(ev[0], st);
     CK(launch_camera(s->g, d_wave, n, B.P, B.R, B.queue[0], B.counts, s->prec, st), "camera launch");
     if (ev) cudaEventRecord(ev[1], st);
@@ -386,8 +388,12 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
         CK(launch_shade(s->g, d_wave, B.P, B.R, B.H, qin, cin, n, qout, cout, s->shade_minb, s->grid, s->prec, st),
            "shade launch");
         if (binning && it + 1 < iters) {
-            CK(launch_queue_binning(s->g, B.R, qout, cout, n, s->sort_bits, B.stage_key, B.bins, B.stage,
-                                    B.counts + 2, st),
+            QueueSortBufs Q{B.stage_key, B.bins, nullptr, nullptr, nullptr, nullptr};
+            if (B.qradix) {
+                Q.keys = B.qradix; Q.keys2 = B.qradix + B.cap; Q.vals2 = B.qradix + 2 * (size_t)B.cap;
+                Q.scratch = B.qradix + 3 * (size_t)B.cap;
+            }
+            CK(launch_queue_binning(s->g, B.R, qout, cout, n, s->sort_bits, Q, B.stage, B.counts + 2, st),
                "queue binning");
             qin = B.stage;
             cin = B.counts + 2;
@@ -463,6 +469,7 @@ int alloc_wave_bufs(WaveBufs &B, uint32_t cap, uint32_t cap_waves, bool sorting,
     al(&ctrl, 1024);
     if (sorting) {
         al(&B.stage, N * 4); al(&B.stage_key, N * 2); al(&B.bins, 65536 * 4);
+        al(&B.qradix, queue_radix_words(cap) * 4);
     }
     al(&B.waves, (size_t)cap_waves * sizeof(WaveDesc));
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc wave buffers");
@@ -582,7 +589,7 @@ static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint
     B.counts = s->counts;
     B.work = s->d_work;
     B.err = s->d_err;
-    B.stage = s->d_stage; B.stage_key = s->d_stage_key; B.bins = s->d_bins;
+    B.stage = s->d_stage; B.stage_key = s->d_stage_key; B.bins = s->d_bins; B.qradix = s->d_qradix;
     B.cap = s->cap_paths;
     uint32_t nwaves = (h + rows - 1) / rows + 1;  // + the graph's descriptor slot
     if (nwaves > s->cap_waves) {
@@ -671,7 +678,7 @@ extern "C" int psy_render_bucket_noalloc(PsyScene *s, const PsyBucket *b, uint32
     B.counts = (uint32_t *)ctrl;            // [2]
     B.work = (uint32_t *)(ctrl + 256);      // persistent-kernel work counter
     B.err = (int *)(ctrl + 512);            // device error word
-    B.stage = nullptr; B.stage_key = nullptr; B.bins = nullptr;
+    B.stage = nullptr; B.stage_key = nullptr; B.bins = nullptr; B.qradix = nullptr;
     B.cap = (uint32_t)C;
     B.waves = (WaveDesc *)take(sizeof(WaveDesc));  // the bucket is one wave
     B.cap_waves = 1;
@@ -872,7 +879,7 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
     // 4. ray-sort key width
     {
         std::vector<TuneCfg> v;
-        for (int b : {0, 4, 10, 13, 16}) { TuneCfg c = cur; c.sort_bits = b; if (b != cur.sort_bits) v.push_back(c); }
+        for (int b : {0, 4, 10, 13, 16, 19, 25}) { TuneCfg c = cur; c.sort_bits = b; if (b != cur.sort_bits) v.push_back(c); }
         try_set(v);
     }
     // 5. wave size
@@ -993,9 +1000,12 @@ int psy_debug_set_shade(PsyScene *s, int minb) {
     s->shade_minb = minb;
     return PSY_OK;
 }
-// Queue binning key width between wavefront iterations: 0 (off), 4, 10, 13, 16.
+// Queue binning key width between wavefront iterations: 0 (off), 4, 10, 13, 16
+// (counting sort), 19, 25, 31 (two-point keys, radix sort).
 int psy_debug_set_sort(PsyScene *s, int bits) {
-    if (!s || !(bits == 0 || bits == 4 || bits == 10 || bits == 13 || bits == 16)) return fail(PSY_E_INVALID, "bad sort bits");
+    if (!s || !(bits == 0 || bits == 4 || bits == 10 || bits == 13 || bits == 16 || bits == 19 || bits == 25 ||
+                bits == 31))
+        return fail(PSY_E_INVALID, "bad sort bits");
     s->sort_bits = bits;
     return PSY_OK;
 }

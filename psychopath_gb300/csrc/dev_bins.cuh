@@ -39,3 +39,26 @@ static __global__ void __launch_bounds__(1024) k_scan_bins(uint32_t *hist, uint3
         run += c;
     }
 }
+
+// Two-point sort key of a ray: 6-D Morton code of the ray's origin and of
+// the point at distance len along its unit direction, p bits per coordinate
+// over the box (lo, 1 / extent) (bit b of coordinate k at bit 6b + k).
+__device__ __forceinline__ uint32_t tp_cell(float v, float lo, float inv, float cells) {
+    float c = (v - lo) * inv * cells;
+    c = fminf(fmaxf(c, 0.0f), cells - 1.0f);  // NaN -> 0
+    return (uint32_t)c;
+}
+__device__ __forceinline__ uint32_t two_point_key(float ox, float oy, float oz, float dx, float dy, float dz, float4 lo,
+                                                  float4 inv, float len, int p) {
+    const float cells = (float)(1u << p);
+    float l2 = dx * dx + dy * dy + dz * dz;
+    float s = l2 > 0.0f ? len / sqrtf(l2) : 0.0f;
+    uint32_t c[6] = {tp_cell(ox, lo.x, inv.x, cells), tp_cell(oy, lo.y, inv.y, cells), tp_cell(oz, lo.z, inv.z, cells),
+                     tp_cell(ox + dx * s, lo.x, inv.x, cells), tp_cell(oy + dy * s, lo.y, inv.y, cells),
+                     tp_cell(oz + dz * s, lo.z, inv.z, cells)};
+    uint32_t key = 0;
+    for (int b = 0; b < p; b++)
+#pragma unroll
+        for (int k = 0; k < 6; k++) key |= ((c[k] >> b) & 1u) << (6 * b + k);
+    return key;
+}

@@ -7,6 +7,7 @@
 #include "dev_bins.cuh"
 #include "dev_surface.cuh"
 #include "kernels.cuh"
+#include "radix_sort.h"
 
 using namespace psyd;
 
@@ -368,7 +369,9 @@ cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, R
 // octant: key = occlusion flag, direction octant, then a Morton code of the
 // origin's cell (k bits per axis of the scene box), `bits` = 4 + 3k bits in
 // all.  A counting sort (order inside a bin arbitrary); paths are
-// independent, so the image does not change.
+// independent, so the image does not change.  Wider keys (19, 25, 31 bits)
+// use the two-point key of the trace calls' ray order and a stable radix
+// sort (radix_sort.cu).
 __device__ __forceinline__ uint32_t queue_key(const GScene &S, float4 o, float4 d, bool occl, int bits) {
     uint32_t key = (occl ? 1u : 0u) | (ray_code(v3(d)) << 1);
     int per = (bits - 4) / 3;
@@ -412,17 +415,46 @@ __global__ void k_queue_scatter(const uint32_t *__restrict__ queue, const uint32
     }
 }
 
+// Two-point keys (occlusion flag above a 6p-bit key) and the path indices.
+__global__ void k_queue_tp_keys(RayBuf R, const uint32_t *__restrict__ queue, const uint32_t *__restrict__ count,
+                                float4 lo, float4 inv, float len, int p, uint32_t *__restrict__ keys,
+                                uint32_t *__restrict__ vals) {
+    uint32_t n = *count;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        uint32_t path = queue[q];
+        float4 o = R.o[path], d = R.d[path];
+        uint32_t key = two_point_key(o.x, o.y, o.z, d.x, d.y, d.z, lo, inv, len, p);
+        keys[q] = key | ((R.occl[path] != 0 ? 1u : 0u) << (6 * p));
+        vals[q] = path;
+    }
+}
+
+size_t queue_radix_words(uint32_t n) { return 3 * (size_t)n + radix_sort_scratch_words(n); }
+
 cudaError_t launch_queue_binning(const GScene &S, RayBuf R, const uint32_t *queue, const uint32_t *count,
-                                 uint32_t max_count, int bits, uint16_t *keys, uint32_t *hist, uint32_t *out,
+                                 uint32_t max_count, int bits, const QueueSortBufs &Q, uint32_t *out,
                                  uint32_t *out_count, cudaStream_t st) {
-    uint32_t nbins = 1u << bits;
-    cudaError_t e = cudaMemsetAsync(hist, 0, nbins * sizeof(uint32_t), st);
-    if (e != cudaSuccess) return e;
     int g = (int)std::min<uint32_t>((max_count + 255) / 256, 152u * 16u);
     if (g < 1) g = 1;
-    k_queue_keys<<<g, 256, 0, st>>>(S, R, queue, count, bits, keys, hist);
-    k_scan_bins<<<1, 1024, 0, st>>>(hist, nbins);
-    k_queue_scatter<<<g, 256, 0, st>>>(queue, count, keys, hist, out, out_count);
+    if (bits > 16) {
+        // the radix passes alternate buffers: start where the last pass
+        // lands in `out`
+        const int p = (bits - 1) / 6, passes = (bits + 7) / 8;
+        uint32_t *vals = (passes & 1) ? Q.vals2 : out, *vals2 = (passes & 1) ? out : Q.vals2;
+        float4 lo, inv;
+        float len;
+        two_point_box(S, lo, inv, len);
+        k_queue_tp_keys<<<g, 256, 0, st>>>(R, queue, count, lo, inv, len, p, Q.keys, vals);
+        cudaError_t e = radix_sort_pairs_dev(Q.keys, vals, Q.keys2, vals2, Q.scratch, count, max_count, bits, st);
+        if (e != cudaSuccess) return e;
+        return cudaMemcpyAsync(out_count, count, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+    }
+    uint32_t nbins = 1u << bits;
+    cudaError_t e = cudaMemsetAsync(Q.bins, 0, nbins * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    k_queue_keys<<<g, 256, 0, st>>>(S, R, queue, count, bits, Q.keys16, Q.bins);
+    k_scan_bins<<<1, 1024, 0, st>>>(Q.bins, nbins);
+    k_queue_scatter<<<g, 256, 0, st>>>(queue, count, Q.keys16, Q.bins, out, out_count);
     return cudaGetLastError();
 }
 

@@ -62,6 +62,19 @@ void psy_upload_trace_constants(const uint8_t table[8][48], const float magenta[
 cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order, PsyHit *hits,
                               PsySurfaceHit *full, int stack, int minb, int *d_err, unsigned long long *counters,
                               cudaStream_t st);
+// Box of the two-point sort keys: the scene box grown on every side by the
+// key length len = 1/20 of the scene box diagonal.
+inline void two_point_box(const GScene &S, float4 &lo, float4 &inv, float &len) {
+    float ext[3], d2 = 0.0f;
+    for (int a = 0; a < 3; a++) {
+        float iv = (&S.bounds_inv_extent.x)[a];
+        ext[a] = iv > 0.0f ? 1.0f / iv : 0.0f;
+        d2 += ext[a] * ext[a];
+    }
+    len = d2 > 0.0f ? sqrtf(d2) / 20.0f : 1.0f;
+    lo = make_float4(S.bounds_min.x - len, S.bounds_min.y - len, S.bounds_min.z - len, 0.0f);
+    inv = make_float4(1.0f / (ext[0] + 2.0f * len), 1.0f / (ext[1] + 2.0f * len), 1.0f / (ext[2] + 2.0f * len), 0.0f);
+}
 // Ray order of trace calls (two-point keys, stable radix sort): n words each.
 struct RayOrderBufs {
     uint32_t *keys, *vals, *keys2, *vals2;
@@ -99,12 +112,24 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                          const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
                          int minb, int grid, int prec, cudaStream_t st);
-// Groups the live paths of queue[0 .. *count) by their next ray (occlusion
-// flag, direction octant, origin cell; `bits` = 4, 10, 13 or 16) into
-// out[0 .. n) and sets *out_count = n.  keys: max_count u16; hist: 2^bits u32.
+// Scratch of the queue ordering: u16 keys and 2^16 counters (bins) for the
+// counting sort, u32 keys / second buffers / radix scratch for the radix
+// sort (null when absent).
+struct QueueSortBufs {
+    uint16_t *keys16;
+    uint32_t *bins;
+    uint32_t *keys, *keys2, *vals2, *scratch;
+};
+// Groups the live paths of queue[0 .. *count) by their next ray into
+// out[0 .. n) and sets *out_count = n.  bits 4, 10, 13, 16: counting sort by
+// occlusion flag, direction octant, origin cell (bits = 4 + 3k); bits 19,
+// 25, 31: stable radix sort by occlusion flag above a two-point key of
+// (bits - 1) / 6 bits per coordinate.
 cudaError_t launch_queue_binning(const GScene &S, RayBuf R, const uint32_t *queue, const uint32_t *count,
-                                 uint32_t max_count, int bits, uint16_t *keys, uint32_t *hist, uint32_t *out,
+                                 uint32_t max_count, int bits, const QueueSortBufs &Q, uint32_t *out,
                                  uint32_t *out_count, cudaStream_t st);
+// Words of QueueSortBufs' radix part (keys, keys2, vals2, scratch) for n paths.
+size_t queue_radix_words(uint32_t n);
 // All device buffers one render wave needs (owned by a scene, or carved from
 // a static scratch array by the no-allocation entry point).
 struct WaveBufs {
@@ -118,6 +143,7 @@ struct WaveBufs {
     uint32_t *stage;       // binned queue (may be null: no binning)
     uint16_t *stage_key;   // binning keys
     uint32_t *bins;        // 2^16 bin counters
+    uint32_t *qradix;      // radix ordering scratch, queue_radix_words(cap) (may be null)
     uint32_t cap;          // paths per wave
     WaveDesc *waves;       // wave descriptors (device)
     uint32_t cap_waves;

@@ -23,8 +23,10 @@ constexpr int kWarps = kThreads / 32;
 
 uint32_t tiles(uint32_t n) { return (n + kTile - 1) / kTile; }
 
-__global__ void __launch_bounds__(kThreads) k_rs_count(const uint32_t *__restrict__ keys, uint32_t n, int shift,
+__global__ void __launch_bounds__(kThreads) k_rs_count(const uint32_t *__restrict__ keys, uint32_t n_host,
+                                                       const uint32_t *__restrict__ n_dev, int shift,
                                                        uint32_t *__restrict__ counts, uint32_t ntiles) {
+    const uint32_t n = n_dev ? *n_dev : n_host;
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -82,10 +84,13 @@ __global__ void __launch_bounds__(1024) k_rs_rows(uint32_t *__restrict__ counts,
 }
 
 __global__ void __launch_bounds__(kThreads) k_rs_scatter(const uint32_t *__restrict__ keys,
-                                                         const uint32_t *__restrict__ vals, uint32_t n, int shift,
+                                                         const uint32_t *__restrict__ vals, uint32_t n_host,
+                                                         const uint32_t *__restrict__ n_dev, int shift,
                                                          const uint32_t *__restrict__ counts, uint32_t ntiles,
                                                          const uint32_t *__restrict__ tot, uint32_t *__restrict__ okeys,
                                                          uint32_t *__restrict__ ovals) {
+    const uint32_t n = n_dev ? *n_dev : n_host;
+    if (blockIdx.x * kTile >= n) return;  // a tile past the device-side count (whole block)
     __shared__ uint32_t cnt[kWarps][256];  // per warp: digit counts, then the warp's offsets in the tile
     __shared__ uint32_t goff[256];         // global position of the tile's first key of each digit
     __shared__ uint32_t tstart[256];       // tile position of the first key of each digit
@@ -169,14 +174,30 @@ cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys2, ui
         const uint32_t nt = tiles(n);
         uint32_t *counts = scratch, *tot = scratch + 256 * (size_t)nt;
         for (int shift = 0; shift < bits; shift += 8) {
-            k_rs_count<<<nt, kThreads, 0, st>>>(ka, n, shift, counts, nt);
+            k_rs_count<<<nt, kThreads, 0, st>>>(ka, n, nullptr, shift, counts, nt);
             k_rs_rows<<<256, 1024, 0, st>>>(counts, nt, tot);
-            k_rs_scatter<<<nt, kThreads, 0, st>>>(ka, va, n, shift, counts, nt, tot, kb, vb);
+            k_rs_scatter<<<nt, kThreads, 0, st>>>(ka, va, n, nullptr, shift, counts, nt, tot, kb, vb);
             std::swap(ka, kb);
             std::swap(va, vb);
         }
     }
     *out_keys = ka;
     *out_vals = va;
+    return cudaGetLastError();
+}
+
+cudaError_t radix_sort_pairs_dev(uint32_t *keys, uint32_t *vals, uint32_t *keys2, uint32_t *vals2, uint32_t *scratch,
+                                 const uint32_t *d_n, uint32_t max_n, int bits, cudaStream_t st) {
+    if (max_n == 0) return cudaSuccess;
+    uint32_t *ka = keys, *va = vals, *kb = keys2, *vb = vals2;
+    const uint32_t nt = tiles(max_n);
+    uint32_t *counts = scratch, *tot = scratch + 256 * (size_t)nt;
+    for (int shift = 0; shift < bits; shift += 8) {
+        k_rs_count<<<nt, kThreads, 0, st>>>(ka, 0, d_n, shift, counts, nt);
+        k_rs_rows<<<256, 1024, 0, st>>>(counts, nt, tot);
+        k_rs_scatter<<<nt, kThreads, 0, st>>>(ka, va, 0, d_n, shift, counts, nt, tot, kb, vb);
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
     return cudaGetLastError();
 }

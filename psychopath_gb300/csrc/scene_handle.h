@@ -81,6 +81,7 @@ struct PsyScene {
     uint32_t *d_stage = nullptr;         // binning staging queue
     uint16_t *d_stage_key = nullptr;
     uint32_t *d_bins = nullptr;
+    uint32_t *d_qradix = nullptr;        // radix queue ordering scratch (queue_radix_words)
     WaveDesc *d_waves = nullptr;         // wave descriptors of one render call
     uint32_t cap_waves = 0;
     int minb = 4;                        // trace kernel register budget (target resident blocks per SM)

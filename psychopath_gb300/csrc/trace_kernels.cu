@@ -419,31 +419,12 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
 // Ray Tracing", I3D 2020); then a stable radix sort of (key, ray index).
 // Each ray's hit is still written at its own index, so results do not
 // depend on the order.
-__device__ __forceinline__ uint32_t spread5_6(uint32_t v) {  // bit b -> bit 6b
-    uint32_t r = 0;
-#pragma unroll
-    for (int b = 0; b < 5; b++) r |= ((v >> b) & 1u) << (6 * b);
-    return r;
-}
-__device__ __forceinline__ uint32_t cell5(float v, float lo, float inv) {
-    float c = (v - lo) * inv * 32.0f;
-    c = fminf(fmaxf(c, 0.0f), 31.0f);  // NaN -> 0
-    return (uint32_t)c;
-}
 __global__ void k_ray_keys(const PsyRay *__restrict__ rays, uint32_t n, float4 lo, float4 inv, float len,
                            uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float *r = reinterpret_cast<const float *>(rays + i);
-    float ox = r[0], oy = r[1], oz = r[2], dx = r[3], dy = r[4], dz = r[5];
-    float l2 = dx * dx + dy * dy + dz * dz;
-    float s = l2 > 0.0f ? len / sqrtf(l2) : 0.0f;
-    uint32_t c[6] = {cell5(ox, lo.x, inv.x), cell5(oy, lo.y, inv.y), cell5(oz, lo.z, inv.z),
-                     cell5(ox + dx * s, lo.x, inv.x), cell5(oy + dy * s, lo.y, inv.y), cell5(oz + dz * s, lo.z, inv.z)};
-    uint32_t key = 0;
-#pragma unroll
-    for (int k = 0; k < 6; k++) key |= spread5_6(c[k]) << k;
-    keys[i] = key;
+    keys[i] = two_point_key(r[0], r[1], r[2], r[3], r[4], r[5], lo, inv, len, 5);
     vals[i] = i;
 }
 
@@ -451,16 +432,9 @@ cudaError_t launch_ray_order(const GScene &S, const PsyRay *rays, uint32_t n, co
                              const uint32_t **order, cudaStream_t st) {
     *order = nullptr;
     if (n == 0) return cudaSuccess;
-    float ext[3], lo[3], d2 = 0.0f;
-    for (int a = 0; a < 3; a++) {
-        float iv = (&S.bounds_inv_extent.x)[a];
-        ext[a] = iv > 0.0f ? 1.0f / iv : 0.0f;
-        lo[a] = (&S.bounds_min.x)[a];
-        d2 += ext[a] * ext[a];
-    }
-    float len = d2 > 0.0f ? sqrtf(d2) / 20.0f : 1.0f;
-    float4 glo = make_float4(lo[0] - len, lo[1] - len, lo[2] - len, 0.0f);
-    float4 ginv = make_float4(1.0f / (ext[0] + 2.0f * len), 1.0f / (ext[1] + 2.0f * len), 1.0f / (ext[2] + 2.0f * len), 0.0f);
+    float4 glo, ginv;
+    float len;
+    two_point_box(S, glo, ginv, len);
     k_ray_keys<<<(n + 255) / 256, 256, 0, st>>>(rays, n, glo, ginv, len, B.keys, B.vals);
     uint32_t *ok = nullptr, *ov = nullptr;
     cudaError_t e = radix_sort_pairs(B.keys, B.vals, B.keys2, B.vals2, B.scratch, n, 30, &ok, &ov, st);

@@ -91,7 +91,7 @@ def test_paths_match_oracle_samples(gpu_lib):
     assert rel_rmse(img, ref[8:16, 8:16]) < 0.02
 
 
-@pytest.mark.parametrize("bits", [4, 10, 13, 16])
+@pytest.mark.parametrize("bits", [4, 10, 13, 16, 19, 25, 31])
 def test_ray_binning_does_not_change_image(gpu_lib, bits):
     """Binning the wavefront queue by ray key only reorders independent
     paths: the image is bit-identical to the unbinned one."""
@@ -103,6 +103,26 @@ def test_ray_binning_does_not_change_image(gpu_lib, bits):
     g.set_sort(bits)
     b, _ = r.render()
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_radix_queue_order_many_tiles(gpu_lib, graph):
+    """Two-point radix ordering of the wavefront queues over many sort tiles
+    (~98k paths, the queue length read on the device), launched kernel by
+    kernel and replayed from a CUDA graph: bit-identical image."""
+    import torch
+    s = sc.sphere_small(128, 96, 8, 6, level=3)
+    g = gpu.Scene(s)
+    r = gpu.Renderer(g)
+    g.set_sort(0)
+    a, _ = r.render()
+    g.set_graph(graph)
+    d = torch.zeros(s.height * s.width * 3, dtype=torch.float32, device="cuda")
+    for bits in (19, 25):
+        g.set_sort(bits)
+        r.render_device(d.data_ptr())  # no stats: the graph path when enabled
+        torch.cuda.synchronize()
+        assert np.array_equal(a, d.cpu().numpy().reshape(a.shape))
 
 
 def test_f32_shading_precision_error(gpu_lib):
