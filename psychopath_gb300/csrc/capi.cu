@@ -833,16 +833,23 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
     double best = 0, t = 0;
     err = measure(cur, best);
     double default_s = best;
+    // the fastest candidate of a set replaces the current choice when it
+    // beats it by 2%: differences inside the run-to-run noise keep the
+    // earlier (simpler) choice, and the order of the set does not matter
     auto try_set = [&](std::vector<TuneCfg> cands) {
+        double set_best = best;
+        TuneCfg set_cfg_best = cur;
         for (const TuneCfg &c : cands) {
             if (err != PSY_OK) return;
             err = measure(c, t);
-            // a candidate must beat the current choice by 2%: differences
-            // inside the run-to-run noise keep the earlier (simpler) choice
-            if (err == PSY_OK && t < 0.98 * best) {
-                best = t;
-                cur = c;
+            if (err == PSY_OK && t < set_best) {
+                set_best = t;
+                set_cfg_best = c;
             }
+        }
+        if (err == PSY_OK && set_best < 0.98 * best) {
+            best = set_best;
+            cur = set_cfg_best;
         }
     };
     // 1. trace kernel and register budget
