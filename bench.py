@@ -479,7 +479,8 @@ def run_traversal(args):
     stream = torch.cuda.Stream()  # non-null handle: kernels and events on one stream
     torch.cuda.set_stream(stream)
     configs = [("plain", 0, 4, False), ("minb8", 0, 8, False), ("minb8+binned", 0, 8, True),
-               ("persistent8+binned", 1, 8, True)]
+               ("persistent8+binned", 1, 8, True), ("static8", 3, 8, False), ("static8+binned", 3, 8, True),
+               ("static10+binned", 3, 10, True), ("static12+binned", 3, 12, True), ("static6+binned", 3, 6, True)]
     out = {}
     for name, rays in sets.items():
         n = len(rays)

@@ -223,6 +223,15 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
                     if (!(lo[a][c] <= hi[a][c])) g.ordered_slabs = 0u;
         }
     }
+    // the static-scene traversal: FP32 nodes without motion keys, ordered
+    // boxes, static meshes, untransformed mesh instances
+    g.static_fast = (g.use_fp16 == 0u && g.ordered_slabs == 1u) ? 1u : 0u;
+    for (const GNode &n : hs.nodes)
+        if (n.meta.y > 1) g.static_fast = 0u;
+    for (const GMesh &m : hs.meshes)
+        if (m.ts != 1) g.static_fast = 0u;
+    for (const GInstance &in : hs.instances)
+        if (in.kind == PSY_INST_MESH && in.xc != 0) g.static_fast = 0u;
     g.distant_energy_total = hs.distant_energy_total;
     g.lt_root_energy = hs.lt_root_energy;
     for (int a = 0; a < 3; a++) {
@@ -305,8 +314,9 @@ static int trace_device_core(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyH
         RayOrderBufs rb{b, b + n, b + 2 * (size_t)n, b + 3 * (size_t)n, b + 4 * (size_t)n};
         CK(launch_ray_order(s->g, d_rays, n, rb, &order, st), "ray order");
     }
-    if (d_full || s->trace_mode == 0)
-        CK(launch_trace_rays(s->g, d_rays, n, order, d_hits, d_full, s->stack, s->minb, s->d_err, ctr, st),
+    if (d_full || s->trace_mode == 0 || s->trace_mode == 3)
+        CK(launch_trace_rays(s->g, d_rays, n, order, d_hits, d_full, s->stack, s->minb, s->d_err, ctr, st,
+                             s->trace_mode == 3),
            "trace launch");
     else if (s->trace_mode == 2)
         CK(launch_trace_packet_rays(s->g, d_rays, n, order, d_hits, s->stack, s->d_err, ctr, st), "trace launch");
@@ -379,7 +389,8 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
             CK(launch_trace_packet_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->grid, B.err, ctr, st),
                "trace launch");
         else
-            CK(launch_trace_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, s->grid, B.err, ctr, st),
+            CK(launch_trace_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, s->grid, B.err, ctr, st,
+                                  s->trace_mode == 3),
                "trace launch");
         if (ev) cudaEventRecord(ev[3 + 3 * it], st);
         uint32_t *qout = qin == B.queue[1] ? B.queue[0] : B.queue[1];
@@ -857,6 +868,8 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
         std::vector<TuneCfg> v;
         for (int m : {4, 5, 6, 8}) { TuneCfg c = cur; c.trace_mode = 0; c.minb = m; v.push_back(c); }
         for (int m : {4, 6, 8}) { TuneCfg c = cur; c.trace_mode = 1; c.minb = m; v.push_back(c); }
+        if (s->g.static_fast)  // the static-scene traversal
+            for (int m : {8, 10, 12}) { TuneCfg c = cur; c.trace_mode = 3; c.minb = m; v.push_back(c); }
         // warp packets (trace mode 2) are not tried: 2-7x slower on every
         // measured workload, as one-thread-per-ray keeps more rays in flight
         try_set(v);
@@ -950,6 +963,15 @@ int psy_debug_mesh_bvh_info(PsyScene *s, uint32_t object, uint32_t *tri_order, u
     if (node_count) *node_count = s->mesh_node_count[m];
     return PSY_OK;
 }
+// Host-side only (no device): the traversal table as the device holds it and
+// the push tables of the static-scene traversal.
+int psy_debug_push_tables(uint8_t *table, uint8_t *rows, uint16_t *lut) {
+    if (!table || !rows || !lut) return fail(PSY_E_INVALID, "null argument");
+    psy_traversal_table_device(reinterpret_cast<uint8_t(*)[48]>(table));
+    if (!psy_push_tables_host(reinterpret_cast<uint8_t(*)[48]>(rows), reinterpret_cast<uint16_t(*)[16]>(lut)))
+        return fail(PSY_E_INVALID, "push tables need more rows");
+    return PSY_OK;
+}
 // Host-side build only (no device): BVH facts of a mesh object.
 int psy_debug_host_build(const PsySceneDesc *desc, const PsySceneOptions *opts, uint32_t object, uint32_t *tri_order,
                          uint32_t *node_count, uint32_t *max_stack) {
@@ -969,6 +991,13 @@ int psy_debug_scene_info(PsyScene *s, uint32_t *max_stack, uint32_t *nodes, uint
     if (max_stack) *max_stack = s->max_stack;
     if (nodes) *nodes = s->node_count;
     if (stack_variant) *stack_variant = (uint32_t)s->stack;
+    return PSY_OK;
+}
+// Scene facts the kernel choice depends on: bit 0 = the static-scene
+// traversal applies, bit 1 = ordered child boxes, bit 2 = FP16 bounds.
+int psy_debug_scene_flags(PsyScene *s, uint32_t *flags) {
+    if (!s || !flags) return fail(PSY_E_INVALID, "null");
+    *flags = (s->g.static_fast ? 1u : 0u) | (s->g.ordered_slabs ? 2u : 0u) | (s->g.use_fp16 ? 4u : 0u);
     return PSY_OK;
 }
 // Traversal counters of renders: enable (and zero) or read them.
@@ -992,12 +1021,16 @@ int psy_debug_counters(PsyScene *s, int enable, uint64_t *nodes, uint64_t *tris,
     return PSY_OK;
 }
 // Traversal kernel choice: mode 0 = one thread per ray, 1 = persistent with
-// lane refill; minb = resident blocks per SM the register budget targets.
+// lane refill, 2 = warp packets, 3 = the static-scene traversal (one thread
+// per ray; scenes without it fall back to mode 0's kernels); minb = resident
+// blocks per SM the register budget targets.
 int psy_debug_set_trace(PsyScene *s, int mode, int minb) {
-    if (!s || mode < 0 || mode > 2) return fail(PSY_E_INVALID, "bad trace mode");
+    if (!s || mode < 0 || mode > 3) return fail(PSY_E_INVALID, "bad trace mode");
     s->trace_mode = mode;
-    // persistent kernel: 4, 6 or 8 blocks per SM; one thread per ray: 4, 5 or 6
+    // persistent kernel: 4, 6 or 8 blocks per SM; one thread per ray: 4, 5,
+    // 6 or 8; static-scene traversal: 6, 8, 10 or 12
     if (mode == 1) s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : 4);
+    else if (mode == 3) s->minb = minb >= 12 ? 12 : (minb >= 10 ? 10 : (minb >= 8 ? 8 : 6));
     else s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : (minb == 5 ? 5 : 4));
     return PSY_OK;
 }

@@ -389,6 +389,196 @@ DI bool trace_ray(const GScene &S, const uint8_t *table, V3 o, V3 d, float tmax,
     }
 }
 
+// ------------------------------------------------------------------ static-scene traversal
+// Scenes whose meshes are all static and untransformed, whose nodes carry no
+// motion keys and whose child boxes are ordered (GScene::static_fast) take a
+// traversal with a much smaller live state than trace_ray: no local space,
+// no instance matrix, no mesh record, and the hit keeps only its kind,
+// triangle and instance (t is the final max_t; the barycentrics are
+// recomputed once at the end by repeating the winning test, which is
+// deterministic and passes with an unbounded max_t).  Visit order, node and
+// triangle tests and their arithmetic are trace_ray's, so hits are identical.
+//
+// Child push by table: for each (ray octant, traversal code) a push row
+// (c_push_row) and for each row and 4-bit hit mask a 16-bit entry
+// (c_push_lut): bits 0-1 the child to descend into, bits 2-7 up to three
+// children to push (deepest first), bits 8-10 how many, bit 11 set when any
+// child was hit.  The entries follow the traversal table's front-to-back
+// order and ignore mask bits past the node's child count.
+#define PSY_PUSH_ROWS 32
+static __constant__ uint8_t c_push_row[8][48];
+static __constant__ uint16_t c_push_lut[PSY_PUSH_ROWS][16];
+
+DI void load_push_tables(uint8_t *row, uint16_t *lut) {
+    for (int i = threadIdx.x; i < 8 * 48; i += blockDim.x) row[i] = (&c_push_row[0][0])[i];
+    for (int i = threadIdx.x; i < PSY_PUSH_ROWS * 16; i += blockDim.x) lut[i] = (&c_push_lut[0][0])[i];
+    __syncthreads();
+}
+
+DI uint32_t sel4(const uint4 &c, uint32_t i) {
+    uint32_t lo = (i & 1u) ? c.y : c.x, hi = (i & 1u) ? c.w : c.z;
+    return (i & 2u) ? hi : lo;
+}
+
+// Child hit mask of a static node (no motion keys; the count mask is applied
+// by the push table).  safe: slab_safe holds for the ray (boxes are ordered).
+DI uint32_t node_hits_static(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, uint32_t oct, bool safe,
+                             uint32_t &code, uint4 &child) {
+    const GNode *n = S.nodes + ni;
+    const float4 *bb = reinterpret_cast<const float4 *>(n);
+    child = __ldg(&n->child);
+    code = __ldg(&n->meta.z) & 0xFFu;
+    if (safe) {
+        uint32_t sx = oct & 1u, sy = (oct >> 1) & 1u, sz = (oct >> 2) & 1u;
+        float4 nx = __ldg(bb + sx), fx = __ldg(bb + (sx ^ 1u));
+        float4 ny = __ldg(bb + 2 + sy), fy = __ldg(bb + 2 + (sy ^ 1u));
+        float4 nz = __ldg(bb + 4 + sz), fz = __ldg(bb + 4 + (sz ^ 1u));
+        float tnx[4], tfx[4], tny[4], tfy[4], tnz[4], tfz[4];
+        f32x2 ox = pk2(o.x, o.x), oy = pk2(o.y, o.y), oz = pk2(o.z, o.z);
+        f32x2 dx = pk2(di.x, di.x), dy = pk2(di.y, di.y), dz = pk2(di.z, di.z);
+        slab_axis4(nx, ox, dx, tnx); slab_axis4(fx, ox, dx, tfx);
+        slab_axis4(ny, oy, dy, tny); slab_axis4(fy, oy, dy, tfy);
+        slab_axis4(nz, oz, dz, tnz); slab_axis4(fz, oz, dz, tfz);
+        uint32_t m = 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            float far_t = fminf(fmin3f(tfx[c], tfy[c], tfz[c]) * PSY_BBOX_MAXT_ADJUST, tmax);
+            float near_t = fmax3f(tnx[c], tny[c], fmaxf(tnz[c], 0.0f));
+            m |= near_t < far_t ? (1u << c) : 0u;
+        }
+        return m;
+    }
+    float4 xl = __ldg(bb), xh = __ldg(bb + 1), yl = __ldg(bb + 2), yh = __ldg(bb + 3), zl = __ldg(bb + 4),
+           zh = __ldg(bb + 5);
+    uint32_t m = 0;
+    m |= slab_hit(xl.x, xh.x, yl.x, yh.x, zl.x, zh.x, o, di, tmax) ? 1u : 0u;
+    m |= slab_hit(xl.y, xh.y, yl.y, yh.y, zl.y, zh.y, o, di, tmax) ? 2u : 0u;
+    m |= slab_hit(xl.z, xh.z, yl.z, yh.z, zl.z, zh.z, o, di, tmax) ? 4u : 0u;
+    m |= slab_hit(xl.w, xh.w, yl.w, yh.w, zl.w, zh.w, o, di, tmax) ? 8u : 0u;
+    return m;
+}
+
+// Corners of rectangle light triangle `which` (0: p1 p2 p3, 1: p3 p4 p1), as
+// rect_hit builds them.
+DI void rect_tri(const GScene &S, const GInstance &in, float time, uint32_t which, V3 &a, V3 &b, V3 &c) {
+    const GLight L = S.lights[in.obj];
+    float w = light_dim(S, L, 0, time), h = light_dim(S, L, 1, time);
+    Xf si = xf_inverse(instance_xf_at(S, in, time));
+    V3 p1, p2, p3, p4;
+    rect_corners(w, h, si, &p1, &p2, &p3, &p4);
+    if (which == 0) { a = p1; b = p2; c = p3; }
+    else { a = p3; b = p4; c = p1; }
+}
+
+template <int STACK>
+DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut, V3 o, V3 d, float tmax,
+                         float time, bool occl, HitRec &hit) {
+    hit.kind = PSY_HIT_MISS_K;
+    if (S.top_root == PSY_REF_NONE) return true;
+    Xf ident = xf_identity();
+    V3 wo = xf_point(o, ident);
+    V3 di = recip(xf_vector(d, ident));
+    uint32_t oct = ray_code(di);
+    const uint8_t *prow = prow_tab + 48 * oct;
+    bool safe = slab_safe(wo, di, tmax);
+    uint32_t stack[STACK + 4];
+    int sp = 0;
+    uint32_t cur = S.top_root;
+    bool in_inst = false;
+    uint32_t slot = 0, hkind = PSY_HIT_MISS_K, hprim = 0, hslot = 0;
+    TriPre pre = tri_precompute(d);
+    while (true) {
+        while (!psy_is_leaf(cur)) {
+            uint32_t code;
+            uint4 ch;
+            uint32_t m = node_hits_static(S, cur, wo, di, tmax, oct, safe, code, ch);
+            uint32_t e = lut[16u * prow[code] + m];
+            if (!(e & 0x800u)) goto pop;
+            int np = (int)((e >> 8) & 7u);
+            if (sp + np > STACK) return false;
+            // three unconditional stores (the stack has spare entries); only
+            // np of them are kept
+            stack[sp] = sel4(ch, (e >> 2) & 3u);
+            stack[sp + 1] = sel4(ch, (e >> 4) & 3u);
+            stack[sp + 2] = sel4(ch, (e >> 6) & 3u);
+            sp += np;
+            cur = sel4(ch, e & 3u);
+        }
+        if (!in_inst) {
+            slot = psy_leaf_first(cur);
+            GInstance in = S.instances[slot];
+            if (in.kind == PSY_INST_MESH) {
+                if (sp >= STACK) return false;
+                stack[sp++] = PSY_REF_NONE;  // leave-instance marker
+                in_inst = true;
+                safe = slab_safe(wo, di, tmax);
+                cur = S.meshes[in.obj].root;
+                continue;
+            } else if (in.kind == PSY_INST_RECT) {
+                float t, b0, b1, b2;
+                uint32_t which;
+                if (rect_hit(S, in, o, d, tmax, time, t, b0, b1, b2, which)) {
+                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
+                    hkind = PSY_HIT_LIGHT_K; hprim = which; hslot = slot;
+                    tmax = t;
+                }
+            } else {
+                Xf x = instance_xf_at(S, in, time);
+                V3 ol = in.xc ? xf_point(o, x) : wo;
+                float t;
+                if (sphere_hit(S, in, ol, d, tmax, time, t)) {
+                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
+                    hkind = PSY_HIT_LIGHT_K; hprim = 0xFFFFFFFFu; hslot = slot;  // prim 0, no barycentrics
+                    tmax = t;
+                }
+            }
+        } else {
+            uint32_t first = psy_leaf_first(cur), ntri = psy_leaf_count(cur);
+            for (uint32_t k = 0; k < ntri; k++) {
+                uint32_t tri = first + k;
+                const float4 *tp = S.tris + 3 * (size_t)tri;
+                V3 p0 = v3(__ldg(tp)), p1 = v3(__ldg(tp + 1)), p2 = v3(__ldg(tp + 2));
+                float t, b0, b1, b2;
+                if (tri_intersect(o, pre, tmax, p0, p1, p2, t, b0, b1, b2)) {
+                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
+                    hkind = PSY_HIT_SURFACE_K; hprim = tri; hslot = slot;
+                    tmax = t;
+                }
+            }
+        }
+    pop:
+        while (true) {
+            if (sp == 0) goto done;
+            cur = stack[--sp];
+            if (cur != PSY_REF_NONE) break;
+            in_inst = false;  // leaving the instance (world space is the instance's space)
+            safe = slab_safe(wo, di, tmax);
+        }
+    }
+done:
+    hit.kind = hkind;
+    if (hkind == PSY_HIT_MISS_K) return true;
+    hit.slot = hslot;
+    hit.t = tmax;
+    hit.b0 = hit.b1 = hit.b2 = 0.0f;
+    const float inf = __int_as_float(0x7f800000);
+    float t2, b0, b1, b2;
+    if (hkind == PSY_HIT_SURFACE_K) {
+        hit.prim = hprim;
+        const float4 *tp = S.tris + 3 * (size_t)hprim;
+        V3 p0 = v3(__ldg(tp)), p1 = v3(__ldg(tp + 1)), p2 = v3(__ldg(tp + 2));
+        if (tri_intersect(o, pre, inf, p0, p1, p2, t2, b0, b1, b2)) { hit.b0 = b0; hit.b1 = b1; hit.b2 = b2; }
+    } else if (hprim == 0xFFFFFFFFu) {
+        hit.prim = 0;  // sphere light
+    } else {
+        hit.prim = hprim;
+        V3 a, b, c;
+        rect_tri(S, S.instances[hslot], time, hprim, a, b, c);
+        if (tri_intersect(o, pre, inf, a, b, c, t2, b0, b1, b2)) { hit.b0 = b0; hit.b1 = b1; hit.b2 = b2; }
+    }
+    return true;
+}
+
 }  // namespace psyd
 
 namespace psyd {

@@ -79,12 +79,15 @@ static void extend_traversal_table(uint8_t t[8][48]) {
             else t[rd][k] = (uint8_t)(t[rd][k] | (2u << 4) | (3u << 6));
         }
 }
+void psy_traversal_table_device(uint8_t t[8][48]) {
+    traversal_table_host(t);
+    extend_traversal_table(t);
+}
 void psy_upload_constants() {
     uint32_t d[8][32];
     uint8_t t[8][48];
     sobol_dirs_host(d);
-    traversal_table_host(t);
-    extend_traversal_table(t);
+    psy_traversal_table_device(t);
     cudaMemcpyToSymbol(c_sobol_dirs, d, sizeof(d));
     cudaMemcpyToSymbol(c_traversal_table, t, sizeof(t));
     psy_upload_trace_constants(t, nullptr);

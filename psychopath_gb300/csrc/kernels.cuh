@@ -51,6 +51,12 @@ struct WaveDesc {
 };
 
 void psy_upload_constants();  // Sobol directions + traversal table -> __constant__
+// The traversal table as the device holds it (positions past a node's child
+// count name its empty slots).
+void psy_traversal_table_device(uint8_t t[8][48]);
+// Push tables of the static-scene traversal built from that table (false:
+// more distinct rows than the device table holds).
+bool psy_push_tables_host(uint8_t rows[8][48], uint16_t lut[32][16]);
 // The traversal translation unit's own copies of its constants (null: skip).
 void psy_upload_trace_constants(const uint8_t table[8][48], const float magenta[3]);
 
@@ -58,10 +64,10 @@ void psy_upload_trace_constants(const uint8_t table[8][48], const float magenta[
 // minb: resident blocks of 128 threads per SM the register budget targets
 // (4 = the compiler's choice, 5 or 6 = fewer registers, some spills).
 // order (optional): thread q traces ray order[q] (hits still land at the
-// ray's own index).
+// ray's own index).  fast: as for launch_trace_queue.
 cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order, PsyHit *hits,
                               PsySurfaceHit *full, int stack, int minb, int *d_err, unsigned long long *counters,
-                              cudaStream_t st);
+                              cudaStream_t st, bool fast = false);
 // Box of the two-point sort keys: the scene box grown on every side by the
 // key length len = 1/20 of the scene box diagonal.
 inline void two_point_box(const GScene &S, float4 &lo, float4 &inv, float &len) {
@@ -103,10 +109,12 @@ cudaError_t launch_trace_packet_queue(const GScene &S, RayBuf R, HitBuf H, const
 cudaError_t launch_trace_packet_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order,
                                      PsyHit *hits, int stack, int *d_err, unsigned long long *counters,
                                      cudaStream_t st);
-// Trace the queued rays of a wave.
+// Trace the queued rays of a wave.  fast: the static-scene traversal when the
+// scene allows it (GScene::static_fast) and no counters are requested;
+// minb 6, 8, 10 or 12 there.
 cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
                                uint32_t max_count, int stack, int minb, int grid, int *d_err,
-                               unsigned long long *counters, cudaStream_t st);
+                               unsigned long long *counters, cudaStream_t st, bool fast = false);
 // LightPath::next for the queued paths; live paths go to next_queue.
 // minb: register budget for 4 (compiler's choice), 6 or 8 resident blocks.
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,

@@ -140,6 +140,8 @@ struct GScene {
     uint32_t width, height, spp, seed, max_bounces;
     uint32_t use_fp16;
     uint32_t ordered_slabs;      // every child box of every node has lo <= hi on each axis (host-checked)
+    uint32_t static_fast;        // FP32 nodes without motion keys, ordered boxes, every mesh static and every
+                                 // mesh instance untransformed: the static-scene traversal applies
     float distant_energy_total;  // sum of distant light energies
     float lt_root_energy;
     float4 bounds_min, bounds_inv_extent;  // scene box, for the ray sort key's origin cell

@@ -13,14 +13,22 @@
 
 using namespace psyd;
 
+// Set once the push tables of the static-scene traversal are on the device;
+// that traversal is launched only then.
+static bool g_push_tables = false;
+
 // ------------------------------------------------------------------ ray tracing
-template <int STACK, bool COUNT, int MINB>
+// STATIC: the static-scene traversal (trace_ray_static; the scene must have
+// static_fast set, and the launch passes no counters).
+template <int STACK, bool COUNT, int MINB, bool STATIC = false>
 __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay *__restrict__ rays, uint32_t n,
                                                     const uint32_t *__restrict__ order, PsyHit *__restrict__ hits,
                                                     PsySurfaceHit *__restrict__ full, int *err,
                                                     unsigned long long *counters) {
     __shared__ uint8_t table[8 * 48];
-    load_traversal_table(table);
+    __shared__ uint16_t push_lut[STATIC ? PSY_PUSH_ROWS * 16 : 1];
+    if (STATIC) load_push_tables(table, push_lut);
+    else load_traversal_table(table);
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t i = q;
     TraceCount tc{0, 0};
@@ -31,7 +39,10 @@ __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay
         float tmax = r[6], time = r[7];
         uint32_t flags = reinterpret_cast<const uint32_t *>(r)[9];
         HitRec h;
-        if (!trace_ray<STACK, COUNT>(S, table, o, d, tmax, time, (flags & PSY_RAY_OCCLUSION) != 0, h, &tc)) {
+        bool oc = (flags & PSY_RAY_OCCLUSION) != 0;
+        bool ok = STATIC ? trace_ray_static<STACK>(S, table, push_lut, o, d, tmax, time, oc, h)
+                         : trace_ray<STACK, COUNT>(S, table, o, d, tmax, time, oc, h, &tc);
+        if (!ok) {
             atomicExch(err, PSY_E_OVERFLOW);
             h.kind = PSY_HIT_MISS_K;
         }
@@ -88,9 +99,21 @@ __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay
 // budget only: node and triangle counts do not depend on the launch shape.
 cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order, PsyHit *hits,
                               PsySurfaceHit *full, int stack, int minb, int *d_err, unsigned long long *counters,
-                              cudaStream_t st) {
+                              cudaStream_t st, bool fast) {
     if (n == 0) return cudaSuccess;
     dim3 b(128), g((n + 127) / 128);
+    if (fast && g_push_tables && S.static_fast && !counters) {
+#define TF(SZ, MB) k_trace_rays<SZ, false, MB, true><<<g, b, 0, st>>>(S, rays, n, order, hits, full, d_err, nullptr)
+#define TFS(SZ)                          \
+    if (minb >= 12) TF(SZ, 12);          \
+    else if (minb >= 10) TF(SZ, 10);     \
+    else if (minb >= 8) TF(SZ, 8);       \
+    else TF(SZ, 6)
+        if (stack <= 64) { TFS(64); } else { TFS(192); }
+#undef TFS
+#undef TF
+        return cudaGetLastError();
+    }
 #define TR(SZ, C, MB) k_trace_rays<SZ, C, MB><<<g, b, 0, st>>>(S, rays, n, order, hits, full, d_err, counters)
 #define TRS(SZ)                                                   \
     if (counters) TR(SZ, true, 4);                                \
@@ -355,12 +378,14 @@ cudaError_t launch_trace_packet_rays(const GScene &S, const PsyRay *rays, uint32
 // Queue-driven trace for the render wavefront: a grid-stride loop over the
 // live paths listed in queue[0 .. *count).  COUNT adds the work counters
 // (node visits, triangle tests, rays) into counters[0..2].
-template <int STACK, bool COUNT, int MINB>
+template <int STACK, bool COUNT, int MINB, bool STATIC = false>
 __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
                                                      const uint32_t *__restrict__ count, int *err,
                                                      unsigned long long *counters) {
     __shared__ uint8_t table[8 * 48];
-    load_traversal_table(table);
+    __shared__ uint16_t push_lut[STATIC ? PSY_PUSH_ROWS * 16 : 1];
+    if (STATIC) load_push_tables(table, push_lut);
+    else load_traversal_table(table);
     uint32_t n = *count;
     TraceCount tc{0, 0};
     uint32_t nr = 0;
@@ -368,7 +393,10 @@ __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, H
         uint32_t p = queue[q];
         float4 ro = R.o[p], rd = R.d[p];
         HitRec h;
-        if (!trace_ray<STACK, COUNT>(S, table, v3(ro), v3(rd), ro.w, rd.w, R.occl[p] != 0, h, &tc)) {
+        bool oc = R.occl[p] != 0;
+        bool ok = STATIC ? trace_ray_static<STACK>(S, table, push_lut, v3(ro), v3(rd), ro.w, rd.w, oc, h)
+                         : trace_ray<STACK, COUNT>(S, table, v3(ro), v3(rd), ro.w, rd.w, oc, h, &tc);
+        if (!ok) {
             atomicExch(err, PSY_E_OVERFLOW);
             h.kind = PSY_HIT_MISS_K;
         }
@@ -393,9 +421,21 @@ __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, H
 
 cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
                                uint32_t max_count, int stack, int minb, int grid, int *d_err,
-                               unsigned long long *counters, cudaStream_t st) {
+                               unsigned long long *counters, cudaStream_t st, bool fast) {
     if (grid <= 0) grid = (int)((max_count + 127) / 128);
     if (grid == 0) return cudaSuccess;
+    if (fast && g_push_tables && S.static_fast && !counters) {
+#define TF(SZ, MB) k_trace_queue<SZ, false, MB, true><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, nullptr)
+#define TFS(SZ)                          \
+    if (minb >= 12) TF(SZ, 12);          \
+    else if (minb >= 10) TF(SZ, 10);     \
+    else if (minb >= 8) TF(SZ, 8);       \
+    else TF(SZ, 6)
+        if (stack <= 64) { TFS(64); } else { TFS(192); }
+#undef TFS
+#undef TF
+        return cudaGetLastError();
+    }
 #define TQ(SZ, C, MB) k_trace_queue<SZ, C, MB><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, counters)
 #define TQS(SZ)                                                   \
     if (counters) TQ(SZ, true, 4);                                \
@@ -442,10 +482,61 @@ cudaError_t launch_ray_order(const GScene &S, const PsyRay *rays, uint32_t n, co
     return e;
 }
 
+// Push tables of the static-scene traversal from the device traversal table
+// (positions past a node's child count already name its empty slots).
+// Codes 0..26 order four children, 27..44 three, 45..47 two.
+static bool push_tables_host(const uint8_t table[8][48], uint8_t rows[8][48], uint16_t lut[PSY_PUSH_ROWS][16]) {
+    uint32_t keys[PSY_PUSH_ROWS];
+    int nrows = 0;
+    for (int oct = 0; oct < 8; oct++)
+        for (int code = 0; code < 48; code++) {
+            uint32_t count = code < 27 ? 4u : (code < 45 ? 3u : 2u);
+            uint32_t key = table[oct][code] | (count << 8);
+            int r = 0;
+            while (r < nrows && keys[r] != key) r++;
+            if (r == nrows) {
+                if (nrows == PSY_PUSH_ROWS) return false;  // (8 + 8 + 8 + 2 distinct pairs are expected)
+                keys[nrows++] = key;
+                for (uint32_t m = 0; m < 16; m++) {
+                    uint32_t me = m & ((1u << count) - 1u), list[4], k = 0;
+                    for (int i = 0; i < 4; i++) {
+                        uint32_t ci = (table[oct][code] >> (2 * i)) & 3u;
+                        if ((me >> ci) & 1u) list[k++] = ci;
+                    }
+                    uint32_t e = 0;
+                    if (k > 0) {
+                        e = list[0] | ((k - 1) << 8) | 0x800u;
+                        for (uint32_t j = 0; j + 1 < k; j++) e |= list[k - 1 - j] << (2 + 2 * j);
+                    }
+                    lut[r][m] = (uint16_t)e;
+                }
+            }
+            rows[oct][code] = (uint8_t)r;
+        }
+    for (int r = nrows; r < PSY_PUSH_ROWS; r++)
+        for (int m = 0; m < 16; m++) lut[r][m] = 0;
+    return true;
+}
+
+// The push tables as the device receives them (host-side only; for tests).
+bool psy_push_tables_host(uint8_t rows[8][48], uint16_t lut[32][16]) {
+    static_assert(PSY_PUSH_ROWS == 32, "table size of the debug export");
+    uint8_t t[8][48];
+    psy_traversal_table_device(t);
+    return push_tables_host(t, rows, lut);
+}
+
 // Constants of this translation unit: the child-order table and the colour
 // of unshaded instances (kernels.cu keeps its own copies).
 void psy_upload_trace_constants(const uint8_t table[8][48], const float magenta[3]) {
-    if (table) cudaMemcpyToSymbol(c_traversal_table, table, 8 * 48);
+    if (table) {
+        cudaMemcpyToSymbol(c_traversal_table, table, 8 * 48);
+        uint8_t rows[8][48];
+        uint16_t lut[PSY_PUSH_ROWS][16];
+        if (push_tables_host(table, rows, lut) && cudaMemcpyToSymbol(c_push_row, rows, sizeof(rows)) == cudaSuccess &&
+            cudaMemcpyToSymbol(c_push_lut, lut, sizeof(lut)) == cudaSuccess)
+            g_push_tables = true;
+    }
     if (magenta) {
         GColor c{PSY_COLOR_XYZ_K, magenta[0], magenta[1], magenta[2]};
         cudaMemcpyToSymbol(c_magenta, &c, sizeof(c));

@@ -69,6 +69,8 @@ def lib(path=None):
     L.psy_debug_set_ray_order.argtypes = [vp, C.c_int]
     L.psy_debug_ray_order.argtypes = [vp, vp, u32, vp, vp, vp]
     L.psy_debug_render_sized.argtypes = [vp, u32, u32, u32, u32, vp, vp]
+    L.psy_debug_push_tables.argtypes = [vp, vp, vp]
+    L.psy_debug_scene_flags.argtypes = [vp, C.POINTER(u32)]
     L.psy_server_create.argtypes = [vp, C.POINTER(vp)]
     L.psy_server_add_scene.argtypes = [vp, vp, C.POINTER(u32)]
     L.psy_submit.argtypes = [vp, vp, C.POINTER(C.c_uint64)]
@@ -100,6 +102,17 @@ def host_build_info(scene_data, obj, bounds="fp32"):
     nc, ms = C.c_uint32(), C.c_uint32()
     _check(lib().psy_debug_host_build(C.byref(desc), C.byref(opts), obj, order.ctypes.data, C.byref(nc), C.byref(ms)))
     return order[:n], nc.value, ms.value
+
+
+def push_tables():
+    """Host-side only (no GPU needed): the traversal table as the device holds
+    it (8 octants x 48 codes) and the static-scene traversal's push tables
+    (row per octant and code; 32 rows x 16 hit masks of 16-bit entries)."""
+    table = np.zeros((8, 48), dtype=np.uint8)
+    rows = np.zeros((8, 48), dtype=np.uint8)
+    lut = np.zeros((32, 16), dtype=np.uint16)
+    _check(lib().psy_debug_push_tables(table.ctypes.data, rows.ctypes.data, lut.ctypes.data))
+    return table, rows, lut
 
 
 class Scene:
@@ -154,9 +167,18 @@ class Scene:
         _check(lib().psy_debug_counters(self.h, 1 if enable else 0, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
 
+    def flags(self):
+        """Scene facts the traversal kernel choice depends on: {'static_fast',
+        'ordered_slabs', 'fp16'}."""
+        f = C.c_uint32()
+        _check(lib().psy_debug_scene_flags(self.h, C.byref(f)))
+        return {"static_fast": bool(f.value & 1), "ordered_slabs": bool(f.value & 2), "fp16": bool(f.value & 4)}
+
     def set_trace(self, mode=1, minb=4):
         """Traversal kernel: mode 0 = one thread per ray, 1 = persistent with
-        lane refill; minb = target resident blocks per SM (4 or 8)."""
+        lane refill, 2 = warp packets, 3 = the static-scene traversal (scenes
+        with motion, instance transforms or FP16 bounds use mode 0's kernels);
+        minb = target resident blocks per SM (4-8; 6-12 for mode 3)."""
         _check(lib().psy_debug_set_trace(self.h, mode, minb))
 
     def set_shade(self, minb):

@@ -131,7 +131,7 @@ def test_empty_batch_and_misses(gpu_lib):
     assert (h["kind"] == abi.PSY_HIT_MISS).all()
 
 
-@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 5), (0, 6), (0, 8), (1, 4), (1, 6), (1, 8), (2, 4)])
+@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 5), (0, 6), (0, 8), (1, 4), (1, 6), (1, 8), (2, 4), (3, 8)])
 def test_trace_kernel_variants_identical(gpu_lib, mode, minb):
     """Every traversal kernel variant (one thread per ray, persistent with lane
     refill at each register budget, warp packets) returns identical hits."""
@@ -147,7 +147,7 @@ def test_trace_kernel_variants_identical(gpu_lib, mode, minb):
     assert np.array_equal(h, ref)
 
 
-@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 8), (1, 8), (2, 4)])
+@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 8), (1, 8), (2, 4), (3, 10)])
 def test_binned_ray_order_identical(gpu_lib, mode, minb):
     """Sorting a large batch by two-point key only changes which thread
     traces which ray: hits are identical to the given order."""
@@ -225,3 +225,38 @@ def test_warp_packets_match_per_ray(gpu_lib, case):
     tr.trace(rays)
     rn, rt, _ = g.counters(False)
     assert (pn, pt) == (rn, rt)  # same node and triangle tests per ray
+
+
+@pytest.mark.parametrize("minb", [6, 8, 10, 12])
+def test_static_scene_traversal_identical(gpu_lib, minb):
+    """The static-scene traversal (trace mode 3) returns the same hits, bit
+    for bit, as the general kernel on static scenes: closest and any hit,
+    finite max_t, axis-parallel rays (the unordered slab test), the full
+    surface output, and misses; it agrees with the oracle like mode 0."""
+    cases = []
+    sd, P, F = sc.grid_small(256, 128)
+    cases.append((sd, np.concatenate([scenes.incoherent_rays(P, F, 1 << 15, seed=7), scenes.coherent_rays(96)])))
+    s = sc.sphere_small(level=4)
+    cases.append((s, sc.targeted_rays(20000, [-1.1, -0.1, -1.1], [1.1, 2.1, 1.1], [-4, 0.05, -4], [4, 4, 4], seed=5)))
+    rays = sc.random_rays(20000, [-0.95, 0.05, -0.95], [0.95, 1.95, 0.95], seed=6, occl_frac=0.3)
+    rays["max_t"][1::5] = 0.7
+    ax = rays[::7].copy()  # axis-parallel directions: zero direction components
+    ax["d"][:, 0] = 0.0
+    ax["d"][:, 2] = 0.0
+    ax["d"][:, 1] = np.where(np.arange(len(ax)) % 2 == 0, 1.0, -1.0).astype(np.float32)
+    cases.append((sc.cornell(), np.concatenate([rays, ax])))
+    n_static = 0
+    for sd, rays in cases:
+        g = gpu.Scene(sd)
+        n_static += g.flags()["static_fast"]
+        tr = gpu.Tracer(g)
+        g.set_trace(0, 4)
+        ref, fref = tr.trace(rays, full=True)
+        ref2 = tr.trace(rays)
+        g.set_trace(3, minb)
+        h = tr.trace(rays)
+        h2, f2 = tr.trace(rays, full=True)
+        assert np.array_equal(h, ref2)
+        assert np.array_equal(h2, ref) and np.array_equal(f2, fref)
+        g.close()
+    assert n_static >= 2  # the grid and the sphere scenes qualify
