@@ -241,9 +241,9 @@ def test_static_scene_traversal_identical(gpu_lib, minb):
     rays = sc.random_rays(20000, [-0.95, 0.05, -0.95], [0.95, 1.95, 0.95], seed=6, occl_frac=0.3)
     rays["max_t"][1::5] = 0.7
     ax = rays[::7].copy()  # axis-parallel directions: zero direction components
-    ax["d"][:, 0] = 0.0
-    ax["d"][:, 2] = 0.0
-    ax["d"][:, 1] = np.where(np.arange(len(ax)) % 2 == 0, 1.0, -1.0).astype(np.float32)
+    ax["dir"][:, 0] = 0.0
+    ax["dir"][:, 2] = 0.0
+    ax["dir"][:, 1] = np.where(np.arange(len(ax)) % 2 == 0, 1.0, -1.0).astype(np.float32)
     cases.append((sc.cornell(), np.concatenate([rays, ax])))
     n_static = 0
     for sd, rays in cases:
