@@ -480,7 +480,8 @@ def run_traversal(args):
     torch.cuda.set_stream(stream)
     configs = [("plain", 0, 4, False), ("minb8", 0, 8, False), ("minb8+binned", 0, 8, True),
                ("persistent8+binned", 1, 8, True), ("static8", 3, 8, False), ("static8+binned", 3, 8, True),
-               ("static10+binned", 3, 10, True), ("static12+binned", 3, 12, True), ("static6+binned", 3, 6, True)]
+               ("static10+binned", 3, 10, True), ("static12+binned", 3, 12, True), ("static6+binned", 3, 6, True),
+               ("spec8+binned", 4, 8, True), ("spec10+binned", 4, 10, True)]
     out = {}
     for name, rays in sets.items():
         n = len(rays)
@@ -523,7 +524,14 @@ def run_traversal(args):
             e1.record(stream)
             torch.cuda.synchronize()
             sec = e0.elapsed_time(e1) / 1e3 / args.steps
-            identical = bool(np.array_equal(d_hits.cpu().numpy(), ref_hits))
+            got = d_hits.cpu().numpy()
+            identical = bool(np.array_equal(got, ref_hits))
+            # forms that may break exact t ties differently (speculative
+            # traversal): rays whose hit differs, and whether every such hit
+            # has the same t
+            hg_, hr_ = got.view(abi.hit_dtype()), ref_hits.view(abi.hit_dtype())
+            ndiff = int((hg_ != hr_).sum())
+            ties_only = bool(np.array_equal(hg_["t"], hr_["t"]) and np.array_equal(hg_["kind"], hr_["kind"]))
             # the traversal kernel alone: a binned call is the ray sort plus
             # the kernel over the sorted order; time the kernel on that same
             # order (rays gathered on the device, trace in the given order)
@@ -545,7 +553,8 @@ def run_traversal(args):
             gbs = alg * n / ksec / 1e9
             res["configs"][cname] = {"trace_mode": mode, "minb": minb, "binned": binned, "ms_per_call": sec * 1e3,
                                      "kernel_ms": ksec * 1e3, "mrays_per_s": n / sec / 1e6, "achieved_gbs": gbs,
-                                     "frac": gbs / peak, "hits_identical_to_plain": identical}
+                                     "frac": gbs / peak, "hits_identical_to_plain": identical,
+                                     "hits_differing": ndiff, "differences_are_t_ties": ties_only}
         best = max(res["configs"].items(), key=lambda kv: kv[1]["mrays_per_s"])
         res["best"] = best[0]
         out[name] = res

@@ -169,6 +169,7 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
         psy_set_magenta(m);
         g_device_init = 1;
     });
+    if (!psy_trace_tables_ready()) return fail(PSY_E_CUDA, "traversal push tables were not uploaded");
     PsyScene *s = new PsyScene();
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete s;
@@ -314,9 +315,9 @@ static int trace_device_core(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyH
         RayOrderBufs rb{b, b + n, b + 2 * (size_t)n, b + 3 * (size_t)n, b + 4 * (size_t)n};
         CK(launch_ray_order(s->g, d_rays, n, rb, &order, st), "ray order");
     }
-    if (d_full || s->trace_mode == 0 || s->trace_mode == 3)
+    if (d_full || s->trace_mode == 0 || s->trace_mode >= 3)
         CK(launch_trace_rays(s->g, d_rays, n, order, d_hits, d_full, s->stack, s->minb, s->d_err, ctr, st,
-                             s->trace_mode == 3),
+                             s->trace_mode >= 3 ? s->trace_mode - 2 : 0),
            "trace launch");
     else if (s->trace_mode == 2)
         CK(launch_trace_packet_rays(s->g, d_rays, n, order, d_hits, s->stack, s->d_err, ctr, st), "trace launch");
@@ -390,7 +391,7 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
                "trace launch");
         else
             CK(launch_trace_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, s->grid, B.err, ctr, st,
-                                  s->trace_mode == 3),
+                                  s->trace_mode >= 3 ? s->trace_mode - 2 : 0),
                "trace launch");
         if (ev) cudaEventRecord(ev[3 + 3 * it], st);
         uint32_t *qout = qin == B.queue[1] ? B.queue[0] : B.queue[1];
@@ -1022,15 +1023,16 @@ int psy_debug_counters(PsyScene *s, int enable, uint64_t *nodes, uint64_t *tris,
 }
 // Traversal kernel choice: mode 0 = one thread per ray, 1 = persistent with
 // lane refill, 2 = warp packets, 3 = the static-scene traversal (one thread
-// per ray; scenes without it fall back to mode 0's kernels); minb = resident
-// blocks per SM the register budget targets.
+// per ray; scenes without it fall back to mode 0's kernels), 4 = its
+// speculative form; minb = resident blocks per SM the register budget
+// targets.
 int psy_debug_set_trace(PsyScene *s, int mode, int minb) {
-    if (!s || mode < 0 || mode > 3) return fail(PSY_E_INVALID, "bad trace mode");
+    if (!s || mode < 0 || mode > 4) return fail(PSY_E_INVALID, "bad trace mode");
     s->trace_mode = mode;
     // persistent kernel: 4, 6 or 8 blocks per SM; one thread per ray: 4, 5,
     // 6 or 8; static-scene traversal: 6, 8, 10 or 12
     if (mode == 1) s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : 4);
-    else if (mode == 3) s->minb = minb >= 12 ? 12 : (minb >= 10 ? 10 : (minb >= 8 ? 8 : 6));
+    else if (mode >= 3) s->minb = minb >= 12 ? 12 : (minb >= 10 ? 10 : (minb >= 8 ? 8 : 6));
     else s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : (minb == 5 ? 5 : 4));
     return PSY_OK;
 }

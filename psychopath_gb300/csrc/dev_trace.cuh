@@ -246,159 +246,6 @@ DI bool sphere_hit(const GScene &S, const GInstance &in, V3 ol, V3 d, float tmax
     return true;
 }
 
-// Trace one ray.  `occl`: any-hit (shadow ray).  Returns false on stack
-// overflow (the scene needs a deeper stack than STACK).
-// Traversal work counters (ray x node tests and ray x triangle tests).
-struct TraceCount {
-    uint32_t nodes, tris;
-};
-
-// Copies the traversal table into shared memory (per-lane indexed reads of
-// __constant__ memory would serialize across the warp).
-DI void load_traversal_table(uint8_t *smem) {
-    for (int i = threadIdx.x; i < 8 * 48; i += blockDim.x) smem[i] = (&c_traversal_table[0][0])[i];
-    __syncthreads();
-}
-
-template <int STACK, bool COUNT = false>
-DI bool trace_ray(const GScene &S, const uint8_t *table, V3 o, V3 d, float tmax, float time, bool occl, HitRec &hit,
-                  TraceCount *cnt = nullptr) {
-    hit.kind = PSY_HIT_MISS_K;
-    if (S.top_root == PSY_REF_NONE) return true;
-    Xf ident = xf_identity();
-    // world level: update_local(identity)
-    V3 wo = xf_point(o, ident);
-    V3 wdi = recip(xf_vector(d, ident));
-    V3 lo = wo, ldi = wdi;
-    uint32_t oct = ray_code(wdi);
-    const uint8_t *row = table + 48 * oct;
-    // slab_safe holds for the whole ray in a space (tmax only shrinks to a finite t)
-    bool safe = S.ordered_slabs && slab_safe(lo, ldi, tmax);
-    // 4 spare entries take the unconditional stores of the child push
-    uint32_t stack[STACK + 4];
-    int sp = 0;
-    uint32_t cur = S.top_root;
-    bool in_inst = false;
-    uint32_t slot = 0;
-    GMesh mesh;
-    Xf mat;
-    bool has_xf = false;
-    TriPre pre = tri_precompute(d);
-    while (true) {
-        // descend internal nodes
-        while (!psy_is_leaf(cur)) {
-            uint32_t code, count;
-            uint4 ch;
-            uint32_t m = S.use_fp16 ? node_hits_h(S, cur, lo, ldi, tmax, time, oct, safe, code, count, ch)
-                                    : node_hits(S, cur, lo, ldi, tmax, time, oct, safe, code, count, ch);
-            if (COUNT) cnt->nodes++;
-            if (m == 0) goto pop;
-            // children in the table's visit order: push all hit children
-            // but the first, descend into the first.  Every lane stores at
-            // each of the four positions and advances the stack pointer only
-            // for hit children, so lanes with different hit masks run the
-            // same instructions.  The device table maps positions past the
-            // node's child count to its empty slots (never in m).
-            uint32_t order = row[code];
-            uint32_t next = PSY_REF_NONE;
-            if (sp + __popc(m) - 1 > STACK) return false;
-#pragma unroll
-            for (int i = 3; i >= 0; i--) {
-                uint32_t ci = (order >> (i * 2)) & 3u;
-                bool h = (m >> ci) & 1u;
-                uint32_t c = ci == 0 ? ch.x : (ci == 1 ? ch.y : (ci == 2 ? ch.z : ch.w));
-                stack[sp] = next;  // kept only if this child is hit and a candidate exists
-                sp += (h && next != PSY_REF_NONE) ? 1 : 0;
-                next = h ? c : next;
-            }
-            (void)count;
-            cur = next;
-        }
-        // leaf
-        if (!in_inst) {
-            slot = psy_leaf_first(cur);
-            GInstance in = S.instances[slot];
-            if (in.kind == PSY_INST_MESH) {
-                mesh = S.meshes[in.obj];
-                has_xf = in.xc != 0;
-                if (has_xf) {
-                    Xf x = lerp_slice_xf(S.xforms + 3 * in.xs, in.xc, time);
-                    lo = xf_point(o, x);
-                    ldi = recip(xf_vector(d, x));
-                    mat = instance_mat(S, in, time);
-                } else {
-                    mat = ident;
-                }
-                if (sp >= STACK) return false;
-                stack[sp++] = PSY_REF_NONE;  // leave-instance marker
-                in_inst = true;
-                oct = ray_code(ldi);
-                row = table + 48 * oct;
-                safe = S.ordered_slabs && slab_safe(lo, ldi, tmax);
-                cur = mesh.root;
-                continue;
-            } else if (in.kind == PSY_INST_RECT) {
-                float t, b0, b1, b2;
-                uint32_t which;
-                if (rect_hit(S, in, o, d, tmax, time, t, b0, b1, b2, which)) {
-                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
-                    hit.kind = PSY_HIT_LIGHT_K; hit.prim = which; hit.slot = slot;
-                    hit.t = t; hit.b0 = b0; hit.b1 = b1; hit.b2 = b2;
-                    tmax = t;
-                }
-            } else {
-                Xf x = instance_xf_at(S, in, time);
-                V3 ol = in.xc ? xf_point(o, x) : wo;
-                float t;
-                if (sphere_hit(S, in, ol, d, tmax, time, t)) {
-                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
-                    hit.kind = PSY_HIT_LIGHT_K; hit.prim = 0; hit.slot = slot;
-                    hit.t = t; hit.b0 = hit.b1 = hit.b2 = 0.0f;
-                    tmax = t;
-                }
-            }
-        } else {
-            uint32_t first = psy_leaf_first(cur), ntri = psy_leaf_count(cur);
-            for (uint32_t k = 0; k < ntri; k++) {
-                uint32_t tri = first + k;
-                V3 p0, p1, p2;
-                fetch_tri(S, mesh, tri, time, has_xf, mat, p0, p1, p2);
-                float t, b0, b1, b2;
-                if (COUNT) cnt->tris++;
-                if (tri_intersect(o, pre, tmax, p0, p1, p2, t, b0, b1, b2)) {
-                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
-                    hit.kind = PSY_HIT_SURFACE_K; hit.prim = tri; hit.slot = slot;
-                    hit.t = t; hit.b0 = b0; hit.b1 = b1; hit.b2 = b2;
-                    tmax = t;
-                }
-            }
-        }
-    pop:
-        while (true) {
-            if (sp == 0) return true;
-            cur = stack[--sp];
-            if (cur != PSY_REF_NONE) break;
-            // leaving the instance: back to world space
-            in_inst = false;
-            lo = wo;
-            ldi = wdi;
-            oct = ray_code(wdi);
-            row = table + 48 * oct;
-            safe = S.ordered_slabs && slab_safe(lo, ldi, tmax);
-        }
-    }
-}
-
-// ------------------------------------------------------------------ static-scene traversal
-// Scenes whose meshes are all static and untransformed, whose nodes carry no
-// motion keys and whose child boxes are ordered (GScene::static_fast) take a
-// traversal with a much smaller live state than trace_ray: no local space,
-// no instance matrix, no mesh record, and the hit keeps only its kind,
-// triangle and instance (t is the final max_t; the barycentrics are
-// recomputed once at the end by repeating the winning test, which is
-// deterministic and passes with an unbounded max_t).  Visit order, node and
-// triangle tests and their arithmetic are trace_ray's, so hits are identical.
-//
 // Child push by table: for each (ray octant, traversal code) a push row
 // (c_push_row) and for each row and 4-bit hit mask a 16-bit entry
 // (c_push_lut): bits 0-1 the child to descend into, bits 2-7 up to three
@@ -420,6 +267,240 @@ DI uint32_t sel4(const uint4 &c, uint32_t i) {
     return (i & 2u) ? hi : lo;
 }
 
+// Corners of rectangle light triangle `which` (0: p1 p2 p3, 1: p3 p4 p1), as
+// rect_hit builds them.
+DI void rect_tri(const GScene &S, const GInstance &in, float time, uint32_t which, V3 &a, V3 &b, V3 &c) {
+    const GLight L = S.lights[in.obj];
+    float w = light_dim(S, L, 0, time), h = light_dim(S, L, 1, time);
+    Xf si = xf_inverse(instance_xf_at(S, in, time));
+    V3 p1, p2, p3, p4;
+    rect_corners(w, h, si, &p1, &p2, &p3, &p4);
+    if (which == 0) { a = p1; b = p2; c = p3; }
+    else { a = p3; b = p4; c = p1; }
+}
+
+// The world-level ray of Tracer::trace (update_local with the identity):
+// the same arithmetic as transforming by the identity matrix.
+DI V3 world_origin(V3 o) { return xf_point(o, xf_identity()); }
+DI V3 world_dir_inv(V3 d) { return recip(xf_vector(d, xf_identity())); }
+
+// fetch_tri with the instance matrix read from a shared-memory slot (three
+// float4 rows, the layout of Xf).
+DI void fetch_tri_xfm(const GScene &S, uint32_t mts, uint32_t mvb, uint32_t tri, float time, bool xf,
+                      const float4 *xfm, V3 &p0, V3 &p1, V3 &p2) {
+    if (mts == 1) {
+        const float4 *t = S.tris + 3 * (size_t)tri;
+        p0 = v3(__ldg(t)); p1 = v3(__ldg(t + 1)); p2 = v3(__ldg(t + 2));
+    } else {
+        uint4 ix = __ldg(S.tri_idx + tri);
+        const float4 *vb = S.verts + mvb;
+        p0 = lerp_slice_v3(vb + (size_t)ix.x * mts, mts, time);
+        p1 = lerp_slice_v3(vb + (size_t)ix.y * mts, mts, time);
+        p2 = lerp_slice_v3(vb + (size_t)ix.z * mts, mts, time);
+    }
+    if (xf) {
+        float4 a = xfm[0], b = xfm[1], c = xfm[2];
+        Xf mat;
+        mat.m[0] = a.x; mat.m[1] = a.y; mat.m[2] = a.z; mat.m[3] = a.w;
+        mat.m[4] = b.x; mat.m[5] = b.y; mat.m[6] = b.z; mat.m[7] = b.w;
+        mat.m[8] = c.x; mat.m[9] = c.y; mat.m[10] = c.z; mat.m[11] = c.w;
+        p0 = xf_point(p0, mat);
+        p1 = xf_point(p1, mat);
+        p2 = xf_point(p2, mat);
+    }
+}
+
+// Fills the hit record once traversal is done: t is the final max_t (each
+// accepted hit set max_t to its t), and the barycentrics come from repeating
+// the winning triangle test -- the same arithmetic on the same inputs, with
+// an unbounded max_t, which only removes the upper bound the test already
+// passed.  hprim: BVH-order triangle (surface), 0 / 1 (rectangle light
+// triangle) or ~0 (sphere light).
+template <bool STATIC>
+DI void finish_hit(const GScene &S, V3 o, const TriPre &pre, float time, float tmax, uint32_t hkind, uint32_t hprim,
+                   uint32_t hslot, HitRec &hit) {
+    hit.kind = hkind;
+    if (hkind == PSY_HIT_MISS_K) return;
+    hit.slot = hslot;
+    hit.t = tmax;
+    hit.b0 = hit.b1 = hit.b2 = 0.0f;
+    const float inf = __int_as_float(0x7f800000);
+    float t2, b0, b1, b2;
+    const GInstance in = S.instances[hslot];
+    if (hkind == PSY_HIT_SURFACE_K) {
+        hit.prim = hprim;
+        V3 p0, p1, p2;
+        if (STATIC) {  // static, untransformed meshes: pre-gathered triangles
+            const float4 *tp = S.tris + 3 * (size_t)hprim;
+            p0 = v3(__ldg(tp)); p1 = v3(__ldg(tp + 1)); p2 = v3(__ldg(tp + 2));
+        } else {
+            const GMesh M = S.meshes[in.obj];
+            bool xf = in.xc != 0;
+            Xf mat = xf ? instance_mat(S, in, time) : xf_identity();
+            fetch_tri(S, M, hprim, time, xf, mat, p0, p1, p2);
+        }
+        if (tri_intersect(o, pre, inf, p0, p1, p2, t2, b0, b1, b2)) { hit.b0 = b0; hit.b1 = b1; hit.b2 = b2; }
+    } else if (hprim == 0xFFFFFFFFu) {
+        hit.prim = 0;  // sphere light
+    } else {
+        hit.prim = hprim;
+        V3 a, b, c;
+        rect_tri(S, in, time, hprim, a, b, c);
+        if (tri_intersect(o, pre, inf, a, b, c, t2, b0, b1, b2)) { hit.b0 = b0; hit.b1 = b1; hit.b2 = b2; }
+    }
+}
+
+// Trace one ray.  `occl`: any-hit (shadow ray).  Returns false on stack
+// overflow (the scene needs a deeper stack than STACK).
+// Traversal work counters (ray x node tests and ray x triangle tests).
+struct TraceCount {
+    uint32_t nodes, tris;
+};
+
+// Copies the traversal table into shared memory (per-lane indexed reads of
+// __constant__ memory would serialize across the warp).
+DI void load_traversal_table(uint8_t *smem) {
+    for (int i = threadIdx.x; i < 8 * 48; i += blockDim.x) smem[i] = (&c_traversal_table[0][0])[i];
+    __syncthreads();
+}
+
+// The hit keeps only its kind, triangle (or light triangle) and instance
+// while traversing (finish_hit completes it).  Children are pushed through
+// the push tables: prow_tab is the per-octant push-row table, lut the
+// entries (load_push_tables).
+template <int STACK, bool COUNT = false>
+DI bool trace_ray(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut, float4 *xfm, V3 o, V3 d, float tmax,
+                  float time, bool occl, HitRec &hit, TraceCount *cnt = nullptr) {
+    hit.kind = PSY_HIT_MISS_K;
+    if (S.top_root == PSY_REF_NONE) return true;
+    // world level: update_local(identity); recomputed when leaving an
+    // instance rather than kept
+    V3 lo = world_origin(o), ldi = world_dir_inv(d);
+    uint32_t oct = ray_code(ldi);
+    const uint8_t *prow = prow_tab + 48 * oct;
+    // slab_safe holds for the whole ray in a space (tmax only shrinks to a finite t)
+    bool safe = S.ordered_slabs && slab_safe(lo, ldi, tmax);
+    // 3 spare entries take the unconditional stores of the child push
+    uint32_t stack[STACK + 4];
+    int sp = 0;
+    uint32_t cur = S.top_root;
+    bool in_inst = false;
+    uint32_t slot = 0, hkind = PSY_HIT_MISS_K, hprim = 0, hslot = 0;
+    uint32_t mts = 1, mvb = 0;  // entered mesh: vertex time samples and first vertex
+    bool has_xf = false;
+    TriPre pre = tri_precompute(d);
+    while (true) {
+        // descend internal nodes
+        while (!psy_is_leaf(cur)) {
+            uint32_t code, count;
+            uint4 ch;
+            uint32_t m = S.use_fp16 ? node_hits_h(S, cur, lo, ldi, tmax, time, oct, safe, code, count, ch)
+                                    : node_hits(S, cur, lo, ldi, tmax, time, oct, safe, code, count, ch);
+            (void)count;
+            if (COUNT) cnt->nodes++;
+            // children in the table's front-to-back order: descend into the
+            // first hit child, push the others (deepest first); three
+            // unconditional stores, of which np are kept
+            uint32_t e = lut[16u * prow[code] + m];
+            if (!(e & 0x800u)) goto pop;
+            int np = (int)((e >> 8) & 7u);
+            if (sp + np > STACK) return false;
+            stack[sp] = sel4(ch, (e >> 2) & 3u);
+            stack[sp + 1] = sel4(ch, (e >> 4) & 3u);
+            stack[sp + 2] = sel4(ch, (e >> 6) & 3u);
+            sp += np;
+            cur = sel4(ch, e & 3u);
+        }
+        // leaf
+        if (!in_inst) {
+            slot = psy_leaf_first(cur);
+            GInstance in = S.instances[slot];
+            if (in.kind == PSY_INST_MESH) {
+                const GMesh mesh = S.meshes[in.obj];
+                mts = mesh.ts;
+                mvb = mesh.vert_base;
+                has_xf = in.xc != 0;
+                if (has_xf) {
+                    Xf x = lerp_slice_xf(S.xforms + 3 * in.xs, in.xc, time);
+                    lo = xf_point(o, x);
+                    ldi = recip(xf_vector(d, x));
+                    // object -> world matrix of the triangles: kept in this
+                    // thread's shared-memory slot, read by each triangle fetch
+                    Xf mat = instance_mat(S, in, time);
+                    xfm[0] = make_float4(mat.m[0], mat.m[1], mat.m[2], mat.m[3]);
+                    xfm[1] = make_float4(mat.m[4], mat.m[5], mat.m[6], mat.m[7]);
+                    xfm[2] = make_float4(mat.m[8], mat.m[9], mat.m[10], mat.m[11]);
+                }
+                if (sp >= STACK) return false;
+                stack[sp++] = PSY_REF_NONE;  // leave-instance marker
+                in_inst = true;
+                oct = ray_code(ldi);
+                prow = prow_tab + 48 * oct;
+                safe = S.ordered_slabs && slab_safe(lo, ldi, tmax);
+                cur = mesh.root;
+                continue;
+            } else if (in.kind == PSY_INST_RECT) {
+                float t, b0, b1, b2;
+                uint32_t which;
+                if (rect_hit(S, in, o, d, tmax, time, t, b0, b1, b2, which)) {
+                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
+                    hkind = PSY_HIT_LIGHT_K; hprim = which; hslot = slot;
+                    tmax = t;
+                }
+            } else {
+                Xf x = instance_xf_at(S, in, time);
+                V3 ol = in.xc ? xf_point(o, x) : lo;  // lo: the world origin at this level
+                float t;
+                if (sphere_hit(S, in, ol, d, tmax, time, t)) {
+                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
+                    hkind = PSY_HIT_LIGHT_K; hprim = 0xFFFFFFFFu; hslot = slot;
+                    tmax = t;
+                }
+            }
+        } else {
+            uint32_t first = psy_leaf_first(cur), ntri = psy_leaf_count(cur);
+            for (uint32_t k = 0; k < ntri; k++) {
+                uint32_t tri = first + k;
+                V3 p0, p1, p2;
+                fetch_tri_xfm(S, mts, mvb, tri, time, has_xf, xfm, p0, p1, p2);
+                float t, b0, b1, b2;
+                if (COUNT) cnt->tris++;
+                if (tri_intersect(o, pre, tmax, p0, p1, p2, t, b0, b1, b2)) {
+                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
+                    hkind = PSY_HIT_SURFACE_K; hprim = tri; hslot = slot;
+                    tmax = t;
+                }
+            }
+        }
+    pop:
+        while (true) {
+            if (sp == 0) goto done;
+            cur = stack[--sp];
+            if (cur != PSY_REF_NONE) break;
+            // leaving the instance: back to world space
+            in_inst = false;
+            lo = world_origin(o);
+            ldi = world_dir_inv(d);
+            oct = ray_code(ldi);
+            prow = prow_tab + 48 * oct;
+            safe = S.ordered_slabs && slab_safe(lo, ldi, tmax);
+        }
+    }
+done:
+    finish_hit<false>(S, o, pre, time, tmax, hkind, hprim, hslot, hit);
+    return true;
+}
+
+// ------------------------------------------------------------------ static-scene traversal
+// Scenes whose meshes are all static and untransformed, whose nodes carry no
+// motion keys and whose child boxes are ordered (GScene::static_fast) take a
+// traversal with a much smaller live state than trace_ray: no local space,
+// no instance matrix, no mesh record, and the hit keeps only its kind,
+// triangle and instance (t is the final max_t; the barycentrics are
+// recomputed once at the end by repeating the winning test, which is
+// deterministic and passes with an unbounded max_t).  Visit order, node and
+// triangle tests and their arithmetic are trace_ray's, so hits are identical.
+//
 // Child hit mask of a static node (no motion keys; the count mask is applied
 // by the push table).  safe: slab_safe holds for the ray (boxes are ordered).
 DI uint32_t node_hits_static(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, uint32_t oct, bool safe,
@@ -458,19 +539,33 @@ DI uint32_t node_hits_static(const GScene &S, uint32_t ni, V3 o, V3 di, float tm
     return m;
 }
 
-// Corners of rectangle light triangle `which` (0: p1 p2 p3, 1: p3 p4 p1), as
-// rect_hit builds them.
-DI void rect_tri(const GScene &S, const GInstance &in, float time, uint32_t which, V3 &a, V3 &b, V3 &c) {
-    const GLight L = S.lights[in.obj];
-    float w = light_dim(S, L, 0, time), h = light_dim(S, L, 1, time);
-    Xf si = xf_inverse(instance_xf_at(S, in, time));
-    V3 p1, p2, p3, p4;
-    rect_corners(w, h, si, &p1, &p2, &p3, &p4);
-    if (which == 0) { a = p1; b = p2; c = p3; }
-    else { a = p3; b = p4; c = p1; }
+// Static-scene triangle leaf: tests its (up to three) triangles.
+DI void static_leaf(const GScene &S, uint32_t leaf, V3 o, const TriPre &pre, uint32_t slot, float &tmax,
+                    uint32_t &hkind, uint32_t &hprim, uint32_t &hslot, bool occl, bool &occluded) {
+    uint32_t first = psy_leaf_first(leaf), ntri = psy_leaf_count(leaf);
+    for (uint32_t k = 0; k < ntri; k++) {
+        uint32_t tri = first + k;
+        const float4 *tp = S.tris + 3 * (size_t)tri;
+        V3 p0 = v3(__ldg(tp)), p1 = v3(__ldg(tp + 1)), p2 = v3(__ldg(tp + 2));
+        float t, b0, b1, b2;
+        if (tri_intersect(o, pre, tmax, p0, p1, p2, t, b0, b1, b2)) {
+            if (occl) { occluded = true; return; }
+            hkind = PSY_HIT_SURFACE_K; hprim = tri; hslot = slot;
+            tmax = t;
+        }
+    }
 }
 
-template <int STACK>
+// SPEC: speculative traversal (Aila & Laine, "Understanding the Efficiency
+// of Ray Traversal on GPUs", 2009): a closest-hit ray that reaches a
+// triangle leaf postpones it and keeps traversing the nodes on its stack
+// while other lanes of the warp are still looking for a leaf, so the warp
+// tests nodes and triangles with more lanes at a time.  The postponed leaf is
+// still tested before everything after it in the visit order; the nodes
+// tested meanwhile use the max_t of before the leaf, so a ray can visit more
+// nodes and triangles than the reference, and the closest hit differs only
+// where a triangle the reference culls lies at exactly the same t (a tie).
+template <int STACK, bool SPEC = false>
 DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut, V3 o, V3 d, float tmax,
                          float time, bool occl, HitRec &hit) {
     hit.kind = PSY_HIT_MISS_K;
@@ -487,22 +582,55 @@ DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_
     bool in_inst = false;
     uint32_t slot = 0, hkind = PSY_HIT_MISS_K, hprim = 0, hslot = 0;
     TriPre pre = tri_precompute(d);
+    const bool spec = SPEC && !occl;  // shadow rays stop at their first hit instead
+    uint32_t pleaf = PSY_REF_NONE;     // postponed triangle leaf (SPEC)
+    bool occluded = false;
     while (true) {
         while (!psy_is_leaf(cur)) {
             uint32_t code;
             uint4 ch;
             uint32_t m = node_hits_static(S, cur, wo, di, tmax, oct, safe, code, ch);
             uint32_t e = lut[16u * prow[code] + m];
-            if (!(e & 0x800u)) goto pop;
-            int np = (int)((e >> 8) & 7u);
-            if (sp + np > STACK) return false;
-            // three unconditional stores (the stack has spare entries); only
-            // np of them are kept
-            stack[sp] = sel4(ch, (e >> 2) & 3u);
-            stack[sp + 1] = sel4(ch, (e >> 4) & 3u);
-            stack[sp + 2] = sel4(ch, (e >> 6) & 3u);
-            sp += np;
-            cur = sel4(ch, e & 3u);
+            if (!(e & 0x800u)) {
+                if (!spec || pleaf == PSY_REF_NONE) goto pop;
+                // speculating: go on only with a node of this mesh on top
+                if (sp > 0 && !psy_is_leaf(stack[sp - 1])) {
+                    cur = stack[--sp];
+                } else {
+                    cur = PSY_REF_NONE;
+                    break;
+                }
+            } else {
+                int np = (int)((e >> 8) & 7u);
+                if (sp + np > STACK) return false;
+                // three unconditional stores (the stack has spare entries);
+                // only np of them are kept
+                stack[sp] = sel4(ch, (e >> 2) & 3u);
+                stack[sp + 1] = sel4(ch, (e >> 4) & 3u);
+                stack[sp + 2] = sel4(ch, (e >> 6) & 3u);
+                sp += np;
+                cur = sel4(ch, e & 3u);
+            }
+            if (spec) {
+                if (in_inst && pleaf == PSY_REF_NONE && psy_is_leaf(cur)) {
+                    pleaf = cur;  // postpone the first triangle leaf
+                    if (sp > 0 && !psy_is_leaf(stack[sp - 1])) {
+                        cur = stack[--sp];
+                    } else {
+                        cur = PSY_REF_NONE;
+                        break;
+                    }
+                }
+                // stop once every lane still here holds a leaf
+                if (!__any_sync(__activemask(), pleaf == PSY_REF_NONE)) break;
+            }
+        }
+        if (SPEC && pleaf != PSY_REF_NONE) {
+            static_leaf(S, pleaf, o, pre, slot, tmax, hkind, hprim, hslot, false, occluded);
+            pleaf = PSY_REF_NONE;
+            if (!psy_is_leaf(cur)) continue;  // stopped by the vote: traverse on from cur
+            if (cur == PSY_REF_NONE) goto pop;
+            // else cur is the next triangle leaf of the same mesh
         }
         if (!in_inst) {
             slot = psy_leaf_first(cur);
@@ -533,18 +661,8 @@ DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_
                 }
             }
         } else {
-            uint32_t first = psy_leaf_first(cur), ntri = psy_leaf_count(cur);
-            for (uint32_t k = 0; k < ntri; k++) {
-                uint32_t tri = first + k;
-                const float4 *tp = S.tris + 3 * (size_t)tri;
-                V3 p0 = v3(__ldg(tp)), p1 = v3(__ldg(tp + 1)), p2 = v3(__ldg(tp + 2));
-                float t, b0, b1, b2;
-                if (tri_intersect(o, pre, tmax, p0, p1, p2, t, b0, b1, b2)) {
-                    if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
-                    hkind = PSY_HIT_SURFACE_K; hprim = tri; hslot = slot;
-                    tmax = t;
-                }
-            }
+            static_leaf(S, cur, o, pre, slot, tmax, hkind, hprim, hslot, occl, occluded);
+            if (occluded) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
         }
     pop:
         while (true) {
@@ -556,26 +674,7 @@ DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_
         }
     }
 done:
-    hit.kind = hkind;
-    if (hkind == PSY_HIT_MISS_K) return true;
-    hit.slot = hslot;
-    hit.t = tmax;
-    hit.b0 = hit.b1 = hit.b2 = 0.0f;
-    const float inf = __int_as_float(0x7f800000);
-    float t2, b0, b1, b2;
-    if (hkind == PSY_HIT_SURFACE_K) {
-        hit.prim = hprim;
-        const float4 *tp = S.tris + 3 * (size_t)hprim;
-        V3 p0 = v3(__ldg(tp)), p1 = v3(__ldg(tp + 1)), p2 = v3(__ldg(tp + 2));
-        if (tri_intersect(o, pre, inf, p0, p1, p2, t2, b0, b1, b2)) { hit.b0 = b0; hit.b1 = b1; hit.b2 = b2; }
-    } else if (hprim == 0xFFFFFFFFu) {
-        hit.prim = 0;  // sphere light
-    } else {
-        hit.prim = hprim;
-        V3 a, b, c;
-        rect_tri(S, S.instances[hslot], time, hprim, a, b, c);
-        if (tri_intersect(o, pre, inf, a, b, c, t2, b0, b1, b2)) { hit.b0 = b0; hit.b1 = b1; hit.b2 = b2; }
-    }
+    finish_hit<true>(S, o, pre, time, tmax, hkind, hprim, hslot, hit);
     return true;
 }
 

@@ -57,6 +57,8 @@ void psy_traversal_table_device(uint8_t t[8][48]);
 // Push tables of the static-scene traversal built from that table (false:
 // more distinct rows than the device table holds).
 bool psy_push_tables_host(uint8_t rows[8][48], uint16_t lut[32][16]);
+// True once the traversal kernels' push tables are on the device.
+bool psy_trace_tables_ready();
 // The traversal translation unit's own copies of its constants (null: skip).
 void psy_upload_trace_constants(const uint8_t table[8][48], const float magenta[3]);
 
@@ -67,7 +69,7 @@ void psy_upload_trace_constants(const uint8_t table[8][48], const float magenta[
 // ray's own index).  fast: as for launch_trace_queue.
 cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order, PsyHit *hits,
                               PsySurfaceHit *full, int stack, int minb, int *d_err, unsigned long long *counters,
-                              cudaStream_t st, bool fast = false);
+                              cudaStream_t st, int fast = 0);
 // Box of the two-point sort keys: the scene box grown on every side by the
 // key length len = 1/20 of the scene box diagonal.
 inline void two_point_box(const GScene &S, float4 &lo, float4 &inv, float &len) {
@@ -109,12 +111,12 @@ cudaError_t launch_trace_packet_queue(const GScene &S, RayBuf R, HitBuf H, const
 cudaError_t launch_trace_packet_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order,
                                      PsyHit *hits, int stack, int *d_err, unsigned long long *counters,
                                      cudaStream_t st);
-// Trace the queued rays of a wave.  fast: the static-scene traversal when the
-// scene allows it (GScene::static_fast) and no counters are requested;
-// minb 6, 8, 10 or 12 there.
+// Trace the queued rays of a wave.  fast: the static-scene traversal (1) or
+// its speculative form (2) when the scene allows it (GScene::static_fast)
+// and no counters are requested; minb 6, 8, 10 or 12 there.
 cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
                                uint32_t max_count, int stack, int minb, int grid, int *d_err,
-                               unsigned long long *counters, cudaStream_t st, bool fast = false);
+                               unsigned long long *counters, cudaStream_t st, int fast = 0);
 // LightPath::next for the queued paths; live paths go to next_queue.
 // minb: register budget for 4 (compiler's choice), 6 or 8 resident blocks.
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,

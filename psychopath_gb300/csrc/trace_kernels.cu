@@ -19,16 +19,17 @@ static bool g_push_tables = false;
 
 // ------------------------------------------------------------------ ray tracing
 // STATIC: the static-scene traversal (trace_ray_static; the scene must have
-// static_fast set, and the launch passes no counters).
-template <int STACK, bool COUNT, int MINB, bool STATIC = false>
+// static_fast set, and the launch passes no counters); SPEC: its speculative
+// form.
+template <int STACK, bool COUNT, int MINB, bool STATIC = false, bool SPEC = false>
 __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay *__restrict__ rays, uint32_t n,
                                                     const uint32_t *__restrict__ order, PsyHit *__restrict__ hits,
                                                     PsySurfaceHit *__restrict__ full, int *err,
                                                     unsigned long long *counters) {
-    __shared__ uint8_t table[8 * 48];
-    __shared__ uint16_t push_lut[STATIC ? PSY_PUSH_ROWS * 16 : 1];
-    if (STATIC) load_push_tables(table, push_lut);
-    else load_traversal_table(table);
+    __shared__ uint8_t table[8 * 48];  // push rows per octant and traversal code
+    __shared__ uint16_t push_lut[PSY_PUSH_ROWS * 16];
+    __shared__ float4 xfm[STATIC ? 1 : 3 * 128];  // instance matrix slot per thread (general traversal)
+    load_push_tables(table, push_lut);
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t i = q;
     TraceCount tc{0, 0};
@@ -40,8 +41,8 @@ __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay
         uint32_t flags = reinterpret_cast<const uint32_t *>(r)[9];
         HitRec h;
         bool oc = (flags & PSY_RAY_OCCLUSION) != 0;
-        bool ok = STATIC ? trace_ray_static<STACK>(S, table, push_lut, o, d, tmax, time, oc, h)
-                         : trace_ray<STACK, COUNT>(S, table, o, d, tmax, time, oc, h, &tc);
+        bool ok = STATIC ? trace_ray_static<STACK, SPEC>(S, table, push_lut, o, d, tmax, time, oc, h)
+                         : trace_ray<STACK, COUNT>(S, table, push_lut, xfm + 3 * threadIdx.x, o, d, tmax, time, oc, h, &tc);
         if (!ok) {
             atomicExch(err, PSY_E_OVERFLOW);
             h.kind = PSY_HIT_MISS_K;
@@ -99,17 +100,21 @@ __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay
 // budget only: node and triangle counts do not depend on the launch shape.
 cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order, PsyHit *hits,
                               PsySurfaceHit *full, int stack, int minb, int *d_err, unsigned long long *counters,
-                              cudaStream_t st, bool fast) {
+                              cudaStream_t st, int fast) {
     if (n == 0) return cudaSuccess;
     dim3 b(128), g((n + 127) / 128);
-    if (fast && g_push_tables && S.static_fast && !counters) {
-#define TF(SZ, MB) k_trace_rays<SZ, false, MB, true><<<g, b, 0, st>>>(S, rays, n, order, hits, full, d_err, nullptr)
-#define TFS(SZ)                          \
-    if (minb >= 12) TF(SZ, 12);          \
-    else if (minb >= 10) TF(SZ, 10);     \
-    else if (minb >= 8) TF(SZ, 8);       \
-    else TF(SZ, 6)
-        if (stack <= 64) { TFS(64); } else { TFS(192); }
+    if (fast && S.static_fast && !counters) {
+#define TF(SZ, MB, SP) k_trace_rays<SZ, false, MB, true, SP><<<g, b, 0, st>>>(S, rays, n, order, hits, full, d_err, nullptr)
+#define TFS(SZ, SP)                          \
+    if (minb >= 12) TF(SZ, 12, SP);          \
+    else if (minb >= 10) TF(SZ, 10, SP);     \
+    else if (minb >= 8) TF(SZ, 8, SP);       \
+    else TF(SZ, 6, SP)
+        if (fast == 2) {
+            if (stack <= 64) { TFS(64, true); } else { TFS(192, true); }
+        } else {
+            if (stack <= 64) { TFS(64, false); } else { TFS(192, false); }
+        }
 #undef TFS
 #undef TF
         return cudaGetLastError();
@@ -378,14 +383,14 @@ cudaError_t launch_trace_packet_rays(const GScene &S, const PsyRay *rays, uint32
 // Queue-driven trace for the render wavefront: a grid-stride loop over the
 // live paths listed in queue[0 .. *count).  COUNT adds the work counters
 // (node visits, triangle tests, rays) into counters[0..2].
-template <int STACK, bool COUNT, int MINB, bool STATIC = false>
+template <int STACK, bool COUNT, int MINB, bool STATIC = false, bool SPEC = false>
 __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
                                                      const uint32_t *__restrict__ count, int *err,
                                                      unsigned long long *counters) {
-    __shared__ uint8_t table[8 * 48];
-    __shared__ uint16_t push_lut[STATIC ? PSY_PUSH_ROWS * 16 : 1];
-    if (STATIC) load_push_tables(table, push_lut);
-    else load_traversal_table(table);
+    __shared__ uint8_t table[8 * 48];  // push rows per octant and traversal code
+    __shared__ uint16_t push_lut[PSY_PUSH_ROWS * 16];
+    __shared__ float4 xfm[STATIC ? 1 : 3 * 128];  // instance matrix slot per thread (general traversal)
+    load_push_tables(table, push_lut);
     uint32_t n = *count;
     TraceCount tc{0, 0};
     uint32_t nr = 0;
@@ -394,8 +399,9 @@ __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, H
         float4 ro = R.o[p], rd = R.d[p];
         HitRec h;
         bool oc = R.occl[p] != 0;
-        bool ok = STATIC ? trace_ray_static<STACK>(S, table, push_lut, v3(ro), v3(rd), ro.w, rd.w, oc, h)
-                         : trace_ray<STACK, COUNT>(S, table, v3(ro), v3(rd), ro.w, rd.w, oc, h, &tc);
+        bool ok = STATIC ? trace_ray_static<STACK, SPEC>(S, table, push_lut, v3(ro), v3(rd), ro.w, rd.w, oc, h)
+                         : trace_ray<STACK, COUNT>(S, table, push_lut, xfm + 3 * threadIdx.x, v3(ro), v3(rd), ro.w, rd.w, oc,
+                                                   h, &tc);
         if (!ok) {
             atomicExch(err, PSY_E_OVERFLOW);
             h.kind = PSY_HIT_MISS_K;
@@ -421,17 +427,21 @@ __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, H
 
 cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
                                uint32_t max_count, int stack, int minb, int grid, int *d_err,
-                               unsigned long long *counters, cudaStream_t st, bool fast) {
+                               unsigned long long *counters, cudaStream_t st, int fast) {
     if (grid <= 0) grid = (int)((max_count + 127) / 128);
     if (grid == 0) return cudaSuccess;
-    if (fast && g_push_tables && S.static_fast && !counters) {
-#define TF(SZ, MB) k_trace_queue<SZ, false, MB, true><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, nullptr)
-#define TFS(SZ)                          \
-    if (minb >= 12) TF(SZ, 12);          \
-    else if (minb >= 10) TF(SZ, 10);     \
-    else if (minb >= 8) TF(SZ, 8);       \
-    else TF(SZ, 6)
-        if (stack <= 64) { TFS(64); } else { TFS(192); }
+    if (fast && S.static_fast && !counters) {
+#define TF(SZ, MB, SP) k_trace_queue<SZ, false, MB, true, SP><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, nullptr)
+#define TFS(SZ, SP)                          \
+    if (minb >= 12) TF(SZ, 12, SP);          \
+    else if (minb >= 10) TF(SZ, 10, SP);     \
+    else if (minb >= 8) TF(SZ, 8, SP);       \
+    else TF(SZ, 6, SP)
+        if (fast == 2) {
+            if (stack <= 64) { TFS(64, true); } else { TFS(192, true); }
+        } else {
+            if (stack <= 64) { TFS(64, false); } else { TFS(192, false); }
+        }
 #undef TFS
 #undef TF
         return cudaGetLastError();
@@ -517,6 +527,8 @@ static bool push_tables_host(const uint8_t table[8][48], uint8_t rows[8][48], ui
         for (int m = 0; m < 16; m++) lut[r][m] = 0;
     return true;
 }
+
+bool psy_trace_tables_ready() { return g_push_tables; }
 
 // The push tables as the device receives them (host-side only; for tests).
 bool psy_push_tables_host(uint8_t rows[8][48], uint16_t lut[32][16]) {

@@ -181,3 +181,18 @@ def test_f32_shading_sphere_lights(gpu_lib):
     assert not (bad_g & ~bad_o).any()
     ok = ~(bad_g | bad_o)
     assert rel_rmse(img[ok], ref[ok]) < 0.01, rel_rmse(img[ok], ref[ok])
+
+
+def test_speculative_traversal_render(gpu_lib):
+    """The speculative traversal's image equals the static-scene traversal's
+    up to tie-broken hits (none expected on this scene at this size)."""
+    s = sc.sphere_small(24, 16, 4, 6, level=3)
+    g = gpu.Scene(s)
+    r = gpu.Renderer(g)
+    g.set_trace(3, 8)
+    a, _ = r.render()
+    g.set_trace(4, 8)
+    b, _ = r.render()
+    rel = np.sqrt(np.mean((a.astype(np.float64) - b) ** 2)) / np.sqrt(np.mean(a.astype(np.float64) ** 2))
+    assert rel < 1e-3
+    g.close()

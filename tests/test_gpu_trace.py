@@ -260,3 +260,34 @@ def test_static_scene_traversal_identical(gpu_lib, minb):
         assert np.array_equal(h2, ref) and np.array_equal(f2, fref)
         g.close()
     assert n_static >= 2  # the grid and the sphere scenes qualify
+
+
+@pytest.mark.parametrize("minb", [8, 10])
+def test_speculative_traversal_differs_only_at_ties(gpu_lib, minb):
+    """The speculative static-scene traversal (trace mode 4) tests the same
+    leaves in the same order plus, at times, nodes and triangles the
+    reference culls after a hit; the closest hit may then differ only where
+    a second triangle lies at exactly the same t.  Shadow rays do not
+    speculate and are identical."""
+    sd, P, F = sc.grid_small(256, 128)
+    rays = np.concatenate([scenes.incoherent_rays(P, F, 1 << 15, seed=7), scenes.coherent_rays(96)])
+    cases = [(sd, rays),
+             (sc.sphere_small(level=4),
+              sc.targeted_rays(20000, [-1.1, -0.1, -1.1], [1.1, 2.1, 1.1], [-4, 0.05, -4], [4, 4, 4], seed=5)),
+             (sc.cornell(), sc.random_rays(20000, [-0.95, 0.05, -0.95], [0.95, 1.95, 0.95], seed=6, occl_frac=0.3))]
+    for sd, rays in cases:
+        g = gpu.Scene(sd)
+        tr = gpu.Tracer(g)
+        g.set_trace(0, 4)
+        ref = tr.trace(rays)
+        g.set_trace(4, minb)
+        h = tr.trace(rays)
+        assert np.array_equal(h["kind"], ref["kind"])
+        occ = (rays["flags"] & abi.PSY_RAY_OCCLUSION) != 0
+        assert np.array_equal(h[occ], ref[occ])
+        diff = h["prim"] != ref["prim"]
+        assert np.array_equal(h["t"][diff], ref["t"][diff])  # only exact ties
+        assert diff.mean() < 1e-3
+        same = ~diff
+        assert np.array_equal(h[same], ref[same])
+        g.close()
