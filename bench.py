@@ -386,7 +386,10 @@ def run_ours(args):
             peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
         except Exception:
             pass
-    traffic = None  # no ncu capture with a known ray count for the frame's trace launches
+    # DRAM traffic of the frame's traversal launches: bytes per traced ray
+    # from an ncu capture of the same launch form on a smaller frame of the
+    # same scene (the committed summary), times this frame's rays
+    traffic = frame_traffic(args.workload, tune, n_rays_c) if not rows_split else None  # bytes per frame
     rows = max(1, tune["wave_paths"] // (W * spp))
     waves = math.ceil(H / rows)
     iters = 2 * sd.max_bounces + 3
@@ -418,9 +421,10 @@ def run_ours(args):
                 "note": "psy_render_image (host XYZ buffer, D2H inside the timed loop); the scene is resident (uploaded "
                         "once at psy_scene_create), so a step has no input upload"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": peak_src, "kernel": "k_trace_queue",
+                     "traffic": traffic, "traffic_per": "frame (all traversal launches of one frame)",
+                     "peak_source": peak_src, "kernel": "k_trace_queue",
                      "per_frame": {"rays": n_rays_c, "node_tests": n_nodes, "tri_tests": n_tris,
-                                   "trace_kernel_s": trace_s / frames}},
+                                   "alg_bytes": alg_bytes_frame, "trace_kernel_s": trace_s / frames}},
         "clocks": clk,
         "gpu_launches": launches_per_frame * args.steps,
     }
@@ -433,6 +437,20 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def frame_traffic(workload, tune, rays):
+    """DRAM bytes (read + write) of a frame's traversal launches: the
+    committed per-ray figure for this workload and launch form, times the
+    rays traced; None without a matching summary."""
+    path = os.path.join(HERE, "profiles", "frame_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    kv = dict(l.split(":", 1) for l in open(path) if ":" in l and not l.startswith("#"))
+    launch = "%d,%d" % (tune.get("trace_mode", -1), tune.get("minb", -1))
+    if kv.get("workload", "").strip() != workload or kv.get("launch", "").strip() != launch:
+        return None
+    return float(kv["dram_bytes_per_ray"]) * rays
 
 
 # ---------------------------------------------------------------- traversal microbenchmark

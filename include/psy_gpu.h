@@ -349,7 +349,9 @@ typedef struct PsyTuneOptions {
 } PsyTuneOptions;
 
 typedef struct PsyTuneResult {
-    uint32_t trace_mode;   /* 0: one thread per ray, 1: persistent, 2: warp packets */
+    uint32_t trace_mode;   /* 0: one thread per ray, 1: persistent, 2: warp packets,
+                              3: static-scene traversal (scenes without motion or mesh
+                              instance transforms), 4: its speculative form */
     uint32_t minb;         /* register budget (resident blocks per SM) */
     uint32_t stack;        /* traversal stack entries */
     uint32_t grid;         /* wavefront kernel grid (0: sized by the queue) */
