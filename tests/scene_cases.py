@@ -23,6 +23,30 @@ def grid_small(nx=64, ny=32):
     return scenes.grid_mesh(nx, ny)
 
 
+def deep_stack(n_obj=24, seed=1):
+    """Objects whose BVHs are as deep as the build allows: each mesh is 60
+    clusters of 8 triangles at geometrically shrinking sizes and spacing, and
+    the objects themselves sit at geometrically shrinking offsets, so the
+    worst-case traversal stack (instance BVH + marker + mesh BVH) exceeds 64
+    entries and the 192-entry kernels run.  Static, untransformed meshes."""
+    rng = np.random.default_rng(seed)
+    s = scenes.SceneData(16, 16, 1, seed, 2)
+    sh = s.add_shader(abi.PSY_SHADER_LAMBERT, (0.7, 0.7, 0.7))
+    for m in range(n_obj):
+        off = np.array([0.0, 3.0 * (1.0 - 1.5 ** (-m)), 0.0])
+        scale = 0.3 * 1.5 ** (-m)
+        P, F = [], []
+        for k in range(60):
+            c, sz = 1.0 - 1.5 ** (-k), 0.2 * 1.5 ** (-k)
+            for _ in range(8):
+                p0 = np.array([c, 0.0, 0.0]) + rng.uniform(-sz, sz, 3)
+                P += [p0, p0 + [sz * 0.3, 0.0, 0.0], p0 + [0.0, sz * 0.3, 0.0]]
+                F.append([len(P) - 3, len(P) - 2, len(P) - 1])
+        s.add_instance(s.add_mesh(np.array(P) * scale + off, np.array(F, dtype=np.uint32)), sh)
+    s.set_camera([scenes.look_at((0.5, 1.5, 6.0), (0.5, 1.5, 0.0))], [50.0])
+    return s
+
+
 def random_rays(n, lo, hi, seed, time_random=False, occl_frac=0.0, max_t=None):
     rng = np.random.default_rng(seed)
     o = rng.uniform(lo, hi, (n, 3)).astype(np.float32)

@@ -291,3 +291,28 @@ def test_speculative_traversal_differs_only_at_ties(gpu_lib, minb):
         same = ~diff
         assert np.array_equal(h[same], ref[same])
         g.close()
+
+
+def test_deep_tree_large_stack_kernels(gpu_lib):
+    """A scene whose worst-case stack needs the 192-entry kernels: hits agree
+    with the oracle, and the general and static-scene kernels at every
+    register budget return identical hits."""
+    s = sc.deep_stack()
+    # rays from random origins toward random triangles' centroids
+    rng = np.random.default_rng(12)
+    cents = np.concatenate([od["verts"][0][od["indices"]].mean(axis=1) for od in s.objects])
+    tgt = cents[rng.integers(0, len(cents), 20000)]
+    org = rng.uniform([-1, -1, 2], [2, 4, 4], (20000, 3))
+    rays = scenes.rays_array(org.astype(np.float32), (tgt - org).astype(np.float32))
+    rays["flags"][::4] = abi.PSY_RAY_OCCLUSION
+    hg, ho, _, _ = _run(s, rays)
+    _assert_parity(sc.compare_hits(hg, ho), 2000)
+    g = gpu.Scene(s)
+    assert g.info()["stack_variant"] == 192 and g.flags()["static_fast"]
+    tr = gpu.Tracer(g)
+    g.set_trace(0, 4)
+    ref = tr.trace(rays)
+    for mode, minb in [(0, 8), (3, 6), (3, 8), (3, 10), (3, 12), (1, 8)]:
+        g.set_trace(mode, minb)
+        assert np.array_equal(tr.trace(rays), ref), (mode, minb)
+    g.close()

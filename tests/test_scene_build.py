@@ -56,3 +56,10 @@ def test_gpu_bvh_needs_a_device(gpu_lib):
     nc, ms = C.c_uint32(), C.c_uint32()
     rc = gpu_lib.psy_debug_host_build(C.byref(desc), C.byref(opts), 0, order.ctypes.data, C.byref(nc), C.byref(ms))
     assert rc == abi.PSY_E_UNSUPPORTED
+
+
+def test_deep_scene_needs_the_large_stack(gpu_lib):
+    """The deep test scene's worst-case stack exceeds 64 entries, so its GPU
+    traces run the 192-entry kernels."""
+    _, _, max_stack = gpu.host_build_info(sc.deep_stack(), 0)
+    assert 64 < max_stack <= 192
