@@ -247,18 +247,26 @@ DI bool sphere_hit(const GScene &S, const GInstance &in, V3 ol, V3 d, float tmax
 }
 
 // Child push by table: for each (ray octant, traversal code) a push row
-// (c_push_row) and for each row and 4-bit hit mask a 16-bit entry
-// (c_push_lut): bits 0-1 the child to descend into, bits 2-7 up to three
+// (g_push_row) and for each row and 4-bit hit mask a 16-bit entry
+// (g_push_lut): bits 0-1 the child to descend into, bits 2-7 up to three
 // children to push (deepest first), bits 8-10 how many, bit 11 set when any
 // child was hit.  The entries follow the traversal table's front-to-back
 // order and ignore mask bits past the node's child count.
 #define PSY_PUSH_ROWS 32
-static __constant__ uint8_t c_push_row[8][48];
-static __constant__ uint16_t c_push_lut[PSY_PUSH_ROWS][16];
+// Global memory (not __constant__): every block copies them with one
+// coalesced 16-byte load per thread, where per-lane indexed reads of
+// constant memory would be serialized across the warp.
+static __device__ __align__(16) uint8_t g_push_row[8 * 48];
+static __device__ __align__(16) uint16_t g_push_lut[PSY_PUSH_ROWS * 16];
 
+// Shared-memory copies of the push tables (row: 384 bytes, lut: 1 KB; both
+// 16-byte aligned); blocks of at least 88 threads.
 DI void load_push_tables(uint8_t *row, uint16_t *lut) {
-    for (int i = threadIdx.x; i < 8 * 48; i += blockDim.x) row[i] = (&c_push_row[0][0])[i];
-    for (int i = threadIdx.x; i < PSY_PUSH_ROWS * 16; i += blockDim.x) lut[i] = (&c_push_lut[0][0])[i];
+    int t = threadIdx.x;
+    if (t < 24)
+        reinterpret_cast<uint4 *>(row)[t] = reinterpret_cast<const uint4 *>(g_push_row)[t];
+    else if (t < 24 + 64)
+        reinterpret_cast<uint4 *>(lut)[t - 24] = reinterpret_cast<const uint4 *>(g_push_lut)[t - 24];
     __syncthreads();
 }
 

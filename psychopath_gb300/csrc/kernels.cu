@@ -120,6 +120,9 @@ template <class RT>
 __global__ void k_camera(GScene S, const WaveDesc *__restrict__ gwave, PathState P, RayBuf R, uint32_t *queue,
                          uint32_t *count) {
     __shared__ WaveDesc wdesc;
+    // blocks past the wave's paths (the grid covers its capacity) leave
+    // before the descriptor copy; block 0 always stays to write the count
+    if (blockIdx.x > 0 && blockIdx.x * blockDim.x >= gwave->npaths) return;
     load_wave(gwave, wdesc);
     uint32_t n = wdesc.npaths;
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -199,8 +202,11 @@ __global__ void __launch_bounds__(128, MINB) k_shade(GScene S, const WaveDesc *_
                                                const uint32_t *__restrict__ count, uint32_t *next_queue,
                                                uint32_t *next_count) {
     __shared__ WaveDesc wdesc;
-    load_wave(gwave, wdesc);
     uint32_t n = *count;
+    // blocks past the queue's length (the grid covers the wave's capacity)
+    // leave at once, before the descriptor copy and its barrier
+    if (blockIdx.x * blockDim.x >= n) return;
+    load_wave(gwave, wdesc);
     uint32_t stride = gridDim.x * blockDim.x;
     uint32_t nloop = (n + stride - 1) / stride * stride;  // keep whole warps in the loop for the ballot
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nloop; q += stride) {
@@ -466,6 +472,7 @@ cudaError_t launch_queue_binning(const GScene &S, RayBuf R, const uint32_t *queu
 // summing the pixel's samples in sample order.
 __global__ void k_accumulate(GScene S, const WaveDesc *__restrict__ gwave, PathState P) {
     __shared__ WaveDesc wdesc;
+    if (blockIdx.x * blockDim.x >= gwave->npix) return;  // past the wave's pixels, before the copy
     load_wave(gwave, wdesc);
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= wdesc.npix) return;

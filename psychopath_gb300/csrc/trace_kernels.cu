@@ -26,9 +26,10 @@ __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay
                                                     const uint32_t *__restrict__ order, PsyHit *__restrict__ hits,
                                                     PsySurfaceHit *__restrict__ full, int *err,
                                                     unsigned long long *counters) {
-    __shared__ uint8_t table[8 * 48];  // push rows per octant and traversal code
-    __shared__ uint16_t push_lut[PSY_PUSH_ROWS * 16];
+    __shared__ __align__(16) uint8_t table[8 * 48];  // push rows per octant and traversal code
+    __shared__ __align__(16) uint16_t push_lut[PSY_PUSH_ROWS * 16];
     __shared__ float4 xfm[STATIC ? 1 : 3 * 128];  // instance matrix slot per thread (general traversal)
+    if (blockIdx.x * blockDim.x >= n) return;  // (whole block: before the table barrier)
     load_push_tables(table, push_lut);
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t i = q;
@@ -387,11 +388,14 @@ template <int STACK, bool COUNT, int MINB, bool STATIC = false, bool SPEC = fals
 __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
                                                      const uint32_t *__restrict__ count, int *err,
                                                      unsigned long long *counters) {
-    __shared__ uint8_t table[8 * 48];  // push rows per octant and traversal code
-    __shared__ uint16_t push_lut[PSY_PUSH_ROWS * 16];
+    __shared__ __align__(16) uint8_t table[8 * 48];  // push rows per octant and traversal code
+    __shared__ __align__(16) uint16_t push_lut[PSY_PUSH_ROWS * 16];
     __shared__ float4 xfm[STATIC ? 1 : 3 * 128];  // instance matrix slot per thread (general traversal)
-    load_push_tables(table, push_lut);
     uint32_t n = *count;
+    // blocks past the queue's length (the grid covers the wave's capacity)
+    // leave at once, before the table copy and its barrier
+    if (blockIdx.x * blockDim.x >= n) return;
+    load_push_tables(table, push_lut);
     TraceCount tc{0, 0};
     uint32_t nr = 0;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
@@ -545,8 +549,8 @@ void psy_upload_trace_constants(const uint8_t table[8][48], const float magenta[
         cudaMemcpyToSymbol(c_traversal_table, table, 8 * 48);
         uint8_t rows[8][48];
         uint16_t lut[PSY_PUSH_ROWS][16];
-        if (push_tables_host(table, rows, lut) && cudaMemcpyToSymbol(c_push_row, rows, sizeof(rows)) == cudaSuccess &&
-            cudaMemcpyToSymbol(c_push_lut, lut, sizeof(lut)) == cudaSuccess)
+        if (push_tables_host(table, rows, lut) && cudaMemcpyToSymbol(g_push_row, rows, sizeof(rows)) == cudaSuccess &&
+            cudaMemcpyToSymbol(g_push_lut, lut, sizeof(lut)) == cudaSuccess)
             g_push_tables = true;
     }
     if (magenta) {
