@@ -299,6 +299,16 @@ int psy_render_image(PsyScene *scene, const uint32_t *crop, float *xyz_out,
  * stream); both buffers are device memory. */
 int psy_xyz_to_srgb8(const float *d_xyz, uint32_t width, uint32_t height, uint8_t *d_rgba, void *stream);
 
+/* Halton sample generation, replacing halton::sample(index, dimension) of
+ * sub_crates/halton (src/lib.rs includes the code build.rs:101-225
+ * generates): Halton points with Faure digit permutations in the first 128
+ * prime bases, bit-exact.  d_out[i] = sample(d_indices[i], dimension) for
+ * i < n (both device buffers), on `stream` (NULL: the legacy default
+ * stream).  dimension >= 128 returns PSY_E_INVALID (the reference panics).
+ * The first call on a device uploads the permutation tables (~80 KB of
+ * device memory, kept until exit). */
+int psy_halton_samples(uint32_t dimension, const uint32_t *d_indices, uint32_t n, float *d_out, void *stream);
+
 /* Render one bucket without allocating device memory.  This call has no
  * counterpart in the reference: it exists for hosts that cannot call
  * cudaMalloc once they are running -- for example a process whose device

@@ -8,7 +8,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libpsy_oracle.so")
-SOURCES = ["psy_oracle.cpp", "oracle_sobol.cpp"]
+SOURCES = ["psy_oracle.cpp", "oracle_sobol.cpp", "oracle_halton.cpp"]
 HEADERS = ["psy_oracle.h", "oracle_math.h", "oracle_shading.h"]
 
 
@@ -82,5 +82,7 @@ def lib():
         L.psyo_quick_select_ints.argtypes = [C.POINTER(C.c_int32), u32, u32]
         L.psyo_increment_ulp_check.restype = C.c_int
         L.psyo_mesh_bvh_info.argtypes = [vp, u32, vp, up]
+        L.psyo_halton_sample.restype = C.c_int
+        L.psyo_halton_sample.argtypes = [u32, u32, fp]
         _lib = L
     return _lib

@@ -78,6 +78,10 @@ int psyo_increment_ulp_check(void);
  * the build (original triangle indices) and the number of BVH4 nodes. */
 int psyo_mesh_bvh_info(PsyoScene *s, uint32_t object, uint32_t *tri_order, uint32_t *node_count);
 
+/* halton::sample(index, dimension) (sub_crates/halton), restated in
+ * oracle_halton.cpp; -1 for dimension >= 128. */
+int psyo_halton_sample(uint32_t index, uint32_t dimension, float *out);
+
 #ifdef __cplusplus
 }
 #endif

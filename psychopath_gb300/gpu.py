@@ -25,7 +25,7 @@ EXPORTED = [
     "psy_rays_traced", "psy_render_bucket", "psy_render_image_device", "psy_render_image", "psy_last_error",
     "psy_version", "psy_render_bucket_noalloc", "psy_server_create", "psy_server_add_scene", "psy_submit",
     "psy_poll", "psy_wait", "psy_cancel", "psy_server_stats", "psy_server_destroy", "psy_autotune",
-    "psy_xyz_to_srgb8",
+    "psy_xyz_to_srgb8", "psy_halton_samples",
 ]
 
 
@@ -81,6 +81,7 @@ def lib(path=None):
     L.psy_server_destroy.argtypes = [vp]
     L.psy_autotune.argtypes = [vp, vp, vp]
     L.psy_xyz_to_srgb8.argtypes = [vp, u32, u32, vp, vp]
+    L.psy_halton_samples.argtypes = [u32, vp, u32, vp, vp]
     _lib = L
     return L
 
@@ -102,6 +103,23 @@ def host_build_info(scene_data, obj, bounds="fp32"):
     nc, ms = C.c_uint32(), C.c_uint32()
     _check(lib().psy_debug_host_build(C.byref(desc), C.byref(opts), obj, order.ctypes.data, C.byref(nc), C.byref(ms)))
     return order[:n], nc.value, ms.value
+
+
+def halton_samples_device(dimension, d_indices_ptr, n, d_out_ptr, stream=None):
+    """psy_halton_samples: halton::sample(index, dimension) for n device-resident
+    u32 indices into n device floats."""
+    _check(lib().psy_halton_samples(dimension, d_indices_ptr, n, d_out_ptr, stream))
+
+
+def halton_samples(dimension, indices):
+    """halton::sample(index, dimension) for a host array of indices, computed on
+    the GPU (device buffers through torch); returns float32 numpy."""
+    import torch
+    idx = torch.from_numpy(np.ascontiguousarray(indices, dtype=np.uint32).view(np.int32)).cuda()
+    out = torch.empty(idx.numel(), dtype=torch.float32, device="cuda")
+    halton_samples_device(dimension, idx.data_ptr(), idx.numel(), out.data_ptr())
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
 
 
 def push_tables():
