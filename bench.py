@@ -60,8 +60,8 @@ def parse_args():
     ap.add_argument("--form", default="both", choices=["both", "plain", "optimized"],
                     help="frame workloads: which forms to time (the headline is the optimized one)")
     ap.add_argument("--launch", default="",
-                    help="optimized form: fixed launch configuration 'mode,minb[,queue binning bits]' instead of "
-                         "psy_autotune (profiling a known configuration)")
+                    help="optimized form: fixed launch configuration 'mode,minb[,queue binning bits[,wave paths]]' "
+                         "instead of psy_autotune (profiling a known configuration)")
     return ap.parse_args()
 
 
@@ -308,9 +308,11 @@ def run_ours(args):
         if args.launch:
             vals = [int(x) for x in args.launch.split(",")]
             mode, minb, bits = vals[0], vals[1], (vals[2] if len(vals) > 2 else 0)
+            wave = vals[3] if len(vals) > 3 else 1 << 24
             scene.set_trace(mode, minb)
             scene.set_sort(bits)
-            tune = {"trace_mode": mode, "minb": minb, "wave_paths": 1 << 24, "sort_bits": bits, "use_graph": 0,
+            scene.set_launch(0, wave)
+            tune = {"trace_mode": mode, "minb": minb, "wave_paths": wave, "sort_bits": bits, "use_graph": 0,
                     "fixed": True}
         else:
             tune = scene.autotune()
