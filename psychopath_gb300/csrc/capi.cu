@@ -917,6 +917,75 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
         TuneCfg c = cur; c.graph = !cur.graph;
         try_set({c});
     }
+    // 7. waves beyond the probe band, timed on the whole image: a larger
+    //    wave pays the late, sparsely filled iterations once for more paths
+    //    (mesh-stress frame: 16M -> 128M paths per wave, 447 -> 483 M
+    //    samples/s).  Sizes whose wave buffers fit in the buffers already
+    //    held plus a quarter of the free device memory; a candidate that
+    //    cannot allocate is skipped.
+    if (err == PSY_OK) {
+        const uint64_t kBytesPerPath = 224;  // ensure_render's buffers per path (185-207 bytes), rounded up
+        uint64_t img = (uint64_t)W * H * spp;
+        size_t fb = 0, tb = 0;
+        cudaMemGetInfo(&fb, &tb);
+        uint64_t budget = (uint64_t)s->cap_paths * kBytesPerPath + fb / 4;
+        std::vector<uint64_t> sizes;
+        for (uint64_t w : {(uint64_t)cur.wave_paths * 2, (uint64_t)cur.wave_paths * 4, img})
+            if (w > cur.wave_paths && w <= img && w * kBytesPerPath <= budget && w <= 0xFFFFFFFFull &&
+                (sizes.empty() || w > sizes.back()))
+                sizes.push_back(w);
+        float *d_full = nullptr;
+        if (!sizes.empty() && cudaMalloc((void **)&d_full, (size_t)W * H * 12) == cudaSuccess) {
+            auto measure_full = [&](const TuneCfg &c, double &out) -> int {
+                set_cfg(s, c);
+                int r = render_region(s, 0, 0, W, H, spp, s->g.seed, d_full, W, st, nullptr);
+                if (r != PSY_OK) return r;
+                double best_t = 1e30;
+                for (uint32_t k = 0; k < 2; k++) {
+                    cudaEventRecord(e0, st);
+                    r = render_region(s, 0, 0, W, H, spp, s->g.seed, d_full, W, st, nullptr);
+                    if (r != PSY_OK) return r;
+                    cudaEventRecord(e1, st);
+                    CK(cudaEventSynchronize(e1), "probe sync");
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    best_t = std::min(best_t, (double)ms * 1e-3);
+                }
+                out = best_t;
+                return PSY_OK;
+            };
+            double base_t = 0.0;
+            if (measure_full(cur, base_t) == PSY_OK) {
+                ncand++;
+                TuneCfg best_c = cur;
+                double best_t = base_t;
+                for (uint64_t w : sizes) {
+                    TuneCfg c = cur;
+                    c.wave_paths = (uint32_t)w;
+                    double t = 0.0;
+                    int r = measure_full(c, t);
+                    ncand++;
+                    if (r != PSY_OK) {  // did not fit after all: keep what was measured
+                        cudaGetLastError();
+                        break;
+                    }
+                    if (t < 0.98 * best_t) {
+                        best_t = t;
+                        best_c = c;
+                    }
+                }
+                cur = best_c;
+            } else {
+                cudaGetLastError();
+            }
+            cudaFree(d_full);
+            set_cfg(s, cur);
+            // release wave buffers larger than the chosen waves need
+            uint64_t need = std::min<uint64_t>(img, (uint64_t)std::max<uint64_t>(1, cur.wave_paths / ((uint64_t)W * spp)) *
+                                                        (uint64_t)W * spp);
+            if ((uint64_t)s->cap_paths > need) free_render(s);
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(d_img);
