@@ -355,7 +355,10 @@ int psy_render_bucket_noalloc(PsyScene *scene, const PsyBucket *bucket, uint32_t
 typedef struct PsyTuneOptions {
     uint32_t probe_paths;  /* 0: 16,777,216 (capped at the whole image) */
     uint32_t repeats;      /* timed probe renders per candidate, best taken (0: 3) */
-    uint32_t reserved[6];
+    uint32_t max_wave_mib; /* cap on the wave buffers the last (whole-image, larger
+                              waves) step may choose, MiB; 0: the buffers already
+                              held plus a quarter of the free device memory */
+    uint32_t reserved[5];
 } PsyTuneOptions;
 
 typedef struct PsyTuneResult {

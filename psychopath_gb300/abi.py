@@ -136,7 +136,8 @@ class PsyServerStats(C.Structure):
 
 
 class PsyTuneOptions(C.Structure):
-    _fields_ = [("probe_paths", C.c_uint32), ("repeats", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+    _fields_ = [("probe_paths", C.c_uint32), ("repeats", C.c_uint32), ("max_wave_mib", C.c_uint32),
+                ("reserved", C.c_uint32 * 5)]
 
 
 class PsyTuneResult(C.Structure):

@@ -921,14 +921,15 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
     //    wave pays the late, sparsely filled iterations once for more paths
     //    (mesh-stress frame: 16M -> 128M paths per wave, 447 -> 483 M
     //    samples/s).  Sizes whose wave buffers fit in the buffers already
-    //    held plus a quarter of the free device memory; a candidate that
-    //    cannot allocate is skipped.
+    //    held plus a quarter of the free device memory (or the caller's
+    //    max_wave_mib); a candidate that cannot allocate ends the step.
     if (err == PSY_OK) {
         const uint64_t kBytesPerPath = 224;  // ensure_render's buffers per path (185-207 bytes), rounded up
         uint64_t img = (uint64_t)W * H * spp;
         size_t fb = 0, tb = 0;
         cudaMemGetInfo(&fb, &tb);
         uint64_t budget = (uint64_t)s->cap_paths * kBytesPerPath + fb / 4;
+        if (opts && opts->max_wave_mib) budget = std::min<uint64_t>(budget, (uint64_t)opts->max_wave_mib << 20);
         std::vector<uint64_t> sizes;
         for (uint64_t w : {(uint64_t)cur.wave_paths * 2, (uint64_t)cur.wave_paths * 4, img})
             if (w > cur.wave_paths && w <= img && w * kBytesPerPath <= budget && w <= 0xFFFFFFFFull &&
@@ -972,6 +973,31 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
                     if (t < 0.98 * best_t) {
                         best_t = t;
                         best_c = c;
+                    }
+                }
+                // with a larger wave, the grid of the wavefront kernels again:
+                // a grid sized by a huge wave spends ~0.5 ms per launch
+                // scheduling blocks that find the late queues empty
+                if (best_c.wave_paths != cur.wave_paths) {
+                    int dev = 0, sms = 152;
+                    cudaGetDevice(&dev);
+                    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                    TuneCfg base_c = best_c;
+                    for (int k : {0, 16, 32, 64}) {
+                        TuneCfg c = base_c;
+                        c.grid = k * sms;
+                        if (c.grid == base_c.grid) continue;
+                        double t = 0.0;
+                        int r = measure_full(c, t);
+                        ncand++;
+                        if (r != PSY_OK) {
+                            cudaGetLastError();
+                            break;
+                        }
+                        if (t < 0.98 * best_t) {
+                            best_t = t;
+                            best_c = c;
+                        }
                     }
                 }
                 cur = best_c;

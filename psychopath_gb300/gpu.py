@@ -212,11 +212,13 @@ class Scene:
     def set_launch(self, grid=0, wave_paths=0):
         _check(lib().psy_debug_set_launch(self.h, grid, wave_paths))
 
-    def autotune(self, probe_paths=0, repeats=0):
+    def autotune(self, probe_paths=0, repeats=0, max_wave_mib=0):
         """psy_autotune: time a probe render under candidate launch
-        configurations and keep the fastest on the scene (images unchanged)."""
+        configurations and keep the fastest on the scene (images unchanged).
+        max_wave_mib caps the wave buffers of the larger-wave step (0: the
+        library's bound)."""
         o = abi.PsyTuneOptions()
-        o.probe_paths, o.repeats = probe_paths, repeats
+        o.probe_paths, o.repeats, o.max_wave_mib = probe_paths, repeats, max_wave_mib
         r = abi.PsyTuneResult()
         _check(lib().psy_autotune(self.h, C.byref(o), C.byref(r)))
         return r.as_dict()

@@ -38,3 +38,21 @@ def test_autotune_keeps_image(gpu_lib, case):
     torch.cuda.synchronize()
     assert np.array_equal(d.cpu().numpy().reshape(before.shape), before)
     g.close()
+
+
+def test_autotune_wave_size_bounded_and_image_unchanged(gpu_lib):
+    """An image larger than the probe band gets the larger-wave step; a
+    caller's max_wave_mib bounds it, and the image is the same bit for bit
+    whatever wave size is chosen (paths are independent)."""
+    s = sc.sphere_small(1024, 1024, 24, 2, level=3)  # 25.2M paths: more than the 16M probe band
+    g = gpu.Scene(s, shading="f32")
+    r = gpu.Renderer(g)
+    g.set_launch(0, 1 << 22)
+    before, _ = r.render()
+    res = g.autotune(repeats=1, max_wave_mib=64)  # no larger wave fits in 64 MiB
+    assert res["wave_paths"] <= 1 << 24
+    res2 = g.autotune(repeats=1)
+    assert res2["wave_paths"] <= 1024 * 1024 * 24
+    after, _ = r.render()
+    assert np.array_equal(before, after)
+    g.close()
