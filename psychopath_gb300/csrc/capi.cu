@@ -958,8 +958,9 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
             double base_t = 0.0;
             if (measure_full(cur, base_t) == PSY_OK) {
                 ncand++;
-                TuneCfg best_c = cur;
-                double best_t = base_t;
+                // the fastest candidate, if it beats the starting point by 2%
+                TuneCfg best_c = cur, fastest_c = cur;
+                double best_t = base_t, fastest_t = base_t;
                 for (uint64_t w : sizes) {
                     TuneCfg c = cur;
                     c.wave_paths = (uint32_t)w;
@@ -970,10 +971,14 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
                         cudaGetLastError();
                         break;
                     }
-                    if (t < 0.98 * best_t) {
-                        best_t = t;
-                        best_c = c;
+                    if (t < fastest_t) {
+                        fastest_t = t;
+                        fastest_c = c;
                     }
+                }
+                if (fastest_t < 0.98 * base_t) {
+                    best_t = fastest_t;
+                    best_c = fastest_c;
                 }
                 // with a larger wave, the grid of the wavefront kernels again:
                 // a grid sized by a huge wave spends ~0.5 ms per launch
@@ -982,7 +987,8 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
                     int dev = 0, sms = 152;
                     cudaGetDevice(&dev);
                     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-                    TuneCfg base_c = best_c;
+                    TuneCfg base_c = best_c, grid_c = best_c;
+                    double base_wt = best_t, grid_t = best_t;
                     for (int k : {0, 16, 32, 64}) {
                         TuneCfg c = base_c;
                         c.grid = k * sms;
@@ -994,10 +1000,14 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
                             cudaGetLastError();
                             break;
                         }
-                        if (t < 0.98 * best_t) {
-                            best_t = t;
-                            best_c = c;
+                        if (t < grid_t) {
+                            grid_t = t;
+                            grid_c = c;
                         }
+                    }
+                    if (grid_t < 0.98 * base_wt) {
+                        best_t = grid_t;
+                        best_c = grid_c;
                     }
                 }
                 cur = best_c;

@@ -220,20 +220,22 @@ __global__ void __launch_bounds__(128, MINB) k_shade(GScene S, const WaveDesc *_
             float2 tw = P.tw[p];
             float time = tw.x, wl = tw.y;
             uint4 ki = H.ki[p];
-            float4 tb = H.tb[p];
-            float4 ro = R.o[p], rd = R.d[p];
-            V3 o = v3(ro), d = v3(rd);
             V4 color = v4(P.color[p]);
             V4 latt = v4(P.latt[p]);
-            float4 nbo = P.nb_o[p];
-            float csp = nbo.w;  // closure_sample_pdf
-            uint32_t seed = P.seed[p];
-            const WaveSeg &w = wdesc.seg[seg_of_path(wdesc, p)];
-            uint32_t lp = p - w.path_begin;
-            uint32_t pix = lp / w.spp;
-            uint32_t si = lp - pix * w.spp;
-            uint32_t px = w.x0 + pix % w.w, py = w.y0 + pix / w.w;
             if (ev == EV_CAMERA || ev == EV_BOUNCE) {
+                // the hit's barycentrics, the ray and the sampling state are
+                // read only here (a shadow-ray result needs none of them)
+                float4 tb = H.tb[p];
+                float4 ro = R.o[p], rd = R.d[p];
+                V3 o = v3(ro), d = v3(rd);
+                float4 nbo = P.nb_o[p];
+                float csp = nbo.w;  // closure_sample_pdf
+                uint32_t seed = P.seed[p];
+                const WaveSeg &w = wdesc.seg[seg_of_path(wdesc, p)];
+                uint32_t lp = p - w.path_begin;
+                uint32_t pix = lp / w.spp;
+                uint32_t si = lp - pix * w.spp;
+                uint32_t px = w.x0 + pix % w.w, py = w.y0 + pix / w.w;
                 if (ki.x == PSY_HIT_SURFACE_K || ki.x == PSY_HIT_LIGHT_K) {
                     HitRec h;
                     h.kind = ki.x; h.prim = ki.y; h.slot = ki.z;
