@@ -980,35 +980,50 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
                     best_t = fastest_t;
                     best_c = fastest_c;
                 }
-                // with a larger wave, the grid of the wavefront kernels again:
-                // a grid sized by a huge wave spends ~0.5 ms per launch
-                // scheduling blocks that find the late queues empty
+                // with a larger wave, the grid of the wavefront kernels and
+                // the queue-ordering key again, on the whole image: a grid
+                // sized by a huge wave spends ~0.5 ms per launch scheduling
+                // blocks that find the late queues empty, and a wave of the
+                // whole frame repays a wider key (mesh stress, one wave:
+                // 13 bits 484, 19 bits 495 M samples/s)
                 if (best_c.wave_paths != cur.wave_paths) {
                     int dev = 0, sms = 152;
                     cudaGetDevice(&dev);
                     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-                    TuneCfg base_c = best_c, grid_c = best_c;
-                    double base_wt = best_t, grid_t = best_t;
+                    auto recheck = [&](const std::vector<TuneCfg> &cands) {
+                        TuneCfg set_c = best_c;
+                        double set_t = best_t;
+                        for (const TuneCfg &c : cands) {
+                            double t = 0.0;
+                            int r = measure_full(c, t);
+                            ncand++;
+                            if (r != PSY_OK) {
+                                cudaGetLastError();
+                                break;
+                            }
+                            if (t < set_t) {
+                                set_t = t;
+                                set_c = c;
+                            }
+                        }
+                        if (set_t < 0.98 * best_t) {
+                            best_t = set_t;
+                            best_c = set_c;
+                        }
+                    };
+                    std::vector<TuneCfg> grids, keys;
                     for (int k : {0, 16, 32, 64}) {
-                        TuneCfg c = base_c;
+                        TuneCfg c = best_c;
                         c.grid = k * sms;
-                        if (c.grid == base_c.grid) continue;
-                        double t = 0.0;
-                        int r = measure_full(c, t);
-                        ncand++;
-                        if (r != PSY_OK) {
-                            cudaGetLastError();
-                            break;
-                        }
-                        if (t < grid_t) {
-                            grid_t = t;
-                            grid_c = c;
-                        }
+                        if (c.grid != best_c.grid) grids.push_back(c);
                     }
-                    if (grid_t < 0.98 * base_wt) {
-                        best_t = grid_t;
-                        best_c = grid_c;
+                    recheck(grids);
+                    for (int b : {10, 13, 16, 19, 25}) {
+                        TuneCfg c = best_c;
+                        c.sort_bits = b;
+                        if (b != best_c.sort_bits) keys.push_back(c);
                     }
+                    recheck(keys);
                 }
                 cur = best_c;
             } else {
