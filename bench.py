@@ -395,7 +395,11 @@ def run_ours(args):
     rows = max(1, tune["wave_paths"] // (W * spp))
     waves = math.ceil(H / rows)
     iters = 2 * sd.max_bounces + 3
-    binning = 3 * (iters - 1) if tune["sort_bits"] else 0  # keys, scan, scatter between iterations
+    # queue ordering between iterations: keys, scan, scatter (counting sort,
+    # <= 16 bits) or keys + three kernels per 8-bit radix pass (wider keys)
+    bits = tune["sort_bits"]
+    per_binning = 0 if not bits else (3 if bits <= 16 else 1 + 3 * ((bits + 7) // 8))
+    binning = per_binning * (iters - 1)
     launches_per_frame = waves * (2 + 2 * iters + binning) + waves  # + the ray-count kernel of stats frames
     line = {
         "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
