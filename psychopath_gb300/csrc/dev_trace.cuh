@@ -358,8 +358,6 @@ DI void finish_hit(const GScene &S, V3 o, const TriPre &pre, float time, float t
     }
 }
 
-// Trace one ray.  `occl`: any-hit (shadow ray).  Returns false on stack
-// overflow (the scene needs a deeper stack than STACK).
 // Traversal work counters (ray x node tests and ray x triangle tests).
 struct TraceCount {
     uint32_t nodes, tris;
@@ -372,10 +370,13 @@ DI void load_traversal_table(uint8_t *smem) {
     __syncthreads();
 }
 
-// The hit keeps only its kind, triangle (or light triangle) and instance
-// while traversing (finish_hit completes it).  Children are pushed through
-// the push tables: prow_tab is the per-octant push-row table, lut the
-// entries (load_push_tables).
+// Trace one ray.  `occl`: any-hit (shadow ray).  Returns false on stack
+// overflow (the scene needs a deeper stack than STACK).  The hit keeps only
+// its kind, triangle (or light triangle) and instance while traversing
+// (finish_hit completes it).  Children are pushed through the push tables:
+// prow_tab is the per-octant push-row table, lut the entries
+// (load_push_tables).  xfm: this thread's three-float4 shared-memory slot
+// for the entered instance's object-to-world matrix.
 template <int STACK, bool COUNT = false>
 DI bool trace_ray(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut, float4 *xfm, V3 o, V3 d, float tmax,
                   float time, bool occl, HitRec &hit, TraceCount *cnt = nullptr) {
