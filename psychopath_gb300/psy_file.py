@@ -26,9 +26,14 @@ older layout -- `Shaders {}` and `Objects {}` sections at Scene level and
 `layout="auto"` accepts them by treating both sections as part of the root
 assembly and applying a mesh's binding to its instances that have none.
 
-Nested assemblies (an Instance of an Assembly) are not flattened: the host
-that owns the scene's assembly hierarchy flattens them before building the
-scene description, and this reader raises PsyFileError for them.
+Nested assemblies are flattened into the one-level description: every
+instance of an object inside instanced assemblies becomes a root instance
+whose transform keys combine those of its enclosing instances as the
+tracer's TransformStack does at trace time, so geometry, transforms and
+shaders are the reference's.  Two things differ from tracing the hierarchy:
+instance ids are renumbered in depth-first order, and lights inside nested
+assemblies join the root light tree, so light selection probabilities (not
+the converged image) differ from the reference's per-assembly light trees.
 """
 import math
 import struct
@@ -416,6 +421,141 @@ class PsyScene:
         self.object_names, self.shader_names = object_names, shader_names
 
 
+# ---------------------------------------------------------------- assemblies
+class _Assembly:
+    """One Assembly section: its shaders, objects and sub-assemblies by name
+    (names are scoped to the assembly, as AssemblyBuilder's maps are,
+    src/scene/assembly.rs:150-300) and its Instance nodes."""
+
+    def __init__(self):
+        self.shaders, self.objects, self.binds, self.assemblies, self.instances = {}, {}, {}, {}, []
+
+
+def _parse_assembly(content, sd, text, layout):
+    """Reads the children of an Assembly (parse_assembly,
+    src/parse/psy_assembly.rs:17-188): shaders, meshes and lights are added
+    to the scene once; sub-assemblies are read into their own scopes and
+    instanced later."""
+    a = _Assembly()
+    for c in content:
+        t = c.type_name
+        if t == "SurfaceShader":
+            if c.is_leaf or c.ident is None:
+                raise PsyFileError("line %d: a SurfaceShader needs a $name and a body" % _line(text, c.offset))
+            a.shaders[c.ident] = sd.add_shader(0)
+            sd.shaders[a.shaders[c.ident]] = _shader(c, text)
+        elif t == "MeshSurface":
+            if c.is_leaf or c.ident is None:
+                raise PsyFileError("line %d: a MeshSurface needs a $name and a body" % _line(text, c.offset))
+            v, n, tr = _mesh(c, text)
+            a.objects[c.ident] = sd.add_mesh(v, tr, n)
+            if layout == "auto" and c.leaves("SurfaceShaderBind"):
+                # older layout: the shader is bound on the object
+                a.binds[c.ident] = c.leaves("SurfaceShaderBind")[0]
+        elif t == "SphereLight":
+            radii = [k[0] for k in _light_keys(c, text, "Radius", 1)]
+            a.objects[c.ident] = sd.add_sphere_light(radii, _colors(c, text))
+        elif t == "RectangleLight":
+            dims = _light_keys(c, text, "Dimensions", 2)
+            a.objects[c.ident] = sd.add_rect_light(dims, _colors(c, text))
+        elif t == "Assembly":
+            if c.is_leaf or c.ident is None:
+                raise PsyFileError("line %d: an Assembly needs a $name and a body" % _line(text, c.offset))
+            a.assemblies[c.ident] = _parse_assembly(list(c.children), sd, text, layout)
+        elif t == "Instance":
+            a.instances.append(c)
+    return a
+
+
+def _instantiate(a, parent_keys, sd, text):
+    """Adds the instances of assembly `a` to the scene with the transform
+    keys of its enclosing instances combined as the tracer's TransformStack
+    does at trace time (src/tracer.rs:96-110, src/transform_stack.rs:33-62):
+    an instance of an object gets the combined keys; an instance of a
+    sub-assembly pushes its keys and instances that assembly's content."""
+    for c in a.instances:
+        data = c.leaves("Data")
+        if len(data) != 1:
+            raise PsyFileError("line %d: an Instance needs exactly one Data" % _line(text, c.offset))
+        name = data[0].contents.strip()
+        if name not in a.objects and name not in a.assemblies:
+            raise PsyFileError("line %d: Instance of unknown data '%s'" % (_line(text, data[0].offset), name))
+        bind = c.leaves("SurfaceShaderBind") or ([a.binds[name]] if name in a.binds else [])
+        shader = -1
+        if bind:
+            sname = bind[0].contents.strip()
+            if sname not in a.shaders:
+                raise PsyFileError("line %d: unknown shader '%s'" % (_line(text, bind[0].offset), sname))
+            shader = a.shaders[sname]
+        keys = merge_transform_keys(parent_keys, [parse_matrix(t.contents, t, text) for t in c.leaves("Transform")])
+        if name in a.objects:
+            sd.add_instance(a.objects[name], shader, keys)
+        else:
+            # the tracer ignores a shader bound on an assembly instance; the
+            # objects inside use their own assembly's bindings
+            _instantiate(a.assemblies[name], keys, sd, text)
+
+
+# ---------------------------------------------------------------- transform keys
+def _f32_3x4(m):
+    return np.asarray(m, dtype=np.float64)[:3, :4].astype(np.float32)
+
+
+def _to4(o):
+    m = np.zeros((4, 4), dtype=np.float64)
+    m[:3, :4] = o
+    m[3, 3] = 1.0
+    return m
+
+
+def xf_mul(a, b):
+    """`a * b` for the reference's Transform (sub_crates/math3d/src/transform.rs:89-96,
+    glam's Affine3A product with b applied after a): rows of b times
+    columns of a, each sum in f32 left to right; 4x4 row-layout matrices."""
+    L, R = _f32_3x4(b), _f32_3x4(a)
+    o = np.zeros((3, 4), dtype=np.float32)
+    for r in range(3):
+        for c in range(3):
+            o[r, c] = (L[r, 0] * R[0, c] + L[r, 1] * R[1, c]) + L[r, 2] * R[2, c]
+        o[r, 3] = ((L[r, 0] * R[0, 3] + L[r, 1] * R[1, 3]) + L[r, 2] * R[2, 3]) + L[r, 3]
+    return _to4(o)
+
+
+def xf_lerp(a, b, alpha):
+    """Transform lerp (src/lerp.rs:109-113): a * (1 - alpha) + b * alpha per element, f32."""
+    alpha = np.float32(alpha)
+    ia = np.float32(1.0) - alpha
+    return _to4(_f32_3x4(a) * ia + _f32_3x4(b) * alpha)
+
+
+def lerp_slice_keys(keys, alpha):
+    """lerp_slice (src/lerp.rs:20-35) over transform keys, f32."""
+    alpha = np.float32(alpha)
+    if len(keys) == 1 or alpha == np.float32(1.0):
+        return keys[-1]
+    tmp = alpha * np.float32(len(keys) - 1)
+    i1 = int(tmp)
+    return xf_lerp(keys[i1], keys[i1 + 1], tmp - np.float32(i1))
+
+
+def merge_transform_keys(parent, child):
+    """TransformStack::push (src/transform_stack.rs:33-62) with
+    merge_slices_to (src/algorithm.rs:266-305): the enclosing keys times the
+    instance's keys, the shorter list lerped at the longer one's key times
+    i / (n - 1).  An empty side leaves the other unchanged."""
+    if not parent:
+        return list(child)
+    if not child:
+        return list(parent)
+    if len(parent) == len(child):
+        return [xf_mul(p, c) for p, c in zip(parent, child)]
+    if len(parent) > len(child):
+        s = np.float32(len(parent) - 1)
+        return [xf_mul(p, lerp_slice_keys(child, np.float32(i) / s)) for i, p in enumerate(parent)]
+    s = np.float32(len(child) - 1)
+    return [xf_mul(lerp_slice_keys(parent, np.float32(i) / s), c) for i, c in enumerate(child)]
+
+
 def load_psy(text, scene_index=0, layout="auto", max_bounces=2):
     """Parse .psy text and return the scene_index-th Scene as a PsyScene.
     max_bounces is the bounce limit of the light paths (the reference
@@ -460,51 +600,9 @@ def load_psy(text, scene_index=0, layout="auto", max_bounces=2):
                 content = list(s.children) + content
     elif layout != "current":
         raise ValueError("layout is 'auto' or 'current'")
-    shader_names, object_names, object_binds = {}, {}, {}
-    instances = []
-    for c in content:
-        t = c.type_name
-        if t == "SurfaceShader":
-            if c.is_leaf or c.ident is None:
-                raise PsyFileError("line %d: a SurfaceShader needs a $name and a body" % _line(text, c.offset))
-            shader_names[c.ident] = sd.add_shader(0)
-            sd.shaders[shader_names[c.ident]] = _shader(c, text)
-        elif t == "MeshSurface":
-            if c.is_leaf or c.ident is None:
-                raise PsyFileError("line %d: a MeshSurface needs a $name and a body" % _line(text, c.offset))
-            v, n, tr = _mesh(c, text)
-            object_names[c.ident] = sd.add_mesh(v, tr, n)
-            if layout == "auto" and c.leaves("SurfaceShaderBind"):
-                # older layout: the shader is bound on the object
-                object_binds[c.ident] = c.leaves("SurfaceShaderBind")[0]
-        elif t == "SphereLight":
-            radii = [k[0] for k in _light_keys(c, text, "Radius", 1)]
-            object_names[c.ident] = sd.add_sphere_light(radii, _colors(c, text))
-        elif t == "RectangleLight":
-            dims = _light_keys(c, text, "Dimensions", 2)
-            object_names[c.ident] = sd.add_rect_light(dims, _colors(c, text))
-        elif t == "Assembly":
-            raise PsyFileError("line %d: nested assemblies are flattened by the host, not read here"
-                               % _line(text, c.offset))
-        elif t == "Instance":
-            instances.append(c)
-    for c in instances:
-        data = c.leaves("Data")
-        if len(data) != 1:
-            raise PsyFileError("line %d: an Instance needs exactly one Data" % _line(text, c.offset))
-        name = data[0].contents.strip()
-        if name not in object_names:
-            raise PsyFileError("line %d: Instance of unknown data '%s'" % (_line(text, data[0].offset), name))
-        bind = c.leaves("SurfaceShaderBind") or ([object_binds[name]] if name in object_binds else [])
-        shader = -1
-        if bind:
-            sname = bind[0].contents.strip()
-            if sname not in shader_names:
-                raise PsyFileError("line %d: unknown shader '%s'" % (_line(text, bind[0].offset), sname))
-            shader = shader_names[sname]
-        keys = [parse_matrix(t.contents, t, text) for t in c.leaves("Transform")]
-        sd.add_instance(object_names[name], shader, keys)
-    return PsyScene(sd, scene.ident, p[1:-1], object_names, shader_names)
+    root = _parse_assembly(content, sd, text, layout)
+    _instantiate(root, [], sd, text)
+    return PsyScene(sd, scene.ident, p[1:-1], root.objects, root.shaders)
 
 
 def load_psy_file(path, **kw):
