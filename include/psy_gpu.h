@@ -339,19 +339,25 @@ int psy_render_bucket_noalloc(PsyScene *scene, const PsyBucket *bucket, uint32_t
  * full-width rows in the middle of the scene's image with about probe_paths
  * paths (all samples of each pixel).  Coordinate descent over, in order: the
  * trace kernel (one thread per ray with a register budget of 4, 5, 6 or 8
- * resident blocks per SM, or persistent with lane refill at 4, 6 or 8),
- * the shading kernel's register budget (4, 6 or 8 blocks per SM),
- * the traversal stack depth (64 or 192 entries, if the scene fits),
- * the queue tile (grid of the wavefront kernels: sized by the queue, or a
- * grid-stride grid of 8, 16 or 32 blocks per SM), the key width of the
- * queue binning between wavefront iterations (0 = off, 4 = occlusion flag
- * and direction octant, 10 / 13 / 16 = also 2 / 3 / 4 bits per axis of the
- * origin's cell), the wave size (paths per wave) and CUDA graph replay.
- * A candidate replaces the current choice only when its probe time is at
- * least 2% lower.  Every candidate renders the same image bit for bit (only
- * scheduling changes), so tuning never changes results.  The chosen
- * configuration stays on the scene.  No counterpart in the reference (its renderer has no GPU
- * launch parameters). */
+ * resident blocks per SM, persistent with lane refill at 4, 6 or 8, or --
+ * on scenes without motion or mesh instance transforms -- the static-scene
+ * traversal at 8, 10 or 12), the shading kernel's register budget (4, 6 or
+ * 8 blocks per SM), the traversal stack depth (64 or 192 entries, if the
+ * scene fits), the queue tile (grid of the wavefront kernels: sized by the
+ * queue, or a grid-stride grid of 8, 16 or 32 blocks per SM), the key width
+ * of the queue binning between wavefront iterations (0 = off, 4 = occlusion
+ * flag and direction octant, 10 / 13 / 16 = also 2 / 3 / 4 bits per axis of
+ * the origin's cell, 19 / 25 = occlusion flag above a two-point key, radix
+ * sorted), the wave size (paths per wave) and CUDA graph replay; the
+ * fastest candidate of each set replaces the current choice when its probe
+ * time is at least 2% lower.  A last step times the whole image with larger
+ * waves (twice, four times the chosen one, the whole image), bounded by
+ * max_wave_mib or by the buffers already held plus a quarter of the free
+ * device memory; when the wave grows, the grid and the key width are timed
+ * again on the whole image.  Every candidate renders the same image bit for
+ * bit (only scheduling changes), so tuning never changes results.  The
+ * chosen configuration stays on the scene.  No counterpart in the reference
+ * (its renderer has no GPU launch parameters). */
 typedef struct PsyTuneOptions {
     uint32_t probe_paths;  /* 0: 16,777,216 (capped at the whole image) */
     uint32_t repeats;      /* timed probe renders per candidate, best taken (0: 3) */
