@@ -1107,6 +1107,21 @@ int psy_debug_host_build(const PsySceneDesc *desc, const PsySceneOptions *opts, 
     if (node_count) *node_count = hs.mesh_node_count[m];
     return PSY_OK;
 }
+// Host-side build only (no device): the whole scene's BVH4 nodes (128 bytes
+// each) and motion bounds (96 bytes per key), built with worker threads or
+// on one thread.  With null arrays only the counts are returned.
+int psy_debug_host_nodes(const PsySceneDesc *desc, const PsySceneOptions *opts, int serial, void *nodes,
+                         uint32_t *node_count, void *bounds_ext, uint32_t *ext_count) {
+    HostScene hs;
+    std::string err;
+    int rc = build_host_scene(desc, opts, hs, err, nullptr, serial != 0);
+    if (rc != PSY_OK) return fail(rc, err);
+    if (node_count) *node_count = (uint32_t)hs.nodes.size();
+    if (ext_count) *ext_count = (uint32_t)hs.bounds_ext.size();
+    if (nodes) std::memcpy(nodes, hs.nodes.data(), hs.nodes.size() * sizeof(GNode));
+    if (bounds_ext) std::memcpy(bounds_ext, hs.bounds_ext.data(), hs.bounds_ext.size() * sizeof(GBounds4));
+    return PSY_OK;
+}
 int psy_debug_scene_info(PsyScene *s, uint32_t *max_stack, uint32_t *nodes, uint32_t *stack_variant) {
     if (!s) return fail(PSY_E_INVALID, "null");
     if (max_stack) *max_stack = s->max_stack;

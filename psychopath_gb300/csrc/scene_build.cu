@@ -13,7 +13,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <functional>
+#include <thread>
 
 #include "scene_build.h"
 
@@ -166,9 +168,46 @@ struct Base {
     std::vector<Node> nodes;
     std::vector<BB> bounds;
     const BoundsFn &bf;
-    explicit Base(const BoundsFn &f) : bf(f) {}
+    std::vector<BB> midc;  // each object's box at time 0.5 by id (prepare())
+    const std::vector<BB> *midc_ref = nullptr;  // a worker's view of its parent build's cache
+    bool serial = false;                        // no worker threads
+    explicit Base(const BoundsFn &f, bool serial_build = false) : bf(f), serial(serial_build) {}
+    // subtrees of at least kParallelMin objects above depth kParallelDepth
+    // are built on two threads (up to 2^kParallelDepth at once)
+    static constexpr size_t kParallelDepth = 4, kParallelMin = 1u << 15;
 
-    BB mid(uint32_t id) const { Bounds b = bf(id); return bb_lerp_slice(b.p, b.n, 0.5f); }
+    // Appends another build's nodes and bounds (indices shifted); returns
+    // the index of its root here.
+    uint32_t splice(const Base &o, uint32_t root) {
+        uint32_t nb = (uint32_t)nodes.size(), bb = (uint32_t)bounds.size();
+        bounds.insert(bounds.end(), o.bounds.begin(), o.bounds.end());
+        for (Node n : o.nodes) {
+            n.b0 += bb;
+            n.b1 += bb;
+            if (!n.leaf) {
+                n.c0 += nb;
+                n.c1 += nb;
+            }
+            nodes.push_back(n);
+        }
+        return root + nb;
+    }
+
+    // Caches the time-0.5 boxes of objects 0..n-1, which every split of the
+    // build evaluates again (the same values: a cache, not a change).
+    void prepare(uint32_t n) {
+        midc.resize(n);
+        for (uint32_t i = 0; i < n; i++) {
+            Bounds b = bf(i);
+            midc[i] = bb_lerp_slice(b.p, b.n, 0.5f);
+        }
+    }
+    BB mid(uint32_t id) const {
+        const std::vector<BB> &c = midc_ref ? *midc_ref : midc;
+        if (id < c.size()) return c[id];
+        Bounds b = bf(id);
+        return bb_lerp_slice(b.p, b.n, 0.5f);
+    }
 
     template <class P>
     static size_t partition(uint32_t *s, size_t len, P pred) {
@@ -203,18 +242,46 @@ struct Base {
             float ext = cb.mx[d] - cb.mn[d];
             for (int v = 0; v < NB - 1; v++) divs[d][v] = cb.mn[d] + ext * ((float)(v + 1) / (float)NB);
         }
-        BB bl[3][NB - 1], br[3][NB - 1];
-        size_t cl[3][NB - 1] = {}, cr[3][NB - 1] = {};
+        // Split v of axis d puts an object left when its centroid c <= divs[d][v]
+        // (src/accel/objects_split.rs:166-198).  The divisions do not decrease
+        // with v, so an object is left exactly for v >= its bin (the first v
+        // with c <= divs[d][v]; NB - 1 when none, NaN included): bin boxes
+        // and counts, then prefix / suffix unions give every split's sides.
+        // Box union is min / max, exact, so the sides equal the one-object-
+        // at-a-time unions (up to the sign of a zero, which no cost
+        // comparison sees).
+        BB binb[3][NB];
+        size_t binc[3][NB] = {};
         for (int d = 0; d < 3; d++)
-            for (int v = 0; v < NB - 1; v++) { bl[d][v] = bb_empty(); br[d][v] = bb_empty(); }
+            for (int k = 0; k < NB; k++) binb[d][k] = bb_empty();
         for (size_t i = 0; i < len; i++) {
             const BB &b = mids[i];
             for (int d = 0; d < 3; d++) {
                 float c = (b.mn[d] + b.mx[d]) * 0.5f;
-                for (int v = 0; v < NB - 1; v++) {
-                    if (c <= divs[d][v]) { bl[d][v] = bb_or(bl[d][v], b); cl[d][v]++; }
-                    else { br[d][v] = bb_or(br[d][v], b); cr[d][v]++; }
-                }
+                int k = 0;
+                while (k < NB - 1 && !(c <= divs[d][k])) k++;
+                binb[d][k] = bb_or(binb[d][k], b);
+                binc[d][k]++;
+            }
+        }
+        BB bl[3][NB - 1], br[3][NB - 1];
+        size_t cl[3][NB - 1] = {}, cr[3][NB - 1] = {};
+        for (int d = 0; d < 3; d++) {
+            BB acc = bb_empty();
+            size_t cnt = 0;
+            for (int v = 0; v < NB - 1; v++) {
+                acc = bb_or(acc, binb[d][v]);
+                cnt += binc[d][v];
+                bl[d][v] = acc;
+                cl[d][v] = cnt;
+            }
+            acc = bb_empty();
+            cnt = 0;
+            for (int v = NB - 2; v >= 0; v--) {
+                acc = bb_or(acc, binb[d][v + 1]);
+                cnt += binc[d][v + 1];
+                br[d][v] = acc;
+                cr[d][v] = cnt;
             }
         }
         int dim = 0;
@@ -312,8 +379,47 @@ struct Base {
         uint64_t lg = 63 - (uint64_t)__builtin_clzll((unsigned long long)len);
         if (lg < (42 - depth)) sah(objs, len, &si, &axis);
         else median(objs, len, &si, &axis);
-        uint32_t c0 = build(offset, depth + 1, per_leaf, objs, si);
-        uint32_t c1 = build(offset + (uint32_t)si, depth + 1, per_leaf, objs + si, len - si);
+        uint32_t c0, c1;
+        if (!serial && depth < kParallelDepth && len - si >= kParallelMin && si >= kParallelMin) {
+            // the right subtree on a worker thread, into its own node and
+            // bounds arrays (the two sides touch disjoint object ranges),
+            // spliced in afterwards: the tree is the same, only its storage
+            // order differs, and the BVH4 collapse follows the child indices
+            Base right(bf);
+            right.midc_ref = midc_ref ? midc_ref : &midc;
+            uint32_t rroot = 0;
+            std::exception_ptr failure;
+            std::thread th;
+            bool threaded = false;
+            try {
+                th = std::thread([&] {
+                    try {
+                        rroot = right.build(offset + (uint32_t)si, depth + 1, per_leaf, objs + si, len - si);
+                    } catch (...) {
+                        failure = std::current_exception();
+                    }
+                });
+                threaded = true;
+            } catch (...) {  // no thread to be had: build both sides here
+            }
+            if (threaded) {
+                try {
+                    c0 = build(offset, depth + 1, per_leaf, objs, si);
+                } catch (...) {
+                    th.join();
+                    throw;
+                }
+                th.join();
+                if (failure) std::rethrow_exception(failure);
+                c1 = splice(right, rroot);
+            } else {
+                c0 = build(offset, depth + 1, per_leaf, objs, si);
+                c1 = build(offset + (uint32_t)si, depth + 1, per_leaf, objs + si, len - si);
+            }
+        } else {
+            c0 = build(offset, depth + 1, per_leaf, objs, si);
+            c1 = build(offset + (uint32_t)si, depth + 1, per_leaf, objs + si, len - si);
+        }
         std::vector<BB> merged;
         merge(&bounds[nodes[c0].b0], nodes[c0].b1 - nodes[c0].b0, &bounds[nodes[c1].b0], nodes[c1].b1 - nodes[c1].b0, merged);
         uint32_t b0 = (uint32_t)bounds.size();
@@ -515,7 +621,7 @@ static uint32_t node_maxpush(const std::vector<GNode> &nodes, uint32_t base, uin
 }
 
 int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostScene &hs, std::string &err,
-                     const GpuMeshBuild *gpu_build) {
+                     const GpuMeshBuild *gpu_build, bool serial) {
     if (!d) { err = "null scene description"; return PSY_E_INVALID; }
     if (d->num_objects && !d->objects) { err = "objects pointer is null"; return PSY_E_INVALID; }
     if (d->num_instances && !d->instances) { err = "instances pointer is null"; return PSY_E_INVALID; }
@@ -602,7 +708,8 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
             bool on_gpu = opts && opts->bvh_build == PSY_BVH_GPU && ts == 1;
             LbvhOutput lb;
             BoundsFn bf = [&](uint32_t t) { return Bounds{&tb[(size_t)t * ts], (size_t)ts}; };
-            Base base(bf);
+            Base base(bf, serial);
+            if (!on_gpu) base.prepare(nt);
             if (on_gpu) {
                 if (!gpu_build) { err = "GPU BVH build needs a CUDA device"; return PSY_E_UNSUPPORTED; }
                 LbvhInput li{od.verts, nv, od.indices, nt, (uint32_t)hs.nodes.size(), (uint32_t)hs.tri_idx.size()};
@@ -711,7 +818,8 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
     uint32_t top_push = 0;
     if (ni > 0) {
         BoundsFn bf = [&](uint32_t i) { return Bounds{ibounds[i].data(), ibounds[i].size()}; };
-        Base base(bf);
+        Base base(bf, serial);
+        base.prepare(ni);
         base.build(0, 0, 1, iorder.data(), ni);
         Collapser col{base, hs, [](uint32_t o0, uint32_t) { return psy_make_leaf(o0, 1); }};
         hs.top_root = col.emit(0, &top_push);
@@ -753,7 +861,8 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
         for (size_t i = 0; i < lights.size(); i++) lord[i] = (uint32_t)i;
         auto lbounds = [&](uint32_t li) -> const std::vector<BB> & { return ibounds[hs.instances[lights[li]].id]; };
         BoundsFn bf = [&](uint32_t li) { const auto &b = lbounds(li); return Bounds{b.data(), b.size()}; };
-        Base splitter(bf);
+        Base splitter(bf, serial);
+        splitter.prepare((uint32_t)lights.size());
         std::function<uint32_t(uint32_t, uint32_t *, size_t)> rb = [&](uint32_t off, uint32_t *o, size_t len) -> uint32_t {
             uint32_t me = (uint32_t)nodes.size();
             if (len == 1) {

@@ -58,8 +58,10 @@ using GpuMeshBuild = std::function<int(const LbvhInput &, LbvhOutput &, std::str
 // PSY_E_* code with a message in `err`.  gpu_build is needed when the
 // options ask for GPU-built mesh BVHs (a host-only build then fails with
 // PSY_E_UNSUPPORTED).
+// serial: build every BVH on the calling thread (large subtrees otherwise go
+// to worker threads; the result is the same).
 int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostScene &hs, std::string &err,
-                     const GpuMeshBuild *gpu_build = nullptr);
+                     const GpuMeshBuild *gpu_build = nullptr, bool serial = false);
 
 // rec709_to_xyz((1, 0, 1)) in the reference's f32 arithmetic (the colour of
 // the tracer's shader for instances that have none).

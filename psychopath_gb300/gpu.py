@@ -71,6 +71,7 @@ def lib(path=None):
     L.psy_debug_render_sized.argtypes = [vp, u32, u32, u32, u32, vp, vp]
     L.psy_debug_push_tables.argtypes = [vp, vp, vp]
     L.psy_debug_scene_flags.argtypes = [vp, C.POINTER(u32)]
+    L.psy_debug_host_nodes.argtypes = [vp, vp, C.c_int, vp, C.POINTER(u32), vp, C.POINTER(u32)]
     L.psy_server_create.argtypes = [vp, C.POINTER(vp)]
     L.psy_server_add_scene.argtypes = [vp, vp, C.POINTER(u32)]
     L.psy_submit.argtypes = [vp, vp, C.POINTER(C.c_uint64)]
@@ -103,6 +104,22 @@ def host_build_info(scene_data, obj, bounds="fp32"):
     nc, ms = C.c_uint32(), C.c_uint32()
     _check(lib().psy_debug_host_build(C.byref(desc), C.byref(opts), obj, order.ctypes.data, C.byref(nc), C.byref(ms)))
     return order[:n], nc.value, ms.value
+
+
+def host_nodes(scene_data, serial=False, bounds="fp32"):
+    """Host-side build only (no GPU needed): the scene's BVH4 node records and
+    motion bounds as raw bytes (128 and 96 bytes per entry)."""
+    desc = scene_data.desc()
+    opts = abi.PsySceneOptions()
+    opts.bounds_precision = abi.PSY_BOUNDS_FP16 if bounds == "fp16" else abi.PSY_BOUNDS_FP32
+    nc, ec = C.c_uint32(), C.c_uint32()
+    _check(lib().psy_debug_host_nodes(C.byref(desc), C.byref(opts), 1 if serial else 0, None, C.byref(nc), None,
+                                      C.byref(ec)))
+    nodes = np.zeros(nc.value * 128, dtype=np.uint8)
+    ext = np.zeros(max(1, ec.value) * 96, dtype=np.uint8)
+    _check(lib().psy_debug_host_nodes(C.byref(desc), C.byref(opts), 1 if serial else 0, nodes.ctypes.data,
+                                      C.byref(nc), ext.ctypes.data, C.byref(ec)))
+    return nodes, ext[:ec.value * 96]
 
 
 def halton_samples_device(dimension, d_indices_ptr, n, d_out_ptr, stream=None):

@@ -63,3 +63,23 @@ def test_deep_scene_needs_the_large_stack(gpu_lib):
     traces run the 192-entry kernels."""
     _, _, max_stack = gpu.host_build_info(sc.deep_stack(), 0)
     assert 64 < max_stack <= 192
+
+
+@pytest.mark.parametrize("case", ["grid", "sphere", "motion", "deep"])
+def test_threaded_bvh_build_equals_serial(gpu_lib, case):
+    """Large subtrees of the host SAH build run on worker threads into their
+    own arrays and are spliced in; the scene's BVH4 nodes and motion bounds
+    must be byte-identical to a build on one thread."""
+    from psychopath_gb300 import scenes
+    if case == "grid":
+        s, _, _ = scenes.grid_mesh(512, 256)  # 262,144 triangles: several threaded levels
+    elif case == "sphere":
+        s = sc.sphere_small(level=7)
+    elif case == "motion":
+        s = sc.motion_small(n=100, level=6)  # the deforming mesh: 81,920 triangles, 3 keys
+    else:
+        s = sc.deep_stack()
+    a_nodes, a_ext = gpu.host_nodes(s)
+    b_nodes, b_ext = gpu.host_nodes(s, serial=True)
+    assert a_nodes.size > 0
+    assert np.array_equal(a_nodes, b_nodes) and np.array_equal(a_ext, b_ext)
