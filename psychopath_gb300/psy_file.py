@@ -429,6 +429,7 @@ class _Assembly:
 
     def __init__(self):
         self.shaders, self.objects, self.binds, self.assemblies, self.instances = {}, {}, {}, {}, []
+        self.defined_at = {}  # object / assembly name -> position of its definition
 
 
 def _parse_assembly(content, sd, text, layout):
@@ -437,8 +438,10 @@ def _parse_assembly(content, sd, text, layout):
     to the scene once; sub-assemblies are read into their own scopes and
     instanced later."""
     a = _Assembly()
-    for c in content:
+    for pos, c in enumerate(content):
         t = c.type_name
+        if t in ("MeshSurface", "SphereLight", "RectangleLight", "Assembly") and c.ident is not None:
+            a.defined_at.setdefault(c.ident, pos)
         if t == "SurfaceShader":
             if c.is_leaf or c.ident is None:
                 raise PsyFileError("line %d: a SurfaceShader needs a $name and a body" % _line(text, c.offset))
@@ -463,7 +466,7 @@ def _parse_assembly(content, sd, text, layout):
                 raise PsyFileError("line %d: an Assembly needs a $name and a body" % _line(text, c.offset))
             a.assemblies[c.ident] = _parse_assembly(list(c.children), sd, text, layout)
         elif t == "Instance":
-            a.instances.append(c)
+            a.instances.append((pos, c))
     return a
 
 
@@ -473,12 +476,14 @@ def _instantiate(a, parent_keys, sd, text):
     does at trace time (src/tracer.rs:96-110, src/transform_stack.rs:33-62):
     an instance of an object gets the combined keys; an instance of a
     sub-assembly pushes its keys and instances that assembly's content."""
-    for c in a.instances:
+    for pos, c in a.instances:
         data = c.leaves("Data")
         if len(data) != 1:
             raise PsyFileError("line %d: an Instance needs exactly one Data" % _line(text, c.offset))
         name = data[0].contents.strip()
-        if name not in a.objects and name not in a.assemblies:
+        # the reference adds an instance when it reads it, so its data must be
+        # defined above it in the same assembly (src/parse/psy_assembly.rs:76-89)
+        if (name not in a.objects and name not in a.assemblies) or a.defined_at.get(name, pos) > pos:
             raise PsyFileError("line %d: Instance of unknown data '%s'" % (_line(text, data[0].offset), name))
         bind = c.leaves("SurfaceShaderBind") or ([a.binds[name]] if name in a.binds else [])
         shader = -1

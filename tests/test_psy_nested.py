@@ -146,8 +146,17 @@ def test_nested_assemblies_flatten():
     sd.desc()
 
 
+_LATE = NESTED.replace(
+    "        Instance { Data [$tri] SurfaceShaderBind [$Red] }\n",
+    "").replace(
+    "        SurfaceShader $Red { Type [Lambert] Color [rec709, 0.8 0.1 0.1] }\n        MeshSurface $tri",
+    "        SurfaceShader $Red { Type [Lambert] Color [rec709, 0.8 0.1 0.1] }\n"
+    "        Instance { Data [$tri] SurfaceShaderBind [$Red] }\n        MeshSurface $tri")
+
+
 @pytest.mark.parametrize("bad,msg", [
     (NESTED.replace("Data [$pair]", "Data [$nothere]"), "unknown data"),
+    (_LATE, "unknown data"),  # instanced above its definition, which the reference rejects
     (NESTED.replace("Instance { Data [$tri] SurfaceShaderBind [$Red] }",
                     "Instance { Data [$quad] }"), "unknown data"),  # $quad is scoped to $cluster
 ])
