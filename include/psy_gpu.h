@@ -276,7 +276,8 @@ typedef struct PsyRenderStats {
 /* Render one bucket: spp samples per pixel with the scene's seed.
  * xyz_out (host) receives bucket.w*bucket.h*3 floats, row-major, the XYZ
  * value each pixel would hold after the reference's accumulation
- * (src/renderer.rs:299-310).  stats may be NULL. */
+ * (src/renderer.rs:299-310).  stats may be NULL.  An empty bucket, spp == 0
+ * or a bucket reaching past the image returns PSY_E_INVALID. */
 int psy_render_bucket(PsyScene *scene, const PsyBucket *bucket, uint32_t spp,
                       uint32_t seed, float *xyz_out, PsyRenderStats *stats);
 
@@ -325,7 +326,9 @@ int psy_halton_samples(uint32_t dimension, const uint32_t *d_indices, uint32_t n
  * the start of each call.  The scene itself must have been created (its
  * geometry upload is the one allocation, made at psy_scene_create).
  * The first call on a device looks up that array's device address, so make
- * the first call before any stream capture.  Every call shares the array:
+ * the first call before any stream capture.  The scene's device (the one
+ * current at psy_scene_create) must be the current device; otherwise the
+ * call returns PSY_E_INVALID.  Every call shares the array:
  * calls that overlap on the GPU (other threads, other streams) race and must
  * be serialised by the caller.  The call runs on `stream` (NULL: the scene's
  * stream) and returns after that stream has finished the bucket. */

@@ -171,7 +171,8 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
     });
     if (!psy_trace_tables_ready()) return fail(PSY_E_CUDA, "traversal push tables were not uploaded");
     PsyScene *s = new PsyScene();
-    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaGetDevice(&s->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete s;
         return fail(PSY_E_CUDA, "cudaStreamCreate failed");
     }
@@ -495,10 +496,11 @@ int alloc_wave_bufs(WaveBufs &B, uint32_t cap, uint32_t cap_waves, bool sorting,
 }
 
 // Render the pixels of region (x0, y0, w, h) of a cam_w x cam_h image into
-// d_xyz (row stride img_w) as a sequence of waves of whole pixel rows.
+// d_xyz (row stride img_w; image pixel (ox, oy) is d_xyz[0]) as a sequence of
+// waves of whole pixel rows.
 int render_region_core(PsyScene *s, const WaveBufs &B, uint32_t rows, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
-                       uint32_t spp, uint32_t seed, float *d_xyz, uint32_t img_w, uint32_t cam_w, uint32_t cam_h,
-                       cudaStream_t st, PsyRenderStats *stats) {
+                       uint32_t spp, uint32_t seed, float *d_xyz, uint32_t img_w, uint32_t ox, uint32_t oy,
+                       uint32_t cam_w, uint32_t cam_h, cudaStream_t st, PsyRenderStats *stats) {
     if (spp == 0 || w == 0 || h == 0) return PSY_OK;
     uint32_t iters = 2 * s->g.max_bounces + 3;
     bool timing = stats != nullptr;
@@ -511,6 +513,7 @@ int render_region_core(PsyScene *s, const WaveBufs &B, uint32_t rows, uint32_t x
         g.spp = spp; g.seed = seed;
         g.img_w = cam_w; g.img_h = cam_h;
         g.out = d_xyz; g.out_stride = img_w;
+        g.out_x0 = ox; g.out_y0 = oy;
         d.nseg = 1; d.npix = g.w * g.h; d.npaths = d.npix * spp;
         waves.push_back(d);
     }
@@ -580,8 +583,8 @@ int render_region_core(PsyScene *s, const WaveBufs &B, uint32_t rows, uint32_t x
 // Render with the scene's own wavefront buffers (allocated on first use,
 // sized for waves of whole pixel rows up to wave_paths paths).
 static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h, uint32_t spp, uint32_t seed,
-                         float *d_xyz, uint32_t img_w, cudaStream_t st, PsyRenderStats *stats, uint32_t cam_w = 0,
-                         uint32_t cam_h = 0) {
+                         float *d_xyz, uint32_t img_w, uint32_t ox, uint32_t oy, cudaStream_t st,
+                         PsyRenderStats *stats, uint32_t cam_w = 0, uint32_t cam_h = 0) {
     if (cam_w == 0) { cam_w = s->g.width; cam_h = s->g.height; }
     if (spp == 0 || w == 0 || h == 0) return PSY_OK;
     uint64_t row_paths = (uint64_t)w * spp;
@@ -614,7 +617,7 @@ static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint
     }
     B.waves = s->d_waves;
     B.cap_waves = s->cap_waves;
-    return render_region_core(s, B, rows, x0, y0, w, h, spp, seed, d_xyz, img_w, cam_w, cam_h, st, stats);
+    return render_region_core(s, B, rows, x0, y0, w, h, spp, seed, d_xyz, img_w, ox, oy, cam_w, cam_h, st, stats);
 }
 
 
@@ -640,12 +643,13 @@ namespace {
 std::mutex g_noalloc_mu;
 void *g_noalloc_ptr[64] = {nullptr};
 
-// Device address of the scratch array on the current device (set up on the
-// first call per device).
-int noalloc_base(unsigned char **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+// Device address of the scratch array on device `dev`, which must be the
+// current device (set up on the first call per device).
+int noalloc_base(int dev, unsigned char **out) {
+    int cur = 0;
+    cudaError_t e = cudaGetDevice(&cur);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (cur != dev) return fail(PSY_E_INVALID, "the scene's device is not the current device");
     if (dev < 0 || dev >= 64) return fail(PSY_E_UNSUPPORTED, "device index beyond 63");
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     if (!g_noalloc_ptr[dev]) {
@@ -670,7 +674,7 @@ extern "C" int psy_render_bucket_noalloc(PsyScene *s, const PsyBucket *b, uint32
         return fail(PSY_E_INVALID, "bucket too large for the no-allocation scratch: w*h*spp must be <= " +
                                        std::to_string(PSY_NOALLOC_MAX_SAMPLES));
     unsigned char *base = nullptr;
-    int r = noalloc_base(&base);
+    int r = noalloc_base(s->device, &base);
     if (r != PSY_OK) return r;
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -699,12 +703,11 @@ extern "C" int psy_render_bucket_noalloc(PsyScene *s, const PsyBucket *b, uint32
     // every call shares the scratch: clear the control block (queue lengths,
     // work counter, error word); the camera kernel writes all path state
     CK(cudaMemsetAsync(ctrl, 0, 1024, st), "clear scratch control block");
-    // the bucket's pixels land at (x - b.x, y - b.y) of a bucket-sized image
-    float *img = d_xyz_out - ((size_t)b->y * b->w + b->x) * 3;
+    // the bucket's pixels land at (x - b.x, y - b.y) of the bucket-sized output
     int sort = s->sort_bits;
     s->sort_bits = 0;
-    r = render_region_core(s, B, b->h, b->x, b->y, b->w, b->h, spp, seed, img, b->w, s->g.width, s->g.height, st,
-                           nullptr);
+    r = render_region_core(s, B, b->h, b->x, b->y, b->w, b->h, spp, seed, d_xyz_out, b->w, b->x, b->y, s->g.width,
+                           s->g.height, st, nullptr);
     s->sort_bits = sort;
     if (r != PSY_OK) return r;
     int h = 0;
@@ -729,7 +732,7 @@ int psy_render_image_device(PsyScene *s, const uint32_t *crop, float *d_xyz, voi
     }
     cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
     if (stats) std::memset(stats, 0, sizeof(*stats));
-    int r = render_region(s, x0, y0, w, h, s->g.spp, s->g.seed, d_xyz, W, st, stats);
+    int r = render_region(s, x0, y0, w, h, s->g.spp, s->g.seed, d_xyz, W, 0, 0, st, stats);
     if (r != PSY_OK) return r;
     if (stats) return check_err(s);
     return PSY_OK;
@@ -758,7 +761,8 @@ int psy_render_image(PsyScene *s, const uint32_t *crop, float *xyz_out, PsyRende
 int psy_render_bucket(PsyScene *s, const PsyBucket *b, uint32_t spp, uint32_t seed, float *xyz_out,
                       PsyRenderStats *stats) {
     if (!s || !b || !xyz_out) return fail(PSY_E_INVALID, "null argument");
-    if (b->w == 0 || b->h == 0 || b->x + b->w > s->g.width || b->y + b->h > s->g.height)
+    if (b->w == 0 || b->h == 0 || spp == 0) return fail(PSY_E_INVALID, "empty bucket or zero spp");
+    if ((uint64_t)b->x + b->w > s->g.width || (uint64_t)b->y + b->h > s->g.height)
         return fail(PSY_E_INVALID, "bucket outside the image");
     std::lock_guard<std::mutex> lk(s->mu);
     size_t bytes = (size_t)b->w * b->h * 3 * sizeof(float);
@@ -769,11 +773,8 @@ int psy_render_bucket(PsyScene *s, const PsyBucket *b, uint32_t spp, uint32_t se
         s->cap_xyz = bytes;
     }
     if (stats) std::memset(stats, 0, sizeof(*stats));
-    // the bucket's pixels land at (x - b.x, y - b.y) of a bucket-sized buffer:
-    // offset the base pointer so the accumulate kernel's image indexing works
-    // with row stride b->w.
-    float *base = s->d_xyz - ((size_t)b->y * b->w + b->x) * 3;
-    int r = render_region(s, b->x, b->y, b->w, b->h, spp, seed, base, b->w, s->stream, stats);
+    // the bucket's pixels land at (x - b.x, y - b.y) of a bucket-sized buffer
+    int r = render_region(s, b->x, b->y, b->w, b->h, spp, seed, s->d_xyz, b->w, b->x, b->y, s->stream, stats);
     if (r != PSY_OK) return r;
     CK(cudaMemcpyAsync(xyz_out, s->d_xyz, bytes, cudaMemcpyDeviceToHost, s->stream), "copy bucket");
     CK(cudaStreamSynchronize(s->stream), "sync");
@@ -823,13 +824,12 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
     // time one configuration: one untimed render, then the best of reps
     auto measure = [&](const TuneCfg &c, double &out) -> int {
         set_cfg(s, c);
-        float *base = d_img - (size_t)y0 * W * 3;
-        int r = render_region(s, 0, y0, W, rows, spp, s->g.seed, base, W, st, nullptr);
+        int r = render_region(s, 0, y0, W, rows, spp, s->g.seed, d_img, W, 0, y0, st, nullptr);
         if (r != PSY_OK) return r;
         double best = 1e30;
         for (uint32_t k = 0; k < reps; k++) {
             cudaEventRecord(e0, st);
-            r = render_region(s, 0, y0, W, rows, spp, s->g.seed, base, W, st, nullptr);
+            r = render_region(s, 0, y0, W, rows, spp, s->g.seed, d_img, W, 0, y0, st, nullptr);
             if (r != PSY_OK) return r;
             cudaEventRecord(e1, st);
             CK(cudaEventSynchronize(e1), "probe sync");
@@ -939,12 +939,12 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
         if (!sizes.empty() && cudaMalloc((void **)&d_full, (size_t)W * H * 12) == cudaSuccess) {
             auto measure_full = [&](const TuneCfg &c, double &out) -> int {
                 set_cfg(s, c);
-                int r = render_region(s, 0, 0, W, H, spp, s->g.seed, d_full, W, st, nullptr);
+                int r = render_region(s, 0, 0, W, H, spp, s->g.seed, d_full, W, 0, 0, st, nullptr);
                 if (r != PSY_OK) return r;
                 double best_t = 1e30;
                 for (uint32_t k = 0; k < 2; k++) {
                     cudaEventRecord(e0, st);
-                    r = render_region(s, 0, 0, W, H, spp, s->g.seed, d_full, W, st, nullptr);
+                    r = render_region(s, 0, 0, W, H, spp, s->g.seed, d_full, W, 0, 0, st, nullptr);
                     if (r != PSY_OK) return r;
                     cudaEventRecord(e1, st);
                     CK(cudaEventSynchronize(e1), "probe sync");
@@ -1201,7 +1201,7 @@ int psy_debug_render_sized(PsyScene *s, uint32_t width, uint32_t height, uint32_
     if (!s || !d_xyz || width == 0 || height == 0 || spp == 0) return fail(PSY_E_INVALID, "invalid argument");
     std::lock_guard<std::mutex> lk(s->mu);
     cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
-    int r = render_region(s, 0, 0, width, height, spp, seed, d_xyz, width, st, nullptr, width, height);
+    int r = render_region(s, 0, 0, width, height, spp, seed, d_xyz, width, 0, 0, st, nullptr, width, height);
     if (r != PSY_OK) return r;
     CK(cudaStreamSynchronize(st), "sync");
     return check_err(s);

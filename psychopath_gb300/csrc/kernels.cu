@@ -488,7 +488,7 @@ __global__ void k_accumulate(GScene S, const WaveDesc *__restrict__ gwave, PathS
         V3 c = xyz_from_spectral(v4(P.color[p]), P.tw[p].y);
         acc = acc + (c / inv);
     }
-    float *o = w.out + ((size_t)y * w.out_stride + x) * 3;
+    float *o = w.out + ((size_t)(y - w.out_y0) * w.out_stride + (x - w.out_x0)) * 3;
     o[0] = acc.x; o[1] = acc.y; o[2] = acc.z;
 }
 

@@ -39,10 +39,12 @@ struct WaveSeg {
     uint32_t x0, y0, w, h;  // pixel rectangle in the segment's image
     uint32_t spp, seed;
     uint32_t img_w, img_h;  // resolution the camera maps (the request's image)
-    float *out;             // XYZ image base of the segment's image
+    float *out;             // XYZ buffer of the segment's pixels
     uint32_t out_stride;    // row stride of `out` in pixels
     uint32_t path_begin;    // first path of the segment in the wave
     uint32_t pix_begin;     // first pixel of the segment in the wave
+    uint32_t out_x0;        // image pixel (out_x0, out_y0) is out[0]
+    uint32_t out_y0;
     uint32_t pad;
 };
 struct WaveDesc {
@@ -159,7 +161,8 @@ struct WaveBufs {
     uint32_t cap_waves;
 };
 // Per-pixel XYZ (sum over samples in sample order / spp) into each segment's
-// image, out[(y * out_stride + x) * 3].  The grid covers max_pix pixels.
+// image, out[((y - out_y0) * out_stride + x - out_x0) * 3].  The grid covers
+// max_pix pixels.
 cudaError_t launch_accumulate(const GScene &S, const WaveDesc *d_wave, uint32_t max_pix, PathState P, cudaStream_t st);
 // 3x3 matrix passed by value to a kernel.
 struct Mat3f {

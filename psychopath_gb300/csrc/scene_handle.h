@@ -45,6 +45,7 @@ struct WaveGraph {
 
 struct PsyScene {
     GScene g{};
+    int device = 0;                      // the device current at psy_scene_create (holds all scene memory)
     std::vector<void *> allocs;
     uint64_t device_bytes = 0;
     cudaStream_t stream = nullptr;

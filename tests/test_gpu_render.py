@@ -79,6 +79,26 @@ def test_render_deterministic_and_bucket(gpu_lib):
     assert not d[:4].any()
 
 
+def test_bucket_rejects_bad_arguments(gpu_lib):
+    """A bucket whose x + w or y + h passes 2^32 (checked in 64 bits), an
+    empty bucket and spp == 0 are rejected before any launch, by both bucket
+    entry points."""
+    import ctypes as C
+    import torch
+    from psychopath_gb300 import abi
+    g = gpu.Scene(sc.cornell(32, 32, 4, 2))
+    out = np.zeros(32 * 32 * 3, dtype=np.float32)
+    d_out = torch.zeros(32 * 32 * 3, dtype=torch.float32, device="cuda")
+    cases = [((0xFFFFFFF0, 0, 32, 8), 4), ((0, 0xFFFFFFF0, 8, 32), 4), ((0, 0, 0, 8), 4), ((0, 0, 8, 8), 0),
+             ((30, 0, 4, 4), 4)]
+    for (x, y, w, h), spp in cases:
+        b = abi.PsyBucket(x, y, w, h)
+        assert gpu_lib.psy_render_bucket(g.h, C.byref(b), spp, 0, out.ctypes.data, None) == abi.PSY_E_INVALID
+        assert gpu_lib.psy_render_bucket_noalloc(g.h, C.byref(b), spp, 0, C.c_void_p(d_out.data_ptr()),
+                                                 None) == abi.PSY_E_INVALID
+    g.close()
+
+
 def test_paths_match_oracle_samples(gpu_lib):
     """Per-sample path colours of one bucket, GPU vs oracle (median relative
     difference 1e-5 or better)."""
