@@ -25,16 +25,16 @@ struct BBox {
 static inline BBox bbox_new() { return BBox{v3(INFINITY, INFINITY, INFINITY), v3(-INFINITY, -INFINITY, -INFINITY)}; }
 static inline BBox bunion(BBox a, BBox b) { return BBox{vmin3(a.min, b.min), vmax3(a.max, b.max)}; }
 static inline BBox bunion_pt(BBox a, V3 p) { return BBox{vmin3(a.min, p), vmax3(a.max, p)}; }
-static inline float surface_area(BBox b) {
+static inline real surface_area(BBox b) {
     V3 d = b.max - b.min;
     return ((d.x * d.y) + (d.y * d.z) + (d.z * d.x)) * 2.0f;
 }
 static inline V3 bcenter(BBox b) { return lerp3(b.min, b.max, 0.5f); }
-static inline float diagonal(BBox b) { return length(b.max - b.min); }
-static inline float diagonal2(BBox b) { return length2(b.max - b.min); }
-static inline BBox blerp(BBox a, BBox b, float alpha) { return BBox{lerp3(a.min, b.min, alpha), lerp3(a.max, b.max, alpha)}; }
-static inline BBox lerp_slice_bbox(const BBox *s, size_t n, float alpha) {
-    size_t i; float a2;
+static inline real diagonal(BBox b) { return length(b.max - b.min); }
+static inline real diagonal2(BBox b) { return length2(b.max - b.min); }
+static inline BBox blerp(BBox a, BBox b, real alpha) { return BBox{lerp3(a.min, b.min, alpha), lerp3(a.max, b.max, alpha)}; }
+static inline BBox lerp_slice_bbox(const BBox *s, size_t n, real alpha) {
+    size_t i; real a2;
     if (lerp_slice_index(n, alpha, &i, &a2)) return s[i];
     return blerp(s[i], s[i + 1], a2);
 }
@@ -59,17 +59,17 @@ static void transform_bbox_slice_from(const std::vector<BBox> &in, const Xf *xf,
     } else if (in.size() == nx) {
         for (size_t i = 0; i < nx; i++) out.push_back(btransformed(in[i], xf_inverse(xf[i])));
     } else if (in.size() > nx) {
-        float s = (float)(in.size() - 1);
-        for (size_t i = 0; i < in.size(); i++) out.push_back(btransformed(in[i], xf_inverse(lerp_slice_xf(xf, nx, (float)i / s))));
+        real s = (real)(in.size() - 1);
+        for (size_t i = 0; i < in.size(); i++) out.push_back(btransformed(in[i], xf_inverse(lerp_slice_xf(xf, nx, (real)i / s))));
     } else {
-        float s = (float)(nx - 1);
-        for (size_t i = 0; i < nx; i++) out.push_back(btransformed(lerp_slice_bbox(in.data(), in.size(), (float)i / s), xf_inverse(xf[i])));
+        real s = (real)(nx - 1);
+        for (size_t i = 0; i < nx; i++) out.push_back(btransformed(lerp_slice_bbox(in.data(), in.size(), (real)i / s), xf_inverse(xf[i])));
     }
 }
 
 // BBox4 (src/bbox4.rs)
 struct BBox4 {
-    float xmin[4], xmax[4], ymin[4], ymax[4], zmin[4], zmax[4];
+    real xmin[4], xmax[4], ymin[4], ymax[4], zmin[4], zmax[4];
 };
 static BBox4 bbox4_from(const BBox b[4]) {
     BBox4 o;
@@ -80,9 +80,9 @@ static BBox4 bbox4_from(const BBox b[4]) {
     }
     return o;
 }
-static BBox4 bbox4_lerp(const BBox4 &a, const BBox4 &b, float alpha) {
+static BBox4 bbox4_lerp(const BBox4 &a, const BBox4 &b, real alpha) {
     BBox4 o;
-    float ia = 1.0f - alpha;
+    real ia = 1.0f - alpha;
     for (int i = 0; i < 4; i++) {
         o.xmin[i] = (a.xmin[i] * ia) + (b.xmin[i] * alpha); o.xmax[i] = (a.xmax[i] * ia) + (b.xmax[i] * alpha);
         o.ymin[i] = (a.ymin[i] * ia) + (b.ymin[i] * alpha); o.ymax[i] = (a.ymax[i] * ia) + (b.ymax[i] * alpha);
@@ -90,17 +90,17 @@ static BBox4 bbox4_lerp(const BBox4 &a, const BBox4 &b, float alpha) {
     }
     return o;
 }
-static const float BBOX_MAXT_ADJUST = 1.00000024f;
+static const real BBOX_MAXT_ADJUST = 1.00000024f;
 // BBox4::intersect_ray (src/bbox4.rs:63-97); returns a 4-bit hit mask.
-static inline uint32_t bbox4_intersect(const BBox4 &b, V3 o, V3 di, float max_t) {
+static inline uint32_t bbox4_intersect(const BBox4 &b, V3 o, V3 di, real max_t) {
     uint32_t mask = 0;
     for (int i = 0; i < 4; i++) {
-        float t1x = (b.xmin[i] - o.x) * di.x, t1y = (b.ymin[i] - o.y) * di.y, t1z = (b.zmin[i] - o.z) * di.z;
-        float t2x = (b.xmax[i] - o.x) * di.x, t2y = (b.ymax[i] - o.y) * di.y, t2z = (b.zmax[i] - o.z) * di.z;
-        float fx = vmax(t1x, t2x), fy = vmax(t1y, t2y), fz = vmax(t1z, t2z);
-        float nx = vmin(t1x, t2x), ny = vmin(t1y, t2y), nz = vmin(t1z, t2z);
-        float far_t = vmin(vmin(fx, vmin(fy, fz)) * BBOX_MAXT_ADJUST, max_t);
-        float near_t = vmax(vmax(nx, ny), vmax(nz, 0.0f));
+        real t1x = (b.xmin[i] - o.x) * di.x, t1y = (b.ymin[i] - o.y) * di.y, t1z = (b.zmin[i] - o.z) * di.z;
+        real t2x = (b.xmax[i] - o.x) * di.x, t2y = (b.ymax[i] - o.y) * di.y, t2z = (b.zmax[i] - o.z) * di.z;
+        real fx = vmax(t1x, t2x), fy = vmax(t1y, t2y), fz = vmax(t1z, t2z);
+        real nx = vmin(t1x, t2x), ny = vmin(t1y, t2y), nz = vmin(t1z, t2z);
+        real far_t = vmin(vmin(fx, vmin(fy, fz)) * BBOX_MAXT_ADJUST, max_t);
+        real near_t = vmax(vmax(nx, ny), vmax(nz, 0.0f));
         if (near_t < far_t) mask |= 1u << i;
     }
     return mask;
@@ -109,7 +109,7 @@ static inline uint32_t bbox4_intersect(const BBox4 &b, V3 o, V3 di, float max_t)
 // ================================================================ BVH base build
 // src/accel/bvh_base.rs, src/accel/objects_split.rs, src/algorithm.rs
 static const size_t BVH_MAX_DEPTH = 42;
-static const float USE_UNION_FACTOR = 1.4f;
+static const real USE_UNION_FACTOR = 1.4f;
 static const int SAH_BIN_COUNT = 13;
 
 struct BoundsSlice {
@@ -146,11 +146,11 @@ struct Splitter {
     void sah_split(uint32_t *objs, size_t len, size_t *split_i, size_t *split_axis) const {
         BBox bounds = bbox_new();
         for (size_t i = 0; i < len; i++) bounds = bunion_pt(bounds, bcenter(tb(objs[i])));
-        float divs[3][SAH_BIN_COUNT - 1];
+        real divs[3][SAH_BIN_COUNT - 1];
         for (int d = 0; d < 3; d++) {
-            float extent = bounds.max[d] - bounds.min[d];
+            real extent = bounds.max[d] - bounds.min[d];
             for (int dv = 0; dv < SAH_BIN_COUNT - 1; dv++) {
-                float part = extent * ((float)(dv + 1) / (float)SAH_BIN_COUNT);
+                real part = extent * ((real)(dv + 1) / (real)SAH_BIN_COUNT);
                 divs[d][dv] = bounds.min[d] + part;
             }
         }
@@ -168,18 +168,18 @@ struct Splitter {
                 }
         }
         int dim = 0;
-        float div_n = 0.0f, smallest = INFINITY;
+        real div_n = 0.0f, smallest = INFINITY;
         for (int d = 0; d < 3; d++)
             for (int dv = 0; dv < SAH_BIN_COUNT - 1; dv++) {
-                float lc = surface_area(binl[d][dv]) * (float)cntl[d][dv];
-                float rc = surface_area(binr[d][dv]) * (float)cntr[d][dv];
-                float ld = diagonal(binl[d][dv]), rd = diagonal(binr[d][dv]);
-                float tot = (lc * ld) + (rc * rd);
+                real lc = surface_area(binl[d][dv]) * (real)cntl[d][dv];
+                real rc = surface_area(binr[d][dv]) * (real)cntr[d][dv];
+                real ld = diagonal(binl[d][dv]), rd = diagonal(binr[d][dv]);
+                real tot = (lc * ld) + (rc * rd);
                 if (tot < smallest) { dim = d; div_n = divs[d][dv]; smallest = tot; }
             }
         size_t si = partition(objs, len, [&](uint32_t o) {
             BBox b = tb(o);
-            float c = (b.min[dim] + b.max[dim]) * 0.5f;
+            real c = (b.min[dim] + b.max[dim]) * 0.5f;
             return c < div_n;
         });
         if (si < 1) si = 1;
@@ -209,17 +209,17 @@ struct Splitter {
         BBox bounds = bbox_new();
         for (size_t i = 0; i < len; i++) bounds = bunion(bounds, tb(objs[i]));
         int axis = 0;
-        float largest = -INFINITY;
+        real largest = -INFINITY;
         for (int i = 0; i < 3; i++) {
-            float e = bounds.max[i] - bounds.min[i];
+            real e = bounds.max[i] - bounds.min[i];
             if (e > largest) { largest = e; axis = i; }
         }
         size_t place = len / 2;
         if (place == 0) place = 1;
         quick_select(objs, len, place, [&](uint32_t a, uint32_t b) {
             BBox ta = tb(a), tbb = tb(b);
-            float ca = (ta.min[axis] + ta.max[axis]) * 0.5f;
-            float cb = (tbb.min[axis] + tbb.max[axis]) * 0.5f;
+            real ca = (ta.min[axis] + ta.max[axis]) * 0.5f;
+            real cb = (tbb.min[axis] + tbb.max[axis]) * 0.5f;
             return ca < cb;
         });
         *split_i = place;
@@ -242,11 +242,11 @@ static void merge_bounds(const BBox *a, size_t na, const BBox *b, size_t nb, std
     if (na == nb) {
         for (size_t i = 0; i < na; i++) out.push_back(bunion(a[i], b[i]));
     } else if (na > nb) {
-        float s = (float)(na - 1);
-        for (size_t i = 0; i < na; i++) out.push_back(bunion(a[i], lerp_slice_bbox(b, nb, (float)i / s)));
+        real s = (real)(na - 1);
+        for (size_t i = 0; i < na; i++) out.push_back(bunion(a[i], lerp_slice_bbox(b, nb, (real)i / s)));
     } else {
-        float s = (float)(nb - 1);
-        for (size_t i = 0; i < nb; i++) out.push_back(bunion(lerp_slice_bbox(a, na, (float)i / s), b[i]));
+        real s = (real)(nb - 1);
+        for (size_t i = 0; i < nb; i++) out.push_back(bunion(lerp_slice_bbox(a, na, (real)i / s), b[i]));
     }
 }
 
@@ -262,9 +262,9 @@ struct BVHBase {
     void push_reduced(std::vector<BBox> &samples) {
         BBox u = bbox_new();
         for (auto &b : samples) u = bunion(u, b);
-        float avg = 0.0f;
+        real avg = 0.0f;
         for (auto &b : samples) avg = avg + surface_area(b);
-        avg = avg / (float)samples.size();
+        avg = avg / (real)samples.size();
         if (surface_area(u) <= (avg * USE_UNION_FACTOR)) bounds.push_back(u);
         else bounds.insert(bounds.end(), samples.begin(), samples.end());
     }
@@ -284,8 +284,8 @@ struct BVHBase {
                 if (bs.n == max_len) {
                     for (size_t k = 0; k < bs.n; k++) cache[k] = bunion(cache[k], bs.p[k]);
                 } else {
-                    float s = (float)(max_len - 1);
-                    for (size_t k = 0; k < max_len; k++) cache[k] = bunion(cache[k], lerp_slice_bbox(bs.p, bs.n, (float)k / s));
+                    real s = (real)(max_len - 1);
+                    for (size_t k = 0; k < max_len; k++) cache[k] = bunion(cache[k], lerp_slice_bbox(bs.p, bs.n, (real)k / s));
                 }
             }
             push_reduced(cache);
@@ -411,7 +411,7 @@ static size_t construct_from_base(BVH4 &out, const BVHBase<Bounder> &base, size_
         out.bounds.push_back(bbox4_from(bb));
     } else {
         for (size_t k = 0; k < blen; k++) {
-            float time = (float)k / (float)(blen - 1);
+            real time = (real)k / (real)(blen - 1);
             BBox bb[4];
             for (int i = 0; i < 4; i++)
                 bb[i] = ch[i] ? lerp_slice_bbox(&base.bounds[ch[i]->b0], ch[i]->b1 - ch[i]->b0, time) : bbox_new();
@@ -447,20 +447,20 @@ static void bvh4_from_objects(BVH4 &out, uint32_t *objs, size_t len, size_t per_
 static const uint8_t OCCLUSION_FLAG = 1, DONE_FLAG = 2;
 struct RayBatch {
     std::vector<V3> orig_local, dir_inv_local, orig, dir;
-    std::vector<float> max_t, time, wavelength;
+    std::vector<real> max_t, time, wavelength;
     std::vector<uint8_t> flags;
     size_t size() const { return orig.size(); }
     void clear() {
         orig_local.clear(); dir_inv_local.clear(); orig.clear(); dir.clear();
         max_t.clear(); time.clear(); wavelength.clear(); flags.clear();
     }
-    void push(V3 o, V3 d, float mt, float t, float wl, bool occl) {
+    void push(V3 o, V3 d, real mt, real t, real wl, bool occl) {
         orig_local.push_back(o); dir_inv_local.push_back(d);  // placeholders, as the reference
         orig.push_back(o); dir.push_back(d);
         max_t.push_back(mt); time.push_back(t); wavelength.push_back(wl);
         flags.push_back(occl ? OCCLUSION_FLAG : 0);
     }
-    void set_from_ray(size_t i, V3 o, V3 d, float mt, float t, float wl, bool occl) {
+    void set_from_ray(size_t i, V3 o, V3 d, real mt, real t, real wl, bool occl) {
         orig_local[i] = o;
         dir_inv_local[i] = v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
         max_t[i] = mt; time[i] = t;
@@ -565,67 +565,67 @@ static inline uint32_t ray_code(V3 d) {
 // src/surface/triangle.rs
 struct TriPre {
     int i[3];
-    float s[3];
+    real s[3];
 };
 static inline TriPre tri_precompute(V3 d) {
-    float xa = std::fabs(d.x), ya = std::fabs(d.y), za = std::fabs(d.z);
+    real xa = std::fabs(d.x), ya = std::fabs(d.y), za = std::fabs(d.z);
     TriPre p;
     if (xa > ya && xa > za) { p.i[0] = 1; p.i[1] = 2; p.i[2] = 0; }
     else if (ya > za) { p.i[0] = 2; p.i[1] = 0; p.i[2] = 1; }
     else { p.i[0] = 0; p.i[1] = 1; p.i[2] = 2; }
-    float dx = d[p.i[0]], dy = d[p.i[1]], dz = d[p.i[2]];
+    real dx = d[p.i[0]], dy = d[p.i[1]], dz = d[p.i[2]];
     p.s[0] = dx / dz; p.s[1] = dy / dz; p.s[2] = 1.0f / dz;
     return p;
 }
-static inline float max_abs_3(float a, float b, float c) {
+static inline real max_abs_3(real a, real b, real c) {
     a = std::fabs(a); b = std::fabs(b); c = std::fabs(c);
     if (a > b && a > c) return a;
     if (b > c) return b;
     return c;
 }
-static inline bool tri_intersect(V3 o, const TriPre &pre, float max_t, V3 t0, V3 t1, V3 t2, float out[4]) {
+static inline bool tri_intersect(V3 o, const TriPre &pre, real max_t, V3 t0, V3 t1, V3 t2, real out[4]) {
     V3 p0 = t0 - o, p1 = t1 - o, p2 = t2 - o;
-    float p0x = p0[pre.i[0]] - (pre.s[0] * p0[pre.i[2]]);
-    float p0y = p0[pre.i[1]] - (pre.s[1] * p0[pre.i[2]]);
-    float p1x = p1[pre.i[0]] - (pre.s[0] * p1[pre.i[2]]);
-    float p1y = p1[pre.i[1]] - (pre.s[1] * p1[pre.i[2]]);
-    float p2x = p2[pre.i[0]] - (pre.s[0] * p2[pre.i[2]]);
-    float p2y = p2[pre.i[1]] - (pre.s[1] * p2[pre.i[2]]);
-    float e0 = (p1x * p2y) - (p1y * p2x);
-    float e1 = (p2x * p0y) - (p2y * p0x);
-    float e2 = (p0x * p1y) - (p0y * p1x);
+    real p0x = p0[pre.i[0]] - (pre.s[0] * p0[pre.i[2]]);
+    real p0y = p0[pre.i[1]] - (pre.s[1] * p0[pre.i[2]]);
+    real p1x = p1[pre.i[0]] - (pre.s[0] * p1[pre.i[2]]);
+    real p1y = p1[pre.i[1]] - (pre.s[1] * p1[pre.i[2]]);
+    real p2x = p2[pre.i[0]] - (pre.s[0] * p2[pre.i[2]]);
+    real p2y = p2[pre.i[1]] - (pre.s[1] * p2[pre.i[2]]);
+    real e0 = (p1x * p2y) - (p1y * p2x);
+    real e1 = (p2x * p0y) - (p2y * p0x);
+    real e2 = (p0x * p1y) - (p0y * p1x);
     if (e0 == 0.0f || e1 == 0.0f || e2 == 0.0f) {
-        e0 = (float)(((double)p1x * (double)p2y) - ((double)p1y * (double)p2x));
-        e1 = (float)(((double)p2x * (double)p0y) - ((double)p2y * (double)p0x));
-        e2 = (float)(((double)p0x * (double)p1y) - ((double)p0y * (double)p1x));
+        e0 = (real)(((double)p1x * (double)p2y) - ((double)p1y * (double)p2x));
+        e1 = (real)(((double)p2x * (double)p0y) - ((double)p2y * (double)p0x));
+        e2 = (real)(((double)p0x * (double)p1y) - ((double)p0y * (double)p1x));
     }
     if ((e0 < 0.0f || e1 < 0.0f || e2 < 0.0f) && (e0 > 0.0f || e1 > 0.0f || e2 > 0.0f)) return false;
-    float det = e0 + e1 + e2;
+    real det = e0 + e1 + e2;
     if (det == 0.0f) return false;
-    float p0z = pre.s[2] * p0[pre.i[2]];
-    float p1z = pre.s[2] * p1[pre.i[2]];
-    float p2z = pre.s[2] * p2[pre.i[2]];
-    float t_scaled = (e0 * p0z) + (e1 * p1z) + (e2 * p2z);
+    real p0z = pre.s[2] * p0[pre.i[2]];
+    real p1z = pre.s[2] * p1[pre.i[2]];
+    real p2z = pre.s[2] * p2[pre.i[2]];
+    real t_scaled = (e0 * p0z) + (e1 * p1z) + (e2 * p2z);
     if ((det > 0.0f && (t_scaled <= 0.0f || t_scaled > (max_t * det))) ||
         (det < 0.0f && (t_scaled >= 0.0f || t_scaled < (max_t * det))))
         return false;
-    float inv_det = 1.0f / det;
-    float b0 = e0 * inv_det, b1 = e1 * inv_det, b2 = e2 * inv_det;
-    float t = t_scaled * inv_det;
-    float max_zt = max_abs_3(p0z, p1z, p2z);
-    float dz = fp_gamma(3) * max_zt;
-    float max_xt = max_abs_3(p0x, p1x, p2x);
-    float max_yt = max_abs_3(p0y, p1y, p2y);
-    float dx = fp_gamma(5) * (max_xt + max_zt);
-    float dy = fp_gamma(5) * (max_yt + max_zt);
-    float de = 2.0f * ((fp_gamma(2) * max_xt * max_yt) + (dy * max_xt + dx * max_yt));
-    float max_e = max_abs_3(e0, e1, e2);
-    float dt = 3.0f * ((fp_gamma(3) * max_e * max_zt) + (de * max_zt + dz * max_e)) * std::fabs(inv_det);
+    real inv_det = 1.0f / det;
+    real b0 = e0 * inv_det, b1 = e1 * inv_det, b2 = e2 * inv_det;
+    real t = t_scaled * inv_det;
+    real max_zt = max_abs_3(p0z, p1z, p2z);
+    real dz = fp_gamma(3) * max_zt;
+    real max_xt = max_abs_3(p0x, p1x, p2x);
+    real max_yt = max_abs_3(p0y, p1y, p2y);
+    real dx = fp_gamma(5) * (max_xt + max_zt);
+    real dy = fp_gamma(5) * (max_yt + max_zt);
+    real de = 2.0f * ((fp_gamma(2) * max_xt * max_yt) + (dy * max_xt + dx * max_yt));
+    real max_e = max_abs_3(e0, e1, e2);
+    real dt = 3.0f * ((fp_gamma(3) * max_e * max_zt) + (de * max_zt + dz * max_e)) * std::fabs(inv_det);
     if (t <= dt) return false;
     out[0] = t; out[1] = b0; out[2] = b1; out[3] = b2;
     return true;
 }
-static inline void surface_point(V3 t0, V3 t1, V3 t2, float b0, float b1, float b2, V3 *pos, float *err) {
+static inline void surface_point(V3 t0, V3 t1, V3 t2, real b0, real b1, real b2, V3 *pos, real *err) {
     *pos = (t0 * b0) + (t1 * b1) + (t2 * b2);
     V3 e = ((vabs(t0) * b0) + (vabs(t1) * b1) + (vabs(t2) * b2)) * fp_gamma(7);
     *err = max_elem3(e);
@@ -635,9 +635,9 @@ static inline void surface_point(V3 t0, V3 t1, V3 t2, float b0, float b1, float 
 struct Isect {
     uint32_t kind;  // PSY_HIT_*
     uint32_t prim, inst;
-    float t, b0, b1, b2;
+    real t, b0, b1, b2;
     V3 incoming, pos, nor, nor_g;
-    float pos_err, sample_pdf;
+    real pos_err, sample_pdf;
     Closure closure;
     int32_t shader;
 };
@@ -650,12 +650,12 @@ struct Mesh {
     BVH4 accel;
 };
 struct RectLight {
-    std::vector<float> dims;  // [key][2]
+    std::vector<real> dims;  // [key][2]
     std::vector<Color> colors;
     std::vector<BBox> bounds;
 };
 struct SphereLight {
-    std::vector<float> radii;
+    std::vector<real> radii;
     std::vector<Color> colors;
     std::vector<BBox> bounds;
 };
@@ -670,7 +670,7 @@ struct Instance {
     uint32_t xs, xc;
 };
 struct DistantLight {
-    std::vector<float> radii;
+    std::vector<real> radii;
     std::vector<V3> dirs;
     std::vector<Color> colors;
 };
@@ -679,7 +679,7 @@ struct LightTreeNode {
     size_t light_index;     // leaf: index into light_instances
     size_t child0, nchild;  // inner: children in pool
     std::vector<BBox> bounds;
-    float energy;
+    real energy;
 };
 
 static Color to_color(const PsyColor &c) { return Color{c.kind, c.v[0], c.v[1], c.v[2]}; }
@@ -700,7 +700,7 @@ struct PsyoScene {
     bool lt_empty = true;
     // camera
     std::vector<Xf> cam_xf;
-    std::vector<float> cam_tfov, cam_ap, cam_fd;
+    std::vector<real> cam_tfov, cam_ap, cam_fd;
     Color background;
     std::vector<DistantLight> distant;
     uint32_t width, height, spp, seed, max_bounces;
@@ -713,16 +713,16 @@ namespace {
 struct LTBuilderNode {
     bool leaf;
     size_t b0, b1;
-    float energy;
+    real energy;
     size_t child_index;
 };
 struct LTBuilder {
     std::vector<LTBuilderNode> nodes;
     std::vector<BBox> bounds;
     const std::vector<std::vector<BBox>> &inst_bounds;  // by instance id
-    const std::vector<float> &inst_energy;              // by light instance slot value
+    const std::vector<real> &inst_energy;              // by light instance slot value
     std::vector<Instance> &lights;
-    LTBuilder(const std::vector<std::vector<BBox>> &ib, const std::vector<float> &ie, std::vector<Instance> &l)
+    LTBuilder(const std::vector<std::vector<BBox>> &ib, const std::vector<real> &ie, std::vector<Instance> &l)
         : inst_bounds(ib), inst_energy(ie), lights(l) {}
 
     size_t build(size_t offset, uint32_t *objs, size_t len, size_t *rb0, size_t *rb1) {
@@ -751,7 +751,7 @@ struct LTBuilder {
         std::vector<BBox> merged;
         merge_bounds(&bounds[c1b0], c1b1 - c1b0, &bounds[c2b0], c2b1 - c2b0, merged);
         bounds.insert(bounds.end(), merged.begin(), merged.end());
-        float e = nodes[me + 1].energy + nodes[c2].energy;
+        real e = nodes[me + 1].energy + nodes[c2].energy;
         nodes[me] = LTBuilderNode{false, bi, bounds.size(), e, c2};
         *rb0 = bi; *rb1 = bounds.size();
         return me;
@@ -800,15 +800,15 @@ static void lt_construct(PsyoScene &s, const LTBuilder &b, size_t ni, size_t slo
 }  // namespace
 
 // ======================================================================= scene build
-static float rect_energy(const RectLight &r) {
-    float a = 0.0f;
+static real rect_energy(const RectLight &r) {
+    real a = 0.0f;
     for (auto &c : r.colors) a = a + color_energy(c);
-    return a / (float)r.colors.size();
+    return a / (real)r.colors.size();
 }
-static float sphere_energy(const SphereLight &r) {
-    float a = 0.0f;
+static real sphere_energy(const SphereLight &r) {
+    real a = 0.0f;
     for (auto &c : r.colors) a = a + color_energy(c);
-    return a / (float)r.colors.size();
+    return a / (real)r.colors.size();
 }
 
 extern "C" PsyoScene *psyo_scene_create(const PsySceneDesc *d) {
@@ -826,7 +826,7 @@ extern "C" PsyoScene *psyo_scene_create(const PsySceneDesc *d) {
     }
     for (uint32_t i = 0; i < d->num_xforms; i++) {
         Xf x;
-        std::memcpy(x.m, d->xforms[i].m, sizeof(x.m));
+        for (int k = 0; k < 12; k++) x.m[k] = d->xforms[i].m[k];
         s->xforms.push_back(x);
     }
     // objects (TriangleMesh::from_verts_and_indices, src/surface/triangle_mesh.rs:29-115)
@@ -881,7 +881,7 @@ extern "C" PsyoScene *psyo_scene_create(const PsySceneDesc *d) {
             ob.index = (uint32_t)s->rects.size();
             RectLight r;
             for (uint32_t k = 0; k < od.time_samples; k++) {
-                float w = od.dims[k * 2], h = od.dims[k * 2 + 1];
+                real w = od.dims[k * 2], h = od.dims[k * 2 + 1];
                 r.dims.push_back(w); r.dims.push_back(h);
                 r.colors.push_back(to_color(od.colors[k]));
                 r.bounds.push_back(BBox{v3(w * -0.5f, h * -0.5f, 0.0f), v3(w * 0.5f, h * 0.5f, 0.0f)});
@@ -891,7 +891,7 @@ extern "C" PsyoScene *psyo_scene_create(const PsySceneDesc *d) {
             ob.index = (uint32_t)s->spheres.size();
             SphereLight r;
             for (uint32_t k = 0; k < od.time_samples; k++) {
-                float rad = od.dims[k];
+                real rad = od.dims[k];
                 r.radii.push_back(rad);
                 r.colors.push_back(to_color(od.colors[k]));
                 r.bounds.push_back(BBox{v3(-rad, -rad, -rad), v3(rad, rad, rad)});
@@ -930,7 +930,7 @@ extern "C" PsyoScene *psyo_scene_create(const PsySceneDesc *d) {
     }
     if (!s->light_instances.empty()) {
         std::vector<Instance> lights = s->light_instances;
-        std::vector<float> energy(lights.size());
+        std::vector<real> energy(lights.size());
         for (size_t i = 0; i < lights.size(); i++) {
             const Object &ob = s->objects[lights[i].object];
             energy[i] = ob.kind == PSY_OBJ_RECT_LIGHT ? rect_energy(s->rects[ob.index]) : sphere_energy(s->spheres[ob.index]);
@@ -950,17 +950,17 @@ extern "C" PsyoScene *psyo_scene_create(const PsySceneDesc *d) {
     const PsyCameraDesc &c = d->camera;
     for (uint32_t i = 0; i < c.num_transforms; i++) {
         Xf x;
-        std::memcpy(x.m, c.transforms[i].m, sizeof(x.m));
+        for (int k = 0; k < 12; k++) x.m[k] = c.transforms[i].m[k];
         s->cam_xf.push_back(x);
     }
     for (uint32_t i = 0; i < c.num_fovs; i++) {
-        float n = c.fovs[i];
+        real n = c.fovs[i];
         s->cam_tfov.push_back(std::sin(n / 2.0f) / std::cos(n / 2.0f));
     }
-    std::vector<float> ap(c.aperture_radii, c.aperture_radii + c.num_aperture_radii);
-    std::vector<float> fd(c.focus_distances, c.focus_distances + c.num_focus_distances);
+    std::vector<real> ap(c.aperture_radii, c.aperture_radii + c.num_aperture_radii);
+    std::vector<real> fd(c.focus_distances, c.focus_distances + c.num_focus_distances);
     if (ap.empty() || fd.empty()) { ap = {0.0f}; fd = {1.0f}; }
-    for (float f : fd)
+    for (real f : fd)
         if (f == 0.0f) { ap = {0.0f}; fd = {1.0f}; break; }
     s->cam_ap = ap; s->cam_fd = fd;
     s->background = to_color(d->background);
@@ -1023,7 +1023,7 @@ struct Tracer {
                     if (node.nbounds == 1) {
                         h = bbox4_intersect(bvh.bounds[node.bounds0], rays.orig_local[ri], rays.dir_inv_local[ri], rays.max_t[ri]);
                     } else {
-                        size_t i; float a2;
+                        size_t i; real a2;
                         const BBox4 *bb = &bvh.bounds[node.bounds0];
                         BBox4 b = lerp_slice_index(node.nbounds, rays.time[ri], &i, &a2) ? bb[i] : bbox4_lerp(bb[i], bb[i + 1], a2);
                         h = bbox4_intersect(b, rays.orig_local[ri], rays.dir_inv_local[ri], rays.max_t[ri]);
@@ -1069,12 +1069,12 @@ struct Tracer {
             }
             rs.do_next_task([&](uint16_t ri) {
                 if (rays.is_done(ri)) return;
-                float rt = rays.time[ri];
+                real rt = rays.time[ri];
                 Xf mat = (nspace > 1) ? xf_inverse(lerp_slice_xf(space, nspace, rt)) : static_mat;
                 bool hit = false;
                 V3 ht[3];
                 const uint32_t *hix = nullptr;
-                float hd[4];
+                real hd[4] = {0, 0, 0, 0};
                 TriPre pre = tri_precompute(rays.dir[ri]);
                 for (size_t ti = o0; ti < o1; ti++) {
                     const uint32_t *ix = &m.idx[ti * 4];
@@ -1087,7 +1087,7 @@ struct Tracer {
                             if (nspace != 0) tri[k] = xf_point(tri[k], mat);
                         }
                     }
-                    float r[4];
+                    real r[4];
                     cnt.tri_tests++;
                     if (tri_intersect(rays.orig[ri], pre, rays.max_t[ri], tri[0], tri[1], tri[2], r)) {
                         if (rays.is_occlusion(ri)) {
@@ -1131,38 +1131,38 @@ struct Tracer {
     }
 
     // RectangleLight::sample_pdf (src/light/rectangle_light.rs:52-96)
-    static float rect_sample_pdf(const RectLight &L, const Xf &space_xf, V3 arr, V3 sample_dir, V3 hit, float time) {
-        float w = lerp_slice_f_pair(L.dims, 0, time), h = lerp_slice_f_pair(L.dims, 1, time);
+    static real rect_sample_pdf(const RectLight &L, const Xf &space_xf, V3 arr, V3 sample_dir, V3 hit, real time) {
+        real w = lerp_slice_f_pair(L.dims, 0, time), h = lerp_slice_f_pair(L.dims, 1, time);
         Xf si = xf_inverse(space_xf);
         V3 p1 = xf_point(v3(w * 0.5f, h * 0.5f, 0.0f), si);
         V3 p2 = xf_point(v3(w * -0.5f, h * 0.5f, 0.0f), si);
         V3 p3 = xf_point(v3(w * -0.5f, h * -0.5f, 0.0f), si);
         V3 p4 = xf_point(v3(w * 0.5f, h * -0.5f, 0.0f), si);
         V3 sp1 = normalized(p1 - arr), sp2 = normalized(p2 - arr), sp3 = normalized(p3 - arr), sp4 = normalized(p4 - arr);
-        float a1 = spherical_triangle_solid_angle(sp2, sp1, sp3);
-        float a2 = spherical_triangle_solid_angle(sp4, sp1, sp3);
+        real a1 = spherical_triangle_solid_angle(sp2, sp1, sp3);
+        real a2 = spherical_triangle_solid_angle(sp4, sp1, sp3);
         V3 normal = xf_normal(v3(0.0f, 0.0f, 1.0f), si);
         if ((a1 + a2) < 0.01f) {
-            float area = triangle_surface_area(p2, p1, p3) + triangle_surface_area(p4, p1, p3);
+            real area = triangle_surface_area(p2, p1, p3) + triangle_surface_area(p4, p1, p3);
             return length2(hit - arr) / std::fabs(dot(normalized(sample_dir), normalized(normal))) / area;
         }
         return 1.0f / (a1 + a2);
     }
-    static float lerp_slice_f_pair(const std::vector<float> &dims, int c, float time) {
+    static real lerp_slice_f_pair(const std::vector<real> &dims, int c, real time) {
         size_t n = dims.size() / 2;
-        size_t i; float a2;
+        size_t i; real a2;
         if (lerp_slice_index(n, time, &i, &a2)) return dims[i * 2 + c];
         return lerpf(dims[i * 2 + c], dims[(i + 1) * 2 + c], a2);
     }
 
-    Xf space_at(float t) const { return nspace ? lerp_slice_xf(space, nspace, t) : xf_identity(); }
+    Xf space_at(real t) const { return nspace ? lerp_slice_xf(space, nspace, t) : xf_identity(); }
 
     void rect_intersect(const RectLight &L, uint32_t inst_id, RayBatch &rays) {
         rs.pop_do_next_task([&](uint16_t ri) {
-            float time = rays.time[ri];
+            real time = rays.time[ri];
             V3 o = rays.orig[ri], dir = rays.dir[ri];
-            float max_t = rays.max_t[ri];
-            float w = lerp_slice_f_pair(L.dims, 0, time), h = lerp_slice_f_pair(L.dims, 1, time);
+            real max_t = rays.max_t[ri];
+            real w = lerp_slice_f_pair(L.dims, 0, time), h = lerp_slice_f_pair(L.dims, 1, time);
             Xf xf = space_at(time);
             Xf si = xf_inverse(xf);
             V3 p1 = xf_point(v3(w * 0.5f, h * 0.5f, 0.0f), si);
@@ -1172,7 +1172,7 @@ struct Tracer {
             TriPre pre = tri_precompute(dir);
             V3 tris[2][3] = {{p1, p2, p3}, {p3, p4, p1}};
             for (int k = 0; k < 2; k++) {
-                float r[4];
+                real r[4];
                 cnt.tri_tests++;
                 if (tri_intersect(o, pre, max_t, tris[k][0], tris[k][1], tris[k][2], r) && r[0] < max_t) {
                     Isect &is = isects[ri];
@@ -1189,7 +1189,7 @@ struct Tracer {
                         is.incoming = dir;
                         is.nor = nn; is.nor_g = nn;
                         is.sample_pdf = rect_sample_pdf(L, xf, o, dir, is.pos, time);
-                        float isa = (float)(1.0 / ((double)w * (double)h));
+                        real isa = (real)(1.0 / ((double)w * (double)h));
                         Color col = color_mul(lerp_slice_color(L.colors.data(), L.colors.size(), time), isa);
                         is.closure = Closure{CL_EMIT, col, 0.0f, 0.0f};
                         is.shader = -1;
@@ -1202,7 +1202,7 @@ struct Tracer {
     }
 
     // SphereLight::sample_pdf (src/light/sphere_light.rs:51-81)
-    static float sphere_sample_pdf(const SphereLight &L, const Xf &space_xf, V3 arr_w, float time) {
+    static real sphere_sample_pdf(const SphereLight &L, const Xf &space_xf, V3 arr_w, real time) {
         V3 arr = xf_point(arr_w, space_xf);
         double radius = (double)lerp_slice_f(L.radii.data(), L.radii.size(), time);
         double d2 = (double)length2(v3(0, 0, 0) - arr);
@@ -1210,30 +1210,30 @@ struct Tracer {
         if (d > radius) {
             double st2 = std::fmin((radius * radius) / d2, 1.0);
             double ct2 = 1.0 - st2;
-            return (float)uniform_sample_cone_pdf(std::sqrt(ct2));
+            return (real)uniform_sample_cone_pdf(std::sqrt(ct2));
         }
-        return (float)(1.0 / (4.0 * PI_64));
+        return (real)(1.0 / (4.0 * PI_64));
     }
 
     void sphere_intersect(const SphereLight &L, uint32_t inst_id, RayBatch &rays) {
         rs.pop_do_next_task([&](uint16_t ri) {
-            float time = rays.time[ri];
+            real time = rays.time[ri];
             Xf xf = space_at(time);
-            float radius = lerp_slice_f(L.radii.data(), L.radii.size(), time);
+            real radius = lerp_slice_f(L.radii.data(), L.radii.size(), time);
             V3 o = rays.orig_local[ri];
             V3 dir = xf_vector(rays.dir[ri], xf);
-            float a = length2(dir);
-            float b = 2.0f * dot(dir, o);
-            float c = length2(o) - (radius * radius);
-            float disc = (b * b) - (4.0f * a * c);
+            real a = length2(dir);
+            real b = 2.0f * dot(dir, o);
+            real c = length2(o) - (radius * radius);
+            real disc = (b * b) - (4.0f * a * c);
             if (disc < 0.0f) return;
             disc = std::sqrt(disc);
-            float q = (b < 0.0f) ? -0.5f * (b - disc) : -0.5f * (b + disc);
-            float t0 = q / a;
-            float t1 = (q != 0.0f) ? c / q : rays.max_t[ri];
+            real q = (b < 0.0f) ? -0.5f * (b - disc) : -0.5f * (b + disc);
+            real t0 = q / a;
+            real t1 = (q != 0.0f) ? c / q : rays.max_t[ri];
             if (t0 > t1) std::swap(t0, t1);
             if (t0 > rays.max_t[ri] || t1 <= 0.0f) return;
-            float t;
+            real t;
             if (t0 > 0.0f) t = t0;
             else if (t1 <= rays.max_t[ri]) t = t1;
             else return;
@@ -1256,7 +1256,7 @@ struct Tracer {
             is.incoming = rays.dir[ri];
             is.nor = nrm; is.nor_g = nrm;
             is.sample_pdf = sphere_sample_pdf(L, xf, rays.orig[ri], time);
-            float isa = (float)(1.0 / (4.0 * PI_64 * (double)radius * (double)radius));
+            real isa = (real)(1.0 / (4.0 * PI_64 * (double)radius * (double)radius));
             is.closure = Closure{CL_EMIT, color_mul(lerp_slice_color(L.colors.data(), L.colors.size(), time), isa), 0.0f, 0.0f};
             is.shader = -1;
             rays.max_t[ri] = t;
@@ -1313,36 +1313,36 @@ struct Tracer {
 namespace {
 
 // LightTree::select (src/accel/light_tree.rs:135-201)
-static bool lt_select(const PsyoScene &s, V3 inc, V3 pos, V3 nor, V3 nor_g, const Closure &sc, float time, float n,
-                      size_t *light_index, float *pdf, float *whittled) {
+static bool lt_select(const PsyoScene &s, V3 inc, V3 pos, V3 nor, V3 nor_g, const Closure &sc, real time, real n,
+                      size_t *light_index, real *pdf, real *whittled) {
     if (s.lt_empty) return false;
     auto node_prob = [&](const LightTreeNode &nd) {
         BBox bb = lerp_slice_bbox(nd.bounds.data(), nd.bounds.size(), time);
         V3 dd = bcenter(bb) - pos;
-        float r2 = diagonal2(bb) * 0.25f;
-        float inv_sa = 1.0f / r2;
-        float contrib = closure_estimate_sphere(sc, inc, dd, r2, nor, nor_g);
+        real r2 = diagonal2(bb) * 0.25f;
+        real inv_sa = 1.0f / r2;
+        real contrib = closure_estimate_sphere(sc, inc, dd, r2, nor, nor_g);
         return nd.energy * inv_sa * contrib;
     };
     const LightTreeNode *node = &s.lt[0];
-    float tot = 1.0f;
+    real tot = 1.0f;
     while (!node->leaf) {
-        float ps[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        float total = 0.0f;
+        real ps[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        real total = 0.0f;
         for (size_t i = 0; i < node->nchild; i++) {
-            float p = node_prob(s.lt[node->child0 + i]);
+            real p = node_prob(s.lt[node->child0 + i]);
             ps[i] = p;
             total += p;
         }
         if (total <= 0.0f) {
-            float p = 1.0f / (float)node->nchild;
+            real p = 1.0f / (real)node->nchild;
             for (int i = 0; i < 8; i++) ps[i] = p;
         } else {
             for (int i = 0; i < 8; i++) ps[i] /= total;
         }
-        float base = 0.0f;
+        real base = 0.0f;
         for (size_t i = 0; i < 8; i++) {
-            float p = ps[i];
+            real p = ps[i];
             if ((n <= base + p) || (i == node->nchild - 1)) {
                 tot *= p;
                 node = &s.lt[node->child0 + i];
@@ -1359,9 +1359,9 @@ static bool lt_select(const PsyoScene &s, V3 inc, V3 pos, V3 nor, V3 nor_g, cons
 }
 
 // RectangleLight::sample_from_point (src/light/rectangle_light.rs:121-243)
-static V4 rect_sample(const RectLight &L, const Xf &space, V3 arr, float u, float v, float wl, float time, V3 *sp,
-                      V3 *sn, float *serr, float *pdf) {
-    float w = Tracer::lerp_slice_f_pair(L.dims, 0, time), h = Tracer::lerp_slice_f_pair(L.dims, 1, time);
+static V4 rect_sample(const RectLight &L, const Xf &space, V3 arr, real u, real v, real wl, real time, V3 *sp,
+                      V3 *sn, real *serr, real *pdf) {
+    real w = Tracer::lerp_slice_f_pair(L.dims, 0, time), h = Tracer::lerp_slice_f_pair(L.dims, 1, time);
     Color col = lerp_slice_color(L.colors.data(), L.colors.size(), time);
     double sa = (double)w * (double)h;
     double sai = 1.0 / sa;
@@ -1372,23 +1372,23 @@ static V4 rect_sample(const RectLight &L, const Xf &space, V3 arr, float u, floa
     V3 p4 = xf_point(v3(w * 0.5f, h * -0.5f, 0.0f), si);
     V3 lp1 = p1 - arr, lp2 = p2 - arr, lp3 = p3 - arr, lp4 = p4 - arr;
     V3 sp1 = normalized(lp1), sp2 = normalized(lp2), sp3 = normalized(lp3), sp4 = normalized(lp4);
-    float a1 = spherical_triangle_solid_angle(sp2, sp1, sp3);
-    float a2 = spherical_triangle_solid_angle(sp4, sp1, sp3);
+    real a1 = spherical_triangle_solid_angle(sp2, sp1, sp3);
+    real a2 = spherical_triangle_solid_angle(sp4, sp1, sp3);
     V3 normal = xf_normal(v3(0.0f, 0.0f, 1.0f), si);
     if ((a1 + a2) < 0.01f) {
-        float sa1 = triangle_surface_area(p2, p1, p3);
-        float sa2 = triangle_surface_area(p4, p1, p3);
-        float th = sa1 / (sa1 + sa2);
+        real sa1 = triangle_surface_area(p2, p1, p3);
+        real sa2 = triangle_surface_area(p4, p1, p3);
+        real th = sa1 / (sa1 + sa2);
         V3 spt = (u < th) ? uniform_sample_triangle(p2, p1, p3, v, u / th)
                           : uniform_sample_triangle(p4, p1, p3, v, (u - th) / (1.0f - th));
         V3 shadow_vec = spt - arr;
-        V4 ss = color_to_spectral(col, wl) * (float)sai * 0.5f;
+        V4 ss = color_to_spectral(col, wl) * (real)sai * 0.5f;
         *pdf = length2(spt - arr) / std::fabs(dot(normalized(shadow_vec), normalized(normal))) / (sa1 + sa2);
         *sp = spt; *sn = normal; *serr = 0.0001f;
         return ss;
     }
-    float prob_1 = std::isinf(a1) ? 1.0f : (std::isinf(a2) ? 0.0f : a1 / (a1 + a2));
-    float prob_2 = 1.0f - prob_1;
+    real prob_1 = std::isinf(a1) ? 1.0f : (std::isinf(a2) ? 0.0f : a1 / (a1 + a2));
+    real prob_2 = 1.0f - prob_1;
     V3 shadow_vec = (u < prob_1) ? uniform_sample_spherical_triangle(sp2, sp1, sp3, v, u / prob_1)
                                  : uniform_sample_spherical_triangle(sp4, sp1, sp3, v, 1.0f - ((u - prob_1) / prob_2));
     V3 arr_local = xf_point(arr, space);
@@ -1402,12 +1402,12 @@ static V4 rect_sample(const RectLight &L, const Xf &space, V3 arr, float u, floa
     *sn = normal;
     *serr = 0.0001f;
     *pdf = 1.0f / (a1 + a2);
-    return color_to_spectral(col, wl) * (float)sai * 0.5f;
+    return color_to_spectral(col, wl) * (real)sai * 0.5f;
 }
 
 // SphereLight::sample_from_point (src/light/sphere_light.rs:85-192)
-static V4 sphere_sample(const SphereLight &L, const Xf &space, V3 arr_w, float u, float v, float wl, float time, V3 *sp,
-                        V3 *sn, float *serr, float *pdf) {
+static V4 sphere_sample(const SphereLight &L, const Xf &space, V3 arr_w, real u, real v, real wl, real time, V3 *sp,
+                        V3 *sn, real *serr, real *pdf) {
     V3 arr = xf_point(arr_w, space);
     V3 pos = v3(0, 0, 0);
     Xf inv = xf_inverse(space);
@@ -1420,8 +1420,8 @@ static V4 sphere_sample(const SphereLight &L, const Xf &space, V3 arr_w, float u
     V3 z, x, y;
     coordinate_system_from_vector(zv, &z, &x, &y);
     x = normalized(x); y = normalized(y); z = normalized(z);
-    float rf = (float)radius;
-    float err = length(xf_vector(v3(rf, rf, rf), inv)) * 0.001f;
+    real rf = (real)radius;
+    real err = length(xf_vector(v3(rf, rf, rf), inv)) * 0.001f;
     if (d > radius) {
         double st2 = std::fmin((radius * radius) / d2, 1.0);
         double ct2 = 1.0 - st2;
@@ -1436,15 +1436,15 @@ static V4 sphere_sample(const SphereLight &L, const Xf &space, V3 arr_w, float u
         double cos_a = (dd <= 0.0) ? st : ((d / radius) * sin_theta2) + (cos_theta * std::sqrt(dd));
         double sin_a = std::sqrt(std::fmax(1.0 - (cos_a * cos_a), 0.0));
         double phi = (double)v * 2.0 * PI_64;
-        V3 s2 = v3((float)(std::cos(phi) * sin_a * radius), (float)(std::sin(phi) * sin_a * radius), (float)(d - (cos_a * radius)));
+        V3 s2 = v3((real)(std::cos(phi) * sin_a * radius), (real)(std::sin(phi) * sin_a * radius), (real)(d - (cos_a * radius)));
         V3 svec = (x * s2.x) + (y * s2.y) + (z * s2.z);
         V3 normal = normalized(arr + svec);
         V3 point = normal * rf;
         *sp = xf_point(point, inv);
         *sn = xf_normal(normal, inv);
         *serr = err;
-        *pdf = (float)uniform_sample_cone_pdf(ct);
-        return color_to_spectral(col, wl) * (float)sai;
+        *pdf = (real)uniform_sample_cone_pdf(ct);
+        return color_to_spectral(col, wl) * (real)sai;
     }
     V3 svec = uniform_sample_sphere(u, v);
     V3 normal = normalized(arr + svec);
@@ -1452,8 +1452,8 @@ static V4 sphere_sample(const SphereLight &L, const Xf &space, V3 arr_w, float u
     *sp = xf_point(point, inv);
     *sn = xf_normal(normal, inv);
     *serr = err;
-    *pdf = (float)(1.0 / (4.0 * PI_64));
-    return color_to_spectral(col, wl) * (float)sai;
+    *pdf = (real)(1.0 / (4.0 * PI_64));
+    return color_to_spectral(col, wl) * (real)sai;
 }
 
 enum { LS_NONE = 0, LS_DISTANT = 1, LS_SURFACE = 2 };
@@ -1462,39 +1462,39 @@ struct LightSample {
     V4 color;
     V3 dir;            // distant
     V3 sp, sn;         // surface
-    float serr;
-    float pdf, sel_pdf;
+    real serr;
+    real pdf, sel_pdf;
 };
 
-static float distant_energy(const DistantLight &l) {
-    float a = 0.0f;
+static real distant_energy(const DistantLight &l) {
+    real a = 0.0f;
     for (auto &c : l.colors) a = a + color_energy(c);
-    return a / (float)l.colors.size();
+    return a / (real)l.colors.size();
 }
 
 // Scene::sample_lights (src/scene/mod.rs:28-99) + Assembly::sample_lights
 // (src/scene/assembly.rs:46-140) for the root assembly.
-static LightSample scene_sample_lights(const PsyoScene &s, float n, float u, float v, float w, float wl, float time,
+static LightSample scene_sample_lights(const PsyoScene &s, real n, real u, real v, real w, real wl, real time,
                                        const Isect &is) {
     LightSample out{};
     out.kind = LS_NONE;
-    float wle = 0.0f;
+    real wle = 0.0f;
     for (auto &l : s.distant) wle = wle + distant_energy(l);
-    float wl_energy = (wle <= 0.0f) ? 0.0f : 1.0f;
-    float ll_energy = (s.lt_empty || s.lt[0].energy <= 0.0f) ? 0.0f : 1.0f;
-    float tot = wl_energy + ll_energy;
+    real wl_energy = (wle <= 0.0f) ? 0.0f : 1.0f;
+    real ll_energy = (s.lt_empty || s.lt[0].energy <= 0.0f) ? 0.0f : 1.0f;
+    real tot = wl_energy + ll_energy;
     if (tot <= 0.0f) return out;
-    float wl_prob = wl_energy / tot;
+    real wl_prob = wl_energy / tot;
     if (n < wl_prob) {
-        float nn = n / wl_prob;
-        float total = 0.0f;
+        real nn = n / wl_prob;
+        real total = 0.0f;
         for (auto &l : s.distant) total = total + distant_energy(l);
-        float target = nn * total;
-        float x = 0.0f;
+        real target = nn * total;
+        real x = 0.0f;
         size_t pick = s.distant.size() - 1;
-        float p = 0.0f;
+        real p = 0.0f;
         for (size_t i = 0; i < s.distant.size(); i++) {
-            float wgt = distant_energy(s.distant[i]);
+            real wgt = distant_energy(s.distant[i]);
             x += wgt;
             if (x > target) { pick = i; p = wgt / total; break; }
             if (i == s.distant.size() - 1) p = wgt / total;
@@ -1509,17 +1509,17 @@ static LightSample scene_sample_lights(const PsyoScene &s, float n, float u, flo
         double ctm = std::cos(radius);
         V3 smp = normalized(uniform_sample_cone(u, v, ctm));
         out.kind = LS_DISTANT;
-        out.color = color_to_spectral(col, wl) * (float)sai;
+        out.color = color_to_spectral(col, wl) * (real)sai;
         out.dir = (x3 * smp.x) + (y3 * smp.y) + (z * smp.z);
-        out.pdf = (float)uniform_sample_cone_pdf(ctm);
+        out.pdf = (real)uniform_sample_cone_pdf(ctm);
         out.sel_pdf = p * wl_prob;
         return out;
     }
-    float nl = (n - wl_prob) / (1.0f - wl_prob);
+    real nl = (n - wl_prob) / (1.0f - wl_prob);
     if (is.kind != PSY_HIT_SURFACE && is.kind != PSY_HIT_LIGHT) return out;
     Xf ident = xf_identity();
     size_t li;
-    float sel_pdf, whittled;
+    real sel_pdf, whittled;
     if (!lt_select(s, xf_vector(is.incoming, ident), xf_point(is.pos, ident), xf_normal(is.nor, ident),
                    xf_normal(is.nor_g, ident), is.closure, time, nl, &li, &sel_pdf, &whittled))
         return out;
@@ -1527,7 +1527,7 @@ static LightSample scene_sample_lights(const PsyoScene &s, float n, float u, flo
     Xf xf = inst.xc ? lerp_slice_xf(&s.xforms[inst.xs], inst.xc, time) : xf_identity();
     const Object &ob = s.objects[inst.object];
     V4 col;
-    float pdf;
+    real pdf;
     if (ob.kind == PSY_OBJ_RECT_LIGHT) col = rect_sample(s.rects[ob.index], xf, is.pos, u, v, wl, time, &out.sp, &out.sn, &out.serr, &pdf);
     else col = sphere_sample(s.spheres[ob.index], xf, is.pos, u, v, wl, time, &out.sp, &out.sn, &out.serr, &pdf);
     out.kind = LS_SURFACE;
@@ -1547,21 +1547,21 @@ struct LightPath {
     uint32_t px, py;
     uint32_t sample_number;
     uint32_t dim_offset;
-    float time, wavelength;
+    real time, wavelength;
     bool has_next_bounce;
     V3 nb_orig, nb_dir;
     V4 next_attenuation_fac;
-    float closure_sample_pdf;
+    real closure_sample_pdf;
     V4 light_attenuation, pending_color_addition, color;
     uint32_t rays;  // rays traced (statistics only)
 };
 
-static void camera_generate_ray(const PsyoScene &s, float x, float y, float time, float u, float v, V3 *o, V3 *d) {
+static void camera_generate_ray(const PsyoScene &s, real x, real y, real time, real u, real v, V3 *o, V3 *d) {
     Xf xf = lerp_slice_xf(s.cam_xf.data(), s.cam_xf.size(), time);
-    float tfov = lerp_slice_f(s.cam_tfov.data(), s.cam_tfov.size(), time);
-    float ar = lerp_slice_f(s.cam_ap.data(), s.cam_ap.size(), time);
-    float fd = lerp_slice_f(s.cam_fd.data(), s.cam_fd.size(), time);
-    float cu, cv;
+    real tfov = lerp_slice_f(s.cam_tfov.data(), s.cam_tfov.size(), time);
+    real ar = lerp_slice_f(s.cam_ap.data(), s.cam_ap.size(), time);
+    real fd = lerp_slice_f(s.cam_fd.data(), s.cam_fd.size(), time);
+    real cu, cv;
     square_to_circle((u * 2.0f) - 1.0f, (v * 2.0f) - 1.0f, &cu, &cv);
     V3 orig = v3(ar * cu, ar * cv, 0.0f);
     V3 dir = normalized(v3((x * tfov) - (orig.x / fd), (y * tfov) - (orig.y / fd), 1.0f));
@@ -1584,7 +1584,7 @@ static bool path_next(LightPath &p, const PsyoScene &s, const Isect &is, RayBatc
                 if (p.event == EV_CAMERA) {
                     p.color = p.color + c;
                 } else {
-                    float mis = power_heuristic(p.closure_sample_pdf, is.sample_pdf);
+                    real mis = power_heuristic(p.closure_sample_pdf, is.sample_pdf);
                     p.color = p.color + c * p.light_attenuation / splat4(mis);
                 }
                 return false;
@@ -1598,9 +1598,9 @@ static bool path_next(LightPath &p, const PsyoScene &s, const Isect &is, RayBatc
             bool found = false;
             if (li.kind != LS_NONE && !(li.pdf <= 0.0f) && !(li.sel_pdf <= 0.0f)) {
                 V4 att;
-                float cpdf;
+                real cpdf;
                 V3 so, sd;
-                float smax;
+                real smax;
                 if (li.kind == LS_DISTANT) {
                     att = closure_evaluate(cl, rays.dir[ri], li.dir, is.nor, is.nor_g, p.wavelength, &cpdf);
                     so = robust_ray_origin(is.pos, is.pos_err, normalized(is.nor_g), li.dir);
@@ -1615,7 +1615,7 @@ static bool path_next(LightPath &p, const PsyoScene &s, const Isect &is, RayBatc
                     smax = 1.0f;
                 }
                 if (!(max_elem4(att) <= 0.0f)) {
-                    float lmis = power_heuristic(li.pdf, cpdf);
+                    real lmis = power_heuristic(li.pdf, cpdf);
                     p.pending_color_addition = li.color * att * p.light_attenuation / splat4(lmis * li.sel_pdf);
                     rays.set_from_ray(ri, so, sd, smax, p.time, p.wavelength, true);
                     found = true;
@@ -1629,7 +1629,7 @@ static bool path_next(LightPath &p, const PsyoScene &s, const Isect &is, RayBatc
                 float b4[4];
                 next_lds(p, b4);
                 V3 dir;
-                float pdf;
+                real pdf;
                 V4 filt = closure_sample(cl, is.incoming, is.nor, is.nor_g, b4[0], b4[1], p.wavelength, &dir, &pdf);
                 if ((pdf > 0.0f) && (max_elem4(filt) > 0.0f)) {
                     p.next_attenuation_fac = filt;
@@ -1685,22 +1685,22 @@ struct Worker {
     void gen(const BucketJob &b, uint32_t spp, uint32_t seed) {
         paths.clear();
         rays.clear();
-        float cmpx = 1.0f / (float)s.width, cmpy = 1.0f / (float)s.height;
-        float min_x = -1.0f, max_x = 1.0f;
-        float min_y = -((float)s.height / (float)s.width), max_y = (float)s.height / (float)s.width;
-        float xe = max_x - min_x, ye = max_y - min_y;
+        real cmpx = 1.0f / (real)s.width, cmpy = 1.0f / (real)s.height;
+        real min_x = -1.0f, max_x = 1.0f;
+        real min_y = -((real)s.height / (real)s.width), max_y = (real)s.height / (real)s.width;
+        real xe = max_x - min_x, ye = max_y - min_y;
         for (uint32_t y = b.y; y < b.y + b.h; y++)
             for (uint32_t x = b.x; x < b.x + b.w; x++)
                 for (uint32_t si = 0; si < spp; si++) {
                     float d[4], d4[4];
                     get_sample_4d(si, 0, x, y, seed, d);
                     get_sample_4d(si, 1, x, y, seed, d4);
-                    float fx = probit(d[3], 2.0f / 6.0f) + 0.5f;
-                    float fy = probit(d4[0], 2.0f / 6.0f) + 0.5f;
-                    float sx = (fx + (float)x) * cmpx;
-                    float sy = (fy + (float)y) * cmpy;
-                    float ix = (sx - 0.5f) * xe, iy = (0.5f - sy) * ye;
-                    float wl = map_0_1_to_wavelength(golden_ratio_sample(si, hash_u32((x << 16) ^ y, seed)));
+                    real fx = probit(d[3], 2.0f / 6.0f) + 0.5f;
+                    real fy = probit(d4[0], 2.0f / 6.0f) + 0.5f;
+                    real sx = (fx + (real)x) * cmpx;
+                    real sy = (fy + (real)y) * cmpy;
+                    real ix = (sx - 0.5f) * xe, iy = (0.5f - sy) * ye;
+                    real wl = map_0_1_to_wavelength(golden_ratio_sample(si, hash_u32((x << 16) ^ y, seed)));
                     LightPath p{};
                     p.event = EV_CAMERA;
                     p.sampling_seed = seed ^ 0x40d4682bu;
@@ -1879,6 +1879,8 @@ extern "C" int psyo_render_sampled(PsyoScene *s, uint32_t spb, uint32_t nthreads
     }
     if (max_buckets && jobs.size() > max_buckets) jobs.resize(max_buckets);
     std::memset(xyz, 0, sizeof(float) * W * H * 3);
+    // accumulate in the arithmetic type (f64 in the FP64 oracle), store f32
+    std::vector<real> acc(W * H * 3, (real)0);
     std::atomic<size_t> next{0};
     std::mutex mu;
     PsyRenderStats tot{};
@@ -1897,10 +1899,10 @@ extern "C" int psyo_render_sampled(PsyoScene *s, uint32_t spb, uint32_t nthreads
             wk.st.samples += wk.paths.size();
             wk.run();
             auto a0 = std::chrono::steady_clock::now();
-            float inv = (float)s->spp;
+            real inv = (real)s->spp;
             for (auto &p : wk.paths) {
                 V3 c = xyz_from_spectral(p.color, p.wavelength);
-                float *px = xyz + ((size_t)p.py * W + p.px) * 3;
+                real *px = acc.data() + ((size_t)p.py * W + p.px) * 3;
                 px[0] += c.x / inv; px[1] += c.y / inv; px[2] += c.z / inv;
             }
             auto a1 = std::chrono::steady_clock::now();
@@ -1921,6 +1923,7 @@ extern "C" int psyo_render_sampled(PsyoScene *s, uint32_t spb, uint32_t nthreads
     for (uint32_t t = 1; t < nthreads; t++) th.emplace_back(work);
     work();
     for (auto &t : th) t.join();
+    for (size_t i = 0; i < W * H * 3; i++) xyz[i] = (float)acc[i];
     tot.total_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     if (stats) *stats = tot;
     return PSY_OK;
@@ -1961,6 +1964,7 @@ extern "C" float psyo_golden_ratio_sample(uint32_t i, uint32_t scramble) { retur
 extern "C" float psyo_probit(float n, float width) { return probit(n, width); }
 extern "C" float psyo_fast_exp(float p) { return fast_exp(p); }
 extern "C" void psyo_traversal_table(uint8_t *out) { std::memcpy(out, TRAVERSAL_TABLE, sizeof(TRAVERSAL_TABLE)); }
+#ifndef PSYO_F64  // f32 known-answer hooks (the FP64 oracle exports renders only)
 extern "C" void psyo_xf_mul(const float *a, const float *b, float *out) {
     Xf x, y;
     std::memcpy(x.m, a, 48); std::memcpy(y.m, b, 48);
@@ -1992,6 +1996,7 @@ extern "C" void psyo_xf_normal(const float *m, const float *n, float *out) {
     out[0] = r.x; out[1] = r.y; out[2] = r.z;
 }
 extern "C" float psyo_lerp_slice(const float *s, uint32_t n, float alpha) { return lerp_slice_f(s, n, alpha); }
+#endif
 extern "C" void psyo_xyz_to_spectrum(const float *xyz, float hero, float *out4) {
     V4 r = color_to_spectral(Color{COL_XYZ, xyz[0], xyz[1], xyz[2]}, hero);
     for (int k = 0; k < 4; k++) out4[k] = r[k];
@@ -2089,6 +2094,7 @@ extern "C" void psyo_xyz_to_srgb8(const float *xyz, uint32_t w, uint32_t h, uint
             o[0] = q(gamma(rgb[0])); o[1] = q(gamma(rgb[1])); o[2] = q(gamma(rgb[2])); o[3] = 255;
         }
 }
+#ifndef PSYO_F64
 extern "C" int psyo_intersect_triangle(const float *o, const float *d, float max_t, const float *p0, const float *p1,
                                        const float *p2, float *out) {
     TriPre pre = tri_precompute(v3(d[0], d[1], d[2]));
@@ -2097,6 +2103,7 @@ extern "C" int psyo_intersect_triangle(const float *o, const float *d, float max
                ? 1
                : 0;
 }
+#endif
 extern "C" uint32_t psyo_quick_select_ints(int32_t *list, uint32_t n, uint32_t place) {
     std::vector<uint32_t> idx(n);
     for (uint32_t i = 0; i < n; i++) idx[i] = i;

@@ -4,21 +4,26 @@ import ctypes as C
 
 import numpy as np
 
-from . import lib as _lib
+from . import lib as _lib32
+from . import lib64 as _lib64
 
 
 class OracleScene:
-    def __init__(self, scene_data):
+    """A scene in the oracle.  f64=True uses the FP64 oracle build (the same
+    algorithm with f64 arithmetic) for trace and render calls."""
+
+    def __init__(self, scene_data, f64=False):
         self._data = scene_data
         self._desc = scene_data.desc()
-        self.h = _lib().psyo_scene_create(C.byref(self._desc))
+        self._L = _lib64() if f64 else _lib32()
+        self.h = self._L.psyo_scene_create(C.byref(self._desc))
         if not self.h:
             raise RuntimeError("oracle scene build failed")
         self.width, self.height, self.spp = scene_data.width, scene_data.height, scene_data.spp
 
     def close(self):
         if self.h:
-            _lib().psyo_scene_destroy(self.h)
+            self._L.psyo_scene_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -36,7 +41,7 @@ class OracleScene:
         hits = np.zeros(n, dtype=abi.hit_dtype())
         fh = np.zeros(n, dtype=abi.surface_hit_dtype()) if full else None
         nt, tt = C.c_uint64(0), C.c_uint64(0)
-        rc = _lib().psyo_trace(self.h, rays.ctypes.data, n, hits.ctypes.data,
+        rc = self._L.psyo_trace(self.h, rays.ctypes.data, n, hits.ctypes.data,
                                fh.ctypes.data if full else None, C.byref(nt), C.byref(tt), threads)
         if rc != 0:
             raise RuntimeError("psyo_trace failed: %d" % rc)
@@ -47,7 +52,7 @@ class OracleScene:
         img = np.zeros((self.height, self.width, 3), dtype=np.float32)
         st = abi.PsyRenderStats()
         cr = (C.c_uint32 * 4)(*crop) if crop is not None else None
-        rc = _lib().psyo_render(self.h, spb, threads, cr, max_buckets, img.ctypes.data, C.byref(st))
+        rc = self._L.psyo_render(self.h, spb, threads, cr, max_buckets, img.ctypes.data, C.byref(st))
         if rc != 0:
             raise RuntimeError("psyo_render failed: %d" % rc)
         return img, st.as_dict()
@@ -58,7 +63,7 @@ class OracleScene:
         from psychopath_gb300 import abi
         img = np.zeros((self.height, self.width, 3), dtype=np.float32)
         st = abi.PsyRenderStats()
-        rc = _lib().psyo_render_sampled(self.h, spb, threads, None, stride, max_buckets, img.ctypes.data, C.byref(st))
+        rc = self._L.psyo_render_sampled(self.h, spb, threads, None, stride, max_buckets, img.ctypes.data, C.byref(st))
         if rc != 0:
             raise RuntimeError("psyo_render_sampled failed: %d" % rc)
         return img, st.as_dict()
@@ -70,7 +75,7 @@ class OracleScene:
         wl = np.zeros(n, dtype=np.float32)
         nr = np.zeros(n, dtype=np.uint32)
         b = abi.PsyBucket(x, y, w, h)
-        rc = _lib().psyo_render_paths(self.h, C.byref(b), col.ctypes.data, wl.ctypes.data, nr.ctypes.data)
+        rc = self._L.psyo_render_paths(self.h, C.byref(b), col.ctypes.data, wl.ctypes.data, nr.ctypes.data)
         if rc != 0:
             raise RuntimeError("psyo_render_paths failed: %d" % rc)
         return col, wl, nr
@@ -80,7 +85,7 @@ class OracleScene:
         n = o["indices"].shape[0]
         order = np.zeros(n, dtype=np.uint32)
         nc = C.c_uint32(0)
-        rc = _lib().psyo_mesh_bvh_info(self.h, obj, order.ctypes.data, C.byref(nc))
+        rc = self._L.psyo_mesh_bvh_info(self.h, obj, order.ctypes.data, C.byref(nc))
         if rc != 0:
             raise RuntimeError("bvh info failed")
         return order, nc.value
