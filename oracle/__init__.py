@@ -56,6 +56,7 @@ def _bind_scene_calls(L):
     L.psyo_render_sampled.argtypes = [vp, u32, u32, vp, u32, u32, vp, vp]
     L.psyo_render_paths.argtypes = [vp, vp, vp, vp, vp]
     L.psyo_mesh_bvh_info.argtypes = [vp, u32, vp, C.POINTER(u32)]
+    L.psyo_light_tree_info.argtypes = [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]
 
 
 def lib64():
@@ -85,6 +86,7 @@ def lib():
         L.psyo_get_sample_4d.argtypes = [u32, u32, u32, u32, u32, fp]
         L.psyo_golden_ratio_sample.restype = f32
         L.psyo_golden_ratio_sample.argtypes = [u32, u32]
+        L.psyo_wavelengths.argtypes = [u32, u32, u32, u32, fp]
         L.psyo_probit.restype = f32
         L.psyo_probit.argtypes = [f32, f32]
         L.psyo_fast_exp.restype = f32
@@ -99,6 +101,10 @@ def lib():
         L.psyo_xf_lerp.argtypes = [fp, fp, f32, fp]
         L.psyo_xf_point.argtypes = [fp, fp, fp]
         L.psyo_xf_normal.argtypes = [fp, fp, fp]
+        L.psyo_xf_vector.argtypes = [fp, fp, fp]
+        L.psyo_lerp3.argtypes = [fp, fp, f32, fp]
+        L.psyo_lerp.restype = f32
+        L.psyo_lerp.argtypes = [f32, f32, f32]
         L.psyo_lerp_slice.restype = f32
         L.psyo_lerp_slice.argtypes = [fp, u32, f32]
         L.psyo_xyz_to_spectrum.argtypes = [fp, f32, fp]

@@ -1944,6 +1944,28 @@ extern "C" int psyo_render_paths(PsyoScene *s, const PsyBucket *b, float *color4
     return PSY_OK;
 }
 
+// Shape of the scene's light tree: node count, leaf count and depth (levels
+// of nodes from the root to the deepest leaf; 0 for an empty tree).
+extern "C" int psyo_light_tree_info(PsyoScene *s, uint32_t *nodes, uint32_t *leaves, uint32_t *depth) {
+    if (!s) return PSY_E_INVALID;
+    uint32_t nl = 0, dmax = 0;
+    if (!s->lt_empty) {
+        std::vector<std::pair<size_t, uint32_t>> st{{0, 1}};
+        while (!st.empty()) {
+            auto [n, d] = st.back();
+            st.pop_back();
+            dmax = std::max(dmax, d);
+            const LightTreeNode &ln = s->lt[n];
+            if (ln.leaf) { nl++; continue; }
+            for (size_t c = 0; c < ln.nchild; c++) st.push_back({ln.child0 + c, d + 1});
+        }
+    }
+    if (nodes) *nodes = s->lt_empty ? 0u : (uint32_t)s->lt.size();
+    if (leaves) *leaves = nl;
+    if (depth) *depth = dmax;
+    return PSY_OK;
+}
+
 extern "C" int psyo_mesh_bvh_info(PsyoScene *s, uint32_t object, uint32_t *tri_order, uint32_t *node_count) {
     if (!s || object >= s->objects.size() || s->objects[object].kind != PSY_OBJ_MESH) return PSY_E_INVALID;
     const Mesh &m = s->meshes[s->objects[object].index];
@@ -1961,6 +1983,12 @@ extern "C" void psyo_get_sample_4d(uint32_t i, uint32_t set, uint32_t px, uint32
     get_sample_4d(i, set, px, py, seed, out4);
 }
 extern "C" float psyo_golden_ratio_sample(uint32_t i, uint32_t scramble) { return golden_ratio_sample(i, scramble); }
+// The 4 wavelengths render_job gives sample si of pixel (x, y)
+// (src/renderer.rs:261-265 with src/color.rs:20-43).
+extern "C" void psyo_wavelengths(uint32_t si, uint32_t x, uint32_t y, uint32_t seed, float *out4) {
+    float hero = (float)map_0_1_to_wavelength(golden_ratio_sample(si, hash_u32((x << 16) ^ y, seed)));
+    for (int k = 0; k < 4; k++) out4[k] = (float)nth_wavelength(hero, k);
+}
 extern "C" float psyo_probit(float n, float width) { return probit(n, width); }
 extern "C" float psyo_fast_exp(float p) { return fast_exp(p); }
 extern "C" void psyo_traversal_table(uint8_t *out) { std::memcpy(out, TRAVERSAL_TABLE, sizeof(TRAVERSAL_TABLE)); }
@@ -1989,6 +2017,17 @@ extern "C" void psyo_xf_point(const float *m, const float *p, float *out) {
     V3 r = xf_point(v3(p[0], p[1], p[2]), x);
     out[0] = r.x; out[1] = r.y; out[2] = r.z;
 }
+extern "C" void psyo_xf_vector(const float *m, const float *v, float *out) {
+    Xf x;
+    std::memcpy(x.m, m, 48);
+    V3 r = xf_vector(v3(v[0], v[1], v[2]), x);
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+extern "C" void psyo_lerp3(const float *a, const float *b, float alpha, float *out) {
+    V3 r = lerp3(v3(a[0], a[1], a[2]), v3(b[0], b[1], b[2]), alpha);
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+extern "C" float psyo_lerp(float a, float b, float alpha) { return lerpf(a, b, alpha); }
 extern "C" void psyo_xf_normal(const float *m, const float *n, float *out) {
     Xf x;
     std::memcpy(x.m, m, 48);

@@ -53,6 +53,7 @@ uint64_t psyo_hash_u64(uint64_t n, uint64_t seed);
 float psyo_hash_u32_to_f32(uint32_t n, uint32_t seed);
 void psyo_get_sample_4d(uint32_t i, uint32_t set, uint32_t px, uint32_t py, uint32_t seed, float *out4);
 float psyo_golden_ratio_sample(uint32_t i, uint32_t scramble);
+void psyo_wavelengths(uint32_t sample, uint32_t x, uint32_t y, uint32_t seed, float *out4);
 float psyo_probit(float n, float width);
 float psyo_fast_exp(float p);
 void psyo_hilbert_d2xy(uint32_t d, uint32_t *x, uint32_t *y);
@@ -63,6 +64,9 @@ void psyo_xf_inverse(const float *a, float *out);
 void psyo_xf_lerp(const float *a, const float *b, float alpha, float *out);
 void psyo_xf_point(const float *m, const float *p, float *out);
 void psyo_xf_normal(const float *m, const float *n, float *out);
+void psyo_xf_vector(const float *m, const float *v, float *out);
+void psyo_lerp3(const float *a, const float *b, float alpha, float *out);
+float psyo_lerp(float a, float b, float alpha);
 float psyo_lerp_slice(const float *s, uint32_t n, float alpha);
 void psyo_xyz_to_spectrum(const float *xyz, float hero_wavelength, float *out4);
 void psyo_spectrum_to_xyz(const float *e4, float hero_wavelength, float *xyz_out);
@@ -77,6 +81,9 @@ int psyo_increment_ulp_check(void);
 /* BVH dump for tree-identity checks: the mesh object's triangle order after
  * the build (original triangle indices) and the number of BVH4 nodes. */
 int psyo_mesh_bvh_info(PsyoScene *s, uint32_t object, uint32_t *tri_order, uint32_t *node_count);
+/* Light tree shape: node count, leaf count, depth (levels root to deepest
+ * leaf). */
+int psyo_light_tree_info(PsyoScene *s, uint32_t *nodes, uint32_t *leaves, uint32_t *depth);
 
 /* halton::sample(index, dimension) (sub_crates/halton), restated in
  * oracle_halton.cpp; -1 for dimension >= 128. */

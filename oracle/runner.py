@@ -80,6 +80,14 @@ class OracleScene:
             raise RuntimeError("psyo_render_paths failed: %d" % rc)
         return col, wl, nr
 
+    def light_tree_info(self):
+        """(nodes, leaves, depth) of the scene's light tree."""
+        n, l, d = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        rc = self._L.psyo_light_tree_info(self.h, C.byref(n), C.byref(l), C.byref(d))
+        if rc != 0:
+            raise RuntimeError("light tree info failed")
+        return n.value, l.value, d.value
+
     def mesh_bvh_info(self, obj):
         o = self._data.objects[obj]
         n = o["indices"].shape[0]

@@ -430,6 +430,7 @@ class _Assembly:
     def __init__(self):
         self.shaders, self.objects, self.binds, self.assemblies, self.instances = {}, {}, {}, {}, []
         self.defined_at = {}  # object / assembly name -> position of its definition
+        self.shader_at = {}   # shader name -> position of its definition
 
 
 def _parse_assembly(content, sd, text, layout):
@@ -440,11 +441,19 @@ def _parse_assembly(content, sd, text, layout):
     a = _Assembly()
     for pos, c in enumerate(content):
         t = c.type_name
+        # objects and assemblies share one name space, shaders have their
+        # own; a name defined twice is rejected as AssemblyBuilder does
+        # (add_object / add_assembly / add_surface_shader, src/scene/assembly.rs:184-221)
         if t in ("MeshSurface", "SphereLight", "RectangleLight", "Assembly") and c.ident is not None:
-            a.defined_at.setdefault(c.ident, pos)
+            if c.ident in a.defined_at:
+                raise PsyFileError("line %d: '%s' is already defined in this assembly" % (_line(text, c.offset), c.ident))
+            a.defined_at[c.ident] = pos
         if t == "SurfaceShader":
             if c.is_leaf or c.ident is None:
                 raise PsyFileError("line %d: a SurfaceShader needs a $name and a body" % _line(text, c.offset))
+            if c.ident in a.shaders:
+                raise PsyFileError("line %d: shader '%s' is already defined in this assembly" % (_line(text, c.offset), c.ident))
+            a.shader_at[c.ident] = pos
             a.shaders[c.ident] = sd.add_shader(0)
             sd.shaders[a.shaders[c.ident]] = _shader(c, text)
         elif t == "MeshSurface":
@@ -489,7 +498,9 @@ def _instantiate(a, parent_keys, sd, text):
         shader = -1
         if bind:
             sname = bind[0].contents.strip()
-            if sname not in a.shaders:
+            # add_instance looks the shader up when it reads the Instance
+            # (src/scene/assembly.rs:250-255): it must be defined above it
+            if sname not in a.shaders or a.shader_at.get(sname, pos) > pos:
                 raise PsyFileError("line %d: unknown shader '%s'" % (_line(text, bind[0].offset), sname))
             shader = a.shaders[sname]
         keys = merge_transform_keys(parent_keys, [parse_matrix(t.contents, t, text) for t in c.leaves("Transform")])

@@ -1,5 +1,7 @@
 """The oracle against the known answers of the reference's own unit tests
-(and independent Python restatements of the integer hashes)."""
+(each cites the reference test it repeats) and against independent Python
+restatements of the integer hashes, the samplers' hash branch, the
+wavelength mapping and the traversal table generator."""
 import ctypes as C
 import os
 
@@ -15,7 +17,7 @@ def xf(*v):
 
 
 def test_transform_multiply_kat(oracle_lib):
-    # sub_crates/math3d/src/transform.rs:181-194
+    # sub_crates/math3d/src/transform.rs:153-166 (multiply_test)
     a = xf(1.0, 2.0, 2.0, 1.5, 3.0, 6.0, 7.0, 8.0, 9.0, 2.0, 11.0, 12.0)
     b = xf(1.0, 5.0, 9.0, 13.0, 2.0, 6.0, 10.0, 14.0, 3.0, 7.0, 11.0, 15.0)
     out = F12()
@@ -24,7 +26,7 @@ def test_transform_multiply_kat(oracle_lib):
 
 
 def test_transform_inverse_kat(oracle_lib):
-    # sub_crates/math3d/src/transform.rs:196-205: a * a^-1 ~= identity (1e-7)
+    # sub_crates/math3d/src/transform.rs:168-177 (inverse_test): a * a^-1 ~= identity (1e-7)
     a = xf(1.0, 0.33, 0.0, -2.0, 0.0, 1.0, 0.0, 0.0, 2.1, 0.7, 1.3, 0.0)
     inv, prod = F12(), F12()
     oracle_lib.psyo_xf_inverse(a, inv)
@@ -35,7 +37,7 @@ def test_transform_inverse_kat(oracle_lib):
 
 
 def test_point_matrix_kat(oracle_lib):
-    # sub_crates/math3d/src/point.rs:372-390
+    # sub_crates/math3d/src/point.rs:166-184 (mul_matrix_1, mul_matrix_2)
     m = xf(1.0, 2.0, 2.0, 1.5, 3.0, 6.0, 7.0, 8.0, 9.0, 2.0, 11.0, 12.0)
     out = F3()
     oracle_lib.psyo_xf_point(m, F3(1.0, 2.5, 4.0), out)
@@ -43,7 +45,7 @@ def test_point_matrix_kat(oracle_lib):
 
 
 def test_point_matrix_compose(oracle_lib):
-    # sub_crates/math3d/src/point.rs:392-407: p * (m1 * m2) ~= (p * m1) * m2
+    # sub_crates/math3d/src/point.rs:186-201 (mul_matrix_3): p * (m1 * m2) ~= (p * m1) * m2
     m1 = xf(1.0, 2.0, 2.0, 1.5, 3.0, 6.0, 7.0, 8.0, 9.0, 2.0, 11.0, 12.0)
     m2 = xf(4.0, 1.0, 2.0, 3.5, 3.0, 6.0, 5.0, 2.0, 2.0, 2.0, 4.0, 12.0)
     p = F3(1.0, 2.5, 4.0)
@@ -56,7 +58,7 @@ def test_point_matrix_compose(oracle_lib):
 
 
 def test_lerp_matrix_kat(oracle_lib):
-    # src/lerp.rs:526-550
+    # src/lerp.rs:216-240 (lerp_matrix)
     a = xf(0.0, 2.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0, 8.0, 9.0, 10.0, 11.0)
     b = xf(-1.0, 1.0, 3.0, 4.0, 5.0, 6.0, 7.0, 8.0, 9.0, 10.0, 11.0, 12.0)
     expect = {0.25: [-0.25, 1.75, 2.25, 3.25, 4.25, 5.25, 6.25, 7.25, 8.25, 9.25, 10.25, 11.25],
@@ -72,20 +74,53 @@ def test_lerp_matrix_kat(oracle_lib):
         assert list(out) == e
 
 
+def test_vector_matrix_kat(oracle_lib):
+    # sub_crates/math3d/src/vector.rs:220-236 (mul_matrix_1, mul_matrix_2)
+    m = xf(1.0, 2.0, 2.0, 1.5, 3.0, 6.0, 7.0, 8.0, 9.0, 2.0, 11.0, 12.0)
+    out = F3()
+    oracle_lib.psyo_xf_vector(m, F3(1.0, 2.5, 4.0), out)
+    assert list(out) == [14.0, 46.0, 58.0]
+
+
+def test_normal_matrix_kat(oracle_lib):
+    # sub_crates/math3d/src/normal.rs:209-220 (mul_matrix_1): within 4 ulps
+    m = xf(1.0, 2.0, 2.0, 1.5, 3.0, 6.0, 7.0, 8.0, 9.0, 2.0, 11.0, 12.0)
+    out = F3()
+    oracle_lib.psyo_xf_normal(m, F3(1.0, 2.5, 4.0), out)
+    for got, want in zip(out, (-4.0625, 1.78125, -0.03125)):
+        g, w = np.float32(got).view(np.int32), np.float32(want).view(np.int32)
+        assert abs(int(g) - int(w)) <= 4, (got, want)
+
+
+@pytest.mark.parametrize("alpha,want", [(0.0, 1.0), (1.0, 2.0), (0.5, 1.5)])
+def test_lerp_kat(oracle_lib, alpha, want):
+    # src/lerp.rs:141-166 (lerp1, lerp2, lerp3)
+    assert oracle_lib.psyo_lerp(1.0, 2.0, alpha) == want
+
+
+@pytest.mark.parametrize("alpha,want", [(0.0, (1.0, 2.0, 1.0)), (1.0, (-2.0, 1.0, -1.0)), (0.5, (-0.5, 1.5, 0.0))])
+def test_lerp_point_normal_vector_kat(oracle_lib, alpha, want):
+    # src/lerp.rs:242-321 (lerp_point_*, lerp_normal_*, lerp_vector_*: one
+    # storage type and one lerp for all three here, as in math3d over glam)
+    out = F3()
+    oracle_lib.psyo_lerp3(F3(1.0, 2.0, 1.0), F3(-2.0, 1.0, -1.0), alpha, out)
+    assert tuple(out) == want
+
+
 @pytest.mark.parametrize("alpha,want", [(0.0, 0.0), (1.0, 4.0), (0.5, 2.0), (0.25, 1.0), (0.75, 3.0), (0.625, 2.5)])
 def test_lerp_slice_kat(oracle_lib, alpha, want):
-    # src/lerp.rs:478-524
+    # src/lerp.rs:166-214 (lerp_slice1 .. lerp_slice6)
     s = (C.c_float * 5)(0.0, 1.0, 2.0, 3.0, 4.0)
     assert oracle_lib.psyo_lerp_slice(s, 5, alpha) == want
 
 
 def test_ulp_kats(oracle_lib):
-    # src/fp_utils.rs:84-131
+    # src/fp_utils.rs:88-130 (inc_ulp, dec_ulp, inc_ulp_zero, dec_ulp_zero, inc_dec_ulp, dec_inc_ulp)
     assert oracle_lib.psyo_increment_ulp_check() == 1
 
 
 def test_hilbert_reversible(oracle_lib):
-    # src/hilbert.rs:65-77
+    # src/hilbert.rs:69-76 (reversible; d = 54 and more)
     x, y = C.c_uint32(), C.c_uint32()
     for d in (54, 0, 1, 7, 1000, 65535):
         oracle_lib.psyo_hilbert_d2xy(d, C.byref(x), C.byref(y))
@@ -94,7 +129,7 @@ def test_hilbert_reversible(oracle_lib):
 
 @pytest.mark.parametrize("place", [5, 3, 0, 9])
 def test_quick_select(oracle_lib, place):
-    # src/algorithm.rs:307-351
+    # src/algorithm.rs:324-350 (quick_select_1 .. quick_select_4)
     lst = (C.c_int32 * 10)(8, 9, 7, 4, 6, 1, 0, 5, 3, 2)
     assert oracle_lib.psyo_quick_select_ints(lst, 10, place) == place
 
@@ -128,19 +163,105 @@ def test_hashes_bit_exact(oracle_lib):
         assert oracle_lib.psyo_hash_u32_to_f32(n, s) == f
 
 
+def _golden_ratio_sample(i, scramble):
+    # src/renderer.rs:728-737
+    n = ((i + _hash_u32(scramble, 0)) * 2654435769) & 0xFFFFFFFF
+    return np.float32(np.float32(n) * np.float32(1.0 / 4294967296.0))
+
+
+def _wavelengths(si, x, y, seed):
+    # render_job's hero wavelength (src/renderer.rs:261-265) and
+    # wavelengths() (src/color.rs:20-43), in f32 steps
+    g = _golden_ratio_sample(si, _hash_u32(((x << 16) ^ y) & 0xFFFFFFFF, seed))
+    hero = np.float32(g * np.float32(320.0)) + np.float32(380.0)
+    out = []
+    for k in range(4):
+        wl = np.float32(hero + np.float32(np.float32(80.0) * np.float32(k)))
+        out.append(np.float32(wl - np.float32(320.0)) if wl > np.float32(700.0) else wl)
+    return np.array(out, dtype=np.float32)
+
+
+def _sample_4d_hash_branch(i, dset, px, py, seed):
+    # get_sample_4d for dimension sets past the Sobol sets (src/renderer.rs:714-723)
+    s = (px ^ ((py << 16) & 0xFFFFFFFF) ^ ((seed * 0x736caf6f) & 0xFFFFFFFF)) & 0xFFFFFFFF
+    return np.array([np.float32(np.float32(_hash_u32(((dset * 4 + k) ^ ((i << 16) & 0xFFFFFFFF)) & 0xFFFFFFFF, s))
+                                * np.float32(1.0 / 4294967296.0)) for k in range(4)], dtype=np.float32)
+
+
 def test_golden_ratio_and_wavelength(oracle_lib):
     for i in range(64):
         for scr in (0, 1, 0xdeadbeef):
-            n = ((i + _hash_u32(scr, 0)) * 2654435769) & 0xFFFFFFFF
-            want = np.float32(np.float32(n) * np.float32(1.0 / 4294967296.0))
-            assert oracle_lib.psyo_golden_ratio_sample(i, scr) == want
+            assert oracle_lib.psyo_golden_ratio_sample(i, scr) == _golden_ratio_sample(i, scr)
+    out = (C.c_float * 4)()
+    rng = np.random.default_rng(11)
+    for si, x, y, seed in rng.integers(0, [4096, 4096, 4096, 2 ** 32], size=(300, 4)):
+        oracle_lib.psyo_wavelengths(int(si), int(x), int(y), int(seed), out)
+        assert np.array_equal(np.array(list(out), dtype=np.float32), _wavelengths(int(si), int(x), int(y), int(seed)))
+
+
+def test_sample_4d_hash_branch(oracle_lib):
+    out = (C.c_float * 4)()
+    rng = np.random.default_rng(12)
+    for i, dset, px, py, seed in rng.integers(0, [65536, 64, 4096, 4096, 2 ** 32], size=(300, 5)):
+        dset = int(dset) + 2  # sets 0 and 1 are Sobol-Burley
+        oracle_lib.psyo_get_sample_4d(int(i), dset, int(px), int(py), int(seed), out)
+        want = _sample_4d_hash_branch(int(i), dset, int(px), int(py), int(seed))
+        assert np.array_equal(np.array(list(out), dtype=np.float32), want)
+
+
+def traversal_table_restated():
+    """The traversal table of sub_crates/bvh_order/build.rs:17-76: for each
+    ray octant, 27 four-child rows (split axes s0 top, s1 left, s2 right),
+    9 + 9 three-child rows (left-heavy, right-heavy) and 3 two-child rows;
+    each entry packs a child permutation 2 bits per position."""
+    table = []
+    for rd in range(8):
+        ray = [rd & 1, (rd >> 1) & 1, (rd >> 2) & 1]
+        row = []
+        for s2 in range(3):
+            for s1 in range(3):
+                for s0 in range(3):
+                    p = [0, 1, 2, 3]
+                    if ray[s1]:
+                        p[0], p[1] = p[1], p[0]
+                    if ray[s2]:
+                        p[2], p[3] = p[3], p[2]
+                    if ray[s0]:
+                        p = [p[2], p[3], p[0], p[1]]
+                    row.append(p[0] + (p[1] << 2) + (p[2] << 4) + (p[3] << 6))
+        for s1 in range(3):
+            for s0 in range(3):
+                p = [0, 1, 2]
+                if ray[s1]:
+                    p[0], p[1] = p[1], p[0]
+                if ray[s0]:
+                    p[0], p[1] = p[1], p[0]
+                    p[0], p[2] = p[2], p[0]
+                row.append(p[0] + (p[1] << 2) + (p[2] << 4))
+        for s1 in range(3):
+            for s0 in range(3):
+                p = [0, 1, 2]
+                if ray[s1]:
+                    p[1], p[2] = p[2], p[1]
+                if ray[s0]:
+                    p[0], p[2] = p[2], p[0]
+                    p[0], p[1] = p[1], p[0]
+                row.append(p[0] + (p[1] << 2) + (p[2] << 4))
+        for s0 in range(3):
+            p = [0, 1]
+            if ray[s0]:
+                p[0], p[1] = p[1], p[0]
+            row.append(p[0] + (p[1] << 2))
+        table.append(row)
+    return np.array(table, dtype=np.uint8)
 
 
 def test_traversal_table(oracle_lib):
-    # sub_crates/bvh_order/build.rs: every row is a permutation of the children
+    # equals the generator's table, entry for entry
     t = (C.c_uint8 * (8 * 48))()
     oracle_lib.psyo_traversal_table(t)
     t = np.frombuffer(t, dtype=np.uint8).reshape(8, 48)
+    assert np.array_equal(t, traversal_table_restated())
     for rd in range(8):
         for k in range(27):
             assert sorted((t[rd, k] >> (2 * i)) & 3 for i in range(4)) == [0, 1, 2, 3]
@@ -199,9 +320,12 @@ def test_triangle_watertight_shared_edge(oracle_lib):
 
 
 def test_meng_tables_match_reference():
-    src = "/root/reference/sub_crates/spectral_upsampling/src/meng/meng_spectra_tables.rs"
-    if not os.path.exists(src):
-        pytest.skip("reference tree not present")
+    """Regenerates the spectral tables from the reference's source file when
+    PSY_REFERENCE_ROOT names a checkout of the reference (skipped otherwise)."""
+    root = os.environ.get("PSY_REFERENCE_ROOT", "")
+    src = os.path.join(root, "sub_crates", "spectral_upsampling", "src", "meng", "meng_spectra_tables.rs")
+    if not root or not os.path.exists(src):
+        pytest.skip("PSY_REFERENCE_ROOT not set to a reference checkout")
     import subprocess
     import sys
     import tempfile

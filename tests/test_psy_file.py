@@ -153,10 +153,13 @@ def test_errors_name_the_line(bad, msg):
     assert msg in str(e.value)
 
 
-REF = "/root/reference/example_scenes"
+# A checkout of the reference (its example_scenes/ directory), named by the
+# PSY_REFERENCE_ROOT environment variable; the test is skipped without one.
+REF = os.path.join(os.environ.get("PSY_REFERENCE_ROOT", ""), "example_scenes")
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference example scenes not present")
+@pytest.mark.skipif(not os.environ.get("PSY_REFERENCE_ROOT") or not os.path.isdir(REF),
+                    reason="PSY_REFERENCE_ROOT not set to a reference checkout")
 @pytest.mark.parametrize("name,objects,instances,shaders,res", [
     ("cube.psy", 3, 3, 1, (960, 540)),
     ("cornell_box.psy", None, None, 3, (512, 512)),

@@ -154,9 +154,35 @@ _LATE = NESTED.replace(
     "        Instance { Data [$tri] SurfaceShaderBind [$Red] }\n        MeshSurface $tri")
 
 
+# a shader bound by an Instance above the shader's definition
+_LATE_SHADER = NESTED.replace(
+    "        SurfaceShader $Red { Type [Lambert] Color [rec709, 0.8 0.1 0.1] }\n        MeshSurface $tri",
+    "        MeshSurface $tri").replace(
+    "        Instance { Data [$tri] SurfaceShaderBind [$Red] }\n",
+    "        Instance { Data [$tri] SurfaceShaderBind [$Red] }\n"
+    "        SurfaceShader $Red { Type [Lambert] Color [rec709, 0.8 0.1 0.1] }\n")
+# a second object of the same name after an Instance of the first
+_REDEFINED = NESTED.replace(
+    "        Instance { Data [$tri] SurfaceShaderBind [$Red] }\n",
+    "        Instance { Data [$tri] SurfaceShaderBind [$Red] }\n"
+    "        MeshSurface $tri { Vertices [0 0 0  3 0 0  0 3 0] FaceVertCounts [3] FaceVertIndices [0 1 2] }\n")
+_REDEFINED_SHADER = NESTED.replace(
+    "        MeshSurface $tri { Vertices [0 0 0  1 0 0",
+    "        SurfaceShader $Red { Type [Lambert] Color [rec709, 0.2 0.2 0.2] }\n"
+    "        MeshSurface $tri { Vertices [0 0 0  1 0 0")
+
+
+def test_mutated_scenes_differ_from_nested():
+    for t in (_LATE, _LATE_SHADER, _REDEFINED, _REDEFINED_SHADER):
+        assert t != NESTED
+
+
 @pytest.mark.parametrize("bad,msg", [
     (NESTED.replace("Data [$pair]", "Data [$nothere]"), "unknown data"),
     (_LATE, "unknown data"),  # instanced above its definition, which the reference rejects
+    (_LATE_SHADER, "unknown shader"),  # bound above the shader's definition (src/scene/assembly.rs:250-255)
+    (_REDEFINED, "already defined"),  # AssemblyBuilder::add_object rejects a used name
+    (_REDEFINED_SHADER, "already defined"),  # add_surface_shader rejects a used name
     (NESTED.replace("Instance { Data [$tri] SurfaceShaderBind [$Red] }",
                     "Instance { Data [$quad] }"), "unknown data"),  # $quad is scoped to $cluster
 ])
