@@ -291,6 +291,20 @@ int psy_render_image_device(PsyScene *scene, const uint32_t *crop,
 int psy_render_image(PsyScene *scene, const uint32_t *crop, float *xyz_out,
                      PsyRenderStats *stats);
 
+/* One share of a frame rendered on several GPUs: the image rows first_row,
+ * first_row + row_step, first_row + 2 * row_step, ... (all columns), into
+ * d_xyz, a DEVICE buffer of n * width * 3 floats holding those rows in order
+ * (n = ceil((height - first_row) / row_step)).  Each pixel is the one a
+ * whole-image render gives.  With row_step = N and first_row = rank, N GPUs
+ * split a frame into interleaved rows, which balances their work as the
+ * reference's bucket queue balances its threads (Renderer::render hands
+ * Hilbert-ordered buckets to whichever thread is free,
+ * src/renderer.rs:150-180).  Asynchronous on `stream` (NULL: the scene's
+ * stream); stats (if not NULL) are filled after an internal sync.
+ * row_step = 0 returns PSY_E_INVALID. */
+int psy_render_rows_device(PsyScene *scene, uint32_t first_row, uint32_t row_step,
+                           float *d_xyz, void *stream, PsyRenderStats *stats);
+
 /* Image output as the reference writes PNGs (Image::write_png,
  * src/image.rs:138-164): the XYZ image d_xyz (width*height*3 floats, row 0
  * first, as the render calls produce) becomes RGBA8 in d_rgba

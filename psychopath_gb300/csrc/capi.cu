@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "psy_debug.h"
 #include "scene_build.h"
 #include "radix_sort.h"
 #include "scene_handle.h"
@@ -38,6 +39,17 @@ int cuda_fail(cudaError_t e, const char *what) {
 
 std::once_flag g_const_once;
 int g_device_init = 0;
+// Sobol directions, traversal tables and the unassigned-shader colour to the
+// device's constant banks (once per process).
+void upload_device_constants() {
+    std::call_once(g_const_once, []() {
+        psy_upload_constants();
+        float m[3];
+        unassigned_magenta_xyz(m);
+        psy_set_magenta(m);
+        g_device_init = 1;
+    });
+}
 
 }  // namespace
 
@@ -162,13 +174,7 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
     int rc = build_host_scene(desc, opts, hs, err, have_gpu ? &gpu_build : nullptr);
     if (rc != PSY_OK) return fail(rc, err);
     if (!have_gpu) return fail(PSY_E_CUDA, "no CUDA device available");
-    std::call_once(g_const_once, []() {
-        psy_upload_constants();
-        float m[3];
-        unassigned_magenta_xyz(m);
-        psy_set_magenta(m);
-        g_device_init = 1;
-    });
+    upload_device_constants();
     if (!psy_trace_tables_ready()) return fail(PSY_E_CUDA, "traversal push tables were not uploaded");
     PsyScene *s = new PsyScene();
     if (cudaGetDevice(&s->device) != cudaSuccess ||
@@ -225,9 +231,9 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
                     if (!(lo[a][c] <= hi[a][c])) g.ordered_slabs = 0u;
         }
     }
-    // the static-scene traversal: FP32 nodes without motion keys, ordered
-    // boxes, static meshes, untransformed mesh instances
-    g.static_fast = (g.use_fp16 == 0u && g.ordered_slabs == 1u) ? 1u : 0u;
+    // the static-scene traversal: nodes without motion keys (FP32 or FP16),
+    // ordered boxes, static meshes, untransformed mesh instances
+    g.static_fast = g.ordered_slabs == 1u ? 1u : 0u;
     for (const GNode &n : hs.nodes)
         if (n.meta.y > 1) g.static_fast = 0u;
     for (const GMesh &m : hs.meshes)
@@ -495,25 +501,27 @@ int alloc_wave_bufs(WaveBufs &B, uint32_t cap, uint32_t cap_waves, bool sorting,
     return PSY_OK;
 }
 
-// Render the pixels of region (x0, y0, w, h) of a cam_w x cam_h image into
-// d_xyz (row stride img_w; image pixel (ox, oy) is d_xyz[0]) as a sequence of
-// waves of whole pixel rows.
+// Render h rows of w pixels from (x0, y0) of a cam_w x cam_h image -- image
+// rows y0, y0 + ystep, ..., y0 + (h - 1) * ystep -- into d_xyz (row stride
+// img_w): region row k, column x lands in out row orow + k, column x - ox.
+// Waves of `rows` region rows each.
 int render_region_core(PsyScene *s, const WaveBufs &B, uint32_t rows, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
-                       uint32_t spp, uint32_t seed, float *d_xyz, uint32_t img_w, uint32_t ox, uint32_t oy,
-                       uint32_t cam_w, uint32_t cam_h, cudaStream_t st, PsyRenderStats *stats) {
+                       uint32_t spp, uint32_t seed, float *d_xyz, uint32_t img_w, uint32_t ox, uint32_t orow,
+                       uint32_t cam_w, uint32_t cam_h, cudaStream_t st, PsyRenderStats *stats, uint32_t ystep) {
     if (spp == 0 || w == 0 || h == 0) return PSY_OK;
     uint32_t iters = 2 * s->g.max_bounces + 3;
     bool timing = stats != nullptr;
     // one single-segment descriptor per wave, uploaded with one copy
     std::vector<WaveDesc> waves;
-    for (uint32_t y = y0; y < y0 + h; y += rows) {
+    for (uint32_t k = 0; k < h; k += rows) {
         WaveDesc d{};
         WaveSeg &g = d.seg[0];
-        g.x0 = x0; g.y0 = y; g.w = w; g.h = std::min(rows, y0 + h - y);
+        g.x0 = x0; g.y0 = y0 + k * ystep; g.w = w; g.h = std::min(rows, h - k);
+        g.ystep = ystep;
         g.spp = spp; g.seed = seed;
         g.img_w = cam_w; g.img_h = cam_h;
         g.out = d_xyz; g.out_stride = img_w;
-        g.out_x0 = ox; g.out_y0 = oy;
+        g.out_x0 = ox; g.orow0 = orow + k;
         d.nseg = 1; d.npix = g.w * g.h; d.npaths = d.npix * spp;
         waves.push_back(d);
     }
@@ -582,9 +590,12 @@ int render_region_core(PsyScene *s, const WaveBufs &B, uint32_t rows, uint32_t x
 
 // Render with the scene's own wavefront buffers (allocated on first use,
 // sized for waves of whole pixel rows up to wave_paths paths).
+// Region (x0, y0, w, h) into d_xyz with row stride img_w, where image pixel
+// (ox, oy) is d_xyz[0]; with ystep > 1 the region is the h rows y0,
+// y0 + ystep, ... and out row k holds region row k (oy unused).
 static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h, uint32_t spp, uint32_t seed,
                          float *d_xyz, uint32_t img_w, uint32_t ox, uint32_t oy, cudaStream_t st,
-                         PsyRenderStats *stats, uint32_t cam_w = 0, uint32_t cam_h = 0) {
+                         PsyRenderStats *stats, uint32_t cam_w = 0, uint32_t cam_h = 0, uint32_t ystep = 1) {
     if (cam_w == 0) { cam_w = s->g.width; cam_h = s->g.height; }
     if (spp == 0 || w == 0 || h == 0) return PSY_OK;
     uint64_t row_paths = (uint64_t)w * spp;
@@ -617,7 +628,8 @@ static int render_region(PsyScene *s, uint32_t x0, uint32_t y0, uint32_t w, uint
     }
     B.waves = s->d_waves;
     B.cap_waves = s->cap_waves;
-    return render_region_core(s, B, rows, x0, y0, w, h, spp, seed, d_xyz, img_w, ox, oy, cam_w, cam_h, st, stats);
+    return render_region_core(s, B, rows, x0, y0, w, h, spp, seed, d_xyz, img_w, ox, ystep > 1 ? 0 : y0 - oy, cam_w,
+                              cam_h, st, stats, ystep);
 }
 
 
@@ -706,8 +718,8 @@ extern "C" int psy_render_bucket_noalloc(PsyScene *s, const PsyBucket *b, uint32
     // the bucket's pixels land at (x - b.x, y - b.y) of the bucket-sized output
     int sort = s->sort_bits;
     s->sort_bits = 0;
-    r = render_region_core(s, B, b->h, b->x, b->y, b->w, b->h, spp, seed, d_xyz_out, b->w, b->x, b->y, s->g.width,
-                           s->g.height, st, nullptr);
+    r = render_region_core(s, B, b->h, b->x, b->y, b->w, b->h, spp, seed, d_xyz_out, b->w, b->x, 0, s->g.width,
+                           s->g.height, st, nullptr, 1);
     s->sort_bits = sort;
     if (r != PSY_OK) return r;
     int h = 0;
@@ -733,6 +745,21 @@ int psy_render_image_device(PsyScene *s, const uint32_t *crop, float *d_xyz, voi
     cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
     if (stats) std::memset(stats, 0, sizeof(*stats));
     int r = render_region(s, x0, y0, w, h, s->g.spp, s->g.seed, d_xyz, W, 0, 0, st, stats);
+    if (r != PSY_OK) return r;
+    if (stats) return check_err(s);
+    return PSY_OK;
+}
+
+int psy_render_rows_device(PsyScene *s, uint32_t first_row, uint32_t row_step, float *d_xyz, void *stream,
+                           PsyRenderStats *stats) {
+    if (!s || !d_xyz || row_step == 0) return fail(PSY_E_INVALID, "null argument or zero row step");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    uint32_t W = s->g.width, H = s->g.height;
+    if (first_row >= H) return PSY_OK;
+    uint32_t n = (H - first_row + row_step - 1) / row_step;
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    int r = render_region(s, 0, first_row, W, n, s->g.spp, s->g.seed, d_xyz, W, 0, 0, st, stats, 0, 0, row_step);
     if (r != PSY_OK) return r;
     if (stats) return check_err(s);
     return PSY_OK;
@@ -1238,6 +1265,46 @@ int psy_debug_set_graph(PsyScene *s, int on) {
     std::lock_guard<std::mutex> lk(s->mu);
     s->use_graph = on != 0;
     if (!s->use_graph) s->graph.reset();
+    return PSY_OK;
+}
+// One bucket as one wave; every path's final colour and hero wavelength.
+int psy_debug_render_paths(PsyScene *s, const PsyBucket *b, uint32_t spp, uint32_t seed, float *color4,
+                           float *wavelength) {
+    if (!s || !b || !color4) return fail(PSY_E_INVALID, "null argument");
+    if (b->w == 0 || b->h == 0 || spp == 0) return fail(PSY_E_INVALID, "empty bucket or zero spp");
+    if ((uint64_t)b->x + b->w > s->g.width || (uint64_t)b->y + b->h > s->g.height)
+        return fail(PSY_E_INVALID, "bucket outside the image");
+    uint64_t n = (uint64_t)b->w * b->h * spp;
+    if (n > (1u << 20)) return fail(PSY_E_INVALID, "at most 1,048,576 samples");
+    std::lock_guard<std::mutex> lk(s->mu);
+    size_t bytes = (size_t)b->w * b->h * 3 * sizeof(float);
+    if (s->cap_xyz < bytes) {
+        if (s->d_xyz) cudaFree(s->d_xyz);
+        s->d_xyz = nullptr;
+        CK(cudaMalloc((void **)&s->d_xyz, bytes), "cudaMalloc bucket");
+        s->cap_xyz = bytes;
+    }
+    uint32_t wave = s->wave_paths;
+    s->wave_paths = std::max<uint32_t>(wave, (uint32_t)n);  // the whole bucket in one wave
+    int r = render_region(s, b->x, b->y, b->w, b->h, spp, seed, s->d_xyz, b->w, b->x, b->y, s->stream, nullptr);
+    s->wave_paths = wave;
+    if (r != PSY_OK) return r;
+    std::vector<float2> tw(n);
+    CK(cudaMemcpyAsync(color4, s->P.color, n * sizeof(float4), cudaMemcpyDeviceToHost, s->stream), "copy colours");
+    CK(cudaMemcpyAsync(tw.data(), s->P.tw, n * sizeof(float2), cudaMemcpyDeviceToHost, s->stream), "copy wavelengths");
+    CK(cudaStreamSynchronize(s->stream), "sync");
+    if (wavelength)
+        for (size_t i = 0; i < n; i++) wavelength[i] = tw[i].y;
+    return check_err(s);
+}
+// Sampler values on the device (ops in psy_debug.h).
+int psy_debug_samplers(int op, const uint32_t *d_args, uint32_t n, uint32_t *d_out, void *stream) {
+    if (op < 0 || op > 4) return fail(PSY_E_INVALID, "bad sampler op");
+    if (n && (!d_args || !d_out)) return fail(PSY_E_INVALID, "null argument");
+    upload_device_constants();  // the Sobol direction numbers
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(launch_debug_samplers(op, d_args, n, d_out, st), "sampler kernel");
+    CK(cudaStreamSynchronize(st), "sync");
     return PSY_OK;
 }
 

@@ -130,7 +130,7 @@ __global__ void k_camera(GScene S, const WaveDesc *__restrict__ gwave, PathState
     if (p >= n) return;
     const WaveSeg &w = wdesc.seg[seg_of_path(wdesc, p)];
     uint32_t lp = (p - w.path_begin) / w.spp, si = (p - w.path_begin) - lp * w.spp;
-    uint32_t x = w.x0 + lp % w.w, y = w.y0 + lp / w.w;
+    uint32_t x = w.x0 + lp % w.w, y = w.y0 + (lp / w.w) * w.ystep;
     float cmpx = 1.0f / (float)w.img_w, cmpy = 1.0f / (float)w.img_h;
     float min_x = -1.0f, max_x = 1.0f;
     float min_y = -((float)w.img_h / (float)w.img_w), max_y = (float)w.img_h / (float)w.img_w;
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade(GScene S, const WaveDesc *_
                 uint32_t lp = p - w.path_begin;
                 uint32_t pix = lp / w.spp;
                 uint32_t si = lp - pix * w.spp;
-                uint32_t px = w.x0 + pix % w.w, py = w.y0 + pix / w.w;
+                uint32_t px = w.x0 + pix % w.w, py = w.y0 + (pix / w.w) * w.ystep;
                 if (ki.x == PSY_HIT_SURFACE_K || ki.x == PSY_HIT_LIGHT_K) {
                     HitRec h;
                     h.kind = ki.x; h.prim = ki.y; h.slot = ki.z;
@@ -480,7 +480,8 @@ __global__ void k_accumulate(GScene S, const WaveDesc *__restrict__ gwave, PathS
     if (q >= wdesc.npix) return;
     const WaveSeg &w = wdesc.seg[seg_of_pixel(wdesc, q)];
     uint32_t lq = q - w.pix_begin;
-    uint32_t x = w.x0 + lq % w.w, y = w.y0 + lq / w.w;
+    uint32_t lr = lq / w.w;
+    uint32_t x = w.x0 + (lq - lr * w.w), y = w.y0 + lr * w.ystep;
     float inv = (float)w.spp;
     V3 acc = v3(0.0f, 0.0f, 0.0f);
     for (uint32_t s = 0; s < w.spp; s++) {
@@ -488,13 +489,55 @@ __global__ void k_accumulate(GScene S, const WaveDesc *__restrict__ gwave, PathS
         V3 c = xyz_from_spectral(v4(P.color[p]), P.tw[p].y);
         acc = acc + (c / inv);
     }
-    float *o = w.out + ((size_t)(y - w.out_y0) * w.out_stride + (x - w.out_x0)) * 3;
+    float *o = w.out + ((size_t)(w.orow0 + lr) * w.out_stride + (x - w.out_x0)) * 3;
     o[0] = acc.x; o[1] = acc.y; o[2] = acc.z;
 }
 
 cudaError_t launch_accumulate(const GScene &S, const WaveDesc *d_wave, uint32_t max_pix, PathState P, cudaStream_t st) {
     if (max_pix == 0) return cudaSuccess;
     k_accumulate<<<(max_pix + 127) / 128, 128, 0, st>>>(S, d_wave, P);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ sampler values (tests)
+// The samplers of the render path evaluated on the device for bit-for-bit
+// comparison with the oracle.  args[i] = (a, b, c, d, e); out[i] = 4 words:
+//   op 0: hash_u32(a, b)                                   (src/hash.rs:1-10)
+//   op 1: hash_u32_to_f32(a, b), f32 bits                  (src/hash.rs:26-29)
+//   op 2: golden_ratio_sample(a, b), f32 bits              (src/renderer.rs:728-737)
+//   op 3: get_sample_4d(i = a, set = b, px = c, py = d, seed = e), 4 x f32 bits
+//                                                          (src/renderer.rs:698-725)
+//   op 4: the 4 wavelengths of sample a of pixel (c, d) with seed e, f32 bits
+//         (hero from golden_ratio_sample as render_job does, src/renderer.rs:261-265;
+//          wavelengths, src/color.rs:20-43)
+__global__ void k_debug_samplers(int op, const uint32_t *__restrict__ args, uint32_t n, uint32_t *__restrict__ out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t *a = args + (size_t)i * 5;
+    uint32_t *o = out + (size_t)i * 4;
+    float f[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    uint32_t u0 = 0;
+    if (op == 0) {
+        u0 = hash_u32(a[0], a[1]);
+    } else if (op == 1) {
+        u0 = __float_as_uint(hash_u32_to_f32(a[0], a[1]));
+    } else if (op == 2) {
+        u0 = __float_as_uint(golden_ratio_sample(a[0], a[1]));
+    } else if (op == 3) {
+        get_sample_4d(a[0], a[1], a[2], a[3], a[4], f);
+    } else {
+        float hero = map_0_1_to_wavelength(golden_ratio_sample(a[0], hash_u32((a[2] << 16) ^ a[3], a[4])));
+        for (int k = 0; k < 4; k++) f[k] = nth_wavelength(hero, k);
+    }
+    if (op <= 2) {
+        o[0] = u0; o[1] = 0u; o[2] = 0u; o[3] = 0u;
+    } else {
+        for (int k = 0; k < 4; k++) o[k] = __float_as_uint(f[k]);
+    }
+}
+cudaError_t launch_debug_samplers(int op, const uint32_t *d_args, uint32_t n, uint32_t *d_out, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_debug_samplers<<<(n + 127) / 128, 128, 0, st>>>(op, d_args, n, d_out);
     return cudaGetLastError();
 }
 

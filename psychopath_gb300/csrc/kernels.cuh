@@ -43,9 +43,9 @@ struct WaveSeg {
     uint32_t out_stride;    // row stride of `out` in pixels
     uint32_t path_begin;    // first path of the segment in the wave
     uint32_t pix_begin;     // first pixel of the segment in the wave
-    uint32_t out_x0;        // image pixel (out_x0, out_y0) is out[0]
-    uint32_t out_y0;
-    uint32_t pad;
+    uint32_t out_x0;        // out column of image column x: x - out_x0
+    uint32_t orow0;         // out row of the segment's first row
+    uint32_t ystep;         // image rows of the segment: y0, y0 + ystep, ... (h rows)
 };
 struct WaveDesc {
     uint32_t nseg, npaths, npix, pad;
@@ -161,9 +161,13 @@ struct WaveBufs {
     uint32_t cap_waves;
 };
 // Per-pixel XYZ (sum over samples in sample order / spp) into each segment's
-// image, out[((y - out_y0) * out_stride + x - out_x0) * 3].  The grid covers
-// max_pix pixels.
+// image: local row r (image row y0 + r * ystep) and column x land at
+// out[((orow0 + r) * out_stride + x - out_x0) * 3].  The grid covers max_pix
+// pixels.
 cudaError_t launch_accumulate(const GScene &S, const WaveDesc *d_wave, uint32_t max_pix, PathState P, cudaStream_t st);
+// Sampler values for tests (op 0-4 as psy_debug_samplers documents):
+// d_args holds n rows of 5 words, d_out n rows of 4 words.
+cudaError_t launch_debug_samplers(int op, const uint32_t *d_args, uint32_t n, uint32_t *d_out, cudaStream_t st);
 // 3x3 matrix passed by value to a kernel.
 struct Mat3f {
     float m[9];

@@ -162,6 +162,7 @@ bool issue_wave(PsyServer *s, Lane &L, std::string &err) {
         g.spp = q->r.spp; g.seed = q->r.seed;
         g.img_w = q->r.width; g.img_h = q->r.height;
         g.out = q->d_img; g.out_stride = q->r.width;
+        g.ystep = 1; g.orow0 = q->next_row;
         g.path_begin = paths; g.pix_begin = pix;
         paths += take * row_paths;
         pix += take * q->r.width;

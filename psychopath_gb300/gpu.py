@@ -25,7 +25,7 @@ EXPORTED = [
     "psy_rays_traced", "psy_render_bucket", "psy_render_image_device", "psy_render_image", "psy_last_error",
     "psy_version", "psy_render_bucket_noalloc", "psy_server_create", "psy_server_add_scene", "psy_submit",
     "psy_poll", "psy_wait", "psy_cancel", "psy_server_stats", "psy_server_destroy", "psy_autotune",
-    "psy_xyz_to_srgb8", "psy_halton_samples",
+    "psy_xyz_to_srgb8", "psy_halton_samples", "psy_render_rows_device",
 ]
 
 
@@ -55,6 +55,7 @@ def lib(path=None):
     L.psy_render_image_device.argtypes = [vp, vp, vp, vp, vp]
     L.psy_render_image.argtypes = [vp, vp, vp, vp]
     L.psy_render_bucket_noalloc.argtypes = [vp, vp, u32, u32, vp, vp]
+    L.psy_render_rows_device.argtypes = [vp, u32, u32, vp, vp, vp]
     L.psy_last_error.restype = C.c_char_p
     L.psy_version.restype = C.c_char_p
     L.psy_debug_mesh_bvh_info.argtypes = [vp, u32, vp, C.POINTER(u32)]
@@ -72,6 +73,8 @@ def lib(path=None):
     L.psy_debug_push_tables.argtypes = [vp, vp, vp]
     L.psy_debug_scene_flags.argtypes = [vp, C.POINTER(u32)]
     L.psy_debug_host_nodes.argtypes = [vp, vp, C.c_int, vp, C.POINTER(u32), vp, C.POINTER(u32)]
+    L.psy_debug_render_paths.argtypes = [vp, vp, u32, u32, vp, vp]
+    L.psy_debug_samplers.argtypes = [C.c_int, vp, u32, vp, vp]
     L.psy_server_create.argtypes = [vp, C.POINTER(vp)]
     L.psy_server_add_scene.argtypes = [vp, vp, C.POINTER(u32)]
     L.psy_submit.argtypes = [vp, vp, C.POINTER(C.c_uint64)]
@@ -137,6 +140,23 @@ def halton_samples(dimension, indices):
     halton_samples_device(dimension, idx.data_ptr(), idx.numel(), out.data_ptr())
     torch.cuda.synchronize()
     return out.cpu().numpy()
+
+
+SAMPLER_OPS = {"hash_u32": 0, "hash_u32_to_f32": 1, "golden_ratio_sample": 2, "get_sample_4d": 3,
+               "wavelengths": 4}
+
+
+def device_samplers(op, args):
+    """psy_debug_samplers: the render path's samplers evaluated on the GPU.
+    args: (n, 5) uint32 rows (a, b, c, d, e); returns (n, 4) uint32 words
+    (f32 results as their bits)."""
+    import torch
+    args = np.ascontiguousarray(args, dtype=np.uint32).reshape(-1, 5)
+    n = args.shape[0]
+    d_args = torch.from_numpy(args.view(np.int32).copy()).cuda()
+    d_out = torch.zeros((n, 4), dtype=torch.int32, device="cuda")
+    _check(lib().psy_debug_samplers(SAMPLER_OPS[op], d_args.data_ptr(), n, d_out.data_ptr(), None))
+    return d_out.cpu().numpy().view(np.uint32)
 
 
 def push_tables():
@@ -309,6 +329,14 @@ class Renderer:
         _check(lib().psy_render_image_device(self.scene.h, cr, d_xyz_ptr, stream, C.byref(st) if stats else None))
         return st.as_dict() if stats else None
 
+    def render_rows_device(self, first_row, row_step, d_xyz_ptr, stream=None, stats=False):
+        """psy_render_rows_device: image rows first_row, first_row +
+        row_step, ... into a compact device buffer (rows x width x 3)."""
+        st = abi.PsyRenderStats() if stats else None
+        _check(lib().psy_render_rows_device(self.scene.h, first_row, row_step, d_xyz_ptr, stream,
+                                            C.byref(st) if stats else None))
+        return st.as_dict() if stats else None
+
     def render_bucket_noalloc(self, x, y, w, h, d_xyz_ptr, spp=None, seed=None, stream=None):
         """psy_render_bucket_noalloc: render into a caller-owned DEVICE buffer
         of w*h*3 floats; the library allocates no device memory for it."""
@@ -316,6 +344,20 @@ class Renderer:
         _check(lib().psy_render_bucket_noalloc(self.scene.h, C.byref(b),
                                                spp if spp is not None else self.scene.spp,
                                                seed if seed is not None else self.scene.data.seed, d_xyz_ptr, stream))
+
+    def render_paths(self, x, y, w, h, spp=None, seed=None):
+        """psy_debug_render_paths: every path's final colour (n, 4) and hero
+        wavelength (n,) of a bucket, sample s of pixel (x', y') at index
+        ((y' - y) * w + (x' - x)) * spp + s."""
+        spp = spp if spp is not None else self.scene.spp
+        n = w * h * spp
+        col = np.zeros((n, 4), dtype=np.float32)
+        wl = np.zeros(n, dtype=np.float32)
+        b = abi.PsyBucket(x, y, w, h)
+        _check(lib().psy_debug_render_paths(self.scene.h, C.byref(b), spp,
+                                            seed if seed is not None else self.scene.data.seed,
+                                            col.ctypes.data, wl.ctypes.data))
+        return col, wl
 
     def render_bucket(self, x, y, w, h, spp=None, seed=None):
         out = np.zeros((h, w, 3), dtype=np.float32)

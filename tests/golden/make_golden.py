@@ -1,6 +1,8 @@
 """Generates the golden fixtures of the parity tests (tests/golden/*.npz)
 from the CPU oracle on seeded inputs: per-ray hits on four scenes, a small
-Cornell render, Halton samples of every dimension and hash values.  The
+Cornell render, Halton samples of every dimension, hash values, golden-ratio
+samples, get_sample_4d values (Sobol-Burley and hash sets) and the camera's
+hero wavelengths.  The
 reference (a Rust crate) cannot be built here, so the oracle -- pinned by
 the reference's own unit-test answers (tests/test_oracle_kats.py) -- is the
 source; the fixtures freeze its outputs so that a later change to the oracle
@@ -47,6 +49,36 @@ HALTON_INDICES = np.array(list(range(48)) + [65535, 65536, 2 ** 31, 2 ** 32 - 1]
                           [int(x) for x in np.random.default_rng(105).integers(0, 2 ** 32, 12)], dtype=np.uint32)
 
 
+def golden_ratio_args():
+    """(sample index, scramble) pairs of golden_ratio_sample."""
+    rng = np.random.default_rng(106)
+    a = [(i, s) for i in range(16) for s in (0, 1, 0xDEADBEEF)]
+    a += [tuple(int(v) for v in r) for r in rng.integers(0, 2 ** 32, size=(64, 2))]
+    return np.array(a, dtype=np.uint32)
+
+
+def sample_4d_args():
+    """(sample index, dimension set, px, py, seed) rows of get_sample_4d:
+    the two Sobol-Burley sets the camera uses and hash-branch sets."""
+    rng = np.random.default_rng(107)
+    rows = []
+    for dset in (0, 1, 2, 5, 31):
+        for i in list(range(8)) + [int(v) for v in rng.integers(0, 65536, 8)]:
+            px, py, seed = (int(v) for v in rng.integers(0, [4096, 4096, 2 ** 32]))
+            rows.append((i, dset, px, py, seed))
+    rows.append((0, 0, 0, 0, 0))
+    rows.append((0xFFFFFFFF, 1, 4095, 4095, 0xFFFFFFFF))
+    return np.array(rows, dtype=np.uint32)
+
+
+def wavelength_args():
+    """(sample index, x, y, seed) rows of the camera's 4 hero wavelengths."""
+    rng = np.random.default_rng(108)
+    rows = [(i, 0, 0, 0) for i in range(8)]
+    rows += [tuple(int(v) for v in r) for r in rng.integers(0, [4096, 4096, 4096, 2 ** 32], size=(64, 4))]
+    return np.array(rows, dtype=np.uint32)
+
+
 def main():
     L = oracle_lib()
     for name, sd, rays in golden_ray_sets():
@@ -65,8 +97,24 @@ def main():
     seeds = np.array([0, 1, 0x736CAF6F, 0xFFFFFFFF], dtype=np.uint32)
     h32 = np.array([[L.psyo_hash_u32(int(a), int(s)) for a in n] for s in seeds], dtype=np.uint32)
     hf = np.array([[L.psyo_hash_u32_to_f32(int(a), int(s)) for a in n] for s in seeds], dtype=np.float32)
+    ga, gv = golden_ratio_args(), []
+    for i, scr in ga:
+        gv.append(L.psyo_golden_ratio_sample(int(i), int(scr)))
+    s4a = sample_4d_args()
+    s4v = np.zeros((len(s4a), 4), dtype=np.float32)
+    out = (C.c_float * 4)()
+    for r, (i, dset, px, py, seed) in enumerate(s4a):
+        L.psyo_get_sample_4d(int(i), int(dset), int(px), int(py), int(seed), out)
+        s4v[r] = list(out)
+    wla = wavelength_args()
+    wlv = np.zeros((len(wla), 4), dtype=np.float32)
+    for r, (si, x, y, seed) in enumerate(wla):
+        L.psyo_wavelengths(int(si), int(x), int(y), int(seed), out)
+        wlv[r] = list(out)
     np.savez_compressed(os.path.join(HERE, "samplers.npz"), halton_indices=HALTON_INDICES, halton=hal,
-                        hash_n=n, hash_seeds=seeds, hash_u32=h32, hash_u32_to_f32=hf)
+                        hash_n=n, hash_seeds=seeds, hash_u32=h32, hash_u32_to_f32=hf,
+                        golden_args=ga, golden=np.array(gv, dtype=np.float32), sample_4d_args=s4a,
+                        sample_4d=s4v, wavelength_args=wla, wavelengths=wlv)
     print("golden fixtures written to", HERE)
 
 

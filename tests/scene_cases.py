@@ -19,6 +19,50 @@ def motion_small(w=32, h=18, spp=4, bounces=2, n=40, level=3, lights=8):
     return scenes.motion_instances(w, h, spp, max_bounces=bounces, n_instances=n, level=level, n_lights=lights)
 
 
+def cornell_lens(w=32, h=32, spp=8, bounces=2):
+    """The Cornell box seen through a thin lens with a moving camera: 3
+    camera keys (the eye moves and turns), 2 field-of-view keys, 2 aperture
+    radii and 2 focus distances, all lerped by the sample time
+    (Camera::generate_ray, src/camera.rs:74-102)."""
+    s = scenes.cornell_box(w, h, spp, max_bounces=bounces)
+    keys = [scenes.look_at((0.25 * k - 0.25, 1.0 + 0.05 * k, 3.9 - 0.2 * k), (0.1 * k, 1.0, 0.0)) for k in range(3)]
+    s.set_camera(keys, [40.0, 46.0], aperture_radii=[0.06, 0.1], focus_distances=[3.2, 4.1])
+    return s
+
+
+def flat_grid_edges(n=8):
+    """A flat n x n grid of unit quads at y = 0 (2 triangles each) with
+    integer vertex coordinates, and rays straight down through its vertices,
+    edge midpoints and diagonal midpoints: the edge functions of the
+    watertight test are exactly zero there, so the f64 retest
+    (src/surface/triangle.rs:82-86) runs, and shared edges must still give
+    exactly one closest hit."""
+    xs = np.arange(n + 1, dtype=np.float64)
+    X, Z = np.meshgrid(xs, xs)
+    P = np.stack([X.ravel(), np.zeros(X.size), Z.ravel()], 1)
+    ii = np.arange(n)[:, None] * (n + 1) + np.arange(n)[None, :]
+    a, b, c, d = ii, ii + 1, ii + n + 2, ii + n + 1
+    f = np.concatenate([np.stack([a, b, c], -1).reshape(-1, 3), np.stack([a, c, d], -1).reshape(-1, 3)], 0)
+    s = scenes.SceneData(16, 16, 1, 0, 2)
+    sh = s.add_shader(abi.PSY_SHADER_LAMBERT, (0.7, 0.7, 0.7))
+    s.add_instance(s.add_mesh(P, f.astype(np.uint32)), sh)
+    s.set_camera([scenes.look_at((n / 2, 5.0, n / 2 + 5.0), (n / 2, 0.0, n / 2))], [50.0])
+    pts = []
+    for i in range(n + 1):
+        for j in range(n + 1):
+            pts.append((i, j))                  # vertices (incl. the border)
+            if i < n:
+                pts.append((i + 0.5, j))        # edges along x
+            if j < n:
+                pts.append((i, j + 0.5))        # edges along z
+            if i < n and j < n:
+                pts.append((i + 0.5, j + 0.5))  # the quads' diagonals
+    pts = np.array(pts, dtype=np.float32)
+    o = np.stack([pts[:, 0], np.full(len(pts), 3.0, np.float32), pts[:, 1]], 1)
+    dirs = np.tile(np.array([[0.0, -1.0, 0.0]], np.float32), (len(pts), 1))
+    return s, scenes.rays_array(o, dirs)
+
+
 def grid_small(nx=64, ny=32):
     return scenes.grid_mesh(nx, ny)
 

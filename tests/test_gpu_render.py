@@ -1,10 +1,15 @@
 """Renderer parity: GPU renders (camera -> wavefront light paths -> XYZ
 accumulation) against the oracle's bucket renderer on the same scene and
-seed.  Both evaluate the same sample sequences, so images agree closely;
-they are not bit-identical because sin/cos/acos/log come from different
-math libraries (CUDA vs the host libm) and rare paths diverge after an ulp
-difference.  Tolerances (stated per test): relative image RMSE and the
-fraction of pixels beyond 1e-3 relative difference."""
+seed.  Both evaluate the same sample sequences with the same f32/f64
+operations, so images agree to rounding: they are not bit-identical because
+sin/cos/acos/log come from different math libraries (CUDA vs the host libm,
+1-2 ulp apart) and the difference grows along a path's bounces.
+
+Bars (measured on a GB300 on these scenes, then a margin of about 7x):
+relative image RMSE below RENDER_REL = 1e-6 (measured at most 1.4e-7) and
+no more than RENDER_OFF = 0.1% of pixels beyond 1e-4 relative difference
+(measured 0).  The f32 shading variant is held to its own measured error
+with the same margin, inside its 1% precision budget."""
 import numpy as np
 import pytest
 
@@ -20,9 +25,17 @@ def rel_rmse(a, b):
     return float(np.sqrt(np.mean((a.astype(np.float64) - b) ** 2)) / max(1e-12, np.sqrt(np.mean(b.astype(np.float64) ** 2))))
 
 
-def frac_off(a, b, tol=1e-3):
+def frac_off(a, b, tol=1e-4):
     d = np.abs(a.astype(np.float64) - b) / np.maximum(np.abs(b), 1e-3)
     return float(np.mean(d.max(axis=-1) > tol))
+
+
+# Image bars of the renders against the oracle (relative image RMSE; share of
+# pixels beyond 1e-4 relative difference).
+RENDER_REL, RENDER_OFF = 1e-6, 0.001
+# Per-path bars of test_paths_match_oracle_samples (measured: at most 1 of
+# 2,048 paths beyond 1e-4 relative, the 4-bounce Cornell box).
+PATH_REL, PATH_ABS, PATH_DIVERGED = 1e-4, 1e-7, 0.002
 
 
 def _render_both(s):
@@ -38,8 +51,8 @@ def test_cornell_render(gpu_lib, bounces):
     s = sc.cornell(32, 32, 8, bounces)
     img, ref, st, ost, g = _render_both(s)
     assert np.isfinite(img).all()
-    assert rel_rmse(img, ref) < 0.02, rel_rmse(img, ref)
-    assert frac_off(img, ref) < 0.05, frac_off(img, ref)
+    assert rel_rmse(img, ref) < RENDER_REL, rel_rmse(img, ref)
+    assert frac_off(img, ref) <= RENDER_OFF, frac_off(img, ref)
     assert st["samples"] == 32 * 32 * 8
     # both count the same rays up to rare divergent paths
     assert abs(st["ray_count"] - ost["ray_count"]) <= 0.01 * ost["ray_count"]
@@ -48,15 +61,15 @@ def test_cornell_render(gpu_lib, bounces):
 def test_sphere_ggx_render(gpu_lib):
     s = sc.sphere_small(24, 16, 4, 6, level=3)
     img, ref, st, ost, g = _render_both(s)
-    assert rel_rmse(img, ref) < 0.03, rel_rmse(img, ref)
-    assert frac_off(img, ref) < 0.08, frac_off(img, ref)
+    assert rel_rmse(img, ref) < RENDER_REL, rel_rmse(img, ref)
+    assert frac_off(img, ref) <= RENDER_OFF, frac_off(img, ref)
 
 
 def test_motion_render(gpu_lib):
     s = sc.motion_small(24, 16, 4, 2)
     img, ref, st, ost, g = _render_both(s)
-    assert rel_rmse(img, ref) < 0.03, rel_rmse(img, ref)
-    assert frac_off(img, ref) < 0.08, frac_off(img, ref)
+    assert rel_rmse(img, ref) < RENDER_REL, rel_rmse(img, ref)
+    assert frac_off(img, ref) <= RENDER_OFF, frac_off(img, ref)
 
 
 def test_render_deterministic_and_bucket(gpu_lib):
@@ -79,6 +92,30 @@ def test_render_deterministic_and_bucket(gpu_lib):
     assert not d[:4].any()
 
 
+def test_interleaved_rows_equal_whole_image(gpu_lib):
+    """psy_render_rows_device (one rank's share of a multi-GPU frame): rows
+    first, first + step, ... equal the whole-image render's rows bit for bit,
+    with small waves too (several waves per share)."""
+    import torch
+    s = sc.sphere_small(24, 17, 4, 6, level=3)
+    g = gpu.Scene(s)
+    r = gpu.Renderer(g)
+    full, _ = r.render()
+    for wave in (0, 96):
+        if wave:
+            g.set_launch(wave_paths=wave * 4)
+        for step in (1, 2, 3, 8):
+            for first in range(min(step, 3)):
+                n = len(range(first, s.height, step))
+                d = torch.full((n * s.width * 3,), -1.0, dtype=torch.float32, device="cuda")
+                st = r.render_rows_device(first, step, d.data_ptr(), stats=True)
+                torch.cuda.synchronize()
+                got = d.cpu().numpy().reshape(n, s.width, 3)
+                assert np.array_equal(got, full[first::step]), (wave, step, first)
+                assert st["samples"] == n * s.width * s.spp
+    g.close()
+
+
 def test_bucket_rejects_bad_arguments(gpu_lib):
     """A bucket whose x + w or y + h passes 2^32 (checked in 64 bits), an
     empty bucket and spp == 0 are rejected before any launch, by both bucket
@@ -99,16 +136,28 @@ def test_bucket_rejects_bad_arguments(gpu_lib):
     g.close()
 
 
-def test_paths_match_oracle_samples(gpu_lib):
-    """Per-sample path colours of one bucket, GPU vs oracle (median relative
-    difference 1e-5 or better)."""
-    s = sc.cornell(32, 32, 4, 2)
+@pytest.mark.parametrize("case", ["cornell", "ggx", "motion"])
+def test_paths_match_oracle_samples(gpu_lib, case):
+    """Per-sample results of one bucket, GPU vs oracle, path by path: the
+    hero wavelength of every sample bit for bit, and each path's final
+    4-wavelength colour within PATH_REL relative (PATH_ABS absolute for
+    near-zero values) for all but PATH_DIVERGED of the paths (a path whose
+    direction flips after a last-ulp sin/cos difference)."""
+    s = {"cornell": sc.cornell(32, 32, 16, 4), "ggx": sc.sphere_small(32, 18, 16, 6, level=3),
+         "motion": sc.motion_small(32, 18, 16, 2)}[case]
+    x, y, w, h = 8, 4, 16, 8
     o = OracleScene(s)
-    col, wl, nr = o.render_paths(8, 8, 8, 8)
+    col, wl, _ = o.render_paths(x, y, w, h)
     g = gpu.Scene(s)
-    img, _ = gpu.Renderer(g).render_bucket(8, 8, 8, 8)
-    ref, _ = o.render(threads=4, crop=(8, 8, 15, 15))
-    assert rel_rmse(img, ref[8:16, 8:16]) < 0.02
+    gcol, gwl = gpu.Renderer(g).render_paths(x, y, w, h)
+    assert np.array_equal(gwl.view(np.uint32), wl.view(np.uint32))
+    fin = np.isfinite(col).all(axis=1) & np.isfinite(gcol).all(axis=1)
+    assert np.array_equal(np.isfinite(col).all(axis=1), np.isfinite(gcol).all(axis=1))
+    d = np.abs(gcol[fin].astype(np.float64) - col[fin])
+    bad = (d > PATH_REL * np.abs(col[fin]) + PATH_ABS).any(axis=1)
+    print("%s: %d paths, %d beyond %.0e, max abs diff %.3e" % (case, len(col), bad.sum(), PATH_REL, d.max()))
+    assert bad.mean() <= PATH_DIVERGED, (bad.sum(), len(bad))
+    g.close()
 
 
 @pytest.mark.parametrize("bits", [4, 10, 13, 16, 19, 25, 31])
@@ -146,15 +195,17 @@ def test_radix_queue_order_many_tiles(gpu_lib, graph):
 
 
 def test_f32_shading_precision_error(gpu_lib):
-    """The f32 shading variant (no FP64 outside the triangle retest) stays
-    within 1% relative RMSE of the f64 oracle render (the precision budget of
-    the optimized form)."""
+    """The f32 shading variant (no FP64 outside the triangle retest) against
+    the oracle and the FP64 oracle: inside the 1% precision budget of the
+    optimized form, and held to its measured error (1.1e-5 relative RMSE on
+    this GGX scene) with a 10x margin."""
     s = sc.sphere_small(48, 27, 16, 6, level=4)
     g = gpu.Scene(s, shading="f32")
     img, _ = gpu.Renderer(g).render()
-    o = OracleScene(s)
-    ref, _ = o.render(threads=8)
-    assert rel_rmse(img, ref) < 0.01, rel_rmse(img, ref)
+    ref, _ = OracleScene(s).render(threads=8)
+    ref64, _ = OracleScene(s, f64=True).render(threads=8)
+    assert rel_rmse(img, ref) < 1e-4, rel_rmse(img, ref)
+    assert rel_rmse(img, ref64) < 1e-4, rel_rmse(img, ref64)
 
 
 @pytest.mark.parametrize("minb", [6, 8])
@@ -200,7 +251,8 @@ def test_f32_shading_sphere_lights(gpu_lib):
     bad_o = ~np.isfinite(ref).all(axis=-1)
     assert not (bad_g & ~bad_o).any()
     ok = ~(bad_g | bad_o)
-    assert rel_rmse(img[ok], ref[ok]) < 0.01, rel_rmse(img[ok], ref[ok])
+    # measured 2.2e-8 (the sphere lights' cone sampling is f32 in both)
+    assert rel_rmse(img[ok], ref[ok]) < 1e-6, rel_rmse(img[ok], ref[ok])
 
 
 def test_speculative_traversal_render(gpu_lib):
@@ -216,3 +268,32 @@ def test_speculative_traversal_render(gpu_lib):
     rel = np.sqrt(np.mean((a.astype(np.float64) - b) ** 2)) / np.sqrt(np.mean(a.astype(np.float64) ** 2))
     assert rel < 1e-3
     g.close()
+
+
+def test_light_tree_64_lights(gpu_lib):
+    """64 sphere lights (the motion + instancing configuration's count): the
+    oracle's 8-ary light tree has inner levels below the root, so light
+    selection descends LightTree::select (src/accel/light_tree.rs:135-201)
+    more than one level; the GPU render matches the oracle's."""
+    s = sc.motion_small(48, 27, 8, 2, lights=64)
+    o = OracleScene(s)
+    nodes, leaves, depth = o.light_tree_info()
+    assert leaves == 64 and depth >= 3, (nodes, leaves, depth)
+    img, ref, st, ost, g = _render_both(s)
+    ok = np.isfinite(img).all(-1) & np.isfinite(ref).all(-1)
+    print("64 lights: rel RMSE %.3e, pixels off %.4f" % (rel_rmse(img[ok], ref[ok]), frac_off(img[ok], ref[ok])))
+    assert rel_rmse(img[ok], ref[ok]) < RENDER_REL, rel_rmse(img[ok], ref[ok])
+    assert frac_off(img[ok], ref[ok]) < RENDER_OFF, frac_off(img[ok], ref[ok])
+
+
+def test_thin_lens_camera_motion(gpu_lib):
+    """Thin lens (aperture radii and focus distances keyed over time) on a
+    moving camera with 3 transform keys and 2 field-of-view keys
+    (Camera::generate_ray, src/camera.rs:74-102; square_to_circle,
+    src/sampling/monte_carlo.rs:10-32): GPU render against the oracle."""
+    s = sc.cornell_lens(32, 32, 8, 2)
+    img, ref, st, ost, g = _render_both(s)
+    assert np.isfinite(img).all()
+    print("lens: rel RMSE %.3e, pixels off %.4f" % (rel_rmse(img, ref), frac_off(img, ref)))
+    assert rel_rmse(img, ref) < RENDER_REL, rel_rmse(img, ref)
+    assert frac_off(img, ref) < RENDER_OFF, frac_off(img, ref)

@@ -42,6 +42,53 @@ def test_cornell_random_rays(gpu_lib):
     assert st["t_bit_exact"] == 1.0, st
 
 
+def test_exact_edge_and_vertex_hits(gpu_lib):
+    """Rays straight down through the vertices, edges and diagonals of a flat
+    integer grid: every edge function the watertight test computes for the
+    hit triangle is exactly zero somewhere, so the f64 retest
+    (src/surface/triangle.rs:82-86) decides.  The GPU must pick the same
+    triangle as the oracle at every such shared edge, with the same t and
+    barycentrics, bit for bit, with FP32 and FP16 child bounds and the
+    static-scene traversal.
+
+    With FP16 bounds every oracle hit is found, at the same t.  The rays run
+    exactly in faces of the flat grid's boxes (origin on the face, direction
+    component 0): there the f32 slab distance is 0 * inf = NaN and the f32
+    box test culls the box, while the outward-rounded FP16 box holds the ray
+    strictly inside.  So FP16 visits more boxes: at a shared edge it can
+    find another of the triangles tied at exactly that t first (an exact
+    tie, allowed by the trace parity rule), and on the grid's border it finds
+    edge hits the f32 boxes cull -- hits gained, never one lost."""
+    s, rays = sc.flat_grid_edges(8)
+    o = OracleScene(s)
+    ho, _, _, _ = o.trace(rays, threads=1)
+    bmin = np.minimum(np.minimum(ho["b0"], ho["b1"]), ho["b2"])
+    hit = ho["kind"] == abi.PSY_HIT_SURFACE
+    assert (bmin[hit] == 0).all() and hit.sum() >= 200
+    for bounds, modes in (("fp32", [(0, 4), (3, 10)]), ("fp16", [(0, 4), (3, 10)])):
+        g = gpu.Scene(s, bounds=bounds)
+        tr = gpu.Tracer(g)
+        for mode, minb in modes:
+            g.set_trace(mode, minb)
+            hg = tr.trace(rays)
+            if bounds == "fp32":
+                for f in ("kind", "prim", "inst", "t", "b0", "b1", "b2"):
+                    assert np.array_equal(hg[f], ho[f]), (bounds, mode, f)
+            else:
+                assert np.array_equal(hg["kind"][hit], ho["kind"][hit]) and np.array_equal(hg["t"][hit], ho["t"][hit])
+                other = hit & (hg["prim"] != ho["prim"])
+                gmin = np.minimum(np.minimum(hg["b0"], hg["b1"]), hg["b2"])
+                assert (gmin[other] == 0).all()  # the other triangle is hit on its edge too: a tie
+                same = hit & ~other
+                for f in ("b0", "b1", "b2"):
+                    assert np.array_equal(hg[f][same], ho[f][same]), (bounds, mode, f)
+                gained = ~hit & (hg["kind"] == abi.PSY_HIT_SURFACE)
+                o = rays["orig"]
+                border = (o[:, 0] == 0) | (o[:, 0] == 8) | (o[:, 2] == 0) | (o[:, 2] == 8)
+                assert not (gained & ~border).any() and (hg["kind"][~hit & ~gained] == ho["kind"][~hit & ~gained]).all()
+        g.close()
+
+
 def test_cornell_occlusion_and_max_t(gpu_lib):
     rays = sc.random_rays(20000, [-0.95, 0.05, -0.95], [0.95, 1.95, 0.95], seed=2, occl_frac=0.5, max_t=3.0)
     hg, ho, _, _ = _run(sc.cornell(), rays)
