@@ -41,6 +41,9 @@ def build(force=False, verbose=False):
             return LIB_PATH
     common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
                      "-I", os.path.join(HERE, "..", "include")]
+    # extra nvcc flags (e.g. -DPSY_SSTACK=8 for another shared-memory stack
+    # depth); pass force=True when changing them
+    common += os.environ.get("PSY_NVCC_EXTRA", "").split()
     objs = []
 
     def compile_one(src):

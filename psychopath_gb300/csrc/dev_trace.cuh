@@ -141,43 +141,69 @@ DI uint32_t node_hits(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, flo
     return m & ((1u << count) - 1u);
 }
 
-// FP16 node variant: decode the outward-rounded half offsets to f32 bounds
-// (anchor + offset, rounded outward again by one ulp so the f32 box
-// contains the f16 box), then the same slab test.
-DI float h2f_lo(uint32_t bits16, float anchor) {
-    float v = __half2float(__ushort_as_half((unsigned short)bits16));
-    float r = anchor + v;
-    return decrement_ulp(r);
+// FP16 node variant: a child bound is decoded as the f32 sum anchor +
+// offset, rounded to nearest, in one instruction (PTX add.rn.f32.f16: the
+// f16 operand converts exactly).  The build chose every offset so that this
+// sum already lies outside the f32 bound (psy_layout.h, GNodeH), so the
+// decoded boxes contain the f32 boxes and the same slab arithmetic hits
+// every child the f32 test hits.
+DI float dec_h(unsigned short h, float anchor) {
+    float r;
+    asm("add.rn.f32.f16 %0, %1, %2;" : "=f"(r) : "h"(h), "f"(anchor));
+    return r;
 }
-DI float h2f_hi(uint32_t bits16, float anchor) {
-    float v = __half2float(__ushort_as_half((unsigned short)bits16));
-    float r = anchor + v;
-    return increment_ulp(r);
+// The four children's bounds of one slab (4 x f16 in a uint2).
+DI float4 dec_plane(uint2 q, float anchor) {
+    unsigned short h0, h1, h2, h3;
+    asm("mov.b32 {%0, %1}, %2;" : "=h"(h0), "=h"(h1) : "r"(q.x));
+    asm("mov.b32 {%0, %1}, %2;" : "=h"(h2), "=h"(h3) : "r"(q.y));
+    return make_float4(dec_h(h0, anchor), dec_h(h1, anchor), dec_h(h2, anchor), dec_h(h3, anchor));
+}
+// Child hit mask from decoded FP16 planes; the planes of slab s (xlo, xhi,
+// ylo, yhi, zlo, zhi) are at pl[s].  safe: octant-ordered planes as in
+// node_hits (the decoded boxes are ordered too: lo16 <= lo32 <= hi32 <= hi16).
+DI uint32_t fp16_hits(const uint2 *pl, float4 a, V3 o, V3 di, float tmax, uint32_t oct, bool safe) {
+    if (safe) {
+        uint32_t sx = oct & 1u, sy = (oct >> 1) & 1u, sz = (oct >> 2) & 1u;
+        float4 nx = dec_plane(__ldg(pl + sx), a.x), fx = dec_plane(__ldg(pl + (sx ^ 1u)), a.x);
+        float4 ny = dec_plane(__ldg(pl + 2 + sy), a.y), fy = dec_plane(__ldg(pl + 2 + (sy ^ 1u)), a.y);
+        float4 nz = dec_plane(__ldg(pl + 4 + sz), a.z), fz = dec_plane(__ldg(pl + 4 + (sz ^ 1u)), a.z);
+        float tnx[4], tfx[4], tny[4], tfy[4], tnz[4], tfz[4];
+        f32x2 ox = pk2(o.x, o.x), oy = pk2(o.y, o.y), oz = pk2(o.z, o.z);
+        f32x2 dx = pk2(di.x, di.x), dy = pk2(di.y, di.y), dz = pk2(di.z, di.z);
+        slab_axis4(nx, ox, dx, tnx); slab_axis4(fx, ox, dx, tfx);
+        slab_axis4(ny, oy, dy, tny); slab_axis4(fy, oy, dy, tfy);
+        slab_axis4(nz, oz, dz, tnz); slab_axis4(fz, oz, dz, tfz);
+        uint32_t m = 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            float far_t = fminf(fmin3f(tfx[c], tfy[c], tfz[c]) * PSY_BBOX_MAXT_ADJUST, tmax);
+            float near_t = fmax3f(tnx[c], tny[c], fmaxf(tnz[c], 0.0f));
+            m |= near_t < far_t ? (1u << c) : 0u;
+        }
+        return m;
+    }
+    float4 xl = dec_plane(__ldg(pl), a.x), xh = dec_plane(__ldg(pl + 1), a.x);
+    float4 yl = dec_plane(__ldg(pl + 2), a.y), yh = dec_plane(__ldg(pl + 3), a.y);
+    float4 zl = dec_plane(__ldg(pl + 4), a.z), zh = dec_plane(__ldg(pl + 5), a.z);
+    uint32_t m = 0;
+    m |= slab_hit(xl.x, xh.x, yl.x, yh.x, zl.x, zh.x, o, di, tmax) ? 1u : 0u;
+    m |= slab_hit(xl.y, xh.y, yl.y, yh.y, zl.y, zh.y, o, di, tmax) ? 2u : 0u;
+    m |= slab_hit(xl.z, xh.z, yl.z, yh.z, zl.z, zh.z, o, di, tmax) ? 4u : 0u;
+    m |= slab_hit(xl.w, xh.w, yl.w, yh.w, zl.w, zh.w, o, di, tmax) ? 8u : 0u;
+    return m;
 }
 DI uint32_t node_hits_h(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, float time, uint32_t oct, bool safe,
                         uint32_t &code, uint32_t &count, uint4 &child) {
     const GNodeH *n = S.nodes_h + ni;
     float4 a = __ldg(&n->anchor);
-    if ((__float_as_uint(a.w) >> 16) & 1u)  // motion node: keys only in f32
-        return node_hits(S, ni, o, di, tmax, time, oct, safe, code, count, child);
-    uint2 xl = __ldg(&n->xlo), xh = __ldg(&n->xhi), yl = __ldg(&n->ylo), yh = __ldg(&n->yhi), zl = __ldg(&n->zlo),
-          zh = __ldg(&n->zhi);
-    child = __ldg(&n->child);
     uint32_t meta = __float_as_uint(a.w);
+    if (meta & PSY_NODEH_F32)  // motion keys or offsets past the f16 range: the f32 node
+        return node_hits(S, ni, o, di, tmax, time, oct, safe, code, count, child);
+    child = __ldg(&n->child);
     code = meta & 0xFFu;
     count = (meta >> 8) & 0xFFu;
-    uint32_t m = 0;
-#pragma unroll
-    for (int l = 0; l < 4; l++) {
-        uint32_t sh = (l & 1) * 16;
-        uint32_t xlo = (l < 2 ? xl.x : xl.y) >> sh, xhi = (l < 2 ? xh.x : xh.y) >> sh;
-        uint32_t ylo = (l < 2 ? yl.x : yl.y) >> sh, yhi = (l < 2 ? yh.x : yh.y) >> sh;
-        uint32_t zlo = (l < 2 ? zl.x : zl.y) >> sh, zhi = (l < 2 ? zh.x : zh.y) >> sh;
-        bool h = slab_hit(h2f_lo(xlo & 0xFFFF, a.x), h2f_hi(xhi & 0xFFFF, a.x), h2f_lo(ylo & 0xFFFF, a.y),
-                          h2f_hi(yhi & 0xFFFF, a.y), h2f_lo(zlo & 0xFFFF, a.z), h2f_hi(zhi & 0xFFFF, a.z), o, di, tmax);
-        m |= h ? (1u << l) : 0u;
-    }
-    return m & ((1u << count) - 1u);
+    return fp16_hits(&n->xlo, a, o, di, tmax, oct, safe) & ((1u << count) - 1u);
 }
 
 // World-space vertices of triangle `tri` (global index) of mesh `M` at
@@ -500,6 +526,29 @@ done:
     return true;
 }
 
+// ------------------------------------------------------------------ short stack in shared memory
+// Threads per block of the traversal kernels.
+#define PSY_TRACE_BLOCK 128
+// Entries of each thread's traversal stack kept in shared memory.
+#ifndef PSY_SSTACK
+#define PSY_SSTACK 16
+#endif
+// Traversal stack of one thread: entries 0 .. K-1 in shared memory, in this
+// thread's column of a block-wide array (entry j at sh[j * PSY_TRACE_BLOCK],
+// so the 32 lanes of a warp use 32 different banks whatever their depths),
+// entries K .. STACK + 3 in local memory.  Rays rarely go deeper than K, so
+// pushes and pops stay out of the L1 / L2 path that local memory takes.
+template <int STACK, int K>
+struct TravStack {
+    uint32_t *sh;
+    uint32_t loc[STACK + 4 - K];
+    DI void set(int i, uint32_t v) {
+        if (K > 0 && i < K) sh[i * PSY_TRACE_BLOCK] = v;
+        else loc[i - K] = v;
+    }
+    DI uint32_t get(int i) const { return (K > 0 && i < K) ? sh[i * PSY_TRACE_BLOCK] : loc[i - K]; }
+};
+
 // ------------------------------------------------------------------ static-scene traversal
 // Scenes whose meshes are all static and untransformed, whose nodes carry no
 // motion keys and whose child boxes are ordered (GScene::static_fast) take a
@@ -548,6 +597,19 @@ DI uint32_t node_hits_static(const GScene &S, uint32_t ni, V3 o, V3 di, float tm
     return m;
 }
 
+// The static-scene test on an FP16 node (nodes flagged PSY_NODEH_F32 use
+// their f32 copy); the count mask is applied by the push table.
+DI uint32_t node_hits_static_h(const GScene &S, uint32_t ni, V3 o, V3 di, float tmax, uint32_t oct, bool safe,
+                               uint32_t &code, uint4 &child) {
+    const GNodeH *n = S.nodes_h + ni;
+    float4 a = __ldg(&n->anchor);
+    uint32_t meta = __float_as_uint(a.w);
+    if (meta & PSY_NODEH_F32) return node_hits_static(S, ni, o, di, tmax, oct, safe, code, child);
+    child = __ldg(&n->child);
+    code = meta & 0xFFu;
+    return fp16_hits(&n->xlo, a, o, di, tmax, oct, safe);
+}
+
 // Static-scene triangle leaf: tests its (up to three) triangles.
 DI void static_leaf(const GScene &S, uint32_t leaf, V3 o, const TriPre &pre, uint32_t slot, float &tmax,
                     uint32_t &hkind, uint32_t &hprim, uint32_t &hslot, bool occl, bool &occluded) {
@@ -574,9 +636,11 @@ DI void static_leaf(const GScene &S, uint32_t leaf, V3 o, const TriPre &pre, uin
 // tested meanwhile use the max_t of before the leaf, so a ray can visit more
 // nodes and triangles than the reference, and the closest hit differs only
 // where a triangle the reference culls lies at exactly the same t (a tie).
-template <int STACK, bool SPEC = false>
-DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut, V3 o, V3 d, float tmax,
-                         float time, bool occl, HitRec &hit) {
+// H16: the scene's nodes are read from the FP16 copy.  sstack: this thread's
+// column of the block's shared-memory stack (PSY_SSTACK entries).
+template <int STACK, bool SPEC = false, bool H16 = false>
+DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut, uint32_t *sstack, V3 o, V3 d,
+                         float tmax, float time, bool occl, HitRec &hit) {
     hit.kind = PSY_HIT_MISS_K;
     if (S.top_root == PSY_REF_NONE) return true;
     Xf ident = xf_identity();
@@ -585,7 +649,8 @@ DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_
     uint32_t oct = ray_code(di);
     const uint8_t *prow = prow_tab + 48 * oct;
     bool safe = slab_safe(wo, di, tmax);
-    uint32_t stack[STACK + 4];
+    TravStack<STACK, PSY_SSTACK> stack;
+    stack.sh = sstack;
     int sp = 0;
     uint32_t cur = S.top_root;
     bool in_inst = false;
@@ -598,13 +663,14 @@ DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_
         while (!psy_is_leaf(cur)) {
             uint32_t code;
             uint4 ch;
-            uint32_t m = node_hits_static(S, cur, wo, di, tmax, oct, safe, code, ch);
+            uint32_t m = H16 ? node_hits_static_h(S, cur, wo, di, tmax, oct, safe, code, ch)
+                             : node_hits_static(S, cur, wo, di, tmax, oct, safe, code, ch);
             uint32_t e = lut[16u * prow[code] + m];
             if (!(e & 0x800u)) {
                 if (!spec || pleaf == PSY_REF_NONE) goto pop;
                 // speculating: go on only with a node of this mesh on top
-                if (sp > 0 && !psy_is_leaf(stack[sp - 1])) {
-                    cur = stack[--sp];
+                if (sp > 0 && !psy_is_leaf(stack.get(sp - 1))) {
+                    cur = stack.get(--sp);
                 } else {
                     cur = PSY_REF_NONE;
                     break;
@@ -614,17 +680,17 @@ DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_
                 if (sp + np > STACK) return false;
                 // three unconditional stores (the stack has spare entries);
                 // only np of them are kept
-                stack[sp] = sel4(ch, (e >> 2) & 3u);
-                stack[sp + 1] = sel4(ch, (e >> 4) & 3u);
-                stack[sp + 2] = sel4(ch, (e >> 6) & 3u);
+                stack.set(sp, sel4(ch, (e >> 2) & 3u));
+                stack.set(sp + 1, sel4(ch, (e >> 4) & 3u));
+                stack.set(sp + 2, sel4(ch, (e >> 6) & 3u));
                 sp += np;
                 cur = sel4(ch, e & 3u);
             }
             if (spec) {
                 if (in_inst && pleaf == PSY_REF_NONE && psy_is_leaf(cur)) {
                     pleaf = cur;  // postpone the first triangle leaf
-                    if (sp > 0 && !psy_is_leaf(stack[sp - 1])) {
-                        cur = stack[--sp];
+                    if (sp > 0 && !psy_is_leaf(stack.get(sp - 1))) {
+                        cur = stack.get(--sp);
                     } else {
                         cur = PSY_REF_NONE;
                         break;
@@ -646,7 +712,7 @@ DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_
             GInstance in = S.instances[slot];
             if (in.kind == PSY_INST_MESH) {
                 if (sp >= STACK) return false;
-                stack[sp++] = PSY_REF_NONE;  // leave-instance marker
+                stack.set(sp++, PSY_REF_NONE);  // leave-instance marker
                 in_inst = true;
                 safe = slab_safe(wo, di, tmax);
                 cur = S.meshes[in.obj].root;
@@ -676,7 +742,7 @@ DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_
     pop:
         while (true) {
             if (sp == 0) goto done;
-            cur = stack[--sp];
+            cur = stack.get(--sp);
             if (cur != PSY_REF_NONE) break;
             in_inst = false;  // leaving the instance (world space is the instance's space)
             safe = slab_safe(wo, di, tmax);

@@ -40,12 +40,17 @@ struct __align__(16) GBounds4 {
     float4 xlo, xhi, ylo, yhi, zlo, zhi;
 };
 // Half-precision variant: child bounds as f16 offsets from an f32 anchor,
-// rounded outward.  64 bytes per node.
+// chosen so the decoded f32 bound fl32(anchor + offset) lies outside the f32
+// bound (the decoded box contains the f32 box).  80 bytes per node.
 struct __align__(16) GNodeH {
-    float4 anchor;       // xyz: node anchor (min corner of the union of children), w: unused
+    float4 anchor;  // xyz: node anchor (min corner of the union of children), w: meta bits
+                    // (traversal code | child count << 8 | PSY_NODEH_F32 flags)
     uint2 xlo, xhi, ylo, yhi, zlo, zhi;  // 4 x f16 per slab (48 bytes)
     uint4 child;
 };
+// Meta bits of GNodeH: the node has motion keys (bit 16) or an offset that
+// does not fit an f16 (bit 17); the traversal then reads the f32 node.
+#define PSY_NODEH_F32 0x30000u
 
 #define PSY_COLOR_XYZ_K 0u
 #define PSY_COLOR_BLACKBODY_K 1u
@@ -140,8 +145,8 @@ struct GScene {
     uint32_t width, height, spp, seed, max_bounces;
     uint32_t use_fp16;
     uint32_t ordered_slabs;      // every child box of every node has lo <= hi on each axis (host-checked)
-    uint32_t static_fast;        // FP32 nodes without motion keys, ordered boxes, every mesh static and every
-                                 // mesh instance untransformed: the static-scene traversal applies
+    uint32_t static_fast;        // nodes without motion keys (FP32 or FP16), ordered boxes, every mesh static
+                                 // and every mesh instance untransformed: the static-scene traversal applies
     float distant_energy_total;  // sum of distant light energies
     float lt_root_energy;
     float4 bounds_min, bounds_inv_extent;  // scene box, for the ray sort key's origin cell

@@ -561,6 +561,46 @@ uint16_t f16_up(float x) {
     __half h = __float2half_ru(x);
     return __half_as_ushort(h);
 }
+float f16_value(uint16_t h) { return __half2float(__ushort_as_half(h)); }
+
+// f16 offsets of the FP16 node copy.  The device decodes a child bound as
+// the f32 sum anchor + offset, rounded to nearest (one instruction, PTX
+// add.rn.f32.f16), so the offset is chosen for that sum to lie on the outer
+// side of the f32 bound itself: fl32(a + h) <= lo, fl32(a + h) >= hi.  The
+// decoded box then contains the f32 box and, the slab arithmetic being
+// monotone, every child the f32 test hits is hit.  Start from the f16
+// rounding of the exact difference, step outward one f16 ulp at a time until
+// the f32 sum is outside (the check is the device's own arithmetic).
+// Offsets are >= 0 (the anchor is the minimum lo); false when an offset does
+// not fit an f16 (the node keeps its f32 bounds).
+bool f16_offset_lo(float a, float lo, uint16_t &out) {
+    double d = (double)lo - (double)a;
+    if (!(d >= 0.0) || !std::isfinite(d)) return false;
+    float fd = (float)d;
+    if ((double)fd > d) fd = std::nextafter(fd, -INFINITY);
+    if (fd > 65504.0f) return false;
+    uint16_t h = f16_down(fd);
+    while (a + f16_value(h) > lo) {
+        if (h == 0) return false;  // a + 0 = a <= lo: not reached
+        h--;                       // next f16 toward 0 (non-negative patterns order like values)
+    }
+    out = h;
+    return true;
+}
+bool f16_offset_hi(float a, float hi, uint16_t &out) {
+    double d = (double)hi - (double)a;
+    if (!(d >= 0.0) || !std::isfinite(d)) return false;
+    float fd = (float)d;
+    if ((double)fd < d) fd = std::nextafter(fd, INFINITY);
+    if (fd > 65504.0f) return false;
+    uint16_t h = f16_up(fd);
+    while (!(a + f16_value(h) >= hi)) {
+        if (h >= 0x7BFFu) return false;  // past the largest finite f16
+        h++;
+    }
+    out = h;
+    return true;
+}
 
 }  // namespace
 
@@ -1013,11 +1053,8 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
                 for (uint32_t l = 0; l < cc; l++) m = std::min(m, lo[a][l]);
                 anchor[a] = std::isfinite(m) ? m : 0.0f;
             }
-            uint32_t meta = (n.meta.z & 0xFFFFu) | ((n.meta.y > 1 ? 1u : 0u) << 16);
-            float metaf;
-            std::memcpy(&metaf, &meta, 4);
-            h.anchor = f4(anchor[0], anchor[1], anchor[2], metaf);
             uint16_t q[6][4];
+            bool fits = true;
             for (int a = 0; a < 3; a++)
                 for (int l = 0; l < 4; l++) {
                     if ((uint32_t)l >= cc) {
@@ -1025,15 +1062,15 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
                         q[a * 2 + 1][l] = 0xFC00;  // -inf hi
                         continue;
                     }
-                    // offsets computed in f64 so rounding to f16 is the only rounding
-                    double dlo = (double)lo[a][l] - (double)anchor[a];
-                    double dhi = (double)hi[a][l] - (double)anchor[a];
-                    float flo = (float)dlo, fhi = (float)dhi;
-                    if ((double)flo > dlo) flo = std::nextafter(flo, -INFINITY);
-                    if ((double)fhi < dhi) fhi = std::nextafter(fhi, INFINITY);
-                    q[a * 2][l] = f16_down(flo);
-                    q[a * 2 + 1][l] = f16_up(fhi);
+                    fits = fits && f16_offset_lo(anchor[a], lo[a][l], q[a * 2][l]) &&
+                           f16_offset_hi(anchor[a], hi[a][l], q[a * 2 + 1][l]);
                 }
+            // bit 16: motion keys, bit 17: an offset does not fit an f16; either
+            // way the traversal reads this node's f32 copy
+            uint32_t meta = (n.meta.z & 0xFFFFu) | ((n.meta.y > 1 ? 1u : 0u) << 16) | ((fits ? 0u : 1u) << 17);
+            float metaf;
+            std::memcpy(&metaf, &meta, 4);
+            h.anchor = f4(anchor[0], anchor[1], anchor[2], metaf);
             auto pack = [&](int s) { return make_uint2((uint32_t)q[s][0] | ((uint32_t)q[s][1] << 16), (uint32_t)q[s][2] | ((uint32_t)q[s][3] << 16)); };
             h.xlo = pack(0); h.xhi = pack(1); h.ylo = pack(2); h.yhi = pack(3); h.zlo = pack(4); h.zhi = pack(5);
             h.child = n.child;

@@ -20,8 +20,8 @@ static bool g_push_tables = false;
 // ------------------------------------------------------------------ ray tracing
 // STATIC: the static-scene traversal (trace_ray_static; the scene must have
 // static_fast set, and the launch passes no counters); SPEC: its speculative
-// form.
-template <int STACK, bool COUNT, int MINB, bool STATIC = false, bool SPEC = false>
+// form; H16: the static-scene traversal over the FP16 node copy.
+template <int STACK, bool COUNT, int MINB, bool STATIC = false, bool SPEC = false, bool H16 = false>
 __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay *__restrict__ rays, uint32_t n,
                                                     const uint32_t *__restrict__ order, PsyHit *__restrict__ hits,
                                                     PsySurfaceHit *__restrict__ full, int *err,
@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay
     __shared__ __align__(16) uint8_t table[8 * 48];  // push rows per octant and traversal code
     __shared__ __align__(16) uint16_t push_lut[PSY_PUSH_ROWS * 16];
     __shared__ float4 xfm[STATIC ? 1 : 3 * 128];  // instance matrix slot per thread (general traversal)
+    __shared__ uint32_t sstack[STATIC && PSY_SSTACK > 0 ? PSY_SSTACK * PSY_TRACE_BLOCK : 1];  // stack tops (static)
     if (blockIdx.x * blockDim.x >= n) return;  // (whole block: before the table barrier)
     load_push_tables(table, push_lut);
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -42,7 +43,8 @@ __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay
         uint32_t flags = reinterpret_cast<const uint32_t *>(r)[9];
         HitRec h;
         bool oc = (flags & PSY_RAY_OCCLUSION) != 0;
-        bool ok = STATIC ? trace_ray_static<STACK, SPEC>(S, table, push_lut, o, d, tmax, time, oc, h)
+        bool ok = STATIC ? trace_ray_static<STACK, SPEC, H16>(S, table, push_lut, sstack + threadIdx.x, o, d, tmax,
+                                                              time, oc, h)
                          : trace_ray<STACK, COUNT>(S, table, push_lut, xfm + 3 * threadIdx.x, o, d, tmax, time, oc, h, &tc);
         if (!ok) {
             atomicExch(err, PSY_E_OVERFLOW);
@@ -105,16 +107,19 @@ cudaError_t launch_trace_rays(const GScene &S, const PsyRay *rays, uint32_t n, c
     if (n == 0) return cudaSuccess;
     dim3 b(128), g((n + 127) / 128);
     if (fast && S.static_fast && !counters) {
-#define TF(SZ, MB, SP) k_trace_rays<SZ, false, MB, true, SP><<<g, b, 0, st>>>(S, rays, n, order, hits, full, d_err, nullptr)
-#define TFS(SZ, SP)                          \
-    if (minb >= 12) TF(SZ, 12, SP);          \
-    else if (minb >= 10) TF(SZ, 10, SP);     \
-    else if (minb >= 8) TF(SZ, 8, SP);       \
-    else TF(SZ, 6, SP)
-        if (fast == 2) {
-            if (stack <= 64) { TFS(64, true); } else { TFS(192, true); }
+#define TF(SZ, MB, SP, H) \
+    k_trace_rays<SZ, false, MB, true, SP, H><<<g, b, 0, st>>>(S, rays, n, order, hits, full, d_err, nullptr)
+#define TFS(SZ, SP, H)                          \
+    if (minb >= 12) TF(SZ, 12, SP, H);          \
+    else if (minb >= 10) TF(SZ, 10, SP, H);     \
+    else if (minb >= 8) TF(SZ, 8, SP, H);       \
+    else TF(SZ, 6, SP, H)
+        if (S.use_fp16) {  // FP16 nodes (the speculative form reads f32 nodes only)
+            if (stack <= 64) { TFS(64, false, true); } else { TFS(192, false, true); }
+        } else if (fast == 2) {
+            if (stack <= 64) { TFS(64, true, false); } else { TFS(192, true, false); }
         } else {
-            if (stack <= 64) { TFS(64, false); } else { TFS(192, false); }
+            if (stack <= 64) { TFS(64, false, false); } else { TFS(192, false, false); }
         }
 #undef TFS
 #undef TF
@@ -384,13 +389,14 @@ cudaError_t launch_trace_packet_rays(const GScene &S, const PsyRay *rays, uint32
 // Queue-driven trace for the render wavefront: a grid-stride loop over the
 // live paths listed in queue[0 .. *count).  COUNT adds the work counters
 // (node visits, triangle tests, rays) into counters[0..2].
-template <int STACK, bool COUNT, int MINB, bool STATIC = false, bool SPEC = false>
+template <int STACK, bool COUNT, int MINB, bool STATIC = false, bool SPEC = false, bool H16 = false>
 __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
                                                      const uint32_t *__restrict__ count, int *err,
                                                      unsigned long long *counters) {
     __shared__ __align__(16) uint8_t table[8 * 48];  // push rows per octant and traversal code
     __shared__ __align__(16) uint16_t push_lut[PSY_PUSH_ROWS * 16];
     __shared__ float4 xfm[STATIC ? 1 : 3 * 128];  // instance matrix slot per thread (general traversal)
+    __shared__ uint32_t sstack[STATIC && PSY_SSTACK > 0 ? PSY_SSTACK * PSY_TRACE_BLOCK : 1];  // stack tops (static)
     uint32_t n = *count;
     // blocks past the queue's length (the grid covers the wave's capacity)
     // leave at once, before the table copy and its barrier
@@ -403,7 +409,8 @@ __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, H
         float4 ro = R.o[p], rd = R.d[p];
         HitRec h;
         bool oc = R.occl[p] != 0;
-        bool ok = STATIC ? trace_ray_static<STACK, SPEC>(S, table, push_lut, v3(ro), v3(rd), ro.w, rd.w, oc, h)
+        bool ok = STATIC ? trace_ray_static<STACK, SPEC, H16>(S, table, push_lut, sstack + threadIdx.x, v3(ro), v3(rd),
+                                                              ro.w, rd.w, oc, h)
                          : trace_ray<STACK, COUNT>(S, table, push_lut, xfm + 3 * threadIdx.x, v3(ro), v3(rd), ro.w, rd.w, oc,
                                                    h, &tc);
         if (!ok) {
@@ -435,16 +442,19 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
     if (grid <= 0) grid = (int)((max_count + 127) / 128);
     if (grid == 0) return cudaSuccess;
     if (fast && S.static_fast && !counters) {
-#define TF(SZ, MB, SP) k_trace_queue<SZ, false, MB, true, SP><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, nullptr)
-#define TFS(SZ, SP)                          \
-    if (minb >= 12) TF(SZ, 12, SP);          \
-    else if (minb >= 10) TF(SZ, 10, SP);     \
-    else if (minb >= 8) TF(SZ, 8, SP);       \
-    else TF(SZ, 6, SP)
-        if (fast == 2) {
-            if (stack <= 64) { TFS(64, true); } else { TFS(192, true); }
+#define TF(SZ, MB, SP, HH) \
+    k_trace_queue<SZ, false, MB, true, SP, HH><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, nullptr)
+#define TFS(SZ, SP, HH)                          \
+    if (minb >= 12) TF(SZ, 12, SP, HH);          \
+    else if (minb >= 10) TF(SZ, 10, SP, HH);     \
+    else if (minb >= 8) TF(SZ, 8, SP, HH);       \
+    else TF(SZ, 6, SP, HH)
+        if (S.use_fp16) {  // FP16 nodes (the speculative form reads f32 nodes only)
+            if (stack <= 64) { TFS(64, false, true); } else { TFS(192, false, true); }
+        } else if (fast == 2) {
+            if (stack <= 64) { TFS(64, true, false); } else { TFS(192, true, false); }
         } else {
-            if (stack <= 64) { TFS(64, false); } else { TFS(192, false); }
+            if (stack <= 64) { TFS(64, false, false); } else { TFS(192, false, false); }
         }
 #undef TFS
 #undef TF
