@@ -15,8 +15,9 @@ restatement of the reference's CPU renderer; the Rust binary cannot be built
 here) on all host threads, each step a bounded sample of the same frame.
 Multi-GPU (one process per GPU under torchrun): by default every rank
 renders its own full frame with its own seed (weak scaling, no collective on
-the data path); with --split rows the ranks render bands of one frame with
-the frame's seed and all-gather the bands once per frame (strong scaling;
+the data path); with --split rows the ranks render interleaved rows of one
+frame (rank r: rows r, r + N, ...) with the frame's seed and all-gather the
+rows once per frame (strong scaling;
 pixels identical to a 1-GPU render).  value = all ranks' samples / the
 slowest rank's time.
 """
@@ -30,6 +31,9 @@ import tempfile
 import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# bytes of one wave descriptor (WaveDesc: 16-byte header + 16 segments of 64
+# bytes), uploaded per wave by every render call
+WAVE_DESC_BYTES = 16 + 16 * 64
 sys.path.insert(0, HERE)
 
 L2_FLUSH_BYTES = 256 << 20
@@ -43,10 +47,13 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--bounds", default="fp32", choices=["fp32", "fp16"])
     ap.add_argument("--workload", default="mesh_stress",
-                    choices=["mesh_stress", "cornell", "motion", "traversal", "serving"])
+                    choices=["mesh_stress", "cornell", "motion", "traversal", "serving", "parity"])
     ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of Poisson arrivals")
     ap.add_argument("--rate", type=float, default=40.0, help="serving: mean arrivals per second")
     ap.add_argument("--wave-paths", type=int, default=1 << 23, help="serving: paths per wave of each scene lane")
+    ap.add_argument("--policy", default="shortest", choices=["fifo", "shortest"],
+                    help="serving: admission / wave packing order (shortest remaining samples first, with aging)")
+    ap.add_argument("--aging-ms", type=int, default=2000, help="serving: aging bound of the shortest-first policy")
     ap.add_argument("--plain-seconds", type=float, default=20.0,
                     help="serving: bound on the one-at-a-time plain-path baseline run")
     ap.add_argument("--rays", type=int, default=1 << 24, help="rays per set of the traversal microbenchmark")
@@ -54,9 +61,11 @@ def parse_args():
     ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (profiling on smaller cases)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="frame workloads: skip the bounded traversal and serving runs added to the line")
     ap.add_argument("--split", default="replicas", choices=["replicas", "rows"],
                     help="N>1 frame workloads: 'replicas' = every rank renders its own frame (weak scaling); "
-                         "'rows' = the ranks split one frame's rows and all-gather the bands (strong scaling)")
+                         "'rows' = the ranks render interleaved rows of one frame and all-gather them (strong scaling)")
     ap.add_argument("--form", default="both", choices=["both", "plain", "optimized"],
                     help="frame workloads: which forms to time (the headline is the optimized one)")
     ap.add_argument("--launch", default="",
@@ -210,16 +219,22 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- GPU
-def time_frames(rend, xyz, flush, stream, steps, warmup, barrier, crop=None, post=None):
+def time_frames(rend, xyz, flush, stream, steps, warmup, barrier, share=None, post=None):
     """W untimed frames, then K frames bracketed by CUDA events on the
-    render stream (L2 flushed before each).  crop: the region this rank
-    renders; post: called after each frame inside the timed region (the
-    band all-gather of a row split).  Returns (elapsed s, summed
-    traversal-kernel s, rays, samples)."""
+    render stream (L2 flushed before each).  share: (first row, row step) of
+    this rank's interleaved rows (None: the whole image); post: called after
+    each frame inside the timed region (the all-gather of a row split).
+    Returns (elapsed s, summed traversal-kernel s, rays, samples)."""
     import torch
     sp = stream.cuda_stream
+
+    def frame(stats):
+        if share is None:
+            return rend.render_device(xyz.data_ptr(), stream=sp, stats=stats)
+        return rend.render_rows_device(share[0], share[1], xyz.data_ptr(), stream=sp, stats=stats)
+
     for _ in range(warmup):
-        rend.render_device(xyz.data_ptr(), stream=sp, crop=crop)
+        frame(False)
         if post:
             post()
     torch.cuda.synchronize()
@@ -230,7 +245,7 @@ def time_frames(rend, xyz, flush, stream, steps, warmup, barrier, crop=None, pos
     ev0.record(stream)
     for _ in range(steps):
         flush.zero_()
-        st = rend.render_device(xyz.data_ptr(), stream=sp, stats=True, crop=crop)
+        st = frame(True)
         if post:
             post()
         trace_s += st["trace_time"]
@@ -264,11 +279,10 @@ def run_ours(args):
     if args.spp:
         sd.spp = args.spp
     W, H, spp = sd.width, sd.height, sd.spp
-    crop, gather = None, None
+    share, gather = None, None
     if rows_split:
         from psychopath_gb300 import multi
-        bands = multi.row_bands(H, world)
-        crop = multi.band_crop(bands[rank], W)
+        share = (rank, world)  # this rank's interleaved rows: rank, rank + world, ...
 
     def barrier():
         if world > 1:
@@ -283,8 +297,10 @@ def run_ours(args):
     xyz = torch.zeros(H * W * 3, dtype=torch.float32, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     if rows_split:
-        def gather():  # one all-gather of the bands per frame (NCCL)
-            multi.gather_bands(xyz.view(H, W, 3), bands, rank, world)
+        n_rows = len(multi.rows_of(H, world, rank))
+
+        def gather():  # one all-gather of the ranks' rows per frame (NCCL)
+            multi.gather_rows(xyz[: n_rows * W * 3].view(n_rows, W, 3), H, rank, world)
 
     # plain form
     t0 = time.perf_counter()
@@ -294,7 +310,7 @@ def run_ours(args):
     p_el, p_trace, p_rays, p_samples = 1.0, 0.0, 0, 0
     if args.form == "both":
         p_el, p_trace, p_rays, p_samples = time_frames(gpu.Renderer(plain), xyz, flush, stream, args.steps,
-                                                       args.warmup, barrier, crop, gather)
+                                                       args.warmup, barrier, share, gather)
         plain_img = xyz.cpu().numpy().copy()
     if args.form == "plain":
         scene = plain  # report the plain form as the line's value
@@ -325,7 +341,7 @@ def run_ours(args):
     n_nodes, n_tris, n_rays_c = scene.counters(False)
     clocks = ClockSampler(local)
     clocks.start()
-    elapsed, trace_s, rays, samples = time_frames(rend, xyz, flush, stream, args.steps, args.warmup, barrier, crop,
+    elapsed, trace_s, rays, samples = time_frames(rend, xyz, flush, stream, args.steps, args.warmup, barrier, share,
                                                   gather)
     clk = clocks.stop()
     opt_img = xyz.cpu().numpy()
@@ -357,9 +373,9 @@ def run_ours(args):
     torch.cuda.synchronize()
     e0 = time.perf_counter()
     for _ in range(args.steps):
-        if rows_split:  # band on the device, all-gather, full image to the host
-            rend.render_device(xyz.data_ptr(), stream=stream.cuda_stream, crop=crop)
-            img = multi.gather_bands(xyz.view(H, W, 3), bands, rank, world).cpu().numpy()
+        if rows_split:  # rows on the device, all-gather, full image to the host
+            rend.render_rows_device(rank, world, xyz.data_ptr(), stream=stream.cuda_stream)
+            img = multi.gather_rows(xyz[: n_rows * W * 3].view(n_rows, W, 3), H, rank, world).cpu().numpy()
         else:
             img, _ = rend.render()
     e_el = time.perf_counter() - e0
@@ -400,7 +416,8 @@ def run_ours(args):
     bits = tune["sort_bits"]
     per_binning = 0 if not bits else (3 if bits <= 16 else 1 + 3 * ((bits + 7) // 8))
     binning = per_binning * (iters - 1)
-    launches_per_frame = waves * (2 + 2 * iters + binning) + waves  # + the ray-count kernel of stats frames
+    # camera, (trace, shadow-result shade, hit shade) per iteration, accumulate
+    launches_per_frame = waves * (2 + 3 * iters + binning) + waves  # + the ray-count kernel of stats frames
     line = {
         "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
@@ -422,10 +439,11 @@ def run_ours(args):
         "speedup_vs_plain": value / plain_value if plain_value else None,
         "rel_rmse_vs_plain": rmse,
         "nonfinite_pixels": nonfinite,
-        "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": W * H * 3 * 4,
-                "note": "psy_render_image (host XYZ buffer, D2H inside the timed loop); the scene is resident (uploaded "
-                        "once at psy_scene_create), so a step has no input upload"},
+        "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": waves * WAVE_DESC_BYTES,
+                "d2h_bytes_per_step": W * H * 3 * 4 + 8,
+                "note": "psy_render_image with a host XYZ buffer and render statistics: per step the wave "
+                        "descriptors go up (%d B each) and the image and the ray count (8 B) come back, inside the "
+                        "timed loop; the scene is resident (uploaded once at psy_scene_create)" % WAVE_DESC_BYTES},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "traffic_per": "frame (all traversal launches of one frame)",
                      "peak_source": peak_src, "kernel": "k_trace_queue",
@@ -434,6 +452,28 @@ def run_ours(args):
         "clocks": clk,
         "gpu_launches": launches_per_frame * args.steps,
     }
+    if world == 1 and not args.no_sub:
+        scene.close()  # the frame's wave buffers (up to ~27 GB) are not needed past this point
+        del xyz, flush
+        if args.form == "both" and plain_value:
+            line["headline_form"] = served_fp16_frames(args, sd, plain_value, plain_img)
+        # bounded runs of the traversal microbenchmark and of serving, so one
+        # default run reports all three headline measurements
+        sub_args = argparse.Namespace(**vars(args))
+        sub_args.steps, sub_args.warmup = 3, 2
+        line["sub"] = {
+            "traversal_incoherent": run_traversal(sub_args, set_names=("incoherent",),
+                                                  config_names=("plain", "static10+binned"), with_gpu_bvh=False,
+                                                  emit=False)}
+        sub_args.duration, sub_args.rate, sub_args.plain_seconds = 20.0, 10.0, 10.0
+        sub_args.bounds = "fp16"
+        sv = run_serving(sub_args, emit=False)
+        line["sub"]["serving"] = {k: sv[k] for k in ("value", "unit", "latency_ms", "offered_samples_per_s", "overloaded",
+                                                     "plain_one_at_a_time", "tuned_one_at_a_time", "served_over_plain",
+                                                     "served_over_tuned_one_at_a_time", "requests_sharing_a_wave",
+                                                     "hbm_peak_bytes", "clocks")}
+        line["sub"]["serving"]["workload"] = sv["config"]["workload"]
+        line["sub"]["serving"]["form"] = "fp16 bounds, f32 shading, autotuned; policy %s" % sv["config"]["policy"]
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         cb = cpu_render_sample(sd, args.cpu_seconds, threads)
@@ -443,6 +483,47 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def served_fp16_frames(args, sd, plain_value, plain_img):
+    """The benchmark spec's headline form on this frame: a scene with FP16 child
+    bounds and f32 shading, autotuned, served as a lane of the render server
+    (waves of the tuned size, CUDA-graph replay); K frames submitted as K
+    requests with host result buffers and timed from the first submit to the
+    last result in host memory.  Against the plain form's samples/s on the
+    same frame, and the image's relative RMSE against the plain image."""
+    import numpy as np
+    from psychopath_gb300 import gpu
+    g = gpu.Scene(sd, bounds="fp16", shading="f32")
+    t0 = time.perf_counter()
+    tune = g.autotune()
+    tune_s = time.perf_counter() - t0
+    srv = gpu.Server(hbm_budget_bytes=120 * 10**9, wave_paths=tune["wave_paths"], use_graphs=True,
+                     policy=args.policy, aging_ms=args.aging_ms)
+    lane = srv.add_scene(g)
+    W, H, spp = sd.width, sd.height, sd.spp
+    for _ in range(max(1, args.warmup)):
+        srv.wait(srv.submit(lane, W, H, spp, sd.seed), timeout=3600.0)
+    t1 = time.perf_counter()
+    ids = [srv.submit(lane, W, H, spp, sd.seed) for _ in range(args.steps)]
+    sts = [srv.wait(i, timeout=3600.0) for i in ids]
+    el = time.perf_counter() - t1
+    if any(st["state"] != 2 for st in sts):
+        raise RuntimeError("served frame failed")
+    img = srv.result(ids[-1]).reshape(H, W, 3)
+    srv.close()
+    g.close()
+    value = W * H * spp * args.steps / el
+    rmse = None
+    if plain_img is not None:
+        p = plain_img.reshape(H, W, 3)
+        ok = np.isfinite(img) & np.isfinite(p)
+        a, b = img[ok].astype(np.float64), p[ok].astype(np.float64)
+        rmse = float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))
+    return {"form": "served + autotuned + FP16 child bounds (f32 shading); %d frames as requests with host results"
+                    % args.steps,
+            "value": value, "unit": "samples/s", "vs_plain": value / plain_value, "rel_rmse_vs_plain": rmse,
+            "autotune": tune, "autotune_s": round(tune_s, 2)}
 
 
 def frame_traffic(workload, tune, rays):
@@ -473,7 +554,7 @@ def traversal_traffic(launch, rays):
     return float(kv["dram_bytes_per_ray"]) * rays
 
 
-def run_traversal(args):
+def run_traversal(args, set_names=("coherent", "incoherent"), config_names=None, with_gpu_bvh=True, emit=True):
     """16M coherent (pinhole) and 16M incoherent (cosine-hemisphere from random
     surface points, seed 7) rays against the 2048x1024-quad displaced grid
     (4,194,304 tris): Mrays/s, algorithmic GB/s, closest-hit agreement with the
@@ -490,7 +571,11 @@ def run_traversal(args):
     build_mod.build()
     sd, P, F = scenes.grid_mesh(2048, 1024)
     n_side = int(round(math.sqrt(args.rays)))
-    sets = {"coherent": scenes.coherent_rays(n_side), "incoherent": scenes.incoherent_rays(P, F, n_side * n_side, seed=7)}
+    sets = {}
+    if "coherent" in set_names:
+        sets["coherent"] = scenes.coherent_rays(n_side)
+    if "incoherent" in set_names:
+        sets["incoherent"] = scenes.incoherent_rays(P, F, n_side * n_side, seed=7)
     t0 = time.perf_counter()
     g = gpu.Scene(sd, bounds=args.bounds)
     sah_build_s = time.perf_counter() - t0
@@ -506,6 +591,8 @@ def run_traversal(args):
                ("persistent8+binned", 1, 8, True), ("static8", 3, 8, False), ("static8+binned", 3, 8, True),
                ("static10+binned", 3, 10, True), ("static12+binned", 3, 12, True), ("static6+binned", 3, 6, True),
                ("spec8+binned", 4, 8, True), ("spec10+binned", 4, 10, True)]
+    if config_names is not None:
+        configs = [c for c in configs if c[0] in config_names]
     out = {}
     for name, rays in sets.items():
         n = len(rays)
@@ -586,6 +673,16 @@ def run_traversal(args):
     # the same rays against a GPU-built tree (PSY_BVH_GPU): creation time,
     # speed with the best launch configuration, hits against the SAH tree
     g.close()
+    if not with_gpu_bvh:
+        inc = out["incoherent"]
+        bc = inc["configs"][inc["best"]]
+        return {"rays": inc["rays"], "best": inc["best"], "mrays_per_s": bc["mrays_per_s"],
+                "ms_per_call": bc["ms_per_call"], "kernel_ms": bc["kernel_ms"],
+                "frac_kernel": bc["frac"], "frac_call": inc["alg_bytes_per_ray"] * inc["rays"] / (bc["ms_per_call"] * 1e-3)
+                / 1e9 / peak, "alg_bytes_per_ray": inc["alg_bytes_per_ray"], "peak_gbs": peak,
+                "hit_agreement": inc["hit_agreement"], "disagree_not_near_edge": inc["disagree_not_near_edge"],
+                "sample": inc["sample"], "plain_mrays_per_s": inc["configs"]["plain"]["mrays_per_s"],
+                "hits_identical_to_plain": bc["hits_identical_to_plain"], "bounds": args.bounds}
     t0 = time.perf_counter()
     gb = gpu.Scene(sd, bounds=args.bounds, bvh="gpu")
     gpu_build_s = time.perf_counter() - t0
@@ -632,7 +729,9 @@ def run_traversal(args):
                                  "kernel's own CUDA-event time (for a binned call: the kernel on the call's sorted "
                                  "order, without the sort)"},
             "sets": out, "gpu_bvh": gpu_bvh}
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 # ---------------------------------------------------------------- serving
@@ -651,7 +750,7 @@ def serving_requests(duration, rate, seed=2024):
                     (1, 4, 16, 64)[int(rng.integers(0, 4))], int(rng.integers(0, 1 << 30))))
 
 
-def run_serving(args):
+def run_serving(args, emit=True):
     """Three resident scenes (cornell, mesh_stress, motion); requests arrive
     as a Poisson process and are served by psy_submit with host result
     buffers (so every latency includes the result's device-to-host copy).
@@ -675,7 +774,8 @@ def run_serving(args):
     plain_gs = [gpu.Scene(sd, bounds=args.bounds) for sd in sds]  # f64 shading, default launch
     reqs = serving_requests(args.duration, args.rate)
     offered = sum(r * r * spp for (_, _, r, spp, _) in reqs) / args.duration
-    srv = gpu.Server(hbm_budget_bytes=120 * 10**9, wave_paths=args.wave_paths, use_graphs=True)
+    srv = gpu.Server(hbm_budget_bytes=120 * 10**9, wave_paths=args.wave_paths, use_graphs=True, policy=args.policy,
+                     aging_ms=args.aging_ms)
     lanes = [srv.add_scene(g) for g in gs]
     # warm-up: capture each lane's graphs, touch the image pool
     for _ in range(max(1, args.warmup)):
@@ -717,23 +817,33 @@ def run_serving(args):
     samples = sum(r * r * spp for (_, _, r, spp, _) in reqs)
     served = samples / (end - start)
     lat = np.array(lat) * 1e3
-    # the same requests one at a time on the plain path (device image, then
-    # the result copied to the host), over a bounded prefix of the list
+    # the same requests one at a time (device image, then the result copied
+    # to the host), over a bounded prefix of the list: first with the plain
+    # path (f64 shading, default launch), then with the served scenes
+    # themselves (f32 shading, the tuned launch) -- served / tuned isolates
+    # the batching gain, served / plain adds the precision and launch gains
     dev = torch.empty(1024 * 1024 * 3, dtype=torch.float32, device="cuda")
     host = torch.empty(1024 * 1024 * 3, dtype=torch.float32, pin_memory=False)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    p_samples, p_secs, p_n = 0, 0.0, 0
-    for (_, k, res, spp, seed) in reqs:
-        if p_secs >= args.plain_seconds:
-            break
-        t1 = time.perf_counter()
-        plain_gs[k].render_sized(res, res, spp, seed, dev.data_ptr(), stream=stream.cuda_stream)
-        host[: res * res * 3].copy_(dev[: res * res * 3])
-        p_secs += time.perf_counter() - t1
-        p_samples += res * res * spp
-        p_n += 1
+
+    def one_at_a_time(scenes_, n_max, seconds):
+        samples_, secs_, n_ = 0, 0.0, 0
+        for (_, k, res, spp, seed) in reqs[:n_max]:
+            if secs_ >= seconds:
+                break
+            t1 = time.perf_counter()
+            scenes_[k].render_sized(res, res, spp, seed, dev.data_ptr(), stream=stream.cuda_stream)
+            host[: res * res * 3].copy_(dev[: res * res * 3])
+            secs_ += time.perf_counter() - t1
+            samples_ += res * res * spp
+            n_ += 1
+        return samples_, secs_, n_
+
+    p_samples, p_secs, p_n = one_at_a_time(plain_gs, len(reqs), args.plain_seconds)
+    t_samples, t_secs, t_n = one_at_a_time(gs, p_n, 1e30)
     plain = p_samples / p_secs
+    tuned = t_samples / t_secs
     line = {
         "metric": "samples/s (served)", "value": served, "unit": "samples/s", "n_gpus": 1, "steps": len(reqs),
         "warmup": args.warmup, "ms_per_step": (end - start) / max(1, len(reqs)) * 1e3, "higher_is_better": True,
@@ -742,6 +852,7 @@ def run_serving(args):
                                "resolution {256,512,1024}^2, spp {1,4,16,64}, HBM budget 120 GB" %
                                (", ".join(names), args.rate, args.duration, len(reqs)),
                    "bounds": args.bounds, "wave_paths": args.wave_paths, "graphs": True,
+                   "policy": args.policy, "aging_ms": args.aging_ms,
                    "form": "served scenes: f32 shading, autotuned launch; plain: f64 shading, default launch",
                    "autotune": tunes, "scene_build_s": round(build_s, 2)},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
@@ -751,8 +862,13 @@ def run_serving(args):
         "overloaded": offered > served * 1.02,
         "requests_sharing_a_wave": int(shared),
         "plain_one_at_a_time": {"value": plain, "unit": "samples/s", "requests": p_n,
-                                "note": "psy render of each request alone (render_sized + D2H), same request list prefix"},
+                                "note": "each request alone on the plain path (f64 shading, default launch; "
+                                        "render_sized + D2H), a prefix of the same request list"},
+        "tuned_one_at_a_time": {"value": tuned, "unit": "samples/s", "requests": t_n,
+                                "note": "each request alone on the served scenes themselves (f32 shading, tuned "
+                                        "launch), the same prefix: served / this = the batching gain"},
         "served_over_plain": served / plain,
+        "served_over_tuned_one_at_a_time": served / tuned,
         "e2e": {"value": served, "unit": "samples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(sum(r * r * 12 for (_, _, r, _, _) in reqs) / max(1, len(reqs))),
                 "note": "psy_submit with host result buffers; latency ends when the image is in host memory"},
@@ -761,6 +877,95 @@ def run_serving(args):
         "gpu_launches": stats["kernel_launches"] - base["kernel_launches"],
         "clocks": clk,
     }
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
+
+
+# ---------------------------------------------------------------- image parity at full size
+def image_errors(img, ref):
+    """Relative image RMSE over pixels finite in both, the share of pixels
+    with a channel beyond 1e-3 and 1e-2 relative difference, and the
+    non-finite pixel counts."""
+    import numpy as np
+    fin_a, fin_b = np.isfinite(img).all(-1), np.isfinite(ref).all(-1)
+    ok = fin_a & fin_b
+    a, b = img[ok].astype(np.float64), ref[ok].astype(np.float64)
+    rel = float(np.sqrt(np.mean((a - b) ** 2)) / max(1e-30, np.sqrt(np.mean(b ** 2))))
+    d = (np.abs(a - b) / np.maximum(np.abs(b), 1e-3)).max(axis=-1)
+    return {"rel_rmse": rel, "px_beyond_1e-3": float(np.mean(d > 1e-3)), "px_beyond_1e-2": float(np.mean(d > 1e-2)),
+            "nonfinite": [int((~fin_a).sum()), int((~fin_b).sum())]}
+
+
+def run_parity(args):
+    """Image parity at the configurations' sizes: every GPU form of the
+    renderer against the CPU oracle (f32, the reference's arithmetic) and the
+    FP64 oracle (the same algorithm in f64), on the same scene, seed and
+    samples.  Cornell 512x512x16 at 2 and 4 bounces and motion + instancing
+    1280x720x32 in full; mesh stress 1920x1080x64 on its central 480x270 crop
+    (1/16 of the frame, the icosphere's silhouette and its shadow).  Forms:
+    plain (f64 shading, FP32 bounds), optimized (f32 shading, static-scene
+    traversal where the scene allows it), fp16 (the optimized form with FP16
+    child bounds), gpu_bvh (the optimized form on the GPU-built tree), served
+    (the fp16 form through the render server, the frame as one request).
+    The launch configuration does not change an image (tested bit for bit),
+    so the forms run the default launch apart from the traversal kernel."""
+    import numpy as np
+    import torch
+    from psychopath_gb300 import build, gpu, scenes
+    from oracle.runner import OracleScene
+    torch.cuda.set_device(0)
+    build.build()
+    threads = os.cpu_count() or 1
+    cases = [("cornell_b2", scenes.cornell_box(max_bounces=2), None),
+             ("cornell_b4", scenes.cornell_box(max_bounces=4), None),
+             ("motion", scenes.motion_instances(), None),
+             ("mesh_stress", scenes.mesh_stress(level=args.level), (720, 405, 1199, 674))]
+    out = {}
+    for name, sd, crop in cases:
+        t0 = time.perf_counter()
+        ref, _ = OracleScene(sd).render(threads=threads, crop=crop)
+        t1 = time.perf_counter()
+        ref64, _ = OracleScene(sd, f64=True).render(threads=threads, crop=crop)
+        t2 = time.perf_counter()
+        sl = (slice(None), slice(None)) if crop is None else (slice(crop[1], crop[3] + 1), slice(crop[0], crop[2] + 1))
+        ref, ref64 = ref[sl], ref64[sl]
+        res = {"size": [sd.width, sd.height, sd.spp], "max_bounces": sd.max_bounces,
+               "region": "full frame" if crop is None else "crop x %d-%d, y %d-%d" % (crop[0], crop[2], crop[1], crop[3]),
+               "oracle_s": round(t1 - t0, 2), "oracle64_s": round(t2 - t1, 2),
+               "oracle_vs_oracle64": image_errors(ref, ref64), "forms": {}}
+        forms = [("plain", dict(), None), ("optimized", dict(shading="f32"), 3),
+                 ("fp16", dict(shading="f32", bounds="fp16"), 3), ("gpu_bvh", dict(shading="f32", bvh="gpu"), 3)]
+        imgs = {}
+        for fname, kw, mode in forms:
+            g = gpu.Scene(sd, **kw)
+            if mode is not None:
+                g.set_trace(mode, 10)  # falls back to the general kernel where the scene needs it
+            img, _ = gpu.Renderer(g).render(crop=crop)
+            imgs[fname] = img[sl]
+            res["forms"][fname] = {"vs_oracle": image_errors(img[sl], ref), "vs_oracle64": image_errors(img[sl], ref64)}
+            if fname == "fp16":
+                # the served form: the same scene as a lane of the render server
+                srv = gpu.Server(hbm_budget_bytes=120 * 10**9, use_graphs=True)
+                lane = srv.add_scene(g)
+                rid = srv.submit(lane, sd.width, sd.height, sd.spp, sd.seed)
+                st = srv.wait(rid, timeout=3600.0)
+                simg = srv.result(rid).reshape(sd.height, sd.width, 3)
+                srv.close()
+                if st["state"] != 2:
+                    raise RuntimeError("served render ended in state %d" % st["state"])
+                res["forms"]["served"] = {"vs_oracle": image_errors(simg[sl], ref),
+                                          "vs_oracle64": image_errors(simg[sl], ref64),
+                                          "identical_to_fp16_form": bool(np.array_equal(simg[sl], img[sl],
+                                                                                        equal_nan=True))}
+            g.close()
+        res["fp16_vs_optimized"] = image_errors(imgs["fp16"], imgs["optimized"])
+        out[name] = res
+        print(json.dumps({"parity": name, **res}), flush=True)
+    worst = max(f["vs_oracle64"]["rel_rmse"] for r in out.values() for f in r["forms"].values())
+    line = {"metric": "relative image RMSE vs the FP64 oracle (worst form and configuration)", "value": worst,
+            "unit": "relative RMSE", "n_gpus": 1, "higher_is_better": False, "data": "synthetic (seeded scenes)",
+            "configs": out}
     print(json.dumps(line), flush=True)
 
 
@@ -770,6 +975,8 @@ def main():
         return run_traversal(args)
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload == "parity":
+        return run_parity(args)
     if args.impl == "reference":
         run_reference(args)
     else:
