@@ -424,8 +424,19 @@ typedef struct PsyServerOptions {
     uint32_t max_active;       /* requests admitted at once (0: 64) */
     uint32_t use_graphs;       /* 1: replay each wave's launch sequence from a CUDA graph */
     uint32_t waves_in_flight;  /* queued waves per lane, 1..4 (0: 2) */
-    uint32_t reserved[4];
+    uint32_t policy;           /* PSY_SCHED_*: order of admission and of rows in a wave (0: FIFO) */
+    uint32_t aging_ms;         /* PSY_SCHED_SHORTEST: a request waiting longer than this goes first
+                                  (0: 1000 ms) */
+    uint32_t reserved[2];
 } PsyServerOptions;
+
+/* Scheduling policies.  FIFO: requests are admitted and their rows packed
+ * into waves in arrival order.  SHORTEST: the request with the fewest
+ * samples left goes first (small requests finish in one wave instead of
+ * waiting behind large ones), except that requests older than aging_ms go
+ * first in arrival order, which bounds how long a large request waits. */
+#define PSY_SCHED_FIFO 0u
+#define PSY_SCHED_SHORTEST 1u
 
 typedef struct PsyRequest {
     uint32_t scene;            /* lane index from psy_server_add_scene */

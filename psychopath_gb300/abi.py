@@ -23,6 +23,7 @@ PSY_RAY_OCCLUSION = 1
 PSY_NOALLOC_MAX_SAMPLES = 262144
 PSY_HIT_MISS, PSY_HIT_OCCLUDE, PSY_HIT_SURFACE, PSY_HIT_LIGHT = 0, 1, 2, 3
 PSY_REQ_QUEUED, PSY_REQ_RUNNING, PSY_REQ_DONE, PSY_REQ_CANCELLED, PSY_REQ_FAILED = 0, 1, 2, 3, 4
+PSY_SCHED_FIFO, PSY_SCHED_SHORTEST = 0, 1
 
 _fp = C.POINTER(C.c_float)
 _up = C.POINTER(C.c_uint32)
@@ -110,7 +111,8 @@ class PsyRenderStats(C.Structure):
 
 class PsyServerOptions(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("wave_paths", C.c_uint32), ("max_active", C.c_uint32),
-                ("use_graphs", C.c_uint32), ("waves_in_flight", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+                ("use_graphs", C.c_uint32), ("waves_in_flight", C.c_uint32), ("policy", C.c_uint32),
+                ("aging_ms", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
 class PsyRequest(C.Structure):

@@ -337,15 +337,19 @@ DI float ggx_g(float vh, float vn, float rough) {
     if ((vh * vn) <= 0.0f) return 0.0f;
     return 2.0f / (1.0f + sqrtf(1.0f + rough * rough * (1.0f - vn * vn) / (vn * vn)));
 }
-DI V4 closure_evaluate(const Closure &cl, V3 inc, V3 out, V3 nor, V3 nor_g, float wl, float *pdf) {
-    if (cl.kind == PSY_CL_EMIT) { *pdf = 1.0f; return color_to_spectral(cl.color, wl); }
+// spec: the closure colour's spectrum at the path's wavelengths,
+// color_to_spectral(cl.color, wl), computed once per shading point by the
+// caller (the light sample's evaluation and the bounce sample use the same
+// value, as the reference computes it in each).
+DI V4 closure_evaluate(const Closure &cl, V4 spec, V3 inc, V3 out, V3 nor, V3 nor_g, float *pdf) {
+    if (cl.kind == PSY_CL_EMIT) { *pdf = 1.0f; return spec; }
     V3 nn, fng;
     if (cl.kind == PSY_CL_LAMBERT) {
         flip_normals(inc, nor, nor_g, &nn, &fng);
         if (dot(fng, out) >= 0.0f) {
             float fac = rmax(dot(nn, normalized(out)), 0.0f) * PSY_INV_PI;
             *pdf = fac;
-            return color_to_spectral(cl.color, wl) * fac;
+            return spec * fac;
         }
         *pdf = 0.0f;
         return splat4(0.0f);
@@ -360,7 +364,7 @@ DI V4 closure_evaluate(const Closure &cl, V3 inc, V3 out, V3 nor, V3 nor_g, floa
     float ha = rclamp(dot(hh, aa), -1.0f, 1.0f);
     float hb = rclamp(dot(hh, bb), -1.0f, 1.0f);
     float nh = rclamp(dot(nn, hh), -1.0f, 1.0f);
-    V4 ss = color_to_spectral(cl.color, wl);
+    V4 ss = spec;
     float rev = 1.0f - cl.fresnel;
     V4 col_f;
 #pragma unroll
@@ -372,8 +376,8 @@ DI V4 closure_evaluate(const Closure &cl, V3 inc, V3 out, V3 nor, V3 nor_g, floa
     *pdf = dist * PSY_INV_PI;
     return col_f * (dist * g1 * g2) * PSY_INV_PI;
 }
-DI V4 closure_sample(const Closure &cl, V3 inc, V3 nor, V3 nor_g, float u, float v, float wl, V3 *out, float *pdf) {
-    if (cl.kind == PSY_CL_EMIT) { *out = v3(0.0f, 0.0f, 0.0f); *pdf = 1.0f; return color_to_spectral(cl.color, wl); }
+DI V4 closure_sample(const Closure &cl, V4 spec, V3 inc, V3 nor, V3 nor_g, float u, float v, V3 *out, float *pdf) {
+    if (cl.kind == PSY_CL_EMIT) { *out = v3(0.0f, 0.0f, 0.0f); *pdf = 1.0f; return spec; }
     V3 nn, fng;
     flip_normals(inc, nor, nor_g, &nn, &fng);
     if (cl.kind == PSY_CL_LAMBERT) {
@@ -381,7 +385,7 @@ DI V4 closure_sample(const Closure &cl, V3 inc, V3 nor, V3 nor_g, float u, float
         float p = dir.z * PSY_INV_PI;
         V3 o = zup_to_vec(dir, nn);
         *out = o;
-        if (dot(fng, o) >= 0.0f) { *pdf = p; return color_to_spectral(cl.color, wl) * p; }
+        if (dot(fng, o) >= 0.0f) { *pdf = p; return spec * p; }
         *pdf = 0.0f;
         return splat4(0.0f);
     }
@@ -393,7 +397,7 @@ DI V4 closure_sample(const Closure &cl, V3 inc, V3 nor, V3 nor_g, float u, float
     half_dir = normalized(zup_to_vec(half_dir, nn));
     V3 o = inc - (half_dir * 2.0f * dot(inc, half_dir));
     *out = o;
-    if (dot(fng, o) >= 0.0f) return closure_evaluate(cl, inc, o, nor, nor_g, wl, pdf);
+    if (dot(fng, o) >= 0.0f) return closure_evaluate(cl, spec, inc, o, nor, nor_g, pdf);
     *pdf = 0.0f;
     return splat4(0.0f);
 }

@@ -195,12 +195,24 @@ __device__ __forceinline__ void push_live(bool alive, uint32_t p, uint32_t *next
     if (alive) next_queue[base + __popc(mask & ((1u << lane) - 1u))] = p;
 }
 
-// LightPath::next (src/renderer.rs:449-691).
+// LightPath::next (src/renderer.rs:449-691), in two kernels over the same
+// queue of paths whose rays were just traced: k_shade_hit takes the paths
+// whose ray was a camera or bounce ray (surface hit, emission, background,
+// light sample and bounce -- the heavy part), k_shade_shadow those whose ray
+// was a shadow ray (add the pending light, set up the next bounce -- a few
+// loads and stores).  Each skips the other kind, so the shadow results run
+// at the occupancy of their own small register footprint rather than the
+// hit kernel's; a queue ordered by ray key (the occlusion flag is its top
+// bit) keeps the kinds contiguous, so skipped warps leave at once.
+// k_shade_shadow runs first and marks the paths it shaded (PSY_SHADED_BIT
+// in their flags); k_shade_hit skips the marked paths and clears the mark,
+// so each path of the queue is shaded once per iteration.
+#define PSY_SHADED_BIT (1u << 11)
 template <class RT, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_shade(GScene S, const WaveDesc *__restrict__ gwave, PathState P, RayBuf R,
-                                               HitBuf H, const uint32_t *__restrict__ queue,
-                                               const uint32_t *__restrict__ count, uint32_t *next_queue,
-                                               uint32_t *next_count) {
+__global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDesc *__restrict__ gwave, PathState P,
+                                                   RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
+                                                   const uint32_t *__restrict__ count, uint32_t *next_queue,
+                                                   uint32_t *next_count) {
     __shared__ WaveDesc wdesc;
     uint32_t n = *count;
     // blocks past the queue's length (the grid covers the wave's capacity)
@@ -212,9 +224,14 @@ __global__ void __launch_bounds__(128, MINB) k_shade(GScene S, const WaveDesc *_
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nloop; q += stride) {
         bool alive = false;
         uint32_t p = 0;
+        uint32_t fl = 0;
         if (q < n) {
             p = queue[q];
-            uint32_t fl = P.flags[p];
+            fl = P.flags[p];
+        }
+        if (q < n && (fl & PSY_SHADED_BIT)) {
+            P.flags[p] = fl & ~PSY_SHADED_BIT;  // shaded by k_shade_shadow this iteration
+        } else if (q < n) {
             uint32_t ev = fl & 3u, bounce = (fl >> 2) & 0xFFu, has_nb = (fl >> 10) & 1u, nrays = fl >> 16;
             nrays += 1;
             float2 tw = P.tw[p];
@@ -222,133 +239,160 @@ __global__ void __launch_bounds__(128, MINB) k_shade(GScene S, const WaveDesc *_
             uint4 ki = H.ki[p];
             V4 color = v4(P.color[p]);
             V4 latt = v4(P.latt[p]);
-            if (ev == EV_CAMERA || ev == EV_BOUNCE) {
-                // the hit's barycentrics, the ray and the sampling state are
-                // read only here (a shadow-ray result needs none of them)
-                float4 tb = H.tb[p];
-                float4 ro = R.o[p], rd = R.d[p];
-                V3 o = v3(ro), d = v3(rd);
-                float4 nbo = P.nb_o[p];
-                float csp = nbo.w;  // closure_sample_pdf
-                uint32_t seed = P.seed[p];
-                const WaveSeg &w = wdesc.seg[seg_of_path(wdesc, p)];
-                uint32_t lp = p - w.path_begin;
-                uint32_t pix = lp / w.spp;
-                uint32_t si = lp - pix * w.spp;
-                uint32_t px = w.x0 + pix % w.w, py = w.y0 + (pix / w.w) * w.ystep;
-                if (ki.x == PSY_HIT_SURFACE_K || ki.x == PSY_HIT_LIGHT_K) {
-                    HitRec h;
-                    h.kind = ki.x; h.prim = ki.y; h.slot = ki.z;
-                    h.t = tb.x; h.b0 = tb.y; h.b1 = tb.z; h.b2 = tb.w;
-                    SurfData sd;
-                    resolve_hit<RT>(S, h, o, d, time, sd);
-                    const Closure &cl = sd.closure;
-                    if (cl.kind == PSY_CL_EMIT) {
-                        V4 c = color_to_spectral(cl.color, wl);
-                        if (ev == EV_CAMERA) {
-                            color = color + c;
-                        } else {
-                            float mis = power_heuristic(csp, sd.sample_pdf);
-                            color = color + c * latt / splat4(mis);
-                        }
-                        P.color[p] = f4(color);
+            // the hit's barycentrics, the ray and the sampling state
+            float4 tb = H.tb[p];
+            float4 ro = R.o[p], rd = R.d[p];
+            V3 o = v3(ro), d = v3(rd);
+            float4 nbo = P.nb_o[p];
+            float csp = nbo.w;  // closure_sample_pdf
+            uint32_t seed = P.seed[p];
+            const WaveSeg &w = wdesc.seg[seg_of_path(wdesc, p)];
+            uint32_t lp = p - w.path_begin;
+            uint32_t pix = lp / w.spp;
+            uint32_t si = lp - pix * w.spp;
+            uint32_t px = w.x0 + pix % w.w, py = w.y0 + (pix / w.w) * w.ystep;
+            if (ki.x == PSY_HIT_SURFACE_K || ki.x == PSY_HIT_LIGHT_K) {
+                HitRec h;
+                h.kind = ki.x; h.prim = ki.y; h.slot = ki.z;
+                h.t = tb.x; h.b0 = tb.y; h.b1 = tb.z; h.b2 = tb.w;
+                SurfData sd;
+                resolve_hit<RT>(S, h, o, d, time, sd);
+                const Closure &cl = sd.closure;
+                if (cl.kind == PSY_CL_EMIT) {
+                    V4 c = color_to_spectral(cl.color, wl);
+                    if (ev == EV_CAMERA) {
+                        color = color + c;
                     } else {
-                        latt = latt / splat4(csp);
-                        seed += 1;
-                        float smp[4];
-                        get_sample_4d(si, 0, px, py, seed, smp);
-                        LightSample li = scene_sample_lights<RT>(S, smp[0], smp[1], smp[2], wl, time, d, sd.pos,
-                                                                 sd.nor, sd.nor_g, cl);
-                        bool found = false;
-                        if (li.kind != 0 && !(li.pdf <= 0.0f) && !(li.sel_pdf <= 0.0f)) {
-                            V4 att;
-                            float cpdf;
-                            V3 so, sdir;
-                            float smax;
-                            if (li.kind == 1) {
-                                att = closure_evaluate(cl, d, li.dir, sd.nor, sd.nor_g, wl, &cpdf);
-                                so = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), li.dir);
-                                sdir = li.dir;
-                                smax = CUDART_INF_F;
-                            } else {
-                                V3 dir = li.sp - sd.pos;
-                                att = closure_evaluate(cl, d, dir, sd.nor, sd.nor_g, wl, &cpdf);
-                                so = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
-                                V3 oe = robust_ray_origin(li.sp, li.serr, normalized(li.sn), neg(dir));
-                                sdir = oe - so;
-                                smax = 1.0f;
-                            }
-                            if (!(max_elem4(att) <= 0.0f)) {
-                                float lmis = power_heuristic(li.pdf, cpdf);
-                                V4 pend = li.color * att * latt / splat4(lmis * li.sel_pdf);
-                                P.pending[p] = f4(pend);
-                                R.o[p] = make_float4(so.x, so.y, so.z, smax);
-                                R.d[p] = make_float4(sdir.x, sdir.y, sdir.z, time);
-                                R.occl[p] = 1;
-                                found = true;
-                            }
-                        }
-                        bool do_bounce = false;
-                        V4 nafac = v4(P.nafac[p]);
-                        if (bounce < S.max_bounces) {
-                            bounce += 1;
-                            seed += 1;
-                            float b4[4];
-                            get_sample_4d(si, 0, px, py, seed, b4);
-                            V3 dir;
-                            float pdf;
-                            V4 filt = closure_sample(cl, d, sd.nor, sd.nor_g, b4[0], b4[1], wl, &dir, &pdf);
-                            if ((pdf > 0.0f) && (max_elem4(filt) > 0.0f)) {
-                                nafac = filt;
-                                csp = pdf;
-                                V3 nb = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
-                                P.nafac[p] = f4(nafac);
-                                P.nb_o[p] = make_float4(nb.x, nb.y, nb.z, csp);
-                                P.nb_d[p] = make_float4(dir.x, dir.y, dir.z, 0.0f);
-                                has_nb = 1;
-                                do_bounce = true;
-                            }
-                        } else {
-                            has_nb = 0;
-                        }
-                        if (found) {
-                            ev = EV_SHADOW;
-                            alive = true;
-                        } else if (do_bounce) {
-                            float4 nb = P.nb_o[p], nd = P.nb_d[p];
-                            R.o[p] = make_float4(nb.x, nb.y, nb.z, CUDART_INF_F);
-                            R.d[p] = make_float4(nd.x, nd.y, nd.z, time);
-                            R.occl[p] = 0;
-                            ev = EV_BOUNCE;
-                            latt = latt * nafac;
-                            alive = true;
-                        }
-                        P.latt[p] = f4(latt);
-                        P.seed[p] = seed;
+                        float mis = power_heuristic(csp, sd.sample_pdf);
+                        color = color + c * latt / splat4(mis);
                     }
-                } else {
-                    V4 bg = color_to_spectral(S.background, wl);
-                    color = color + bg * latt / splat4(csp);
                     P.color[p] = f4(color);
+                } else {
+                    latt = latt / splat4(csp);
+                    seed += 1;
+                    // the surface colour's spectrum: shared by the light
+                    // sample's evaluation and the bounce sample
+                    V4 cspec = color_to_spectral(cl.color, wl);
+                    float smp[4];
+                    get_sample_4d(si, 0, px, py, seed, smp);
+                    LightSample li = scene_sample_lights<RT>(S, smp[0], smp[1], smp[2], wl, time, d, sd.pos,
+                                                             sd.nor, sd.nor_g, cl);
+                    bool found = false;
+                    if (li.kind != 0 && !(li.pdf <= 0.0f) && !(li.sel_pdf <= 0.0f)) {
+                        V4 att;
+                        float cpdf;
+                        V3 so, sdir;
+                        float smax;
+                        if (li.kind == 1) {
+                            att = closure_evaluate(cl, cspec, d, li.dir, sd.nor, sd.nor_g, &cpdf);
+                            so = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), li.dir);
+                            sdir = li.dir;
+                            smax = CUDART_INF_F;
+                        } else {
+                            V3 dir = li.sp - sd.pos;
+                            att = closure_evaluate(cl, cspec, d, dir, sd.nor, sd.nor_g, &cpdf);
+                            so = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
+                            V3 oe = robust_ray_origin(li.sp, li.serr, normalized(li.sn), neg(dir));
+                            sdir = oe - so;
+                            smax = 1.0f;
+                        }
+                        if (!(max_elem4(att) <= 0.0f)) {
+                            float lmis = power_heuristic(li.pdf, cpdf);
+                            V4 pend = li.color * att * latt / splat4(lmis * li.sel_pdf);
+                            P.pending[p] = f4(pend);
+                            R.o[p] = make_float4(so.x, so.y, so.z, smax);
+                            R.d[p] = make_float4(sdir.x, sdir.y, sdir.z, time);
+                            R.occl[p] = 1;
+                            found = true;
+                        }
+                    }
+                    bool do_bounce = false;
+                    V4 nafac = v4(P.nafac[p]);
+                    if (bounce < S.max_bounces) {
+                        bounce += 1;
+                        seed += 1;
+                        float b4[4];
+                        get_sample_4d(si, 0, px, py, seed, b4);
+                        V3 dir;
+                        float pdf;
+                        V4 filt = closure_sample(cl, cspec, d, sd.nor, sd.nor_g, b4[0], b4[1], &dir, &pdf);
+                        if ((pdf > 0.0f) && (max_elem4(filt) > 0.0f)) {
+                            nafac = filt;
+                            csp = pdf;
+                            V3 nb = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
+                            P.nafac[p] = f4(nafac);
+                            P.nb_o[p] = make_float4(nb.x, nb.y, nb.z, csp);
+                            P.nb_d[p] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                            has_nb = 1;
+                            do_bounce = true;
+                        }
+                    } else {
+                        has_nb = 0;
+                    }
+                    if (found) {
+                        ev = EV_SHADOW;
+                        alive = true;
+                    } else if (do_bounce) {
+                        float4 nb = P.nb_o[p], nd = P.nb_d[p];
+                        R.o[p] = make_float4(nb.x, nb.y, nb.z, CUDART_INF_F);
+                        R.d[p] = make_float4(nd.x, nd.y, nd.z, time);
+                        R.occl[p] = 0;
+                        ev = EV_BOUNCE;
+                        latt = latt * nafac;
+                        alive = true;
+                    }
+                    P.latt[p] = f4(latt);
+                    P.seed[p] = seed;
                 }
             } else {
-                // shadow ray result
-                if (ki.x == PSY_HIT_MISS_K) {
-                    color = color + v4(P.pending[p]);
-                    P.color[p] = f4(color);
-                }
-                if (has_nb) {
-                    float4 nb = P.nb_o[p], nd = P.nb_d[p];
-                    R.o[p] = make_float4(nb.x, nb.y, nb.z, CUDART_INF_F);
-                    R.d[p] = make_float4(nd.x, nd.y, nd.z, time);
-                    R.occl[p] = 0;
-                    latt = latt * v4(P.nafac[p]);
-                    P.latt[p] = f4(latt);
-                    ev = EV_BOUNCE;
-                    alive = true;
-                }
+                V4 bg = color_to_spectral(S.background, wl);
+                color = color + bg * latt / splat4(csp);
+                P.color[p] = f4(color);
             }
             P.flags[p] = ev | (bounce << 2) | (has_nb << 10) | (nrays << 16);
+        }
+        push_live(alive, p, next_queue, next_count);
+    }
+}
+
+// Shadow-ray results: the pending light contribution when the shadow ray
+// was not occluded, then the next bounce ray if the path has one.
+__global__ void __launch_bounds__(128, 12) k_shade_shadow(PathState P, RayBuf R, HitBuf H,
+                                                         const uint32_t *__restrict__ queue,
+                                                         const uint32_t *__restrict__ count, uint32_t *next_queue,
+                                                         uint32_t *next_count) {
+    uint32_t n = *count;
+    if (blockIdx.x * blockDim.x >= n) return;
+    uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t nloop = (n + stride - 1) / stride * stride;  // keep whole warps in the loop for the ballot
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nloop; q += stride) {
+        bool alive = false;
+        uint32_t p = 0;
+        uint32_t fl = 0;
+        if (q < n) {
+            p = queue[q];
+            fl = P.flags[p];
+        }
+        if (q < n && (fl & 3u) == EV_SHADOW) {
+            uint32_t ev = fl & 3u, bounce = (fl >> 2) & 0xFFu, has_nb = (fl >> 10) & 1u, nrays = fl >> 16;
+            nrays += 1;
+            uint32_t kind = H.ki[p].x;
+            if (kind == PSY_HIT_MISS_K) {
+                V4 color = v4(P.color[p]) + v4(P.pending[p]);
+                P.color[p] = f4(color);
+            }
+            if (has_nb) {
+                float time = P.tw[p].x;
+                float4 nb = P.nb_o[p], nd = P.nb_d[p];
+                R.o[p] = make_float4(nb.x, nb.y, nb.z, CUDART_INF_F);
+                R.d[p] = make_float4(nd.x, nd.y, nd.z, time);
+                R.occl[p] = 0;
+                V4 latt = v4(P.latt[p]) * v4(P.nafac[p]);
+                P.latt[p] = f4(latt);
+                ev = EV_BOUNCE;
+                alive = true;
+            }
+            P.flags[p] = ev | (bounce << 2) | (has_nb << 10) | (nrays << 16) | PSY_SHADED_BIT;
         }
         push_live(alive, p, next_queue, next_count);
     }
@@ -359,7 +403,8 @@ cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, R
                          int minb, int grid, int prec, cudaStream_t st) {
     if (grid <= 0) grid = (int)((max_count + 127) / 128);
     if (grid == 0) return cudaSuccess;
-#define SH(RT, MB) k_shade<RT, MB><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count)
+    k_shade_shadow<<<grid, 128, 0, st>>>(P, R, H, queue, count, next_queue, next_count);
+#define SH(RT, MB) k_shade_hit<RT, MB><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count)
     // budget 4 = the compiler's own choice (MINB 0 = unspecified)
     if (prec == 1) {
         if (minb >= 8) SH(float, 8);

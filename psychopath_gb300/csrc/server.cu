@@ -36,6 +36,7 @@ constexpr int kRing = 4;  // wave descriptor slots per lane (>= waves in flight)
 struct Req {
     uint64_t id = 0;
     PsyRequest r{};
+    uint64_t rows_left_samples() const { return (uint64_t)(r.height - next_row) * r.width * r.spp; }
     uint32_t state = PSY_REQ_QUEUED;
     int err = 0;
     float *d_img = nullptr;   // where accumulate writes (own buffer or the caller's)
@@ -47,6 +48,13 @@ struct Req {
     bool overflow = false;
     uint32_t waves = 0, shared_waves = 0;
     Clock::time_point t_submit, t_admit, t_done;
+};
+
+// A finished request whose result the finisher copies out (copy: to the
+// caller's host buffer) before it is published.
+struct Finish {
+    Req *q;
+    bool copy;
 };
 
 struct Flight {
@@ -65,7 +73,7 @@ struct Lane {
     int *h_err = nullptr;        // pinned error word of each slot's wave
     cudaEvent_t ev[kRing] = {};
     std::deque<Flight> inflight;
-    std::deque<Req *> active;    // admitted requests with rows left, FIFO
+    std::deque<Req *> active;    // admitted requests with rows left, in arrival order
     WaveGraph graphs[kRing];
     int next_slot = 0;
 };
@@ -91,6 +99,13 @@ struct PsyServer {
     uint64_t done = 0, samples_done = 0, waves = 0, launches = 0;
     cudaMemPool_t pool = nullptr;
     cudaStream_t copy_st = nullptr;
+    // finished requests whose results the finisher thread copies out, so
+    // the scheduler keeps issuing waves meanwhile (a copy to pageable host
+    // memory blocks the calling thread)
+    std::thread fin_thr;
+    std::condition_variable cv_fin;
+    std::deque<std::vector<Finish>> fin_q;
+    bool fin_stop = false;
 };
 
 namespace {
@@ -140,6 +155,23 @@ void set_fatal(PsyServer *s, int code, const std::string &msg) {
 
 std::string cuda_msg(cudaError_t e, const char *what) { return std::string(what) + ": " + cudaGetErrorString(e); }
 
+// Scheduling order (PsyServerOptions.policy): under PSY_SCHED_SHORTEST,
+// requests older than aging_ms first (in arrival order), then the others by
+// fewest samples left, ties in arrival order; under FIFO, arrival order.
+// `samples` gives a request's remaining work.
+template <class Work>
+void sched_order(const PsyServer *s, std::vector<Req *> &v, Work samples) {
+    if (s->opt.policy != PSY_SCHED_SHORTEST) return;  // v is in arrival order already
+    auto now = Clock::now();
+    double age_s = s->opt.aging_ms * 1e-3;
+    std::stable_sort(v.begin(), v.end(), [&](const Req *a, const Req *b) {
+        bool oa = secs(a->t_submit, now) > age_s, ob = secs(b->t_submit, now) > age_s;
+        if (oa != ob) return oa;
+        if (oa) return false;  // both aged: arrival order (stable)
+        return samples(a) < samples(b);
+    });
+}
+
 // Packs rows of the lane's active requests into the next wave and issues it.
 // Called with the lock held.  Returns false when there was nothing to issue.
 bool issue_wave(PsyServer *s, Lane &L, std::string &err) {
@@ -150,12 +182,14 @@ bool issue_wave(PsyServer *s, Lane &L, std::string &err) {
     Flight f;
     f.slot = slot;
     uint32_t paths = 0, pix = 0;
-    for (Req *q : L.active) {
+    std::vector<Req *> order(L.active.begin(), L.active.end());
+    sched_order(s, order, [](const Req *q) { return q->rows_left_samples(); });
+    for (Req *q : order) {
         if (d.nseg >= PSY_WAVE_MAX_SEGS || paths >= cap) break;
         if (q->cancel) continue;
         uint32_t row_paths = q->r.width * q->r.spp;
         uint32_t fit = (cap - paths) / row_paths;
-        if (fit == 0) break;  // keep FIFO order: the head waits for the next wave
+        if (fit == 0) break;  // keep the order: this request waits for the next wave
         uint32_t take = std::min(fit, q->r.height - q->next_row);
         WaveSeg &g = d.seg[d.nseg++];
         g.x0 = 0; g.y0 = q->next_row; g.w = q->r.width; g.h = take;
@@ -213,18 +247,14 @@ bool issue_wave(PsyServer *s, Lane &L, std::string &err) {
     L.inflight.push_back(std::move(f));
     L.next_slot = (slot + 1) % kRing;
     s->waves++;
-    // camera + (trace, shade) per iteration + accumulate, and the three
-    // queue-binning kernels between iterations when binning is on
+    // camera + (trace, shadow-result shade, hit shade) per iteration +
+    // accumulate, and the three queue-binning kernels between iterations
+    // when binning is on
     uint64_t iters = 2 * sc->g.max_bounces + 3;
-    s->launches += 2 + iters * 2 + (sc->sort_bits > 0 ? 3 * (iters - 1) : 0);
+    s->launches += 2 + iters * 3 + (sc->sort_bits > 0 ? 3 * (iters - 1) : 0);
     return true;
 }
 
-// Results of finished requests, copied out without the lock held.
-struct Finish {
-    Req *q;
-    bool copy;
-};
 
 void scheduler(PsyServer *s) {
     cudaSetDevice(s->device);
@@ -279,54 +309,29 @@ void scheduler(PsyServer *s) {
             set_fatal(s, PSY_E_CUDA, err);
             break;
         }
-        // 2. finish: copy results out (lock released), then publish
+        // 2. finish: the finisher thread copies the results out and
+        // publishes them; the scheduler goes on issuing waves
         if (!fin.empty()) {
-            lk.unlock();
-            cudaError_t ce = cudaSuccess;
-            for (Finish &f : fin) {
-                if (f.copy && ce == cudaSuccess)
-                    ce = cudaMemcpyAsync(f.q->r.xyz_out, f.q->d_img, (size_t)f.q->r.width * f.q->r.height * 12,
-                                         cudaMemcpyDeviceToHost, s->copy_st);
-            }
-            if (ce == cudaSuccess) ce = cudaStreamSynchronize(s->copy_st);
-            for (Finish &f : fin)
-                if (f.q->own_img && ce == cudaSuccess) ce = cudaFreeAsync(f.q->d_img, s->copy_st);
-            lk.lock();
-            if (ce != cudaSuccess) {
-                set_fatal(s, PSY_E_CUDA, cuda_msg(ce, "result copy"));
-                break;
-            }
-            auto now = Clock::now();
-            for (Finish &f : fin) {
-                Req &q = *f.q;
-                q.outstanding = 0;
-                q.d_img = q.own_img ? nullptr : q.d_img;
-                s->used -= q.img_bytes;
-                s->n_active--;
-                q.t_done = now;
-                if (q.cancel) {
-                    q.state = PSY_REQ_CANCELLED;
-                } else if (q.overflow) {
-                    q.state = PSY_REQ_FAILED;
-                    q.err = PSY_E_OVERFLOW;
-                } else {
-                    q.state = PSY_REQ_DONE;
-                    s->samples_done += (uint64_t)q.r.width * q.r.height * q.r.spp;
-                }
-                s->done++;
-            }
-            s->cv_done.notify_all();
+            s->fin_q.push_back(std::move(fin));
+            s->cv_fin.notify_one();
         }
-        // 3. admission: FIFO while the budget and the active limit allow
-        while (!s->pending.empty() && s->n_active < s->opt.max_active) {
-            Req *q = s->pending.front();
+        // 3. admission, in policy order, while the budget and the active
+        // limit allow (a request that does not fit the budget waits, and so
+        // do the ones after it)
+        std::vector<Req *> cand;
+        for (Req *q : s->pending) {
             if (q->cancel) {
-                s->pending.pop_front();
                 q->state = PSY_REQ_CANCELLED;
                 q->t_done = Clock::now();
                 s->cv_done.notify_all();
-                continue;
+            } else {
+                cand.push_back(q);
             }
+        }
+        if (cand.size() != s->pending.size()) s->pending.assign(cand.begin(), cand.end());
+        sched_order(s, cand, [](const Req *q) { return (uint64_t)q->r.width * q->r.height * q->r.spp; });
+        for (Req *q : cand) {
+            if (s->n_active >= s->opt.max_active) break;
             uint64_t bytes = q->r.d_xyz_out ? 0 : (uint64_t)q->r.width * q->r.height * 12;
             if (s->used + bytes > s->opt.hbm_budget_bytes) break;
             Lane &L = *s->lanes[q->r.scene];
@@ -348,7 +353,7 @@ void scheduler(PsyServer *s) {
             s->n_active++;
             q->state = PSY_REQ_RUNNING;
             q->t_admit = Clock::now();
-            s->pending.pop_front();
+            s->pending.erase(std::find(s->pending.begin(), s->pending.end(), q));
             L.active.push_back(q);
         }
         if (s->fatal) break;
@@ -366,11 +371,67 @@ void scheduler(PsyServer *s) {
             set_fatal(s, PSY_E_CUDA, err);
             break;
         }
-        // 5. wait: poll the GPU while waves are in flight, else sleep until work
+        // 5. wait: poll the GPU while waves are in flight; with requests
+        // waiting for memory or a slot, sleep until the finisher (or a
+        // submit or cancel) wakes the loop, at most 1 ms; else until work
         if (any_inflight)
             s->cv_work.wait_for(lk, std::chrono::microseconds(100));
+        else if (!s->pending.empty())
+            s->cv_work.wait_for(lk, std::chrono::milliseconds(1));
         else
             s->cv_work.wait(lk, [s] { return s->stop || !s->pending.empty(); });
+    }
+}
+
+// The finisher thread: copies finished requests' results to the callers'
+// host buffers and frees their images (lock released), then publishes the
+// requests' final states and wakes the scheduler (memory freed for
+// admission) and the waiters.
+void finisher(PsyServer *s) {
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    while (true) {
+        s->cv_fin.wait(lk, [s] { return s->fin_stop || !s->fin_q.empty(); });
+        if (s->fin_q.empty()) break;  // stopping with nothing left
+        std::vector<Finish> fin = std::move(s->fin_q.front());
+        s->fin_q.pop_front();
+        lk.unlock();
+        cudaError_t ce = cudaSuccess;
+        for (Finish &f : fin) {
+            if (f.copy && ce == cudaSuccess)
+                ce = cudaMemcpyAsync(f.q->r.xyz_out, f.q->d_img, (size_t)f.q->r.width * f.q->r.height * 12,
+                                     cudaMemcpyDeviceToHost, s->copy_st);
+        }
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(s->copy_st);
+        for (Finish &f : fin)
+            if (f.q->own_img && ce == cudaSuccess) ce = cudaFreeAsync(f.q->d_img, s->copy_st);
+        lk.lock();
+        if (ce != cudaSuccess) {
+            set_fatal(s, PSY_E_CUDA, cuda_msg(ce, "result copy"));
+            s->cv_work.notify_all();
+            continue;
+        }
+        auto now = Clock::now();
+        for (Finish &f : fin) {
+            Req &q = *f.q;
+            q.outstanding = 0;
+            q.d_img = q.own_img ? nullptr : q.d_img;
+            s->used -= q.img_bytes;
+            s->n_active--;
+            q.t_done = now;
+            if (q.cancel) {
+                q.state = PSY_REQ_CANCELLED;
+            } else if (q.overflow) {
+                q.state = PSY_REQ_FAILED;
+                q.err = PSY_E_OVERFLOW;
+            } else {
+                q.state = PSY_REQ_DONE;
+                s->samples_done += (uint64_t)q.r.width * q.r.height * q.r.spp;
+            }
+            s->done++;
+        }
+        s->cv_done.notify_all();
+        s->cv_work.notify_one();
     }
 }
 
@@ -389,6 +450,8 @@ int psy_server_create(const PsyServerOptions *opts, PsyServer **out) {
     if (s->opt.max_active == 0) s->opt.max_active = 64;
     if (s->opt.waves_in_flight == 0) s->opt.waves_in_flight = 2;
     if (s->opt.waves_in_flight > kRing) return fail(PSY_E_INVALID, "waves_in_flight above 4");
+    if (s->opt.policy > PSY_SCHED_SHORTEST) return fail(PSY_E_INVALID, "unknown scheduling policy");
+    if (s->opt.aging_ms == 0) s->opt.aging_ms = 1000;
     cudaError_t e = cudaGetDevice(&s->device);
     if (e != cudaSuccess) return psy_cuda_fail(e, "cudaGetDevice");
     cudaMemPoolProps pp{};
@@ -406,6 +469,7 @@ int psy_server_create(const PsyServerOptions *opts, PsyServer **out) {
     }
     PsyServer *raw = s.release();
     raw->thr = std::thread(scheduler, raw);
+    raw->fin_thr = std::thread(finisher, raw);
     *out = raw;
     return PSY_OK;
 }
@@ -536,6 +600,12 @@ int psy_server_destroy(PsyServer *s) {
         s->cv_work.notify_all();
     }
     if (s->thr.joinable()) s->thr.join();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->fin_stop = true;  // the finisher completes the batches handed to it, then leaves
+        s->cv_fin.notify_all();
+    }
+    if (s->fin_thr.joinable()) s->fin_thr.join();
     for (auto &lp : s->lanes) cudaStreamSynchronize(lp->st);
     cudaStreamSynchronize(s->copy_st);
     {

@@ -373,13 +373,16 @@ class Server:
     """Render server over resident scenes (psy_server_*, psy_submit,
     psy_poll, psy_wait, psy_cancel)."""
 
-    def __init__(self, hbm_budget_bytes=0, wave_paths=0, max_active=0, use_graphs=False, waves_in_flight=0):
+    def __init__(self, hbm_budget_bytes=0, wave_paths=0, max_active=0, use_graphs=False, waves_in_flight=0,
+                 policy="fifo", aging_ms=0):
         o = abi.PsyServerOptions()
         o.hbm_budget_bytes = hbm_budget_bytes
         o.wave_paths = wave_paths
         o.max_active = max_active
         o.use_graphs = 1 if use_graphs else 0
         o.waves_in_flight = waves_in_flight
+        o.policy = abi.PSY_SCHED_SHORTEST if policy == "shortest" else abi.PSY_SCHED_FIFO
+        o.aging_ms = aging_ms
         h = C.c_void_p()
         _check(lib().psy_server_create(C.byref(o), C.byref(h)))
         self.h = h

@@ -70,6 +70,34 @@ def test_request_same_alone_and_in_mix(scenes3):
     srv.close()
 
 
+def test_shortest_policy_same_images_small_first(scenes3):
+    """PSY_SCHED_SHORTEST: every image is bit-identical to the FIFO server's;
+    small requests submitted right after a large one finish before it (the
+    large one has rows left after the first wave), and with a short aging
+    bound the large request is not starved (it still finishes while small
+    requests keep arriving)."""
+    s = scenes3[1]
+    big = (s.width * 4, s.height * 4, 16, 5)
+    smalls = [(16, 8, 1, 10 + k) for k in range(6)]
+    srv, lanes = _server([s], wave_paths=4096)
+    ref = {}
+    for r in [big] + smalls:
+        rid = srv.submit(lanes[0], *r)
+        assert srv.wait(rid)["state"] == abi.PSY_REQ_DONE
+        ref[r] = srv.result(rid).copy()
+    srv.close()
+    for aging in (60000, 1):
+        srv, lanes = _server([s], wave_paths=4096, policy="shortest", aging_ms=aging, waves_in_flight=1)
+        ids = [srv.submit(lanes[0], *r) for r in [big] + smalls]
+        sts = [srv.wait(rid) for rid in ids]
+        assert all(st["state"] == abi.PSY_REQ_DONE for st in sts)
+        for rid, r in zip(ids, [big] + smalls):
+            assert np.array_equal(srv.result(rid), ref[r])
+        if aging == 60000:  # no aging within the test: strictly shortest first
+            assert max(st["latency_s"] for st in sts[1:]) < sts[0]["latency_s"]
+        srv.close()
+
+
 def test_served_request_equals_plain_render(scenes3):
     """A request at the scene's own resolution, spp and seed gives exactly
     the image of psy_render_image; graphs on or off."""
