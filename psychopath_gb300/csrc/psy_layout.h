@@ -39,14 +39,18 @@ struct __align__(16) GNode {
 struct __align__(16) GBounds4 {
     float4 xlo, xhi, ylo, yhi, zlo, zhi;
 };
-// Half-precision variant: child bounds as f16 offsets from an f32 anchor,
-// chosen so the decoded f32 bound fl32(anchor + offset) lies outside the f32
-// bound (the decoded box contains the f32 box).  80 bytes per node.
+// Half-precision variant: child bounds as f16 offsets, lower bounds from the
+// min corner of the children's union (anchor), upper bounds from its max
+// corner (decoded as fl32(anchor + ext)), each chosen so the decoded f32
+// bound fl32(corner + offset) lies outside the f32 bound (the decoded box
+// contains the f32 box).  96 bytes per node.
 struct __align__(16) GNodeH {
-    float4 anchor;  // xyz: node anchor (min corner of the union of children), w: meta bits
+    float4 anchor;  // xyz: min corner of the union of the children, w: meta bits
                     // (traversal code | child count << 8 | PSY_NODEH_F32 flags)
-    uint2 xlo, xhi, ylo, yhi, zlo, zhi;  // 4 x f16 per slab (48 bytes)
     uint4 child;
+    uint2 ext;      // f16 extents x | y << 16 and z: the max corner is fl32(anchor + ext)
+    uint2 xlo, xhi, ylo, yhi, zlo, zhi;  // 4 x f16 per slab (48 bytes)
+    uint2 pad;
 };
 // Meta bits of GNodeH: the node has motion keys (bit 16) or an offset that
 // does not fit an f16 (bit 17); the traversal then reads the f32 node.

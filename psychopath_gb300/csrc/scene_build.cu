@@ -552,54 +552,43 @@ void push_xf(std::vector<float4> &v, const M34 &m) {
     v.push_back(f4(m.m[8], m.m[9], m.m[10], m.m[11]));
 }
 
-// Round a float to f16 toward -inf / +inf.
-uint16_t f16_down(float x) {
-    __half h = __float2half_rd(x);
-    return __half_as_ushort(h);
-}
-uint16_t f16_up(float x) {
-    __half h = __float2half_ru(x);
-    return __half_as_ushort(h);
-}
 float f16_value(uint16_t h) { return __half2float(__ushort_as_half(h)); }
 
-// f16 offsets of the FP16 node copy.  The device decodes a child bound as
-// the f32 sum anchor + offset, rounded to nearest (one instruction, PTX
-// add.rn.f32.f16), so the offset is chosen for that sum to lie on the outer
-// side of the f32 bound itself: fl32(a + h) <= lo, fl32(a + h) >= hi.  The
-// decoded box then contains the f32 box and, the slab arithmetic being
-// monotone, every child the f32 test hits is hit.  Start from the f16
-// rounding of the exact difference, step outward one f16 ulp at a time until
-// the f32 sum is outside (the check is the device's own arithmetic).
-// Offsets are >= 0 (the anchor is the minimum lo); false when an offset does
-// not fit an f16 (the node keeps its f32 bounds).
-bool f16_offset_lo(float a, float lo, uint16_t &out) {
-    double d = (double)lo - (double)a;
-    if (!(d >= 0.0) || !std::isfinite(d)) return false;
-    float fd = (float)d;
-    if ((double)fd > d) fd = std::nextafter(fd, -INFINITY);
-    if (fd > 65504.0f) return false;
-    uint16_t h = f16_down(fd);
-    while (a + f16_value(h) > lo) {
-        if (h == 0) return false;  // a + 0 = a <= lo: not reached
-        h--;                       // next f16 toward 0 (non-negative patterns order like values)
-    }
-    out = h;
-    return true;
+// Adjacent f16 values toward +inf / -inf (finite patterns; both zeros step
+// to the smallest value on the side of the step).
+uint16_t f16_step_up(uint16_t h) {
+    if (h == 0x8000u || h == 0x0000u) return 0x0001u;
+    return (h & 0x8000u) ? (uint16_t)(h - 1) : (uint16_t)(h + 1);
 }
-bool f16_offset_hi(float a, float hi, uint16_t &out) {
-    double d = (double)hi - (double)a;
-    if (!(d >= 0.0) || !std::isfinite(d)) return false;
-    float fd = (float)d;
-    if ((double)fd < d) fd = std::nextafter(fd, INFINITY);
-    if (fd > 65504.0f) return false;
-    uint16_t h = f16_up(fd);
-    while (!(a + f16_value(h) >= hi)) {
-        if (h >= 0x7BFFu) return false;  // past the largest finite f16
-        h++;
+uint16_t f16_step_down(uint16_t h) {
+    if (h == 0x0000u || h == 0x8000u) return 0x8001u;
+    return (h & 0x8000u) ? (uint16_t)(h + 1) : (uint16_t)(h - 1);
+}
+
+// f16 offsets of the FP16 node copy.  The device decodes a bound as the f32
+// sum anchor + offset, rounded to nearest (one instruction, PTX
+// add.rn.f32.f16), so the offset is chosen for that sum to lie on the outer
+// side of the f32 bound itself: fl32(a + h) <= target for a lower bound
+// (dir < 0), >= target for an upper one (dir > 0).  The decoded box then
+// contains the f32 box and, the slab arithmetic being monotone, every child
+// the f32 test hits is hit.  Start from the f16 nearest to the exact
+// difference and step outward one f16 ulp at a time until the f32 sum --
+// the device's own arithmetic -- is outside.  False when the difference is
+// past the f16 range (the node keeps its f32 bounds).
+bool f16_offset(float a, float target, int dir, uint16_t &out) {
+    double d = (double)target - (double)a;
+    if (!std::isfinite(d) || std::fabs(d) > 65000.0) return false;
+    uint16_t h = __half_as_ushort(__float2half_rn((float)d));
+    for (int k = 0; k < 64; k++) {
+        float v = a + f16_value(h);
+        if (dir < 0 ? (v <= target) : (v >= target)) {
+            out = h;
+            return true;
+        }
+        h = dir < 0 ? f16_step_down(h) : f16_step_up(h);
+        if ((h & 0x7C00u) == 0x7C00u) return false;  // stepped past the largest finite f16
     }
-    out = h;
-    return true;
+    return false;
 }
 
 }  // namespace
@@ -1047,14 +1036,26 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
             uint32_t cc = n.meta.z >> 8;
             float lo[3][4] = {{n.xlo.x, n.xlo.y, n.xlo.z, n.xlo.w}, {n.ylo.x, n.ylo.y, n.ylo.z, n.ylo.w}, {n.zlo.x, n.zlo.y, n.zlo.z, n.zlo.w}};
             float hi[3][4] = {{n.xhi.x, n.xhi.y, n.xhi.z, n.xhi.w}, {n.yhi.x, n.yhi.y, n.yhi.z, n.yhi.w}, {n.zhi.x, n.zhi.y, n.zhi.z, n.zhi.w}};
-            float anchor[3];
+            // per axis: the min corner (anchor) and max corner of the
+            // children's union; lower bounds are offsets from the min
+            // corner, upper bounds from the max corner (decoded on the
+            // device as fl32(anchor + extent)), so every face near the
+            // node's own faces -- most of them -- is encoded by a small
+            // offset, i.e. nearly exactly
+            float anchor[3], top[3];
+            uint16_t ext[3] = {0, 0, 0};
+            bool fits = true;
             for (int a = 0; a < 3; a++) {
-                float m = INFINITY;
-                for (uint32_t l = 0; l < cc; l++) m = std::min(m, lo[a][l]);
+                float m = INFINITY, M = -INFINITY;
+                for (uint32_t l = 0; l < cc; l++) {
+                    m = std::min(m, lo[a][l]);
+                    M = std::max(M, hi[a][l]);
+                }
                 anchor[a] = std::isfinite(m) ? m : 0.0f;
+                if (std::isfinite(M) && std::isfinite(m)) fits = fits && f16_offset(anchor[a], M, +1, ext[a]);
+                top[a] = anchor[a] + f16_value(ext[a]);
             }
             uint16_t q[6][4];
-            bool fits = true;
             for (int a = 0; a < 3; a++)
                 for (int l = 0; l < 4; l++) {
                     if ((uint32_t)l >= cc) {
@@ -1062,8 +1063,8 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
                         q[a * 2 + 1][l] = 0xFC00;  // -inf hi
                         continue;
                     }
-                    fits = fits && f16_offset_lo(anchor[a], lo[a][l], q[a * 2][l]) &&
-                           f16_offset_hi(anchor[a], hi[a][l], q[a * 2 + 1][l]);
+                    fits = fits && f16_offset(anchor[a], lo[a][l], -1, q[a * 2][l]) &&
+                           f16_offset(top[a], hi[a][l], +1, q[a * 2 + 1][l]);
                 }
             // bit 16: motion keys, bit 17: an offset does not fit an f16; either
             // way the traversal reads this node's f32 copy
@@ -1071,8 +1072,10 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
             float metaf;
             std::memcpy(&metaf, &meta, 4);
             h.anchor = f4(anchor[0], anchor[1], anchor[2], metaf);
+            h.ext = make_uint2((uint32_t)ext[0] | ((uint32_t)ext[1] << 16), (uint32_t)ext[2]);
             auto pack = [&](int s) { return make_uint2((uint32_t)q[s][0] | ((uint32_t)q[s][1] << 16), (uint32_t)q[s][2] | ((uint32_t)q[s][3] << 16)); };
             h.xlo = pack(0); h.xhi = pack(1); h.ylo = pack(2); h.yhi = pack(3); h.zlo = pack(4); h.zhi = pack(5);
+            h.pad = make_uint2(0u, 0u);
             h.child = n.child;
         }
     }

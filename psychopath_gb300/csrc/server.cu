@@ -248,10 +248,13 @@ bool issue_wave(PsyServer *s, Lane &L, std::string &err) {
     L.next_slot = (slot + 1) % kRing;
     s->waves++;
     // camera + (trace, shadow-result shade, hit shade) per iteration +
-    // accumulate, and the three queue-binning kernels between iterations
-    // when binning is on
+    // accumulate, and the queue-ordering kernels between iterations when
+    // the lane orders its queues (keys + scan + scatter, or keys + three
+    // kernels per 8-bit radix pass)
     uint64_t iters = 2 * sc->g.max_bounces + 3;
-    s->launches += 2 + iters * 3 + (sc->sort_bits > 0 ? 3 * (iters - 1) : 0);
+    int bits = (sc->sort_bits > 0 && L.B.stage) ? sc->sort_bits : 0;
+    uint64_t per_binning = bits == 0 ? 0 : (bits <= 16 ? 3 : 1 + 3 * (uint64_t)((bits + 7) / 8));
+    s->launches += 2 + iters * 3 + per_binning * (iters - 1);
     return true;
 }
 
@@ -483,7 +486,9 @@ int psy_server_add_scene(PsyServer *s, PsyScene *scene, uint32_t *lane) {
         std::lock_guard<std::mutex> lk(s->mu);
         if (s->fatal) return fail(s->fatal, s->fatal_msg);
     }
-    int r = alloc_wave_bufs(L->B, s->opt.wave_paths, kRing, false, L->allocs, L->bytes);
+    // queue-ordering scratch when the scene orders its wavefront queues
+    // (its tuned launch), so served waves run the scene's own configuration
+    int r = alloc_wave_bufs(L->B, s->opt.wave_paths, kRing, scene->sort_bits > 0, L->allocs, L->bytes);
     auto cleanup = [&]() {
         for (void *p : L->allocs) cudaFree(p);
         if (L->h_ring) cudaFreeHost(L->h_ring);
