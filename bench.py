@@ -463,7 +463,8 @@ def run_ours(args):
         sub_args.steps, sub_args.warmup = 3, 2
         line["sub"] = {
             "traversal_incoherent": run_traversal(sub_args, set_names=("incoherent",),
-                                                  config_names=("plain", "static10+binned"), with_gpu_bvh=False,
+                                                  config_names=("plain", "static10+binned", "refill10+binned"),
+                                                  with_gpu_bvh=False,
                                                   emit=False)}
         sub_args.duration, sub_args.rate, sub_args.plain_seconds = 20.0, 10.0, 10.0
         sub_args.bounds = "fp16"
@@ -591,7 +592,8 @@ def run_traversal(args, set_names=("coherent", "incoherent"), config_names=None,
     configs = [("plain", 0, 4, False), ("minb8", 0, 8, False), ("minb8+binned", 0, 8, True),
                ("persistent8+binned", 1, 8, True), ("static8", 3, 8, False), ("static8+binned", 3, 8, True),
                ("static10+binned", 3, 10, True), ("static12+binned", 3, 12, True), ("static6+binned", 3, 6, True),
-               ("spec8+binned", 4, 8, True), ("spec10+binned", 4, 10, True)]
+               ("spec8+binned", 4, 8, True), ("spec10+binned", 4, 10, True), ("refill10", 5, 10, False),
+               ("refill10+binned", 5, 10, True)]
     if config_names is not None:
         configs = [c for c in configs if c[0] in config_names]
     out = {}

@@ -358,7 +358,8 @@ int psy_render_bucket_noalloc(PsyScene *scene, const PsyBucket *bucket, uint32_t
  * trace kernel (one thread per ray with a register budget of 4, 5, 6 or 8
  * resident blocks per SM, persistent with lane refill at 4, 6 or 8, or --
  * on scenes without motion or mesh instance transforms -- the static-scene
- * traversal at 8, 10 or 12), the shading kernel's register budget (4, 6 or
+ * traversal at 8, 10 or 12 and its lane-refill form), the shading kernel's
+ * register budget (4, 6 or
  * 8 blocks per SM), the traversal stack depth (64 or 192 entries, if the
  * scene fits), the queue tile (grid of the wavefront kernels: sized by the
  * queue, or a grid-stride grid of 8, 16 or 32 blocks per SM), the key width
@@ -387,7 +388,8 @@ typedef struct PsyTuneOptions {
 typedef struct PsyTuneResult {
     uint32_t trace_mode;   /* 0: one thread per ray, 1: persistent, 2: warp packets,
                               3: static-scene traversal (scenes without motion or mesh
-                              instance transforms), 4: its speculative form */
+                              instance transforms), 4: its speculative form, 5: the
+                              static-scene traversal with lane refill */
     uint32_t minb;         /* register budget (resident blocks per SM) */
     uint32_t stack;        /* traversal stack entries */
     uint32_t grid;         /* wavefront kernel grid (0: sized by the queue) */

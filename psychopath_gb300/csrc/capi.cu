@@ -322,7 +322,10 @@ static int trace_device_core(PsyScene *s, const PsyRay *d_rays, uint32_t n, PsyH
         RayOrderBufs rb{b, b + n, b + 2 * (size_t)n, b + 3 * (size_t)n, b + 4 * (size_t)n};
         CK(launch_ray_order(s->g, d_rays, n, rb, &order, st), "ray order");
     }
-    if (d_full || s->trace_mode == 0 || s->trace_mode >= 3)
+    if (s->trace_mode == 5 && s->g.static_fast && !d_full && !ctr)
+        CK(launch_trace_static_refill_rays(s->g, d_rays, n, order, d_hits, s->stack, s->d_work, s->d_err, st),
+           "trace launch");
+    else if (d_full || s->trace_mode == 0 || s->trace_mode >= 3)
         CK(launch_trace_rays(s->g, d_rays, n, order, d_hits, d_full, s->stack, s->minb, s->d_err, ctr, st,
                              s->trace_mode >= 3 ? s->trace_mode - 2 : 0),
            "trace launch");
@@ -390,7 +393,10 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
     uint32_t *qin = B.queue[0], *cin = B.counts;
     for (uint32_t it = 0; it < iters; it++) {
         if (ev) cudaEventRecord(ev[2 + 3 * it], st);
-        if (s->trace_mode == 1)
+        if (s->trace_mode == 5 && s->g.static_fast && !ctr)
+            CK(launch_trace_static_refill_queue(s->g, B.R, B.H, qin, cin, n, s->stack, B.work, B.err, st),
+               "trace launch");
+        else if (s->trace_mode == 1)
             CK(launch_trace_persist_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, B.work, B.err, ctr, st),
                "trace launch");
         else if (s->trace_mode == 2)
@@ -896,8 +902,10 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
         std::vector<TuneCfg> v;
         for (int m : {4, 5, 6, 8}) { TuneCfg c = cur; c.trace_mode = 0; c.minb = m; v.push_back(c); }
         for (int m : {4, 6, 8}) { TuneCfg c = cur; c.trace_mode = 1; c.minb = m; v.push_back(c); }
-        if (s->g.static_fast)  // the static-scene traversal
+        if (s->g.static_fast) {  // the static-scene traversal, and its lane-refill form
             for (int m : {8, 10, 12}) { TuneCfg c = cur; c.trace_mode = 3; c.minb = m; v.push_back(c); }
+            TuneCfg c = cur; c.trace_mode = 5; c.minb = 10; v.push_back(c);
+        }
         // warp packets (trace mode 2) are not tried: 2-7x slower on every
         // measured workload, as one-thread-per-ray keeps more rays in flight
         try_set(v);
@@ -1189,10 +1197,11 @@ int psy_debug_counters(PsyScene *s, int enable, uint64_t *nodes, uint64_t *tris,
 // speculative form; minb = resident blocks per SM the register budget
 // targets.
 int psy_debug_set_trace(PsyScene *s, int mode, int minb) {
-    if (!s || mode < 0 || mode > 4) return fail(PSY_E_INVALID, "bad trace mode");
+    if (!s || mode < 0 || mode > 5) return fail(PSY_E_INVALID, "bad trace mode");
     s->trace_mode = mode;
     // persistent kernel: 4, 6 or 8 blocks per SM; one thread per ray: 4, 5,
-    // 6 or 8; static-scene traversal: 6, 8, 10 or 12
+    // 6 or 8; static-scene traversal: 6, 8, 10 or 12 (its lane-refill form,
+    // mode 5, always 10)
     if (mode == 1) s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : 4);
     else if (mode >= 3) s->minb = minb >= 12 ? 12 : (minb >= 10 ? 10 : (minb >= 8 ? 8 : 6));
     else s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : (minb == 5 ? 5 : 4));

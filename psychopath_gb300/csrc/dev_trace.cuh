@@ -765,6 +765,108 @@ done:
     return true;
 }
 
+// ------------------------------------------------------------------ static-scene traversal with lane refill
+// trace_ray_static's traversal cut into steps (descend to a leaf, test it,
+// pop), so that a persistent kernel can give a lane whose ray finished the
+// next ray of its queue while the other lanes of the warp go on (Aila &
+// Laine 2009).  Node and triangle tests, visit order and hit records are
+// trace_ray_static's, so hits are identical.
+struct SLane {
+    V3 o, d;        // the ray as given
+    V3 wo, di;      // world-level origin and inverse direction (identity transform, as trace_ray_static)
+    float tmax, time;
+    TriPre pre;
+    uint32_t cur, slot, hkind, hprim, hslot;
+    int sp;
+    uint32_t oct;
+    bool occl, in_inst, safe;
+};
+DI void slane_init(const GScene &S, SLane &L, V3 o, V3 d, float tmax, float time, bool occl) {
+    Xf ident = xf_identity();
+    L.o = o; L.d = d;
+    L.wo = xf_point(o, ident);
+    L.di = recip(xf_vector(d, ident));
+    L.tmax = tmax; L.time = time;
+    L.pre = tri_precompute(d);
+    L.cur = S.top_root;
+    L.slot = 0; L.hkind = PSY_HIT_MISS_K; L.hprim = 0; L.hslot = 0;
+    L.sp = 0;
+    L.oct = ray_code(L.di);
+    L.occl = occl; L.in_inst = false;
+    L.safe = slab_safe(L.wo, L.di, tmax);
+}
+// One step of lane L.  Returns 0 to go on, 1 when the ray is finished (hit
+// filled), -1 on stack overflow.
+template <int STACK, bool H16>
+DI int slane_step(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut, SLane &L, uint32_t *stack,
+                  HitRec &hit) {
+    if (L.cur == PSY_REF_NONE) {  // empty scene
+        hit.kind = PSY_HIT_MISS_K;
+        return 1;
+    }
+    const uint8_t *prow = prow_tab + 48 * L.oct;
+    while (!psy_is_leaf(L.cur)) {
+        uint32_t code;
+        uint4 ch;
+        uint32_t m = H16 ? node_hits_static_h(S, L.cur, L.wo, L.di, L.tmax, L.oct, L.safe, code, ch)
+                         : node_hits_static(S, L.cur, L.wo, L.di, L.tmax, L.oct, L.safe, code, ch);
+        uint32_t e = lut[16u * prow[code] + m];
+        if (!(e & 0x800u)) goto pop;
+        int np = (int)((e >> 8) & 7u);
+        if (L.sp + np > STACK) return -1;
+        stack[L.sp] = sel4(ch, (e >> 2) & 3u);
+        stack[L.sp + 1] = sel4(ch, (e >> 4) & 3u);
+        stack[L.sp + 2] = sel4(ch, (e >> 6) & 3u);
+        L.sp += np;
+        L.cur = sel4(ch, e & 3u);
+    }
+    if (!L.in_inst) {
+        L.slot = psy_leaf_first(L.cur);
+        GInstance in = S.instances[L.slot];
+        if (in.kind == PSY_INST_MESH) {
+            if (L.sp >= STACK) return -1;
+            stack[L.sp++] = PSY_REF_NONE;  // leave-instance marker
+            L.in_inst = true;
+            L.safe = slab_safe(L.wo, L.di, L.tmax);
+            L.cur = S.meshes[in.obj].root;
+            return 0;
+        } else if (in.kind == PSY_INST_RECT) {
+            float t, b0, b1, b2;
+            uint32_t which;
+            if (rect_hit(S, in, L.o, L.d, L.tmax, L.time, t, b0, b1, b2, which)) {
+                if (L.occl) { hit.kind = PSY_HIT_OCCLUDE_K; return 1; }
+                L.hkind = PSY_HIT_LIGHT_K; L.hprim = which; L.hslot = L.slot;
+                L.tmax = t;
+            }
+        } else {
+            Xf x = instance_xf_at(S, in, L.time);
+            V3 ol = in.xc ? xf_point(L.o, x) : L.wo;
+            float t;
+            if (sphere_hit(S, in, ol, L.d, L.tmax, L.time, t)) {
+                if (L.occl) { hit.kind = PSY_HIT_OCCLUDE_K; return 1; }
+                L.hkind = PSY_HIT_LIGHT_K; L.hprim = 0xFFFFFFFFu; L.hslot = L.slot;
+                L.tmax = t;
+            }
+        }
+    } else {
+        bool occluded = false;
+        static_leaf(S, L.cur, L.o, L.pre, L.slot, L.tmax, L.hkind, L.hprim, L.hslot, L.occl, occluded);
+        if (occluded) { hit.kind = PSY_HIT_OCCLUDE_K; return 1; }
+    }
+pop:
+    while (true) {
+        if (L.sp == 0) {
+            finish_hit<true>(S, L.o, L.pre, L.time, L.tmax, L.hkind, L.hprim, L.hslot, hit);
+            return 1;
+        }
+        L.cur = stack[--L.sp];
+        if (L.cur != PSY_REF_NONE) break;
+        L.in_inst = false;  // leaving the instance (world space is the instance's space)
+        L.safe = slab_safe(L.wo, L.di, L.tmax);
+    }
+    return 0;
+}
+
 }  // namespace psyd
 
 namespace psyd {

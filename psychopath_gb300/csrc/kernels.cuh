@@ -95,6 +95,13 @@ cudaError_t launch_ray_order(const GScene &S, const PsyRay *rays, uint32_t n, co
 // Persistent traversal kernels with per-lane ray refill.  `minb` selects the
 // register budget (4 or 8 resident blocks of 128 threads per SM); `work` is a
 // device counter the launch zeroes first.
+// The static-scene traversal with lane refill (trace mode 5; the scene must
+// have static_fast set): persistent blocks, work counter `work`.
+cudaError_t launch_trace_static_refill_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue,
+                                             const uint32_t *count, uint32_t max_count, int stack, uint32_t *work,
+                                             int *d_err, cudaStream_t st);
+cudaError_t launch_trace_static_refill_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order,
+                                            PsyHit *hits, int stack, uint32_t *work, int *d_err, cudaStream_t st);
 cudaError_t launch_trace_persist_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue,
                                        const uint32_t *count, uint32_t max_count, int stack, int minb, uint32_t *work,
                                        int *d_err, unsigned long long *counters, cudaStream_t st);

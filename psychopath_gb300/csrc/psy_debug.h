@@ -44,8 +44,9 @@ int psy_debug_scene_flags(PsyScene *scene, uint32_t *flags);
 /* Enable (and zero) or read the traversal counters of renders. */
 int psy_debug_counters(PsyScene *scene, int enable, uint64_t *nodes, uint64_t *tris, uint64_t *rays);
 /* Trace kernel: 0 one thread per ray, 1 persistent with lane refill, 2 warp
- * packets, 3 static-scene traversal, 4 its speculative form; minb = target
- * resident blocks per SM of the register budget. */
+ * packets, 3 static-scene traversal, 4 its speculative form, 5 the
+ * static-scene traversal with lane refill; minb = target resident blocks
+ * per SM of the register budget. */
 int psy_debug_set_trace(PsyScene *scene, int mode, int minb);
 /* Shading kernel register budget: 4, 6 or 8 resident blocks per SM. */
 int psy_debug_set_shade(PsyScene *scene, int minb);

@@ -289,6 +289,106 @@ static cudaError_t launch_persist(const GScene &S, const IO &io, uint32_t max_co
     return cudaGetLastError();
 }
 
+// Static-scene traversal with lane refill (trace mode 5): the persistent
+// loop of k_trace_persist over the static-scene traversal's steps
+// (slane_step), so a lane whose ray finished -- a shadow ray that met an
+// occluder early, a camera ray that left the scene -- takes the next ray
+// while the others of its warp go on.  Hits are trace_ray_static's.
+template <int STACK, int MINB, bool H16, class IO>
+__global__ void __launch_bounds__(128, MINB) k_trace_static_refill(GScene S, IO io, uint32_t *work, int *err) {
+    __shared__ __align__(16) uint8_t table[8 * 48];  // push rows per octant and traversal code
+    __shared__ __align__(16) uint16_t push_lut[PSY_PUSH_ROWS * 16];
+    load_push_tables(table, push_lut);
+    const uint32_t n = io.n();
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint32_t stack[STACK + 4];  // 3 spare entries take the unconditional stores of the child push
+    SLane L;
+    HitRec hit;
+    bool active = false, exhausted = false;
+    uint32_t id = 0;
+    while (true) {
+        unsigned idle = __ballot_sync(FULL, !active);
+        if (idle && !exhausted) {
+            int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(work, (uint32_t)__popc(idle));
+            base = __shfl_sync(FULL, base, leader);
+            if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+            if (!active) {
+                uint32_t my = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (my < n) {
+                    V3 o, d;
+                    float tmax, time;
+                    bool oc;
+                    id = io.load(my, o, d, tmax, time, oc);
+                    slane_init(S, L, o, d, tmax, time, oc);
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(FULL, active)) break;
+        if (active) {
+            int r = slane_step<STACK, H16>(S, table, push_lut, L, stack, hit);
+            if (r != 0) {
+                if (r < 0) {
+                    atomicExch(err, PSY_E_OVERFLOW);
+                    hit.kind = PSY_HIT_MISS_K;
+                }
+                io.store(S, id, hit);
+                active = false;
+            }
+        }
+    }
+}
+
+template <class IO, int STACK, bool H16>
+static int refill_grid() {
+    static int g = 0;
+    if (g == 0) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trace_static_refill<STACK, 10, H16, IO>, 128, 0);
+        g = sms * (per > 0 ? per : 1);
+    }
+    return g;
+}
+
+template <class IO>
+static cudaError_t launch_static_refill(const GScene &S, const IO &io, uint32_t max_count, int stack, uint32_t *work,
+                                        int *d_err, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+#define TS(SZ, H)                                                                                 \
+    {                                                                                             \
+        int g = refill_grid<IO, SZ, H>();                                                         \
+        uint32_t need = (max_count + 127) / 128;                                                  \
+        if ((uint32_t)g > need) g = (int)need;                                                    \
+        if (g > 0) k_trace_static_refill<SZ, 10, H, IO><<<g, 128, 0, st>>>(S, io, work, d_err);  \
+    }
+    if (S.use_fp16) {
+        if (stack <= 64) TS(64, true) else TS(192, true)
+    } else {
+        if (stack <= 64) TS(64, false) else TS(192, false)
+    }
+#undef TS
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_static_refill_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue,
+                                             const uint32_t *count, uint32_t max_count, int stack, uint32_t *work,
+                                             int *d_err, cudaStream_t st) {
+    IOQueue io{queue, count, R.o, R.d, R.occl, H.ki, H.tb};
+    return launch_static_refill(S, io, max_count, stack, work, d_err, st);
+}
+cudaError_t launch_trace_static_refill_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order,
+                                            PsyHit *hits, int stack, uint32_t *work, int *d_err, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    IORays io{rays, n, hits, order};
+    return launch_static_refill(S, io, n, stack, work, d_err, st);
+}
+
 cudaError_t launch_trace_persist_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue,
                                        const uint32_t *count, uint32_t max_count, int stack, int minb, uint32_t *work,
                                        int *d_err, unsigned long long *counters, cudaStream_t st) {

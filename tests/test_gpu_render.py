@@ -223,12 +223,12 @@ def test_shade_register_budget_does_not_change_image(gpu_lib, minb):
         g.close()
 
 
-@pytest.mark.parametrize("mode,minb", [(1, 8), (2, 4), (3, 8), (3, 12)])
+@pytest.mark.parametrize("mode,minb", [(1, 8), (2, 4), (3, 8), (3, 12), (5, 10)])
 def test_trace_mode_does_not_change_image(gpu_lib, mode, minb):
     """The wavefront renders the same image with the persistent, the
-    warp-packet and the static-scene traversal (on the static scene; the
-    motion scene falls back to the general kernel) as with one thread per
-    ray."""
+    warp-packet, the static-scene traversal and its lane-refill form (on the
+    static scene; the motion scene falls back to the general kernel) as with
+    one thread per ray."""
     for s in (sc.sphere_small(24, 16, 4, 6, level=3), sc.motion_small(24, 16, 4, 2)):
         g = gpu.Scene(s)
         r = gpu.Renderer(g)

@@ -194,7 +194,7 @@ def test_trace_kernel_variants_identical(gpu_lib, mode, minb):
     assert np.array_equal(h, ref)
 
 
-@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 8), (1, 8), (2, 4), (3, 10)])
+@pytest.mark.parametrize("mode,minb", [(0, 4), (0, 8), (1, 8), (2, 4), (3, 10), (5, 10)])
 def test_binned_ray_order_identical(gpu_lib, mode, minb):
     """Sorting a large batch by two-point key only changes which thread
     traces which ray: hits are identical to the given order."""
@@ -274,12 +274,14 @@ def test_warp_packets_match_per_ray(gpu_lib, case):
     assert (pn, pt) == (rn, rt)  # same node and triangle tests per ray
 
 
-@pytest.mark.parametrize("minb", [6, 8, 10, 12])
-def test_static_scene_traversal_identical(gpu_lib, minb):
-    """The static-scene traversal (trace mode 3) returns the same hits, bit
-    for bit, as the general kernel on static scenes: closest and any hit,
-    finite max_t, axis-parallel rays (the unordered slab test), the full
-    surface output, and misses; it agrees with the oracle like mode 0."""
+@pytest.mark.parametrize("mode,minb", [(3, 6), (3, 8), (3, 10), (3, 12), (5, 10)])
+@pytest.mark.parametrize("bounds", ["fp32", "fp16"])
+def test_static_scene_traversal_identical(gpu_lib, mode, minb, bounds):
+    """The static-scene traversal (trace mode 3) and its lane-refill form
+    (mode 5) return the same hits, bit for bit, as the general kernel on
+    static scenes: closest and any hit, finite max_t, axis-parallel rays (the
+    unordered slab test), the full surface output, and misses; with FP32 and
+    with FP16 child bounds."""
     cases = []
     sd, P, F = sc.grid_small(256, 128)
     cases.append((sd, np.concatenate([scenes.incoherent_rays(P, F, 1 << 15, seed=7), scenes.coherent_rays(96)])))
@@ -294,13 +296,13 @@ def test_static_scene_traversal_identical(gpu_lib, minb):
     cases.append((sc.cornell(), np.concatenate([rays, ax])))
     n_static = 0
     for sd, rays in cases:
-        g = gpu.Scene(sd)
+        g = gpu.Scene(sd, bounds=bounds)
         n_static += g.flags()["static_fast"]
         tr = gpu.Tracer(g)
         g.set_trace(0, 4)
         ref, fref = tr.trace(rays, full=True)
         ref2 = tr.trace(rays)
-        g.set_trace(3, minb)
+        g.set_trace(mode, minb)
         h = tr.trace(rays)
         h2, f2 = tr.trace(rays, full=True)
         assert np.array_equal(h, ref2)
@@ -359,7 +361,7 @@ def test_deep_tree_large_stack_kernels(gpu_lib):
     tr = gpu.Tracer(g)
     g.set_trace(0, 4)
     ref = tr.trace(rays)
-    for mode, minb in [(0, 8), (3, 6), (3, 8), (3, 10), (3, 12), (1, 8)]:
+    for mode, minb in [(0, 8), (3, 6), (3, 8), (3, 10), (3, 12), (1, 8), (5, 10)]:
         g.set_trace(mode, minb)
         assert np.array_equal(tr.trace(rays), ref), (mode, minb)
     g.close()
