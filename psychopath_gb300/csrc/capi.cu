@@ -1157,6 +1157,16 @@ int psy_debug_host_nodes(const PsySceneDesc *desc, const PsySceneOptions *opts, 
     if (bounds_ext) std::memcpy(bounds_ext, hs.bounds_ext.data(), hs.bounds_ext.size() * sizeof(GBounds4));
     return PSY_OK;
 }
+int psy_debug_host_nodes_h(const PsySceneDesc *desc, const PsySceneOptions *opts, void *nodes_h,
+                           uint32_t *node_count) {
+    HostScene hs;
+    std::string err;
+    int rc = build_host_scene(desc, opts, hs, err, nullptr, false);
+    if (rc != PSY_OK) return fail(rc, err);
+    if (node_count) *node_count = (uint32_t)hs.nodes_h.size();
+    if (nodes_h) std::memcpy(nodes_h, hs.nodes_h.data(), hs.nodes_h.size() * sizeof(GNodeH));
+    return PSY_OK;
+}
 int psy_debug_scene_info(PsyScene *s, uint32_t *max_stack, uint32_t *nodes, uint32_t *stack_variant) {
     if (!s) return fail(PSY_E_INVALID, "null");
     if (max_stack) *max_stack = s->max_stack;

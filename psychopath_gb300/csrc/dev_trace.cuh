@@ -160,8 +160,8 @@ DI float4 dec_plane(uint2 q, float anchor) {
     asm("mov.b32 {%0, %1}, %2;" : "=h"(h2), "=h"(h3) : "r"(q.y));
     return make_float4(dec_h(h0, anchor), dec_h(h1, anchor), dec_h(h2, anchor), dec_h(h3, anchor));
 }
-// Child hit mask of an FP16 node.  Lower bounds decode from the node's min
-// corner a (anchor), upper bounds from its max corner, itself decoded as
+// Child hit mask of an FP16 node.  Lower bounds decode from the node's
+// anchor a, upper bounds from its top corner, itself decoded as
 // fl32(a + ext).  safe: octant-ordered planes as in node_hits (the decoded
 // boxes are ordered too: lo16 <= lo32 <= hi32 <= hi16).
 DI uint32_t fp16_hits(const GNodeH *n, float4 a, V3 o, V3 di, float tmax, uint32_t oct, bool safe) {

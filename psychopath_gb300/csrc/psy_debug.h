@@ -34,6 +34,11 @@ int psy_debug_host_build(const PsySceneDesc *desc, const PsySceneOptions *opts, 
  * one thread.  Null arrays return the counts only. */
 int psy_debug_host_nodes(const PsySceneDesc *desc, const PsySceneOptions *opts, int serial, void *nodes,
                          uint32_t *node_count, void *bounds_ext, uint32_t *ext_count);
+/* Host build only: the FP16 node copies (96 bytes each, same indices as the
+ * BVH4 nodes; none unless opts asks for FP16 bounds).  Null nodes_h returns
+ * the count only. */
+int psy_debug_host_nodes_h(const PsySceneDesc *desc, const PsySceneOptions *opts, void *nodes_h,
+                           uint32_t *node_count);
 /* Worst-case stack depth, node count and the stack variant (64 or 192). */
 int psy_debug_scene_info(PsyScene *scene, uint32_t *max_stack, uint32_t *nodes, uint32_t *stack_variant);
 /* bit 0: the static-scene traversal applies; bit 1: ordered child boxes;

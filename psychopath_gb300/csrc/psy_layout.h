@@ -39,16 +39,17 @@ struct __align__(16) GNode {
 struct __align__(16) GBounds4 {
     float4 xlo, xhi, ylo, yhi, zlo, zhi;
 };
-// Half-precision variant: child bounds as f16 offsets, lower bounds from the
-// min corner of the children's union (anchor), upper bounds from its max
-// corner (decoded as fl32(anchor + ext)), each chosen so the decoded f32
-// bound fl32(corner + offset) lies outside the f32 bound (the decoded box
-// contains the f32 box).  96 bytes per node.
+// Half-precision variant: child bounds as signed f16 offsets, lower bounds
+// from an anchor (per axis the min corner of the children's union, or the
+// plane of a child that is flat on that axis), upper bounds from a top
+// corner decoded as fl32(anchor + ext), each chosen so the decoded f32 bound
+// fl32(corner + offset) lies outside the f32 bound (the decoded box contains
+// the f32 box; a flat child decodes exactly flat).  96 bytes per node.
 struct __align__(16) GNodeH {
-    float4 anchor;  // xyz: min corner of the union of the children, w: meta bits
+    float4 anchor;  // xyz: per axis the children's min corner or a flat child's plane, w: meta bits
                     // (traversal code | child count << 8 | PSY_NODEH_F32 flags)
     uint4 child;
-    uint2 ext;      // f16 extents x | y << 16 and z: the max corner is fl32(anchor + ext)
+    uint2 ext;      // f16 extents x | y << 16 and z: the top corner is fl32(anchor + ext)
     uint2 xlo, xhi, ylo, yhi, zlo, zhi;  // 4 x f16 per slab (48 bytes)
     uint2 pad;
 };

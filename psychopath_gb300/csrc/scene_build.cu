@@ -1042,17 +1042,33 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
             // device as fl32(anchor + extent)), so every face near the
             // node's own faces -- most of them -- is encoded by a small
             // offset, i.e. nearly exactly
+            //
+            // A child box that is flat on an axis (lo == hi: a floor, a wall,
+            // an axis-aligned quad) must decode flat: a slab of even 1e-5
+            // around a ground plane holds the origins of the rays that leave
+            // the plane, which would all enter its box and test its
+            // triangles.  On such an axis the plane itself is the anchor
+            // and the upper bounds are encoded from it too (extent 0), so
+            // the plane's offsets are 0 and exact; a node where a flat face
+            // still does not decode exactly keeps its f32 bounds.
             float anchor[3], top[3];
             uint16_t ext[3] = {0, 0, 0};
             bool fits = true;
             for (int a = 0; a < 3; a++) {
                 float m = INFINITY, M = -INFINITY;
+                int flat = -1;
                 for (uint32_t l = 0; l < cc; l++) {
                     m = std::min(m, lo[a][l]);
                     M = std::max(M, hi[a][l]);
+                    if (flat < 0 && lo[a][l] == hi[a][l]) flat = (int)l;
                 }
-                anchor[a] = std::isfinite(m) ? m : 0.0f;
-                if (std::isfinite(M) && std::isfinite(m)) fits = fits && f16_offset(anchor[a], M, +1, ext[a]);
+                if (flat >= 0) {
+                    anchor[a] = lo[a][flat];
+                    ext[a] = 0;
+                } else {
+                    anchor[a] = std::isfinite(m) ? m : 0.0f;
+                    if (std::isfinite(M) && std::isfinite(m)) fits = fits && f16_offset(anchor[a], M, +1, ext[a]);
+                }
                 top[a] = anchor[a] + f16_value(ext[a]);
             }
             uint16_t q[6][4];
@@ -1065,6 +1081,9 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
                     }
                     fits = fits && f16_offset(anchor[a], lo[a][l], -1, q[a * 2][l]) &&
                            f16_offset(top[a], hi[a][l], +1, q[a * 2 + 1][l]);
+                    if (fits && lo[a][l] == hi[a][l])  // a flat face decodes exactly, or the node stays f32
+                        fits = anchor[a] + f16_value(q[a * 2][l]) == lo[a][l] &&
+                               top[a] + f16_value(q[a * 2 + 1][l]) == hi[a][l];
                 }
             // bit 16: motion keys, bit 17: an offset does not fit an f16; either
             // way the traversal reads this node's f32 copy

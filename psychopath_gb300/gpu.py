@@ -73,6 +73,7 @@ def lib(path=None):
     L.psy_debug_push_tables.argtypes = [vp, vp, vp]
     L.psy_debug_scene_flags.argtypes = [vp, C.POINTER(u32)]
     L.psy_debug_host_nodes.argtypes = [vp, vp, C.c_int, vp, C.POINTER(u32), vp, C.POINTER(u32)]
+    L.psy_debug_host_nodes_h.argtypes = [vp, vp, vp, C.POINTER(u32)]
     L.psy_debug_render_paths.argtypes = [vp, vp, u32, u32, vp, vp]
     L.psy_debug_samplers.argtypes = [C.c_int, vp, u32, vp, vp]
     L.psy_server_create.argtypes = [vp, C.POINTER(vp)]
@@ -123,6 +124,19 @@ def host_nodes(scene_data, serial=False, bounds="fp32"):
     _check(lib().psy_debug_host_nodes(C.byref(desc), C.byref(opts), 1 if serial else 0, nodes.ctypes.data,
                                       C.byref(nc), ext.ctypes.data, C.byref(ec)))
     return nodes, ext[:ec.value * 96]
+
+
+def host_nodes_h(scene_data):
+    """Host-side build only (no GPU needed): the FP16 node copies of the
+    scene's BVH4 nodes as raw bytes, 96 per node."""
+    desc = scene_data.desc()
+    opts = abi.PsySceneOptions()
+    opts.bounds_precision = abi.PSY_BOUNDS_FP16
+    nc = C.c_uint32()
+    _check(lib().psy_debug_host_nodes_h(C.byref(desc), C.byref(opts), None, C.byref(nc)))
+    nodes = np.zeros(nc.value * 96, dtype=np.uint8)
+    _check(lib().psy_debug_host_nodes_h(C.byref(desc), C.byref(opts), nodes.ctypes.data, C.byref(nc)))
+    return nodes
 
 
 def halton_samples_device(dimension, d_indices_ptr, n, d_out_ptr, stream=None):
