@@ -69,7 +69,8 @@ def parse_args():
     ap.add_argument("--form", default="both", choices=["both", "plain", "optimized"],
                     help="frame workloads: which forms to time (the headline is the optimized one)")
     ap.add_argument("--launch", default="",
-                    help="optimized form: fixed launch configuration 'mode,minb[,queue binning bits[,wave paths]]' "
+                    help="optimized form: fixed launch configuration 'mode,minb[,queue binning bits[,wave paths"
+                         "[,grid]]]' (grid -1: each wavefront kernel's resident blocks) "
                          "instead of psy_autotune (profiling a known configuration)")
     return ap.parse_args()
 
@@ -325,11 +326,12 @@ def run_ours(args):
             vals = [int(x) for x in args.launch.split(",")]
             mode, minb, bits = vals[0], vals[1], (vals[2] if len(vals) > 2 else 0)
             wave = vals[3] if len(vals) > 3 else 1 << 24
+            grid = vals[4] if len(vals) > 4 else 0
             scene.set_trace(mode, minb)
             scene.set_sort(bits)
-            scene.set_launch(0, wave)
+            scene.set_launch(grid, wave)
             tune = {"trace_mode": mode, "minb": minb, "wave_paths": wave, "sort_bits": bits, "use_graph": 0,
-                    "fixed": True}
+                    "grid": grid, "fixed": True}
         else:
             tune = scene.autotune()
         tune_s = time.perf_counter() - t0

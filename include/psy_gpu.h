@@ -362,7 +362,8 @@ int psy_render_bucket_noalloc(PsyScene *scene, const PsyBucket *bucket, uint32_t
  * register budget (4, 6 or
  * 8 blocks per SM), the traversal stack depth (64 or 192 entries, if the
  * scene fits), the queue tile (grid of the wavefront kernels: sized by the
- * queue, or a grid-stride grid of 8, 16 or 32 blocks per SM), the key width
+ * queue, a grid-stride grid of 8, 16 or 32 blocks per SM, or each kernel's
+ * resident blocks striding over the queue), the key width
  * of the queue binning between wavefront iterations (0 = off, 4 = occlusion
  * flag and direction octant, 10 / 13 / 16 = also 2 / 3 / 4 bits per axis of
  * the origin's cell, 19 / 25 = occlusion flag above a two-point key, radix
@@ -385,6 +386,8 @@ typedef struct PsyTuneOptions {
     uint32_t reserved[5];
 } PsyTuneOptions;
 
+#define PSY_TUNE_GRID_RESIDENT 0xFFFFFFFFu
+
 typedef struct PsyTuneResult {
     uint32_t trace_mode;   /* 0: one thread per ray, 1: persistent, 2: warp packets,
                               3: static-scene traversal (scenes without motion or mesh
@@ -392,7 +395,8 @@ typedef struct PsyTuneResult {
                               static-scene traversal with lane refill */
     uint32_t minb;         /* register budget (resident blocks per SM) */
     uint32_t stack;        /* traversal stack entries */
-    uint32_t grid;         /* wavefront kernel grid (0: sized by the queue) */
+    uint32_t grid;         /* wavefront kernel grid (0: sized by the queue,
+                              PSY_TUNE_GRID_RESIDENT: each kernel's resident blocks) */
     uint32_t sort_bits;
     uint32_t wave_paths;
     uint32_t use_graph;

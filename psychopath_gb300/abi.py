@@ -24,6 +24,7 @@ PSY_NOALLOC_MAX_SAMPLES = 262144
 PSY_HIT_MISS, PSY_HIT_OCCLUDE, PSY_HIT_SURFACE, PSY_HIT_LIGHT = 0, 1, 2, 3
 PSY_REQ_QUEUED, PSY_REQ_RUNNING, PSY_REQ_DONE, PSY_REQ_CANCELLED, PSY_REQ_FAILED = 0, 1, 2, 3, 4
 PSY_SCHED_FIFO, PSY_SCHED_SHORTEST = 0, 1
+PSY_TUNE_GRID_RESIDENT = 0xFFFFFFFF
 
 _fp = C.POINTER(C.c_float)
 _up = C.POINTER(C.c_uint32)
@@ -148,7 +149,10 @@ class PsyTuneResult(C.Structure):
                 ("shade_minb", C.c_uint32), ("candidates", C.c_uint32), ("default_s", C.c_double), ("best_s", C.c_double)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        if d["grid"] == PSY_TUNE_GRID_RESIDENT:
+            d["grid"] = -1  # each wavefront kernel's resident blocks
+        return d
 
 
 # numpy structured dtypes with the same layout (for bulk ray / hit buffers)

@@ -4,7 +4,10 @@ Each translation unit compiles in its own nvcc process (in parallel), then
 one nvcc link step makes the shared library in psychopath_gb300/_lib/.
 Floating point: --fmad=false on the device and -ffp-contract=off on the host
 so every operation rounds as written (parity with the reference's CPU
-arithmetic); precise division and square root stay on (nvcc defaults).
+arithmetic); precise division and square root stay on (nvcc defaults).  The
+one exception is wave_f32.cu, the f32 camera and hit-shading kernels of the
+optimized form, compiled with FMA contraction (its error against the FP64
+oracle is measured).
 """
 import os
 import subprocess
@@ -16,7 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(OUT_DIR, "libpsy_gpu.so")
 SOURCES = ["kernels.cu", "trace_kernels.cu", "scene_build.cu", "capi.cu", "server.cu", "bvh_build.cu",
-           "radix_sort.cu", "halton.cu"]
+           "radix_sort.cu", "halton.cu", "wave_f32.cu"]
+FMAD = {"wave_f32.cu": "--fmad=true"}  # per-source override of --fmad=false
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -48,7 +52,8 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
-        cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + common
+        cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + [FMAD.get(src, f) if f == "--fmad=false" else f
+                                                                   for f in common]
         if verbose:
             cmd += ["-Xptxas", "-v"]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -930,6 +930,7 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         std::vector<TuneCfg> v;
         for (int k : {0, 8, 16, 32}) { TuneCfg c = cur; c.grid = k * sms; if (c.grid != cur.grid) v.push_back(c); }
+        if (cur.grid != PSY_GRID_RESIDENT) { TuneCfg c = cur; c.grid = PSY_GRID_RESIDENT; v.push_back(c); }
         try_set(v);
     }
     // 4. ray-sort key width
@@ -1047,9 +1048,9 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
                         }
                     };
                     std::vector<TuneCfg> grids, keys;
-                    for (int k : {0, 16, 32, 64}) {
+                    for (int k : {-1, 0, 16, 32, 64}) {
                         TuneCfg c = best_c;
-                        c.grid = k * sms;
+                        c.grid = k < 0 ? PSY_GRID_RESIDENT : k * sms;
                         if (c.grid != best_c.grid) grids.push_back(c);
                     }
                     recheck(grids);

@@ -1,13 +1,17 @@
 // Kernels of the GB300 tracing path: camera ray generation, the light-path
-// state machine and accumulation (traversal kernels: trace_kernels.cu).
+// state machine and accumulation (traversal kernels: trace_kernels.cu; the
+// f32 camera and hit-shading kernels of the optimized form: wave_f32.cu).
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 #include "dev_bins.cuh"
 #include "dev_surface.cuh"
 #include "kernels.cuh"
 #include "radix_sort.h"
+#include "wave_kernels.cuh"
 
 using namespace psyd;
 
@@ -91,269 +95,18 @@ void psy_upload_constants() {
     cudaMemcpyToSymbol(c_sobol_dirs, d, sizeof(d));
     cudaMemcpyToSymbol(c_traversal_table, t, sizeof(t));
     psy_upload_trace_constants(t, nullptr);
-}
-
-// ------------------------------------------------------------------ wave segments
-// Copies the wave descriptor into shared memory (one read per block).
-__device__ __forceinline__ void load_wave(const WaveDesc *__restrict__ g, WaveDesc &sm) {
-    const uint32_t *src = reinterpret_cast<const uint32_t *>(g);
-    uint32_t *dst = reinterpret_cast<uint32_t *>(&sm);
-    for (int i = threadIdx.x; i < (int)(sizeof(WaveDesc) / 4); i += blockDim.x) dst[i] = src[i];
-    __syncthreads();
-}
-__device__ __forceinline__ int seg_of_path(const WaveDesc &wd, uint32_t p) {
-    int i = 0;
-    while (i + 1 < (int)wd.nseg && p >= wd.seg[i + 1].path_begin) i++;
-    return i;
-}
-__device__ __forceinline__ int seg_of_pixel(const WaveDesc &wd, uint32_t q) {
-    int i = 0;
-    while (i + 1 < (int)wd.nseg && q >= wd.seg[i + 1].pix_begin) i++;
-    return i;
-}
-
-// ------------------------------------------------------------------ camera
-// Ray generation of Renderer::render_job (src/renderer.rs:241-275) and
-// LightPath::new (src/renderer.rs:392-431) / Camera::generate_ray
-// (src/camera.rs:74-102).
-template <class RT>
-__global__ void k_camera(GScene S, const WaveDesc *__restrict__ gwave, PathState P, RayBuf R, uint32_t *queue,
-                         uint32_t *count) {
-    __shared__ WaveDesc wdesc;
-    // blocks past the wave's paths (the grid covers its capacity) leave
-    // before the descriptor copy; block 0 always stays to write the count
-    if (blockIdx.x > 0 && blockIdx.x * blockDim.x >= gwave->npaths) return;
-    load_wave(gwave, wdesc);
-    uint32_t n = wdesc.npaths;
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p == 0) *count = n;
-    if (p >= n) return;
-    const WaveSeg &w = wdesc.seg[seg_of_path(wdesc, p)];
-    uint32_t lp = (p - w.path_begin) / w.spp, si = (p - w.path_begin) - lp * w.spp;
-    uint32_t x = w.x0 + lp % w.w, y = w.y0 + (lp / w.w) * w.ystep;
-    float cmpx = 1.0f / (float)w.img_w, cmpy = 1.0f / (float)w.img_h;
-    float min_x = -1.0f, max_x = 1.0f;
-    float min_y = -((float)w.img_h / (float)w.img_w), max_y = (float)w.img_h / (float)w.img_w;
-    float xe = max_x - min_x, ye = max_y - min_y;
-    float d[4], d4[4];
-    get_sample_4d(si, 0, x, y, w.seed, d);
-    get_sample_4d(si, 1, x, y, w.seed, d4);
-    float fx = probit<RT>(d[3], 2.0f / 6.0f) + 0.5f;
-    float fy = probit<RT>(d4[0], 2.0f / 6.0f) + 0.5f;
-    float sx = (fx + (float)x) * cmpx;
-    float sy = (fy + (float)y) * cmpy;
-    float ix = (sx - 0.5f) * xe, iy = (0.5f - sy) * ye;
-    float wl = map_0_1_to_wavelength(golden_ratio_sample(si, hash_u32((x << 16) ^ y, w.seed)));
-    float time = d[0];
-    // Camera::generate_ray
-    Xf xf = lerp_slice_xf(S.cam_xf, S.n_cam_xf, time);
-    float tfov = lerp_slice_f(S.cam_tfov, S.n_cam_tfov, time);
-    float ar = lerp_slice_f(S.cam_ap, S.n_cam_ap, time);
-    float fd = lerp_slice_f(S.cam_fd, S.n_cam_fd, time);
-    float cu, cv;
-    square_to_circle((d[1] * 2.0f) - 1.0f, (d[2] * 2.0f) - 1.0f, &cu, &cv);
-    V3 orig = v3(ar * cu, ar * cv, 0.0f);
-    V3 dir = normalized(v3((ix * tfov) - (orig.x / fd), (iy * tfov) - (orig.y / fd), 1.0f));
-    V3 wo = xf_point(orig, xf), wd = xf_vector(dir, xf);
-    P.color[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    P.latt[p] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-    P.pending[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    P.nafac[p] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-    P.nb_o[p] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);  // w: closure_sample_pdf = 1
-    P.nb_d[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    P.tw[p] = make_float2(time, wl);
-    P.seed[p] = w.seed ^ 0x40d4682bu;
-    P.flags[p] = 0u;  // EV_CAMERA, bounce 0, no next bounce, 0 rays
-    R.o[p] = make_float4(wo.x, wo.y, wo.z, CUDART_INF_F);
-    R.d[p] = make_float4(wd.x, wd.y, wd.z, time);
-    R.occl[p] = 0;
-    queue[p] = p;
+    psy_upload_wave_f32_constants(d, nullptr);
 }
 
 cudaError_t launch_camera(const GScene &S, const WaveDesc *d_wave, uint32_t max_paths, PathState P, RayBuf R,
                           uint32_t *queue, uint32_t *count, int prec, cudaStream_t st) {
     uint32_t n = max_paths;
     if (n == 0) return cudaSuccess;
-    if (prec == 1) k_camera<float><<<(n + 255) / 256, 256, 0, st>>>(S, d_wave, P, R, queue, count);
-    else k_camera<double><<<(n + 255) / 256, 256, 0, st>>>(S, d_wave, P, R, queue, count);
+    if (prec == 1) return launch_camera_f32(S, d_wave, n, P, R, queue, count, st);
+    k_camera<double><<<(n + 255) / 256, 256, 0, st>>>(S, d_wave, P, R, queue, count);
     return cudaGetLastError();
 }
 
-// ------------------------------------------------------------------ shade
-#define EV_CAMERA 0u
-#define EV_BOUNCE 1u
-#define EV_SHADOW 2u
-
-__device__ __forceinline__ void push_live(bool alive, uint32_t p, uint32_t *next_queue, uint32_t *next_count) {
-    unsigned mask = __ballot_sync(__activemask(), alive);
-    if (mask == 0) return;
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(mask) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(next_count, (uint32_t)__popc(mask));
-    base = __shfl_sync(__activemask(), base, leader);
-    if (alive) next_queue[base + __popc(mask & ((1u << lane) - 1u))] = p;
-}
-
-// LightPath::next (src/renderer.rs:449-691), in two kernels over the same
-// queue of paths whose rays were just traced: k_shade_hit takes the paths
-// whose ray was a camera or bounce ray (surface hit, emission, background,
-// light sample and bounce -- the heavy part), k_shade_shadow those whose ray
-// was a shadow ray (add the pending light, set up the next bounce -- a few
-// loads and stores).  Each skips the other kind, so the shadow results run
-// at the occupancy of their own small register footprint rather than the
-// hit kernel's; a queue ordered by ray key (the occlusion flag is its top
-// bit) keeps the kinds contiguous, so skipped warps leave at once.
-// k_shade_shadow runs first and marks the paths it shaded (PSY_SHADED_BIT
-// in their flags); k_shade_hit skips the marked paths and clears the mark,
-// so each path of the queue is shaded once per iteration.
-#define PSY_SHADED_BIT (1u << 11)
-template <class RT, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDesc *__restrict__ gwave, PathState P,
-                                                   RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
-                                                   const uint32_t *__restrict__ count, uint32_t *next_queue,
-                                                   uint32_t *next_count) {
-    __shared__ WaveDesc wdesc;
-    uint32_t n = *count;
-    // blocks past the queue's length (the grid covers the wave's capacity)
-    // leave at once, before the descriptor copy and its barrier
-    if (blockIdx.x * blockDim.x >= n) return;
-    load_wave(gwave, wdesc);
-    uint32_t stride = gridDim.x * blockDim.x;
-    uint32_t nloop = (n + stride - 1) / stride * stride;  // keep whole warps in the loop for the ballot
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nloop; q += stride) {
-        bool alive = false;
-        uint32_t p = 0;
-        uint32_t fl = 0;
-        if (q < n) {
-            p = queue[q];
-            fl = P.flags[p];
-        }
-        if (q < n && (fl & PSY_SHADED_BIT)) {
-            P.flags[p] = fl & ~PSY_SHADED_BIT;  // shaded by k_shade_shadow this iteration
-        } else if (q < n) {
-            uint32_t ev = fl & 3u, bounce = (fl >> 2) & 0xFFu, has_nb = (fl >> 10) & 1u, nrays = fl >> 16;
-            nrays += 1;
-            float2 tw = P.tw[p];
-            float time = tw.x, wl = tw.y;
-            uint4 ki = H.ki[p];
-            V4 color = v4(P.color[p]);
-            V4 latt = v4(P.latt[p]);
-            // the hit's barycentrics, the ray and the sampling state
-            float4 tb = H.tb[p];
-            float4 ro = R.o[p], rd = R.d[p];
-            V3 o = v3(ro), d = v3(rd);
-            float4 nbo = P.nb_o[p];
-            float csp = nbo.w;  // closure_sample_pdf
-            uint32_t seed = P.seed[p];
-            const WaveSeg &w = wdesc.seg[seg_of_path(wdesc, p)];
-            uint32_t lp = p - w.path_begin;
-            uint32_t pix = lp / w.spp;
-            uint32_t si = lp - pix * w.spp;
-            uint32_t px = w.x0 + pix % w.w, py = w.y0 + (pix / w.w) * w.ystep;
-            if (ki.x == PSY_HIT_SURFACE_K || ki.x == PSY_HIT_LIGHT_K) {
-                HitRec h;
-                h.kind = ki.x; h.prim = ki.y; h.slot = ki.z;
-                h.t = tb.x; h.b0 = tb.y; h.b1 = tb.z; h.b2 = tb.w;
-                SurfData sd;
-                resolve_hit<RT>(S, h, o, d, time, sd);
-                const Closure &cl = sd.closure;
-                if (cl.kind == PSY_CL_EMIT) {
-                    V4 c = color_to_spectral(cl.color, wl);
-                    if (ev == EV_CAMERA) {
-                        color = color + c;
-                    } else {
-                        float mis = power_heuristic(csp, sd.sample_pdf);
-                        color = color + c * latt / splat4(mis);
-                    }
-                    P.color[p] = f4(color);
-                } else {
-                    latt = latt / splat4(csp);
-                    seed += 1;
-                    // the surface colour's spectrum: shared by the light
-                    // sample's evaluation and the bounce sample
-                    V4 cspec = color_to_spectral(cl.color, wl);
-                    float smp[4];
-                    get_sample_4d(si, 0, px, py, seed, smp);
-                    LightSample li = scene_sample_lights<RT>(S, smp[0], smp[1], smp[2], wl, time, d, sd.pos,
-                                                             sd.nor, sd.nor_g, cl);
-                    bool found = false;
-                    if (li.kind != 0 && !(li.pdf <= 0.0f) && !(li.sel_pdf <= 0.0f)) {
-                        V4 att;
-                        float cpdf;
-                        V3 so, sdir;
-                        float smax;
-                        if (li.kind == 1) {
-                            att = closure_evaluate(cl, cspec, d, li.dir, sd.nor, sd.nor_g, &cpdf);
-                            so = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), li.dir);
-                            sdir = li.dir;
-                            smax = CUDART_INF_F;
-                        } else {
-                            V3 dir = li.sp - sd.pos;
-                            att = closure_evaluate(cl, cspec, d, dir, sd.nor, sd.nor_g, &cpdf);
-                            so = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
-                            V3 oe = robust_ray_origin(li.sp, li.serr, normalized(li.sn), neg(dir));
-                            sdir = oe - so;
-                            smax = 1.0f;
-                        }
-                        if (!(max_elem4(att) <= 0.0f)) {
-                            float lmis = power_heuristic(li.pdf, cpdf);
-                            V4 pend = li.color * att * latt / splat4(lmis * li.sel_pdf);
-                            P.pending[p] = f4(pend);
-                            R.o[p] = make_float4(so.x, so.y, so.z, smax);
-                            R.d[p] = make_float4(sdir.x, sdir.y, sdir.z, time);
-                            R.occl[p] = 1;
-                            found = true;
-                        }
-                    }
-                    bool do_bounce = false;
-                    V4 nafac = v4(P.nafac[p]);
-                    if (bounce < S.max_bounces) {
-                        bounce += 1;
-                        seed += 1;
-                        float b4[4];
-                        get_sample_4d(si, 0, px, py, seed, b4);
-                        V3 dir;
-                        float pdf;
-                        V4 filt = closure_sample(cl, cspec, d, sd.nor, sd.nor_g, b4[0], b4[1], &dir, &pdf);
-                        if ((pdf > 0.0f) && (max_elem4(filt) > 0.0f)) {
-                            nafac = filt;
-                            csp = pdf;
-                            V3 nb = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
-                            P.nafac[p] = f4(nafac);
-                            P.nb_o[p] = make_float4(nb.x, nb.y, nb.z, csp);
-                            P.nb_d[p] = make_float4(dir.x, dir.y, dir.z, 0.0f);
-                            has_nb = 1;
-                            do_bounce = true;
-                        }
-                    } else {
-                        has_nb = 0;
-                    }
-                    if (found) {
-                        ev = EV_SHADOW;
-                        alive = true;
-                    } else if (do_bounce) {
-                        float4 nb = P.nb_o[p], nd = P.nb_d[p];
-                        R.o[p] = make_float4(nb.x, nb.y, nb.z, CUDART_INF_F);
-                        R.d[p] = make_float4(nd.x, nd.y, nd.z, time);
-                        R.occl[p] = 0;
-                        ev = EV_BOUNCE;
-                        latt = latt * nafac;
-                        alive = true;
-                    }
-                    P.latt[p] = f4(latt);
-                    P.seed[p] = seed;
-                }
-            } else {
-                V4 bg = color_to_spectral(S.background, wl);
-                color = color + bg * latt / splat4(csp);
-                P.color[p] = f4(color);
-            }
-            P.flags[p] = ev | (bounce << 2) | (has_nb << 10) | (nrays << 16);
-        }
-        push_live(alive, p, next_queue, next_count);
-    }
-}
 
 // Shadow-ray results: the pending light contribution when the shadow ray
 // was not occluded, then the next bounce ray if the path has one.
@@ -398,23 +151,44 @@ __global__ void __launch_bounds__(128, 12) k_shade_shadow(PathState P, RayBuf R,
     }
 }
 
+int queue_grid(const void *fn, int grid, uint32_t max_count) {
+    int need = (int)((max_count + 127) / 128);
+    if (grid > 0 || need == 0) return grid > 0 ? grid : 0;
+    if (grid == 0) return need;
+    // resident blocks of fn: SMs x blocks per SM at 128 threads, cached per
+    // kernel and device (the query is a driver call)
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find({fn, dev});
+    if (it == cache.end()) {
+        int sms = 0, per = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 128, 0);
+        it = cache.emplace(std::make_pair(fn, dev), std::max(1, sms) * std::max(1, per)).first;
+    }
+    return std::min(need, it->second);
+}
+
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                          const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
                          int minb, int grid, int prec, cudaStream_t st) {
-    if (grid <= 0) grid = (int)((max_count + 127) / 128);
-    if (grid == 0) return cudaSuccess;
-    k_shade_shadow<<<grid, 128, 0, st>>>(P, R, H, queue, count, next_queue, next_count);
-#define SH(RT, MB) k_shade_hit<RT, MB><<<grid, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count)
-    // budget 4 = the compiler's own choice (MINB 0 = unspecified)
-    if (prec == 1) {
-        if (minb >= 8) SH(float, 8);
-        else if (minb >= 6) SH(float, 6);
-        else SH(float, 0);
-    } else {
-        if (minb >= 8) SH(double, 8);
-        else if (minb >= 6) SH(double, 6);
-        else SH(double, 0);
+    int gs = queue_grid((const void *)k_shade_shadow, grid, max_count);
+    if (gs == 0) return cudaSuccess;
+    k_shade_shadow<<<gs, 128, 0, st>>>(P, R, H, queue, count, next_queue, next_count);
+#define SH(RT, MB)                                                                                           \
+    {                                                                                                        \
+        int g = queue_grid((const void *)k_shade_hit<RT, MB>, grid, max_count);                              \
+        k_shade_hit<RT, MB><<<g, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count);    \
     }
+    // budget 4 = the compiler's own choice (MINB 0 = unspecified)
+    if (prec == 1) return launch_shade_hit_f32(S, d_wave, P, R, H, queue, count, max_count, next_queue, next_count,
+                                               minb, grid, st);
+    if (minb >= 8) SH(double, 8)
+    else if (minb >= 6) SH(double, 6)
+    else SH(double, 0)
 #undef SH
     return cudaGetLastError();
 }
@@ -636,4 +410,5 @@ void psy_set_magenta(const float xyz[3]) {
     GColor c{PSY_COLOR_XYZ_K, xyz[0], xyz[1], xyz[2]};
     cudaMemcpyToSymbol(c_magenta, &c, sizeof(c));
     psy_upload_trace_constants(nullptr, xyz);
+    psy_upload_wave_f32_constants(nullptr, xyz);
 }

@@ -120,6 +120,25 @@ cudaError_t launch_trace_packet_queue(const GScene &S, RayBuf R, HitBuf H, const
 cudaError_t launch_trace_packet_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order,
                                      PsyHit *hits, int stack, int *d_err, unsigned long long *counters,
                                      cudaStream_t st);
+// The f32 (optimized form) camera and hit-shading kernels, in their own
+// translation unit (wave_f32.cu) compiled with FMA contraction; its copies
+// of the Sobol directions and the unshaded-instance colour are set by
+// psy_upload_wave_f32_constants (null arguments are left alone).
+cudaError_t launch_camera_f32(const GScene &S, const WaveDesc *d_wave, uint32_t max_paths, PathState P, RayBuf R,
+                              uint32_t *queue, uint32_t *count, cudaStream_t st);
+cudaError_t launch_shade_hit_f32(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H,
+                                 const uint32_t *queue, const uint32_t *count, uint32_t max_count,
+                                 uint32_t *next_queue, uint32_t *next_count, int minb, int grid, cudaStream_t st);
+void psy_upload_wave_f32_constants(const uint32_t sobol[8][32], const float magenta[3]);
+// Grid of a wavefront kernel `fn` (128 threads per block) over a device-side
+// queue of at most max_count entries: `grid` > 0 as given, 0 one thread per
+// queue slot, PSY_GRID_RESIDENT (< 0) the blocks of `fn` that are resident
+// on the device at once.  The kernels stride over the queue, so a resident
+// grid covers any count; in the late iterations of a large wave, whose
+// queues hold few paths, it launches a few thousand blocks instead of one
+// per slot of the wave (about a million empty blocks on a 132M-path wave).
+#define PSY_GRID_RESIDENT (-1)
+int queue_grid(const void *fn, int grid, uint32_t max_count);
 // Trace the queued rays of a wave.  fast: the static-scene traversal (1) or
 // its speculative form (2) when the scene allows it (GScene::static_fast)
 // and no counters are requested; minb 6, 8, 10 or 12 there.

@@ -58,8 +58,9 @@ int psy_debug_set_shade(PsyScene *scene, int minb);
 /* Queue binning key width between wavefront iterations: 0, 4, 10, 13, 16,
  * 19, 25 or 31 bits. */
 int psy_debug_set_sort(PsyScene *scene, int bits);
-/* Persistent grid of the wavefront kernels (0: sized by the queue) and the
- * paths per wave (>= 1024 to change it). */
+/* Grid of the wavefront kernels (0: sized by the queue, > 0: that many
+ * blocks striding over the queue, -1: each kernel's resident blocks) and
+ * the paths per wave (>= 1024 to change it). */
 int psy_debug_set_launch(PsyScene *scene, int grid, uint32_t wave_paths);
 /* Replay each wave from a CUDA graph (1) or launch kernel by kernel (0). */
 int psy_debug_set_graph(PsyScene *scene, int on);

@@ -539,15 +539,17 @@ __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, H
 cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32_t *queue, const uint32_t *count,
                                uint32_t max_count, int stack, int minb, int grid, int *d_err,
                                unsigned long long *counters, cudaStream_t st, int fast) {
-    if (grid <= 0) grid = (int)((max_count + 127) / 128);
-    if (grid == 0) return cudaSuccess;
+    if (max_count == 0) return cudaSuccess;
     if (fast && S.static_fast && !counters) {
-#define TF(SZ, MB, SP, HH) \
-    k_trace_queue<SZ, false, MB, true, SP, HH><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, nullptr)
-#define TFS(SZ, SP, HH)                          \
-    if (minb >= 12) TF(SZ, 12, SP, HH);          \
-    else if (minb >= 10) TF(SZ, 10, SP, HH);     \
-    else if (minb >= 8) TF(SZ, 8, SP, HH);       \
+#define TF(SZ, MB, SP, HH)                                                                         \
+    {                                                                                              \
+        int g = queue_grid((const void *)k_trace_queue<SZ, false, MB, true, SP, HH>, grid, max_count); \
+        k_trace_queue<SZ, false, MB, true, SP, HH><<<g, 128, 0, st>>>(S, R, H, queue, count, d_err, nullptr); \
+    }
+#define TFS(SZ, SP, HH)                         \
+    if (minb >= 12) TF(SZ, 12, SP, HH)          \
+    else if (minb >= 10) TF(SZ, 10, SP, HH)     \
+    else if (minb >= 8) TF(SZ, 8, SP, HH)       \
     else TF(SZ, 6, SP, HH)
         if (S.use_fp16) {  // FP16 nodes (the speculative form reads f32 nodes only)
             if (stack <= 64) { TFS(64, false, true); } else { TFS(192, false, true); }
@@ -560,12 +562,16 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
 #undef TF
         return cudaGetLastError();
     }
-#define TQ(SZ, C, MB) k_trace_queue<SZ, C, MB><<<grid, 128, 0, st>>>(S, R, H, queue, count, d_err, counters)
-#define TQS(SZ)                                                   \
-    if (counters) TQ(SZ, true, 4);                                \
-    else if (minb >= 8) TQ(SZ, false, 8);                         \
-    else if (minb >= 6) TQ(SZ, false, 6);                         \
-    else if (minb == 5) TQ(SZ, false, 5);                         \
+#define TQ(SZ, C, MB)                                                                              \
+    {                                                                                              \
+        int g = queue_grid((const void *)k_trace_queue<SZ, C, MB>, grid, max_count);               \
+        k_trace_queue<SZ, C, MB><<<g, 128, 0, st>>>(S, R, H, queue, count, d_err, counters);       \
+    }
+#define TQS(SZ)                                                  \
+    if (counters) TQ(SZ, true, 4)                                \
+    else if (minb >= 8) TQ(SZ, false, 8)                         \
+    else if (minb >= 6) TQ(SZ, false, 6)                         \
+    else if (minb == 5) TQ(SZ, false, 5)                         \
     else TQ(SZ, false, 4)
     if (stack <= 64) { TQS(64); } else { TQS(192); }
 #undef TQS

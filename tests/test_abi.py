@@ -79,3 +79,18 @@ def test_ctypes_layout_matches_header(tmp_path):
         assert int(got[n]) == C.sizeof(T), n
         for f in T._fields_:
             assert int(got["%s.%s" % (n, f[0])]) == getattr(T, f[0]).offset, (n, f[0])
+
+
+def test_ctypes_constants_match_header():
+    """Every integer constant abi.py mirrors has the value the header's
+    #define gives it."""
+    import re
+    from psychopath_gb300 import abi
+    text = open(os.path.join(ROOT, "include", "psy_gpu.h")).read()
+    defs = {m.group(1): int(m.group(2), 0)
+            for m in re.finditer(r"^#define\s+(PSY_\w+)\s+\(?(-?(?:0x[0-9A-Fa-f]+|\d+))[uU]?\)?\s*(?:/\*.*)?$", text, re.M)}
+    mirrored = [n for n in dir(abi) if n.startswith("PSY_") and isinstance(getattr(abi, n), int)]
+    checked = [n for n in mirrored if n in defs]
+    assert len(checked) >= 10
+    for n in checked:
+        assert getattr(abi, n) == defs[n], n

@@ -239,6 +239,27 @@ def test_trace_mode_does_not_change_image(gpu_lib, mode, minb):
         g.close()
 
 
+@pytest.mark.parametrize("grid", [-1, 4, 152])
+def test_wavefront_grid_does_not_change_image(gpu_lib, grid):
+    """Wavefront kernels launched on each kernel's resident blocks (-1) or a
+    small fixed grid (4 blocks: every thread strides over ~48 queue slots)
+    instead of one thread per queue slot, with the general and the
+    static-scene traversal and binned queues: bit-identical image."""
+    s = sc.sphere_small(64, 48, 8, 6, level=3)
+    for shading in ("f64", "f32"):
+        g = gpu.Scene(s, shading=shading)
+        r = gpu.Renderer(g)
+        a, _ = r.render()
+        for mode, minb, bits in ((0, 4, 0), (3, 10, 19)):
+            g.set_trace(mode, minb)
+            g.set_sort(bits)
+            g.set_launch(grid=grid)
+            b, _ = r.render()
+            assert np.array_equal(a, b), (shading, mode, grid)
+            g.set_launch(grid=0)
+        g.close()
+
+
 def test_f32_shading_sphere_lights(gpu_lib):
     """The f32 variant on a motion scene lit by sphere lights (cone sampling
     and its pdf in f32): within 1% relative RMSE of the oracle, and no
