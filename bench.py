@@ -34,6 +34,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 # bytes of one wave descriptor (WaveDesc: 16-byte header + 16 segments of 64
 # bytes), uploaded per wave by every render call
 WAVE_DESC_BYTES = 16 + 16 * 64
+# bytes one FP16 node test reads: anchor and meta 16, extents 8, six planes
+# of four f16 48, child references 16 (the 8-byte pad is not read)
+FP16_NODE_BYTES = 88
 sys.path.insert(0, HERE)
 
 L2_FLUSH_BYTES = 256 << 20
@@ -395,7 +398,7 @@ def run_ours(args):
     # roofline: algorithmic bytes of the traversal kernel (per ray: ray in
     # 32 B + hit out 16 B + 128 B per BVH4 node test + 36 B per triangle
     # test), over the measured traversal-kernel time of the timed frames
-    node_bytes = 64 if args.bounds == "fp16" else 128
+    node_bytes = FP16_NODE_BYTES if args.bounds == "fp16" else 128
     frames = args.steps
     alg_bytes_frame = 48.0 * n_rays_c + node_bytes * n_nodes + 36.0 * n_tris
     achieved = alg_bytes_frame * frames / max(trace_s, 1e-12) / 1e9
@@ -588,7 +591,7 @@ def run_traversal(args, set_names=("coherent", "incoherent"), config_names=None,
     sah_hits = {}
     peaks_path = os.path.join(HERE, "MEASURED_PEAKS.json")
     peak = float(json.load(open(peaks_path))["hbm_gbs"]) if os.path.exists(peaks_path) else 6800.0
-    node_bytes = 64 if args.bounds == "fp16" else 128
+    node_bytes = FP16_NODE_BYTES if args.bounds == "fp16" else 128
     stream = torch.cuda.Stream()  # non-null handle: kernels and events on one stream
     torch.cuda.set_stream(stream)
     configs = [("plain", 0, 4, False), ("minb8", 0, 8, False), ("minb8+binned", 0, 8, True),

@@ -195,10 +195,17 @@ DI float golden_ratio_sample(uint32_t i, uint32_t scramble) {
     uint32_t n = (i + hash_u32(scramble, 0)) * 2654435769u;
     return __uint2float_rn(n) * (1.0f / 4294967296.0f);
 }
-// Sobol direction numbers for 8 dimensions (van der Corput + Joe & Kuo
-// 2..8), filled by the host at library load.  (Only kernels.cu includes the
-// device headers, so the constant banks are defined here.)
-static __constant__ uint32_t c_sobol_dirs[8][32];
+// Sobol generator matrices for 8 dimensions (van der Corput + Joe & Kuo
+// 2..8) as nibble tables, filled by the host at library load (each
+// translation unit that samples has its own copy): entry [dim][p][v] is the
+// XOR of the direction numbers of the set bits of v placed at bits 4p..4p+3
+// of the index.  The Sobol point is the XOR of the direction numbers of the
+// index's set bits (a matrix-vector product over GF(2)), so eight lookups
+// per dimension give the same value as a loop over the index's 32 bits --
+// XOR is associative and commutative -- for an eighth of the instructions.
+// Global memory read through the read-only path: a warp's lookups of one
+// (dim, p) fall in one 64-byte row, one L1 wavefront.
+static __device__ __align__(16) uint32_t g_sobol_nib[8][8][16];
 DI uint32_t laine_karras(uint32_t x, uint32_t seed) {
     x += seed;
     x ^= x * 0x6c50b47cu;
@@ -214,14 +221,10 @@ DI void sobol_burley_4d(uint32_t index, uint32_t set, uint32_t seed, float out[4
 #pragma unroll
     for (uint32_t k = 0; k < 4; k++) {
         uint32_t dim = set * 4 + k;
+        const uint32_t *t = &g_sobol_nib[dim][0][0];
         uint32_t x = 0;
-        uint32_t bits = idx;
-        uint32_t b = 0;
-        while (bits) {
-            if (bits & 1u) x ^= c_sobol_dirs[dim][b];
-            bits >>= 1;
-            b++;
-        }
+#pragma unroll
+        for (uint32_t p = 0; p < 8; p++) x ^= __ldg(t + 16 * p + ((idx >> (4 * p)) & 15u));
         x = nested_uniform_scramble(x, hash_combine(seed, dim));
         out[k] = (float)(x >> 8) * (1.0f / 16777216.0f);
     }

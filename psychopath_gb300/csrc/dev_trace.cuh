@@ -166,9 +166,8 @@ DI float4 dec_plane(uint2 q, float anchor) {
 // boxes are ordered too: lo16 <= lo32 <= hi32 <= hi16).
 DI uint32_t fp16_hits(const GNodeH *n, float4 a, V3 o, V3 di, float tmax, uint32_t oct, bool safe) {
     uint2 e = __ldg(&n->ext);
-    unsigned short ex, ey, ez, ew;
+    unsigned short ex, ey, ez = (unsigned short)(e.y & 0xFFFFu);
     asm("mov.b32 {%0, %1}, %2;" : "=h"(ex), "=h"(ey) : "r"(e.x));
-    asm("mov.b32 {%0, %1}, %2;" : "=h"(ez), "=h"(ew) : "r"(e.y));
     float tx = dec_h(ex, a.x), ty = dec_h(ey, a.y), tz = dec_h(ez, a.z);  // the max corner
     const uint2 *pl = &n->xlo;  // xlo, xhi, ylo, yhi, zlo, zhi
     if (safe) {

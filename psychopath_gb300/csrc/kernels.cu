@@ -87,15 +87,28 @@ void psy_traversal_table_device(uint8_t t[8][48]) {
     traversal_table_host(t);
     extend_traversal_table(t);
 }
-void psy_upload_constants() {
+// The nibble tables of the Sobol generator matrices (see g_sobol_nib).
+static void sobol_nibble_tables(uint32_t nib[8][8][16]) {
     uint32_t d[8][32];
-    uint8_t t[8][48];
     sobol_dirs_host(d);
+    for (int dim = 0; dim < 8; dim++)
+        for (int p = 0; p < 8; p++)
+            for (uint32_t v = 0; v < 16; v++) {
+                uint32_t x = 0;
+                for (int j = 0; j < 4; j++)
+                    if ((v >> j) & 1u) x ^= d[dim][4 * p + j];
+                nib[dim][p][v] = x;
+            }
+}
+void psy_upload_constants() {
+    static uint32_t nib[8][8][16];
+    uint8_t t[8][48];
+    sobol_nibble_tables(nib);
     psy_traversal_table_device(t);
-    cudaMemcpyToSymbol(c_sobol_dirs, d, sizeof(d));
+    cudaMemcpyToSymbol(g_sobol_nib, nib, sizeof(nib));
     cudaMemcpyToSymbol(c_traversal_table, t, sizeof(t));
     psy_upload_trace_constants(t, nullptr);
-    psy_upload_wave_f32_constants(d, nullptr);
+    psy_upload_wave_f32_constants(nib, nullptr);
 }
 
 cudaError_t launch_camera(const GScene &S, const WaveDesc *d_wave, uint32_t max_paths, PathState P, RayBuf R,
@@ -300,7 +313,7 @@ __global__ void k_accumulate(GScene S, const WaveDesc *__restrict__ gwave, PathS
     const WaveSeg &w = wdesc.seg[seg_of_pixel(wdesc, q)];
     uint32_t lq = q - w.pix_begin;
     uint32_t lr = lq / w.w;
-    uint32_t x = w.x0 + (lq - lr * w.w), y = w.y0 + lr * w.ystep;
+    uint32_t x = w.x0 + (lq - lr * w.w);  // the output row is orow0 + lr
     float inv = (float)w.spp;
     V3 acc = v3(0.0f, 0.0f, 0.0f);
     for (uint32_t s = 0; s < w.spp; s++) {

@@ -52,7 +52,7 @@ struct WaveDesc {
     WaveSeg seg[PSY_WAVE_MAX_SEGS];
 };
 
-void psy_upload_constants();  // Sobol directions + traversal table -> __constant__
+void psy_upload_constants();  // Sobol nibble tables, traversal and push tables
 // The traversal table as the device holds it (positions past a node's child
 // count name its empty slots).
 void psy_traversal_table_device(uint8_t t[8][48]);
@@ -122,14 +122,14 @@ cudaError_t launch_trace_packet_rays(const GScene &S, const PsyRay *rays, uint32
                                      cudaStream_t st);
 // The f32 (optimized form) camera and hit-shading kernels, in their own
 // translation unit (wave_f32.cu) compiled with FMA contraction; its copies
-// of the Sobol directions and the unshaded-instance colour are set by
+// of the Sobol nibble tables and the unshaded-instance colour are set by
 // psy_upload_wave_f32_constants (null arguments are left alone).
 cudaError_t launch_camera_f32(const GScene &S, const WaveDesc *d_wave, uint32_t max_paths, PathState P, RayBuf R,
                               uint32_t *queue, uint32_t *count, cudaStream_t st);
 cudaError_t launch_shade_hit_f32(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H,
                                  const uint32_t *queue, const uint32_t *count, uint32_t max_count,
                                  uint32_t *next_queue, uint32_t *next_count, int minb, int grid, cudaStream_t st);
-void psy_upload_wave_f32_constants(const uint32_t sobol[8][32], const float magenta[3]);
+void psy_upload_wave_f32_constants(const uint32_t sobol_nib[8][8][16], const float magenta[3]);
 // Grid of a wavefront kernel `fn` (128 threads per block) over a device-side
 // queue of at most max_count entries: `grid` > 0 as given, 0 one thread per
 // queue slot, PSY_GRID_RESIDENT (< 0) the blocks of `fn` that are resident

@@ -34,9 +34,9 @@ cudaError_t launch_shade_hit_f32(const GScene &S, const WaveDesc *d_wave, PathSt
     return cudaGetLastError();
 }
 
-// This unit's copies of the __constant__ data the camera and shading read.
-void psy_upload_wave_f32_constants(const uint32_t sobol[8][32], const float magenta[3]) {
-    if (sobol) cudaMemcpyToSymbol(c_sobol_dirs, sobol, sizeof(uint32_t) * 8 * 32);
+// This unit's copies of the tables the camera and shading read.
+void psy_upload_wave_f32_constants(const uint32_t sobol_nib[8][8][16], const float magenta[3]) {
+    if (sobol_nib) cudaMemcpyToSymbol(g_sobol_nib, sobol_nib, sizeof(uint32_t) * 8 * 8 * 16);
     if (magenta) {
         GColor c{PSY_COLOR_XYZ_K, magenta[0], magenta[1], magenta[2]};
         cudaMemcpyToSymbol(c_magenta, &c, sizeof(c));

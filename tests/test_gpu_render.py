@@ -272,8 +272,10 @@ def test_f32_shading_sphere_lights(gpu_lib):
     bad_o = ~np.isfinite(ref).all(axis=-1)
     assert not (bad_g & ~bad_o).any()
     ok = ~(bad_g | bad_o)
-    # measured 2.2e-8 (the sphere lights' cone sampling is f32 in both)
-    assert rel_rmse(img[ok], ref[ok]) < 1e-6, rel_rmse(img[ok], ref[ok])
+    # measured 1.1e-6: the f32 shading kernels round a product feeding a sum
+    # once (FMA contraction), the oracle twice (2.2e-8 without contraction);
+    # the sphere lights' cone sampling is f32 in both
+    assert rel_rmse(img[ok], ref[ok]) < 1e-5, rel_rmse(img[ok], ref[ok])
 
 
 def test_speculative_traversal_render(gpu_lib):
