@@ -1218,7 +1218,8 @@ int psy_debug_set_trace(PsyScene *s, int mode, int minb) {
     else s->minb = minb >= 8 ? 8 : (minb >= 6 ? 6 : (minb == 5 ? 5 : 4));
     return PSY_OK;
 }
-// Shading kernel register budget: 4 (compiler's choice), 6 or 8 blocks per SM.
+// Shading kernel register budget: 4 (f32 form: 128 registers; f64 form: the
+// compiler's choice), 6 or 8 blocks per SM.
 int psy_debug_set_shade(PsyScene *s, int minb) {
     if (!s || !(minb == 4 || minb == 6 || minb == 8)) return fail(PSY_E_INVALID, "bad shade budget");
     s->shade_minb = minb;

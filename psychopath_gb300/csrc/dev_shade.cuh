@@ -52,18 +52,23 @@ DI V4 spectrum_xyz_to_p_4(V4 lambdas, float X, float Y, float Z) {
         sb1[k] = t < PSY_MENG_NUM_SAMPLES - 1 ? t : PSY_MENG_NUM_SAMPLES - 1;
     }
     V4 sbf = sb - v4((float)sb0[0], (float)sb0[1], (float)sb0[2], (float)sb0[3]);
-    V4 p[6];
-    for (int i = 0; i < num; i++) {
-        const float *spec = psy_meng_point_spectrum[idx[i]];
+    // the spectrum of cell point k at the four wavelengths (the reference
+    // computes it for every point of the cell first; only the ones combined
+    // below are needed, and each is the same expression)
+    auto point = [&](int k) -> V4 {
+        const float *spec = psy_meng_point_spectrum[idx[k]];
         V4 p0 = v4(spec[sb0[0]], spec[sb0[1]], spec[sb0[2]], spec[sb0[3]]);
         V4 p1 = v4(spec[sb1[0]], spec[sb1[1]], spec[sb1[2]], spec[sb1[3]]);
-        p[i] = p0 * (splat4(1.0f) - sbf) + p1 * sbf;
-    }
+        return p0 * (splat4(1.0f) - sbf) + p1 * sbf;
+    };
     V4 ip = splat4(0.0f);
     if (inside) {
         float u2 = u - (float)ui, v2 = v - (float)vi;
-        ip = p[0] * ((1.0f - u2) * (1.0f - v2)) + p[2] * ((1.0f - u2) * v2) + p[3] * (u2 * v2) + p[1] * (u2 * (1.0f - v2));
+        ip = point(0) * ((1.0f - u2) * (1.0f - v2)) + point(2) * ((1.0f - u2) * v2) + point(3) * (u2 * v2) +
+             point(1) * (u2 * (1.0f - v2));
     } else {
+        // the fan triangle (0, i + 1, i + 2) -- the last one closing on
+        // point 1 -- that holds (u, v); barycentrics from the uv points only
         const float *uv0 = psy_meng_point_uv[idx[0]];
         const float *uv1 = psy_meng_point_uv[idx[1]];
         float ex = u - uv0[0], ey = v - uv0[1];
@@ -89,7 +94,7 @@ DI V4 spectrum_xyz_to_p_4(V4 lambdas, float X, float Y, float Z) {
                 e0y = e1y;
                 continue;
             }
-            ip = p[0] * fw + p[i + 1] * fv + p[(i == num - 2) ? 1 : i + 2] * fu;
+            ip = point(0) * fw + point(i + 1) * fv + point((i == num - 2) ? 1 : i + 2) * fu;
             break;
         }
     }

@@ -196,7 +196,8 @@ cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, R
         int g = queue_grid((const void *)k_shade_hit<RT, MB>, grid, max_count);                              \
         k_shade_hit<RT, MB><<<g, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count);    \
     }
-    // budget 4 = the compiler's own choice (MINB 0 = unspecified)
+    // budget 4: the compiler's own choice in the f64 form (MINB 0 = unspecified,
+    // ~154 registers), at most 128 registers in the f32 form (wave_f32.cu)
     if (prec == 1) return launch_shade_hit_f32(S, d_wave, P, R, H, queue, count, max_count, next_queue, next_count,
                                                minb, grid, st);
     if (minb >= 8) SH(double, 8)

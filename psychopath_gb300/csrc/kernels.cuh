@@ -146,7 +146,8 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
                                uint32_t max_count, int stack, int minb, int grid, int *d_err,
                                unsigned long long *counters, cudaStream_t st, int fast = 0);
 // LightPath::next for the queued paths; live paths go to next_queue.
-// minb: register budget for 4 (compiler's choice), 6 or 8 resident blocks.
+// minb: register budget for 4 (f32 form: at most 128 registers; f64 form: the
+// compiler's choice), 6 or 8 resident blocks.
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
                          const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
                          int minb, int grid, int prec, cudaStream_t st);

@@ -1,8 +1,9 @@
 // Stable LSD radix sort of (key, value) pairs, 8-bit digits.  One pass:
 //   count   per tile of 4096 keys, the count of each digit (shared-memory
 //           histogram) -> counts[digit][tile];
-//   rows    one block per digit: exclusive prefix over the tiles of its row,
-//           the row total -> tot[digit];
+//   rows    one block per digit: exclusive prefix over the tiles of its row
+//           that hold keys (those below the count), the row total ->
+//           tot[digit];
 //   scatter per tile: the digit's base (prefix of tot) + the tile's row
 //           prefix + the key's rank among the tile's equal digits.  Each
 //           warp ranks a contiguous run of the tile's keys (rounds of 32, a
@@ -21,12 +22,13 @@ constexpr int kItems = 16;
 constexpr uint32_t kTile = kThreads * kItems;
 constexpr int kWarps = kThreads / 32;
 
-uint32_t tiles(uint32_t n) { return (n + kTile - 1) / kTile; }
+__host__ __device__ inline uint32_t tiles(uint32_t n) { return (n + kTile - 1) / kTile; }
 
 __global__ void __launch_bounds__(kThreads) k_rs_count(const uint32_t *__restrict__ keys, uint32_t n_host,
                                                        const uint32_t *__restrict__ n_dev, int shift,
                                                        uint32_t *__restrict__ counts, uint32_t ntiles) {
     const uint32_t n = n_dev ? *n_dev : n_host;
+    if (blockIdx.x * kTile >= n) return;  // a tile past the count: no row scan or scatter reads it
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -64,23 +66,25 @@ __device__ __forceinline__ uint32_t block_scan_incl(uint32_t v, uint32_t *warp_s
     return warp ? v + warp_sums[warp - 1] : v;
 }
 
-__global__ void __launch_bounds__(1024) k_rs_rows(uint32_t *__restrict__ counts, uint32_t ntiles,
-                                                  uint32_t *__restrict__ tot) {
+// One block per digit: the exclusive prefix of the digit's row over the
+// tiles in use (those below the count), in chunks of 1024 consecutive
+// entries (coalesced), carrying each chunk's total into the next.
+__global__ void __launch_bounds__(1024) k_rs_rows(uint32_t *__restrict__ counts, uint32_t ntiles, uint32_t n_host,
+                                                  const uint32_t *__restrict__ n_dev, uint32_t *__restrict__ tot) {
     __shared__ uint32_t ws[32];
+    const uint32_t n = n_dev ? *n_dev : n_host;
+    const uint32_t used = min(ntiles, tiles(n));
     uint32_t *row = counts + (size_t)blockIdx.x * ntiles;
-    const uint32_t per = (ntiles + 1023) / 1024, t0 = threadIdx.x * per;
-    uint32_t sum = 0;
-    for (uint32_t k = 0; k < per; k++)
-        if (t0 + k < ntiles) sum += row[t0 + k];
-    uint32_t incl = block_scan_incl<1024>(sum, ws);
-    uint32_t run = incl - sum;
-    for (uint32_t k = 0; k < per; k++) {
-        if (t0 + k >= ntiles) break;
-        uint32_t c = row[t0 + k];
-        row[t0 + k] = run;
-        run += c;
+    uint32_t carry = 0;
+    for (uint32_t c0 = 0; c0 < used; c0 += 1024) {
+        const uint32_t i = c0 + threadIdx.x;
+        const uint32_t v = i < used ? row[i] : 0u;
+        const uint32_t incl = block_scan_incl<1024>(v, ws);
+        if (i < used) row[i] = carry + incl - v;
+        carry += ws[31];  // the scanned warp totals: the last is the chunk's total
+        __syncthreads();  // ws is rewritten by the next chunk's scan
     }
-    if (threadIdx.x == 1023) tot[blockIdx.x] = incl;
+    if (threadIdx.x == 0) tot[blockIdx.x] = carry;
 }
 
 __global__ void __launch_bounds__(kThreads) k_rs_scatter(const uint32_t *__restrict__ keys,
@@ -175,7 +179,7 @@ cudaError_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *keys2, ui
         uint32_t *counts = scratch, *tot = scratch + 256 * (size_t)nt;
         for (int shift = 0; shift < bits; shift += 8) {
             k_rs_count<<<nt, kThreads, 0, st>>>(ka, n, nullptr, shift, counts, nt);
-            k_rs_rows<<<256, 1024, 0, st>>>(counts, nt, tot);
+            k_rs_rows<<<256, 1024, 0, st>>>(counts, nt, n, nullptr, tot);
             k_rs_scatter<<<nt, kThreads, 0, st>>>(ka, va, n, nullptr, shift, counts, nt, tot, kb, vb);
             std::swap(ka, kb);
             std::swap(va, vb);
@@ -194,7 +198,7 @@ cudaError_t radix_sort_pairs_dev(uint32_t *keys, uint32_t *vals, uint32_t *keys2
     uint32_t *counts = scratch, *tot = scratch + 256 * (size_t)nt;
     for (int shift = 0; shift < bits; shift += 8) {
         k_rs_count<<<nt, kThreads, 0, st>>>(ka, 0, d_n, shift, counts, nt);
-        k_rs_rows<<<256, 1024, 0, st>>>(counts, nt, tot);
+        k_rs_rows<<<256, 1024, 0, st>>>(counts, nt, 0, d_n, tot);
         k_rs_scatter<<<nt, kThreads, 0, st>>>(ka, va, 0, d_n, shift, counts, nt, tot, kb, vb);
         std::swap(ka, kb);
         std::swap(va, vb);

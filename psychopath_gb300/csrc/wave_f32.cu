@@ -29,7 +29,7 @@ cudaError_t launch_shade_hit_f32(const GScene &S, const WaveDesc *d_wave, PathSt
     }
     if (minb >= 8) SH(8)
     else if (minb >= 6) SH(6)
-    else SH(0)
+    else SH(4)
 #undef SH
     return cudaGetLastError();
 }

@@ -218,11 +218,12 @@ def test_binned_ray_order_identical(gpu_lib, mode, minb):
     assert np.array_equal(a, b) and np.array_equal(fa, fb)
 
 
-@pytest.mark.parametrize("n", [1, 4095, 4097, 70000, 300001])
+@pytest.mark.parametrize("n", [1, 4095, 4097, 70000, 300001, 4200001])
 def test_ray_order_is_a_stable_sort(gpu_lib, n):
     """The ray order of binned trace calls: a permutation of the rays whose
     keys are non-decreasing, equal keys in their original order (the radix
-    sort is stable); ragged sizes around the 4096-key tile."""
+    sort is stable); ragged sizes around the 4096-key tile, and 1026 tiles
+    (the digit-row scan runs in chunks of 1024 tiles)."""
     sd, P, F = sc.grid_small(64, 32)
     rays = np.concatenate([scenes.incoherent_rays(P, F, n // 2, seed=5), scenes.coherent_rays(256)])[:n]
     if len(rays) < n:
