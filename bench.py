@@ -73,7 +73,8 @@ def parse_args():
                     help="frame workloads: which forms to time (the headline is the optimized one)")
     ap.add_argument("--launch", default="",
                     help="optimized form: fixed launch configuration 'mode,minb[,queue binning bits[,wave paths"
-                         "[,grid]]]' (grid -1: each wavefront kernel's resident blocks) "
+                         "[,grid[,resident tail]]]]' (grid -1: each wavefront kernel's resident blocks; resident "
+                         "tail n: the last n iterations of a wave on resident blocks) "
                          "instead of psy_autotune (profiling a known configuration)")
     return ap.parse_args()
 
@@ -330,11 +331,13 @@ def run_ours(args):
             mode, minb, bits = vals[0], vals[1], (vals[2] if len(vals) > 2 else 0)
             wave = vals[3] if len(vals) > 3 else 1 << 24
             grid = vals[4] if len(vals) > 4 else 0
+            tail = vals[5] if len(vals) > 5 else 0
             scene.set_trace(mode, minb)
             scene.set_sort(bits)
             scene.set_launch(grid, wave)
+            scene.set_resident_tail(tail)
             tune = {"trace_mode": mode, "minb": minb, "wave_paths": wave, "sort_bits": bits, "use_graph": 0,
-                    "grid": grid, "fixed": True}
+                    "grid": grid, "resident_tail": tail, "fixed": True}
         else:
             tune = scene.autotune()
         tune_s = time.perf_counter() - t0

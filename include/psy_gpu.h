@@ -363,7 +363,8 @@ int psy_render_bucket_noalloc(PsyScene *scene, const PsyBucket *bucket, uint32_t
  * 8 blocks per SM), the traversal stack depth (64 or 192 entries, if the
  * scene fits), the queue tile (grid of the wavefront kernels: sized by the
  * queue, a grid-stride grid of 8, 16 or 32 blocks per SM, or each kernel's
- * resident blocks striding over the queue), the key width
+ * resident blocks striding over the queue; then resident blocks for the
+ * last 4, 6, 8 or 10 iterations of a wave only), the key width
  * of the queue binning between wavefront iterations (0 = off, 4 = occlusion
  * flag and direction octant, 10 / 13 / 16 = also 2 / 3 / 4 bits per axis of
  * the origin's cell, 19 / 25 = occlusion flag above a two-point key, radix
@@ -404,6 +405,9 @@ typedef struct PsyTuneResult {
     uint32_t candidates;   /* configurations timed */
     double default_s;      /* probe time of the configuration before tuning */
     double best_s;         /* probe time of the chosen configuration */
+    uint32_t resident_tail; /* the last n wavefront iterations of a wave launch each
+                               kernel on its resident blocks (0: none) */
+    uint32_t reserved;
 } PsyTuneResult;
 
 int psy_autotune(PsyScene *scene, const PsyTuneOptions *opts, PsyTuneResult *result);

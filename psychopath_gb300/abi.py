@@ -146,7 +146,8 @@ class PsyTuneOptions(C.Structure):
 class PsyTuneResult(C.Structure):
     _fields_ = [("trace_mode", C.c_uint32), ("minb", C.c_uint32), ("stack", C.c_uint32), ("grid", C.c_uint32),
                 ("sort_bits", C.c_uint32), ("wave_paths", C.c_uint32), ("use_graph", C.c_uint32),
-                ("shade_minb", C.c_uint32), ("candidates", C.c_uint32), ("default_s", C.c_double), ("best_s", C.c_double)]
+                ("shade_minb", C.c_uint32), ("candidates", C.c_uint32), ("default_s", C.c_double), ("best_s", C.c_double),
+                ("resident_tail", C.c_uint32), ("reserved", C.c_uint32)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}

@@ -393,6 +393,10 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
     uint32_t *qin = B.queue[0], *cin = B.counts;
     for (uint32_t it = 0; it < iters; it++) {
         if (ev) cudaEventRecord(ev[2 + 3 * it], st);
+        // the last resident_tail iterations, whose queues hold few paths,
+        // launch each kernel on its resident blocks (every kernel strides
+        // over its queue, so any grid covers any count)
+        const int grid = (int)it + s->resident_tail >= (int)iters ? PSY_GRID_RESIDENT : s->grid;
         if (s->trace_mode == 5 && s->g.static_fast && !ctr)
             CK(launch_trace_static_refill_queue(s->g, B.R, B.H, qin, cin, n, s->stack, B.work, B.err, st),
                "trace launch");
@@ -400,17 +404,17 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
             CK(launch_trace_persist_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, B.work, B.err, ctr, st),
                "trace launch");
         else if (s->trace_mode == 2)
-            CK(launch_trace_packet_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->grid, B.err, ctr, st),
+            CK(launch_trace_packet_queue(s->g, B.R, B.H, qin, cin, n, s->stack, grid, B.err, ctr, st),
                "trace launch");
         else
-            CK(launch_trace_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, s->grid, B.err, ctr, st,
+            CK(launch_trace_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, grid, B.err, ctr, st,
                                   s->trace_mode >= 3 ? s->trace_mode - 2 : 0),
                "trace launch");
         if (ev) cudaEventRecord(ev[3 + 3 * it], st);
         uint32_t *qout = qin == B.queue[1] ? B.queue[0] : B.queue[1];
         uint32_t *cout = qin == B.queue[1] ? B.counts : B.counts + 1;
         CK(cudaMemsetAsync(cout, 0, 4, st), "memset count");
-        CK(launch_shade(s->g, d_wave, B.P, B.R, B.H, qin, cin, n, qout, cout, s->shade_minb, s->grid, s->prec, st),
+        CK(launch_shade(s->g, d_wave, B.P, B.R, B.H, qin, cin, n, qout, cout, s->shade_minb, grid, s->prec, st),
            "shade launch");
         if (binning && it + 1 < iters) {
             QueueSortBufs Q{B.stage_key, B.bins, nullptr, nullptr, nullptr, nullptr};
@@ -439,7 +443,7 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
 int launch_wave_graph(PsyScene *s, const WaveBufs &B, WaveGraph &G, const WaveDesc *d_wave, uint32_t max_paths,
                       uint32_t max_pix, cudaStream_t st) {
     WaveLaunchKey k{s->trace_mode, s->minb, s->sort_bits, s->prec, s->stack, s->grid, s->shade_minb,
-                    max_paths, max_pix, d_wave, B.P.color};
+                    s->resident_tail, max_paths, max_pix, d_wave, B.P.color};
     if (!G.valid || !(G.key == k)) {
         G.reset();
         cudaStream_t cs = nullptr;
@@ -823,13 +827,15 @@ struct TuneCfg {
     uint32_t wave_paths;
     bool graph;
     int shade_minb;
+    int tail;
 };
 TuneCfg get_cfg(const PsyScene *s) {
-    return {s->trace_mode, s->minb, s->stack, s->grid, s->sort_bits, s->wave_paths, s->use_graph, s->shade_minb};
+    return {s->trace_mode, s->minb, s->stack, s->grid, s->sort_bits, s->wave_paths, s->use_graph, s->shade_minb,
+            s->resident_tail};
 }
 void set_cfg(PsyScene *s, const TuneCfg &c) {
     s->trace_mode = c.trace_mode; s->minb = c.minb; s->stack = c.stack; s->grid = c.grid;
-    s->shade_minb = c.shade_minb;
+    s->shade_minb = c.shade_minb; s->resident_tail = c.tail;
     s->sort_bits = c.sort_bits; s->wave_paths = c.wave_paths;
     if (s->use_graph != c.graph) s->graph.reset();
     s->use_graph = c.graph;
@@ -931,6 +937,16 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
         std::vector<TuneCfg> v;
         for (int k : {0, 8, 16, 32}) { TuneCfg c = cur; c.grid = k * sms; if (c.grid != cur.grid) v.push_back(c); }
         if (cur.grid != PSY_GRID_RESIDENT) { TuneCfg c = cur; c.grid = PSY_GRID_RESIDENT; v.push_back(c); }
+        try_set(v);
+    }
+    // 3b. resident grids for the last iterations of a wave only (their
+    //     queues hold few paths; a grid sized by the wave spends ~0.5 ms per
+    //     launch scheduling blocks that find nothing to do)
+    {
+        const int iters = 2 * (int)s->g.max_bounces + 3;
+        std::vector<TuneCfg> v;
+        for (int k : {4, 6, 8, 10})
+            if (k < iters && k != cur.tail && cur.grid != PSY_GRID_RESIDENT) { TuneCfg c = cur; c.tail = k; v.push_back(c); }
         try_set(v);
     }
     // 4. ray-sort key width
@@ -1054,6 +1070,14 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
                         if (c.grid != best_c.grid) grids.push_back(c);
                     }
                     recheck(grids);
+                    std::vector<TuneCfg> tails;
+                    for (int k : {0, 4, 6, 8, 10}) {
+                        TuneCfg c = best_c;
+                        c.tail = k;
+                        if (k < 2 * (int)s->g.max_bounces + 3 && k != best_c.tail && c.grid != PSY_GRID_RESIDENT)
+                            tails.push_back(c);
+                    }
+                    recheck(tails);
                     for (int b : {10, 13, 16, 19, 25}) {
                         TuneCfg c = best_c;
                         c.sort_bits = b;
@@ -1089,6 +1113,7 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
     res->wave_paths = cur.wave_paths;
     res->use_graph = cur.graph ? 1u : 0u;
     res->shade_minb = (uint32_t)cur.shade_minb;
+    res->resident_tail = (uint32_t)cur.tail;
     res->candidates = ncand;
     res->default_s = default_s;
     res->best_s = best;
@@ -1238,6 +1263,11 @@ int psy_debug_set_launch(PsyScene *s, int grid, uint32_t wave_paths) {
     if (!s) return fail(PSY_E_INVALID, "null");
     s->grid = grid;
     if (wave_paths >= 1024) s->wave_paths = wave_paths;
+    return PSY_OK;
+}
+int psy_debug_set_resident_tail(PsyScene *s, int iterations) {
+    if (!s || iterations < 0) return fail(PSY_E_INVALID, "invalid argument");
+    s->resident_tail = iterations;
     return PSY_OK;
 }
 // Render a whole width x height image with spp samples and seed through the

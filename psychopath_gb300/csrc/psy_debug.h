@@ -62,6 +62,9 @@ int psy_debug_set_sort(PsyScene *scene, int bits);
  * blocks striding over the queue, -1: each kernel's resident blocks) and
  * the paths per wave (>= 1024 to change it). */
 int psy_debug_set_launch(PsyScene *scene, int grid, uint32_t wave_paths);
+/* The last `iterations` wavefront iterations of a wave launch each kernel on
+ * its resident blocks (0: none). */
+int psy_debug_set_resident_tail(PsyScene *scene, int iterations);
 /* Replay each wave from a CUDA graph (1) or launch kernel by kernel (0). */
 int psy_debug_set_graph(PsyScene *scene, int on);
 /* Ray order of trace calls: 0 as given, 1 binned. */

@@ -19,13 +19,13 @@ int psy_cuda_fail(cudaError_t e, const char *what);
 // Launch configuration of the wave sequence; the fields a captured CUDA graph
 // depends on.
 struct WaveLaunchKey {
-    int trace_mode, minb, sort_bits, prec, stack, grid, shade_minb;
+    int trace_mode, minb, sort_bits, prec, stack, grid, shade_minb, tail;
     uint32_t max_paths, max_pix;
     const WaveDesc *d_wave;
     const void *bufs;  // identity of the WaveBufs (its path-state base)
     bool operator==(const WaveLaunchKey &o) const {
         return trace_mode == o.trace_mode && minb == o.minb && sort_bits == o.sort_bits && prec == o.prec &&
-               shade_minb == o.shade_minb &&
+               shade_minb == o.shade_minb && tail == o.tail &&
                stack == o.stack && grid == o.grid && max_paths == o.max_paths && max_pix == o.max_pix &&
                d_wave == o.d_wave && bufs == o.bufs;
     }
@@ -74,7 +74,8 @@ struct PsyScene {
     float *d_xyz = nullptr;
     size_t cap_xyz = 0;
     uint32_t wave_paths = 1u << 24;      // paths per wave
-    int grid = 0;                        // persistent grid for queue kernels (0: size by queue)
+    int grid = 0;                        // grid of the queue kernels (0: size by queue, -1: resident)
+    int resident_tail = 0;               // the last n iterations of a wave launch on resident grids
     bool counting = false;               // accumulate traversal counters during renders
     int trace_mode = 0;                  // 0: one thread per ray, 1: persistent with lane refill, 2: warp packets
     int prec = 0;                        // shading arithmetic: 0 f64 (reference), 1 f32

@@ -61,6 +61,7 @@ def lib(path=None):
     L.psy_debug_mesh_bvh_info.argtypes = [vp, u32, vp, C.POINTER(u32)]
     L.psy_debug_scene_info.argtypes = [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]
     L.psy_debug_set_launch.argtypes = [vp, C.c_int, u32]
+    L.psy_debug_set_resident_tail.argtypes = [vp, C.c_int]
     L.psy_debug_counters.argtypes = [vp, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     L.psy_debug_set_trace.argtypes = [vp, C.c_int, C.c_int]
     L.psy_debug_set_sort.argtypes = [vp, C.c_int]
@@ -262,6 +263,11 @@ class Scene:
 
     def set_launch(self, grid=0, wave_paths=0):
         _check(lib().psy_debug_set_launch(self.h, grid, wave_paths))
+
+    def set_resident_tail(self, iterations):
+        """The last `iterations` wavefront iterations of a wave launch each
+        kernel on its resident blocks (0: none; images unchanged)."""
+        _check(lib().psy_debug_set_resident_tail(self.h, iterations))
 
     def autotune(self, probe_paths=0, repeats=0, max_wave_mib=0):
         """psy_autotune: time a probe render under candidate launch

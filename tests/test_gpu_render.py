@@ -260,6 +260,25 @@ def test_wavefront_grid_does_not_change_image(gpu_lib, grid):
         g.close()
 
 
+@pytest.mark.parametrize("tail", [1, 6, 15])
+def test_resident_tail_does_not_change_image(gpu_lib, tail):
+    """The last `tail` wavefront iterations on resident grids (15 = all of
+    the scene's 2 * 6 + 3 iterations), the rest on grids sized by the wave,
+    with the general and the static-scene traversal: bit-identical image."""
+    s = sc.sphere_small(64, 48, 8, 6, level=3)
+    g = gpu.Scene(s, shading="f32")
+    r = gpu.Renderer(g)
+    a, _ = r.render()
+    for mode, minb, bits in ((0, 4, 0), (3, 10, 19)):
+        g.set_trace(mode, minb)
+        g.set_sort(bits)
+        g.set_resident_tail(tail)
+        b, _ = r.render()
+        assert np.array_equal(a, b), (mode, tail)
+        g.set_resident_tail(0)
+    g.close()
+
+
 def test_f32_shading_sphere_lights(gpu_lib):
     """The f32 variant on a motion scene lit by sphere lights (cone sampling
     and its pdf in f32): within 1% relative RMSE of the oracle, and no
