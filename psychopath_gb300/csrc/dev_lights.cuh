@@ -58,14 +58,21 @@ DI float sphere_sample_pdf(const GScene &S, const GLight &L, const Xf &space, V3
 
 struct LightSample {
     int kind;  // 0 none, 1 distant, 2 surface
-    V4 color;
+    V4 color;  // color_to_spectral(lcol, wl) * s1 * s2
     V3 dir, sp, sn;
     float serr, pdf, sel_pdf;
+    GColor lcol;  // the light's colour at the sample's time
+    float s1, s2;  // its scale factors, applied in this order
 };
 
+// The light samples leave the colour's spectrum to the caller (o.lcol and
+// its scale factors o.s1, o.s2): scene_sample_lights converts it once after
+// its branches, so a warp whose lanes took different lights does not run
+// the spectral upsampling once per branch (the same value: the same
+// function of the same colour, scaled in the same order).
 template <class R>
-DI V4 rect_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr, float u, float v, float wl, float time,
-                  LightSample &o) {
+DI void rect_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr, float u, float v, float time,
+                    LightSample &o) {
     float w = light_dim(S, L, 0, time), h = light_dim(S, L, 1, time);
     GColor col = lerp_slice_color(S.light_colors + L.key_base, L.nkeys, time);
     R sai = (R)1 / ((R)w * (R)h);
@@ -85,7 +92,8 @@ DI V4 rect_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr, flo
         V3 shadow_vec = spt - arr;
         o.pdf = length2(spt - arr) / fabsf(dot(normalized(shadow_vec), normalized(normal))) / (sa1 + sa2);
         o.sp = spt; o.sn = normal; o.serr = 0.0001f;
-        return color_to_spectral(col, wl) * (float)sai * 0.5f;
+        o.lcol = col; o.s1 = (float)sai; o.s2 = 0.5f;
+        return;
     }
     float prob_1 = isinf(a1) ? 1.0f : (isinf(a2) ? 0.0f : a1 / (a1 + a2));
     float prob_2 = 1.0f - prob_1;
@@ -102,12 +110,12 @@ DI V4 rect_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr, flo
     o.sn = normal;
     o.serr = 0.0001f;
     o.pdf = 1.0f / (a1 + a2);
-    return color_to_spectral(col, wl) * (float)sai * 0.5f;
+    o.lcol = col; o.s1 = (float)sai; o.s2 = 0.5f;
 }
 
 template <class R>
-DI V4 sphere_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr_w, float u, float v, float wl, float time,
-                    LightSample &o) {
+DI void sphere_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr_w, float u, float v, float time,
+                      LightSample &o) {
     V3 arr = xf_point(arr_w, space);
     Xf inv = xf_inverse(space);
     R radius = (R)light_dim(S, L, 0, time);
@@ -150,14 +158,15 @@ DI V4 sphere_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr_w,
         o.sp = xf_point(normal * rf, inv);
         o.sn = xf_normal(normal, inv);
         o.pdf = (float)cone_pdf_st2<R>(st2, ct);
-        return color_to_spectral(col, wl) * (float)sai;
+        o.lcol = col; o.s1 = (float)sai; o.s2 = 1.0f;
+        return;
     }
     V3 svec = uniform_sample_sphere(u, v);
     V3 normal = normalized(arr + svec);
     o.sp = xf_point(normal * rf, inv);
     o.sn = xf_normal(normal, inv);
     o.pdf = (float)((R)1 / ((R)4 * pi_r<R>()));
-    return color_to_spectral(col, wl) * (float)sai;
+    o.lcol = col; o.s1 = (float)sai; o.s2 = 1.0f;
 }
 
 DI float bbox_prob(const GScene &S, const GLightTreeNode &nd, float time, V3 pos, const Closure &sc, V3 inc, V3 nor,
@@ -265,27 +274,27 @@ DI LightSample scene_sample_lights(const GScene &S, float n, float u, float v, f
         coordinate_system_from_vector(neg(normalized(direction)), &z, &x3, &y3);
         V3 smp = normalized(uniform_sample_cone<R>(u, v, ctm));
         out.kind = 1;
-        out.color = color_to_spectral(col, wl) * sai_f;
+        out.lcol = col; out.s1 = sai_f; out.s2 = 1.0f;  // x * 1.0f is exact
         out.dir = (x3 * smp.x) + (y3 * smp.y) + (z * smp.z);
         out.pdf = pdf_f;
         out.sel_pdf = p * wl_prob;
-        return out;
+    } else {
+        float nl = (n - wl_prob) / (1.0f - wl_prob);
+        Xf ident = xf_identity();
+        uint32_t li;
+        float sel_pdf;
+        if (!lt_select(S, xf_vector(inc, ident), xf_point(pos, ident), xf_normal(nor, ident), xf_normal(nor_g, ident),
+                       cl, time, nl, &li, &sel_pdf))
+            return out;
+        GInstance inst = S.light_instances[li];
+        Xf xf = instance_xf_at(S, inst, time);
+        const GLight &L = S.lights[inst.obj];
+        if (inst.kind == PSY_INST_RECT) rect_sample<R>(S, L, xf, pos, u, v, time, out);
+        else sphere_sample<R>(S, L, xf, pos, u, v, time, out);
+        out.kind = 2;
+        out.sel_pdf = sel_pdf * (1.0f - wl_prob);
     }
-    float nl = (n - wl_prob) / (1.0f - wl_prob);
-    Xf ident = xf_identity();
-    uint32_t li;
-    float sel_pdf;
-    if (!lt_select(S, xf_vector(inc, ident), xf_point(pos, ident), xf_normal(nor, ident), xf_normal(nor_g, ident), cl,
-                   time, nl, &li, &sel_pdf))
-        return out;
-    GInstance inst = S.light_instances[li];
-    Xf xf = instance_xf_at(S, inst, time);
-    const GLight &L = S.lights[inst.obj];
-    V4 col = (inst.kind == PSY_INST_RECT) ? rect_sample<R>(S, L, xf, pos, u, v, wl, time, out)
-                                          : sphere_sample<R>(S, L, xf, pos, u, v, wl, time, out);
-    out.kind = 2;
-    out.color = col;
-    out.sel_pdf = sel_pdf * (1.0f - wl_prob);
+    out.color = color_to_spectral(out.lcol, wl) * out.s1 * out.s2;
     return out;
 }
 

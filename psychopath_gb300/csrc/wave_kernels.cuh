@@ -188,20 +188,19 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                                                              sd.nor, sd.nor_g, cl);
                     bool found = false;
                     if (li.kind != 0 && !(li.pdf <= 0.0f) && !(li.sel_pdf <= 0.0f)) {
-                        V4 att;
+                        // the direction to the light (a distant light's own,
+                        // else toward the sampled point); the evaluation and
+                        // the shadow ray's origin run once for both kinds, so
+                        // a warp whose lanes sampled different kinds does
+                        // not run them twice
+                        V3 ldir = li.kind == 1 ? li.dir : li.sp - sd.pos;
                         float cpdf;
-                        V3 so, sdir;
-                        float smax;
-                        if (li.kind == 1) {
-                            att = closure_evaluate(cl, cspec, d, li.dir, sd.nor, sd.nor_g, &cpdf);
-                            so = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), li.dir);
-                            sdir = li.dir;
-                            smax = CUDART_INF_F;
-                        } else {
-                            V3 dir = li.sp - sd.pos;
-                            att = closure_evaluate(cl, cspec, d, dir, sd.nor, sd.nor_g, &cpdf);
-                            so = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
-                            V3 oe = robust_ray_origin(li.sp, li.serr, normalized(li.sn), neg(dir));
+                        V4 att = closure_evaluate(cl, cspec, d, ldir, sd.nor, sd.nor_g, &cpdf);
+                        V3 so = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), ldir);
+                        V3 sdir = ldir;
+                        float smax = CUDART_INF_F;
+                        if (li.kind != 1) {
+                            V3 oe = robust_ray_origin(li.sp, li.serr, normalized(li.sn), neg(ldir));
                             sdir = oe - so;
                             smax = 1.0f;
                         }
