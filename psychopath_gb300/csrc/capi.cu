@@ -411,17 +411,36 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
                                   s->trace_mode >= 3 ? s->trace_mode - 2 : 0),
                "trace launch");
         if (ev) cudaEventRecord(ev[3 + 3 * it], st);
+        // the live paths go to the queue and the count this iteration did not
+        // read (the input may be a compacted queue, the binning stage or the
+        // radix sort's second buffer)
         uint32_t *qout = qin == B.queue[1] ? B.queue[0] : B.queue[1];
-        uint32_t *cout = qin == B.queue[1] ? B.counts : B.counts + 1;
+        uint32_t *cout = cin == B.counts + 1 ? B.counts : B.counts + 1;
+        const bool bin_next = binning && it + 1 < iters;
+        // radix-sorted ordering: the shading kernels write each live path's
+        // two-point key beside it (QueueOut), and the sort runs on those
+        QueueOut qo{qout, cout, nullptr, make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f),
+                    0.0f, 0};
+        QueueSortBufs Q{B.stage_key, B.bins, nullptr, nullptr, nullptr, nullptr};
+        if (B.qradix) {
+            Q.keys = B.qradix; Q.keys2 = B.qradix + B.cap; Q.vals2 = B.qradix + 2 * (size_t)B.cap;
+            Q.scratch = B.qradix + 3 * (size_t)B.cap;
+        }
+        const bool radix = bin_next && s->sort_bits > 16;
+        if (radix) {
+            qo.keys = Q.keys;
+            two_point_box(s->g, qo.lo, qo.inv, qo.len);
+            qo.p = (s->sort_bits - 1) / 6;
+        }
         CK(cudaMemsetAsync(cout, 0, 4, st), "memset count");
-        CK(launch_shade(s->g, d_wave, B.P, B.R, B.H, qin, cin, n, qout, cout, s->shade_minb, grid, s->prec, st),
+        CK(launch_shade(s->g, d_wave, B.P, B.R, B.H, qin, cin, n, qo, s->shade_minb, grid, s->prec, st),
            "shade launch");
-        if (binning && it + 1 < iters) {
-            QueueSortBufs Q{B.stage_key, B.bins, nullptr, nullptr, nullptr, nullptr};
-            if (B.qradix) {
-                Q.keys = B.qradix; Q.keys2 = B.qradix + B.cap; Q.vals2 = B.qradix + 2 * (size_t)B.cap;
-                Q.scratch = B.qradix + 3 * (size_t)B.cap;
-            }
+        if (radix) {
+            uint32_t *sorted = nullptr;
+            CK(launch_queue_radix(Q, qout, cout, n, s->sort_bits, &sorted, st), "queue ordering");
+            qin = sorted;
+            cin = cout;
+        } else if (bin_next) {
             CK(launch_queue_binning(s->g, B.R, qout, cout, n, s->sort_bits, Q, B.stage, B.counts + 2, st),
                "queue binning");
             qin = B.stage;

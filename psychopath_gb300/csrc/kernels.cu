@@ -125,15 +125,14 @@ cudaError_t launch_camera(const GScene &S, const WaveDesc *d_wave, uint32_t max_
 // was not occluded, then the next bounce ray if the path has one.
 __global__ void __launch_bounds__(128, 12) k_shade_shadow(PathState P, RayBuf R, HitBuf H,
                                                          const uint32_t *__restrict__ queue,
-                                                         const uint32_t *__restrict__ count, uint32_t *next_queue,
-                                                         uint32_t *next_count) {
+                                                         const uint32_t *__restrict__ count, QueueOut out) {
     uint32_t n = *count;
     if (blockIdx.x * blockDim.x >= n) return;
     uint32_t stride = gridDim.x * blockDim.x;
     uint32_t nloop = (n + stride - 1) / stride * stride;  // keep whole warps in the loop for the ballot
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nloop; q += stride) {
         bool alive = false;
-        uint32_t p = 0;
+        uint32_t p = 0, key = 0;
         uint32_t fl = 0;
         if (q < n) {
             p = queue[q];
@@ -157,10 +156,11 @@ __global__ void __launch_bounds__(128, 12) k_shade_shadow(PathState P, RayBuf R,
                 P.latt[p] = f4(latt);
                 ev = EV_BOUNCE;
                 alive = true;
+                if (out.keys) key = next_ray_key(out, v3(nb), v3(nd), false);
             }
             P.flags[p] = ev | (bounce << 2) | (has_nb << 10) | (nrays << 16) | PSY_SHADED_BIT;
         }
-        push_live(alive, p, next_queue, next_count);
+        push_live(alive, p, key, out);
     }
 }
 
@@ -186,20 +186,19 @@ int queue_grid(const void *fn, int grid, uint32_t max_count) {
 }
 
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
-                         const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
-                         int minb, int grid, int prec, cudaStream_t st) {
+                         const uint32_t *count, uint32_t max_count, const QueueOut &out, int minb, int grid, int prec,
+                         cudaStream_t st) {
     int gs = queue_grid((const void *)k_shade_shadow, grid, max_count);
     if (gs == 0) return cudaSuccess;
-    k_shade_shadow<<<gs, 128, 0, st>>>(P, R, H, queue, count, next_queue, next_count);
+    k_shade_shadow<<<gs, 128, 0, st>>>(P, R, H, queue, count, out);
 #define SH(RT, MB)                                                                                           \
     {                                                                                                        \
         int g = queue_grid((const void *)k_shade_hit<RT, MB>, grid, max_count);                              \
-        k_shade_hit<RT, MB><<<g, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count);    \
+        k_shade_hit<RT, MB><<<g, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, out);                       \
     }
     // budget 4: the compiler's own choice in the f64 form (MINB 0 = unspecified,
     // ~154 registers), at most 128 registers in the f32 form (wave_f32.cu)
-    if (prec == 1) return launch_shade_hit_f32(S, d_wave, P, R, H, queue, count, max_count, next_queue, next_count,
-                                               minb, grid, st);
+    if (prec == 1) return launch_shade_hit_f32(S, d_wave, P, R, H, queue, count, max_count, out, minb, grid, st);
     if (minb >= 8) SH(double, 8)
     else if (minb >= 6) SH(double, 6)
     else SH(double, 0)
@@ -214,8 +213,9 @@ cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, R
 // origin's cell (k bits per axis of the scene box), `bits` = 4 + 3k bits in
 // all.  A counting sort (order inside a bin arbitrary); paths are
 // independent, so the image does not change.  Wider keys (19, 25, 31 bits)
-// use the two-point key of the trace calls' ray order and a stable radix
-// sort (radix_sort.cu).
+// use the two-point key of the trace calls' ray order, computed by the
+// shading kernels as they write each live path's next ray (QueueOut), and a
+// stable radix sort (radix_sort.cu).
 __device__ __forceinline__ uint32_t queue_key(const GScene &S, float4 o, float4 d, bool occl, int bits) {
     uint32_t key = (occl ? 1u : 0u) | (ray_code(v3(d)) << 1);
     int per = (bits - 4) / 3;
@@ -259,40 +259,21 @@ __global__ void k_queue_scatter(const uint32_t *__restrict__ queue, const uint32
     }
 }
 
-// Two-point keys (occlusion flag above a 6p-bit key) and the path indices.
-__global__ void k_queue_tp_keys(RayBuf R, const uint32_t *__restrict__ queue, const uint32_t *__restrict__ count,
-                                float4 lo, float4 inv, float len, int p, uint32_t *__restrict__ keys,
-                                uint32_t *__restrict__ vals) {
-    uint32_t n = *count;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        uint32_t path = queue[q];
-        float4 o = R.o[path], d = R.d[path];
-        uint32_t key = two_point_key(o.x, o.y, o.z, d.x, d.y, d.z, lo, inv, len, p);
-        keys[q] = key | ((R.occl[path] != 0 ? 1u : 0u) << (6 * p));
-        vals[q] = path;
-    }
-}
-
 size_t queue_radix_words(uint32_t n) { return 3 * (size_t)n + radix_sort_scratch_words(n); }
+
+cudaError_t launch_queue_radix(const QueueSortBufs &Q, uint32_t *vals, const uint32_t *count, uint32_t max_count,
+                               int bits, uint32_t **sorted, cudaStream_t st) {
+    const int passes = (bits + 7) / 8;  // each pass moves (keys, vals) to the other buffer pair
+    *sorted = (passes & 1) ? Q.vals2 : vals;
+    return radix_sort_pairs_dev(Q.keys, vals, Q.keys2, Q.vals2, Q.scratch, count, max_count, bits, st);
+}
 
 cudaError_t launch_queue_binning(const GScene &S, RayBuf R, const uint32_t *queue, const uint32_t *count,
                                  uint32_t max_count, int bits, const QueueSortBufs &Q, uint32_t *out,
                                  uint32_t *out_count, cudaStream_t st) {
     int g = (int)std::min<uint32_t>((max_count + 255) / 256, 152u * 16u);
     if (g < 1) g = 1;
-    if (bits > 16) {
-        // the radix passes alternate buffers: start where the last pass
-        // lands in `out`
-        const int p = (bits - 1) / 6, passes = (bits + 7) / 8;
-        uint32_t *vals = (passes & 1) ? Q.vals2 : out, *vals2 = (passes & 1) ? out : Q.vals2;
-        float4 lo, inv;
-        float len;
-        two_point_box(S, lo, inv, len);
-        k_queue_tp_keys<<<g, 256, 0, st>>>(R, queue, count, lo, inv, len, p, Q.keys, vals);
-        cudaError_t e = radix_sort_pairs_dev(Q.keys, vals, Q.keys2, vals2, Q.scratch, count, max_count, bits, st);
-        if (e != cudaSuccess) return e;
-        return cudaMemcpyAsync(out_count, count, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
-    }
+    if (bits > 16) return cudaErrorInvalidValue;  // radix-sorted keys come from the shading kernels
     uint32_t nbins = 1u << bits;
     cudaError_t e = cudaMemsetAsync(Q.bins, 0, nbins * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;

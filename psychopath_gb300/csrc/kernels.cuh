@@ -120,6 +120,19 @@ cudaError_t launch_trace_packet_queue(const GScene &S, RayBuf R, HitBuf H, const
 cudaError_t launch_trace_packet_rays(const GScene &S, const PsyRay *rays, uint32_t n, const uint32_t *order,
                                      PsyHit *hits, int stack, int *d_err, unsigned long long *counters,
                                      cudaStream_t st);
+// Where the shading kernels put the live paths: the queue and its count,
+// and -- when the next queue is ordered by two-point key (the radix-sorted
+// binning) -- each entry's sort key beside it (keys != nullptr): the key of
+// the path's next ray with the occlusion flag above it, computed where the
+// ray is written instead of by a pass that reads every queued ray again.
+// lo, inv, len: the key box (two_point_box); p: bits per coordinate.
+struct QueueOut {
+    uint32_t *queue, *count;
+    uint32_t *keys;
+    float4 lo, inv;
+    float len;
+    int p;
+};
 // The f32 (optimized form) camera and hit-shading kernels, in their own
 // translation unit (wave_f32.cu) compiled with FMA contraction; its copies
 // of the Sobol nibble tables and the unshaded-instance colour are set by
@@ -128,7 +141,7 @@ cudaError_t launch_camera_f32(const GScene &S, const WaveDesc *d_wave, uint32_t 
                               uint32_t *queue, uint32_t *count, cudaStream_t st);
 cudaError_t launch_shade_hit_f32(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H,
                                  const uint32_t *queue, const uint32_t *count, uint32_t max_count,
-                                 uint32_t *next_queue, uint32_t *next_count, int minb, int grid, cudaStream_t st);
+                                 const QueueOut &out, int minb, int grid, cudaStream_t st);
 void psy_upload_wave_f32_constants(const uint32_t sobol_nib[8][8][16], const float magenta[3]);
 // Grid of a wavefront kernel `fn` (128 threads per block) over a device-side
 // queue of at most max_count entries: `grid` > 0 as given, 0 one thread per
@@ -149,8 +162,8 @@ cudaError_t launch_trace_queue(const GScene &S, RayBuf R, HitBuf H, const uint32
 // minb: register budget for 4 (f32 form: at most 128 registers; f64 form: the
 // compiler's choice), 6 or 8 resident blocks.
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,
-                         const uint32_t *count, uint32_t max_count, uint32_t *next_queue, uint32_t *next_count,
-                         int minb, int grid, int prec, cudaStream_t st);
+                         const uint32_t *count, uint32_t max_count, const QueueOut &out, int minb, int grid, int prec,
+                         cudaStream_t st);
 // Scratch of the queue ordering: u16 keys and 2^16 counters (bins) for the
 // counting sort, u32 keys / second buffers / radix scratch for the radix
 // sort (null when absent).
@@ -160,13 +173,21 @@ struct QueueSortBufs {
     uint32_t *keys, *keys2, *vals2, *scratch;
 };
 // Groups the live paths of queue[0 .. *count) by their next ray into
-// out[0 .. n) and sets *out_count = n.  bits 4, 10, 13, 16: counting sort by
-// occlusion flag, direction octant, origin cell (bits = 4 + 3k); bits 19,
-// 25, 31: stable radix sort by occlusion flag above a two-point key of
-// (bits - 1) / 6 bits per coordinate.
+// out[0 .. n) and sets *out_count = n: a counting sort by occlusion flag,
+// direction octant and origin cell, bits 4, 10, 13 or 16 (= 4 + 3k).  Wider
+// keys (19, 25, 31: the occlusion flag above a two-point key of
+// (bits - 1) / 6 bits per coordinate) are written by the shading kernels
+// and radix-sorted by launch_queue_radix.
 cudaError_t launch_queue_binning(const GScene &S, RayBuf R, const uint32_t *queue, const uint32_t *count,
                                  uint32_t max_count, int bits, const QueueSortBufs &Q, uint32_t *out,
                                  uint32_t *out_count, cudaStream_t st);
+// The radix-sorted binning of a queue whose keys the shading kernels wrote
+// (QueueOut::keys = Q.keys, QueueOut::queue = vals, count = the queue's
+// count): a stable radix sort of (Q.keys, vals) by `bits` bits; *sorted is
+// the buffer holding the sorted paths (vals or Q.vals2, by the number of
+// passes).
+cudaError_t launch_queue_radix(const QueueSortBufs &Q, uint32_t *vals, const uint32_t *count, uint32_t max_count,
+                               int bits, uint32_t **sorted, cudaStream_t st);
 // Words of QueueSortBufs' radix part (keys, keys2, vals2, scratch) for n paths.
 size_t queue_radix_words(uint32_t n);
 // All device buffers one render wave needs (owned by a scene, or carved from

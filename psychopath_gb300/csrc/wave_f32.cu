@@ -20,12 +20,12 @@ cudaError_t launch_camera_f32(const GScene &S, const WaveDesc *d_wave, uint32_t 
 
 cudaError_t launch_shade_hit_f32(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H,
                                  const uint32_t *queue, const uint32_t *count, uint32_t max_count,
-                                 uint32_t *next_queue, uint32_t *next_count, int minb, int grid, cudaStream_t st) {
+                                 const QueueOut &out, int minb, int grid, cudaStream_t st) {
 #define SH(MB)                                                                                               \
     {                                                                                                        \
         int g = queue_grid((const void *)k_shade_hit<float, MB>, grid, max_count);                           \
         if (g > 0)                                                                                           \
-            k_shade_hit<float, MB><<<g, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, next_queue, next_count); \
+            k_shade_hit<float, MB><<<g, 128, 0, st>>>(S, d_wave, P, R, H, queue, count, out);                 \
     }
     if (minb >= 8) SH(8)
     else if (minb >= 6) SH(6)

@@ -93,15 +93,26 @@ __global__ void k_camera(GScene S, const WaveDesc *__restrict__ gwave, PathState
 #define EV_BOUNCE 1u
 #define EV_SHADOW 2u
 
-__device__ __forceinline__ void push_live(bool alive, uint32_t p, uint32_t *next_queue, uint32_t *next_count) {
+// Appends the live paths of the warp to out.queue (one atomic per warp),
+// with their sort keys when out.keys is set.
+__device__ __forceinline__ void push_live(bool alive, uint32_t p, uint32_t key, const QueueOut &out) {
     unsigned mask = __ballot_sync(__activemask(), alive);
     if (mask == 0) return;
     int lane = threadIdx.x & 31;
     int leader = __ffs(mask) - 1;
     uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(next_count, (uint32_t)__popc(mask));
+    if (lane == leader) base = atomicAdd(out.count, (uint32_t)__popc(mask));
     base = __shfl_sync(__activemask(), base, leader);
-    if (alive) next_queue[base + __popc(mask & ((1u << lane) - 1u))] = p;
+    if (alive) {
+        uint32_t i = base + __popc(mask & ((1u << lane) - 1u));
+        out.queue[i] = p;
+        if (out.keys) out.keys[i] = key;
+    }
+}
+// The sort key of a path's next ray (two-point key, occlusion flag above).
+__device__ __forceinline__ uint32_t next_ray_key(const QueueOut &out, V3 o, V3 d, bool occl) {
+    return two_point_key(o.x, o.y, o.z, d.x, d.y, d.z, out.lo, out.inv, out.len, out.p) |
+           ((occl ? 1u : 0u) << (6 * out.p));
 }
 
 // LightPath::next (src/renderer.rs:449-691), in two kernels over the same
@@ -120,8 +131,7 @@ __device__ __forceinline__ void push_live(bool alive, uint32_t p, uint32_t *next
 template <class RT, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDesc *__restrict__ gwave, PathState P,
                                                    RayBuf R, HitBuf H, const uint32_t *__restrict__ queue,
-                                                   const uint32_t *__restrict__ count, uint32_t *next_queue,
-                                                   uint32_t *next_count) {
+                                                   const uint32_t *__restrict__ count, QueueOut out) {
     __shared__ WaveDesc wdesc;
     uint32_t n = *count;
     // blocks past the queue's length (the grid covers the wave's capacity)
@@ -132,7 +142,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
     uint32_t nloop = (n + stride - 1) / stride * stride;  // keep whole warps in the loop for the ballot
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nloop; q += stride) {
         bool alive = false;
-        uint32_t p = 0;
+        uint32_t p = 0, key = 0;
         uint32_t fl = 0;
         if (q < n) {
             p = queue[q];
@@ -212,6 +222,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                             R.d[p] = make_float4(sdir.x, sdir.y, sdir.z, time);
                             R.occl[p] = 1;
                             found = true;
+                            if (out.keys) key = next_ray_key(out, so, sdir, true);
                         }
                     }
                     bool do_bounce = false;
@@ -248,6 +259,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                         ev = EV_BOUNCE;
                         latt = latt * nafac;
                         alive = true;
+                        if (out.keys) key = next_ray_key(out, v3(nb), v3(nd), false);
                     }
                     P.latt[p] = f4(latt);
                     P.seed[p] = seed;
@@ -259,6 +271,6 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
             }
             P.flags[p] = ev | (bounce << 2) | (has_nb << 10) | (nrays << 16);
         }
-        push_live(alive, p, next_queue, next_count);
+        push_live(alive, p, key, out);
     }
 }
