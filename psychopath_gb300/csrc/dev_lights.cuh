@@ -25,11 +25,15 @@ DI void rect_corners(float w, float h, const Xf &si, V3 *p1, V3 *p2, V3 *p3, V3 
     *p3 = xf_point(v3(w * -0.5f, h * -0.5f, 0.0f), si);
     *p4 = xf_point(v3(w * 0.5f, h * -0.5f, 0.0f), si);
 }
-// RectangleLight::sample_pdf
+// The inverse of a light instance's space at `time`: precomputed by the
+// host for a single-key transform (the same f32 formula as xf_inverse).
+DI Xf light_inverse(const GScene &S, const GInstance &in, const Xf &space) {
+    return in.xc == 1 ? xf_load(S.xforms_inv + 3 * in.xinv) : xf_inverse(space);
+}
+// RectangleLight::sample_pdf; si: the inverse of the light's space
 template <class R>
-DI float rect_sample_pdf(const GScene &S, const GLight &L, const Xf &space, V3 arr, V3 sample_dir, V3 hit, float time) {
+DI float rect_sample_pdf(const GScene &S, const GLight &L, const Xf &si, V3 arr, V3 sample_dir, V3 hit, float time) {
     float w = light_dim(S, L, 0, time), h = light_dim(S, L, 1, time);
-    Xf si = xf_inverse(space);
     V3 p1, p2, p3, p4;
     rect_corners(w, h, si, &p1, &p2, &p3, &p4);
     V3 sp1 = normalized(p1 - arr), sp2 = normalized(p2 - arr), sp3 = normalized(p3 - arr), sp4 = normalized(p4 - arr);
@@ -69,14 +73,14 @@ struct LightSample {
 // its scale factors o.s1, o.s2): scene_sample_lights converts it once after
 // its branches, so a warp whose lanes took different lights does not run
 // the spectral upsampling once per branch (the same value: the same
-// function of the same colour, scaled in the same order).
+// function of the same colour, scaled in the same order).  `si` is the
+// inverse of the light's space.
 template <class R>
-DI void rect_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr, float u, float v, float time,
-                    LightSample &o) {
+DI void rect_sample(const GScene &S, const GLight &L, const Xf &space, const Xf &si, V3 arr, float u, float v,
+                    float time, LightSample &o) {
     float w = light_dim(S, L, 0, time), h = light_dim(S, L, 1, time);
     GColor col = lerp_slice_color(S.light_colors + L.key_base, L.nkeys, time);
     R sai = (R)1 / ((R)w * (R)h);
-    Xf si = xf_inverse(space);
     V3 p1, p2, p3, p4;
     rect_corners(w, h, si, &p1, &p2, &p3, &p4);
     V3 sp1 = normalized(p1 - arr), sp2 = normalized(p2 - arr), sp3 = normalized(p3 - arr), sp4 = normalized(p4 - arr);
@@ -114,10 +118,9 @@ DI void rect_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr, f
 }
 
 template <class R>
-DI void sphere_sample(const GScene &S, const GLight &L, const Xf &space, V3 arr_w, float u, float v, float time,
-                      LightSample &o) {
+DI void sphere_sample(const GScene &S, const GLight &L, const Xf &space, const Xf &inv, V3 arr_w, float u, float v,
+                      float time, LightSample &o) {
     V3 arr = xf_point(arr_w, space);
-    Xf inv = xf_inverse(space);
     R radius = (R)light_dim(S, L, 0, time);
     GColor col = lerp_slice_color(S.light_colors + L.key_base, L.nkeys, time);
     R sai = (R)1 / ((R)4 * pi_r<R>() * radius * radius);
@@ -288,9 +291,10 @@ DI LightSample scene_sample_lights(const GScene &S, float n, float u, float v, f
             return out;
         GInstance inst = S.light_instances[li];
         Xf xf = instance_xf_at(S, inst, time);
+        Xf xinv = light_inverse(S, inst, xf);
         const GLight &L = S.lights[inst.obj];
-        if (inst.kind == PSY_INST_RECT) rect_sample<R>(S, L, xf, pos, u, v, time, out);
-        else sphere_sample<R>(S, L, xf, pos, u, v, time, out);
+        if (inst.kind == PSY_INST_RECT) rect_sample<R>(S, L, xf, xinv, pos, u, v, time, out);
+        else sphere_sample<R>(S, L, xf, xinv, pos, u, v, time, out);
         out.kind = 2;
         out.sel_pdf = sel_pdf * (1.0f - wl_prob);
     }

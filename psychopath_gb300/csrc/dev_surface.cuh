@@ -64,7 +64,7 @@ __device__ void resolve_hit(const GScene &S, const HitRec &h, V3 o, V3 d, float 
     GColor col = lerp_slice_color(S.light_colors + L.key_base, L.nkeys, time);
     if (in.kind == PSY_INST_RECT) {
         float w = light_dim(S, L, 0, time), hh = light_dim(S, L, 1, time);
-        Xf si = xf_inverse(xf);
+        Xf si = light_inverse(S, in, xf);
         V3 p1, p2, p3, p4;
         rect_corners(w, hh, si, &p1, &p2, &p3, &p4);
         V3 a = h.prim == 0 ? p1 : p3, b = h.prim == 0 ? p2 : p4, c = h.prim == 0 ? p3 : p1;
@@ -72,12 +72,12 @@ __device__ void resolve_hit(const GScene &S, const HitRec &h, V3 o, V3 d, float 
         V3 nn = cross(a - b, a - c);
         sd.nor = nn;
         sd.nor_g = nn;
-        sd.sample_pdf = rect_sample_pdf<R>(S, L, xf, o, d, sd.pos, time);
+        sd.sample_pdf = rect_sample_pdf<R>(S, L, si, o, d, sd.pos, time);
         float isa = (float)(1.0 / ((double)w * (double)hh));
         sd.closure.color = color_mul(col, isa);
     } else {
         float radius = light_dim(S, L, 0, time);
-        Xf ixf = xf_inverse(xf);
+        Xf ixf = light_inverse(S, in, xf);
         V3 ol = in.xc ? xf_point(o, xf) : xf_point(o, xf_identity());
         V3 dir = xf_vector(d, xf);
         V3 unit = normalized(ol + (dir * h.t));

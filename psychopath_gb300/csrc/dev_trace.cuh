@@ -246,8 +246,7 @@ DI bool rect_hit(const GScene &S, const GInstance &in, V3 o, V3 d, float tmax, f
                  float &b1, float &b2, uint32_t &which) {
     const GLight L = S.lights[in.obj];
     float w = light_dim(S, L, 0, time), h = light_dim(S, L, 1, time);
-    Xf xf = instance_xf_at(S, in, time);
-    Xf si = xf_inverse(xf);
+    Xf si = light_inverse(S, in, instance_xf_at(S, in, time));
     V3 p1, p2, p3, p4;
     rect_corners(w, h, si, &p1, &p2, &p3, &p4);
     TriPre pre = tri_precompute(d);
@@ -313,7 +312,7 @@ DI uint32_t sel4(const uint4 &c, uint32_t i) {
 DI void rect_tri(const GScene &S, const GInstance &in, float time, uint32_t which, V3 &a, V3 &b, V3 &c) {
     const GLight L = S.lights[in.obj];
     float w = light_dim(S, L, 0, time), h = light_dim(S, L, 1, time);
-    Xf si = xf_inverse(instance_xf_at(S, in, time));
+    Xf si = light_inverse(S, in, instance_xf_at(S, in, time));
     V3 p1, p2, p3, p4;
     rect_corners(w, h, si, &p1, &p2, &p3, &p4);
     if (which == 0) { a = p1; b = p2; c = p3; }
