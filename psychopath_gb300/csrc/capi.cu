@@ -395,8 +395,12 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
         if (ev) cudaEventRecord(ev[2 + 3 * it], st);
         // the last resident_tail iterations, whose queues hold few paths,
         // launch each kernel on its resident blocks (every kernel strides
-        // over its queue, so any grid covers any count)
-        const int grid = (int)it + s->resident_tail >= (int)iters ? PSY_GRID_RESIDENT : s->grid;
+        // over its queue, so any grid covers any count); the traversal gets
+        // four rounds of them, so the block scheduler still balances the
+        // rays' uneven cost while the tail's first queues are large
+        const bool tail = (int)it + s->resident_tail >= (int)iters;
+        const int grid = tail ? PSY_GRID_RESIDENT : s->grid;
+        const int tgrid = tail ? 4 * PSY_GRID_RESIDENT : s->grid;
         if (s->trace_mode == 5 && s->g.static_fast && !ctr)
             CK(launch_trace_static_refill_queue(s->g, B.R, B.H, qin, cin, n, s->stack, B.work, B.err, st),
                "trace launch");
@@ -404,10 +408,10 @@ int launch_wave(PsyScene *s, const WaveBufs &B, const WaveDesc *d_wave, uint32_t
             CK(launch_trace_persist_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, B.work, B.err, ctr, st),
                "trace launch");
         else if (s->trace_mode == 2)
-            CK(launch_trace_packet_queue(s->g, B.R, B.H, qin, cin, n, s->stack, grid, B.err, ctr, st),
+            CK(launch_trace_packet_queue(s->g, B.R, B.H, qin, cin, n, s->stack, tgrid, B.err, ctr, st),
                "trace launch");
         else
-            CK(launch_trace_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, grid, B.err, ctr, st,
+            CK(launch_trace_queue(s->g, B.R, B.H, qin, cin, n, s->stack, s->minb, tgrid, B.err, ctr, st,
                                   s->trace_mode >= 3 ? s->trace_mode - 2 : 0),
                "trace launch");
         if (ev) cudaEventRecord(ev[3 + 3 * it], st);

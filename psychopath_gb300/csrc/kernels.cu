@@ -168,6 +168,7 @@ int queue_grid(const void *fn, int grid, uint32_t max_count) {
     int need = (int)((max_count + 127) / 128);
     if (grid > 0 || need == 0) return grid > 0 ? grid : 0;
     if (grid == 0) return need;
+    const int rounds = -grid;  // -k: k rounds of the resident blocks
     // resident blocks of fn: SMs x blocks per SM at 128 threads, cached per
     // kernel and device (the query is a driver call)
     static std::mutex mu;
@@ -182,7 +183,7 @@ int queue_grid(const void *fn, int grid, uint32_t max_count) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 128, 0);
         it = cache.emplace(std::make_pair(fn, dev), std::max(1, sms) * std::max(1, per)).first;
     }
-    return std::min(need, it->second);
+    return (int)std::min<int64_t>(need, (int64_t)rounds * it->second);
 }
 
 cudaError_t launch_shade(const GScene &S, const WaveDesc *d_wave, PathState P, RayBuf R, HitBuf H, const uint32_t *queue,

@@ -145,11 +145,12 @@ cudaError_t launch_shade_hit_f32(const GScene &S, const WaveDesc *d_wave, PathSt
 void psy_upload_wave_f32_constants(const uint32_t sobol_nib[8][8][16], const float magenta[3]);
 // Grid of a wavefront kernel `fn` (128 threads per block) over a device-side
 // queue of at most max_count entries: `grid` > 0 as given, 0 one thread per
-// queue slot, PSY_GRID_RESIDENT (< 0) the blocks of `fn` that are resident
-// on the device at once.  The kernels stride over the queue, so a resident
-// grid covers any count; in the late iterations of a large wave, whose
-// queues hold few paths, it launches a few thousand blocks instead of one
-// per slot of the wave (about a million empty blocks on a 132M-path wave).
+// queue slot, PSY_GRID_RESIDENT (-1) the blocks of `fn` that are resident
+// on the device at once, -k k rounds of them.  The kernels stride over the
+// queue, so any grid covers any count; in the late iterations of a large
+// wave, whose queues hold few paths, a resident grid launches a few
+// thousand blocks instead of one per slot of the wave (about a million
+// empty blocks on a 132M-path wave).
 #define PSY_GRID_RESIDENT (-1)
 int queue_grid(const void *fn, int grid, uint32_t max_count);
 // Trace the queued rays of a wave.  fast: the static-scene traversal (1) or
