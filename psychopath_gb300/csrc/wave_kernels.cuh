@@ -73,12 +73,12 @@ __global__ void k_camera(GScene S, const WaveDesc *__restrict__ gwave, PathState
     V3 orig = v3(ar * cu, ar * cv, 0.0f);
     V3 dir = normalized(v3((ix * tfov) - (orig.x / fd), (iy * tfov) - (orig.y / fd), 1.0f));
     V3 wo = xf_point(orig, xf), wd = xf_vector(dir, xf);
+    // The path's colour starts at 0 (the pixel sum reads it whatever the
+    // path does).  Its light attenuation (1), closure-sample pdf (1),
+    // pending light, next attenuation and next bounce ray are not stored:
+    // k_shade_hit takes the first two as constants for a camera event and
+    // writes the others before anything reads them.
     P.color[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    P.latt[p] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-    P.pending[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    P.nafac[p] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-    P.nb_o[p] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);  // w: closure_sample_pdf = 1
-    P.nb_d[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     P.tw[p] = make_float2(time, wl);
     P.seed[p] = w.seed ^ 0x40d4682bu;
     P.flags[p] = 0u;  // EV_CAMERA, bounce 0, no next bounce, 0 rays
@@ -156,14 +156,17 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
             float2 tw = P.tw[p];
             float time = tw.x, wl = tw.y;
             uint4 ki = H.ki[p];
-            V4 color = v4(P.color[p]);
-            V4 latt = v4(P.latt[p]);
+            // colour, light attenuation and closure-sample pdf: a camera
+            // event's are the path's initial 0, 1 and 1 (k_camera stores the
+            // colour only)
+            const bool cam = ev == EV_CAMERA;
+            V4 color = cam ? splat4(0.0f) : v4(P.color[p]);
+            V4 latt = cam ? splat4(1.0f) : v4(P.latt[p]);
+            float csp = cam ? 1.0f : P.nb_o[p].w;
             // the hit's barycentrics, the ray and the sampling state
             float4 tb = H.tb[p];
             float4 ro = R.o[p], rd = R.d[p];
             V3 o = v3(ro), d = v3(rd);
-            float4 nbo = P.nb_o[p];
-            float csp = nbo.w;  // closure_sample_pdf
             uint32_t seed = P.seed[p];
             const WaveSeg &w = wdesc.seg[seg_of_path(wdesc, p)];
             uint32_t lp = p - w.path_begin;
@@ -226,7 +229,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                         }
                     }
                     bool do_bounce = false;
-                    V4 nafac = v4(P.nafac[p]);
+                    V4 nafac = splat4(1.0f);  // set with the bounce, read only then
                     if (bounce < S.max_bounces) {
                         bounce += 1;
                         seed += 1;
