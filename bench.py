@@ -375,8 +375,9 @@ def run_ours(args):
     value = samples_all / elapsed
     plain_value = p_samples_all / p_el if p_samples else None
 
-    # end to end through the public C ABI with a host image buffer
-    img = np.zeros((H, W, 3), dtype=np.float32)
+    # end to end through the public C ABI with a host image buffer (pinned,
+    # as a caller streaming frames off the device would allocate it)
+    img = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True).numpy()
     barrier()
     torch.cuda.synchronize()
     e0 = time.perf_counter()
@@ -385,7 +386,7 @@ def run_ours(args):
             rend.render_rows_device(rank, world, xyz.data_ptr(), stream=stream.cuda_stream)
             img = multi.gather_rows(xyz[: n_rows * W * 3].view(n_rows, W, 3), H, rank, world).cpu().numpy()
         else:
-            img, _ = rend.render()
+            img, _ = rend.render(out=img)
     e_el = time.perf_counter() - e0
     te = torch.tensor([e_el], device="cuda")
     if world > 1:
@@ -449,7 +450,7 @@ def run_ours(args):
         "nonfinite_pixels": nonfinite,
         "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": waves * WAVE_DESC_BYTES,
                 "d2h_bytes_per_step": W * H * 3 * 4 + 8,
-                "note": "psy_render_image with a host XYZ buffer and render statistics: per step the wave "
+                "note": "psy_render_image with a pinned host XYZ buffer and render statistics: per step the wave "
                         "descriptors go up (%d B each) and the image and the ray count (8 B) come back, inside the "
                         "timed loop; the scene is resident (uploaded once at psy_scene_create)" % WAVE_DESC_BYTES},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

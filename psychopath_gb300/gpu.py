@@ -336,8 +336,18 @@ class Renderer:
     def __init__(self, scene):
         self.scene = scene
 
-    def render(self, crop=None):
-        img = np.zeros((self.scene.height, self.scene.width, 3), dtype=np.float32)
+    def render(self, crop=None, out=None):
+        """psy_render_image: the scene's image (height x width x 3 XYZ) into
+        a host array -- `out` when given (C-contiguous float32 of that shape,
+        e.g. a view of pinned memory), else a new one -- and the render
+        statistics."""
+        shape = (self.scene.height, self.scene.width, 3)
+        if out is None:
+            img = np.zeros(shape, dtype=np.float32)
+        else:
+            if out.shape != shape or out.dtype != np.float32 or not out.flags["C_CONTIGUOUS"]:
+                raise ValueError("out must be a C-contiguous float32 array of shape %s" % (shape,))
+            img = out
         st = abi.PsyRenderStats()
         cr = (C.c_uint32 * 4)(*crop) if crop is not None else None
         _check(lib().psy_render_image(self.scene.h, cr, img.ctypes.data, C.byref(st)))
