@@ -195,6 +195,27 @@ int psy_scene_create(const PsySceneDesc *desc, const PsySceneOptions *opts, PsyS
     UP(distant_colors, distant_colors); UP(cam_xf, cam_xf); UP(cam_tfov, cam_tfov); UP(cam_ap, cam_ap);
     UP(cam_fd, cam_fd);
 #undef UP
+    // the spectrum tables of the scene's constant XYZ colours, built on the
+    // device from their XYZ values
+    if (r == PSY_OK) {
+        const float4 *d_sxyz = nullptr;
+        std::vector<float4> sx = hs.spec_xyz;
+        r = upload(s, sx, &d_sxyz);
+        void *p = nullptr;
+        size_t bytes = std::max<size_t>(1, hs.spec_xyz.size()) * PSY_SPEC_TABLE * sizeof(float);
+        if (r == PSY_OK) {
+            cudaError_t e = cudaMalloc(&p, bytes);
+            if (e == cudaSuccess) {
+                s->allocs.push_back(p);
+                s->device_bytes += bytes;
+                e = launch_spectrum_tables(d_sxyz, (uint32_t)hs.spec_xyz.size(), (float *)p, s->stream);
+            }
+            if (e != cudaSuccess) r = cuda_fail(e, "spectrum tables");
+        }
+        g.spec_tables = (const float *)p;
+        s->d_spec_xyz = d_sxyz;
+        s->n_spec = (uint32_t)hs.spec_xyz.size();
+    }
     if (r == PSY_OK) {
         cudaError_t e = cudaMalloc((void **)&s->d_err, sizeof(int));
         if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_work, 64 * sizeof(uint32_t));
@@ -1286,6 +1307,18 @@ int psy_debug_set_launch(PsyScene *s, int grid, uint32_t wave_paths) {
     if (!s) return fail(PSY_E_INVALID, "null");
     s->grid = grid;
     if (wave_paths >= 1024) s->wave_paths = wave_paths;
+    return PSY_OK;
+}
+int psy_debug_color_spectra(PsyScene *s, uint32_t n, const float *d_hero, float *d_exact, float *d_table,
+                            uint32_t *n_colors) {
+    if (!s || !n_colors) return fail(PSY_E_INVALID, "null");
+    *n_colors = s->n_spec;
+    if (n == 0 || s->n_spec == 0) return PSY_OK;
+    if (!d_hero || !d_exact || !d_table) return fail(PSY_E_INVALID, "null");
+    std::lock_guard<std::mutex> lk(s->mu);
+    CK(launch_debug_color_spectra(s->g, s->d_spec_xyz, s->n_spec, d_hero, n, d_exact, d_table, s->stream),
+       "color spectra launch");
+    CK(cudaStreamSynchronize(s->stream), "sync");
     return PSY_OK;
 }
 int psy_debug_set_resident_tail(PsyScene *s, int iterations) {

@@ -62,7 +62,7 @@ DI float sphere_sample_pdf(const GScene &S, const GLight &L, const Xf &space, V3
 
 struct LightSample {
     int kind;  // 0 none, 1 distant, 2 surface
-    V4 color;  // color_to_spectral(lcol, wl) * s1 * s2
+    V4 color;  // color_spectrum(lcol, wl) * s1 * s2
     V3 dir, sp, sn;
     float serr, pdf, sel_pdf;
     GColor lcol;  // the light's colour at the sample's time
@@ -298,7 +298,7 @@ DI LightSample scene_sample_lights(const GScene &S, float n, float u, float v, f
         out.kind = 2;
         out.sel_pdf = sel_pdf * (1.0f - wl_prob);
     }
-    out.color = color_to_spectral(out.lcol, wl) * out.s1 * out.s2;
+    out.color = color_spectrum<R>(S, out.lcol, wl) * out.s1 * out.s2;
     return out;
 }
 

@@ -101,16 +101,78 @@ DI V4 spectrum_xyz_to_p_4(V4 lambdas, float X, float Y, float Z) {
     return ip * inv_norm;
 }
 
+// Meng upsampling of a constant colour at sample s of the point spectra:
+// the weighted point spectra of spectrum_xyz_to_p_4 at one sample instead
+// of lerped at four wavelengths, times 1 / the equal-energy reflectance.
+// Tabulated for every sample, it gives the colour's spectrum at any
+// wavelength as one lerp between two table entries: the same value up to
+// the order of the lerp and the weighted sum (rounding only).
+DI float meng_table_value(float X, float Y, float Z, int s) {
+    float inv_norm = X + Y + Z;
+    float norm = 1.0f / inv_norm;
+    if (!(norm < 3.40282347e+38f)) return 0.0f;
+    float xx = X * norm, yy = Y * norm;
+    const float *M = psy_meng_xy_to_uv;
+    float u = M[0] * xx + M[1] * yy + M[2];
+    float v = M[3] * xx + M[4] * yy + M[5];
+    if (u < 0.0f || u >= (float)PSY_MENG_GRID_WIDTH || v < 0.0f || v >= (float)PSY_MENG_GRID_HEIGHT) return 0.0f;
+    int ui = (int)u, vi = (int)v;
+    const int *cell = psy_meng_grid[ui + PSY_MENG_GRID_WIDTH * vi];
+    int inside = cell[0], num = cell[1];
+    const int *idx = cell + 2;
+    if (num == 0) return 0.0f;
+    auto sp = [&](int k) { return psy_meng_point_spectrum[idx[k]][s]; };
+    float r = 0.0f;
+    if (inside) {
+        float u2 = u - (float)ui, v2 = v - (float)vi;
+        r = sp(0) * ((1.0f - u2) * (1.0f - v2)) + sp(2) * ((1.0f - u2) * v2) + sp(3) * (u2 * v2) +
+            sp(1) * (u2 * (1.0f - v2));
+    } else {
+        const float *uv0 = psy_meng_point_uv[idx[0]];
+        const float *uv1 = psy_meng_point_uv[idx[1]];
+        float ex = u - uv0[0], ey = v - uv0[1];
+        float e0x = uv1[0] - uv0[0], e0y = uv1[1] - uv0[1];
+        float uu = e0x * ey - ex * e0y;
+        for (int i = 0; i < num - 1; i++) {
+            float e1x, e1y;
+            if (i == num - 2) {
+                e1x = uv1[0] - uv0[0];
+                e1y = uv1[1] - uv0[1];
+            } else {
+                const float *uvn = psy_meng_point_uv[idx[i + 2]];
+                e1x = uvn[0] - uv0[0];
+                e1y = uvn[1] - uv0[1];
+            }
+            float vv = ex * e1y - e1x * ey;
+            float area = e0x * e1y - e1x * e0y;
+            float fu = uu / area, fv = vv / area;
+            float fw = 1.0f - fu - fv;
+            if (fu < 0.0f || fv < 0.0f || fw < 0.0f) {
+                uu = -vv;
+                e0x = e1x;
+                e0y = e1y;
+                continue;
+            }
+            r = sp(0) * fw + sp(i + 1) * fv + sp((i == num - 2) ? 1 : i + 2) * fu;
+            break;
+        }
+    }
+    return r * inv_norm * (1.0f / PSY_MENG_EQUAL_ENERGY_REFLECTANCE);
+}
+
 // ------------------------------------------------------------------ colour
+// (a scaled or lerped colour is a new value: its spectrum-table index is dropped)
 DI GColor color_mul(GColor c, float s) {
-    if (c.kind == PSY_COLOR_XYZ_K) return GColor{c.kind, c.a * s, c.b * s, c.c * s};
-    return GColor{c.kind, c.a, c.b * s, c.c};
+    uint32_t kind = c.kind & PSY_COLOR_KIND_MASK;
+    if (kind == PSY_COLOR_XYZ_K) return GColor{kind, c.a * s, c.b * s, c.c * s};
+    return GColor{kind, c.a, c.b * s, c.c};
 }
 DI GColor color_lerp(GColor x, GColor y, float alpha) {
     float ia = 1.0f - alpha;
-    if (x.kind == PSY_COLOR_XYZ_K)
-        return GColor{x.kind, (x.a * ia) + (y.a * alpha), (x.b * ia) + (y.b * alpha), (x.c * ia) + (y.c * alpha)};
-    return GColor{x.kind, (x.a * ia) + (y.a * alpha), (x.b * ia) + (y.b * alpha), 0.0f};
+    uint32_t kind = x.kind & PSY_COLOR_KIND_MASK;
+    if (kind == PSY_COLOR_XYZ_K)
+        return GColor{kind, (x.a * ia) + (y.a * alpha), (x.b * ia) + (y.b * alpha), (x.c * ia) + (y.c * alpha)};
+    return GColor{kind, (x.a * ia) + (y.a * alpha), (x.b * ia) + (y.b * alpha), 0.0f};
 }
 DI GColor lerp_slice_color(const GColor *s, uint32_t n, float alpha) {
     uint32_t i; float a2;
@@ -131,19 +193,45 @@ DI float plancks_law(float temperature, float wavelength) {
 }
 DI V4 color_to_spectral(GColor c, float hero) {
     V4 wls = v4(nth_wavelength(hero, 0), nth_wavelength(hero, 1), nth_wavelength(hero, 2), nth_wavelength(hero, 3));
-    if (c.kind == PSY_COLOR_XYZ_K)
+    const uint32_t kind = c.kind & PSY_COLOR_KIND_MASK;
+    if (kind == PSY_COLOR_XYZ_K)
         return spectrum_xyz_to_p_4(wls, c.a, c.b, c.c) * (1.0f / PSY_MENG_EQUAL_ENERGY_REFLECTANCE);
     V4 o;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         float pl = plancks_law(c.a, wls[k]);
-        if (c.kind != PSY_COLOR_BLACKBODY_K) {
+        if (kind != PSY_COLOR_BLACKBODY_K) {
             float t2 = c.a * c.a;
             pl = pl * 4.0e7f / (t2 * t2);
         }
         o[k] = pl * c.b;
     }
     return o;
+}
+// A colour's spectrum at the four wavelengths of `hero` from its table
+// (the lerp spectrum_xyz_to_p_4 makes between two point-spectrum samples,
+// applied to the combined table).
+DI V4 spectrum_from_table(const float *C, float hero) {
+    V4 o;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float sb = (nth_wavelength(hero, k) - PSY_MENG_SAMPLE_MIN) / (PSY_MENG_SAMPLE_MAX - PSY_MENG_SAMPLE_MIN) *
+                   ((float)PSY_MENG_NUM_SAMPLES - 1.0f);
+        int s0 = (int)sb;
+        int s1 = s0 + 1 < PSY_MENG_NUM_SAMPLES - 1 ? s0 + 1 : PSY_MENG_NUM_SAMPLES - 1;
+        float f = sb - (float)s0;
+        o[k] = __ldg(C + s0) * (1.0f - f) + __ldg(C + s1) * f;
+    }
+    return o;
+}
+// The spectrum of a colour in the shading arithmetic R: the f32 form takes
+// a tabulated colour's spectrum from its table; the f64 form (the
+// reference's arithmetic) and colours without a table run the upsampling.
+template <class R>
+DI V4 color_spectrum(const GScene &S, GColor c, float hero) {
+    const uint32_t t = c.kind >> 16;
+    if (sizeof(R) == sizeof(float) && t != 0u) return spectrum_from_table(S.spec_tables + PSY_SPEC_TABLE * (t - 1u), hero);
+    return color_to_spectral(c, hero);
 }
 DI float x_1931(float w) {
     float t1 = (w - 442.0f) * ((w < 442.0f) ? 0.0624f : 0.0374f);

@@ -284,6 +284,39 @@ cudaError_t launch_queue_binning(const GScene &S, RayBuf R, const uint32_t *queu
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ spectrum tables
+// One block per indexed colour, one thread per sample (see meng_table_value).
+__global__ void k_spectrum_tables(const float4 *__restrict__ xyz, uint32_t n, float *__restrict__ tables) {
+    const uint32_t t = blockIdx.x;
+    if (t >= n) return;
+    const float4 c = xyz[t];
+    for (int s = threadIdx.x; s < PSY_SPEC_TABLE; s += blockDim.x)
+        tables[(size_t)PSY_SPEC_TABLE * t + s] = s < PSY_MENG_NUM_SAMPLES ? meng_table_value(c.x, c.y, c.z, s) : 0.0f;
+}
+// For tests: each indexed colour's spectrum at n hero wavelengths, by the
+// upsampling and from its table ([colour][i][4] floats each).
+__global__ void k_debug_color_spectra(GScene S, const float4 *__restrict__ xyz, uint32_t n_colors,
+                                      const float *__restrict__ hero, uint32_t n, float4 *exact, float4 *table) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_colors * n) return;
+    const uint32_t t = k / n, i = k % n;
+    const float4 c = xyz[t];
+    exact[k] = f4(color_to_spectral(GColor{PSY_COLOR_XYZ_K, c.x, c.y, c.z}, hero[i]));
+    table[k] = f4(spectrum_from_table(S.spec_tables + (size_t)PSY_SPEC_TABLE * t, hero[i]));
+}
+cudaError_t launch_debug_color_spectra(const GScene &S, const float4 *d_xyz, uint32_t n_colors, const float *d_hero,
+                                       uint32_t n, float *d_exact, float *d_table, cudaStream_t st) {
+    const uint32_t total = n_colors * n;
+    k_debug_color_spectra<<<(total + 127) / 128, 128, 0, st>>>(S, d_xyz, n_colors, d_hero, n, (float4 *)d_exact,
+                                                                  (float4 *)d_table);
+    return cudaGetLastError();
+}
+cudaError_t launch_spectrum_tables(const float4 *d_xyz, uint32_t n, float *d_tables, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_spectrum_tables<<<n, 128, 0, st>>>(d_xyz, n, d_tables);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ accumulate
 // XYZ::from_spectral_sample / spp added per pixel (src/renderer.rs:299-310),
 // summing the pixel's samples in sample order.

@@ -214,6 +214,11 @@ struct WaveBufs {
 // out[((orow0 + r) * out_stride + x - out_x0) * 3].  The grid covers max_pix
 // pixels.
 cudaError_t launch_accumulate(const GScene &S, const WaveDesc *d_wave, uint32_t max_pix, PathState P, cudaStream_t st);
+// The spectrum table of each indexed colour (PSY_SPEC_TABLE floats each)
+// from its XYZ value.
+cudaError_t launch_spectrum_tables(const float4 *d_xyz, uint32_t n, float *d_tables, cudaStream_t st);
+cudaError_t launch_debug_color_spectra(const GScene &S, const float4 *d_xyz, uint32_t n_colors, const float *d_hero,
+                                       uint32_t n, float *d_exact, float *d_table, cudaStream_t st);
 // Sampler values for tests (op 0-4 as psy_debug_samplers documents):
 // d_args holds n rows of 5 words, d_out n rows of 4 words.
 cudaError_t launch_debug_samplers(int op, const uint32_t *d_args, uint32_t n, uint32_t *d_out, cudaStream_t st);

@@ -62,6 +62,12 @@ int psy_debug_set_sort(PsyScene *scene, int bits);
  * blocks striding over the queue, -1: each kernel's resident blocks) and
  * the paths per wave (>= 1024 to change it). */
 int psy_debug_set_launch(PsyScene *scene, int grid, uint32_t wave_paths);
+/* The spectrum of each of the scene's tabulated colours (constant XYZ
+ * colours) at n hero wavelengths (device arrays), by the upsampling
+ * (d_exact) and from the colour's table (d_table): n_colors x n x 4 floats
+ * each.  *n_colors is set even when n == 0. */
+int psy_debug_color_spectra(PsyScene *scene, uint32_t n, const float *d_hero, float *d_exact, float *d_table,
+                            uint32_t *n_colors);
 /* The last `iterations` wavefront iterations of a wave launch each kernel on
  * its resident blocks (0: none). */
 int psy_debug_set_resident_tail(PsyScene *scene, int iterations);

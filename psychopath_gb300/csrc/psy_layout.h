@@ -60,6 +60,13 @@ struct __align__(16) GNodeH {
 #define PSY_COLOR_XYZ_K 0u
 #define PSY_COLOR_BLACKBODY_K 1u
 #define PSY_COLOR_TEMPERATURE_K 2u
+// Bits 0-15 of GColor::kind are the colour kind; bits 16-31 are 1 + the
+// index of the colour's precomputed spectrum table (GScene::spec_tables)
+// for the constant XYZ colours the scene stores, 0 for none.
+#define PSY_COLOR_KIND_MASK 0xFFFFu
+// Floats per spectrum table: the 95 samples of the Meng point spectra,
+// combined with the colour's weights, and a pad.
+#define PSY_SPEC_TABLE 96
 // Colour (PsyColor): kind, three values.
 struct __align__(16) GColor {
     uint32_t kind;
@@ -140,6 +147,7 @@ struct GScene {
     const float *distant_radii;
     const float4 *distant_dirs;
     const GColor *distant_colors;
+    const float *spec_tables;      // PSY_SPEC_TABLE floats per indexed colour (see PSY_COLOR_KIND_MASK)
     const float4 *cam_xf;          // 3 float4 per key
     const float *cam_tfov, *cam_ap, *cam_fd;
     uint32_t top_root;             // child reference of the instance BVH root (PSY_REF_NONE: empty)

@@ -1098,6 +1098,19 @@ int build_host_scene(const PsySceneDesc *d, const PsySceneOptions *opts, HostSce
             h.child = n.child;
         }
     }
+    // spectrum tables: every constant XYZ colour the scene stores (shader
+    // colours, light and distant-light colour keys, the background) gets an
+    // index; the device builds the table of each at upload
+    hs.spec_xyz.clear();
+    auto index_color = [&](GColor &c) {
+        if ((c.kind & PSY_COLOR_KIND_MASK) != PSY_COLOR_XYZ_K || hs.spec_xyz.size() >= 0xFFFEu) return;
+        c.kind = (c.kind & PSY_COLOR_KIND_MASK) | ((uint32_t)(hs.spec_xyz.size() + 1) << 16);
+        hs.spec_xyz.push_back(f4(c.a, c.b, c.c, 0.0f));
+    };
+    for (GShader &g : hs.shaders) index_color(g.color);
+    for (GColor &c : hs.light_colors) index_color(c);
+    for (GColor &c : hs.distant_colors) index_color(c);
+    index_color(hs.background);
     if (hs.nodes.empty()) hs.nodes.push_back(GNode{});
     if (hs.bounds_ext.empty()) hs.bounds_ext.push_back(GBounds4{});
     if (hs.tri_idx.empty()) { hs.tri_idx.push_back(make_uint4(0, 0, 0, 0)); hs.tris.resize(3, f4(0, 0, 0, 0)); }

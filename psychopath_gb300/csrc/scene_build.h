@@ -39,6 +39,7 @@ struct HostScene {
     bool lt_empty = true;
     float scene_min[3] = {0, 0, 0}, scene_max[3] = {0, 0, 0};  // union of instance bounds
     GColor background{};
+    std::vector<float4> spec_xyz;  // the XYZ value of each indexed colour (spectrum tables)
     uint32_t width = 0, height = 0, spp = 0, seed = 0, max_bounces = 2;
     // per mesh object (desc order): BVH-order original triangle indices and BVH4 node count
     std::vector<std::vector<uint32_t>> mesh_tri_order;

@@ -76,6 +76,8 @@ struct PsyScene {
     uint32_t wave_paths = 1u << 24;      // paths per wave
     int grid = 0;                        // grid of the queue kernels (0: size by queue, -1: resident)
     int resident_tail = 0;               // the last n iterations of a wave launch on resident grids
+    const float4 *d_spec_xyz = nullptr;  // XYZ of each colour with a spectrum table
+    uint32_t n_spec = 0;
     bool counting = false;               // accumulate traversal counters during renders
     int trace_mode = 0;                  // 0: one thread per ray, 1: persistent with lane refill, 2: warp packets
     int prec = 0;                        // shading arithmetic: 0 f64 (reference), 1 f32

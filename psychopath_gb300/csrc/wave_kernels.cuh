@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                 resolve_hit<RT>(S, h, o, d, time, sd);
                 const Closure &cl = sd.closure;
                 if (cl.kind == PSY_CL_EMIT) {
-                    V4 c = color_to_spectral(cl.color, wl);
+                    V4 c = color_spectrum<RT>(S, cl.color, wl);
                     if (ev == EV_CAMERA) {
                         color = color + c;
                     } else {
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                     seed += 1;
                     // the surface colour's spectrum: shared by the light
                     // sample's evaluation and the bounce sample
-                    V4 cspec = color_to_spectral(cl.color, wl);
+                    V4 cspec = color_spectrum<RT>(S, cl.color, wl);
                     float smp[4];
                     get_sample_4d(si, 0, px, py, seed, smp);
                     LightSample li = scene_sample_lights<RT>(S, smp[0], smp[1], smp[2], wl, time, d, sd.pos,
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                     P.seed[p] = seed;
                 }
             } else {
-                V4 bg = color_to_spectral(S.background, wl);
+                V4 bg = color_spectrum<RT>(S, S.background, wl);
                 color = color + bg * latt / splat4(csp);
                 P.color[p] = f4(color);
             }

@@ -62,6 +62,7 @@ def lib(path=None):
     L.psy_debug_scene_info.argtypes = [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]
     L.psy_debug_set_launch.argtypes = [vp, C.c_int, u32]
     L.psy_debug_set_resident_tail.argtypes = [vp, C.c_int]
+    L.psy_debug_color_spectra.argtypes = [vp, u32, vp, vp, vp, C.POINTER(u32)]
     L.psy_debug_counters.argtypes = [vp, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     L.psy_debug_set_trace.argtypes = [vp, C.c_int, C.c_int]
     L.psy_debug_set_sort.argtypes = [vp, C.c_int]
@@ -263,6 +264,19 @@ class Scene:
 
     def set_launch(self, grid=0, wave_paths=0):
         _check(lib().psy_debug_set_launch(self.h, grid, wave_paths))
+
+    def color_spectra(self, heros):
+        """Each tabulated colour's spectrum at the hero wavelengths `heros`,
+        by the upsampling and from its table: two arrays (colours, n, 4)."""
+        import torch
+        nc = C.c_uint32()
+        _check(lib().psy_debug_color_spectra(self.h, 0, None, None, None, C.byref(nc)))
+        n = len(heros)
+        d_h = torch.from_numpy(np.asarray(heros, dtype=np.float32)).cuda()
+        ex = torch.zeros((max(1, nc.value), n, 4), dtype=torch.float32, device="cuda")
+        tb = torch.zeros_like(ex)
+        _check(lib().psy_debug_color_spectra(self.h, n, d_h.data_ptr(), ex.data_ptr(), tb.data_ptr(), C.byref(nc)))
+        return ex.cpu().numpy()[: nc.value], tb.cpu().numpy()[: nc.value]
 
     def set_resident_tail(self, iterations):
         """The last `iterations` wavefront iterations of a wave launch each

@@ -279,6 +279,32 @@ def test_resident_tail_does_not_change_image(gpu_lib, tail):
     g.close()
 
 
+@pytest.mark.parametrize("case", ["cornell", "mesh_stress", "light_tree_64"])
+def test_color_spectrum_tables(gpu_lib, case):
+    """The f32 form takes each constant XYZ colour's spectrum (shader
+    colours, light and distant-light colours, the background) from a table
+    of its combined Meng point spectra: at any hero wavelength the same
+    value as the upsampling up to rounding (bar 1e-5 relative), and
+    exactly 0 where the upsampling gives 0."""
+    from psychopath_gb300 import scenes
+    if case == "cornell":
+        s = sc.cornell()
+    elif case == "mesh_stress":
+        s = scenes.mesh_stress(64, 36, 1, level=4)
+    else:
+        s = sc.motion_small(48, 27, 8, 2, lights=64)
+    g = gpu.Scene(s, shading="f32")
+    rng = np.random.default_rng(3)
+    heros = np.concatenate([rng.uniform(380.0, 700.0, 4000), [380.0, 459.9999, 460.0, 699.9999]]).astype(np.float32)
+    ex, tb = g.color_spectra(heros)
+    g.close()
+    assert ex.shape[0] >= 2 and ex.shape == tb.shape
+    assert np.array_equal(ex == 0.0, tb == 0.0)
+    scale = np.maximum(np.abs(ex), 1e-30)
+    rel = np.abs(tb.astype(np.float64) - ex) / scale
+    assert rel.max() < 1e-5, rel.max()
+
+
 def test_f32_shading_sphere_lights(gpu_lib):
     """The f32 variant on a motion scene lit by sphere lights (cone sampling
     and its pdf in f32): within 1% relative RMSE of the oracle, and no
