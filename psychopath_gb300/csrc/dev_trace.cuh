@@ -440,15 +440,16 @@ DI bool trace_ray(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut,
             (void)count;
             if (COUNT) cnt->nodes++;
             // children in the table's front-to-back order: descend into the
-            // first hit child, push the others (deepest first); three
-            // unconditional stores, of which np are kept
+            // first hit child, push the others (deepest first); only the np
+            // entries kept are stored (local-memory stores write through to
+            // L2, so unused ones cost traffic)
             uint32_t e = lut[16u * prow[code] + m];
             if (!(e & 0x800u)) goto pop;
             int np = (int)((e >> 8) & 7u);
             if (sp + np > STACK) return false;
-            stack[sp] = sel4(ch, (e >> 2) & 3u);
-            stack[sp + 1] = sel4(ch, (e >> 4) & 3u);
-            stack[sp + 2] = sel4(ch, (e >> 6) & 3u);
+            if (np > 0) stack[sp] = sel4(ch, (e >> 2) & 3u);
+            if (np > 1) stack[sp + 1] = sel4(ch, (e >> 4) & 3u);
+            if (np > 2) stack[sp + 2] = sel4(ch, (e >> 6) & 3u);
             sp += np;
             cur = sel4(ch, e & 3u);
         }
@@ -688,11 +689,11 @@ DI bool trace_ray_static(const GScene &S, const uint8_t *prow_tab, const uint16_
             } else {
                 int np = (int)((e >> 8) & 7u);
                 if (sp + np > STACK) return false;
-                // three unconditional stores (the stack has spare entries);
-                // only np of them are kept
-                stack.set(sp, sel4(ch, (e >> 2) & 3u));
-                stack.set(sp + 1, sel4(ch, (e >> 4) & 3u));
-                stack.set(sp + 2, sel4(ch, (e >> 6) & 3u));
+                // only the np entries kept are stored (local-memory stores
+                // write through to L2, so unused ones cost traffic)
+                if (np > 0) stack.set(sp, sel4(ch, (e >> 2) & 3u));
+                if (np > 1) stack.set(sp + 1, sel4(ch, (e >> 4) & 3u));
+                if (np > 2) stack.set(sp + 2, sel4(ch, (e >> 6) & 3u));
                 sp += np;
                 cur = sel4(ch, e & 3u);
             }
@@ -812,9 +813,9 @@ DI int slane_step(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut,
         if (!(e & 0x800u)) goto pop;
         int np = (int)((e >> 8) & 7u);
         if (L.sp + np > STACK) return -1;
-        stack[L.sp] = sel4(ch, (e >> 2) & 3u);
-        stack[L.sp + 1] = sel4(ch, (e >> 4) & 3u);
-        stack[L.sp + 2] = sel4(ch, (e >> 6) & 3u);
+        if (np > 0) stack[L.sp] = sel4(ch, (e >> 2) & 3u);
+        if (np > 1) stack[L.sp + 1] = sel4(ch, (e >> 4) & 3u);
+        if (np > 2) stack[L.sp + 2] = sel4(ch, (e >> 6) & 3u);
         L.sp += np;
         L.cur = sel4(ch, e & 3u);
     }
