@@ -494,21 +494,23 @@ DI V4 closure_sample(const Closure &cl, V4 spec, V3 inc, V3 nor, V3 nor_g, float
     *pdf = 0.0f;
     return splat4(0.0f);
 }
+// (g and h are evaluated only past the first case -- a light entirely
+// above the horizon, the common one -- with the same expressions)
 DI float sphere_lambert(float nlcos, float rcos) {
-    float nlsin = sqrtf(1.0f - (nlcos * nlcos));
     float rsin2 = 1.0f - (rcos * rcos);
+    float nl = acosf(nlcos);
+    float r = acosf(rcos);
+    if (nl < (PSY_H_PI - r)) return nlcos * rsin2;
+    if (!(nl < PSY_H_PI) && !(nl < (PSY_H_PI + r))) return 0.0f;  // the last case, NaN included
+    float nlsin = sqrtf(1.0f - (nlcos * nlcos));
     float rsin = sqrtf(rsin2);
     float ysin = rcos / nlsin;
     float ycos2 = 1.0f - (ysin * ysin);
     float ycos = sqrtf(ycos2);
     float g = (-2.0f * nlsin * rcos * ycos) + PSY_H_PI - asinf(ysin) + (ysin * ycos);
     float h = nlcos * ((ycos * sqrtf(rsin2 - ycos2)) + (rsin2 * asinf(ycos / rsin)));
-    float nl = acosf(nlcos);
-    float r = acosf(rcos);
-    if (nl < (PSY_H_PI - r)) return nlcos * rsin2;
     if (nl < PSY_H_PI) return (nlcos * rsin2) + g - h;
-    if (nl < (PSY_H_PI + r)) return (g + h) * PSY_INV_PI;
-    return 0.0f;
+    return (g + h) * PSY_INV_PI;
 }
 DI float closure_estimate_sphere(const Closure &cl, V3 inc, V3 to_light, float r2l, V3 nor, V3 nor_g) {
     if (cl.kind == PSY_CL_LAMBERT) {
