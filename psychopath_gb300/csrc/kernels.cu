@@ -151,9 +151,7 @@ __global__ void __launch_bounds__(128, 12) k_shade_shadow(PathState P, RayBuf R,
                 float4 nb = P.nb_o[p], nd = P.nb_d[p];
                 R.o[p] = make_float4(nb.x, nb.y, nb.z, CUDART_INF_F);
                 R.d[p] = make_float4(nd.x, nd.y, nd.z, time);
-                R.occl[p] = 0;
-                V4 latt = v4(P.latt[p]) * v4(P.nafac[p]);
-                P.latt[p] = f4(latt);
+                R.occl[p] = 0;  // the stored attenuation is already the bounce's
                 ev = EV_BOUNCE;
                 alive = true;
                 if (out.keys) key = next_ray_key(out, v3(nb), v3(nd), false);

@@ -230,6 +230,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                     }
                     bool do_bounce = false;
                     V4 nafac = splat4(1.0f);  // set with the bounce, read only then
+                    V3 nbo = v3(0.0f, 0.0f, 0.0f), nbd = v3(0.0f, 0.0f, 0.0f);  // the bounce ray
                     if (bounce < S.max_bounces) {
                         bounce += 1;
                         seed += 1;
@@ -241,28 +242,30 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                         if ((pdf > 0.0f) && (max_elem4(filt) > 0.0f)) {
                             nafac = filt;
                             csp = pdf;
-                            V3 nb = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
-                            P.nafac[p] = f4(nafac);
-                            P.nb_o[p] = make_float4(nb.x, nb.y, nb.z, csp);
-                            P.nb_d[p] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                            nbo = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
+                            nbd = dir;
+                            P.nb_o[p] = make_float4(nbo.x, nbo.y, nbo.z, csp);
+                            P.nb_d[p] = make_float4(nbd.x, nbd.y, nbd.z, 0.0f);
                             has_nb = 1;
                             do_bounce = true;
                         }
                     } else {
                         has_nb = 0;
                     }
+                    // the stored attenuation is the bounce ray's (the light
+                    // sample's pending light above used the current one):
+                    // k_shade_shadow sets up a stored bounce with it as is
+                    if (do_bounce) latt = latt * nafac;
                     if (found) {
                         ev = EV_SHADOW;
                         alive = true;
                     } else if (do_bounce) {
-                        float4 nb = P.nb_o[p], nd = P.nb_d[p];
-                        R.o[p] = make_float4(nb.x, nb.y, nb.z, CUDART_INF_F);
-                        R.d[p] = make_float4(nd.x, nd.y, nd.z, time);
+                        R.o[p] = make_float4(nbo.x, nbo.y, nbo.z, CUDART_INF_F);
+                        R.d[p] = make_float4(nbd.x, nbd.y, nbd.z, time);
                         R.occl[p] = 0;
                         ev = EV_BOUNCE;
-                        latt = latt * nafac;
                         alive = true;
-                        if (out.keys) key = next_ray_key(out, v3(nb), v3(nd), false);
+                        if (out.keys) key = next_ray_key(out, nbo, nbd, false);
                     }
                     P.latt[p] = f4(latt);
                     P.seed[p] = seed;
