@@ -497,7 +497,7 @@ def run_ours(args):
 
 
 def served_fp16_frames(args, sd, plain_value, plain_img):
-    """The benchmark spec's headline form on this frame: a scene with FP16 child
+    """The served, autotuned FP16-bounds form on this frame: a scene with FP16 child
     bounds and f32 shading, autotuned, served as a lane of the render server
     (waves of the tuned size, CUDA-graph replay); K frames submitted as K
     requests with host result buffers and timed from the first submit to the
