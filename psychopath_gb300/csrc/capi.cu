@@ -71,7 +71,7 @@ static int upload(PsyScene *s, const std::vector<T> &v, const T **out) {
 
 static void free_render(PsyScene *s) {
     s->graph.reset();
-    void *ptrs[] = {s->P.color, s->P.latt, s->P.pending, s->P.nb_o, s->P.nb_d, s->P.tw, s->P.seed, s->P.flags,
+    void *ptrs[] = {s->P.color, s->P.latt, s->P.pending, s->P.nafac, s->P.nb_o, s->P.nb_d, s->P.tw, s->P.seed, s->P.flags,
                     s->R.o, s->R.d, s->R.occl, s->H.ki, s->H.tb, s->queue[0], s->queue[1], s->counts, s->d_raycount,
                     s->d_stage, s->d_stage_key, s->d_bins, s->d_qradix, s->d_waves};
     for (void *p : ptrs)
@@ -96,7 +96,7 @@ static int ensure_render(PsyScene *s, uint32_t n) {
     free_render(s);
     size_t N = n;
 #define AL(ptr, bytes) CK(cudaMalloc((void **)&(ptr), (bytes)), "cudaMalloc render state")
-    AL(s->P.color, N * 16); AL(s->P.latt, N * 16); AL(s->P.pending, N * 16);
+    AL(s->P.color, N * 16); AL(s->P.latt, N * 16); AL(s->P.pending, N * 16); AL(s->P.nafac, N * 16);
     AL(s->P.nb_o, N * 16); AL(s->P.nb_d, N * 16); AL(s->P.tw, N * 8); AL(s->P.seed, N * 4); AL(s->P.flags, N * 4);
     AL(s->R.o, N * 16); AL(s->R.d, N * 16); AL(s->R.occl, N);
     AL(s->H.ki, N * 16); AL(s->H.tb, N * 16);
@@ -533,7 +533,7 @@ int alloc_wave_bufs(WaveBufs &B, uint32_t cap, uint32_t cap_waves, bool sorting,
             *p = reinterpret_cast<std::remove_pointer_t<decltype(p)>>(q);
         }
     };
-    al(&B.P.color, N * 16); al(&B.P.latt, N * 16); al(&B.P.pending, N * 16);
+    al(&B.P.color, N * 16); al(&B.P.latt, N * 16); al(&B.P.pending, N * 16); al(&B.P.nafac, N * 16);
     al(&B.P.nb_o, N * 16); al(&B.P.nb_d, N * 16); al(&B.P.tw, N * 8); al(&B.P.seed, N * 4); al(&B.P.flags, N * 4);
     al(&B.R.o, N * 16); al(&B.R.d, N * 16); al(&B.R.occl, N);
     al(&B.H.ki, N * 16); al(&B.H.tb, N * 16);
@@ -751,8 +751,7 @@ extern "C" int psy_render_bucket_noalloc(PsyScene *s, const PsyBucket *b, uint32
     const size_t C = kNoallocPaths;
     WaveBufs B;
     B.P.color = (float4 *)take(C * 16); B.P.latt = (float4 *)take(C * 16); B.P.pending = (float4 *)take(C * 16);
-    take(C * 16);  // a spare slice: the layout and its size stay as documented
-    B.P.nb_o = (float4 *)take(C * 16); B.P.nb_d = (float4 *)take(C * 16);
+    B.P.nafac = (float4 *)take(C * 16); B.P.nb_o = (float4 *)take(C * 16); B.P.nb_d = (float4 *)take(C * 16);
     B.P.tw = (float2 *)take(C * 8); B.P.seed = (uint32_t *)take(C * 4); B.P.flags = (uint32_t *)take(C * 4);
     B.R.o = (float4 *)take(C * 16); B.R.d = (float4 *)take(C * 16); B.R.occl = (uint8_t *)take(C);
     B.H.ki = (uint4 *)take(C * 16); B.H.tb = (float4 *)take(C * 16);
@@ -1021,7 +1020,7 @@ extern "C" int psy_autotune(PsyScene *s, const PsyTuneOptions *opts, PsyTuneResu
     //    held plus a quarter of the free device memory (or the caller's
     //    max_wave_mib); a candidate that cannot allocate ends the step.
     if (err == PSY_OK) {
-        const uint64_t kBytesPerPath = 208;  // ensure_render's buffers per path (169-191 bytes), rounded up
+        const uint64_t kBytesPerPath = 224;  // ensure_render's buffers per path (185-207 bytes), rounded up
         uint64_t img = (uint64_t)W * H * spp;
         size_t fb = 0, tb = 0;
         cudaMemGetInfo(&fb, &tb);

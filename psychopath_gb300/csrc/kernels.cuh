@@ -13,6 +13,7 @@ struct PathState {
     float4 *color;    // accumulated path colour (4 hero wavelengths)
     float4 *latt;     // light_attenuation (times next_attenuation_fac once a bounce is set up)
     float4 *pending;  // pending_color_addition
+    float4 *nafac;    // next_attenuation_fac of the last bounce sample that succeeded
     float4 *nb_o;     // next bounce ray origin, w = closure_sample_pdf
     float4 *nb_d;     // next bounce ray direction, w unused
     float2 *tw;       // (time, wavelength)

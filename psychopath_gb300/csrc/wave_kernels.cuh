@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                         }
                     }
                     bool do_bounce = false;
-                    V4 nafac = splat4(1.0f);  // set with the bounce, read only then
+                    V4 nafac = splat4(1.0f);  // set with a bounce that succeeds
                     V3 nbo = v3(0.0f, 0.0f, 0.0f), nbd = v3(0.0f, 0.0f, 0.0f);  // the bounce ray
                     if (bounce < S.max_bounces) {
                         bounce += 1;
@@ -244,6 +244,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                             csp = pdf;
                             nbo = robust_ray_origin(sd.pos, sd.pos_err, normalized(sd.nor_g), dir);
                             nbd = dir;
+                            P.nafac[p] = f4(nafac);
                             P.nb_o[p] = make_float4(nbo.x, nbo.y, nbo.z, csp);
                             P.nb_d[p] = make_float4(nbd.x, nbd.y, nbd.z, 0.0f);
                             has_nb = 1;
@@ -254,8 +255,13 @@ __global__ void __launch_bounds__(128, MINB) k_shade_hit(GScene S, const WaveDes
                     }
                     // the stored attenuation is the bounce ray's (the light
                     // sample's pending light above used the current one):
-                    // k_shade_shadow sets up a stored bounce with it as is
+                    // k_shade_shadow sets up a stored bounce with it as is.
+                    // A bounce sample that fails keeps the path's earlier
+                    // bounce ray and factor (as the reference's LightPath
+                    // does): with a shadow ray, that stale bounce is set up
+                    // after it, times the stored factor
                     if (do_bounce) latt = latt * nafac;
+                    else if (found && has_nb) latt = latt * v4(P.nafac[p]);
                     if (found) {
                         ev = EV_SHADOW;
                         alive = true;
