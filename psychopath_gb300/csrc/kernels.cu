@@ -330,9 +330,6 @@ __global__ void k_accumulate(GScene S, const WaveDesc *__restrict__ gwave, PathS
     uint32_t x = w.x0 + (lq - lr * w.w);  // the output row is orow0 + lr
     float inv = (float)w.spp;
     V3 acc = v3(0.0f, 0.0f, 0.0f);
-    // unrolled so that several samples' loads are in flight at once; the
-    // sum keeps sample order
-#pragma unroll 8
     for (uint32_t s = 0; s < w.spp; s++) {
         uint32_t p = w.path_begin + lq * w.spp + s;
         V3 c = xyz_from_spectral(v4(P.color[p]), P.tw[p].y);
