@@ -402,6 +402,26 @@ DI void load_traversal_table(uint8_t *smem) {
     __syncthreads();
 }
 
+// The general traversal's per-thread shared-memory slot: the entered
+// instance's object-to-world matrix (3 float4), and with PSY_RAY_SHARED the
+// world ray's origin, direction and triangle-test precompute (3 float4),
+// which the loop reads only at instance entry and exit and at leaves --
+// kept there instead of in registers the node tests need.
+#ifndef PSY_RAY_SHARED
+#define PSY_RAY_SHARED 0
+#endif
+#define PSY_XFM_SLOT (PSY_RAY_SHARED ? 6 : 3)
+DI float4 pack_pre(const TriPre &p) {
+    return make_float4(p.sx, p.sy, p.sz, __int_as_float(p.ix | (p.iy << 2) | (p.iz << 4)));
+}
+DI TriPre unpack_pre(float4 v) {
+    TriPre p;
+    int k = __float_as_int(v.w);
+    p.ix = k & 3; p.iy = (k >> 2) & 3; p.iz = (k >> 4) & 3;
+    p.sx = v.x; p.sy = v.y; p.sz = v.z;
+    return p;
+}
+
 // Trace one ray.  `occl`: any-hit (shadow ray).  Returns false on stack
 // overflow (the scene needs a deeper stack than STACK).  The hit keeps only
 // its kind, triangle (or light triangle) and instance while traversing
@@ -429,7 +449,16 @@ DI bool trace_ray(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut,
     uint32_t slot = 0, hkind = PSY_HIT_MISS_K, hprim = 0, hslot = 0;
     uint32_t mts = 1, mvb = 0;  // entered mesh: vertex time samples and first vertex
     bool has_xf = false;
-    TriPre pre = tri_precompute(d);
+    const TriPre pre0 = tri_precompute(d);
+    if (PSY_RAY_SHARED) {
+        xfm[3] = make_float4(o.x, o.y, o.z, 0.0f);
+        xfm[4] = make_float4(d.x, d.y, d.z, 0.0f);
+        xfm[5] = pack_pre(pre0);
+    }
+    // the world ray and the precompute, from the slot or the registers
+    auto RO = [&]() { return PSY_RAY_SHARED ? v3(xfm[3]) : o; };
+    auto RD = [&]() { return PSY_RAY_SHARED ? v3(xfm[4]) : d; };
+    auto PRE = [&]() { return PSY_RAY_SHARED ? unpack_pre(xfm[5]) : pre0; };
     while (true) {
         // descend internal nodes
         while (!psy_is_leaf(cur)) {
@@ -464,8 +493,8 @@ DI bool trace_ray(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut,
                 has_xf = in.xc != 0;
                 if (has_xf) {
                     Xf x = lerp_slice_xf(S.xforms + 3 * in.xs, in.xc, time);
-                    lo = xf_point(o, x);
-                    ldi = recip(xf_vector(d, x));
+                    lo = xf_point(RO(), x);
+                    ldi = recip(xf_vector(RD(), x));
                     // object -> world matrix of the triangles: kept in this
                     // thread's shared-memory slot, read by each triangle fetch
                     Xf mat = instance_mat(S, in, time);
@@ -484,16 +513,16 @@ DI bool trace_ray(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut,
             } else if (in.kind == PSY_INST_RECT) {
                 float t, b0, b1, b2;
                 uint32_t which;
-                if (rect_hit(S, in, o, d, tmax, time, t, b0, b1, b2, which)) {
+                if (rect_hit(S, in, RO(), RD(), tmax, time, t, b0, b1, b2, which)) {
                     if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
                     hkind = PSY_HIT_LIGHT_K; hprim = which; hslot = slot;
                     tmax = t;
                 }
             } else {
                 Xf x = instance_xf_at(S, in, time);
-                V3 ol = in.xc ? xf_point(o, x) : lo;  // lo: the world origin at this level
+                V3 ol = in.xc ? xf_point(RO(), x) : lo;  // lo: the world origin at this level
                 float t;
-                if (sphere_hit(S, in, ol, d, tmax, time, t)) {
+                if (sphere_hit(S, in, ol, RD(), tmax, time, t)) {
                     if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
                     hkind = PSY_HIT_LIGHT_K; hprim = 0xFFFFFFFFu; hslot = slot;
                     tmax = t;
@@ -507,7 +536,7 @@ DI bool trace_ray(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut,
                 fetch_tri_xfm(S, mts, mvb, tri, time, has_xf, xfm, p0, p1, p2);
                 float t, b0, b1, b2;
                 if (COUNT) cnt->tris++;
-                if (tri_intersect(o, pre, tmax, p0, p1, p2, t, b0, b1, b2)) {
+                if (tri_intersect(RO(), PRE(), tmax, p0, p1, p2, t, b0, b1, b2)) {
                     if (occl) { hit.kind = PSY_HIT_OCCLUDE_K; return true; }
                     hkind = PSY_HIT_SURFACE_K; hprim = tri; hslot = slot;
                     tmax = t;
@@ -521,15 +550,15 @@ DI bool trace_ray(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut,
             if (cur != PSY_REF_NONE) break;
             // leaving the instance: back to world space
             in_inst = false;
-            lo = world_origin(o);
-            ldi = world_dir_inv(d);
+            lo = world_origin(RO());
+            ldi = world_dir_inv(RD());
             oct = ray_code(ldi);
             prow = prow_tab + 48 * oct;
             safe = S.ordered_slabs && slab_safe(lo, ldi, tmax);
         }
     }
 done:
-    finish_hit<false>(S, o, pre, time, tmax, hkind, hprim, hslot, hit);
+    finish_hit<false>(S, RO(), PRE(), time, tmax, hkind, hprim, hslot, hit);
     return true;
 }
 
