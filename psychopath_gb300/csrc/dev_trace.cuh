@@ -403,12 +403,16 @@ DI void load_traversal_table(uint8_t *smem) {
 }
 
 // The general traversal's per-thread shared-memory slot: the entered
-// instance's object-to-world matrix (3 float4), and with PSY_RAY_SHARED the
-// world ray's origin, direction and triangle-test precompute (3 float4),
-// which the loop reads only at instance entry and exit and at leaves --
-// kept there instead of in registers the node tests need.
+// instance's object-to-world matrix (3 float4), and with PSY_RAY_SHARED (the
+// default) the world ray's origin, direction and triangle-test precompute
+// (3 float4), which the loop reads only at instance entry and exit and at
+// leaves -- kept there instead of in registers the node tests need.  At 8
+// blocks per SM (64 registers) the spill stores fall from 520 to 396 bytes
+// and the motion + instancing frame (general kernel) runs 212.7 -> 228.0 M
+// samples/s.  The static-scene traversal gains nothing from it (its spills
+// do not fall) and keeps its ray in registers.
 #ifndef PSY_RAY_SHARED
-#define PSY_RAY_SHARED 0
+#define PSY_RAY_SHARED 1
 #endif
 #define PSY_XFM_SLOT (PSY_RAY_SHARED ? 6 : 3)
 DI float4 pack_pre(const TriPre &p) {
