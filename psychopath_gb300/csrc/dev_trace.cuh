@@ -409,12 +409,14 @@ DI void load_traversal_table(uint8_t *smem) {
 // leaves -- kept there instead of in registers the node tests need.  At 8
 // blocks per SM (64 registers) the spill stores fall from 520 to 396 bytes
 // and the motion + instancing frame (general kernel) runs 212.7 -> 228.0 M
-// samples/s.  The static-scene traversal gains nothing from it (its spills
-// do not fall) and keeps its ray in registers.
+// samples/s.  Only the register-limited variants (more than 4 blocks per
+// SM) use it: with the compiler's own budget nothing spills and the extra
+// shared loads only cost.  The static-scene traversal gains nothing from it
+// (its spills do not fall) and keeps its ray in registers.
 #ifndef PSY_RAY_SHARED
 #define PSY_RAY_SHARED 1
 #endif
-#define PSY_XFM_SLOT (PSY_RAY_SHARED ? 6 : 3)
+#define PSY_XFM_SLOT(MINB) ((PSY_RAY_SHARED && (MINB) > 4) ? 6 : 3)
 DI float4 pack_pre(const TriPre &p) {
     return make_float4(p.sx, p.sy, p.sz, __int_as_float(p.ix | (p.iy << 2) | (p.iz << 4)));
 }
@@ -433,7 +435,7 @@ DI TriPre unpack_pre(float4 v) {
 // prow_tab is the per-octant push-row table, lut the entries
 // (load_push_tables).  xfm: this thread's three-float4 shared-memory slot
 // for the entered instance's object-to-world matrix.
-template <int STACK, bool COUNT = false>
+template <int STACK, bool COUNT = false, bool RSH = false>
 DI bool trace_ray(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut, float4 *xfm, V3 o, V3 d, float tmax,
                   float time, bool occl, HitRec &hit, TraceCount *cnt = nullptr) {
     hit.kind = PSY_HIT_MISS_K;
@@ -454,15 +456,15 @@ DI bool trace_ray(const GScene &S, const uint8_t *prow_tab, const uint16_t *lut,
     uint32_t mts = 1, mvb = 0;  // entered mesh: vertex time samples and first vertex
     bool has_xf = false;
     const TriPre pre0 = tri_precompute(d);
-    if (PSY_RAY_SHARED) {
+    if (RSH) {
         xfm[3] = make_float4(o.x, o.y, o.z, 0.0f);
         xfm[4] = make_float4(d.x, d.y, d.z, 0.0f);
         xfm[5] = pack_pre(pre0);
     }
     // the world ray and the precompute, from the slot or the registers
-    auto RO = [&]() { return PSY_RAY_SHARED ? v3(xfm[3]) : o; };
-    auto RD = [&]() { return PSY_RAY_SHARED ? v3(xfm[4]) : d; };
-    auto PRE = [&]() { return PSY_RAY_SHARED ? unpack_pre(xfm[5]) : pre0; };
+    auto RO = [&]() { return RSH ? v3(xfm[3]) : o; };
+    auto RD = [&]() { return RSH ? v3(xfm[4]) : d; };
+    auto PRE = [&]() { return RSH ? unpack_pre(xfm[5]) : pre0; };
     while (true) {
         // descend internal nodes
         while (!psy_is_leaf(cur)) {

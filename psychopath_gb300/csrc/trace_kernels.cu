@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay
                                                     unsigned long long *counters) {
     __shared__ __align__(16) uint8_t table[8 * 48];  // push rows per octant and traversal code
     __shared__ __align__(16) uint16_t push_lut[PSY_PUSH_ROWS * 16];
-    __shared__ float4 xfm[STATIC ? 1 : PSY_XFM_SLOT * 128];  // per-thread slot of the general traversal
+    __shared__ float4 xfm[STATIC ? 1 : PSY_XFM_SLOT(MINB) * 128];  // per-thread slot of the general traversal
     __shared__ uint32_t sstack[STATIC && PSY_SSTACK > 0 ? PSY_SSTACK * PSY_TRACE_BLOCK : 1];  // stack tops (static)
     if (blockIdx.x * blockDim.x >= n) return;  // (whole block: before the table barrier)
     load_push_tables(table, push_lut);
@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(128, MINB) k_trace_rays(GScene S, const PsyRay
         bool oc = (flags & PSY_RAY_OCCLUSION) != 0;
         bool ok = STATIC ? trace_ray_static<STACK, SPEC, H16>(S, table, push_lut, sstack + threadIdx.x, o, d, tmax,
                                                               time, oc, h)
-                         : trace_ray<STACK, COUNT>(S, table, push_lut, xfm + PSY_XFM_SLOT * threadIdx.x, o, d, tmax, time, oc, h, &tc);
+                         : trace_ray<STACK, COUNT, PSY_XFM_SLOT(MINB) == 6>(S, table, push_lut, xfm + PSY_XFM_SLOT(MINB) * threadIdx.x, o, d, tmax, time, oc, h, &tc);
         if (!ok) {
             atomicExch(err, PSY_E_OVERFLOW);
             h.kind = PSY_HIT_MISS_K;
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, H
                                                      unsigned long long *counters) {
     __shared__ __align__(16) uint8_t table[8 * 48];  // push rows per octant and traversal code
     __shared__ __align__(16) uint16_t push_lut[PSY_PUSH_ROWS * 16];
-    __shared__ float4 xfm[STATIC ? 1 : PSY_XFM_SLOT * 128];  // per-thread slot of the general traversal
+    __shared__ float4 xfm[STATIC ? 1 : PSY_XFM_SLOT(MINB) * 128];  // per-thread slot of the general traversal
     __shared__ uint32_t sstack[STATIC && PSY_SSTACK > 0 ? PSY_SSTACK * PSY_TRACE_BLOCK : 1];  // stack tops (static)
     uint32_t n = *count;
     // blocks past the queue's length (the grid covers the wave's capacity)
@@ -511,7 +511,7 @@ __global__ void __launch_bounds__(128, MINB) k_trace_queue(GScene S, RayBuf R, H
         bool oc = R.occl[p] != 0;
         bool ok = STATIC ? trace_ray_static<STACK, SPEC, H16>(S, table, push_lut, sstack + threadIdx.x, v3(ro), v3(rd),
                                                               ro.w, rd.w, oc, h)
-                         : trace_ray<STACK, COUNT>(S, table, push_lut, xfm + PSY_XFM_SLOT * threadIdx.x, v3(ro), v3(rd), ro.w, rd.w, oc,
+                         : trace_ray<STACK, COUNT, PSY_XFM_SLOT(MINB) == 6>(S, table, push_lut, xfm + PSY_XFM_SLOT(MINB) * threadIdx.x, v3(ro), v3(rd), ro.w, rd.w, oc,
                                                    h, &tc);
         if (!ok) {
             atomicExch(err, PSY_E_OVERFLOW);
