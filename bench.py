@@ -50,7 +50,7 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--bounds", default="fp32", choices=["fp32", "fp16"])
     ap.add_argument("--workload", default="mesh_stress",
-                    choices=["mesh_stress", "cornell", "motion", "traversal", "serving", "parity"])
+                    choices=["mesh_stress", "cornell", "motion", "traversal", "serving", "parity", "compact"])
     ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of Poisson arrivals")
     ap.add_argument("--rate", type=float, default=40.0, help="serving: mean arrivals per second")
     ap.add_argument("--wave-paths", type=int, default=1 << 23, help="serving: paths per wave of each scene lane")
@@ -60,6 +60,7 @@ def parse_args():
     ap.add_argument("--plain-seconds", type=float, default=20.0,
                     help="serving: bound on the one-at-a-time plain-path baseline run")
     ap.add_argument("--rays", type=int, default=1 << 24, help="rays per set of the traversal microbenchmark")
+    ap.add_argument("--elems", type=int, default=1 << 26, help="compact: triples per codec launch")
     ap.add_argument("--level", type=int, default=8, help="icosphere subdivision level of mesh_stress")
     ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (profiling on smaller cases)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
@@ -746,6 +747,151 @@ def run_traversal(args, set_names=("coherent", "incoherent"), config_names=None,
     return line
 
 
+# ---------------------------------------------------------------- compact codecs
+COMPACT_CODECS = [("fluv32", "encode"), ("oct32", "encode"), ("oct32_precise", "encode"), ("unsigned32", "encode"),
+                  ("unsigned40", "encode"), ("signed48", "encode"), ("fluv32", "decode"), ("oct32", "decode"),
+                  ("unsigned32", "decode"), ("unsigned40", "decode"), ("signed48", "decode")]
+
+
+def cpu_compact_sample(fmts, xyz, codes, target_seconds):
+    """The oracle's codecs on a bounded sample: elements per second of each
+    codec on one host thread (the crate's codecs are scalar functions)."""
+    import numpy as np
+    import oracle
+    L = oracle.lib()
+    out = {}
+    per = max(0.05, target_seconds / len(COMPACT_CODECS))
+    for name, op in COMPACT_CODECS:
+        fmt, size = fmts[name]
+        n, done, t0 = 1 << 16, 0, time.perf_counter()
+        buf = np.zeros(n * max(size, 12), np.uint8)
+        while time.perf_counter() - t0 < per:
+            if op == "encode":
+                L.psyo_compact_encode(fmt, xyz.ctypes.data, n, buf.ctypes.data, None)
+            else:
+                L.psyo_compact_decode(fmt, codes[name].ctypes.data, n, buf.ctypes.data)
+            done += n
+        out["%s_%s" % (name, op)] = done / (time.perf_counter() - t0)
+    return out
+
+
+def run_compact(args):
+    """The `compact` crate's codecs (sub_crates/compact) on the GPU: each
+    codec launched on --elems seeded triples (or their codes) resident in HBM,
+    larger than L2; per codec the CUDA-event time per launch, M elements/s and
+    algorithmic GB/s (12-byte triple + code per element) against the
+    measured HBM copy bandwidth.  Every launch's output is compared with the
+    oracle on a 1M-element sample.  The headline is fluv32 encode (the codec
+    the renderer itself uses for colours); e2e is the same codec through the
+    C ABI with the triples in pinned host memory and the codes copied back."""
+    import numpy as np
+    import torch
+    import oracle
+    from psychopath_gb300 import abi, build, compact
+    from tests import compact_cases as cc
+    torch.cuda.set_device(0)
+    build.build()
+    L = oracle.lib()
+    peaks_path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    peak = float(json.load(open(peaks_path))["hbm_gbs"]) if os.path.exists(peaks_path) else 6800.0
+    n = args.elems
+    fmts = {name: (cc.F[name], cc.SIZE[cc.F[name]]) for name in cc.F}
+    host = cc.random_triples(n, seed=2025)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    d_xyz = torch.from_numpy(host.view(np.uint8).reshape(-1)).cuda()
+    d_codes = {name: torch.empty(n * size, dtype=torch.uint8, device="cuda") for name, (_, size) in fmts.items()}
+    d_out = torch.empty(n * 12, dtype=torch.uint8, device="cuda")
+    d_bad = torch.zeros(1, dtype=torch.int32, device="cuda")
+    sample = min(n, 1 << 20)
+    res, launches = {}, 0
+    clocks = ClockSampler(0)
+    clocks.start()
+    for name, op in COMPACT_CODECS:
+        fmt, size = fmts[name]
+
+        def launch():
+            if op == "encode":
+                compact.encode_device(fmt, d_xyz.data_ptr(), n, d_codes[name].data_ptr(), d_bad.data_ptr(),
+                                      stream.cuda_stream)
+            else:
+                compact.decode_device(fmt, d_codes[name].data_ptr(), n, d_out.data_ptr(), stream.cuda_stream)
+        for _ in range(max(3, args.warmup)):
+            launch()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        launches += args.steps
+        sec = e0.elapsed_time(e1) / 1e3 / args.steps
+        # parity on the first `sample` elements against the oracle
+        if op == "encode":
+            got = d_codes[name][:sample * size].cpu().numpy()
+            want = np.zeros(sample * size, np.uint8)
+            L.psyo_compact_encode(fmt, host.ctypes.data, sample, want.ctypes.data, None)
+            ok = bool(np.array_equal(got, want))
+        else:
+            codes = d_codes[name][:sample * size].cpu().numpy()
+            got = d_out[:sample * 12].cpu().numpy().view(np.float32)
+            want = np.zeros(sample * 3, np.float32)
+            L.psyo_compact_decode(fmt, codes.ctypes.data, sample, want.ctypes.data)
+            ok = bool(np.all((np.isnan(got) & np.isnan(want)) | (got.view(np.uint32) == want.view(np.uint32))))
+        gbs = n * (12 + size) / sec / 1e9
+        res["%s_%s" % (name, op)] = {"ms_per_launch": sec * 1e3, "melem_per_s": n / sec / 1e6, "achieved_gbs": gbs,
+                                     "frac": gbs / peak, "bit_exact_vs_oracle": ok, "bytes_per_elem": 12 + size}
+    clk = clocks.stop()
+    # e2e: fluv32 encode through the C ABI from pinned host memory, codes back
+    pinned_in = torch.from_numpy(host.view(np.uint8).reshape(-1)).pin_memory()
+    pinned_out = torch.empty(n * 4, dtype=torch.uint8).pin_memory()
+    fmt = abi.PSY_COMPACT_FLUV32
+
+    def e2e_step():
+        d_xyz.copy_(pinned_in, non_blocking=True)
+        compact.encode_device(fmt, d_xyz.data_ptr(), n, d_codes["fluv32"].data_ptr(), None, stream.cuda_stream)
+        pinned_out.copy_(d_codes["fluv32"], non_blocking=True)
+    for _ in range(max(3, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_sec = e0.elapsed_time(e1) / 1e3 / args.steps
+    want = np.zeros(sample * 4, np.uint8)
+    L.psyo_compact_encode(fmt, host.ctypes.data, sample, want.ctypes.data, None)
+    e2e_ok = bool(np.array_equal(pinned_out[:sample * 4].numpy(), want))
+    cpu = None
+    if not args.no_cpu_baseline:
+        codes = {name: d_codes[name][:(1 << 16) * size].cpu().numpy() for name, (_, size) in fmts.items()}
+        cpu = cpu_compact_sample(fmts, host[:1 << 16].copy(), codes, min(args.cpu_seconds, 11.0))
+    head = res["fluv32_encode"]
+    line = {"metric": "fluv32 encode Melem/s", "value": head["melem_per_s"], "unit": "Melem/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": head["ms_per_launch"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/u8",
+            "data": "synthetic (seeded f32 triples over the whole exponent range, special values mixed in)",
+            "config": {"workload": "compact codecs: %d triples per launch" % n,
+                       "l2": "inputs (%d MB of triples) larger than L2" % (n * 12 // 2 ** 20)},
+            "e2e": {"value": n / e2e_sec / 1e6, "unit": "Melem/s", "h2d_bytes_per_step": n * 12,
+                    "d2h_bytes_per_step": n * 4, "bit_exact_vs_oracle": e2e_ok},
+            "gpu_launches": launches, "clocks": clk,
+            "roofline": {"bound": "hbm", "achieved": head["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": head["frac"], "traffic": None, "kernel": "k_compact<Encode<FLUV32>>",
+                         "note": "16 algorithmic bytes per element (12-byte triple in, 4-byte code out) over the "
+                                 "kernel's CUDA-event time"},
+            "codecs": res}
+    if cpu is not None:
+        line["cpu_baseline"] = {"value": cpu["fluv32_encode"] / 1e6, "unit": "Melem/s", "cores": 1, "kind": "port",
+                                "sample": "the oracle's codecs on 65,536 elements, repeated for about 1 s each",
+                                "codecs_melem_per_s": {k: v / 1e6 for k, v in cpu.items()}}
+    print(json.dumps(line), flush=True)
+    return line
+
+
 # ---------------------------------------------------------------- serving
 def serving_requests(duration, rate, seed=2024):
     """Poisson arrivals: (t, scene, resolution, spp, seed) with the scene
@@ -1009,6 +1155,8 @@ def main():
         return run_serving(args)
     if args.workload == "parity":
         return run_parity(args)
+    if args.workload == "compact":
+        return run_compact(args)
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -324,6 +324,74 @@ int psy_xyz_to_srgb8(const float *d_xyz, uint32_t width, uint32_t height, uint8_
  * device memory, kept until exit). */
 int psy_halton_samples(uint32_t dimension, const uint32_t *d_indices, uint32_t n, float *d_out, void *stream);
 
+/* ------------------------------------------------------- compact codecs */
+
+/* Batch forms of the `compact` crate's encodings (sub_crates/compact), bit
+ * for bit.  Encoders read n (x, y, z) f32 triples (12 bytes each) and write
+ * n codes of psy_compact_element_size() bytes, packed; decoders do the
+ * reverse.  Multi-byte codes are little-endian, as the crate's
+ * to_ne_bytes / u64_to_bytes give on little-endian hosts. */
+#define PSY_COMPACT_FLUV32 0        /* fluv::fluv32 (fluv/fluv32.rs:76-170): XYZ colour, u32 */
+#define PSY_COMPACT_OCT32 1         /* unit_vec::oct32 encode/decode (unit_vec/oct32.rs:15-70), u32 */
+#define PSY_COMPACT_OCT32_PRECISE 2 /* oct32::encode_precise (:24-61); decodes as PSY_COMPACT_OCT32 */
+#define PSY_COMPACT_UNSIGNED32 3    /* shared_exp::unsigned32 (shared_exp/unsigned32.rs:36-85), u32 */
+#define PSY_COMPACT_UNSIGNED40 4    /* shared_exp::unsigned40 (shared_exp/unsigned40.rs:36-120), 5 bytes */
+#define PSY_COMPACT_SIGNED48 5      /* shared_exp::signed48 (shared_exp/signed48.rs:48-144), 6 bytes */
+
+/* Bytes per code of `format`; PSY_E_INVALID for an unknown format. */
+int psy_compact_element_size(uint32_t format, uint32_t *bytes);
+
+/* Encode n triples of d_xyz (device, 3*n floats) into d_out (device, n codes).
+ * The crate's encoders assert their domain in debug builds (fluv32,
+ * unsigned32, unsigned40: no negative or NaN component; signed48: no NaN;
+ * oct32: none) and write the release build's code otherwise; here every
+ * element gets the release build's code and, when d_invalid (a device u32)
+ * is not NULL, the number of elements outside the domain is added to it.
+ * Asynchronous on `stream` (NULL: the legacy default stream). */
+int psy_compact_encode(uint32_t format, const float *d_xyz, uint32_t n, void *d_out, uint32_t *d_invalid,
+                       void *stream);
+
+/* Decode n codes of d_in (device) into d_xyz (device, 3*n floats).  Every
+ * bit pattern decodes (the crate's decoders cannot fail). */
+int psy_compact_decode(uint32_t format, const void *d_in, uint32_t n, float *d_xyz, void *stream);
+
+/* fluv32::decode_yuv (fluv/fluv32.rs:160-170): Y and the raw u', v' bytes. */
+typedef struct PsyYuv {
+    float y;
+    uint8_t u, v;
+    uint8_t pad[2]; /* written as 0 */
+} PsyYuv;
+int psy_fluv32_decode_yuv(const uint32_t *d_in, uint32_t n, PsyYuv *d_yuv, void *stream);
+
+/* Colour compression as Color::write_compressed / Color::from_compressed
+ * (src/color.rs:144-249): 5 bytes per colour, a discriminant byte (0 XYZ,
+ * 1 blackbody, 2 temperature) then the fluv32 code of the XYZ triple, or
+ * the temperature as a saturating u16 and the factor as an IEEE half (round
+ * to nearest even), both little-endian.  d_out / d_in hold 5*n bytes.
+ * d_invalid (optional device u32) counts XYZ colours outside fluv32's domain
+ * and unknown kinds on compression, and unknown discriminants on
+ * decompression (the reference's unreachable!()); such records are
+ * written as zeros. */
+int psy_color_compress(const PsyColor *d_colors, uint32_t n, uint8_t *d_out, uint32_t *d_invalid, void *stream);
+int psy_color_decompress(const uint8_t *d_in, uint32_t n, PsyColor *d_colors, uint32_t *d_invalid, void *stream);
+
+/* Closure compression as SurfaceClosure::write_compressed / from_compressed
+ * (src/shading/surface_closure.rs:157-253), for closures given as shader
+ * descriptions (kind, colour, roughness, fresnel): a discriminant byte
+ * (Lambert 0, GGX 1, Emit 2); a GGX closure then carries roughness and
+ * fresnel, each clamped to [0, 1] and stored as a truncated u16 fraction of
+ * 65535, little-endian; the compressed colour follows (6 bytes in all, 10
+ * for GGX).  Record i starts at byte i*stride, as MicropolyBatch packs them
+ * (src/surface/micropoly_batch.rs:322-332); bytes past a record's end are
+ * left alone.  stride < 6 returns PSY_E_INVALID.  d_invalid (optional)
+ * counts records that do not fit the stride (the reference panics) -- left
+ * unwritten on compression, decoded as a black Emit closure on
+ * decompression -- and the colour errors of psy_color_compress. */
+int psy_closure_compress(const PsyShaderDesc *d_closures, uint32_t n, uint32_t stride, uint8_t *d_out,
+                         uint32_t *d_invalid, void *stream);
+int psy_closure_decompress(const uint8_t *d_in, uint32_t n, uint32_t stride, PsyShaderDesc *d_closures,
+                           uint32_t *d_invalid, void *stream);
+
 /* Render one bucket without allocating device memory.  This call has no
  * counterpart in the reference: it exists for hosts that cannot call
  * cudaMalloc once they are running -- for example a process whose device

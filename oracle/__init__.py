@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libpsy_oracle.so")
 LIB64_PATH = os.path.join(BUILD_DIR, "libpsy_oracle64.so")
-SOURCES = ["psy_oracle.cpp", "oracle_sobol.cpp", "oracle_halton.cpp"]
+SOURCES = ["psy_oracle.cpp", "oracle_sobol.cpp", "oracle_halton.cpp", "oracle_compact.cpp"]
 HEADERS = ["psy_oracle.h", "oracle_math.h", "oracle_shading.h"]
 
 
@@ -119,5 +119,16 @@ def lib():
         L.psyo_increment_ulp_check.restype = C.c_int
         L.psyo_halton_sample.restype = C.c_int
         L.psyo_halton_sample.argtypes = [u32, u32, fp]
+        for n in ("psyo_compact_encode", "psyo_color_compress", "psyo_color_decompress"):
+            getattr(L, n).argtypes = [u32, vp, u32, vp, vp] if n == "psyo_compact_encode" else [vp, u32, vp, vp]
+        L.psyo_compact_decode.argtypes = [u32, vp, u32, vp]
+        L.psyo_signed48_decode_u64.argtypes = [C.c_uint64, fp]
+        L.psyo_fluv32_decode_yuv.argtypes = [vp, u32, vp]
+        L.psyo_f16_from_f32.restype = u32
+        L.psyo_f16_from_f32.argtypes = [f32]
+        L.psyo_f16_to_f32.restype = f32
+        L.psyo_f16_to_f32.argtypes = [u32]
+        L.psyo_closure_compress.argtypes = [vp, u32, u32, vp, vp]
+        L.psyo_closure_decompress.argtypes = [vp, u32, u32, vp, vp]
         _lib = L
     return _lib

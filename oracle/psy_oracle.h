@@ -89,6 +89,21 @@ int psyo_light_tree_info(PsyoScene *s, uint32_t *nodes, uint32_t *leaves, uint32
  * oracle_halton.cpp; -1 for dimension >= 128. */
 int psyo_halton_sample(uint32_t index, uint32_t dimension, float *out);
 
+/* The `compact` crate's encodings and the colour / closure byte formats
+ * (oracle_compact.cpp), with the GPU library's batch signatures; -1 for an
+ * unknown format or a stride below 6.  *invalid receives the number of
+ * elements outside the format's domain. */
+int psyo_compact_encode(uint32_t format, const float *xyz, uint32_t n, uint8_t *out, uint32_t *invalid);
+int psyo_compact_decode(uint32_t format, const uint8_t *in, uint32_t n, float *xyz);
+void psyo_signed48_decode_u64(uint64_t t, float *out);
+void psyo_fluv32_decode_yuv(const uint32_t *in, uint32_t n, PsyYuv *out);
+uint32_t psyo_f16_from_f32(float f);
+float psyo_f16_to_f32(uint32_t h);
+int psyo_color_compress(const PsyColor *c, uint32_t n, uint8_t *out, uint32_t *invalid);
+int psyo_color_decompress(const uint8_t *in, uint32_t n, PsyColor *c, uint32_t *invalid);
+int psyo_closure_compress(const PsyShaderDesc *s, uint32_t n, uint32_t stride, uint8_t *out, uint32_t *invalid);
+int psyo_closure_decompress(const uint8_t *in, uint32_t n, uint32_t stride, PsyShaderDesc *s, uint32_t *invalid);
+
 #ifdef __cplusplus
 }
 #endif

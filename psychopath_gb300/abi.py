@@ -25,6 +25,8 @@ PSY_HIT_MISS, PSY_HIT_OCCLUDE, PSY_HIT_SURFACE, PSY_HIT_LIGHT = 0, 1, 2, 3
 PSY_REQ_QUEUED, PSY_REQ_RUNNING, PSY_REQ_DONE, PSY_REQ_CANCELLED, PSY_REQ_FAILED = 0, 1, 2, 3, 4
 PSY_SCHED_FIFO, PSY_SCHED_SHORTEST = 0, 1
 PSY_TUNE_GRID_RESIDENT = 0xFFFFFFFF
+PSY_COMPACT_FLUV32, PSY_COMPACT_OCT32, PSY_COMPACT_OCT32_PRECISE = 0, 1, 2
+PSY_COMPACT_UNSIGNED32, PSY_COMPACT_UNSIGNED40, PSY_COMPACT_SIGNED48 = 3, 4, 5
 
 _fp = C.POINTER(C.c_float)
 _up = C.POINTER(C.c_uint32)
@@ -36,6 +38,28 @@ class PsyColor(C.Structure):
 
 class PsyShaderDesc(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("color", PsyColor), ("roughness", C.c_float), ("fresnel", C.c_float)]
+
+
+class PsyYuv(C.Structure):
+    _fields_ = [("y", C.c_float), ("u", C.c_uint8), ("v", C.c_uint8), ("pad", C.c_uint8 * 2)]
+
+
+def color_dtype():
+    """numpy mirror of PsyColor (16 bytes)."""
+    import numpy as np
+    return np.dtype([("kind", "<u4"), ("v", "<f4", (3,))])
+
+
+def shader_dtype():
+    """numpy mirror of PsyShaderDesc (28 bytes)."""
+    import numpy as np
+    return np.dtype([("kind", "<u4"), ("color", color_dtype()), ("roughness", "<f4"), ("fresnel", "<f4")])
+
+
+def yuv_dtype():
+    """numpy mirror of PsyYuv (8 bytes)."""
+    import numpy as np
+    return np.dtype([("y", "<f4"), ("u", "u1"), ("v", "u1"), ("pad", "u1", (2,))])
 
 
 class PsyObjectDesc(C.Structure):

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(OUT_DIR, "libpsy_gpu.so")
 SOURCES = ["kernels.cu", "trace_kernels.cu", "scene_build.cu", "capi.cu", "server.cu", "bvh_build.cu",
-           "radix_sort.cu", "halton.cu", "wave_f32.cu"]
+           "radix_sort.cu", "halton.cu", "wave_f32.cu", "compact.cu"]
 FMAD = {"wave_f32.cu": "--fmad=true"}  # per-source override of --fmad=false
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

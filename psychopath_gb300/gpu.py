@@ -25,7 +25,9 @@ EXPORTED = [
     "psy_rays_traced", "psy_render_bucket", "psy_render_image_device", "psy_render_image", "psy_last_error",
     "psy_version", "psy_render_bucket_noalloc", "psy_server_create", "psy_server_add_scene", "psy_submit",
     "psy_poll", "psy_wait", "psy_cancel", "psy_server_stats", "psy_server_destroy", "psy_autotune",
-    "psy_xyz_to_srgb8", "psy_halton_samples", "psy_render_rows_device",
+    "psy_xyz_to_srgb8", "psy_halton_samples", "psy_render_rows_device", "psy_compact_element_size",
+    "psy_compact_encode", "psy_compact_decode", "psy_fluv32_decode_yuv", "psy_color_compress",
+    "psy_color_decompress", "psy_closure_compress", "psy_closure_decompress",
 ]
 
 
@@ -89,6 +91,14 @@ def lib(path=None):
     L.psy_autotune.argtypes = [vp, vp, vp]
     L.psy_xyz_to_srgb8.argtypes = [vp, u32, u32, vp, vp]
     L.psy_halton_samples.argtypes = [u32, vp, u32, vp, vp]
+    L.psy_compact_element_size.argtypes = [u32, C.POINTER(u32)]
+    L.psy_compact_encode.argtypes = [u32, vp, u32, vp, vp, vp]
+    L.psy_compact_decode.argtypes = [u32, vp, u32, vp, vp]
+    L.psy_fluv32_decode_yuv.argtypes = [vp, u32, vp, vp]
+    L.psy_color_compress.argtypes = [vp, u32, vp, vp, vp]
+    L.psy_color_decompress.argtypes = [vp, u32, vp, vp, vp]
+    L.psy_closure_compress.argtypes = [vp, u32, u32, vp, vp, vp]
+    L.psy_closure_decompress.argtypes = [vp, u32, u32, vp, vp, vp]
     _lib = L
     return L
 
