@@ -347,7 +347,9 @@ int psy_compact_element_size(uint32_t format, uint32_t *bytes);
  * oct32: none) and write the release build's code otherwise; here every
  * element gets the release build's code and, when d_invalid (a device u32)
  * is not NULL, the number of elements outside the domain is added to it.
- * Asynchronous on `stream` (NULL: the legacy default stream). */
+ * Asynchronous on `stream` (NULL: the legacy default stream).  Buffers may
+ * have any alignment (16-byte aligned ones take the vector path); d_invalid
+ * must be 4-byte aligned (else PSY_E_INVALID). */
 int psy_compact_encode(uint32_t format, const float *d_xyz, uint32_t n, void *d_out, uint32_t *d_invalid,
                        void *stream);
 
@@ -383,7 +385,8 @@ int psy_color_decompress(const uint8_t *d_in, uint32_t n, PsyColor *d_colors, ui
  * 65535, little-endian; the compressed colour follows (6 bytes in all, 10
  * for GGX).  Record i starts at byte i*stride, as MicropolyBatch packs them
  * (src/surface/micropoly_batch.rs:322-332); bytes past a record's end are
- * left alone.  stride < 6 returns PSY_E_INVALID.  d_invalid (optional)
+ * left alone.  stride < 6, or PsyShaderDesc arrays or d_invalid that are
+ * not 4-byte aligned, return PSY_E_INVALID.  d_invalid (optional)
  * counts records that do not fit the stride (the reference panics) -- left
  * unwritten on compression, decoded as a black Emit closure on
  * decompression -- and the colour errors of psy_color_compress. */

@@ -256,10 +256,13 @@ __global__ void __launch_bounds__(kThreads) k_compact(const uint8_t *__restrict_
     }
 }
 
+bool misaligned(const void *p, uintptr_t a) { return ((uintptr_t)p & (a - 1)) != 0; }
+
 template <class Op>
 int launch(const void *in, void *out, uint32_t n, uint32_t *invalid, void *stream, const char *what) {
     if (n == 0) return PSY_OK;
     if (!in || !out) return psy_fail(PSY_E_INVALID, std::string(what) + ": null buffer");
+    if (misaligned(invalid, 4)) return psy_fail(PSY_E_INVALID, std::string(what) + ": counter not 4-byte aligned");
     const bool vin = ((uintptr_t)in & 15u) == 0, vout = ((uintptr_t)out & 15u) == 0;
     const uint32_t blocks = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
     k_compact<Op><<<blocks, kThreads, 0, (cudaStream_t)stream>>>(static_cast<const uint8_t *>(in),
@@ -416,6 +419,8 @@ extern "C" int psy_closure_compress(const PsyShaderDesc *d_closures, uint32_t n,
     if (stride < 6) return psy_fail(PSY_E_INVALID, "closure compress: stride below the 6-byte minimum record");
     if (n == 0) return PSY_OK;
     if (!d_closures || !d_out) return psy_fail(PSY_E_INVALID, "closure compress: null buffer");
+    if (misaligned(d_closures, 4) || misaligned(d_invalid, 4))
+        return psy_fail(PSY_E_INVALID, "closure compress: closures or counter not 4-byte aligned");
     k_closure_compress<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_closures, n, stride, d_out, d_invalid);
     if (cudaGetLastError() != cudaSuccess) return psy_fail(PSY_E_CUDA, "closure compress: launch failed");
     return PSY_OK;
@@ -427,6 +432,8 @@ extern "C" int psy_closure_decompress(const uint8_t *d_in, uint32_t n, uint32_t 
     if (stride < 6) return psy_fail(PSY_E_INVALID, "closure decompress: stride below the 6-byte minimum record");
     if (n == 0) return PSY_OK;
     if (!d_in || !d_closures) return psy_fail(PSY_E_INVALID, "closure decompress: null buffer");
+    if (misaligned(d_closures, 4) || misaligned(d_invalid, 4))
+        return psy_fail(PSY_E_INVALID, "closure decompress: closures or counter not 4-byte aligned");
     k_closure_decompress<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_in, n, stride, d_closures, d_invalid);
     if (cudaGetLastError() != cudaSuccess) return psy_fail(PSY_E_CUDA, "closure decompress: launch failed");
     return PSY_OK;
