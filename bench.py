@@ -796,10 +796,17 @@ def run_compact(args):
     peak = float(json.load(open(peaks_path))["hbm_gbs"]) if os.path.exists(peaks_path) else 6800.0
     n = args.elems
     fmts = {name: (cc.F[name], cc.SIZE[cc.F[name]]) for name in cc.F}
+    # inputs in each format's domain (what the renderer stores: no NaN; XYZ
+    # colours and the unsigned formats non-negative); the out-of-domain
+    # paths are covered by the tests
     host = cc.random_triples(n, seed=2025)
+    host[np.isnan(host)] = 0.0
+    host_pos = np.abs(host)
+    unsigned = ("fluv32", "unsigned32", "unsigned40")
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     d_xyz = torch.from_numpy(host.view(np.uint8).reshape(-1)).cuda()
+    d_pos = torch.from_numpy(host_pos.view(np.uint8).reshape(-1)).cuda()
     d_codes = {name: torch.empty(n * size, dtype=torch.uint8, device="cuda") for name, (_, size) in fmts.items()}
     d_out = torch.empty(n * 12, dtype=torch.uint8, device="cuda")
     d_bad = torch.zeros(1, dtype=torch.int32, device="cuda")
@@ -810,9 +817,11 @@ def run_compact(args):
     for name, op in COMPACT_CODECS:
         fmt, size = fmts[name]
 
+        src, src_host = (d_pos, host_pos) if name in unsigned else (d_xyz, host)
+
         def launch():
             if op == "encode":
-                compact.encode_device(fmt, d_xyz.data_ptr(), n, d_codes[name].data_ptr(), d_bad.data_ptr(),
+                compact.encode_device(fmt, src.data_ptr(), n, d_codes[name].data_ptr(), d_bad.data_ptr(),
                                       stream.cuda_stream)
             else:
                 compact.decode_device(fmt, d_codes[name].data_ptr(), n, d_out.data_ptr(), stream.cuda_stream)
@@ -831,7 +840,7 @@ def run_compact(args):
         if op == "encode":
             got = d_codes[name][:sample * size].cpu().numpy()
             want = np.zeros(sample * size, np.uint8)
-            L.psyo_compact_encode(fmt, host.ctypes.data, sample, want.ctypes.data, None)
+            L.psyo_compact_encode(fmt, src_host.ctypes.data, sample, want.ctypes.data, None)
             ok = bool(np.array_equal(got, want))
         else:
             codes = d_codes[name][:sample * size].cpu().numpy()
@@ -843,14 +852,15 @@ def run_compact(args):
         res["%s_%s" % (name, op)] = {"ms_per_launch": sec * 1e3, "melem_per_s": n / sec / 1e6, "achieved_gbs": gbs,
                                      "frac": gbs / peak, "bit_exact_vs_oracle": ok, "bytes_per_elem": 12 + size}
     clk = clocks.stop()
+    invalid_total = int(d_bad.item())
     # e2e: fluv32 encode through the C ABI from pinned host memory, codes back
-    pinned_in = torch.from_numpy(host.view(np.uint8).reshape(-1)).pin_memory()
+    pinned_in = torch.from_numpy(host_pos.view(np.uint8).reshape(-1)).pin_memory()
     pinned_out = torch.empty(n * 4, dtype=torch.uint8).pin_memory()
     fmt = abi.PSY_COMPACT_FLUV32
 
     def e2e_step():
-        d_xyz.copy_(pinned_in, non_blocking=True)
-        compact.encode_device(fmt, d_xyz.data_ptr(), n, d_codes["fluv32"].data_ptr(), None, stream.cuda_stream)
+        d_pos.copy_(pinned_in, non_blocking=True)
+        compact.encode_device(fmt, d_pos.data_ptr(), n, d_codes["fluv32"].data_ptr(), None, stream.cuda_stream)
         pinned_out.copy_(d_codes["fluv32"], non_blocking=True)
     for _ in range(max(3, args.warmup)):
         e2e_step()
@@ -863,19 +873,21 @@ def run_compact(args):
     torch.cuda.synchronize()
     e2e_sec = e0.elapsed_time(e1) / 1e3 / args.steps
     want = np.zeros(sample * 4, np.uint8)
-    L.psyo_compact_encode(fmt, host.ctypes.data, sample, want.ctypes.data, None)
+    L.psyo_compact_encode(fmt, host_pos.ctypes.data, sample, want.ctypes.data, None)
     e2e_ok = bool(np.array_equal(pinned_out[:sample * 4].numpy(), want))
     cpu = None
     if not args.no_cpu_baseline:
         codes = {name: d_codes[name][:(1 << 16) * size].cpu().numpy() for name, (_, size) in fmts.items()}
-        cpu = cpu_compact_sample(fmts, host[:1 << 16].copy(), codes, min(args.cpu_seconds, 11.0))
+        cpu = cpu_compact_sample(fmts, host_pos[:1 << 16].copy(), codes, min(args.cpu_seconds, 11.0))
     head = res["fluv32_encode"]
     line = {"metric": "fluv32 encode Melem/s", "value": head["melem_per_s"], "unit": "Melem/s", "n_gpus": 1,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": head["ms_per_launch"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/u8",
             "data": "synthetic (seeded f32 triples over the whole exponent range, special values mixed in)",
             "config": {"workload": "compact codecs: %d triples per launch" % n,
-                       "l2": "inputs (%d MB of triples) larger than L2" % (n * 12 // 2 ** 20)},
+                       "l2": "inputs (%d MB of triples) larger than L2" % (n * 12 // 2 ** 20),
+                       "inputs": "in each format's domain (no NaN; non-negative for fluv32 and the unsigned "
+                                 "formats)", "invalid_inputs_counted": invalid_total},
             "e2e": {"value": n / e2e_sec / 1e6, "unit": "Melem/s", "h2d_bytes_per_step": n * 12,
                     "d2h_bytes_per_step": n * 4, "bit_exact_vs_oracle": e2e_ok},
             "gpu_launches": launches, "clocks": clk,

@@ -95,12 +95,12 @@ def decode(fmt, codes):
     import torch
     size = element_size(fmt)
     if size == 4:
-        c = np.ascontiguousarray(np.asarray(codes, dtype=np.uint64).astype(np.uint32))
+        c = np.asarray(codes, dtype=np.uint64).astype(np.uint32)  # keeps a scalar's shape ()
         lead = c.shape
     else:
         if isinstance(codes, (bytes, bytearray)):
             codes = np.frombuffer(bytes(codes), dtype=np.uint8)
-        c = np.ascontiguousarray(np.asarray(codes, dtype=np.uint8))
+        c = np.asarray(codes, dtype=np.uint8)
         if c.ndim == 0 or c.shape[-1] != size:
             raise ValueError("decode: the last axis must hold %d bytes" % size)
         lead = c.shape[:-1]
@@ -135,7 +135,7 @@ class _Fluv32(_Format):
     def decode_yuv(self, code):
         """(Y, u', v') of each code: Y as float32, the chroma as the raw bytes."""
         import torch
-        c = np.ascontiguousarray(np.asarray(code, dtype=np.uint64).astype(np.uint32))
+        c = np.asarray(code, dtype=np.uint64).astype(np.uint32)  # keeps a scalar's shape ()
         n = c.size
         d_in = _to_device(c)
         d_out = torch.empty(max(1, 8 * n), dtype=torch.uint8, device="cuda")

@@ -66,62 +66,69 @@ __device__ __forceinline__ uint64_t ld_le(const uint8_t *p, int bytes) {
 __device__ __forceinline__ bool nonneg(float3 v) { return v.x >= 0.0f && v.y >= 0.0f && v.z >= 0.0f; }
 __device__ __forceinline__ bool not_nan(float3 v) { return !isnan(v.x) && !isnan(v.y) && !isnan(v.z); }
 
-// One element: input bytes -> output bytes; returns 1 if the element is
-// outside the format's domain.
+// Element operations.  A packing op (kPack) reads one input record from the
+// staged tile and returns its code (the low kOut bytes of a u64, as the
+// crate lays them out little-endian), counting an element outside the
+// format's domain into `bad`; an unpacking op gets one code and writes the
+// output record.
 template <int F>
 struct Encode;
 template <>
 struct Encode<PSY_COMPACT_FLUV32> {
+    static constexpr bool kPack = true;
     static constexpr int kIn = 12, kOut = 4;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
+    __device__ static uint64_t run(const uint8_t *i, uint32_t &bad) {
         const float3 v = ld3(i);
-        *reinterpret_cast<uint32_t *>(o) = psyc::fluv32_encode(v.x, v.y, v.z);
-        return !nonneg(v);
+        bad += !nonneg(v);
+        return psyc::fluv32_encode(v.x, v.y, v.z);
     }
 };
 template <>
 struct Encode<PSY_COMPACT_OCT32> {
+    static constexpr bool kPack = true;
     static constexpr int kIn = 12, kOut = 4;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
+    __device__ static uint64_t run(const uint8_t *i, uint32_t &) {
         const float3 v = ld3(i);
-        *reinterpret_cast<uint32_t *>(o) = psyc::oct32_encode(v.x, v.y, v.z);
-        return 0;
+        return psyc::oct32_encode(v.x, v.y, v.z);
     }
 };
 template <>
 struct Encode<PSY_COMPACT_OCT32_PRECISE> {
+    static constexpr bool kPack = true;
     static constexpr int kIn = 12, kOut = 4;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
+    __device__ static uint64_t run(const uint8_t *i, uint32_t &) {
         const float3 v = ld3(i);
-        *reinterpret_cast<uint32_t *>(o) = psyc::oct32_encode_precise(v.x, v.y, v.z);
-        return 0;
+        return psyc::oct32_encode_precise(v.x, v.y, v.z);
     }
 };
 template <>
 struct Encode<PSY_COMPACT_UNSIGNED32> {
+    static constexpr bool kPack = true;
     static constexpr int kIn = 12, kOut = 4;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
+    __device__ static uint64_t run(const uint8_t *i, uint32_t &bad) {
         const float3 v = ld3(i);
-        *reinterpret_cast<uint32_t *>(o) = psyc::unsigned32_encode(v.x, v.y, v.z);
-        return !nonneg(v);
+        bad += !nonneg(v);
+        return psyc::unsigned32_encode(v.x, v.y, v.z);
     }
 };
 template <>
 struct Encode<PSY_COMPACT_UNSIGNED40> {
+    static constexpr bool kPack = true;
     static constexpr int kIn = 12, kOut = 5;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
+    __device__ static uint64_t run(const uint8_t *i, uint32_t &bad) {
         const float3 v = ld3(i);
-        st_le(o, psyc::unsigned40_encode(v.x, v.y, v.z), 5);
-        return !nonneg(v);
+        bad += !nonneg(v);
+        return psyc::unsigned40_encode(v.x, v.y, v.z);
     }
 };
 template <>
 struct Encode<PSY_COMPACT_SIGNED48> {
+    static constexpr bool kPack = true;
     static constexpr int kIn = 12, kOut = 6;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
+    __device__ static uint64_t run(const uint8_t *i, uint32_t &bad) {
         const float3 v = ld3(i);
-        st_le(o, psyc::signed48_encode(v.x, v.y, v.z), 6);
-        return !not_nan(v);
+        bad += !not_nan(v);
+        return psyc::signed48_encode(v.x, v.y, v.z);
     }
 };
 
@@ -129,49 +136,55 @@ template <int F>
 struct Decode;
 template <>
 struct Decode<PSY_COMPACT_FLUV32> {
+    static constexpr bool kPack = false;
     static constexpr int kIn = 4, kOut = 12;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
-        st3(o, psyc::fluv32_decode(*reinterpret_cast<const uint32_t *>(i)));
+    __device__ static uint32_t run(uint64_t c, uint8_t *o) {
+        st3(o, psyc::fluv32_decode((uint32_t)c));
         return 0;
     }
 };
 template <>
 struct Decode<PSY_COMPACT_OCT32> {
+    static constexpr bool kPack = false;
     static constexpr int kIn = 4, kOut = 12;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
-        st3(o, psyc::oct32_decode(*reinterpret_cast<const uint32_t *>(i)));
+    __device__ static uint32_t run(uint64_t c, uint8_t *o) {
+        st3(o, psyc::oct32_decode((uint32_t)c));
         return 0;
     }
 };
 template <>
 struct Decode<PSY_COMPACT_UNSIGNED32> {
+    static constexpr bool kPack = false;
     static constexpr int kIn = 4, kOut = 12;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
-        st3(o, psyc::unsigned32_decode(*reinterpret_cast<const uint32_t *>(i)));
+    __device__ static uint32_t run(uint64_t c, uint8_t *o) {
+        st3(o, psyc::unsigned32_decode((uint32_t)c));
         return 0;
     }
 };
 template <>
 struct Decode<PSY_COMPACT_UNSIGNED40> {
+    static constexpr bool kPack = false;
     static constexpr int kIn = 5, kOut = 12;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
-        st3(o, psyc::unsigned40_decode(ld_le(i, 5)));
+    __device__ static uint32_t run(uint64_t c, uint8_t *o) {
+        st3(o, psyc::unsigned40_decode(c));
         return 0;
     }
 };
 template <>
 struct Decode<PSY_COMPACT_SIGNED48> {
+    static constexpr bool kPack = false;
     static constexpr int kIn = 6, kOut = 12;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
-        st3(o, psyc::signed48_decode(ld_le(i, 6)));
+    __device__ static uint32_t run(uint64_t c, uint8_t *o) {
+        st3(o, psyc::signed48_decode(c));
         return 0;
     }
 };
 // fluv32 to Y plus the two chroma bytes (fluv32.rs decode_yuv, :160-170)
 struct DecodeYuv {
+    static constexpr bool kPack = false;
     static constexpr int kIn = 4, kOut = sizeof(PsyYuv);
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
-        const uint32_t c = *reinterpret_cast<const uint32_t *>(i);
+    __device__ static uint32_t run(uint64_t c64, uint8_t *o) {
+        const uint32_t c = (uint32_t)c64;
         PsyYuv r;
         r.y = psyc::fluv32_y(c);
         r.u = (uint8_t)(c >> 8);
@@ -184,26 +197,24 @@ struct DecodeYuv {
 
 // Colour (src/color.rs:144-249): one discriminant byte, then the fluv32 code
 // of an XYZ colour (native-endian u32), or a blackbody / temperature colour's
-// temperature as a saturating u16 and its factor as f16, little-endian.
-__device__ __forceinline__ uint32_t color_write(const PsyColor &c, uint8_t *o) {
+// temperature as a saturating u16 and its factor as f16, little-endian: a
+// 40-bit code, discriminant in the low byte.
+__device__ __forceinline__ uint64_t color_code(const PsyColor &c, uint32_t &bad) {
     if (c.kind == PSY_COLOR_XYZ) {
-        o[0] = 0;
-        st_le(o + 1, psyc::fluv32_encode(c.v[0], c.v[1], c.v[2]), 4);
-        return !nonneg(make_float3(c.v[0], c.v[1], c.v[2]));
+        bad += !nonneg(make_float3(c.v[0], c.v[1], c.v[2]));
+        return (uint64_t)psyc::fluv32_encode(c.v[0], c.v[1], c.v[2]) << 8;
     }
     if (c.kind == PSY_COLOR_BLACKBODY || c.kind == PSY_COLOR_TEMPERATURE) {
-        o[0] = (uint8_t)c.kind;
         const uint32_t t = psyc::sat_u32(fminf(c.v[0], 65535.0f));
-        st_le(o + 1, t | (psyc::f32_to_f16_bits(c.v[1]) << 16), 4);
-        return 0;
+        return c.kind | ((uint64_t)(t | (psyc::f32_to_f16_bits(c.v[1]) << 16)) << 8);
     }
-    st_le(o, 0, 5);
-    return 1;  // no such colour in the reference
+    bad += 1;  // no such colour in the reference: written as zeros
+    return 0;
 }
 
-__device__ __forceinline__ uint32_t color_read(const uint8_t *i, PsyColor &c) {
-    const uint32_t w = (uint32_t)ld_le(i + 1, 4);
-    if (i[0] == 0) {
+__device__ __forceinline__ uint32_t color_from_code(uint64_t code, PsyColor &c) {
+    const uint32_t tag = (uint32_t)code & 0xffu, w = (uint32_t)(code >> 8);
+    if (tag == 0) {
         const float3 v = psyc::fluv32_decode(w);
         c.kind = PSY_COLOR_XYZ;
         c.v[0] = v.x;
@@ -212,8 +223,8 @@ __device__ __forceinline__ uint32_t color_read(const uint8_t *i, PsyColor &c) {
         return 0;
     }
     c.v[2] = 0.0f;
-    if (i[0] == 1 || i[0] == 2) {
-        c.kind = i[0];
+    if (tag == 1 || tag == 2) {
+        c.kind = tag;
         c.v[0] = (float)(w & 0xffffu);
         c.v[1] = psyc::f16_bits_to_f32(w >> 16);
         return 0;
@@ -224,35 +235,83 @@ __device__ __forceinline__ uint32_t color_read(const uint8_t *i, PsyColor &c) {
 }
 
 struct ColorCompress {
+    static constexpr bool kPack = true;
     static constexpr int kIn = sizeof(PsyColor), kOut = 5;
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
-        return color_write(*reinterpret_cast<const PsyColor *>(i), o);
+    __device__ static uint64_t run(const uint8_t *i, uint32_t &bad) {
+        return color_code(*reinterpret_cast<const PsyColor *>(i), bad);
     }
 };
 struct ColorDecompress {
+    static constexpr bool kPack = false;
     static constexpr int kIn = 5, kOut = sizeof(PsyColor);
-    __device__ static uint32_t run(const uint8_t *i, uint8_t *o) {
-        return color_read(i, *reinterpret_cast<PsyColor *>(o));
-    }
+    __device__ static uint32_t run(uint64_t c, uint8_t *o) { return color_from_code(c, *reinterpret_cast<PsyColor *>(o)); }
 };
 
+// One tile of kTile elements per block: stage the input bytes, convert, and
+// write the output bytes back.  Packed 5- and 6-byte codes move between the
+// warps' registers and the staged tile as whole 32-bit words: a warp's 32
+// consecutive codes fill 8*kOut words, and each word is put together from
+// the (at most two) codes it overlaps, fetched by shuffle; a code is read
+// back from the two words it overlaps with a funnel shift.
 template <class Op>
 __global__ void __launch_bounds__(kThreads) k_compact(const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
                                                        uint32_t n, uint32_t *__restrict__ invalid, bool vin,
                                                        bool vout) {
     __shared__ __align__(16) uint8_t s_in[kTile * Op::kIn];
     __shared__ __align__(16) uint8_t s_out[kTile * Op::kOut];
+    __shared__ uint32_t s_bad[kThreads / 32];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint64_t first = (uint64_t)blockIdx.x * kTile;
     const uint32_t cnt = (uint32_t)min((uint64_t)kTile, (uint64_t)n - first);
     copy_bytes(s_in, in + first * Op::kIn, cnt * Op::kIn, vin);
     __syncthreads();
     uint32_t bad = 0;
-    for (uint32_t k = threadIdx.x; k < cnt; k += kThreads) bad += Op::run(s_in + k * Op::kIn, s_out + k * Op::kOut);
+    if constexpr (Op::kPack) {
+        for (uint32_t base = warp * 32; base < cnt; base += kThreads) {  // warp-uniform bound
+            const uint32_t k = base + lane;
+            const uint64_t code = k < cnt ? Op::run(s_in + k * Op::kIn, bad) : 0;
+            if constexpr (Op::kOut == 4) {
+                if (k < cnt) reinterpret_cast<uint32_t *>(s_out)[k] = (uint32_t)code;
+            } else {
+                uint32_t *wout = reinterpret_cast<uint32_t *>(s_out + base * Op::kOut);
+                constexpr uint32_t kWords = 8 * Op::kOut;  // words of 32 codes
+#pragma unroll
+                for (uint32_t j = 0; j < 2; j++) {
+                    const uint32_t w = lane + 32 * j, b = 4 * w, e = b / Op::kOut, p = b - e * Op::kOut;
+                    const uint64_t c0 = __shfl_sync(0xffffffffu, code, min(e, 31u));
+                    const uint64_t c1 = __shfl_sync(0xffffffffu, code, min(e + 1, 31u));
+                    if (w < kWords) {
+                        uint64_t v = c0 >> (8 * p);
+                        if (p + 4 > (uint32_t)Op::kOut) v |= c1 << (8 * (Op::kOut - p));
+                        wout[w] = (uint32_t)v;
+                    }
+                }
+            }
+        }
+    } else {
+        for (uint32_t k = threadIdx.x; k < cnt; k += kThreads) {
+            uint64_t code;
+            if constexpr (Op::kIn == 4) {
+                code = reinterpret_cast<const uint32_t *>(s_in)[k];
+            } else {
+                const uint32_t b = k * Op::kIn, o = b & 3u;
+                const uint32_t *w = reinterpret_cast<const uint32_t *>(s_in) + (b >> 2);
+                const uint32_t w0 = w[0], w1 = w[1];
+                const uint32_t hi = (w1 >> (8 * o)) & ((1u << (8 * (Op::kIn - 4))) - 1u);
+                code = __funnelshift_r(w0, w1, 8 * o) | ((uint64_t)hi << 32);
+            }
+            bad += Op::run(code, s_out + k * Op::kOut);
+        }
+    }
+    bad = __reduce_add_sync(0xffffffffu, bad);
+    if (lane == 0) s_bad[warp] = bad;
     __syncthreads();
     copy_bytes(out + first * Op::kOut, s_out, cnt * Op::kOut, vout);
-    if (invalid) {
-        bad = __reduce_add_sync(0xffffffffu, bad);
-        if ((threadIdx.x & 31) == 0 && bad) atomicAdd(invalid, bad);
+    if (invalid && threadIdx.x == 0) {
+        uint32_t sum = 0;
+#pragma unroll
+        for (int i = 0; i < kThreads / 32; i++) sum += s_bad[i];
+        if (sum) atomicAdd(invalid, sum);  // one atomic per block at most
     }
 }
 
@@ -300,7 +359,7 @@ __global__ void k_closure_compress(const PsyShaderDesc *__restrict__ in, uint32_
                 st_le(o + 1, r | (f << 16), 4);
                 oc = o + 5;
             }
-            bad = color_write(s.color, oc);
+            st_le(oc, color_code(s.color, bad), 5);
         }
     }
     if (invalid) {
@@ -328,10 +387,10 @@ __global__ void k_closure_decompress(const uint8_t *__restrict__ in, uint32_t n,
             s.kind = PSY_SHADER_GGX;
             s.roughness = (float)(w & 0xffffu) * (1.0f / 65535.0f);
             s.fresnel = (float)(w >> 16) * (1.0f / 65535.0f);
-            bad = color_read(r + 5, s.color);
+            bad = color_from_code(ld_le(r + 5, 5), s.color);
         } else {
             s.kind = tag == 0 ? PSY_SHADER_LAMBERT : PSY_SHADER_EMIT;
-            bad = color_read(r + 1, s.color) | (tag > 2 ? 1u : 0u);
+            bad = color_from_code(ld_le(r + 1, 5), s.color) | (tag > 2 ? 1u : 0u);
         }
         out[i] = s;
     }

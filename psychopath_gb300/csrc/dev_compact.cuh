@@ -107,51 +107,94 @@ __device__ __forceinline__ double oct_dot64(float3 o, float x, float y, float z)
     return (ox * (double)x + oy * (double)y + oz * (double)z) / l;
 }
 
+// a*b - c*d with Kahan's FMA algorithm: within 2 ulps of the exact value
+// (Jeannerod, Louvet, Muller, "Further analysis of Kahan's algorithm for
+// the accurate computation of 2x2 determinants", Math. Comp. 82, 2013).
+__device__ __forceinline__ float diff_of_products(float a, float b, float c, float d) {
+    const float w = c * d;
+    const float e = fmaf(-c, d, w);  // w - c*d exactly
+    const float f = fmaf(a, b, -w);
+    return f + e;
+}
+
 // The floored grid point and its three upper neighbours; the one whose
 // decoded direction has the largest f64 cosine with the input wins (ties
 // keep the earlier candidate, a cosine <= 0 keeps the floored point).
 //
-// FP64 runs at a small fraction of the f32 rate on this GPU, so the
-// candidates are ranked with f32 cosines first.  Each candidate o is a
-// point of the octahedron (|o|_2 in [0.57, 1.02], |o_i| <= 1.01), so the f32
-// cosine is within 12 * 2^-24 * |v|_1 of the exact one, and the crate's f64
-// value within 1e-15 relative of it.  A comparison whose f32 margin exceeds
-// tol = 2^-16 * |v|_1 (20x the worst case of both errors) therefore has the
-// f64 comparison's outcome; anything closer, or an input whose |v|_1 is
-// outside [2^-100, 2^100] (f32 products could underflow into the margin or
-// overflow), is decided by the crate's own f64 cosines.  The selection
-// follows the crate's sequence exactly, so the code is bit-identical.
+// FP64 runs at a small fraction of the f32 rate on this GPU, and the
+// candidates' cosines differ only in second order (~1e-9), so they are
+// ranked by sin^2 of their angle to the input instead, a first-order
+// quantity computed in f32: |o x v|^2 / (|o|^2 |v|^2) with the cross product
+// by diff_of_products, v scaled by a power of two (exact) to |v|_1 in [1, 2).
+// Every rounding there is relative to the quantity itself, so each f32
+// sin^2 is within 15 * 2^-24 (relative) of the exact value.  With every
+// candidate within 30 degrees of the input and in front of it (cosine > 0:
+// the first candidate beats the floored point's 0), a larger cosine is a
+// smaller sin^2, and the difference of two cosines is at least half the
+// difference of their sin^2.  A comparison whose f32 sin^2 differ by more
+// than 2^-16 of the larger one (8x the sum of both errors) and by more than
+// 2^-40 (the cosines then differ by over 100x the f64 rounding of the
+// crate's cosines) therefore has the outcome of the crate's f64 comparison; any
+// other comparison, and any input outside this regime (|v|_1 outside
+// [2^-100, 2^100], NaN, infinity, a candidate over 30 degrees away), is
+// decided by the crate's own f64 cosines, in the crate's order, so the code
+// is bit-identical.
 __device__ __forceinline__ uint32_t oct32_encode_precise(float x, float y, float z) {
     float2 s = vec3_to_oct(x, y, z);
     s.x = floorf(fminf(fmaxf(s.x, -1.0f), 1.0f) * kOctSteps) * kOctStep;
     s.y = floorf(fminf(fmaxf(s.y, -1.0f), 1.0f) * kOctSteps) * kOctStep;
     float2 cand[4];
     float3 o[4];
-    float df[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         cand[k] = make_float2(s.x + ((k & 2) ? kOctStep : 0.0f), s.y + ((k & 1) ? kOctStep : 0.0f));
         o[k] = oct_to_vec3(cand[k].x, cand[k].y);
-        const float l = sqrtf(o[k].x * o[k].x + o[k].y * o[k].y + o[k].z * o[k].z);
-        df[k] = (o[k].x * x + o[k].y * y + o[k].z * z) / l;
     }
     const float l1 = fabsf(x) + fabsf(y) + fabsf(z);
-    const bool filtered = l1 >= 0x1p-100f && l1 <= 0x1p100f;  // false for NaN and infinity
-    const float tol = l1 * 0x1p-16f;
-    // the current winner: at first the floored point with cosine 0 (exactly known)
-    float2 bc = s;
-    float3 bo = make_float3(0.0f, 0.0f, 0.0f);
-    float best_df = 0.0f;
-    double best_d = 0.0;
-    bool best_d_known = true;  // best_d holds the f64 cosine of the winner
+    bool fast = l1 >= 0x1p-100f && l1 <= 0x1p100f;  // false for NaN and infinity
+    float s2[4];
+    if (fast) {
+        const float sc = exp2_bits(-log2_bits(l1));
+        const float vx = x * sc, vy = y * sc, vz = z * sc;
+        const float vv = vx * vx + vy * vy + vz * vz;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < 4; k++) {
+            const float3 q = o[k];
+            const float cx = diff_of_products(q.y, vz, q.z, vy);
+            const float cy = diff_of_products(q.z, vx, q.x, vz);
+            const float cz = diff_of_products(q.x, vy, q.y, vx);
+            const float oo = q.x * q.x + q.y * q.y + q.z * q.z;
+            s2[k] = (cx * cx + cy * cy + cz * cz) / (oo * vv);
+            const float dt = q.x * vx + q.y * vy + q.z * vz;
+            fast = fast && dt > 0.0f && s2[k] < 0.25f;
+        }
+    }
+    if (!fast) {  // the crate's sequence on f64 cosines
+        float2 bc = s;
+        double best = 0.0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const double d = oct_dot64(o[k], x, y, z);
+            if (d > best) {
+                bc = cand[k];
+                best = d;
+            }
+        }
+        return (to_snorm16(bc.x) << 16) | to_snorm16(bc.y);
+    }
+    // candidate 0 beats the floored point; then each later one in turn
+    float2 bc = cand[0];
+    float3 bo = o[0];
+    float bs2 = s2[0];
+    double best_d = 0.0;
+    bool best_d_known = false;  // best_d holds the f64 cosine of the winner
+#pragma unroll
+    for (int k = 1; k < 4; k++) {
+        const float diff = s2[k] - bs2;
         bool wins;
-        if (filtered && df[k] - best_df > tol) {
-            wins = true;
-            best_d_known = false;
-        } else if (filtered && best_df - df[k] > tol) {
-            wins = false;
+        if (fabsf(diff) > fmaxf(fmaxf(s2[k], bs2) * 0x1p-16f, 0x1p-40f)) {
+            wins = diff < 0.0f;
+            if (wins) best_d_known = false;
         } else {
             if (!best_d_known) best_d = oct_dot64(bo, x, y, z);
             const double d = oct_dot64(o[k], x, y, z);
@@ -162,7 +205,7 @@ __device__ __forceinline__ uint32_t oct32_encode_precise(float x, float y, float
         if (wins) {
             bc = cand[k];
             bo = o[k];
-            best_df = df[k];
+            bs2 = s2[k];
         }
     }
     return (to_snorm16(bc.x) << 16) | to_snorm16(bc.y);
@@ -200,8 +243,8 @@ __device__ __forceinline__ uint64_t unsigned40_encode(float a, float b, float c)
 
 __device__ __forceinline__ float3 unsigned40_decode(uint64_t t) {
     const float m = exp2_bits((int)(t & 127u) - 42);
-    return make_float3((float)((t >> 29) & 2047u) * m, (float)((t >> 18) & 2047u) * m,
-                       (float)((t >> 7) & 2047u) * m);
+    return make_float3((float)(uint32_t)((t >> 29) & 2047u) * m, (float)(uint32_t)((t >> 18) & 2047u) * m,
+                       (float)(uint32_t)((t >> 7) & 2047u) * m);
 }
 
 __device__ __forceinline__ uint64_t signed48_encode(float a, float b, float c) {
@@ -219,8 +262,8 @@ __device__ __forceinline__ uint64_t signed48_encode(float a, float b, float c) {
 
 __device__ __forceinline__ float3 signed48_decode(uint64_t t) {
     const float m = exp2_bits((int)(t & 63u) - 38);
-    const float x = (float)((t >> 34) & 8191u) * m, y = (float)((t >> 20) & 8191u) * m,
-                z = (float)((t >> 6) & 8191u) * m;
+    const float x = (float)(uint32_t)((t >> 34) & 8191u) * m, y = (float)(uint32_t)((t >> 20) & 8191u) * m,
+                z = (float)(uint32_t)((t >> 6) & 8191u) * m;
     return make_float3(__uint_as_float(__float_as_uint(x) | ((uint32_t)(t >> 16) & 0x80000000u)),
                        __uint_as_float(__float_as_uint(y) | ((uint32_t)(t >> 2) & 0x80000000u)),
                        __uint_as_float(__float_as_uint(z) | ((uint32_t)(t << 12) & 0x80000000u)));
