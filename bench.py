@@ -800,13 +800,17 @@ def run_compact(args):
     # colours and the unsigned formats non-negative); the out-of-domain
     # paths are covered by the tests
     host = cc.random_triples(n, seed=2025)
-    host[np.isnan(host)] = 0.0
+    host[~np.isfinite(host)] = 0.0
     host_pos = np.abs(host)
+    # unit-vector formats: directions uniform in [-1, 1)^3, as the crate's
+    # oct32 property tests draw them (tests/proptest_tests.rs)
+    host_dir = np.random.default_rng(2026).uniform(-1.0, 1.0, (n, 3)).astype(np.float32)
     unsigned = ("fluv32", "unsigned32", "unsigned40")
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     d_xyz = torch.from_numpy(host.view(np.uint8).reshape(-1)).cuda()
     d_pos = torch.from_numpy(host_pos.view(np.uint8).reshape(-1)).cuda()
+    d_dir = torch.from_numpy(host_dir.view(np.uint8).reshape(-1)).cuda()
     d_codes = {name: torch.empty(n * size, dtype=torch.uint8, device="cuda") for name, (_, size) in fmts.items()}
     d_out = torch.empty(n * 12, dtype=torch.uint8, device="cuda")
     d_bad = torch.zeros(1, dtype=torch.int32, device="cuda")
@@ -817,7 +821,8 @@ def run_compact(args):
     for name, op in COMPACT_CODECS:
         fmt, size = fmts[name]
 
-        src, src_host = (d_pos, host_pos) if name in unsigned else (d_xyz, host)
+        src, src_host = ((d_pos, host_pos) if name in unsigned else
+                         (d_dir, host_dir) if name.startswith("oct32") else (d_xyz, host))
 
         def launch():
             if op == "encode":
@@ -886,8 +891,9 @@ def run_compact(args):
             "data": "synthetic (seeded f32 triples over the whole exponent range, special values mixed in)",
             "config": {"workload": "compact codecs: %d triples per launch" % n,
                        "l2": "inputs (%d MB of triples) larger than L2" % (n * 12 // 2 ** 20),
-                       "inputs": "in each format's domain (no NaN; non-negative for fluv32 and the unsigned "
-                                 "formats)", "invalid_inputs_counted": invalid_total},
+                       "inputs": "finite, seeded over the whole exponent range (non-negative for fluv32 and the "
+                                 "unsigned formats); oct32: directions uniform in [-1, 1)^3",
+                       "invalid_inputs_counted": invalid_total},
             "e2e": {"value": n / e2e_sec / 1e6, "unit": "Melem/s", "h2d_bytes_per_step": n * 12,
                     "d2h_bytes_per_step": n * 4, "bit_exact_vs_oracle": e2e_ok},
             "gpu_launches": launches, "clocks": clk,

@@ -39,18 +39,36 @@ constexpr float kVScale = 1235.0f / 3.0f;
 constexpr float kVURatio = kVScale / kUScale;
 constexpr uint32_t kFluvBias = 64;  // 127 - 63
 
-__device__ __forceinline__ uint32_t fluv32_uv(float x, float y, float z) {
-    float s = x + 15.0f * y + 3.0f * z;
-    float u = fminf(fmaxf((4.0f * kUScale) * x / s + 0.5f, 0.0f), 255.0f);
-    float v = fminf(fmaxf((9.0f * kVScale) * y / s + 0.5f, 1.0f), 255.0f);
-    return ((uint32_t)u << 8) | (uint32_t)v;
+// One chroma byte: trunc(clamp(fl(fl(a / s) + 0.5), lo, 255)) with the IEEE
+// quotient (fluv32.rs:101-104).  Only the integer matters, so the quotient
+// is first taken with __fdividef (within 2 ulps for 2^-126 < |s| < 2^126):
+// for a result below 256 that puts fl(q + 0.5) within 2^-14 of the exact
+// computation's, so whenever the fast value is over 2^-12 from an integer
+// both floor to the same integer; otherwise (and outside the fast
+// quotient's range) the exact division decides.
+__device__ __forceinline__ uint32_t fluv32_chroma(float a, float s, float lo) {
+    if (s >= 0x1p-100f && s <= 0x1p100f && fabsf(a) <= 0x1p100f) {
+        const float t = __fdividef(a, s) + 0.5f;
+        if (t >= 256.0f) return 255u;
+        const float fl = floorf(t), fr = t - fl;
+        if (t > -1.0f && fr > 0x1p-12f && fr < 1.0f - 0x1p-12f) return (uint32_t)fminf(fmaxf(fl, lo), 255.0f);
+    }
+    return (uint32_t)fminf(fmaxf(a / s + 0.5f, lo), 255.0f);
 }
+
+__device__ __forceinline__ uint32_t fluv32_uv(float x, float y, float z) {
+    const float s = x + 15.0f * y + 3.0f * z;
+    return (fluv32_chroma((4.0f * kUScale) * x, s, 0.0f) << 8) | fluv32_chroma((9.0f * kVScale) * y, s, 1.0f);
+}
+
+// encode_uv((1, 1, 1)): u = 1634/19 + 0.5 = 86.5 -> 0x56, v = 3705/19 + 0.5 = 195.5 -> 0xc3
+constexpr uint32_t kFluvWhiteUV = 0x56c3u;
 
 __device__ __forceinline__ uint32_t fluv32_encode(float x, float y, float z) {
     const uint32_t yb = __float_as_uint(y) & 0x7fffffffu;
-    if (yb < ((kFluvBias + 1) << 23)) return fluv32_uv(1.0f, 1.0f, 1.0f);  // black
+    if (yb < ((kFluvBias + 1) << 23)) return kFluvWhiteUV;  // black
     if (yb >= ((kFluvBias + 128) << 23))  // brighter than the format: brightest Y
-        return 0xffff0000u | (isinf(y) ? fluv32_uv(1.0f, 1.0f, 1.0f) : fluv32_uv(x, y, z));
+        return 0xffff0000u | (isinf(y) ? kFluvWhiteUV : fluv32_uv(x, y, z));
     return (((yb - (kFluvBias << 23)) << 2) & 0xffff0000u) | fluv32_uv(x, y, z);
 }
 
@@ -125,7 +143,9 @@ __device__ __forceinline__ float diff_of_products(float a, float b, float c, flo
 // candidates' cosines differ only in second order (~1e-9), so they are
 // ranked by sin^2 of their angle to the input instead, a first-order
 // quantity computed in f32: |o x v|^2 / (|o|^2 |v|^2) with the cross product
-// by diff_of_products, v scaled by a power of two (exact) to |v|_1 in [1, 2).
+// by diff_of_products, v scaled by a power of two to |v|_1 in [1, 2) (exact,
+// except that components below 2^-149 of |v|_1 may flush: an angle change
+// far under the 2^-40 floor below).
 // Every rounding there is relative to the quantity itself, so each f32
 // sin^2 is within 15 * 2^-24 (relative) of the exact value.  With every
 // candidate within 30 degrees of the input and in front of it (cosine > 0:
@@ -135,8 +155,8 @@ __device__ __forceinline__ float diff_of_products(float a, float b, float c, flo
 // than 2^-16 of the larger one (8x the sum of both errors) and by more than
 // 2^-40 (the cosines then differ by over 100x the f64 rounding of the
 // crate's cosines) therefore has the outcome of the crate's f64 comparison; any
-// other comparison, and any input outside this regime (|v|_1 outside
-// [2^-100, 2^100], NaN, infinity, a candidate over 30 degrees away), is
+// other comparison, and any input outside this regime (a zero vector, NaN,
+// infinity, |v|_1 overflowing, a candidate over 30 degrees away), is
 // decided by the crate's own f64 cosines, in the crate's order, so the code
 // is bit-identical.
 __device__ __forceinline__ uint32_t oct32_encode_precise(float x, float y, float z) {
@@ -151,7 +171,7 @@ __device__ __forceinline__ uint32_t oct32_encode_precise(float x, float y, float
         o[k] = oct_to_vec3(cand[k].x, cand[k].y);
     }
     const float l1 = fabsf(x) + fabsf(y) + fabsf(z);
-    bool fast = l1 >= 0x1p-100f && l1 <= 0x1p100f;  // false for NaN and infinity
+    bool fast = l1 > 0.0f && l1 <= 3.40282347e38f;  // finite, non-zero (false for NaN)
     float s2[4];
     if (fast) {
         const float sc = exp2_bits(-log2_bits(l1));
@@ -192,7 +212,7 @@ __device__ __forceinline__ uint32_t oct32_encode_precise(float x, float y, float
     for (int k = 1; k < 4; k++) {
         const float diff = s2[k] - bs2;
         bool wins;
-        if (fabsf(diff) > fmaxf(fmaxf(s2[k], bs2) * 0x1p-16f, 0x1p-40f)) {
+        if (fabsf(diff) > fmaxf(fmaxf(s2[k], bs2) * 0x1p-16f, 0x1p-45f)) {
             wins = diff < 0.0f;
             if (wins) best_d_known = false;
         } else {
