@@ -3,13 +3,15 @@
 // psy_closure_compress / psy_closure_decompress).
 //
 // The codecs are HBM-bound byte work: 12 bytes of f32 triple in, 4 to 6
-// bytes of code out (or back).  A block owns a tile of 1024 elements,
-// stages the tile's input bytes in shared memory with 16-byte coalesced
-// loads, converts element by element between the two shared buffers, and
-// writes the output tile back with 16-byte coalesced stores, so that the
-// 5- and 6-byte formats (whose elements straddle words) and the 12-byte
-// triples cost no partial-sector traffic.  Pointers that are not 16-byte
-// aligned take a byte-wise copy instead (same results).  Elements outside
+// bytes of code out (or back).  Work goes in tiles of 1024 elements: a
+// tile's input bytes are staged in shared memory with 16-byte coalesced
+// copies, converted element by element between two shared buffers, and
+// written back with 16-byte coalesced stores, so that the 5- and 6-byte
+// formats (whose elements straddle words) and the 12-byte triples cost no
+// partial-sector traffic.  With a 16-byte aligned input, resident blocks
+// stream the tiles with the next tile's copy in flight during conversion;
+// pointers that are not 16-byte aligned take a one-tile-per-block kernel
+// with byte-wise copies instead (same results).  Elements outside
 // a format's domain -- the inputs the reference's debug build rejects with
 // an assertion -- are counted into an optional device counter.
 #include <cuda_runtime.h>
@@ -247,25 +249,16 @@ struct ColorDecompress {
     __device__ static uint32_t run(uint64_t c, uint8_t *o) { return color_from_code(c, *reinterpret_cast<PsyColor *>(o)); }
 };
 
-// One tile of kTile elements per block: stage the input bytes, convert, and
-// write the output bytes back.  Packed 5- and 6-byte codes move between the
-// warps' registers and the staged tile as whole 32-bit words: a warp's 32
-// consecutive codes fill 8*kOut words, and each word is put together from
-// the (at most two) codes it overlaps, fetched by shuffle; a code is read
-// back from the two words it overlaps with a funnel shift.
+// Convert one staged tile of cnt elements from s_in into s_out.  Packed 5-
+// and 6-byte codes move between the warps' registers and the staged tile as
+// whole 32-bit words: a warp's 32 consecutive codes fill 8*kOut words, and
+// each word is put together from the (at most two) codes it overlaps,
+// fetched by shuffle; a code is read back from the two words it overlaps
+// with a funnel shift.
 template <class Op>
-__global__ void __launch_bounds__(kThreads) k_compact(const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
-                                                       uint32_t n, uint32_t *__restrict__ invalid, bool vin,
-                                                       bool vout) {
-    __shared__ __align__(16) uint8_t s_in[kTile * Op::kIn];
-    __shared__ __align__(16) uint8_t s_out[kTile * Op::kOut];
-    __shared__ uint32_t s_bad[kThreads / 32];
+__device__ __forceinline__ void convert_tile(const uint8_t *__restrict__ s_in, uint8_t *__restrict__ s_out,
+                                             uint32_t cnt, uint32_t &bad) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint64_t first = (uint64_t)blockIdx.x * kTile;
-    const uint32_t cnt = (uint32_t)min((uint64_t)kTile, (uint64_t)n - first);
-    copy_bytes(s_in, in + first * Op::kIn, cnt * Op::kIn, vin);
-    __syncthreads();
-    uint32_t bad = 0;
     if constexpr (Op::kPack) {
         for (uint32_t base = warp * 32; base < cnt; base += kThreads) {  // warp-uniform bound
             const uint32_t k = base + lane;
@@ -303,16 +296,102 @@ __global__ void __launch_bounds__(kThreads) k_compact(const uint8_t *__restrict_
             bad += Op::run(code, s_out + k * Op::kOut);
         }
     }
+}
+
+// Block total of the per-thread counts into the optional counter: one
+// atomic per block at most.  Called by every thread of the block.
+__device__ __forceinline__ void count_invalid(uint32_t bad, uint32_t *invalid, uint32_t *s_bad) {
     bad = __reduce_add_sync(0xffffffffu, bad);
-    if (lane == 0) s_bad[warp] = bad;
+    if ((threadIdx.x & 31u) == 0) s_bad[threadIdx.x >> 5] = bad;
     __syncthreads();
-    copy_bytes(out + first * Op::kOut, s_out, cnt * Op::kOut, vout);
     if (invalid && threadIdx.x == 0) {
         uint32_t sum = 0;
 #pragma unroll
         for (int i = 0; i < kThreads / 32; i++) sum += s_bad[i];
-        if (sum) atomicAdd(invalid, sum);  // one atomic per block at most
+        if (sum) atomicAdd(invalid, sum);
     }
+}
+
+// Any alignment: one tile per block, byte-wise copies where a pointer is
+// not 16-byte aligned.
+template <class Op>
+__global__ void __launch_bounds__(kThreads) k_compact(const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
+                                                       uint32_t n, uint32_t *__restrict__ invalid, bool vin,
+                                                       bool vout) {
+    __shared__ __align__(16) uint8_t s_in[kTile * Op::kIn];
+    __shared__ __align__(16) uint8_t s_out[kTile * Op::kOut];
+    __shared__ uint32_t s_bad[kThreads / 32];
+    const uint64_t first = (uint64_t)blockIdx.x * kTile;
+    const uint32_t cnt = (uint32_t)min((uint64_t)kTile, (uint64_t)n - first);
+    copy_bytes(s_in, in + first * Op::kIn, cnt * Op::kIn, vin);
+    __syncthreads();
+    uint32_t bad = 0;
+    convert_tile<Op>(s_in, s_out, cnt, bad);
+    __syncthreads();
+    copy_bytes(out + first * Op::kOut, s_out, cnt * Op::kOut, vout);
+    count_invalid(bad, invalid, s_bad);
+}
+
+// Start the asynchronous copy of `bytes` bytes (16-byte aligned source and
+// destination) into shared memory: 16-byte cp.async per thread, the ragged
+// end (bytes % 16) by plain loads.  Completion: cp.async.wait_group.
+__device__ __forceinline__ void load_tile_async(uint8_t *dst, const uint8_t *src, uint32_t bytes) {
+    const uint32_t n16 = bytes / 16;
+    for (uint32_t i = threadIdx.x; i < n16; i += kThreads) {
+        const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst + 16 * i);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src + 16 * i) : "memory");
+    }
+    for (uint32_t i = n16 * 16 + threadIdx.x; i < bytes; i += kThreads) dst[i] = src[i];
+}
+
+// 16-byte aligned input: resident blocks walk the tiles (tile t, t + grid,
+// ...) with the next tile's load in flight (cp.async into the other half
+// of a double buffer) while the current one converts, so the read stream
+// never waits on conversion.  Each cp.async group is waited for by the
+// hardware (cp.async.wait_group), not by a spin loop.
+template <class Op>
+__global__ void __launch_bounds__(kThreads) k_compact_pipe(const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
+                                                            uint32_t n, uint32_t *__restrict__ invalid, bool vout) {
+    __shared__ __align__(16) uint8_t s_in[2][kTile * Op::kIn];
+    __shared__ __align__(16) uint8_t s_out[kTile * Op::kOut];
+    __shared__ uint32_t s_bad[kThreads / 32];
+    const uint32_t tiles = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
+    uint32_t t = blockIdx.x;  // the launch has at most `tiles` blocks
+    auto count = [&](uint32_t tile) { return (uint32_t)min((uint64_t)kTile, (uint64_t)n - (uint64_t)tile * kTile); };
+    load_tile_async(s_in[0], in + (uint64_t)t * kTile * Op::kIn, count(t) * Op::kIn);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    uint32_t bad = 0, buf = 0;
+    for (; t < tiles; t += gridDim.x) {
+        const uint32_t nt = t + gridDim.x;
+        if (nt < tiles) load_tile_async(s_in[buf ^ 1], in + (uint64_t)nt * kTile * Op::kIn, count(nt) * Op::kIn);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // tile t's group has landed
+        __syncthreads();
+        const uint32_t cnt = count(t);
+        convert_tile<Op>(s_in[buf], s_out, cnt, bad);
+        __syncthreads();
+        copy_bytes(out + (uint64_t)t * kTile * Op::kOut, s_out, cnt * Op::kOut, vout);
+        buf ^= 1;
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    count_invalid(bad, invalid, s_bad);
+}
+
+// Resident blocks per SM of k_compact_pipe<Op> times the SM count (per
+// device, computed once).
+template <class Op>
+uint32_t pipe_grid() {
+    static uint32_t grid[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    if (!grid[dev]) {
+        int sms = 0, per = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_compact_pipe<Op>, kThreads, 0) != cudaSuccess)
+            return 0;
+        grid[dev] = (uint32_t)(sms * (per > 0 ? per : 1));
+    }
+    return grid[dev];
 }
 
 bool misaligned(const void *p, uintptr_t a) { return ((uintptr_t)p & (a - 1)) != 0; }
@@ -324,8 +403,14 @@ int launch(const void *in, void *out, uint32_t n, uint32_t *invalid, void *strea
     if (misaligned(invalid, 4)) return psy_fail(PSY_E_INVALID, std::string(what) + ": counter not 4-byte aligned");
     const bool vin = ((uintptr_t)in & 15u) == 0, vout = ((uintptr_t)out & 15u) == 0;
     const uint32_t blocks = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
-    k_compact<Op><<<blocks, kThreads, 0, (cudaStream_t)stream>>>(static_cast<const uint8_t *>(in),
-                                                                  static_cast<uint8_t *>(out), n, invalid, vin, vout);
+    const uint32_t resident = vin ? pipe_grid<Op>() : 0;
+    if (resident)
+        k_compact_pipe<Op><<<min(blocks, resident), kThreads, 0, (cudaStream_t)stream>>>(
+            static_cast<const uint8_t *>(in), static_cast<uint8_t *>(out), n, invalid, vout);
+    else
+        k_compact<Op><<<blocks, kThreads, 0, (cudaStream_t)stream>>>(static_cast<const uint8_t *>(in),
+                                                                      static_cast<uint8_t *>(out), n, invalid, vin,
+                                                                      vout);
     if (cudaGetLastError() != cudaSuccess) return psy_fail(PSY_E_CUDA, std::string(what) + ": launch failed");
     return PSY_OK;
 }

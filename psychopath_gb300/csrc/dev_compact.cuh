@@ -41,24 +41,33 @@ constexpr uint32_t kFluvBias = 64;  // 127 - 63
 
 // One chroma byte: trunc(clamp(fl(fl(a / s) + 0.5), lo, 255)) with the IEEE
 // quotient (fluv32.rs:101-104).  Only the integer matters, so the quotient
-// is first taken with __fdividef (within 2 ulps for 2^-126 < |s| < 2^126):
-// for a result below 256 that puts fl(q + 0.5) within 2^-14 of the exact
-// computation's, so whenever the fast value is over 2^-12 from an integer
-// both floor to the same integer; otherwise (and outside the fast
-// quotient's range) the exact division decides.
-__device__ __forceinline__ uint32_t fluv32_chroma(float a, float s, float lo) {
-    if (s >= 0x1p-100f && s <= 0x1p100f && fabsf(a) <= 0x1p100f) {
-        const float t = __fdividef(a, s) + 0.5f;
+// is first taken with __fdividef (within 2 ulps for 2^-126 < |s| < 2^126)
+// of a and s both scaled by sc = 2^-clamp(floor(log2 s), -126, 126), which
+// puts s in [2^-23, 4) without changing the quotient (exact, except that an
+// a below 2^-126 of s may lose bits far under the margin; an a that
+// overflows gives infinity as the exact quotient does).  For a result below
+// 256 the fast fl(q + 0.5) is then within 2^-14 of the exact computation's,
+// so whenever it is over 2^-12 from an integer both floor to the same
+// integer; otherwise (and for an s that is zero, negative or NaN) the exact
+// division decides.  An s that overflowed to infinity makes a finite a's
+// quotient 0: fl(0 + 0.5) truncates to lo.
+__device__ __forceinline__ uint32_t fluv32_chroma(float a, float s, float sc, float lo) {
+    if (s > 0.0f && s <= 3.40282347e38f) {
+        const float t = __fdividef(a * sc, s * sc) + 0.5f;
         if (t >= 256.0f) return 255u;
         const float fl = floorf(t), fr = t - fl;
         if (t > -1.0f && fr > 0x1p-12f && fr < 1.0f - 0x1p-12f) return (uint32_t)fminf(fmaxf(fl, lo), 255.0f);
+    } else if (isinf(s) && s > 0.0f && fabsf(a) <= 3.40282347e38f) {
+        return (uint32_t)lo;
     }
     return (uint32_t)fminf(fmaxf(a / s + 0.5f, lo), 255.0f);
 }
 
 __device__ __forceinline__ uint32_t fluv32_uv(float x, float y, float z) {
     const float s = x + 15.0f * y + 3.0f * z;
-    return (fluv32_chroma((4.0f * kUScale) * x, s, 0.0f) << 8) | fluv32_chroma((9.0f * kVScale) * y, s, 1.0f);
+    const float sc = exp2_bits(-min(max(log2_bits(s), -126), 126));  // used only for a positive finite s
+    return (fluv32_chroma((4.0f * kUScale) * x, s, sc, 0.0f) << 8) |
+           fluv32_chroma((9.0f * kVScale) * y, s, sc, 1.0f);
 }
 
 // encode_uv((1, 1, 1)): u = 1634/19 + 0.5 = 86.5 -> 0x56, v = 3705/19 + 0.5 = 195.5 -> 0xc3
