@@ -8,10 +8,10 @@
 // copies, converted element by element between two shared buffers, and
 // written back with 16-byte coalesced stores, so that the 5- and 6-byte
 // formats (whose elements straddle words) and the 12-byte triples cost no
-// partial-sector traffic.  With a 16-byte aligned input, resident blocks
-// stream the tiles with the next tile's copy in flight during conversion;
-// pointers that are not 16-byte aligned take a one-tile-per-block kernel
-// with byte-wise copies instead (same results).  Elements outside
+// partial-sector traffic.  Read-heavy conversions with a 16-byte aligned
+// input stream the tiles through resident blocks with the next tile's copy
+// in flight during conversion; the rest take one tile per block (with
+// byte-wise copies for pointers that are not 16-byte aligned; same results).  Elements outside
 // a format's domain -- the inputs the reference's debug build rejects with
 // an assertion -- are counted into an optional device counter.
 #include <cuda_runtime.h>
@@ -403,7 +403,9 @@ int launch(const void *in, void *out, uint32_t n, uint32_t *invalid, void *strea
     if (misaligned(invalid, 4)) return psy_fail(PSY_E_INVALID, std::string(what) + ": counter not 4-byte aligned");
     const bool vin = ((uintptr_t)in & 15u) == 0, vout = ((uintptr_t)out & 15u) == 0;
     const uint32_t blocks = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
-    const uint32_t resident = vin ? pipe_grid<Op>() : 0;
+    // read-heavy conversions (encoders, colour compression) stream through
+    // resident blocks; write-heavy ones are fastest one tile per block
+    const uint32_t resident = (vin && Op::kIn > Op::kOut) ? pipe_grid<Op>() : 0;
     if (resident)
         k_compact_pipe<Op><<<min(blocks, resident), kThreads, 0, (cudaStream_t)stream>>>(
             static_cast<const uint8_t *>(in), static_cast<uint8_t *>(out), n, invalid, vout);

@@ -51,6 +51,10 @@ constexpr uint32_t kFluvBias = 64;  // 127 - 63
 // integer; otherwise (and for an s that is zero, negative or NaN) the exact
 // division decides.  An s that overflowed to infinity makes a finite a's
 // quotient 0: fl(0 + 0.5) truncates to lo.
+__device__ __noinline__ uint32_t fluv32_chroma_exact(float a, float s, float lo) {
+    return (uint32_t)fminf(fmaxf(a / s + 0.5f, lo), 255.0f);
+}
+
 __device__ __forceinline__ uint32_t fluv32_chroma(float a, float s, float sc, float lo) {
     if (s > 0.0f && s <= 3.40282347e38f) {
         const float t = __fdividef(a * sc, s * sc) + 0.5f;
@@ -60,7 +64,7 @@ __device__ __forceinline__ uint32_t fluv32_chroma(float a, float s, float sc, fl
     } else if (isinf(s) && s > 0.0f && fabsf(a) <= 3.40282347e38f) {
         return (uint32_t)lo;
     }
-    return (uint32_t)fminf(fmaxf(a / s + 0.5f, lo), 255.0f);
+    return fluv32_chroma_exact(a, s, lo);  // out of line: rare
 }
 
 __device__ __forceinline__ uint32_t fluv32_uv(float x, float y, float z) {
@@ -128,7 +132,8 @@ __device__ __forceinline__ uint32_t oct32_encode(float x, float y, float z) {
 }
 
 // The crate's f64 cosine of candidate o with the input v (oct32.rs:26-30).
-__device__ __forceinline__ double oct_dot64(float3 o, float x, float y, float z) {
+// Out of line: only the rare inputs the f32 ranking cannot decide call it.
+__device__ __noinline__ double oct_dot64(float3 o, float x, float y, float z) {
     const double ox = o.x, oy = o.y, oz = o.z;
     const double l = sqrt(ox * ox + oy * oy + oz * oz);
     return (ox * (double)x + oy * (double)y + oz * (double)z) / l;
