@@ -260,6 +260,17 @@ __device__ __forceinline__ void convert_tile(const uint8_t *__restrict__ s_in, u
                                              uint32_t cnt, uint32_t &bad) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     if constexpr (Op::kPack) {
+        // word w = lane + 32 j of a warp's 32 codes starts in code e at byte
+        // p (the same for every chunk): its low bytes are code e's bytes
+        // p.., the rest (when p + 4 > kOut) code e + 1's first bytes
+        constexpr uint32_t kWords = 8 * Op::kOut;  // words of 32 codes
+        uint32_t we[2], wp[2];
+#pragma unroll
+        for (uint32_t j = 0; j < 2; j++) {
+            const uint32_t b = 4 * (lane + 32 * j);
+            we[j] = min(b / Op::kOut, 31u);
+            wp[j] = b - (b / Op::kOut) * Op::kOut;
+        }
         for (uint32_t base = warp * 32; base < cnt; base += kThreads) {  // warp-uniform bound
             const uint32_t k = base + lane;
             const uint64_t code = k < cnt ? Op::run(s_in + k * Op::kIn, bad) : 0;
@@ -267,16 +278,17 @@ __device__ __forceinline__ void convert_tile(const uint8_t *__restrict__ s_in, u
                 if (k < cnt) reinterpret_cast<uint32_t *>(s_out)[k] = (uint32_t)code;
             } else {
                 uint32_t *wout = reinterpret_cast<uint32_t *>(s_out + base * Op::kOut);
-                constexpr uint32_t kWords = 8 * Op::kOut;  // words of 32 codes
+                const uint32_t lo = (uint32_t)code, hi = (uint32_t)(code >> 32);
 #pragma unroll
                 for (uint32_t j = 0; j < 2; j++) {
-                    const uint32_t w = lane + 32 * j, b = 4 * w, e = b / Op::kOut, p = b - e * Op::kOut;
-                    const uint64_t c0 = __shfl_sync(0xffffffffu, code, min(e, 31u));
-                    const uint64_t c1 = __shfl_sync(0xffffffffu, code, min(e + 1, 31u));
+                    const uint32_t l0 = __shfl_sync(0xffffffffu, lo, we[j]);
+                    const uint32_t h0 = __shfl_sync(0xffffffffu, hi, we[j]);
+                    const uint32_t l1 = __shfl_sync(0xffffffffu, lo, min(we[j] + 1, 31u));
+                    const uint32_t w = lane + 32 * j;
                     if (w < kWords) {
-                        uint64_t v = c0 >> (8 * p);
-                        if (p + 4 > (uint32_t)Op::kOut) v |= c1 << (8 * (Op::kOut - p));
-                        wout[w] = (uint32_t)v;
+                        uint32_t v = __funnelshift_rc(l0, h0, 8 * wp[j]);  // (h0:l0) >> 8p, 8p <= 32
+                        if (wp[j] + 4 > (uint32_t)Op::kOut) v |= l1 << (8 * (Op::kOut - wp[j]));
+                        wout[w] = v;
                     }
                 }
             }

@@ -77,12 +77,17 @@ __device__ __forceinline__ uint32_t fluv32_uv(float x, float y, float z) {
 // encode_uv((1, 1, 1)): u = 1634/19 + 0.5 = 86.5 -> 0x56, v = 3705/19 + 0.5 = 195.5 -> 0xc3
 constexpr uint32_t kFluvWhiteUV = 0x56c3u;
 
+// Black (Y below the format) and infinite Y take the chroma of (1, 1, 1);
+// Y above the format saturates to the brightest Y with its own chroma
+// (fluv32.rs:107-126).  One chroma evaluation site, so that a warp whose
+// lanes fall in different cases evaluates it once.
 __device__ __forceinline__ uint32_t fluv32_encode(float x, float y, float z) {
     const uint32_t yb = __float_as_uint(y) & 0x7fffffffu;
-    if (yb < ((kFluvBias + 1) << 23)) return kFluvWhiteUV;  // black
-    if (yb >= ((kFluvBias + 128) << 23))  // brighter than the format: brightest Y
-        return 0xffff0000u | (isinf(y) ? kFluvWhiteUV : fluv32_uv(x, y, z));
-    return (((yb - (kFluvBias << 23)) << 2) & 0xffff0000u) | fluv32_uv(x, y, z);
+    const bool black = yb < ((kFluvBias + 1) << 23), bright = yb >= ((kFluvBias + 128) << 23);
+    uint32_t uv = kFluvWhiteUV;
+    if (!black && !(bright && isinf(y))) uv = fluv32_uv(x, y, z);
+    const uint32_t lum = black ? 0u : bright ? 0xffff0000u : (((yb - (kFluvBias << 23)) << 2) & 0xffff0000u);
+    return lum | uv;
 }
 
 __device__ __forceinline__ float fluv32_y(uint32_t c) {
@@ -269,10 +274,12 @@ __device__ __forceinline__ uint64_t unsigned40_encode(float a, float b, float c)
     if (big < 0x1p-42f) return 0;
     const int e = min(max(log2_bits(big), -32), 95);
     const float inv = exp2_bits(10 - e);
-    const uint64_t x = sat_u32(fminf(a * inv, 2047.0f));
-    const uint64_t y = sat_u32(fminf(b * inv, 2047.0f));
-    const uint64_t z = sat_u32(fminf(c * inv, 2047.0f));
-    return (x << 29) | (y << 18) | (z << 7) | (uint64_t)(e + 32);
+    const uint32_t x = sat_u32(fminf(a * inv, 2047.0f));
+    const uint32_t y = sat_u32(fminf(b * inv, 2047.0f));
+    const uint32_t z = sat_u32(fminf(c * inv, 2047.0f));
+    // bits: x 29..39, y 18..28, z 7..17, exponent 0..6
+    const uint32_t lo = (x << 29) | (y << 18) | (z << 7) | (uint32_t)(e + 32);
+    return ((uint64_t)(x >> 3) << 32) | lo;
 }
 
 __device__ __forceinline__ float3 unsigned40_decode(uint64_t t) {
@@ -287,11 +294,14 @@ __device__ __forceinline__ uint64_t signed48_encode(float a, float b, float c) {
     if (big < 0x1p-38f) return 0;
     const int e = min(max(log2_bits(big), -26), 37);
     const float inv = exp2_bits(12 - e);
-    const uint64_t x = sat_u32(fminf(aa * inv, 8191.0f));
-    const uint64_t y = sat_u32(fminf(ab * inv, 8191.0f));
-    const uint64_t z = sat_u32(fminf(ac * inv, 8191.0f));
-    const uint64_t sx = __float_as_uint(a) >> 31, sy = __float_as_uint(b) >> 31, sz = __float_as_uint(c) >> 31;
-    return (sx << 47) | (x << 34) | (sy << 33) | (y << 20) | (sz << 19) | (z << 6) | (uint64_t)(e + 26);
+    const uint32_t x = sat_u32(fminf(aa * inv, 8191.0f));
+    const uint32_t y = sat_u32(fminf(ab * inv, 8191.0f));
+    const uint32_t z = sat_u32(fminf(ac * inv, 8191.0f));
+    const uint32_t sx = __float_as_uint(a) >> 31, sy = __float_as_uint(b) >> 31, sz = __float_as_uint(c) >> 31;
+    // bits: sign x 47, x 34..46, sign y 33, y 20..32, sign z 19, z 6..18, exponent 0..5
+    const uint32_t lo = (y << 20) | (sz << 19) | (z << 6) | (uint32_t)(e + 26);
+    const uint32_t hi = (sx << 15) | (x << 2) | (sy << 1) | (y >> 12);
+    return ((uint64_t)hi << 32) | lo;
 }
 
 __device__ __forceinline__ float3 signed48_decode(uint64_t t) {
