@@ -39,39 +39,43 @@ constexpr float kVScale = 1235.0f / 3.0f;
 constexpr float kVURatio = kVScale / kUScale;
 constexpr uint32_t kFluvBias = 64;  // 127 - 63
 
-// One chroma byte: trunc(clamp(fl(fl(a / s) + 0.5), lo, 255)) with the IEEE
-// quotient (fluv32.rs:101-104).  Only the integer matters, so the quotient
-// is first taken with __fdividef (within 2 ulps for 2^-126 < |s| < 2^126)
-// of a and s both scaled by sc = 2^-clamp(floor(log2 s), -126, 126), which
-// puts s in [2^-23, 4) without changing the quotient (exact, except that an
-// a below 2^-126 of s may lose bits far under the margin; an a that
-// overflows gives infinity as the exact quotient does).  For a result below
-// 256 the fast fl(q + 0.5) is then within 2^-14 of the exact computation's,
-// so whenever it is over 2^-12 from an integer both floor to the same
-// integer; otherwise (and for an s that is zero, negative or NaN) the exact
-// division decides.  An s that overflowed to infinity makes a finite a's
-// quotient 0: fl(0 + 0.5) truncates to lo.
-__device__ __noinline__ uint32_t fluv32_chroma_exact(float a, float s, float lo) {
-    return (uint32_t)fminf(fmaxf(a / s + 0.5f, lo), 255.0f);
+// The two chroma bytes, trunc(clamp(fl(fl(a / s) + 0.5), lo, 255)) for
+// a = 1634 x (lo 0) and a = 9 * 1235/3 y (lo 1) with the IEEE quotient
+// (fluv32.rs:94-105), as the crate computes them.  Out of line: the fast
+// form below decides all but a few inputs in ten thousand.
+__device__ __noinline__ uint32_t fluv32_uv_exact(float au, float av, float s) {
+    return ((uint32_t)fminf(fmaxf(au / s + 0.5f, 0.0f), 255.0f) << 8) |
+           (uint32_t)fminf(fmaxf(av / s + 0.5f, 1.0f), 255.0f);
 }
 
-__device__ __forceinline__ uint32_t fluv32_chroma(float a, float s, float sc, float lo) {
-    if (s > 0.0f && s <= 3.40282347e38f) {
-        const float t = __fdividef(a * sc, s * sc) + 0.5f;
-        if (t >= 256.0f) return 255u;
-        const float fl = floorf(t), fr = t - fl;
-        if (t > -1.0f && fr > 0x1p-12f && fr < 1.0f - 0x1p-12f) return (uint32_t)fminf(fmaxf(fl, lo), 255.0f);
-    } else if (isinf(s) && s > 0.0f && fabsf(a) <= 3.40282347e38f) {
-        return (uint32_t)lo;
-    }
-    return fluv32_chroma_exact(a, s, lo);  // out of line: rare
+// A fast chroma value t = fl(q + 0.5) floors to the exact computation's
+// integer when it is over 2^-11 from an integer, or at least 256 (both clamp
+// to 255).
+__device__ __forceinline__ bool fluv32_chroma_sure(float t, float fl) {
+    return t >= 256.0f || (t > -1.0f && t - fl > 0x1p-11f && t - fl < 1.0f - 0x1p-11f);
 }
 
+// Only the integers matter, so the quotients are first taken as a * sc *
+// r with r = __fdividef(1, s * sc) (within 2 ulps for 2^-126 < |s * sc| <
+// 2^126) and sc = 2^-clamp(floor(log2 s), -126, 126), which puts s * sc in
+// [2^-23, 4) without changing the quotient (the scalings are exact, except
+// that an a below 2^-126 of s may lose bits far under the margin, and an a
+// that overflows gives infinity as the exact quotient does).  For a
+// quotient below 256 that is within 2^-21.7 relative, 2^-13.7 absolute, of
+// the exact one, and the fast fl(q + 0.5) within 2^-13.3 of the exact
+// computation's; whenever it is over 2^-11 from an integer both floor to
+// the same integer.  Any other case (an s that is zero, negative, not
+// finite or NaN included) takes the exact form.
 __device__ __forceinline__ uint32_t fluv32_uv(float x, float y, float z) {
     const float s = x + 15.0f * y + 3.0f * z;
+    const float au = (4.0f * kUScale) * x, av = (9.0f * kVScale) * y;
     const float sc = exp2_bits(-min(max(log2_bits(s), -126), 126));  // used only for a positive finite s
-    return (fluv32_chroma((4.0f * kUScale) * x, s, sc, 0.0f) << 8) |
-           fluv32_chroma((9.0f * kVScale) * y, s, sc, 1.0f);
+    const float r = __fdividef(1.0f, s * sc);
+    const float tu = (au * sc) * r + 0.5f, tv = (av * sc) * r + 0.5f;
+    const float fu = floorf(tu), fv = floorf(tv);
+    if (s > 0.0f && s <= 3.40282347e38f && fluv32_chroma_sure(tu, fu) && fluv32_chroma_sure(tv, fv))
+        return ((uint32_t)fminf(fmaxf(fu, 0.0f), 255.0f) << 8) | (uint32_t)fminf(fmaxf(fv, 1.0f), 255.0f);
+    return fluv32_uv_exact(au, av, s);
 }
 
 // encode_uv((1, 1, 1)): u = 1634/19 + 0.5 = 86.5 -> 0x56, v = 3705/19 + 0.5 = 195.5 -> 0xc3
