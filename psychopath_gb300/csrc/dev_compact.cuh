@@ -83,13 +83,15 @@ constexpr uint32_t kFluvWhiteUV = 0x56c3u;
 
 // Black (Y below the format) and infinite Y take the chroma of (1, 1, 1);
 // Y above the format saturates to the brightest Y with its own chroma
-// (fluv32.rs:107-126).  One chroma evaluation site, so that a warp whose
-// lanes fall in different cases evaluates it once.
+// (fluv32.rs:107-126).  Branch-free: those lanes evaluate the chroma of
+// (1, 1, 1) itself (86.5 and 195.5 before truncation, far from integer
+// boundaries, so the fast form returns kFluvWhiteUV), and every lane of a
+// warp stays active.
 __device__ __forceinline__ uint32_t fluv32_encode(float x, float y, float z) {
     const uint32_t yb = __float_as_uint(y) & 0x7fffffffu;
     const bool black = yb < ((kFluvBias + 1) << 23), bright = yb >= ((kFluvBias + 128) << 23);
-    uint32_t uv = kFluvWhiteUV;
-    if (!black && !(bright && isinf(y))) uv = fluv32_uv(x, y, z);
+    const bool white = black || (bright && isinf(y));
+    const uint32_t uv = fluv32_uv(white ? 1.0f : x, white ? 1.0f : y, white ? 1.0f : z);
     const uint32_t lum = black ? 0u : bright ? 0xffff0000u : (((yb - (kFluvBias << 23)) << 2) & 0xffff0000u);
     return lum | uv;
 }
