@@ -856,6 +856,49 @@ def run_compact(args):
         gbs = n * (12 + size) / sec / 1e9
         res["%s_%s" % (name, op)] = {"ms_per_launch": sec * 1e3, "melem_per_s": n / sec / 1e6, "achieved_gbs": gbs,
                                      "frac": gbs / peak, "bit_exact_vs_oracle": ok, "bytes_per_elem": 12 + size}
+    # colour records (Color::write_compressed / from_compressed): XYZ,
+    # blackbody and temperature colours in equal parts
+    from psychopath_gb300.gpu import _check, lib as gpu_lib
+    cols = np.zeros(n, abi.color_dtype())
+    cols["kind"] = np.arange(n) % 3
+    cols["v"] = host_pos
+    cols["v"][cols["kind"] != 0, 0] = np.random.default_rng(2027).uniform(1000.0, 12000.0, int((cols["kind"] != 0).sum()))
+    d_cols = torch.from_numpy(cols.view(np.uint8)).cuda()
+    d_crec = torch.empty(n * 5, dtype=torch.uint8, device="cuda")
+    d_cout = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    for op, bytes_per in (("compress", 21), ("decompress", 21)):
+        def claunch():
+            if op == "compress":
+                _check(gpu_lib().psy_color_compress(d_cols.data_ptr(), n, d_crec.data_ptr(), d_bad.data_ptr(),
+                                                    stream.cuda_stream))
+            else:
+                _check(gpu_lib().psy_color_decompress(d_crec.data_ptr(), n, d_cout.data_ptr(), d_bad.data_ptr(),
+                                                      stream.cuda_stream))
+        for _ in range(max(3, args.warmup)):
+            claunch()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            claunch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        launches += args.steps
+        sec = e0.elapsed_time(e1) / 1e3 / args.steps
+        if op == "compress":
+            want = np.zeros(sample * 5, np.uint8)
+            L.psyo_color_compress(cols.ctypes.data, sample, want.ctypes.data, None)
+            ok = bool(np.array_equal(d_crec[:sample * 5].cpu().numpy(), want))
+        else:
+            recs = d_crec[:sample * 5].cpu().numpy()
+            want = np.zeros(sample, abi.color_dtype())
+            L.psyo_color_decompress(recs.ctypes.data, sample, want.ctypes.data, None)
+            got = d_cout[:sample * 16].cpu().numpy().view(abi.color_dtype())
+            ok = bool(np.array_equal(got["kind"], want["kind"]) and np.array_equal(got["v"], want["v"]))
+        gbs = n * bytes_per / sec / 1e9
+        res["color_%s" % op] = {"ms_per_launch": sec * 1e3, "melem_per_s": n / sec / 1e6, "achieved_gbs": gbs,
+                                "frac": gbs / peak, "bit_exact_vs_oracle": ok, "bytes_per_elem": bytes_per}
+    del d_cols, d_crec, d_cout
     clk = clocks.stop()
     invalid_total = int(d_bad.item())
     # e2e: fluv32 encode through the C ABI from pinned host memory, codes back
