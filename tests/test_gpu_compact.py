@@ -240,3 +240,31 @@ def test_crate_style_interface():
     rec = compact.color_compress(cols)
     assert rec.tolist() == [[0, 0xc3, 0x56, 0x00, 0x7e], [1, 0x64, 0x19, 0x00, 0x40]]
     assert compact.color_decompress(rec)["v"][1].tolist() == [6500.0, 2.0, 0.0]
+
+
+def test_closure_records_through_the_python_interface(oracle_lib):
+    """closure_compress / closure_decompress (the MicropolyBatch record
+    layout) equal the oracle's records and round-trip the closures to the
+    records' precision."""
+    import ctypes as C
+    sh = np.zeros(3, abi.shader_dtype())
+    sh["kind"] = [abi.PSY_SHADER_LAMBERT, abi.PSY_SHADER_GGX, abi.PSY_SHADER_EMIT]
+    sh["color"]["kind"] = [abi.PSY_COLOR_XYZ, abi.PSY_COLOR_BLACKBODY, abi.PSY_COLOR_TEMPERATURE]
+    sh["color"]["v"] = [(0.25, 0.5, 0.75), (6500.0, 2.0, 0.0), (3000.0, 0.5, 0.0)]
+    sh["roughness"] = [0.0, 0.5, 0.0]
+    sh["fresnel"] = [0.0, 0.25, 0.0]
+    rec = compact.closure_compress(sh)
+    assert rec.shape == (3, 10)
+    want = np.zeros((3, 10), np.uint8)
+    bad = C.c_uint32()
+    assert oracle_lib.psyo_closure_compress(sh.ctypes.data, 3, 10, want.ctypes.data, C.byref(bad)) == 0
+    assert np.array_equal(rec, want) and bad.value == 0
+    back = compact.closure_decompress(rec)
+    assert back["kind"].tolist() == sh["kind"].tolist()
+    assert back["color"]["kind"].tolist() == sh["color"]["kind"].tolist()
+    assert back[1]["roughness"] == np.float32(32767) * np.float32(1.0 / 65535.0)
+    assert back[1]["fresnel"] == np.float32(16383) * np.float32(1.0 / 65535.0)
+    assert back[1]["color"]["v"].tolist() == [6500.0, 2.0, 0.0]
+    assert np.allclose(back[0]["color"]["v"], sh[0]["color"]["v"], rtol=0.02)
+    with pytest.raises(ValueError):
+        compact.closure_compress(sh, stride=6)  # the GGX record does not fit
