@@ -775,6 +775,61 @@ def cpu_compact_sample(fmts, xyz, codes, target_seconds):
     return out
 
 
+def run_compact_reference(args):
+    """The reference arm of the codec workload: the CPU oracle's fluv32 encode
+    (the crate's `fluv32::encode`, restated) on all host threads, each
+    thread encoding its share of a bounded batch of the same seeded triples
+    (no GPU involved).  Rank 0 alone runs it under torchrun."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle
+    from tests import compact_cases as cc
+    rank, _, _ = dist_env()
+    if rank != 0:
+        return
+    L = oracle.lib()
+    threads = os.cpu_count() or 1
+    n = min(args.elems, 1 << 24)  # a bounded sample of the workload
+    host = np.abs(cc.random_triples(n, seed=2025))
+    host[~np.isfinite(host)] = 0.0
+    out = np.zeros(n * 4, np.uint8)
+    fmt = cc.F["fluv32"]
+    chunk = (n + threads - 1) // threads
+
+    def part(i):
+        lo, hi = i * chunk, min(n, (i + 1) * chunk)
+        if hi > lo:
+            L.psyo_compact_encode(fmt, host[lo:].ctypes.data, hi - lo, out[4 * lo:].ctypes.data, None)
+
+    with ThreadPoolExecutor(threads) as pool:  # ctypes drops the GIL during the call
+        def step():
+            list(pool.map(part, range(threads)))
+        for _ in range(max(3, args.warmup)):
+            step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        secs = time.perf_counter() - t0
+    whole = np.zeros(n * 4, np.uint8)  # the threaded split gives the one-call codes (untimed)
+    L.psyo_compact_encode(fmt, host.ctypes.data, n, whole.ctypes.data, None)
+    if not np.array_equal(out, whole):
+        raise RuntimeError("threaded oracle encode differs from one call")
+    value = n * args.steps / secs / 1e6
+    line = {
+        "impl": "reference", "metric": "fluv32 encode Melem/s", "value": value, "unit": "Melem/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32/u8", "data": "synthetic (seeded f32 triples over the whole exponent range)",
+        "config": {"workload": "compact codecs: %d triples per launch" % args.elems},
+        "cpu_baseline": {"value": value, "unit": "Melem/s", "cores": threads, "kind": "port",
+                         "sample": "%d triples per step, split over %d host threads" % (n, threads)},
+        "e2e": {"value": value, "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU oracle (C++ restatement of the compact crate's fluv32); the Rust crate cannot be built here",
+    }
+    print(json.dumps(line), flush=True)
+    return line
+
+
 def run_compact(args):
     """The `compact` crate's codecs (sub_crates/compact) on the GPU: each
     codec launched on --elems seeded triples (or their codes) resident in HBM,
@@ -1217,7 +1272,7 @@ def main():
     if args.workload == "parity":
         return run_parity(args)
     if args.workload == "compact":
-        return run_compact(args)
+        return run_compact_reference(args) if args.impl == "reference" else run_compact(args)
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -30,3 +30,19 @@ def test_traversal_traffic_matches_its_launch_form():
     per_ray = float(kv["dram_bytes_per_ray"])
     assert bench.traversal_traffic(kv["launch"], 16) == per_ray * 16
     assert bench.traversal_traffic("plain", 16) is None
+
+
+def test_compact_reference_arm_runs_on_the_cpu():
+    """bench.py --impl reference --workload compact times the oracle's codec
+    on the host threads (no GPU) and prints the reference arm's line."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--workload",
+                        "compact", "--elems", "65536", "--steps", "3", "--warmup", "3"],
+                       capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "Melem/s"
+    assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
