@@ -3,6 +3,8 @@ declares (no compute calls: runs without a GPU)."""
 import os
 import re
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -94,3 +96,38 @@ def test_ctypes_constants_match_header():
     assert len(checked) >= 10
     for n in checked:
         assert getattr(abi, n) == defs[n], n
+
+
+def _gpu_present():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_gpu_present(), reason="passes placeholder device pointers: run only where no GPU exists")
+def test_compact_entry_points_validate_before_any_gpu_work(gpu_lib):
+    """Argument errors of the codec calls come back as PSY_E_INVALID (the
+    reference panics or cannot express them) before any launch.  Some calls
+    pass placeholder pointers that the host-side checks must reject, so the
+    test runs only on machines without a GPU."""
+    import ctypes as C
+    from psychopath_gb300 import abi, gpu
+    gpu.lib()  # binds the argument types
+    L = gpu_lib
+    size = C.c_uint32()
+    for fmt, want in ((abi.PSY_COMPACT_FLUV32, 4), (abi.PSY_COMPACT_OCT32_PRECISE, 4),
+                      (abi.PSY_COMPACT_UNSIGNED40, 5), (abi.PSY_COMPACT_SIGNED48, 6)):
+        assert L.psy_compact_element_size(fmt, C.byref(size)) == abi.PSY_OK and size.value == want
+    assert L.psy_compact_element_size(99, C.byref(size)) == abi.PSY_E_INVALID
+    assert L.psy_compact_encode(99, None, 4, None, None, None) == abi.PSY_E_INVALID
+    assert L.psy_compact_decode(99, None, 4, None, None) == abi.PSY_E_INVALID
+    assert L.psy_compact_encode(abi.PSY_COMPACT_FLUV32, None, 0, None, None, None) == abi.PSY_OK  # empty batch
+    assert L.psy_compact_encode(abi.PSY_COMPACT_FLUV32, None, 4, None, None, None) == abi.PSY_E_INVALID
+    assert L.psy_compact_encode(abi.PSY_COMPACT_FLUV32, 16, 4, 16, 2, None) == abi.PSY_E_INVALID  # counter
+    assert L.psy_closure_compress(16, 1, 5, 16, None, None) == abi.PSY_E_INVALID  # stride below 6
+    assert L.psy_closure_compress(18, 1, 10, 16, None, None) == abi.PSY_E_INVALID  # misaligned records
+    assert L.psy_closure_decompress(16, 1, 10, 18, None, None) == abi.PSY_E_INVALID
+    assert L.psy_color_compress(None, 1, None, None, None) == abi.PSY_E_INVALID
+    assert b"compact" in L.psy_last_error() or b"closure" in L.psy_last_error() or b"color" in L.psy_last_error()
